@@ -1,0 +1,298 @@
+#!/usr/bin/env python
+"""Benchmark of the DEM hot path on the 1M-sphere rotating Hertz drum.
+
+One step = one pass of [Leapfrog(reset=True), InsertionSortCollider, ContactLoop] over the
+whole scene (1 000 000 lognormal spheres, 20 000 facets, 2 rotating wall caps,
+Cp2_FrictMat_HertzPhys + Law2_L6Geom_HertzPhys_DMT). ``value`` is particle-steps/s with the
+state resident in HBM; ``e2e`` drives the same step through the C ABI from host buffers
+(wg_run_host: page-locked host state copied in, one step, copied out, every step).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--precision fp32|fp64]
+
+N>1 (launched by torch.distributed.run) runs independent replicas, one scene per GPU
+(the single-scene path has no exchange step); ``value`` is the sum over ranks.
+``--impl reference`` times the CPU restatement of the reference (OpenMP, all host cores) on
+a bounded sample of the same workload and prints the same JSON line.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "particle-steps/s at 1M spheres (FP32 vs FP64 plain); batched jobs/s, p50/p99"
+UNIT = "particle-steps/s"
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def env_rank():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        self.p.wait()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            try:
+                sm.append(float(r[1]))
+                mx = max(mx, float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for nm, v in zip(names, r[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def build_scene(args, seed, n=None, precision=None):
+    from woodem_gb300 import scenes
+    n = n or args.spheres
+    scale = (n / 1e6) ** (1 / 3.0)
+    return scenes.hertz_drum(n=n, seed=seed, diameter=1.2 * scale, length=0.6 * scale, div=201, axDiv=50,
+                             precision=precision or args.precision)
+
+
+# Algorithmic bytes of the FP64 / FP32 contact kernel and of a whole step:
+#   contact kernel: per real contact read+write of the persistent contact state, per potential
+#   contact its key and flags, per particle one read of the gathered state (pos, vel, angVel).
+#   step: + Leapfrog per node, + force sum per contact end and per particle, collider amortised.
+BYTES = {
+    "fp64": dict(real=124 + 124, pot=16, part=96, lf=388, red_end=60, red_part=64 + 16),
+    "fp32": dict(real=76 + 72, pot=16, part=96, lf=388, red_end=48, red_part=64 + 16),
+}
+
+
+def measure_gpu(args, rank, world):
+    from woodem_gb300 import _native
+    S = build_scene(args, seed=args.seed + rank)
+    t0 = time.time()
+    S.run(args.warmup)
+    sim = S._sim
+    L, h = sim.H.L, sim.H.h
+    st0 = sim.stats()
+    log("[rank %d] warmup %d steps done in %.1fs: %d contacts (%d real), %d full runs" %
+        (rank, args.warmup, time.time() - t0, st0.n_contacts, st0.n_real, st0.n_full_runs))
+    clocks = Clocks(int(os.environ.get("LOCAL_RANK", 0))) if rank == 0 else None
+    if clocks:
+        clocks.start()
+    barrier(world)
+    t1 = time.perf_counter()
+    S.run(args.steps)
+    t2 = time.perf_counter()
+    ck = clocks.stop() if clocks else None
+    tot, ph, nl = sim.timing()
+    st1 = sim.stats()
+    n_spheres = args.spheres
+    res = dict(ms=tot, wall=(t2 - t1) * 1e3, phases=ph.tolist(), launches=nl, st0=st0, st1=st1, clocks=ck,
+               n_nodes=S._sim.A.n_nodes, n_par=S._sim.A.n_particles, n_spheres=n_spheres)
+    # e2e through wg_run_host with page-locked host buffers
+    if not args.no_e2e:
+        na = S._sim.A.n_nodes
+        nbytes = 19 * 8 * na
+        p = L.wg_host_alloc(nbytes)
+        if not p:
+            raise MemoryError("wg_host_alloc")
+        import ctypes
+        buf = np.ctypeslib.as_array((ctypes.c_double * (19 * na)).from_address(p))
+        parts = [buf[0:3 * na], buf[3 * na:7 * na], buf[7 * na:10 * na], buf[10 * na:13 * na], buf[13 * na:16 * na],
+                 buf[16 * na:19 * na]]
+        sim.H.check(L.wg_get_nodes(h, *[_native.ptr(x) for x in parts]), "get_nodes")
+        ne = args.e2e_steps
+        sim.H.check(L.wg_run_host(h, 1, *[_native.ptr(x) for x in parts]), "run_host")  # warm
+        barrier(world)
+        te = time.perf_counter()
+        for _ in range(ne):
+            sim.H.check(L.wg_run_host(h, 1, *[_native.ptr(x) for x in parts]), "run_host")
+        te = time.perf_counter() - te
+        L.wg_host_free(p)
+        res["e2e"] = dict(seconds=te, steps=ne, h2d=(3 + 4 + 3 + 3 + 3 + 3) * 8 * na, d2h=(3 + 4 + 3 + 3 + 3 + 3) * 8 * na)
+    S.close()
+    return res
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allreduce_max(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_sample(args, seconds, threads):
+    """Oracle (CPU restatement, OpenMP, reference structure) on a 100k-sphere drum of the same
+    construction; returns (particle-steps/s, steps, spheres)."""
+    from woodem_gb300 import _plan
+    from oracle.oracle import Oracle
+    n = args.cpu_spheres
+    S = build_scene(args, seed=args.seed, n=n, precision="fp64")
+    A = _plan.compile_scene(S)
+    O = Oracle(A, threads=threads, deterministic=False)
+    O.run(2)  # initial sort and first contacts outside the timed sample
+    steps = 0
+    t = time.perf_counter()
+    while True:
+        O.run(5)
+        steps += 5
+        el = time.perf_counter() - t
+        if el > seconds or steps >= 2000:
+            break
+    O.close()
+    return n * steps / el, steps, n, el
+
+
+def peaks():
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=30)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--spheres", type=int, default=1_000_000)
+    ap.add_argument("--cpu-spheres", type=int, default=100_000)
+    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--seed", type=int, default=0)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank, world, local = env_rank()
+    cfg = {"workload": "hertz-drum-1M", "spheres": args.spheres, "facets": 20000, "walls": 2,
+           "law": "Cp2_FrictMat_HertzPhys+Law2_L6Geom_HertzPhys_DMT", "precision": args.precision,
+           "l2": "inputs larger than L2 (device state > 1 GB)", "replicas": world}
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        threads = os.cpu_count() or 1
+        v, steps, n, el = cpu_sample(args, args.cpu_seconds * max(1, args.steps // 300), threads)
+        line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1e3 * el / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64", "data": "synthetic", "config": cfg, "impl": "reference",
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                                 "sample": "%d steps of a %d-sphere drum of the same construction (20k facets, Hertz), "
+                                           "OpenMP restatement of the reference CPU path" % (steps, n)},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+        os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("CUDA_VISIBLE_DEVICES", ""))
+    import __graft_entry__
+    if rank == 0:
+        __graft_entry__.build()
+    barrier(world)
+    __graft_entry__.build()
+    from woodem_gb300 import _native
+    _native.lib()
+    # each rank drives its own GPU (replicas)
+    if world > 1:
+        from woodem_gb300 import core  # noqa
+    res = measure_gpu(args, rank, world)
+    ms = allreduce_max(res["ms"], world)
+    st0, st1 = res["st0"], res["st1"]
+    n_sph = res["n_spheres"]
+    value = world * n_sph * args.steps / (ms / 1e3)
+    hbm, src = peaks()
+    B = BYTES[args.precision]
+    R = 0.5 * (st0.n_real + st1.n_real)
+    P = 0.5 * (st0.n_contacts + st1.n_contacts)
+    Np = res["n_par"]
+    kern_ms = res["phases"][1] / args.steps
+    kbytes = R * B["real"] + (P - R) * B["pot"] + Np * B["part"]
+    achieved = kbytes / (kern_ms / 1e3) / 1e9 if kern_ms > 0 else 0.0
+    nfull = st1.n_full_runs - st0.n_full_runs
+    step_bytes = (res["n_nodes"] * B["lf"] + kbytes + 2 * R * B["red_end"] + Np * B["red_part"])
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if args.precision == "fp64" else "f32+f64", "data": "synthetic", "config": cfg,
+            "roofline": {"bound": "hbm", "kernel": "k_contact_%s" % args.precision, "achieved": achieved, "peak": hbm,
+                         "unit": "GB/s", "frac": achieved / hbm, "traffic": None, "peak_source": src,
+                         "bytes_per_launch": kbytes, "launch_ms": kern_ms},
+            "step": {"contacts": P, "real": R, "full_runs": nfull, "phase_ms": [x / args.steps for x in res["phases"]],
+                     "algorithmic_bytes": step_bytes, "achieved_gbs": step_bytes / (ms / args.steps / 1e3) / 1e9},
+            "gpu_launches": int(res["launches"]), "clocks": res["clocks"]}
+    if "e2e" in res:
+        e = res["e2e"]
+        es = allreduce_max(e["seconds"], world)
+        line["e2e"] = {"value": world * n_sph * e["steps"] / es, "unit": UNIT, "h2d_bytes_per_step": e["h2d"],
+                       "d2h_bytes_per_step": e["d2h"], "steps": e["steps"],
+                       "call": "wg_run_host(1 step) with page-locked host state"}
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        v, steps, n, el = cpu_sample(args, args.cpu_seconds, threads)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": "%d steps of a %d-sphere drum of the same construction (20k facets, Hertz), "
+                                          "OpenMP restatement of the reference CPU path" % (steps, n)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

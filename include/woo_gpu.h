@@ -1,0 +1,164 @@
+/*
+ * woo_gpu.h -- C ABI of the GB300 DEM hot path (libwoogpu.so).
+ *
+ * One call of wg_run(scene, n) performs n steps of the reference's engine list
+ *     Leapfrog(reset=True) -> InsertionSortCollider -> ContactLoop
+ * on the GPU. It replaces, per step:
+ *   - Scene::doOneStep                    core/Scene.cpp:319-389 (engine sequencing, cell update)
+ *   - Leapfrog::run                       pkg/dem/Leapfrog.cpp:103-255
+ *   - InsertionSortCollider::run          pkg/dem/InsertionSortCollider.cpp:445-646
+ *   - ContactLoop::run                    pkg/dem/ContactLoop.cpp:93-259 with the functors
+ *       Cg2_Sphere_Sphere_L6Geom          pkg/dem/Sphere.cpp:88-109
+ *       Cg2_Facet_Sphere_L6Geom           pkg/dem/Facet.cpp:235-288
+ *       Cg2_Wall_Sphere_L6Geom            pkg/dem/Wall.cpp:45-79
+ *       Cp2_FrictMat_FrictPhys            pkg/dem/FrictMat.cpp:13-44
+ *       Cp2_FrictMat_HertzPhys            pkg/dem/Hertz.cpp:9-50
+ *       Law2_L6Geom_FrictPhys_IdealElPl   pkg/dem/IdealElPl.cpp:12-122
+ *       Law2_L6Geom_HertzPhys_DMT         pkg/dem/Hertz.cpp:58-182
+ *
+ * Conventions: plain host pointers and sizes, no CUDA or framework types. Every
+ * function returns WG_OK (0) or a negative WG_ERR_* code; wg_last_error() gives
+ * the message (the reference's exception text where one exists). Arrays are
+ * row-major: 3 doubles per vector, 4 per quaternion (w,x,y,z).
+ */
+#ifndef WOO_GPU_H
+#define WOO_GPU_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define WG_OK 0
+#define WG_ERR_ARG (-1)          /* invalid argument / std::invalid_argument */
+#define WG_ERR_CUDA (-2)         /* CUDA runtime failure */
+#define WG_ERR_NAN (-3)          /* NaN force, IdealElPl.cpp:76-80 */
+#define WG_ERR_UNSUPPORTED (-4)  /* engine/functor/attribute outside the GPU path */
+#define WG_ERR_CAPACITY (-5)     /* a fixed-size buffer is too small */
+#define WG_ERR_PERIODIC (-6)     /* particle spans over half the cell, InsertionSortCollider.cpp:945-949 */
+#define WG_ERR_STATE (-7)        /* call sequence error (e.g. run before particles are set) */
+#define WG_ERR_TIMEOUT (-8)      /* bounded device wait gave up */
+
+enum { WG_SHAPE_SPHERE = 0, WG_SHAPE_WALL = 1, WG_SHAPE_FACET = 2 };
+enum { WG_PREC_FP64 = 0, WG_PREC_FP32 = 1 };
+
+/* Engine and functor attributes read by the hot path. Field names follow the
+   reference attributes; see the comments for the owning class. */
+typedef struct wg_config {
+    double dt;                  /* Scene.dt */
+    double gravity[3];          /* DemField.gravity */
+    uint32_t lone_mask;         /* DemField.loneMask */
+    int32_t deterministic;      /* Scene.deterministic (the GPU path is always deterministic) */
+    int64_t step;               /* Scene.step at upload */
+    double damping;             /* Leapfrog.damping */
+    int32_t reset;              /* Leapfrog.reset (must be 1) */
+    int32_t _pad0;
+    double verlet_dist;         /* InsertionSortCollider.verletDist (<0: relative to min sphere radius) */
+    double bo1_sphere_dist_factor; /* Bo1_Sphere_Aabb.distFactor */
+    int32_t sort_axis;          /* InsertionSortCollider.sortAxis (no effect on the pair set) */
+    int32_t apply_forces;       /* ContactLoop.applyForces */
+    double cg2_ss_dist_factor;  /* Cg2_Sphere_Sphere_L6Geom.distFactor */
+    int32_t trsf_renorm;        /* Cg2_Any_Any_L6Geom__Base.trsfRenorm */
+    int32_t approx_mask;        /* Cg2_Any_Any_L6Geom__Base.approxMask */
+    int32_t no_ratch;           /* Cg2_Any_Any_L6Geom__Base.noRatch */
+    int32_t phys;               /* 0 Cp2_FrictMat_FrictPhys, 1 Cp2_FrictMat_HertzPhys */
+    int32_t law;                /* 0 Law2_L6Geom_FrictPhys_IdealElPl, 1 Law2_L6Geom_HertzPhys_DMT */
+    int32_t no_slip;            /* IdealElPl.noSlip */
+    int32_t no_break;           /* IdealElPl.noBreak */
+    int32_t no_frict;           /* IdealElPl.noFrict */
+    double hz_poisson;          /* Cp2_FrictMat_HertzPhys.poisson */
+    double hz_gamma;            /* Cp2_FrictMat_HertzPhys.gamma */
+    double hz_en;               /* Cp2_FrictMat_HertzPhys.en */
+    double hz_alpha;            /* Cp2_FrictMat_HertzPhys.alpha (must be 0: DMT branch) */
+    int32_t hz_no_attraction;   /* Law2_L6Geom_HertzPhys_DMT.noAttraction */
+    int32_t periodic;           /* Scene.periodic */
+    int32_t homo_deform;        /* Cell.homoDeform */
+    int32_t eval_stress;        /* ContactLoop.evalStress */
+    double cell_hsize[9];       /* Cell.hSize, row-major */
+    double cell_trsf[9];        /* Cell.trsf */
+    double cell_gradv[9];       /* Cell.gradV */
+    double cell_next_gradv[9];  /* Cell.nextGradV */
+    int32_t precision;          /* WG_PREC_FP64 (plain) or WG_PREC_FP32 (FP32 contact math, FP64 accumulation) */
+    int32_t _pad1;
+} wg_config;
+
+typedef struct wg_stats {
+    int64_t step;               /* Scene.step */
+    int64_t n_full_runs;        /* InsertionSortCollider.nFullRuns */
+    int64_t n_contacts;         /* len(S.dem.con): potential + real */
+    int64_t n_real;             /* S.dem.con.countReal() */
+    double time;                /* Scene.time */
+    double verlet_dist;         /* resolved InsertionSortCollider.verletDist */
+    double stress[9];           /* ContactLoop.stress (periodic, evalStress) */
+} wg_stats;
+
+typedef struct wg_scene wg_scene;
+
+/* Create an empty scene on CUDA device `device`. */
+int wg_create(wg_scene** out, int device);
+void wg_destroy(wg_scene* s);
+/* Message of the last error on this scene (or of the last failed wg_create when s is NULL). */
+const char* wg_last_error(const wg_scene* s);
+
+/* Scene description. Nodes carry Node.pos/ori and DemData (pkg/dem/Particle.hpp:169-274);
+   particles carry shape, material index and mask (pkg/dem/Particle.hpp:26-123).
+   nodes3: 3 node indices per particle (-1 unused); wall_axis/wall_sense: Wall.axis/sense;
+   half_thick/fake_vel: Facet.halfThick/fakeVel; radius: Sphere.radius. */
+int wg_set_config(wg_scene* s, const wg_config* c);
+int wg_set_materials(wg_scene* s, int32_t n, const double* density, const double* young,
+                     const double* tan_phi, const double* kt_div_kn);
+int wg_set_nodes(wg_scene* s, int64_t n, const double* pos, const double* ori, const double* vel,
+                 const double* ang_vel, const double* force, const double* torque,
+                 const double* mass, const double* inertia, const uint32_t* flags);
+int wg_set_particles(wg_scene* s, int64_t n, const int32_t* shape, const int32_t* nodes3,
+                     const double* radius, const int32_t* wall_axis, const int32_t* wall_sense,
+                     const double* half_thick, const double* fake_vel, const int32_t* mat,
+                     const uint32_t* mask);
+
+/* Advance n steps with device-resident state. */
+int wg_run(wg_scene* s, int64_t n_steps);
+/* Same step loop driven from host buffers (the reference keeps state in host objects):
+   copies the node state in from host memory, runs n steps, copies it back out. */
+int wg_run_host(wg_scene* s, int64_t n_steps, double* pos, double* ori, double* vel, double* ang_vel,
+                double* force, double* torque);
+/* Replace the dynamic node state (pos, ori, vel, angVel, force, torque) keeping contacts. */
+int wg_put_state(wg_scene* s, const double* pos, const double* ori, const double* vel,
+                 const double* ang_vel, const double* force, const double* torque);
+int wg_get_nodes(wg_scene* s, double* pos, double* ori, double* vel, double* ang_vel,
+                 double* force, double* torque);
+int wg_get_stats(wg_scene* s, wg_stats* out);
+/* Set Cell.nextGradV (row-major) between runs (periodic scenes). */
+int wg_set_next_gradv(wg_scene* s, const double* next_gradv);
+int wg_get_cell(wg_scene* s, double* hsize, double* trsf, double* gradv);
+
+/* Contacts as (lo id, hi id) rows in key order. id_a: Contact.pA; real: geom&&phys;
+   cell_dist: Contact.cellDist for the (lo,hi) orientation; fglob: force on pA in
+   global coordinates; local: phys.force; cpt: geom.node.pos; trsf: L6Geom.trsf. */
+int64_t wg_num_contacts(wg_scene* s);
+int wg_get_contacts(wg_scene* s, int32_t* id_lo, int32_t* id_hi, int32_t* id_a, int32_t* real,
+                    int32_t* cell_dist, double* fglob, double* local, double* cpt, double* trsf);
+/* Aabb.min/max per particle from the last full run (verletDist included), 3 doubles each. */
+int wg_get_aabbs(wg_scene* s, double* mn, double* mx);
+/* Run only the broad phase on the current positions (full run), no stepping. */
+int wg_collide_only(wg_scene* s);
+
+/* Page-locked host memory for wg_run_host buffers (cudaMallocHost); NULL on failure. */
+void* wg_host_alloc(int64_t bytes);
+void wg_host_free(void* p);
+
+/* Timing of the last wg_run, measured with CUDA events on the simulation stream:
+   total milliseconds from the first to the last kernel of the run, the milliseconds spent
+   in each kernel class (0 leapfrog, 1 contact, 2 reduce, 3 collider full runs), and the
+   number of kernel launches. */
+int wg_get_timing(wg_scene* s, double* total_ms, double* phase_ms4, int64_t* launches);
+
+/* Scene generation (host only): seeded random sequential insertion of n non-overlapping
+   spheres, the role of SpherePack::makeCloud (lib/sphere-pack/SpherePack.hpp:75).
+   region_kind 0: box lo..hi; 1: x-axis cylinder through (params[0],params[1]) of radius
+   params[2], clipped at z <= params[3]; 2: periodic box lo..hi. Returns the number placed. */
+int64_t wg_pack_rsa(int64_t n, const double* radii, const double* lo, const double* hi, int32_t region_kind,
+                    const double* params, uint64_t seed, int64_t max_attempts, double* centers);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

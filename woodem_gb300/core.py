@@ -1,0 +1,212 @@
+"""``woo.core`` counterparts: Scene, Cell, Engine, Field.
+
+Mirrors the scripting surface of core/Scene.hpp:149-190, core/Cell.hpp:137-187 and
+core/Engine.hpp:27-104. A Scene owns a device-side simulation (created on the
+first ``run``); engines are descriptors compiled into one device plan, so the
+per-step loop of core/Scene.cpp:319-389 runs entirely on the GPU.
+"""
+import math
+import numpy as np
+
+from . import _plan
+
+NaN = float("nan")
+
+
+class Object:
+    """Keyword-attribute constructor convention of Woo objects (lib/object/Object.hpp:369,417)."""
+
+    _attrs = {}
+
+    def __init__(self, **kw):
+        for cls in reversed(type(self).__mro__):
+            for k, v in getattr(cls, "_attrs", {}).items():
+                if k not in self.__dict__:
+                    object.__setattr__(self, k, v() if callable(v) and not isinstance(v, type) else v)
+        for k, v in kw.items():
+            self._setattr_checked(k, v)
+
+    def _setattr_checked(self, k, v):
+        known = set()
+        for cls in type(self).__mro__:
+            known |= set(getattr(cls, "_attrs", {}).keys())
+        if k not in known and not hasattr(type(self), k):
+            raise AttributeError("%s has no attribute '%s'" % (type(self).__name__, k))
+        setattr(self, k, v)
+
+    def updateAttrs(self, d):
+        for k, v in d.items():
+            self._setattr_checked(k, v)
+
+    def __repr__(self):
+        return "<%s @ %x>" % (type(self).__name__, id(self))
+
+
+class Engine(Object):
+    """Base engine; ``run`` is never called on the host, engines are compiled into the device plan."""
+
+    _attrs = {"label": "", "dead": False, "field": None}
+
+    def critDt(self):
+        return float("inf")
+
+
+class PeriodicEngine(Engine):
+    _attrs = {"stepPeriod": -1, "virtPeriod": 0.0, "realPeriod": 0.0}
+
+
+class Field(Object):
+    _attrs = {}
+
+
+class Cell(Object):
+    """Periodic cell (core/Cell.hpp:22-187). State is integrated on the host once per step
+    (core/Cell.cpp:81-120) and handed to the kernels as a handful of 3x3 matrices."""
+
+    HomoNone, HomoPos, HomoVel, HomoVel2, HomoGradV2 = 0, 1, 2, 3, 4
+
+    def __init__(self, **kw):
+        self.hSize = np.eye(3)
+        self.trsf = np.eye(3)
+        self._gradV = np.zeros((3, 3))
+        self.nextGradV = np.zeros((3, 3))
+        self.homoDeform = Cell.HomoGradV2
+        self.trsfUpperTriangular = False
+        for k, v in kw.items():
+            setattr(self, k, v)
+
+    def setBox(self, *size):
+        if len(size) == 1:
+            size = tuple(size[0])
+        self.hSize = np.diag(np.array(size, dtype=float))
+        self.trsf = np.eye(3)
+
+    @property
+    def gradV(self):
+        return self._gradV
+
+    @gradV.setter
+    def gradV(self, v):
+        raise ValueError("Cell.gradV is not directly settable, set Cell.nextGradV instead, to be applied one step later.")
+
+    def setCurrGradV(self, v):
+        self.nextGradV = np.array(v, dtype=float)
+        self._gradV = np.array(v, dtype=float)
+
+    @property
+    def size(self):
+        return np.linalg.norm(np.asarray(self.hSize), axis=0)
+
+    @property
+    def volume(self):
+        return float(np.linalg.det(np.asarray(self.hSize)))
+
+
+class Scene(Object):
+    """Simulation scene. ``S.run(n)`` advances n steps of the engine list on the GPU."""
+
+    _attrs = {
+        "dt": NaN, "nextDt": NaN, "dtSafety": 0.9, "step": 0, "time": 0.0, "stopAtStep": 0,
+        "trackEnergy": False, "deterministic": False, "isPeriodic": False, "tags": dict,
+        "subStepping": False,
+    }
+
+    def __init__(self, fields=None, **kw):
+        self._engines = []
+        self.fields = list(fields) if fields else []
+        self.cell = Cell()
+        self.gpu = _plan.GpuConfig()
+        self._sim = None
+        super().__init__(**kw)
+        for f in self.fields:
+            f.scene = self
+
+    # reference name for isPeriodic in python is "periodic"
+    @property
+    def periodic(self):
+        return self.isPeriodic
+
+    @periodic.setter
+    def periodic(self, v):
+        self.isPeriodic = bool(v)
+        self._invalidate()
+
+    @property
+    def engines(self):
+        return self._engines
+
+    @engines.setter
+    def engines(self, ee):
+        self._engines = list(ee)
+        for e in self._engines:
+            if getattr(e, "field", None) is None and self.fields:
+                e.field = self.fields[0]
+        self._invalidate()
+
+    @property
+    def dem(self):
+        from .dem import DemField
+        for f in self.fields:
+            if isinstance(f, DemField):
+                return f
+        raise AttributeError("Scene has no DemField")
+
+    @property
+    def lab(self):
+        class _Lab:
+            pass
+        lab = _Lab()
+        for e in self._engines:
+            if getattr(e, "label", ""):
+                setattr(lab, e.label, e)
+            for sub in getattr(e, "_functors", lambda: [])():
+                if getattr(sub, "label", ""):
+                    setattr(lab, sub.label, sub)
+        return lab
+
+    def _invalidate(self):
+        if self._sim is not None:
+            self._sim.close()
+            self._sim = None
+
+    def _ensure_sim(self):
+        if self._sim is None or self._sim.dirty_structure:
+            if self._sim is not None:
+                self._sim.close()
+            self._sim = _plan.Simulation(self)
+        return self._sim
+
+    def run(self, nSteps=None, wait=True):
+        """Run nSteps steps (core/Scene.cpp:33-48). Runs synchronously; ``wait`` is accepted for API parity."""
+        if nSteps is None:
+            if self.stopAtStep > self.step:
+                nSteps = self.stopAtStep - self.step
+            else:
+                raise ValueError("S.run() without nSteps needs stopAtStep > step")
+        if nSteps <= 0:
+            return
+        sim = self._ensure_sim()
+        sim.run(int(nSteps))
+
+    def one(self):
+        self.run(1)
+
+    def wait(self):
+        return
+
+    def stop(self):
+        return
+
+    def sync(self):
+        """Bring device state back to the host containers."""
+        if self._sim is not None:
+            self._sim.pull()
+
+    def close(self):
+        self._invalidate()
+
+    def __del__(self):
+        try:
+            self._invalidate()
+        except Exception:
+            pass

@@ -1,0 +1,866 @@
+// Host side of the GB300 DEM hot path: scene upload, the per-step loop of
+// Scene::doOneStep (core/Scene.cpp:319-389) for the engine list
+// [Leapfrog(reset=True), InsertionSortCollider, ContactLoop], and the C ABI of include/woo_gpu.h.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <vector>
+
+#include "wg_internal.h"
+#include "wg_math.cuh"
+
+namespace wg {
+
+void collide_free(Sim& S);
+
+static thread_local std::string g_createError;
+
+void* Sim::dalloc(size_t bytes) {
+    void* p = nullptr;
+    if (cudaMalloc(&p, std::max<size_t>(bytes, 16)) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    allocs.push_back(p);
+    return p;
+}
+void Sim::dfree(void* p) {
+    if (!p) return;
+    auto it = std::find(allocs.begin(), allocs.end(), p);
+    if (it != allocs.end()) allocs.erase(it);
+    cudaFree(p);
+}
+Sim::~Sim() {
+    if (stream) cudaStreamSynchronize(stream);
+    collide_free(*this);
+    for (void* p : allocs) cudaFree(p);
+    allocs.clear();
+    if (hFlags) cudaFreeHost(hFlags);
+    for (int i = 0; i < 8; i++)
+        if (ev[i]) cudaEventDestroy(ev[i]);
+    if (stream) cudaStreamDestroy(stream);
+}
+
+// ------------------------------------------------------------------ periodic cell (host)
+// Cell::integrateAndUpdate / setNextGradV, core/Cell.cpp:60-120, with 3x3 algebra in the same
+// operation order as the oracle so that the matrices handed to the kernels agree bitwise.
+struct HM {
+    double m[3][3];
+};
+static HM hI() { HM r{}; r.m[0][0] = r.m[1][1] = r.m[2][2] = 1; return r; }
+static HM hmul(const HM& A, const HM& B) {
+    HM r{};
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) r.m[i][j] = (A.m[i][0] * B.m[0][j] + A.m[i][1] * B.m[1][j]) + A.m[i][2] * B.m[2][j];
+    return r;
+}
+static HM hadd(const HM& A, const HM& B) { HM r; for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) r.m[i][j] = A.m[i][j] + B.m[i][j]; return r; }
+static HM hsub(const HM& A, const HM& B) { HM r; for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) r.m[i][j] = A.m[i][j] - B.m[i][j]; return r; }
+static HM hscale(const HM& A, double s) { HM r; for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) r.m[i][j] = A.m[i][j] * s; return r; }
+static HM hdiv(const HM& A, double s) { HM r; for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) r.m[i][j] = A.m[i][j] / s; return r; }
+static HM htr(const HM& A) { HM r; for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) r.m[i][j] = A.m[j][i]; return r; }
+static double hcof(const HM& a, int i, int j) {
+    int i1 = (i + 1) % 3, i2 = (i + 2) % 3, j1 = (j + 1) % 3, j2 = (j + 2) % 3;
+    return a.m[i1][j1] * a.m[i2][j2] - a.m[i1][j2] * a.m[i2][j1];
+}
+static HM hinv(const HM& a) {
+    double c00 = hcof(a, 0, 0), c10 = hcof(a, 1, 0), c20 = hcof(a, 2, 0);
+    double det = (c00 * a.m[0][0] + c10 * a.m[1][0]) + c20 * a.m[2][0];
+    double invdet = 1.0 / det;
+    HM r;
+    r.m[0][0] = c00 * invdet; r.m[0][1] = c10 * invdet; r.m[0][2] = c20 * invdet;
+    r.m[1][0] = hcof(a, 0, 1) * invdet; r.m[1][1] = hcof(a, 1, 1) * invdet; r.m[1][2] = hcof(a, 2, 1) * invdet;
+    r.m[2][0] = hcof(a, 0, 2) * invdet; r.m[2][1] = hcof(a, 1, 2) * invdet; r.m[2][2] = hcof(a, 2, 2) * invdet;
+    return r;
+}
+static double hdet(const HM& a) {
+    return (a.m[0][0] * (a.m[1][1] * a.m[2][2] - a.m[1][2] * a.m[2][1]) - a.m[0][1] * (a.m[1][0] * a.m[2][2] - a.m[1][2] * a.m[2][0])) +
+           a.m[0][2] * (a.m[1][0] * a.m[2][1] - a.m[1][1] * a.m[2][0]);
+}
+static void hlevi(const HM& m, double out[3]) { out[0] = m.m[1][2] - m.m[2][1]; out[1] = m.m[2][0] - m.m[0][2]; out[2] = m.m[0][1] - m.m[1][0]; }
+static HM fromRow(const double* a) { HM r; for (int i = 0; i < 9; i++) r.m[i / 3][i % 3] = a[i]; return r; }
+static void toRow(const HM& m, double* a) { for (int i = 0; i < 9; i++) a[i] = m.m[i / 3][i % 3]; }
+
+struct HostCell {
+    HM trsf, hSize, pprevHsize, gradV, nextGradV;
+    double spinVec[3] = {0, 0, 0};
+    int homoDeform = 4;
+    HM invTrsf, shearTrsf, unshearTrsf;
+    double size[3], cosv[3];
+    bool hasShear = false;
+    void integrateAndUpdate(double dt) {
+        HM trsfInc = hscale(gradV, dt);
+        trsf = hadd(trsf, hmul(trsfInc, trsf));
+        invTrsf = hinv(trsf);
+        HM prevHsize = hSize;
+        if (homoDeform == 4) {
+            HM a = hinv(hsub(hI(), hdiv(hscale(gradV, dt), 2.)));
+            HM b = hadd(hI(), hdiv(hscale(gradV, dt), 2.));
+            hSize = hmul(hmul(a, b), hSize);
+        } else hSize = hadd(hSize, hmul(trsfInc, hSize));
+        pprevHsize = hscale(hadd(prevHsize, hSize), .5);
+        HM Hnorm;
+        for (int i = 0; i < 3; i++) {
+            D3 base{hSize.m[0][i], hSize.m[1][i], hSize.m[2][i]};
+            size[i] = std::sqrt(sqn(base));
+            base = base / size[i];
+            Hnorm.m[0][i] = base.x; Hnorm.m[1][i] = base.y; Hnorm.m[2][i] = base.z;
+        }
+        for (int i = 0; i < 3; i++) {
+            int i1 = (i + 1) % 3, i2 = (i + 2) % 3;
+            cosv[i] = sqn(cross(D3{Hnorm.m[0][i1], Hnorm.m[1][i1], Hnorm.m[2][i1]}, D3{Hnorm.m[0][i2], Hnorm.m[1][i2], Hnorm.m[2][i2]}));
+        }
+        shearTrsf = Hnorm;
+        unshearTrsf = hinv(shearTrsf);
+        hasShear = (hSize.m[0][1] != 0 || hSize.m[0][2] != 0 || hSize.m[1][0] != 0 || hSize.m[1][2] != 0 || hSize.m[2][0] != 0 ||
+                    hSize.m[2][1] != 0);
+    }
+    void setNextGradV() {
+        gradV = nextGradV;
+        HM W = hscale(hsub(gradV, htr(gradV)), .5);
+        double lv[3];
+        hlevi(W, lv);
+        for (int i = 0; i < 3; i++) spinVec[i] = .5 * lv[i];
+    }
+};
+
+struct SimEx : Sim {
+    HostCell cell;
+    // api <-> slot staging for state transfer
+    int32_t* dApiMap = nullptr;   // api node -> slot (-1: not used by any particle)
+    double* dStage = nullptr;     // 19 doubles per api node
+    std::vector<double> hApiStage; // last uploaded api state (for unmapped nodes)
+    std::vector<int32_t> hApiMap;
+};
+
+__global__ void k_put_state(DevNodes N, const int32_t* __restrict__ map, int64_t na, const double* __restrict__ st) {
+    const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= na) return;
+    const int s = map[a];
+    if (s < 0) return;
+    const double* pos = st;
+    const double* ori = st + 3 * na;
+    const double* vel = st + 7 * na;
+    const double* av = st + 10 * na;
+    const double* f = st + 13 * na;
+    const double* t = st + 16 * na;
+    const double r = N.posr[s].w;
+    N.posr[s] = make_double4_32a(pos[3 * a], pos[3 * a + 1], pos[3 * a + 2], r);
+    N.ori[s] = make_double4_32a(ori[4 * a], ori[4 * a + 1], ori[4 * a + 2], ori[4 * a + 3]);
+    N.vel[s] = make_double4_32a(vel[3 * a], vel[3 * a + 1], vel[3 * a + 2], 0.);
+    N.angv[s] = make_double4_32a(av[3 * a], av[3 * a + 1], av[3 * a + 2], 0.);
+    N.force[s] = make_double4_32a(f[3 * a], f[3 * a + 1], f[3 * a + 2], 0.);
+    N.torque[s] = make_double4_32a(t[3 * a], t[3 * a + 1], t[3 * a + 2], 0.);
+}
+__global__ void k_get_state(DevNodes N, const int32_t* __restrict__ map, int64_t na, double* __restrict__ st) {
+    const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= na) return;
+    const int s = map[a];
+    if (s < 0) return;
+    double* pos = st;
+    double* ori = st + 3 * na;
+    double* vel = st + 7 * na;
+    double* av = st + 10 * na;
+    double* f = st + 13 * na;
+    double* t = st + 16 * na;
+    const double4_32a p = N.posr[s], o = N.ori[s], v = N.vel[s], w = N.angv[s], ff = N.force[s], tt = N.torque[s];
+    pos[3 * a] = p.x; pos[3 * a + 1] = p.y; pos[3 * a + 2] = p.z;
+    ori[4 * a] = o.x; ori[4 * a + 1] = o.y; ori[4 * a + 2] = o.z; ori[4 * a + 3] = o.w;
+    vel[3 * a] = v.x; vel[3 * a + 1] = v.y; vel[3 * a + 2] = v.z;
+    av[3 * a] = w.x; av[3 * a + 1] = w.y; av[3 * a + 2] = w.z;
+    f[3 * a] = ff.x; f[3 * a + 1] = ff.y; f[3 * a + 2] = ff.z;
+    t[3 * a] = tt.x; t[3 * a + 1] = tt.y; t[3 * a + 2] = tt.z;
+}
+
+int Sim::ensureContactCapacity(int64_t need) {
+    Sim& S = *this;
+    if (need <= cCap && C.key) return 0;
+    int64_t cap = std::max<int64_t>(need + need / 2, std::max<int64_t>(1024, 2 * cCap));
+    DevContacts nc{}, nb{};
+    for (DevContacts* d : {&nc, &nb}) {
+        d->key = (uint64_t*)dalloc(sizeof(uint64_t) * cap);
+        d->flags = (uint32_t*)dalloc(sizeof(uint32_t) * cap);
+        d->step0 = (int32_t*)dalloc(sizeof(int32_t) * cap);
+        d->cdist = (int32_t*)dalloc(sizeof(int32_t) * cap);
+        for (int q = 0; q < CC_NCOL; q++) d->col[q] = (double*)dalloc(sizeof(double) * cap);
+        if (!d->col[CC_NCOL - 1]) return fail(WG_ERR_CUDA, "out of device memory (contacts)");
+    }
+    if (C.key && C.n > 0) {
+        WG_CUDA_TRY(cudaMemcpyAsync(nc.key, C.key, sizeof(uint64_t) * C.n, cudaMemcpyDeviceToDevice, stream));
+        WG_CUDA_TRY(cudaMemcpyAsync(nc.flags, C.flags, sizeof(uint32_t) * C.n, cudaMemcpyDeviceToDevice, stream));
+        WG_CUDA_TRY(cudaMemcpyAsync(nc.step0, C.step0, sizeof(int32_t) * C.n, cudaMemcpyDeviceToDevice, stream));
+        WG_CUDA_TRY(cudaMemcpyAsync(nc.cdist, C.cdist, sizeof(int32_t) * C.n, cudaMemcpyDeviceToDevice, stream));
+        for (int q = 0; q < CC_NCOL; q++)
+            WG_CUDA_TRY(cudaMemcpyAsync(nc.col[q], C.col[q], sizeof(double) * C.n, cudaMemcpyDeviceToDevice, stream));
+    }
+    WG_CUDA_TRY(cudaStreamSynchronize(stream));
+    nc.n = C.n;
+    for (DevContacts* d : {&C, &Cb}) {
+        if (!d->key) continue;
+        dfree(d->key); dfree(d->flags); dfree(d->step0); dfree(d->cdist);
+        for (int q = 0; q < CC_NCOL; q++) dfree(d->col[q]);
+    }
+    C = nc;
+    Cb = nb;
+    cCap = cap;
+    return 0;
+}
+
+int Sim::prepareParams() {
+    Sim& S = *this;
+    SimEx& X = static_cast<SimEx&>(*this);
+    ScenePar& p = hPar;
+    std::memset(&p, 0, sizeof(p));
+    p.dt = cfg.dt;
+    for (int i = 0; i < 3; i++) p.g[i] = cfg.gravity[i];
+    p.hasGravity = (cfg.gravity[0] != 0 || cfg.gravity[1] != 0 || cfg.gravity[2] != 0);
+    p.damping = cfg.damping;
+    p.ssDistFactor = cfg.cg2_ss_dist_factor;
+    p.bo1DistFactor = cfg.bo1_sphere_dist_factor;
+    p.law = cfg.law;
+    p.phys = cfg.phys;
+    p.reset = cfg.reset;
+    p.applyForces = cfg.apply_forces;
+    p.trsfRenorm = cfg.trsf_renorm;
+    p.approxMask = cfg.approx_mask;
+    p.noRatch = cfg.no_ratch;
+    p.noSlip = cfg.no_slip;
+    p.noBreak = cfg.no_break;
+    p.noFrict = cfg.no_frict;
+    p.noAttraction = cfg.hz_no_attraction;
+    p.hzGamma = cfg.hz_gamma;
+    p.hzPoisson = cfg.hz_poisson;
+    p.hzViscOn = (cfg.hz_en > 0 && cfg.hz_en < 1.);
+    if (p.hzViscOn) {
+        // Cp2_FrictMat_HertzPhys::go, pkg/dem/Hertz.cpp:43 (constant per functor)
+        const double PI = 3.14159265358979323846;
+        double sqrt5 = std::sqrt(5.);
+        double le = std::log(cfg.hz_en);
+        p.hzViscConst = -sqrt5 * le / (std::sqrt(le * le + PI * PI));
+    }
+    p.periodic = cfg.periodic;
+    p.homoDeform = cfg.homo_deform;
+    p.evalStress = cfg.eval_stress;
+    p.loneMask = cfg.lone_mask;
+    // InsertionSortCollider.verletDist < 0: |verletDist| * min sphere radius
+    // (InsertionSortCollider.cpp:290-298)
+    double vd = cfg.verlet_dist;
+    if (vd < 0) {
+        double minR = std::numeric_limits<double>::infinity();
+        // radius of spheres is in posr.w; read back from the host description
+        for (int64_t i = 0; i < nPar; i++)
+            if (hShape[i] == WG_SHAPE_SPHERE) minR = std::min(minR, hRadius[i]);
+        vd = std::isinf(minR) ? 0 : std::abs(vd) * minR;
+    }
+    p.verletDist = vd;
+    p.maxD2 = vd * vd;
+    (void)X;
+    (void)S;
+    return 0;
+}
+
+static void fillCellPar(SimEx& X) {
+    ScenePar& p = X.hPar;
+    HostCell& c = X.cell;
+    toRow(c.hSize, p.hSize);
+    toRow(c.pprevHsize, p.pprevHsize);
+    toRow(c.gradV, p.gradV);
+    toRow(c.nextGradV, p.nextGradV);
+    toRow(hsub(c.nextGradV, c.gradV), p.dGradV);
+    toRow(hscale(hadd(c.gradV, c.nextGradV), .5), p.midGradV);
+    // Cell::intrShiftVel, core/Cell.cpp:28-34
+    if (c.homoDeform == 4) toRow(hmul(c.gradV, c.pprevHsize), p.shiftVelMat);
+    else if (c.homoDeform == 2 || c.homoDeform == 3) toRow(hmul(c.gradV, c.hSize), p.shiftVelMat);
+    else toRow(HM{}, p.shiftVelMat);
+    toRow(c.unshearTrsf, p.unshear);
+    for (int i = 0; i < 3; i++) { p.cellSize[i] = c.size[i]; p.spinVec[i] = c.spinVec[i]; }
+    p.hasShear = c.hasShear;
+    // Leapfrog::run, pkg/dem/Leapfrog.cpp:118-126
+    const double dt = X.cfg.dt;
+    const HM& pprevL = c.gradV;
+    const HM& nnextL = c.nextGradV;
+    HM q = hdiv(hscale(hadd(nnextL, pprevL), dt), 4.);
+    toRow(hinv(hsub(hI(), q)), p.ImLL4hInv);
+    toRow(hadd(hI(), q), p.IpLL4h);
+    toRow(hsub(nnextL, pprevL), p.LmL);
+    double a[3], b[3];
+    hlevi(hscale(hsub(pprevL, htr(pprevL)), .5), a);
+    hlevi(hscale(hsub(nnextL, htr(nnextL)), .5), b);
+    for (int i = 0; i < 3; i++) p.deltaSpinVec[i] = -.5 * a[i] + .5 * b[i];
+    // skew cosines for Cell::shearAlignedExtents (core/Cell.cpp:68-78)
+    for (int i = 0; i < 3; i++) p.cellCos[i] = c.cosv[i];
+}
+
+int Sim::upload() {
+    Sim& S = *this;
+    SimEx& X = static_cast<SimEx&>(*this);
+    if (!haveCfg) return fail(WG_ERR_STATE, "wg_set_config must be called before running");
+    if (nPar == 0) return fail(WG_ERR_STATE, "no particles");
+    if (!cfg.reset) return fail(WG_ERR_UNSUPPORTED, "Leapfrog.reset=False: the GPU path integrates the engine list [Leapfrog(reset=True), InsertionSortCollider, ContactLoop]");
+    if (!((cfg.phys == 0 && cfg.law == 0) || (cfg.phys == 1 && cfg.law == 1)))
+        return fail(WG_ERR_UNSUPPORTED, "unsupported Cp2/Law2 combination (FrictPhys+IdealElPl or HertzPhys+HertzPhys_DMT)");
+    if (cfg.law == 1 && cfg.hz_alpha != 0) return fail(WG_ERR_UNSUPPORTED, "Law2_L6Geom_HertzPhys_DMT with Cp2_FrictMat_HertzPhys.alpha!=0 (Schwarz model) is not supported");
+    if (cfg.precision != WG_PREC_FP64) return fail(WG_ERR_UNSUPPORTED, "precision mode not available in this build");
+    if (cfg.periodic) return fail(WG_ERR_UNSUPPORTED, "periodic cells are not available in this build");
+    for (int64_t i = 0; i < nPar; i++) {
+        if (hMat[i] < 0 || hMat[i] >= (int)hDensity.size()) return fail(WG_ERR_ARG, "particle material index out of range");
+    }
+    // node slots
+    std::vector<int32_t> map(nApiNodes, -1);
+    int64_t nExtra = 0;
+    for (int64_t p = 0; p < nPar; p++) {
+        const int sh = hShape[p];
+        if (sh == WG_SHAPE_SPHERE || sh == WG_SHAPE_WALL) {
+            int32_t a = hNodes3[3 * p];
+            if (a < 0 || a >= nApiNodes) return fail(WG_ERR_ARG, "particle node index out of range");
+            if (map[a] >= 0) return fail(WG_ERR_UNSUPPORTED, "a node shared between particles (clumps, meshes with spheres) is outside the GPU path");
+            map[a] = (int32_t)p;
+        }
+    }
+    for (int64_t p = 0; p < nPar; p++) {
+        if (hShape[p] != WG_SHAPE_FACET) continue;
+        for (int k = 0; k < 3; k++) {
+            int32_t a = hNodes3[3 * p + k];
+            if (a < 0 || a >= nApiNodes) return fail(WG_ERR_ARG, "facet node index out of range");
+            if (map[a] >= 0 && map[a] < nPar) return fail(WG_ERR_UNSUPPORTED, "facet shares a node with a sphere or wall");
+            if (map[a] < 0) map[a] = (int32_t)(nPar + nExtra++);
+        }
+    }
+    const int64_t nSlots = nPar + nExtra;
+    std::vector<double4_32a> posr(nSlots), vel(nSlots), angv(nSlots), ori(nSlots), force(nSlots), torque(nSlots), minert(nSlots);
+    std::vector<uint32_t> flags(nSlots, F_DOF_ALL);
+    for (int64_t s = 0; s < nSlots; s++) {
+        posr[s] = vel[s] = angv[s] = force[s] = torque[s] = minert[s] = make_double4_32a(0, 0, 0, 0);
+        ori[s] = make_double4_32a(1, 0, 0, 0);
+    }
+    const double* st = hApi.data();
+    const int64_t na = nApiNodes;
+    for (int64_t a = 0; a < na; a++) {
+        int32_t s = map[a];
+        if (s < 0) continue;
+        posr[s] = make_double4_32a(st[3 * a], st[3 * a + 1], st[3 * a + 2], 0.);
+        ori[s] = make_double4_32a(st[3 * na + 4 * a], st[3 * na + 4 * a + 1], st[3 * na + 4 * a + 2], st[3 * na + 4 * a + 3]);
+        vel[s] = make_double4_32a(st[7 * na + 3 * a], st[7 * na + 3 * a + 1], st[7 * na + 3 * a + 2], 0);
+        angv[s] = make_double4_32a(st[10 * na + 3 * a], st[10 * na + 3 * a + 1], st[10 * na + 3 * a + 2], 0);
+        force[s] = make_double4_32a(st[13 * na + 3 * a], st[13 * na + 3 * a + 1], st[13 * na + 3 * a + 2], 0);
+        torque[s] = make_double4_32a(st[16 * na + 3 * a], st[16 * na + 3 * a + 1], st[16 * na + 3 * a + 2], 0);
+        minert[s] = make_double4_32a(hInertia[3 * a], hInertia[3 * a + 1], hInertia[3 * a + 2], hMass[a]);
+        flags[s] = hFlagsApi[a];
+    }
+    std::vector<int32_t> shape(nPar), mat(nPar);
+    std::vector<int4> aux(nPar);
+    std::vector<double4_32a> facet(nPar);
+    std::vector<uint32_t> mask(nPar);
+    nSpheres = 0;
+    for (int64_t p = 0; p < nPar; p++) {
+        shape[p] = hShape[p];
+        mat[p] = hMat[p];
+        mask[p] = hMask[p];
+        aux[p] = make_int4(0, 0, 0, 0);
+        facet[p] = make_double4_32a(0, 0, 0, 0);
+        if (hShape[p] == WG_SHAPE_SPHERE) {
+            posr[p].w = hRadius[p];
+            nSpheres++;
+        } else if (hShape[p] == WG_SHAPE_WALL) {
+            if (hAxis[p] < 0 || hAxis[p] > 2) return fail(WG_ERR_ARG, "Wall.axis must be 0, 1 or 2");
+            aux[p] = make_int4(hAxis[p], hSense[p], 0, 0);
+        } else if (hShape[p] == WG_SHAPE_FACET) {
+            aux[p] = make_int4(map[hNodes3[3 * p]], map[hNodes3[3 * p + 1]], map[hNodes3[3 * p + 2]], 0);
+            facet[p] = make_double4_32a(hFakeVel[3 * p], hFakeVel[3 * p + 1], hFakeVel[3 * p + 2], hHalfThick[p]);
+        } else return fail(WG_ERR_UNSUPPORTED, "unknown shape code");
+    }
+    WG_CUDA_TRY(cudaSetDevice(device));
+    N.n = (int32_t)nSlots;
+    N.posr = (double4_32a*)dalloc(sizeof(double4_32a) * nSlots);
+    N.vel = (double4_32a*)dalloc(sizeof(double4_32a) * nSlots);
+    N.angv = (double4_32a*)dalloc(sizeof(double4_32a) * nSlots);
+    N.ori = (double4_32a*)dalloc(sizeof(double4_32a) * nSlots);
+    N.force = (double4_32a*)dalloc(sizeof(double4_32a) * nSlots);
+    N.torque = (double4_32a*)dalloc(sizeof(double4_32a) * nSlots);
+    N.minert = (double4_32a*)dalloc(sizeof(double4_32a) * nSlots);
+    N.lastPos = (double4_32a*)dalloc(sizeof(double4_32a) * nSlots);
+    N.flags = (uint32_t*)dalloc(sizeof(uint32_t) * nSlots);
+    P.n = (int32_t)nPar;
+    P.shape = (int32_t*)dalloc(sizeof(int32_t) * nPar);
+    P.aux = (int4*)dalloc(sizeof(int4) * nPar);
+    P.facet = (double4_32a*)dalloc(sizeof(double4_32a) * nPar);
+    P.mat = (int32_t*)dalloc(sizeof(int32_t) * nPar);
+    P.mask = (uint32_t*)dalloc(sizeof(uint32_t) * nPar);
+    P.mn = (double4_32a*)dalloc(sizeof(double4_32a) * nPar);
+    P.mx = (double4_32a*)dalloc(sizeof(double4_32a) * nPar);
+    I.loStart = (int32_t*)dalloc(sizeof(int32_t) * (nPar + 1));
+    I.hiStart = (int32_t*)dalloc(sizeof(int32_t) * (nPar + 1));
+    I.heavy = (int32_t*)dalloc(sizeof(int32_t) * nPar);
+    dMats = (double4_32a*)dalloc(sizeof(double4_32a) * std::max<size_t>(1, hDensity.size()));
+    dPar = (ScenePar*)dalloc(sizeof(ScenePar));
+    dStep = (long long*)dalloc(sizeof(long long));
+    dFlags = (int*)dalloc(sizeof(int) * 4);
+    X.dApiMap = (int32_t*)dalloc(sizeof(int32_t) * std::max<int64_t>(1, na));
+    X.dStage = (double*)dalloc(sizeof(double) * 19 * std::max<int64_t>(1, na));
+    if (!X.dStage) return fail(WG_ERR_CUDA, "out of device memory (scene)");
+    WG_CUDA_TRY(cudaMallocHost(&hFlags, sizeof(int) * 4));
+    std::vector<double4_32a> mats(hDensity.size());
+    for (size_t m = 0; m < hDensity.size(); m++) mats[m] = make_double4_32a(hDensity[m], hYoung[m], hTanPhi[m], hKtDivKn[m]);
+    WG_CUDA_TRY(cudaMemcpy(N.posr, posr.data(), sizeof(double4_32a) * nSlots, cudaMemcpyHostToDevice));
+    WG_CUDA_TRY(cudaMemcpy(N.vel, vel.data(), sizeof(double4_32a) * nSlots, cudaMemcpyHostToDevice));
+    WG_CUDA_TRY(cudaMemcpy(N.angv, angv.data(), sizeof(double4_32a) * nSlots, cudaMemcpyHostToDevice));
+    WG_CUDA_TRY(cudaMemcpy(N.ori, ori.data(), sizeof(double4_32a) * nSlots, cudaMemcpyHostToDevice));
+    WG_CUDA_TRY(cudaMemcpy(N.force, force.data(), sizeof(double4_32a) * nSlots, cudaMemcpyHostToDevice));
+    WG_CUDA_TRY(cudaMemcpy(N.torque, torque.data(), sizeof(double4_32a) * nSlots, cudaMemcpyHostToDevice));
+    WG_CUDA_TRY(cudaMemcpy(N.minert, minert.data(), sizeof(double4_32a) * nSlots, cudaMemcpyHostToDevice));
+    WG_CUDA_TRY(cudaMemcpy(N.lastPos, posr.data(), sizeof(double4_32a) * nSlots, cudaMemcpyHostToDevice));
+    WG_CUDA_TRY(cudaMemcpy(N.flags, flags.data(), sizeof(uint32_t) * nSlots, cudaMemcpyHostToDevice));
+    WG_CUDA_TRY(cudaMemcpy(P.shape, shape.data(), sizeof(int32_t) * nPar, cudaMemcpyHostToDevice));
+    WG_CUDA_TRY(cudaMemcpy(P.aux, aux.data(), sizeof(int4) * nPar, cudaMemcpyHostToDevice));
+    WG_CUDA_TRY(cudaMemcpy(P.facet, facet.data(), sizeof(double4_32a) * nPar, cudaMemcpyHostToDevice));
+    WG_CUDA_TRY(cudaMemcpy(P.mat, mat.data(), sizeof(int32_t) * nPar, cudaMemcpyHostToDevice));
+    WG_CUDA_TRY(cudaMemcpy(P.mask, mask.data(), sizeof(uint32_t) * nPar, cudaMemcpyHostToDevice));
+    WG_CUDA_TRY(cudaMemcpy(dMats, mats.data(), sizeof(double4_32a) * mats.size(), cudaMemcpyHostToDevice));
+    WG_CUDA_TRY(cudaMemcpy(X.dApiMap, map.data(), sizeof(int32_t) * na, cudaMemcpyHostToDevice));
+    WG_CUDA_TRY(cudaMemcpy(X.dStage, hApi.data(), sizeof(double) * 19 * na, cudaMemcpyHostToDevice));
+    X.hApiMap = map;
+    long long st0 = cfg.step;
+    step = cfg.step;
+    WG_CUDA_TRY(cudaMemcpy(dStep, &st0, sizeof(long long), cudaMemcpyHostToDevice));
+    WG_CUDA_TRY(cudaMemset(dFlags, 0, sizeof(int) * 4));
+    int r = ensureContactCapacity(std::max<int64_t>(1024, 4 * nPar));
+    if (r) return r;
+    C.n = 0;
+    if (cfg.periodic) {
+        X.cell.trsf = fromRow(cfg.cell_trsf);
+        X.cell.hSize = fromRow(cfg.cell_hsize);
+        X.cell.pprevHsize = X.cell.hSize;
+        X.cell.gradV = fromRow(cfg.cell_gradv);
+        X.cell.nextGradV = fromRow(cfg.cell_next_gradv);
+        X.cell.homoDeform = cfg.homo_deform;
+        HM W = hscale(hsub(X.cell.gradV, htr(X.cell.gradV)), .5);
+        double lv[3];
+        hlevi(W, lv);
+        for (int i = 0; i < 3; i++) X.cell.spinVec[i] = .5 * lv[i];
+        X.cell.integrateAndUpdate(0);
+    }
+    prepareParams();
+    WG_CUDA_TRY(cudaMemcpy(dPar, &hPar, sizeof(ScenePar), cudaMemcpyHostToDevice));
+    uploaded = true;
+    initialized = false;
+    return 0;
+}
+
+int Sim::checkErr() {
+    Sim& S = *this;
+    WG_CUDA_TRY(cudaMemcpyAsync(hFlags, dFlags, sizeof(int) * 4, cudaMemcpyDeviceToHost, stream));
+    WG_CUDA_TRY(cudaStreamSynchronize(stream));
+    if (hFlags[1] == 101) return fail(WG_ERR_NAN, "NaN force in contact (message above)?!");
+    if (hFlags[1] == 102) return fail(WG_ERR_NAN, "InsertionSortCollider: NaN in a particle bounding box (NaN position)");
+    if (hFlags[1] == 100) return fail(WG_ERR_ARG, "Cg2_Facet_Sphere_L3Geom: Impossible sphere-facet intersection (all points are outside the edges). (please report bug)");
+    if (hFlags[1] != 0) return fail(WG_ERR_STATE, "device error code " + std::to_string(hFlags[1]));
+    return 0;
+}
+
+int Sim::run(int64_t n) {
+    Sim& S = *this;
+    SimEx& X = static_cast<SimEx&>(*this);
+    if (!uploaded) {
+        int r = upload();
+        if (r) return r;
+    }
+    WG_CUDA_TRY(cudaSetDevice(device));
+    double ph[4] = {0, 0, 0, 0};
+    int64_t launches = 0;
+    WG_CUDA_TRY(cudaEventRecord(ev[6], stream));
+    for (int64_t i = 0; i < n; i++) {
+        if (cfg.periodic) {
+            X.cell.integrateAndUpdate(cfg.dt);
+            fillCellPar(X);
+            WG_CUDA_TRY(cudaMemcpyAsync(dPar, &hPar, sizeof(ScenePar), cudaMemcpyHostToDevice, stream));
+        }
+        WG_CUDA_TRY(cudaEventRecord(ev[0], stream));
+        WG_CUDA_TRY(cudaMemsetAsync(dFlags, 0, sizeof(int), stream));
+        launch_leapfrog(stream, N, P, dPar, dFlags);
+        launches++;
+        WG_CUDA_TRY(cudaEventRecord(ev[1], stream));
+        WG_CUDA_TRY(cudaMemcpyAsync(hFlags, dFlags, sizeof(int), cudaMemcpyDeviceToHost, stream));
+        WG_CUDA_TRY(cudaStreamSynchronize(stream));
+        bool full = !initialized || hFlags[0] != 0 || hPar.verletDist == 0;
+        WG_CUDA_TRY(cudaEventRecord(ev[2], stream));
+        if (full) {
+            int r = collide_full_run(*this);
+            if (r) return r;
+            initialized = true;
+            launches += 12;
+        }
+        WG_CUDA_TRY(cudaEventRecord(ev[3], stream));
+        launch_contact_fp64(stream, N, P, C, dMats, dPar, dStep, dFlags + 1);
+        WG_CUDA_TRY(cudaEventRecord(ev[4], stream));
+        launch_reduce(stream, N, P, C, I, dPar, dStep);
+        launches += 3 + (I.nHeavy > 0);
+        WG_CUDA_TRY(cudaEventRecord(ev[5], stream));
+        WG_CUDA_TRY(cudaGetLastError());
+        WG_CUDA_TRY(cudaEventSynchronize(ev[5]));
+        float a;
+        cudaEventElapsedTime(&a, ev[0], ev[1]); ph[0] += a;
+        cudaEventElapsedTime(&a, ev[3], ev[4]); ph[1] += a;
+        cudaEventElapsedTime(&a, ev[4], ev[5]); ph[2] += a;
+        cudaEventElapsedTime(&a, ev[2], ev[3]); ph[3] += a;
+        if (cfg.periodic) X.cell.setNextGradV();
+        step++;
+        time += cfg.dt;
+    }
+    WG_CUDA_TRY(cudaEventRecord(ev[7], stream));
+    WG_CUDA_TRY(cudaEventSynchronize(ev[7]));
+    float tot = 0;
+    cudaEventElapsedTime(&tot, ev[6], ev[7]);
+    lastTotalMs = tot;
+    for (int q = 0; q < 4; q++) phaseMs[q] = ph[q];
+    lastLaunches = launches;
+    return checkErr();
+}
+
+}  // namespace wg
+
+using namespace wg;
+
+extern "C" {
+
+int wg_create(wg_scene** out, int device) {
+    if (!out) return WG_ERR_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        g_createError = "no CUDA device available";
+        return WG_ERR_CUDA;
+    }
+    if (device < 0 || device >= ndev) {
+        g_createError = "CUDA device index out of range";
+        return WG_ERR_ARG;
+    }
+    if (cudaSetDevice(device) != cudaSuccess) {
+        g_createError = "cudaSetDevice failed";
+        return WG_ERR_CUDA;
+    }
+    SimEx* s = new SimEx();
+    s->device = device;
+    for (int i = 0; i < 8; i++) s->ev[i] = nullptr;
+    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        g_createError = "cudaStreamCreate failed";
+        delete s;
+        return WG_ERR_CUDA;
+    }
+    for (int i = 0; i < 8; i++) cudaEventCreate(&s->ev[i]);
+    std::memset(&s->cfg, 0, sizeof(s->cfg));
+    *out = reinterpret_cast<wg_scene*>(static_cast<Sim*>(s));
+    return WG_OK;
+}
+
+void wg_destroy(wg_scene* s) { delete static_cast<SimEx*>(reinterpret_cast<Sim*>(s)); }
+
+const char* wg_last_error(const wg_scene* s) {
+    if (!s) return g_createError.c_str();
+    return reinterpret_cast<const Sim*>(s)->err.c_str();
+}
+
+static Sim* SIM(wg_scene* s) { return reinterpret_cast<Sim*>(s); }
+
+int wg_set_config(wg_scene* s, const wg_config* c) {
+    if (!s || !c) return WG_ERR_ARG;
+    Sim& S = *SIM(s);
+    if (S.uploaded) return S.fail(WG_ERR_STATE, "configuration is fixed once the scene runs; create a new scene");
+    if (!(c->dt > 0) || !std::isfinite(c->dt)) return S.fail(WG_ERR_ARG, "Scene.dt must be positive and finite");
+    S.cfg = *c;
+    S.haveCfg = true;
+    return WG_OK;
+}
+
+int wg_set_materials(wg_scene* s, int32_t n, const double* density, const double* young, const double* tan_phi,
+                     const double* kt_div_kn) {
+    if (!s || n < 0 || (n > 0 && (!density || !young || !tan_phi || !kt_div_kn))) return WG_ERR_ARG;
+    Sim& S = *SIM(s);
+    if (S.uploaded) return S.fail(WG_ERR_STATE, "materials are fixed once the scene runs");
+    S.hDensity.assign(density, density + n);
+    S.hYoung.assign(young, young + n);
+    S.hTanPhi.assign(tan_phi, tan_phi + n);
+    S.hKtDivKn.assign(kt_div_kn, kt_div_kn + n);
+    return WG_OK;
+}
+
+int wg_set_nodes(wg_scene* s, int64_t n, const double* pos, const double* ori, const double* vel, const double* ang_vel,
+                 const double* force, const double* torque, const double* mass, const double* inertia, const uint32_t* flags) {
+    if (!s || n < 0 || (n > 0 && (!pos || !ori || !vel || !ang_vel || !force || !torque || !mass || !inertia || !flags))) return WG_ERR_ARG;
+    Sim& S = *SIM(s);
+    if (S.uploaded) return S.fail(WG_ERR_STATE, "use wg_put_state to change the state of a running scene");
+    S.nApiNodes = n;
+    S.hApi.resize(19 * n);
+    std::memcpy(S.hApi.data(), pos, sizeof(double) * 3 * n);
+    std::memcpy(S.hApi.data() + 3 * n, ori, sizeof(double) * 4 * n);
+    std::memcpy(S.hApi.data() + 7 * n, vel, sizeof(double) * 3 * n);
+    std::memcpy(S.hApi.data() + 10 * n, ang_vel, sizeof(double) * 3 * n);
+    std::memcpy(S.hApi.data() + 13 * n, force, sizeof(double) * 3 * n);
+    std::memcpy(S.hApi.data() + 16 * n, torque, sizeof(double) * 3 * n);
+    S.hMass.assign(mass, mass + n);
+    S.hInertia.assign(inertia, inertia + 3 * n);
+    S.hFlagsApi.assign(flags, flags + n);
+    return WG_OK;
+}
+
+int wg_set_particles(wg_scene* s, int64_t n, const int32_t* shape, const int32_t* nodes3, const double* radius,
+                     const int32_t* wall_axis, const int32_t* wall_sense, const double* half_thick, const double* fake_vel,
+                     const int32_t* mat, const uint32_t* mask) {
+    if (!s || n < 0 || (n > 0 && (!shape || !nodes3 || !radius || !wall_axis || !wall_sense || !half_thick || !fake_vel || !mat || !mask)))
+        return WG_ERR_ARG;
+    Sim& S = *SIM(s);
+    if (S.uploaded) return S.fail(WG_ERR_STATE, "particles are fixed once the scene runs; create a new scene");
+    if (n >= (int64_t(1) << 31) - 2) return S.fail(WG_ERR_ARG, "too many particles");
+    S.nPar = n;
+    S.hShape.assign(shape, shape + n);
+    S.hNodes3.assign(nodes3, nodes3 + 3 * n);
+    S.hRadius.assign(radius, radius + n);
+    S.hAxis.assign(wall_axis, wall_axis + n);
+    S.hSense.assign(wall_sense, wall_sense + n);
+    S.hHalfThick.assign(half_thick, half_thick + n);
+    S.hFakeVel.assign(fake_vel, fake_vel + 3 * n);
+    S.hMat.assign(mat, mat + n);
+    S.hMask.assign(mask, mask + n);
+    return WG_OK;
+}
+
+int wg_run(wg_scene* s, int64_t n_steps) {
+    if (!s || n_steps < 0) return WG_ERR_ARG;
+    return SIM(s)->run(n_steps);
+}
+
+int wg_collide_only(wg_scene* s) {
+    if (!s) return WG_ERR_ARG;
+    Sim& S = *SIM(s);
+    if (!S.uploaded) {
+        int r = S.upload();
+        if (r) return r;
+    }
+    int r = collide_full_run(S);
+    if (r) return r;
+    S.initialized = true;
+    WG_CUDA_TRY(cudaStreamSynchronize(S.stream));
+    return WG_OK;
+}
+
+int wg_put_state(wg_scene* s, const double* pos, const double* ori, const double* vel, const double* ang_vel, const double* force,
+                 const double* torque) {
+    if (!s) return WG_ERR_ARG;
+    Sim& S = *SIM(s);
+    SimEx& X = static_cast<SimEx&>(S);
+    if (!S.uploaded) {
+        // before the first run the description itself is replaced
+        const int64_t n = S.nApiNodes;
+        if (pos) std::memcpy(S.hApi.data(), pos, sizeof(double) * 3 * n);
+        if (ori) std::memcpy(S.hApi.data() + 3 * n, ori, sizeof(double) * 4 * n);
+        if (vel) std::memcpy(S.hApi.data() + 7 * n, vel, sizeof(double) * 3 * n);
+        if (ang_vel) std::memcpy(S.hApi.data() + 10 * n, ang_vel, sizeof(double) * 3 * n);
+        if (force) std::memcpy(S.hApi.data() + 13 * n, force, sizeof(double) * 3 * n);
+        if (torque) std::memcpy(S.hApi.data() + 16 * n, torque, sizeof(double) * 3 * n);
+        return WG_OK;
+    }
+    const int64_t na = S.nApiNodes;
+    const double* src[6] = {pos, ori, vel, ang_vel, force, torque};
+    const int64_t off[6] = {0, 3, 7, 10, 13, 16}, w[6] = {3, 4, 3, 3, 3, 3};
+    // fill missing components from the current device state
+    if (!(pos && ori && vel && ang_vel && force && torque)) {
+        k_get_state<<<(unsigned)((na + 255) / 256), 256, 0, S.stream>>>(S.N, X.dApiMap, na, X.dStage);
+    }
+    for (int q = 0; q < 6; q++)
+        if (src[q]) WG_CUDA_TRY(cudaMemcpyAsync(X.dStage + off[q] * na, src[q], sizeof(double) * w[q] * na, cudaMemcpyHostToDevice, S.stream));
+    k_put_state<<<(unsigned)((na + 255) / 256), 256, 0, S.stream>>>(S.N, X.dApiMap, na, X.dStage);
+    WG_CUDA_TRY(cudaGetLastError());
+    WG_CUDA_TRY(cudaStreamSynchronize(S.stream));
+    return WG_OK;
+}
+
+int wg_get_nodes(wg_scene* s, double* pos, double* ori, double* vel, double* ang_vel, double* force, double* torque) {
+    if (!s) return WG_ERR_ARG;
+    Sim& S = *SIM(s);
+    SimEx& X = static_cast<SimEx&>(S);
+    const int64_t na = S.nApiNodes;
+    double* dst[6] = {pos, ori, vel, ang_vel, force, torque};
+    const int64_t off[6] = {0, 3, 7, 10, 13, 16}, w[6] = {3, 4, 3, 3, 3, 3};
+    if (!S.uploaded) {
+        for (int q = 0; q < 6; q++)
+            if (dst[q]) std::memcpy(dst[q], S.hApi.data() + off[q] * na, sizeof(double) * w[q] * na);
+        return WG_OK;
+    }
+    k_get_state<<<(unsigned)((na + 255) / 256), 256, 0, S.stream>>>(S.N, X.dApiMap, na, X.dStage);
+    for (int q = 0; q < 6; q++)
+        if (dst[q]) WG_CUDA_TRY(cudaMemcpyAsync(dst[q], X.dStage + off[q] * na, sizeof(double) * w[q] * na, cudaMemcpyDeviceToHost, S.stream));
+    WG_CUDA_TRY(cudaGetLastError());
+    WG_CUDA_TRY(cudaStreamSynchronize(S.stream));
+    return WG_OK;
+}
+
+int wg_run_host(wg_scene* s, int64_t n_steps, double* pos, double* ori, double* vel, double* ang_vel, double* force, double* torque) {
+    int r = wg_put_state(s, pos, ori, vel, ang_vel, force, torque);
+    if (r) return r;
+    r = wg_run(s, n_steps);
+    if (r) return r;
+    return wg_get_nodes(s, pos, ori, vel, ang_vel, force, torque);
+}
+
+int wg_get_stats(wg_scene* s, wg_stats* o) {
+    if (!s || !o) return WG_ERR_ARG;
+    Sim& S = *SIM(s);
+    std::memset(o, 0, sizeof(*o));
+    o->step = S.step;
+    o->time = S.time;
+    o->n_full_runs = S.nFullRuns;
+    o->n_contacts = S.uploaded ? S.C.n : 0;
+    o->verlet_dist = S.hPar.verletDist;
+    if (S.uploaded && S.C.n > 0) {
+        std::vector<uint32_t> fl(S.C.n);
+        WG_CUDA_TRY(cudaMemcpy(fl.data(), S.C.flags, sizeof(uint32_t) * S.C.n, cudaMemcpyDeviceToHost));
+        int64_t r = 0;
+        for (uint32_t f : fl) r += (f & C_REAL) ? 1 : 0;
+        o->n_real = r;
+    }
+    return WG_OK;
+}
+
+int wg_set_next_gradv(wg_scene* s, const double* g) {
+    if (!s || !g) return WG_ERR_ARG;
+    Sim& S = *SIM(s);
+    SimEx& X = static_cast<SimEx&>(S);
+    for (int i = 0; i < 9; i++) S.cfg.cell_next_gradv[i] = g[i];
+    if (S.uploaded) X.cell.nextGradV = fromRow(g);
+    return WG_OK;
+}
+
+int wg_get_cell(wg_scene* s, double* hsize, double* trsf, double* gradv) {
+    if (!s) return WG_ERR_ARG;
+    SimEx& X = static_cast<SimEx&>(*SIM(s));
+    if (!X.uploaded) {
+        if (hsize) std::memcpy(hsize, X.cfg.cell_hsize, sizeof(double) * 9);
+        if (trsf) std::memcpy(trsf, X.cfg.cell_trsf, sizeof(double) * 9);
+        if (gradv) std::memcpy(gradv, X.cfg.cell_gradv, sizeof(double) * 9);
+        return WG_OK;
+    }
+    if (hsize) toRow(X.cell.hSize, hsize);
+    if (trsf) toRow(X.cell.trsf, trsf);
+    if (gradv) toRow(X.cell.gradV, gradv);
+    return WG_OK;
+}
+
+// Contacts listed the way the reference's container holds them after a step: every contact
+// that is real, was removed by the law in the last step (pending), or whose boxes overlap.
+static int collectContacts(Sim& S, std::vector<int64_t>& keep, std::vector<uint64_t>& key, std::vector<uint32_t>& fl,
+                           std::vector<int32_t>& cd, std::vector<std::vector<double>>& cols) {
+    const int64_t n = S.C.n;
+    key.resize(n); fl.resize(n); cd.resize(n);
+    cols.assign(CC_NCOL, std::vector<double>(n));
+    if (n > 0) {
+        WG_CUDA_TRY(cudaMemcpy(key.data(), S.C.key, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost));
+        WG_CUDA_TRY(cudaMemcpy(fl.data(), S.C.flags, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
+        WG_CUDA_TRY(cudaMemcpy(cd.data(), S.C.cdist, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+        for (int q = 0; q < CC_NCOL; q++) WG_CUDA_TRY(cudaMemcpy(cols[q].data(), S.C.col[q], sizeof(double) * n, cudaMemcpyDeviceToHost));
+    }
+    std::vector<double4_32a> mn(S.nPar), mx(S.nPar);
+    if (S.nPar > 0) {
+        WG_CUDA_TRY(cudaMemcpy(mn.data(), S.P.mn, sizeof(double4_32a) * S.nPar, cudaMemcpyDeviceToHost));
+        WG_CUDA_TRY(cudaMemcpy(mx.data(), S.P.mx, sizeof(double4_32a) * S.nPar, cudaMemcpyDeviceToHost));
+    }
+    keep.clear();
+    for (int64_t c = 0; c < n; c++) {
+        if (fl[c] & (C_REAL | C_PENDING)) { keep.push_back(c); continue; }
+        const int a = (int)(key[c] >> 32), b = (int)(key[c] & 0xffffffffu);
+        const double4_32a &m1 = mn[a], &x1 = mx[a], &m2 = mn[b], &x2 = mx[b];
+        if ((m1.x <= x2.x) && (x1.x >= m2.x) && (m1.y <= x2.y) && (x1.y >= m2.y) && (m1.z <= x2.z) && (x1.z >= m2.z)) keep.push_back(c);
+    }
+    return 0;
+}
+
+int64_t wg_num_contacts(wg_scene* s) {
+    if (!s) return WG_ERR_ARG;
+    Sim& S = *SIM(s);
+    if (!S.uploaded) return 0;
+    std::vector<int64_t> keep;
+    std::vector<uint64_t> key;
+    std::vector<uint32_t> fl;
+    std::vector<int32_t> cd;
+    std::vector<std::vector<double>> cols;
+    int r = collectContacts(S, keep, key, fl, cd, cols);
+    if (r) return r;
+    return (int64_t)keep.size();
+}
+
+int wg_get_contacts(wg_scene* s, int32_t* id_lo, int32_t* id_hi, int32_t* id_a, int32_t* real, int32_t* cell_dist, double* fglob,
+                    double* local, double* cpt, double* trsf) {
+    if (!s) return WG_ERR_ARG;
+    Sim& S = *SIM(s);
+    if (!S.uploaded) return WG_OK;
+    std::vector<int64_t> keep;
+    std::vector<uint64_t> key;
+    std::vector<uint32_t> fl;
+    std::vector<int32_t> cd;
+    std::vector<std::vector<double>> cols;
+    int r = collectContacts(S, keep, key, fl, cd, cols);
+    if (r) return r;
+    for (size_t i = 0; i < keep.size(); i++) {
+        const int64_t c = keep[i];
+        const int lo = (int)(key[c] >> 32), hi = (int)(key[c] & 0xffffffffu);
+        const bool isReal = fl[c] & C_REAL;
+        if (id_lo) id_lo[i] = lo;
+        if (id_hi) id_hi[i] = hi;
+        if (id_a) id_a[i] = (fl[c] & C_SWAP) ? hi : lo;
+        if (real) real[i] = isReal ? 1 : 0;
+        int a, b, cc;
+        unpackCellDist(cd[c], a, b, cc);
+        if (cell_dist) { cell_dist[3 * i] = a; cell_dist[3 * i + 1] = b; cell_dist[3 * i + 2] = cc; }
+        for (int k = 0; k < 3; k++) {
+            if (fglob) fglob[3 * i + k] = isReal ? cols[CC_FGX + k][c] : 0.;
+            if (local) local[3 * i + k] = isReal ? cols[CC_FN + k][c] : 0.;
+            if (cpt) cpt[3 * i + k] = isReal ? cols[CC_CPX + k][c] : 0.;
+        }
+        if (trsf) {
+            D3 c0{cols[CC_T0X][c], cols[CC_T0Y][c], cols[CC_T0Z][c]}, c1{cols[CC_T1X][c], cols[CC_T1Y][c], cols[CC_T1Z][c]};
+            D3 c2 = cross(c0, c1);
+            const D3 cc3[3] = {c0, c1, c2};
+            for (int row = 0; row < 3; row++)
+                for (int col = 0; col < 3; col++) trsf[9 * i + 3 * row + col] = isReal ? comp(cc3[col], row) : 0.;
+        }
+    }
+    return WG_OK;
+}
+
+int wg_get_aabbs(wg_scene* s, double* mn, double* mx) {
+    if (!s) return WG_ERR_ARG;
+    Sim& S = *SIM(s);
+    if (!S.uploaded) return S.fail(WG_ERR_STATE, "no boxes before the first run");
+    std::vector<double4_32a> a(S.nPar), b(S.nPar);
+    WG_CUDA_TRY(cudaMemcpy(a.data(), S.P.mn, sizeof(double4_32a) * S.nPar, cudaMemcpyDeviceToHost));
+    WG_CUDA_TRY(cudaMemcpy(b.data(), S.P.mx, sizeof(double4_32a) * S.nPar, cudaMemcpyDeviceToHost));
+    for (int64_t i = 0; i < S.nPar; i++) {
+        mn[3 * i] = a[i].x; mn[3 * i + 1] = a[i].y; mn[3 * i + 2] = a[i].z;
+        mx[3 * i] = b[i].x; mx[3 * i + 1] = b[i].y; mx[3 * i + 2] = b[i].z;
+    }
+    return WG_OK;
+}
+
+void* wg_host_alloc(int64_t bytes) {
+    void* p = nullptr;
+    if (bytes <= 0 || cudaMallocHost(&p, (size_t)bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return p;
+}
+void wg_host_free(void* p) {
+    if (p) cudaFreeHost(p);
+}
+
+int wg_get_timing(wg_scene* s, double* total_ms, double* phase_ms4, int64_t* launches) {
+    if (!s) return WG_ERR_ARG;
+    Sim& S = *SIM(s);
+    if (total_ms) *total_ms = S.lastTotalMs;
+    if (phase_ms4)
+        for (int q = 0; q < 4; q++) phase_ms4[q] = S.phaseMs[q];
+    if (launches) *launches = S.lastLaunches;
+    return WG_OK;
+}
+
+}  // extern "C"

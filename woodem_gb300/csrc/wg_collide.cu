@@ -1,0 +1,739 @@
+// Broad phase: the full run of InsertionSortCollider (pkg/dem/InsertionSortCollider.cpp:445-646).
+//
+// The reference maintains three insertion-sorted bound arrays; every min/max inversion
+// creates a potential contact when the closed 3-axis AABB test passes (:52-58, :63-98) or
+// removes a non-real contact when the boxes separate. After each full run its contact set
+// is therefore
+//     { (i,j) : closed AABB overlap of i and j, Collider::mayCollide(i,j) }  U  { real contacts },
+// and pending (law-removed) contacts survive only while their boxes overlap
+// (ContactContainer::removePending, ContactContainer.hpp:78-93). This file computes exactly
+// that set on the GPU:
+//   1. Bo1 functors + verlet enlargement per particle            (k_aabb)
+//   2. spheres bucketed into a uniform grid whose cell is at least the largest sphere box,
+//      keyed by the cell of the box minimum and radix-sorted      (k_cellkey + cub radix sort)
+//   3. half-shell sweep over the sorted cells: every candidate pair is tested once with the
+//      reference's closed-interval comparisons                   (k_pairs_ss)
+//   4. facets query the cells their box covers; walls (infinite boxes) test every sphere
+//   5. the new pair keys are radix-sorted and merged with the real contacts of the previous
+//      set, carrying their persistent state                      (k_mark_orphans .. k_gather)
+//   6. CSR incidence for the deterministic force sum              (k_lo_start, hi sort, k_hi_start)
+#include <cub/cub.cuh>
+
+#include <algorithm>
+#include <cmath>
+
+#include "wg_internal.h"
+#include "wg_math.cuh"
+
+namespace wg {
+
+struct CollideWork {
+    // sphere and "large" (non-sphere) id lists, built at upload
+    int32_t* sphereIds = nullptr;
+    int nSph = 0;
+    int32_t* largeIds = nullptr;   // facets with finite boxes (cell query)
+    int nLarge = 0;
+    int32_t* globalIds = nullptr;  // walls and oversized boxes (tested against every sphere)
+    int nGlobal = 0;
+    bool largeLargePossible = false;
+    std::vector<int32_t> hLarge, hGlobal;
+    // grid scratch
+    uint32_t* cellKey = nullptr;
+    uint32_t* cellKeySorted = nullptr;
+    int32_t* cellVal = nullptr;
+    int32_t* sid = nullptr;       // sorted sphere ids
+    double4_32a* smn = nullptr;
+    double4_32a* smx = nullptr;
+    uint32_t* smask = nullptr;
+    int32_t* cellOff = nullptr;
+    int64_t cellOffCap = 0;
+    double* red = nullptr;        // reduction partials
+    double* hRed = nullptr;       // pinned
+    // pairs
+    uint64_t* pairs = nullptr;
+    uint64_t* pairsSorted = nullptr;
+    int64_t pairCap = 0;
+    unsigned long long* counter = nullptr;
+    unsigned long long* hCounter = nullptr;
+    // merge scratch
+    int32_t* orph = nullptr;      // flags then exclusive scan
+    uint64_t* orphKey = nullptr;
+    int32_t* orphSrc = nullptr;
+    int32_t* src = nullptr;
+    int64_t mergeCap = 0;
+    uint32_t* hiKeys = nullptr;
+    uint32_t* hiKeysSorted = nullptr;
+    int32_t* hiVals = nullptr;
+    int64_t hiCap = 0;
+    int32_t* heavyCount = nullptr;
+    int32_t* hHeavy = nullptr;
+    void* cubTmp = nullptr;
+    size_t cubBytes = 0;
+};
+
+static const int BS = 256;
+
+// ---------------------------------------------------------------- Bo1 functors + verlet
+// Bo1_Sphere_Aabb::go pkg/dem/Sphere.cpp:50-79, Bo1_Wall_Aabb::go pkg/dem/Wall.cpp:24-33,
+// Bo1_Facet_Aabb::go pkg/dem/Facet.cpp:177-200; enlargement by verletDist and nodeLastPos
+// bookkeeping of updateBboxes_doFullRun pkg/dem/InsertionSortCollider.cpp:386-414.
+__global__ void k_aabb(DevNodes N, DevParticles P, const ScenePar* __restrict__ spp, int* __restrict__ dErr) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P.n) return;
+    const ScenePar& sp = *spp;
+    const int sh = P.shape[p];
+    D3 mn, mx;
+    const double inf = __longlong_as_double(0x7ff0000000000000LL);
+    if (sh == WG_SHAPE_SPHERE) {
+        const double4_32a pr = N.posr[p];
+        const double f = (sp.bo1DistFactor > 0 ? sp.bo1DistFactor : 1.) * pr.w;
+        D3 h{f, f, f};
+        const D3 pos{pr.x, pr.y, pr.z};
+        if (!sp.periodic) {
+            mn = pos - h;
+            mx = pos + h;
+        } else {
+            if (sp.hasShear) {
+                const D3 perp = h;
+                for (int ax = 0; ax < 3; ax++) {
+                    const int ax1 = (ax + 1) % 3, ax2 = (ax + 2) % 3;
+                    setComp(h, ax1, comp(h, ax1) + .5 * comp(perp, ax1) * (1 / sp.cellCos[ax] - 1));
+                    setComp(h, ax2, comp(h, ax2) + .5 * comp(perp, ax2) * (1 / sp.cellCos[ax] - 1));
+                }
+            }
+            DM3 U;
+            for (int k = 0; k < 9; k++) U.m[k] = sp.unshear[k];
+            const D3 u = mul(U, pos);
+            mn = u - h;
+            mx = u + h;
+        }
+        N.lastPos[p] = make_double4_32a(pr.x, pr.y, pr.z, 0.);
+    } else if (sh == WG_SHAPE_WALL) {
+        const int ax = P.aux[p].x;
+        const double4_32a pr = N.posr[p];
+        mn = D3{-inf, -inf, -inf};
+        mx = D3{inf, inf, inf};
+        setComp(mn, ax, comp(D3{pr.x, pr.y, pr.z}, ax));
+        setComp(mx, ax, comp(D3{pr.x, pr.y, pr.z}, ax));
+        N.lastPos[p] = make_double4_32a(pr.x, pr.y, pr.z, 0.);
+    } else {
+        const int4 fn = P.aux[p];
+        const double ht = P.facet[p].w;
+        const D3 htv{ht, ht, ht};
+        const int nn[3] = {fn.x, fn.y, fn.z};
+        for (int k = 0; k < 3; k++) {
+            const double4_32a pr = N.posr[nn[k]];
+            D3 v{pr.x, pr.y, pr.z};
+            if (sp.periodic) {
+                DM3 U;
+                for (int q = 0; q < 9; q++) U.m[q] = sp.unshear[q];
+                v = mul(U, v);
+            }
+            const D3 a = v - htv, b = v + htv;
+            if (k == 0) {
+                mn = a;
+                mx = b;
+            } else {
+                mn = D3{smin(mn.x, a.x), smin(mn.y, a.y), smin(mn.z, a.z)};
+                mx = D3{smax(mx.x, b.x), smax(mx.y, b.y), smax(mx.z, b.z)};
+            }
+            N.lastPos[nn[k]] = make_double4_32a(pr.x, pr.y, pr.z, 0.);
+        }
+        N.lastPos[p] = N.posr[p];
+    }
+    if (sp.verletDist > 0) {
+        const D3 vd{sp.verletDist, sp.verletDist, sp.verletDist};
+        mx = mx + vd;
+        mn = mn - vd;
+    }
+    // a NaN coordinate would silently drop the particle from every pair test: stop the run instead
+    if (isnan(mn.x) || isnan(mn.y) || isnan(mn.z) || isnan(mx.x) || isnan(mx.y) || isnan(mx.z)) atomicCAS(dErr, 0, 102);
+    P.mn[p] = make_double4_32a(mn.x, mn.y, mn.z, 0.);
+    P.mx[p] = make_double4_32a(mx.x, mx.y, mx.z, 0.);
+}
+
+// ---------------------------------------------------------------- grid bounds over spheres
+// partial[b] = {min mn.x, min mn.y, min mn.z, max mn.x, max mn.y, max mn.z, max extent}
+__global__ void k_grid_reduce(DevParticles P, const int32_t* __restrict__ ids, int n, double* __restrict__ partial) {
+    __shared__ double s[7][BS];
+    const double inf = __longlong_as_double(0x7ff0000000000000LL);
+    double v[7] = {inf, inf, inf, -inf, -inf, -inf, 0.};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int p = ids[i];
+        const double4_32a a = P.mn[p], b = P.mx[p];
+        v[0] = fmin(v[0], a.x); v[1] = fmin(v[1], a.y); v[2] = fmin(v[2], a.z);
+        v[3] = fmax(v[3], a.x); v[4] = fmax(v[4], a.y); v[5] = fmax(v[5], a.z);
+        v[6] = fmax(v[6], fmax(fmax(b.x - a.x, b.y - a.y), b.z - a.z));
+    }
+    for (int q = 0; q < 7; q++) s[q][threadIdx.x] = v[q];
+    __syncthreads();
+    for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+        if (threadIdx.x < st) {
+            for (int q = 0; q < 3; q++) s[q][threadIdx.x] = fmin(s[q][threadIdx.x], s[q][threadIdx.x + st]);
+            for (int q = 3; q < 7; q++) s[q][threadIdx.x] = fmax(s[q][threadIdx.x], s[q][threadIdx.x + st]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int q = 0; q < 7; q++) partial[blockIdx.x * 7 + q] = s[q][0];
+}
+
+__device__ __forceinline__ int cellCoord(double v, double o, double h, int n) {
+    double c = floor((v - o) / h);
+    int ci = (int)c;
+    return ci < 0 ? 0 : (ci >= n ? n - 1 : ci);
+}
+
+__global__ void k_cellkey(DevParticles P, const int32_t* __restrict__ ids, int n, Grid G, uint32_t* __restrict__ key,
+                          int32_t* __restrict__ val) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int p = ids[i];
+    const double4_32a a = P.mn[p];
+    const int cx = cellCoord(a.x, G.ox, G.h, G.nx), cy = cellCoord(a.y, G.oy, G.h, G.ny), cz = cellCoord(a.z, G.oz, G.h, G.nz);
+    key[i] = (uint32_t)(((int64_t)cz * G.ny + cy) * G.nx + cx);
+    val[i] = p;
+}
+
+__device__ __forceinline__ int64_t lowerBound32(const uint32_t* a, int64_t n, uint32_t k) {
+    int64_t lo = 0, hi = n;
+    while (lo < hi) {
+        int64_t m = (lo + hi) >> 1;
+        if (a[m] < k) lo = m + 1; else hi = m;
+    }
+    return lo;
+}
+__device__ __forceinline__ int64_t lowerBound64(const uint64_t* a, int64_t n, uint64_t k) {
+    int64_t lo = 0, hi = n;
+    while (lo < hi) {
+        int64_t m = (lo + hi) >> 1;
+        if (a[m] < k) lo = m + 1; else hi = m;
+    }
+    return lo;
+}
+
+// cellOff[k] = number of sorted spheres with cell key < k, k in [0, ncell]
+__global__ void k_cell_off(const uint32_t* __restrict__ skey, int n, int64_t ncell, int32_t* __restrict__ off) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k > ncell) return;
+    off[k] = (int32_t)lowerBound32(skey, n, (uint32_t)k);
+}
+
+__global__ void k_gather_sorted(DevParticles P, const int32_t* __restrict__ sid, int n, double4_32a* __restrict__ smn,
+                                double4_32a* __restrict__ smx, uint32_t* __restrict__ smask) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int p = sid[i];
+    smn[i] = P.mn[p];
+    smx[i] = P.mx[p];
+    smask[i] = P.mask[p];
+}
+
+// closed-interval 3-axis overlap, InsertionSortCollider::spatialOverlap :52-58
+__device__ __forceinline__ bool overlap3(const double4_32a& mn1, const double4_32a& mx1, const double4_32a& mn2, const double4_32a& mx2) {
+    return (mn1.x <= mx2.x) && (mx1.x >= mn2.x) && (mn1.y <= mx2.y) && (mx1.y >= mn2.y) && (mn1.z <= mx2.z) && (mx1.z >= mn2.z);
+}
+// Collider::mayCollide pkg/dem/Collision.cpp:19-41 for particles that share no nodes
+__device__ __forceinline__ bool maskOk(uint32_t a, uint32_t b, uint32_t lone) { return (a & b) != 0 && (a & b & lone) == 0; }
+
+__device__ __forceinline__ void emitPair(int a, int b, uint64_t* pairs, int64_t cap, unsigned long long* counter) {
+    const int lo = a < b ? a : b, hi = a < b ? b : a;
+    const unsigned long long idx = atomicAdd(counter, 1ull);
+    if ((int64_t)idx < cap) pairs[idx] = ((uint64_t)(uint32_t)lo << 32) | (uint32_t)hi;
+}
+
+// Half-shell sweep: particle i tests the rest of its own cell, the next cell in x, and the
+// three-cell x-runs of the rows (dy,dz) in {(1,0),(-1,1),(0,1),(1,1)}; each pair is met once.
+__global__ void k_pairs_ss(const int32_t* __restrict__ sid, const uint32_t* __restrict__ skey, const double4_32a* __restrict__ smn,
+                           const double4_32a* __restrict__ smx, const uint32_t* __restrict__ smask, int n, Grid G,
+                           const int32_t* __restrict__ off, uint32_t lone, uint64_t* __restrict__ pairs, int64_t cap,
+                           unsigned long long* __restrict__ counter) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t k = skey[i];
+    const int cx = (int)(k % (uint32_t)G.nx);
+    const int cy = (int)((k / (uint32_t)G.nx) % (uint32_t)G.ny);
+    const int cz = (int)(k / ((uint32_t)G.nx * (uint32_t)G.ny));
+    const double4_32a mn1 = smn[i], mx1 = smx[i];
+    const uint32_t m1 = smask[i];
+    const int pi = sid[i];
+    // own row: rest of own cell + cell cx+1
+    {
+        const int cx1 = cx + 1 < G.nx ? cx + 1 : cx;
+        const int64_t kEnd = ((int64_t)cz * G.ny + cy) * G.nx + cx1;
+        const int end = off[kEnd + 1];
+        for (int j = i + 1; j < end; j++) {
+            if (overlap3(mn1, mx1, smn[j], smx[j]) && maskOk(m1, smask[j], lone)) emitPair(pi, sid[j], pairs, cap, counter);
+        }
+    }
+    const int DY[4] = {1, -1, 0, 1}, DZ[4] = {0, 1, 1, 1};
+    for (int r = 0; r < 4; r++) {
+        const int y = cy + DY[r], z = cz + DZ[r];
+        if (y < 0 || y >= G.ny || z >= G.nz) continue;
+        const int x0 = cx > 0 ? cx - 1 : 0, x1 = cx + 1 < G.nx ? cx + 1 : cx;
+        const int64_t rowBase = ((int64_t)z * G.ny + y) * G.nx;
+        const int beg = off[rowBase + x0], end = off[rowBase + x1 + 1];
+        for (int j = beg; j < end; j++) {
+            if (overlap3(mn1, mx1, smn[j], smx[j]) && maskOk(m1, smask[j], lone)) emitPair(pi, sid[j], pairs, cap, counter);
+        }
+    }
+}
+
+// A facet (finite box) against the spheres of the cells its box can reach: a sphere j that
+// overlaps it has mn_j in [mn_f - h, mx_f] on every axis.
+__global__ void k_pairs_local(DevParticles P, const int32_t* __restrict__ lids, int nl, const int32_t* __restrict__ sid,
+                              const double4_32a* __restrict__ smn, const double4_32a* __restrict__ smx, const uint32_t* __restrict__ smask,
+                              Grid G, const int32_t* __restrict__ off, uint32_t lone, uint64_t* __restrict__ pairs, int64_t cap,
+                              unsigned long long* __restrict__ counter) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nl) return;
+    const int p = lids[t];
+    const double4_32a mn1 = P.mn[p], mx1 = P.mx[p];
+    const uint32_t m1 = P.mask[p];
+    const int x0 = cellCoord(mn1.x - G.h, G.ox, G.h, G.nx), x1 = cellCoord(mx1.x, G.ox, G.h, G.nx);
+    const int y0 = cellCoord(mn1.y - G.h, G.oy, G.h, G.ny), y1 = cellCoord(mx1.y, G.oy, G.h, G.ny);
+    const int z0 = cellCoord(mn1.z - G.h, G.oz, G.h, G.nz), z1 = cellCoord(mx1.z, G.oz, G.h, G.nz);
+    for (int z = z0; z <= z1; z++)
+        for (int y = y0; y <= y1; y++) {
+            const int64_t rowBase = ((int64_t)z * G.ny + y) * G.nx;
+            const int beg = off[rowBase + x0], end = off[rowBase + x1 + 1];
+            for (int j = beg; j < end; j++) {
+                if (sid[j] == p) continue;
+                if (overlap3(mn1, mx1, smn[j], smx[j]) && maskOk(m1, smask[j], lone)) emitPair(p, sid[j], pairs, cap, counter);
+            }
+        }
+}
+
+// Walls (and any box too large for the grid) against every sphere.
+__global__ void k_pairs_global(DevParticles P, const int32_t* __restrict__ gids, int ng, const int32_t* __restrict__ sph, int ns,
+                               uint32_t lone, uint64_t* __restrict__ pairs, int64_t cap, unsigned long long* __restrict__ counter) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ns) return;
+    const int s = sph[i];
+    const double4_32a mn1 = P.mn[s], mx1 = P.mx[s];
+    const uint32_t m1 = P.mask[s];
+    for (int g = 0; g < ng; g++) {
+        const int w = gids[g];
+        if (w == s) continue;
+        if (overlap3(mn1, mx1, P.mn[w], P.mx[w]) && maskOk(m1, P.mask[w], lone)) emitPair(s, w, pairs, cap, counter);
+    }
+}
+
+// Pairs among non-spheres (only launched when their masks allow contact at all).
+__global__ void k_pairs_large_large(DevParticles P, const int32_t* __restrict__ ids, int n, uint32_t lone,
+                                    uint64_t* __restrict__ pairs, int64_t cap, unsigned long long* __restrict__ counter) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)n * n) return;
+    const int a = (int)(t / n), b = (int)(t % n);
+    if (b <= a) return;
+    const int pa = ids[a], pb = ids[b];
+    // facets sharing a node may not collide (Collision.cpp:27-31)
+    if (P.shape[pa] == WG_SHAPE_FACET && P.shape[pb] == WG_SHAPE_FACET) {
+        const int4 x = P.aux[pa], y = P.aux[pb];
+        const int xa[3] = {x.x, x.y, x.z}, ya[3] = {y.x, y.y, y.z};
+        for (int u = 0; u < 3; u++)
+            for (int v = 0; v < 3; v++)
+                if (xa[u] == ya[v]) return;
+    }
+    if (overlap3(P.mn[pa], P.mx[pa], P.mn[pb], P.mx[pb]) && maskOk(P.mask[pa], P.mask[pb], lone)) emitPair(pa, pb, pairs, cap, counter);
+}
+
+// ---------------------------------------------------------------- merge with previous contacts
+__global__ void k_mark_orphans(DevContacts C, const uint64_t* __restrict__ nk, int64_t nn, int32_t* __restrict__ orph) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= C.n) return;
+    int32_t o = 0;
+    if (C.flags[j] & C_REAL) {
+        const uint64_t k = C.key[j];
+        const int64_t pos = lowerBound64(nk, nn, k);
+        o = (pos < nn && nk[pos] == k) ? 0 : 1;
+    }
+    orph[j] = o;
+}
+__global__ void k_compact_orphans(DevContacts C, const int32_t* __restrict__ orphFlag, const int32_t* __restrict__ orphScan,
+                                  uint64_t* __restrict__ okey, int32_t* __restrict__ osrc) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= C.n) return;
+    if (orphFlag[j]) {
+        const int32_t o = orphScan[j];
+        okey[o] = C.key[j];
+        osrc[o] = (int32_t)j;
+    }
+}
+__global__ void k_place_new(const uint64_t* __restrict__ nk, int64_t nn, const uint64_t* __restrict__ okey, int64_t no,
+                            const uint64_t* __restrict__ oldKey, int64_t nOld, uint64_t* __restrict__ outKey,
+                            int32_t* __restrict__ src) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nn) return;
+    const uint64_t k = nk[i];
+    const int64_t out = i + lowerBound64(okey, no, k);
+    const int64_t pos = lowerBound64(oldKey, nOld, k);
+    outKey[out] = k;
+    src[out] = (pos < nOld && oldKey[pos] == k) ? (int32_t)pos : -1;
+}
+__global__ void k_place_orph(const uint64_t* __restrict__ nk, int64_t nn, const uint64_t* __restrict__ okey,
+                             const int32_t* __restrict__ osrc, int64_t no, uint64_t* __restrict__ outKey, int32_t* __restrict__ src) {
+    const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= no) return;
+    const uint64_t k = okey[o];
+    const int64_t out = o + lowerBound64(nk, nn, k);
+    outKey[out] = k;
+    src[out] = osrc[o];
+}
+// carry persistent state of surviving contacts; new contacts get their functor type and orientation
+// (CGeomDispatcher functor order: Facet/Wall first, ContactLoop.cpp:145-152)
+__global__ void k_gather(DevContacts Cold, DevContacts Cnew, const int32_t* __restrict__ src, DevParticles P,
+                         const long long* __restrict__ dStep) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= Cnew.n) return;
+    const int32_t s = src[i];
+    if (s >= 0) {
+        Cnew.flags[i] = Cold.flags[s] & ~C_PENDING;
+        Cnew.step0[i] = Cold.step0[s];
+        Cnew.cdist[i] = Cold.cdist[s];
+#pragma unroll
+        for (int q = 0; q < CC_NCOL; q++) Cnew.col[q][i] = Cold.col[q][s];
+    } else {
+        const uint64_t k = Cnew.key[i];
+        const int lo = (int)(k >> 32), hi = (int)(k & 0xffffffffu);
+        const int tl = P.shape[lo], th = P.shape[hi];
+        uint32_t fl = 0, ty = CT_NONE;
+        const int a = (tl == WG_SHAPE_SPHERE) ? th : tl;
+        const bool sphLo = (tl == WG_SHAPE_SPHERE), sphHi = (th == WG_SHAPE_SPHERE);
+        if (sphLo && sphHi) ty = CT_SS;
+        else if (sphLo || sphHi) {
+            if (a == WG_SHAPE_FACET) ty = CT_FS;
+            else if (a == WG_SHAPE_WALL) ty = CT_WS;
+            if (sphLo) fl |= C_SWAP;  // the non-sphere (hi) becomes pA
+        }
+        fl |= ty << 2;
+        Cnew.flags[i] = fl;
+        Cnew.step0[i] = (int32_t)(*dStep);
+        Cnew.cdist[i] = packCellDist(0, 0, 0);
+#pragma unroll
+        for (int q = 0; q < CC_NCOL; q++) Cnew.col[q][i] = 0.;
+    }
+}
+
+// ---------------------------------------------------------------- CSR incidence
+__global__ void k_lo_start(const uint64_t* __restrict__ key, int64_t n, int nPar, int32_t* __restrict__ loStart) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p > nPar) return;
+    loStart[p] = (int32_t)lowerBound64(key, n, (uint64_t)(uint32_t)p << 32);
+}
+__global__ void k_hi_keys(const uint64_t* __restrict__ key, int64_t n, uint32_t* __restrict__ hk, int32_t* __restrict__ hv) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    hk[c] = (uint32_t)(key[c] & 0xffffffffu);
+    hv[c] = (int32_t)c;
+}
+__global__ void k_hi_start(const uint32_t* __restrict__ hks, int64_t n, int nPar, int32_t* __restrict__ hiStart) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p > nPar) return;
+    hiStart[p] = (int32_t)lowerBound32(hks, n, (uint32_t)p);
+}
+__global__ void k_heavy(DevIncidence I, DevParticles P, int threshold, int32_t* __restrict__ count) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P.n) return;
+    if (P.shape[p] == WG_SHAPE_FACET) return;
+    const int d = (I.hiStart[p + 1] - I.hiStart[p]) + (I.loStart[p + 1] - I.loStart[p]);
+    if (d > threshold) {
+        const int q = atomicAdd(count, 1);
+        I.heavy[q] = p;
+    }
+}
+
+// ---------------------------------------------------------------- host orchestration
+static int ensureCub(Sim& S, size_t bytes) {
+    CollideWork& W = *S.cw;
+    if (bytes <= W.cubBytes) return 0;
+    if (W.cubTmp) S.dfree(W.cubTmp);
+    W.cubBytes = bytes * 3 / 2 + 1024;
+    W.cubTmp = S.dalloc(W.cubBytes);
+    return W.cubTmp ? 0 : S.fail(WG_ERR_CUDA, "out of device memory (collider scratch)");
+}
+
+template <class T>
+static T* grow(Sim& S, T* p, int64_t& cap, int64_t need) {
+    if (need <= cap && p) return p;
+    if (p) S.dfree(p);
+    cap = std::max<int64_t>(need, cap * 3 / 2 + 1024);
+    return (T*)S.dalloc(sizeof(T) * cap);
+}
+
+static int buildLists(Sim& S) {
+    CollideWork& W = *S.cw;
+    std::vector<int32_t> sph, large, glob;
+    for (int64_t p = 0; p < S.nPar; p++) {
+        if (S.hShape[p] == WG_SHAPE_SPHERE) sph.push_back((int32_t)p);
+        else if (S.hShape[p] == WG_SHAPE_WALL) glob.push_back((int32_t)p);
+        else large.push_back((int32_t)p);
+    }
+    W.nSph = (int)sph.size();
+    W.hLarge = large;
+    W.hGlobal = glob;
+    W.sphereIds = (int32_t*)S.dalloc(sizeof(int32_t) * std::max<size_t>(1, sph.size()));
+    W.largeIds = (int32_t*)S.dalloc(sizeof(int32_t) * std::max<size_t>(1, large.size() + glob.size()));
+    W.globalIds = (int32_t*)S.dalloc(sizeof(int32_t) * std::max<size_t>(1, large.size() + glob.size()));
+    if (!W.sphereIds || !W.largeIds || !W.globalIds) return S.fail(WG_ERR_CUDA, "out of device memory");
+    WG_CUDA_TRY(cudaMemcpy(W.sphereIds, sph.data(), sizeof(int32_t) * sph.size(), cudaMemcpyHostToDevice));
+    // non-sphere pairs are possible only if some pair of them shares a mask bit outside loneMask
+    bool ll = false;
+    std::vector<int32_t> nonSph(large);
+    nonSph.insert(nonSph.end(), glob.begin(), glob.end());
+    {
+        uint32_t seen = 0;  // OR of masks
+        // exact test on distinct mask values
+        std::vector<uint32_t> masks;
+        for (int32_t p : nonSph) masks.push_back(S.hMask[p]);
+        std::sort(masks.begin(), masks.end());
+        masks.erase(std::unique(masks.begin(), masks.end()), masks.end());
+        for (size_t a = 0; a < masks.size() && !ll; a++)
+            for (size_t b = a; b < masks.size() && !ll; b++)
+                if ((masks[a] & masks[b]) != 0 && (masks[a] & masks[b] & S.cfg.lone_mask) == 0) ll = true;
+        (void)seen;
+    }
+    W.largeLargePossible = ll && nonSph.size() > 1;
+    return 0;
+}
+
+int collide_full_run(Sim& S) {
+    cudaStream_t st = S.stream;
+    if (!S.cw) {
+        S.cw = new CollideWork();
+        int r = buildLists(S);
+        if (r) return r;
+    }
+    CollideWork& W = *S.cw;
+    const uint32_t lone = S.cfg.lone_mask;
+    // 1. boxes
+    if (S.nPar > 0) k_aabb<<<(unsigned)((S.nPar + BS - 1) / BS), BS, 0, st>>>(S.N, S.P, S.dPar, S.dFlags + 1);
+    // lastPos for node slots not owned by a particle box computation (dummy slots) stays stale:
+    // they never move (blocked, zero velocity) and are never tested against a stale reference.
+    // 2. grid over spheres
+    Grid G{0, 0, 0, 1, 1, 1, 1, 1};
+    const int ns = W.nSph;
+    if (ns > 0) {
+        const int nb = std::min(1024, (ns + BS - 1) / BS);
+        if (!W.red) {
+            W.red = (double*)S.dalloc(sizeof(double) * 7 * 1024);
+            WG_CUDA_TRY(cudaMallocHost(&W.hRed, sizeof(double) * 7 * 1024));
+        }
+        k_grid_reduce<<<nb, BS, 0, st>>>(S.P, W.sphereIds, ns, W.red);
+        WG_CUDA_TRY(cudaMemcpyAsync(W.hRed, W.red, sizeof(double) * 7 * nb, cudaMemcpyDeviceToHost, st));
+        WG_CUDA_TRY(cudaStreamSynchronize(st));
+        double v[7] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY, 0.};
+        for (int b = 0; b < nb; b++) {
+            for (int q = 0; q < 3; q++) v[q] = std::min(v[q], W.hRed[7 * b + q]);
+            for (int q = 3; q < 7; q++) v[q] = std::max(v[q], W.hRed[7 * b + q]);
+        }
+        if (!(std::isfinite(v[0]) && std::isfinite(v[3]) && std::isfinite(v[6])))
+            return S.fail(WG_ERR_NAN, "InsertionSortCollider: non-finite sphere bounding box (NaN or infinite position)");
+        // cell edge slightly above the largest sphere box, so boxes that overlap sit in adjacent cells
+        double h = v[6] * (1 + 1e-9) + 1e-300;
+        double ext[3] = {v[3] - v[0], v[4] - v[1], v[5] - v[2]};
+        int64_t dims[3];
+        for (;;) {
+            for (int q = 0; q < 3; q++) dims[q] = (int64_t)std::floor(ext[q] / h) + 1;
+            int64_t nc = dims[0] * dims[1] * dims[2];
+            if (nc <= std::max<int64_t>(8 * (int64_t)ns, 1 << 16) && nc < (int64_t(1) << 31)) break;
+            h *= 1.25;
+        }
+        G.ox = v[0]; G.oy = v[1]; G.oz = v[2]; G.h = h;
+        G.nx = (int32_t)dims[0]; G.ny = (int32_t)dims[1]; G.nz = (int32_t)dims[2];
+        G.ncell = dims[0] * dims[1] * dims[2];
+        // sort spheres by cell
+        if (!W.cellKey) {
+            W.cellKey = (uint32_t*)S.dalloc(sizeof(uint32_t) * ns);
+            W.cellKeySorted = (uint32_t*)S.dalloc(sizeof(uint32_t) * ns);
+            W.cellVal = (int32_t*)S.dalloc(sizeof(int32_t) * ns);
+            W.sid = (int32_t*)S.dalloc(sizeof(int32_t) * ns);
+            W.smn = (double4_32a*)S.dalloc(sizeof(double4_32a) * ns);
+            W.smx = (double4_32a*)S.dalloc(sizeof(double4_32a) * ns);
+            W.smask = (uint32_t*)S.dalloc(sizeof(uint32_t) * ns);
+            if (!W.smask) return S.fail(WG_ERR_CUDA, "out of device memory (grid)");
+        }
+        W.cellOff = grow(S, W.cellOff, W.cellOffCap, G.ncell + 1);
+        k_cellkey<<<(ns + BS - 1) / BS, BS, 0, st>>>(S.P, W.sphereIds, ns, G, W.cellKey, W.cellVal);
+        int endBit = 1;
+        while ((int64_t(1) << endBit) < G.ncell) endBit++;
+        size_t tb = 0;
+        cub::DeviceRadixSort::SortPairs(nullptr, tb, W.cellKey, W.cellKeySorted, W.cellVal, W.sid, ns, 0, endBit, st);
+        if (ensureCub(S, tb)) return WG_ERR_CUDA;
+        tb = W.cubBytes;
+        WG_CUDA_TRY(cub::DeviceRadixSort::SortPairs(W.cubTmp, tb, W.cellKey, W.cellKeySorted, W.cellVal, W.sid, ns, 0, endBit, st));
+        k_cell_off<<<(unsigned)((G.ncell + 1 + BS - 1) / BS), BS, 0, st>>>(W.cellKeySorted, ns, G.ncell, W.cellOff);
+        k_gather_sorted<<<(ns + BS - 1) / BS, BS, 0, st>>>(S.P, W.sid, ns, W.smn, W.smx, W.smask);
+    }
+    // lists of large particles: facets with boxes spanning a few cells use the grid, the rest are global
+    {
+        // decide on the host from the facet sizes measured at the previous full run would need a copy;
+        // facet boxes are static in the supported scenes, so classify them once by size here
+        if (W.nLarge == 0 && W.nGlobal == 0 && (!W.hLarge.empty() || !W.hGlobal.empty())) {
+            std::vector<double4_32a> mn(S.nPar), mx(S.nPar);
+            WG_CUDA_TRY(cudaMemcpyAsync(mn.data(), S.P.mn, sizeof(double4_32a) * S.nPar, cudaMemcpyDeviceToHost, st));
+            WG_CUDA_TRY(cudaMemcpyAsync(mx.data(), S.P.mx, sizeof(double4_32a) * S.nPar, cudaMemcpyDeviceToHost, st));
+            WG_CUDA_TRY(cudaStreamSynchronize(st));
+            std::vector<int32_t> loc, glo = W.hGlobal;
+            for (int32_t p : W.hLarge) {
+                double e = std::max({mx[p].x - mn[p].x, mx[p].y - mn[p].y, mx[p].z - mn[p].z});
+                if (ns > 0 && std::isfinite(e) && e <= 8 * G.h) loc.push_back(p);
+                else glo.push_back(p);
+            }
+            W.nLarge = (int)loc.size();
+            W.nGlobal = (int)glo.size();
+            if (W.nLarge) WG_CUDA_TRY(cudaMemcpy(W.largeIds, loc.data(), sizeof(int32_t) * loc.size(), cudaMemcpyHostToDevice));
+            if (W.nGlobal) WG_CUDA_TRY(cudaMemcpy(W.globalIds, glo.data(), sizeof(int32_t) * glo.size(), cudaMemcpyHostToDevice));
+        }
+    }
+    // 3-4. pair generation with a capacity retry
+    if (!W.counter) {
+        W.counter = (unsigned long long*)S.dalloc(sizeof(unsigned long long) * 2);
+        WG_CUDA_TRY(cudaMallocHost(&W.hCounter, sizeof(unsigned long long) * 2));
+    }
+    if (W.pairCap == 0) {
+        int64_t c0 = std::max<int64_t>(1 << 16, 8 * S.nPar);
+        W.pairs = grow(S, W.pairs, W.pairCap, c0);
+        int64_t cap2 = 0;
+        W.pairsSorted = grow(S, W.pairsSorted, cap2, W.pairCap);
+    }
+    int64_t nNew = 0;
+    for (int attempt = 0; attempt < 3; attempt++) {
+        WG_CUDA_TRY(cudaMemsetAsync(W.counter, 0, sizeof(unsigned long long), st));
+        if (ns > 0) {
+            k_pairs_ss<<<(ns + BS - 1) / BS, BS, 0, st>>>(W.sid, W.cellKeySorted, W.smn, W.smx, W.smask, ns, G, W.cellOff, lone,
+                                                        W.pairs, W.pairCap, W.counter);
+            if (W.nLarge > 0)
+                k_pairs_local<<<(W.nLarge + 63) / 64, 64, 0, st>>>(S.P, W.largeIds, W.nLarge, W.sid, W.smn, W.smx, W.smask, G,
+                                                                W.cellOff, lone, W.pairs, W.pairCap, W.counter);
+            if (W.nGlobal > 0)
+                k_pairs_global<<<(ns + BS - 1) / BS, BS, 0, st>>>(S.P, W.globalIds, W.nGlobal, W.sphereIds, ns, lone, W.pairs,
+                                                                W.pairCap, W.counter);
+        }
+        if (W.largeLargePossible) {
+            // all non-spheres against each other
+            int nn = W.nLarge + W.nGlobal;
+            std::vector<int32_t> all;
+            (void)all;
+            int32_t* ids = W.globalIds;
+            if (W.nLarge > 0) {
+                // concatenate: globalIds has room for every non-sphere
+                WG_CUDA_TRY(cudaMemcpyAsync(W.globalIds + W.nGlobal, W.largeIds, sizeof(int32_t) * W.nLarge, cudaMemcpyDeviceToDevice, st));
+            }
+            int64_t tot = (int64_t)nn * nn;
+            k_pairs_large_large<<<(unsigned)((tot + BS - 1) / BS), BS, 0, st>>>(S.P, ids, nn, lone, W.pairs, W.pairCap, W.counter);
+        }
+        WG_CUDA_TRY(cudaMemcpyAsync(W.hCounter, W.counter, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+        WG_CUDA_TRY(cudaStreamSynchronize(st));
+        nNew = (int64_t)W.hCounter[0];
+        if (nNew <= W.pairCap) break;
+        int64_t cap2 = W.pairCap;
+        W.pairs = grow(S, W.pairs, W.pairCap, nNew + nNew / 4);
+        W.pairsSorted = grow(S, W.pairsSorted, cap2, W.pairCap);
+        if (!W.pairs || !W.pairsSorted) return S.fail(WG_ERR_CUDA, "out of device memory (pairs)");
+    }
+    // sort new pair keys
+    int idBits = 1;
+    while ((int64_t(1) << idBits) < S.nPar) idBits++;
+    if (nNew > 0) {
+        size_t tb = 0;
+        cub::DeviceRadixSort::SortKeys(nullptr, tb, W.pairs, W.pairsSorted, nNew, 0, 32 + idBits, st);
+        if (ensureCub(S, tb)) return WG_ERR_CUDA;
+        tb = W.cubBytes;
+        WG_CUDA_TRY(cub::DeviceRadixSort::SortKeys(W.cubTmp, tb, W.pairs, W.pairsSorted, nNew, 0, 32 + idBits, st));
+    }
+    // 5. merge with the previous contact set
+    const int64_t nOld = S.C.n;
+    W.orph = grow(S, W.orph, W.mergeCap, std::max<int64_t>(nOld, 1) * 2 + 2);
+    int64_t capTmp = 0;
+    if (!W.orphKey || W.mergeCap > 0) {
+        // orphKey/orphSrc sized like orph
+        static int64_t dummy;
+        (void)dummy;
+    }
+    int64_t nOrph = 0;
+    if (nOld > 0) {
+        int32_t* flagsArr = W.orph;
+        int32_t* scanArr = W.orph + (std::max<int64_t>(nOld, 1) + 1);
+        k_mark_orphans<<<(unsigned)((nOld + BS - 1) / BS), BS, 0, st>>>(S.C, W.pairsSorted, nNew, flagsArr);
+        size_t tb = 0;
+        cub::DeviceScan::ExclusiveSum(nullptr, tb, flagsArr, scanArr, (int)nOld, st);
+        if (ensureCub(S, tb)) return WG_ERR_CUDA;
+        tb = W.cubBytes;
+        WG_CUDA_TRY(cub::DeviceScan::ExclusiveSum(W.cubTmp, tb, flagsArr, scanArr, (int)nOld, st));
+        int32_t last[2];
+        WG_CUDA_TRY(cudaMemcpyAsync(&last[0], flagsArr + nOld - 1, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+        WG_CUDA_TRY(cudaMemcpyAsync(&last[1], scanArr + nOld - 1, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+        WG_CUDA_TRY(cudaStreamSynchronize(st));
+        nOrph = (int64_t)last[0] + last[1];
+        if (nOrph > 0) {
+            int64_t c1 = 0, c2 = 0;
+            if (W.orphKey) S.dfree(W.orphKey);
+            if (W.orphSrc) S.dfree(W.orphSrc);
+            W.orphKey = grow(S, (uint64_t*)nullptr, c1, nOrph);
+            W.orphSrc = grow(S, (int32_t*)nullptr, c2, nOrph);
+            k_compact_orphans<<<(unsigned)((nOld + BS - 1) / BS), BS, 0, st>>>(S.C, flagsArr, scanArr, W.orphKey, W.orphSrc);
+        }
+    }
+    (void)capTmp;
+    const int64_t nOut = nNew + nOrph;
+    int r = S.ensureContactCapacity(nOut);
+    if (r) return r;
+    int64_t srcCap = 0;
+    if (W.src) S.dfree(W.src);
+    W.src = grow(S, (int32_t*)nullptr, srcCap, std::max<int64_t>(nOut, 1));
+    S.Cb.n = nOut;
+    if (nNew > 0)
+        k_place_new<<<(unsigned)((nNew + BS - 1) / BS), BS, 0, st>>>(W.pairsSorted, nNew, W.orphKey, nOrph, S.C.key, nOld, S.Cb.key,
+                                                                    W.src);
+    if (nOrph > 0)
+        k_place_orph<<<(unsigned)((nOrph + BS - 1) / BS), BS, 0, st>>>(W.pairsSorted, nNew, W.orphKey, W.orphSrc, nOrph, S.Cb.key,
+                                                                      W.src);
+    if (nOut > 0) k_gather<<<(unsigned)((nOut + BS - 1) / BS), BS, 0, st>>>(S.C, S.Cb, W.src, S.P, S.dStep);
+    std::swap(S.C, S.Cb);
+    // 6. CSR incidence
+    const int64_t n = S.C.n;
+    k_lo_start<<<(unsigned)((S.nPar + 1 + BS - 1) / BS), BS, 0, st>>>(S.C.key, n, (int)S.nPar, S.I.loStart);
+    if (W.hiCap < std::max<int64_t>(n, 1)) {
+        if (W.hiKeys) { S.dfree(W.hiKeys); S.dfree(W.hiKeysSorted); S.dfree(W.hiVals); S.dfree(S.I.hiList); }
+        W.hiCap = std::max<int64_t>(n, 1) * 3 / 2 + 1024;
+        W.hiKeys = (uint32_t*)S.dalloc(sizeof(uint32_t) * W.hiCap);
+        W.hiKeysSorted = (uint32_t*)S.dalloc(sizeof(uint32_t) * W.hiCap);
+        W.hiVals = (int32_t*)S.dalloc(sizeof(int32_t) * W.hiCap);
+        S.I.hiList = (int32_t*)S.dalloc(sizeof(int32_t) * W.hiCap);
+        if (!S.I.hiList) return S.fail(WG_ERR_CUDA, "out of device memory (incidence)");
+    }
+    if (n > 0) {
+        k_hi_keys<<<(unsigned)((n + BS - 1) / BS), BS, 0, st>>>(S.C.key, n, W.hiKeys, W.hiVals);
+        size_t tb = 0;
+        cub::DeviceRadixSort::SortPairs(nullptr, tb, W.hiKeys, W.hiKeysSorted, W.hiVals, S.I.hiList, n, 0, idBits, st);
+        if (ensureCub(S, tb)) return WG_ERR_CUDA;
+        tb = W.cubBytes;
+        WG_CUDA_TRY(cub::DeviceRadixSort::SortPairs(W.cubTmp, tb, W.hiKeys, W.hiKeysSorted, W.hiVals, S.I.hiList, n, 0, idBits, st));
+    }
+    k_hi_start<<<(unsigned)((S.nPar + 1 + BS - 1) / BS), BS, 0, st>>>(W.hiKeysSorted, n, (int)S.nPar, S.I.hiStart);
+    // heavy particles
+    if (!W.heavyCount) {
+        W.heavyCount = (int32_t*)S.dalloc(sizeof(int32_t));
+        WG_CUDA_TRY(cudaMallocHost(&W.hHeavy, sizeof(int32_t)));
+    }
+    WG_CUDA_TRY(cudaMemsetAsync(W.heavyCount, 0, sizeof(int32_t), st));
+    k_heavy<<<(unsigned)((S.nPar + BS - 1) / BS), BS, 0, st>>>(S.I, S.P, 64, W.heavyCount);
+    WG_CUDA_TRY(cudaMemcpyAsync(W.hHeavy, W.heavyCount, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    WG_CUDA_TRY(cudaStreamSynchronize(st));
+    S.I.nHeavy = S.cfg.apply_forces ? *W.hHeavy : 0;
+    WG_CUDA_TRY(cudaGetLastError());
+    S.nFullRuns++;
+    return 0;
+}
+
+void collide_free(Sim& S) {
+    if (!S.cw) return;
+    if (S.cw->hRed) cudaFreeHost(S.cw->hRed);
+    if (S.cw->hCounter) cudaFreeHost(S.cw->hCounter);
+    if (S.cw->hHeavy) cudaFreeHost(S.cw->hHeavy);
+    delete S.cw;
+    S.cw = nullptr;
+}
+
+}  // namespace wg

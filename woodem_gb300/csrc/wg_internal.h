@@ -1,0 +1,189 @@
+// Internal declarations of the GB300 DEM hot path: device data layout, kernel
+// launchers and the host-side simulation object behind the C ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "../../include/woo_gpu.h"
+
+namespace wg {
+
+// DemData flag bits (pkg/dem/Particle.hpp:179-186)
+enum : uint32_t {
+    F_DOF_ALL = 63u, F_DOF_RXRYRZ = 56u, F_CLUMPED = 64u, F_CLUMP = 128u, F_GRAVITY_SKIP = 512u, F_DAMPING_SKIP = 2048u
+};
+// contact flag bits
+enum : uint32_t {
+    C_REAL = 1u,     // geom && phys exist
+    C_SWAP = 2u,     // pA is the hi id (functor order Facet/Wall first)
+    C_PENDING = 16u  // law requested removal in the last ContactLoop
+};
+enum { CT_SS = 0, CT_FS = 1, CT_WS = 2, CT_NONE = 3 };
+__host__ __device__ inline uint32_t ctype(uint32_t fl) { return (fl >> 2) & 3u; }
+
+// Per-scene constants read by the kernels (one entry per scene in the batch).
+struct ScenePar {
+    double dt;
+    double g[3];
+    double damping;
+    double verletDist;
+    double maxD2;
+    double ssDistFactor;
+    double bo1DistFactor;
+    double hzViscConst;   // -sqrt(5)*log(en)/sqrt(log(en)^2+pi^2), Hertz.cpp:43
+    double hzGamma;
+    double hzPoisson;
+    int32_t law, phys, reset, applyForces;
+    int32_t trsfRenorm, approxMask, noRatch, noSlip, noBreak, noFrict, noAttraction, hzViscOn;
+    int32_t periodic, homoDeform, hasGravity, evalStress;
+    uint32_t loneMask;
+    int32_t _pad;
+    // periodic cell, integrated on the host each step (core/Cell.cpp:81-120)
+    double hSize[9], pprevHsize[9], gradV[9], nextGradV[9], dGradV[9], midGradV[9], shiftVelMat[9];
+    double ImLL4hInv[9], IpLL4h[9], LmL[9], unshear[9];
+    double deltaSpinVec[3], spinVec[3], cellSize[3], cellCos[3];
+    int32_t hasShear, _pad2;
+};
+
+// Node-slot arrays (uninodal particle p owns slot p; facet vertices follow the particles).
+struct DevNodes {
+    int32_t n;
+    double4_32a* posr;    // x y z radius
+    double4_32a* vel;     // vx vy vz 0
+    double4_32a* angv;    // wx wy wz 0
+    double4_32a* ori;     // w x y z
+    double4_32a* force;   // fx fy fz 0
+    double4_32a* torque;  // tx ty tz 0
+    double4_32a* minert;  // ix iy iz mass
+    double4_32a* lastPos; // verlet reference position
+    uint32_t* flags;
+};
+struct DevParticles {
+    int32_t n;
+    int32_t* shape;   // WG_SHAPE_*
+    int4* aux;        // facet: node slots n0 n1 n2; wall: axis sense
+    double4_32a* facet;   // fakeVel xyz, halfThick
+    int32_t* mat;
+    uint32_t* mask;
+    double4_32a* mn;      // Aabb.min (verletDist included)
+    double4_32a* mx;      // Aabb.max
+};
+enum {
+    CC_T0X, CC_T0Y, CC_T0Z, CC_T1X, CC_T1Y, CC_T1Z,  // L6Geom.trsf columns 0 and 1 (column 2 = c0 x c1)
+    CC_CPX, CC_CPY, CC_CPZ,                          // L6Geom node position (contact point)
+    CC_P0, CC_P1, CC_P2, CC_P3, CC_P4,               // FrictPhys kn kt tanPhi | HertzPhys kn0 kt0 tanPhi alpha_sqrtMK R
+    CC_FN, CC_FT1, CC_FT2,                           // phys.force (local)
+    CC_FGX, CC_FGY, CC_FGZ,                          // force on pA in global coordinates
+    CC_NCOL
+};
+struct DevContacts {
+    int64_t n;
+    uint64_t* key;    // (lo<<32)|hi, sorted ascending
+    uint32_t* flags;
+    int32_t* step0;   // Contact.stepCreated
+    int32_t* cdist;   // Contact.cellDist for (lo,hi), packed 3x10 bits
+    double* col[CC_NCOL];
+};
+// CSR incidence for the deterministic per-particle force sum
+struct DevIncidence {
+    int32_t* loStart;  // nPar+1: contacts with lo==p are [loStart[p], loStart[p+1])
+    int32_t* hiStart;  // nPar+1: hiList[hiStart[p] .. hiStart[p+1]) are contacts with hi==p, ascending
+    int32_t* hiList;
+    int32_t* heavy;    // particles whose degree exceeds the serial threshold
+    int32_t nHeavy;
+};
+
+__host__ __device__ inline int32_t packCellDist(int a, int b, int c) {
+    return (int32_t)(((uint32_t)(a + 512) & 1023u) | (((uint32_t)(b + 512) & 1023u) << 10) | (((uint32_t)(c + 512) & 1023u) << 20));
+}
+__host__ __device__ inline void unpackCellDist(int32_t p, int& a, int& b, int& c) {
+    a = (int)(p & 1023) - 512;
+    b = (int)((p >> 10) & 1023) - 512;
+    c = (int)((p >> 20) & 1023) - 512;
+}
+
+// ------------------------------------------------------------------ launchers (wg_step.cu)
+void launch_leapfrog(cudaStream_t st, const DevNodes& N, const DevParticles& P, const ScenePar* sp, int* dFull);
+void launch_contact_fp64(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C,
+                         const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dErr);
+void launch_reduce(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C,
+                   const DevIncidence& I, const ScenePar* sp, long long* dStep);
+
+// ------------------------------------------------------------------ broad phase (wg_collide.cu)
+struct Grid {
+    double ox, oy, oz, h;
+    int32_t nx, ny, nz;
+    int64_t ncell;
+};
+struct CollideWork;  // scratch owned by the simulation
+struct Sim;
+int collide_full_run(Sim& S);
+
+// ------------------------------------------------------------------ host simulation object
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+struct Sim {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    wg_config cfg{};
+    bool haveCfg = false;
+    // host copies of the description
+    std::vector<double> hDensity, hYoung, hTanPhi, hKtDivKn;
+    int64_t nApiNodes = 0, nPar = 0;
+    std::vector<int32_t> apiNodeToSlot;  // api node index -> slot
+    std::vector<double> hApi;            // 19 doubles per api node: pos ori vel angVel force torque
+    std::vector<double> hMass, hInertia;
+    std::vector<uint32_t> hFlagsApi;
+    std::vector<int32_t> hShape;
+    std::vector<int32_t> hNodes3;
+    std::vector<double> hRadius, hHalfThick, hFakeVel;
+    std::vector<int32_t> hAxis, hSense, hMat;
+    std::vector<uint32_t> hMask;
+    int nSpheres = 0;
+    // device state
+    DevNodes N{};
+    DevParticles P{};
+    DevContacts C{}, Cb{};  // current and spare (merge target)
+    DevIncidence I{};
+    int64_t cCap = 0;
+    double4_32a* dMats = nullptr;
+    ScenePar hPar{};
+    ScenePar* dPar = nullptr;
+    long long* dStep = nullptr;
+    int* dFlags = nullptr;   // [0] full run requested, [1] error code
+    int* hFlags = nullptr;   // pinned mirror
+    std::vector<void*> allocs;
+    CollideWork* cw = nullptr;
+    bool uploaded = false, initialized = false;
+    int64_t step = 0;
+    double time = 0;
+    int64_t nFullRuns = 0;
+    // timing
+    cudaEvent_t ev[8];
+    double lastTotalMs = 0, phaseMs[4] = {0, 0, 0, 0};
+    int64_t lastLaunches = 0;
+
+    ~Sim();
+    void* dalloc(size_t bytes);
+    void dfree(void* p);
+    int fail(int code, const std::string& m) { err = m; return code; }
+    int upload();
+    int prepareParams();
+    int run(int64_t n);
+    int checkErr();
+    int ensureContactCapacity(int64_t need);
+};
+
+#define WG_CUDA_TRY(expr)                                                                  \
+    do {                                                                                   \
+        cudaError_t _e = (expr);                                                           \
+        if (_e != cudaSuccess) return S.fail(WG_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(_e)); \
+    } while (0)
+
+}  // namespace wg

@@ -1,0 +1,596 @@
+// Per-step kernels of the FP64 path: Leapfrog, the fused ContactLoop functors and the
+// deterministic per-particle force/torque sum.
+//
+// Compiled with --fmad=false: every floating-point result is the correctly rounded
+// value of the operation sequence written here, which is the operation sequence of
+// the reference expression cited beside it.
+#include "wg_internal.h"
+#include "wg_math.cuh"
+
+namespace wg {
+
+__device__ __forceinline__ D3 ld3(const double4_32a& v) { return D3{v.x, v.y, v.z}; }
+__device__ __forceinline__ double4_32a st4(D3 a, double w) { return make_double4_32a(a.x, a.y, a.z, w); }
+__device__ __forceinline__ DM3 ldm(const double* m) {
+    DM3 r;
+#pragma unroll
+    for (int i = 0; i < 9; i++) r.m[i] = m[i];
+    return r;
+}
+__device__ __forceinline__ double sgn(double s) { return s < 0 ? -1 : (s > 0 ? 1 : 0); }
+
+// ---------------------------------------------------------------------------------- Leapfrog
+// Leapfrog::run pkg/dem/Leapfrog.cpp:103-255 (spherical integrator; clumps and impose are
+// outside the path), nonviscDamp2nd :32-34, computeAccel/AngAccel :36-47,
+// applyPeriodicCorrections :258-272, leapfrogTranslate :275-278, leapfrogSphericalRotate :280-288,
+// and the verlet-distance test of InsertionSortCollider::updateBboxes_doFullRun
+// pkg/dem/InsertionSortCollider.cpp:339-350 on the new positions.
+__global__ void k_leapfrog(DevNodes N, const int32_t* __restrict__ pshape, int nPar, const ScenePar* __restrict__ spp,
+                           int* __restrict__ dFull) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N.n) return;
+    const ScenePar& sp = *spp;
+    const uint32_t flags = N.flags[i];
+    if (flags & F_CLUMPED) return;
+    const double dt = sp.dt;
+    const double damping = sp.damping;
+    const bool damp = (damping != 0. && !(flags & F_DAMPING_SKIP));
+    const double4_32a pr = N.posr[i];
+    D3 pos = ld3(pr);
+    D3 vel = ld3(N.vel[i]);
+    D3 angVel = ld3(N.angv[i]);
+    const double4_32a mi = N.minert[i];
+    const D3 inertia{mi.x, mi.y, mi.z};
+    const double mass = mi.w;
+    const D3 f = ld3(N.force[i]);
+    const D3 t = ld3(N.torque[i]);
+    const bool blockedAll = (flags & F_DOF_ALL) == F_DOF_ALL;
+    const int homoDeform = sp.periodic ? sp.homoDeform : -1;
+    D3 linAccel{0, 0, 0};
+    if (!blockedAll) {
+        if ((flags & F_DOF_ALL) == 0) linAccel = f / mass;
+        else {
+            if (!(flags & 1u)) linAccel.x = 0. + f.x / mass;
+            if (!(flags & 2u)) linAccel.y = 0. + f.y / mass;
+            if (!(flags & 4u)) linAccel.z = 0. + f.z / mass;
+        }
+        D3 pvf = vel, pva = angVel;
+        if (sp.periodic) {
+            // Cell::pprevFluctVel / pprevFluctAngVel, core/Cell.cpp:36-57
+            if (homoDeform == 2 || homoDeform == 3) pvf = vel - mul(ldm(sp.gradV), pos);
+            else if (homoDeform == 4) pvf = vel - mul(ldm(sp.gradV), pos - (dt / 2) * vel);
+            if (homoDeform == 4) pva = angVel - D3{sp.spinVec[0], sp.spinVec[1], sp.spinVec[2]};
+        }
+        if (damp) {
+            linAccel.x = linAccel.x * (1 - damping * sgn(f.x * (pvf.x + (0.5 * dt) * linAccel.x)));
+            linAccel.y = linAccel.y * (1 - damping * sgn(f.y * (pvf.y + (0.5 * dt) * linAccel.y)));
+            linAccel.z = linAccel.z * (1 - damping * sgn(f.z * (pvf.z + (0.5 * dt) * linAccel.z)));
+        }
+        if (homoDeform == 4)
+            vel = mul(ldm(sp.ImLL4hInv), (mul(ldm(sp.LmL), pos) + mul(ldm(sp.IpLL4h), vel)) + linAccel * dt);
+        else
+            vel = vel + dt * linAccel;
+        if (!isZero(inertia)) {
+            D3 angAccel{0, 0, 0};
+            if ((flags & F_DOF_ALL) == 0) angAccel = D3{t.x / inertia.x, t.y / inertia.y, t.z / inertia.z};
+            else {
+                if (!(flags & 8u)) angAccel.x = 0. + t.x / inertia.x;
+                if (!(flags & 16u)) angAccel.y = 0. + t.y / inertia.y;
+                if (!(flags & 32u)) angAccel.z = 0. + t.z / inertia.z;
+            }
+            if (damp) {
+                angAccel.x = angAccel.x * (1 - damping * sgn(t.x * (pva.x + (0.5 * dt) * angAccel.x)));
+                angAccel.y = angAccel.y * (1 - damping * sgn(t.y * (pva.y + (0.5 * dt) * angAccel.y)));
+                angAccel.z = angAccel.z * (1 - damping * sgn(t.z * (pva.z + (0.5 * dt) * angAccel.z)));
+            }
+            angVel = angVel + dt * angAccel;
+            if (homoDeform == 4) angVel = angVel - D3{sp.deltaSpinVec[0], sp.deltaSpinVec[1], sp.deltaSpinVec[2]};
+        }
+    } else {
+        if (homoDeform == 4) vel = mul(ldm(sp.ImLL4hInv), mul(ldm(sp.LmL), pos) + mul(ldm(sp.IpLL4h), vel));
+    }
+    if (homoDeform >= 0 && homoDeform != 4) {
+        if (homoDeform == 2 || homoDeform == 3) {
+            if (homoDeform == 3) vel = vel + mul(ldm(sp.midGradV), vel - (dt / 2.) * linAccel) * dt;
+            vel = vel + mul(ldm(sp.dGradV), pos);
+        } else if (homoDeform == 1) {
+            pos = pos + mul(ldm(sp.nextGradV), pos) * dt;
+        }
+    }
+    pos = pos + vel * dt;
+    const double4_32a o4 = N.ori[i];
+    DQ ori{o4.x, o4.y, o4.z, o4.w};
+    if (!isZero(angVel)) {
+        const double angle = sqrt(sqn(angVel));
+        const D3 axis = angVel / angle;
+        const double ha = 0.5 * (angle * dt);
+        double s, c;
+        sincos(ha, &s, &c);
+        const DQ q{c, s * axis.x, s * axis.y, s * axis.z};
+        ori = qmul(q, ori);
+    }
+    ori = qnormalized(ori);
+    N.posr[i] = st4(pos, pr.w);
+    N.vel[i] = st4(vel, 0.);
+    N.angv[i] = st4(angVel, 0.);
+    N.ori[i] = make_double4_32a(ori.w, ori.x, ori.y, ori.z);
+    // Leapfrog(reset=True) for nodes whose force is not rebuilt by the contact sum
+    // (facet vertices): force = mass*gravity, torque = 0 (Leapfrog.cpp:240-245)
+    if (sp.reset && (i >= nPar || pshape[i] == WG_SHAPE_FACET)) {
+        D3 G{0, 0, 0};
+        if (sp.hasGravity && !(flags & F_GRAVITY_SKIP)) G = mass * D3{sp.g[0], sp.g[1], sp.g[2]};
+        N.force[i] = st4(G, 0.);
+        N.torque[i] = make_double4_32a(0., 0., 0., 0.);
+    }
+    // verlet test (d2 + moveDueToRot2 > maxD2 with no rotation term for spheres, walls, facets)
+    const D3 lp = ld3(N.lastPos[i]);
+    const double d2 = sqn(lp - pos);
+    if (d2 + 0. > sp.maxD2) atomicOr(dFull, 1);
+}
+
+void launch_leapfrog(cudaStream_t st, const DevNodes& N, const DevParticles& P, const ScenePar* sp, int* dFull) {
+    if (N.n == 0) return;
+    k_leapfrog<<<(N.n + 255) / 256, 256, 0, st>>>(N, P.shape, P.n, sp, dFull);
+}
+
+// ---------------------------------------------------------------------------------- ContactLoop
+struct Geo {
+    D3 pos1, vel1, angVel1, pos2, vel2, angVel2, normal, contPt;
+    double uN, r1, r2;
+};
+
+// Cg2_Sphere_Sphere_L6Geom::go, pkg/dem/Sphere.cpp:88-109
+__device__ __forceinline__ bool geomSS(const DevNodes& N, int A, int B, D3 shift2, bool real, double ssDf, Geo& g) {
+    const double4_32a pa = N.posr[A], pb = N.posr[B];
+    const double r1 = pa.w, r2 = pb.w;
+    const D3 p1 = ld3(pa), p2 = ld3(pb);
+    const D3 relPos = (p2 + shift2) - p1;
+    const double dfr = fabs(ssDf) * (r1 + r2);
+    const double unDistSq = sqn(relPos) - dfr * dfr;
+    if (unDistSq > 0 && !real) return false;
+    const double dist = sqrt(sqn(relPos));
+    g.uN = dist - (r1 + r2);
+    g.normal = relPos / dist;
+    g.contPt = p1 + (r1 + 0.5 * g.uN) * g.normal;
+    g.pos1 = p1;
+    g.vel1 = ld3(N.vel[A]);
+    g.angVel1 = ld3(N.angv[A]);
+    g.pos2 = p2 + shift2;
+    g.vel2 = ld3(N.vel[B]);
+    g.angVel2 = ld3(N.angv[B]);
+    g.r1 = r1;
+    g.r2 = r2;
+    return true;
+}
+
+// Cg2_Wall_Sphere_L6Geom::go, pkg/dem/Wall.cpp:45-79
+__device__ __forceinline__ bool geomWS(const DevNodes& N, const DevParticles& P, const DevContacts& C, int64_t c, int A,
+                                       int B, D3 shift2, bool real, Geo& g) {
+    const int4 aux = P.aux[A];
+    const int ax = aux.x, sense = aux.y;
+    const double4_32a pw = N.posr[A], ps = N.posr[B];
+    const double radius = ps.w;
+    const D3 wallPos = ld3(pw);
+    const D3 spherePos = ld3(ps) + shift2;
+    const double dist = comp(spherePos, ax) - comp(wallPos, ax);
+    if (!real && fabs(dist) > radius) return false;
+    D3 contPt = spherePos;
+    setComp(contPt, ax, comp(wallPos, ax));
+    D3 normal{0, 0, 0};
+    if (sense == 0) {
+        if (!real) setComp(normal, ax, dist > 0 ? 1. : -1.);
+        else setComp(normal, ax, C.col[CC_T0X + ax][c]);
+    } else setComp(normal, ax, sense == 1 ? 1. : -1);
+    g.uN = comp(normal, ax) * dist - radius;
+    g.normal = normal;
+    g.contPt = contPt;
+    g.pos1 = wallPos;
+    g.vel1 = ld3(N.vel[A]);
+    g.angVel1 = ld3(N.angv[A]);
+    g.pos2 = spherePos;
+    g.vel2 = ld3(N.vel[B]);
+    g.angVel2 = ld3(N.angv[B]);
+    g.r1 = -radius;
+    g.r2 = radius;
+    return true;
+}
+
+// CompUtils::closestSegmentPt, lib/base/CompUtils.cpp:57-63
+__device__ __forceinline__ D3 closestSegmentPt(D3 P, D3 A, D3 B) {
+    const D3 BA = B - A;
+    if (sqn(BA) == 0.) return A;
+    const double u = (dot(P, BA) - dot(A, BA)) / sqn(BA);
+    return A + smin(1., smax(0., u)) * BA;
+}
+
+// Cg2_Facet_Sphere_L6Geom::go, pkg/dem/Facet.cpp:235-288 with Facet::interpolatePtLinAngVel :158-174
+// and CompUtils::triangleBarycentrics lib/base/CompUtils.cpp:92-110
+__device__ __forceinline__ bool geomFS(const DevNodes& N, const DevParticles& P, int A, int B, D3 shift2, bool real, Geo& g,
+                                       int* dErr) {
+    const int4 fn = P.aux[A];
+    const double4_32a fd = P.facet[A];
+    const double halfThick = fd.w;
+    const D3 fakeVel{fd.x, fd.y, fd.z};
+    const double4_32a ps = N.posr[B];
+    const double radius = ps.w;
+    const D3 sC = ld3(ps) + shift2;
+    const D3 p0 = ld3(N.posr[fn.x]), p1 = ld3(N.posr[fn.y]), p2 = ld3(N.posr[fn.z]);
+    const D3 nn = cross(p1 - p0, p2 - p0);
+    const D3 fNormal = normalized(nn);
+    const double planeDist = dot(sC - p0, fNormal);
+    if (fabs(planeDist) > (radius + halfThick) && !real) return false;
+    const D3 fC = sC - planeDist * fNormal;
+    const double l0 = dot(cross(p1 - p0, nn), fC - p0);
+    const double l1 = dot(cross(p2 - p1, nn), fC - p1);
+    const double l2 = dot(cross(p0 - p2, nn), fC - p2);
+    const int w = (l0 > 0 ? 1 : 0) + (l1 > 0 ? 2 : 0) + (l2 > 0 ? 4 : 0);
+    D3 contPt;
+    switch (w) {
+        case 0: contPt = fC; break;
+        case 1: contPt = closestSegmentPt(fC, p0, p1); break;
+        case 2: contPt = closestSegmentPt(fC, p1, p2); break;
+        case 4: contPt = closestSegmentPt(fC, p2, p0); break;
+        case 3: contPt = p1; break;
+        case 5: contPt = p0; break;
+        case 6: contPt = p2; break;
+        default: atomicCAS(dErr, 0, 100); return false;  // "Impossible sphere-facet intersection"
+    }
+    D3 normal = sC - contPt;
+    const double rh = radius + halfThick;
+    if (sqn(normal) > rh * rh && !real) return false;
+    const double dist = sqrt(sqn(normal));
+    normal = normal / dist;
+    if (halfThick > 0) contPt = contPt + normal * halfThick;
+    g.uN = (dist - radius) - halfThick;
+    // barycentric interpolation of the facet node velocities at contPt
+    const D3 vB = p1 - p0, vC = p2 - p0, vX = contPt - p0;
+    const double m00 = dot(vB, vB), m01 = dot(vC, vB), m10 = dot(vB, vC), m11 = dot(vC, vC);
+    const double det = m00 * m11 - m10 * m01;
+    const double invdet = 1. / det;
+    const double i00 = m11 * invdet, i10 = -m10 * invdet, i01 = -m01 * invdet, i11 = m00 * invdet;
+    const double b0 = dot(vX, vB), b1 = dot(vX, vC);
+    const double u = i00 * b0 + i01 * b1, v = i10 * b0 + i11 * b1;
+    const double a0 = (1 - u) - v;
+    const D3 v0 = ld3(N.vel[fn.x]), v1 = ld3(N.vel[fn.y]), v2 = ld3(N.vel[fn.z]);
+    D3 linVel = (a0 * v0 + u * v1) + v * v2;
+    const D3 angVel = (cross(p0 - contPt, v0) + cross(p1 - contPt, v1)) + cross(p2 - contPt, v2);
+    if (!isZero(fakeVel)) {
+        if (!isnan(fakeVel.x)) linVel = linVel + fakeVel;
+        else linVel = dot(linVel, fNormal) * fNormal;
+    }
+    g.normal = normal;
+    g.contPt = contPt;
+    g.pos1 = contPt;
+    g.vel1 = linVel;
+    g.angVel1 = angVel;
+    g.pos2 = sC;
+    g.vel2 = ld3(N.vel[B]);
+    g.angVel2 = ld3(N.angv[B]);
+    g.r1 = smax(halfThick, radius);
+    g.r2 = radius;
+    return true;
+}
+
+// Fused ContactLoop body (pkg/dem/ContactLoop.cpp:135-224) for one contact:
+// Cg2 (above) -> Cg2_Any_Any_L6Geom__Base::handleSpheresLikeContact (pkg/dem/L6Geom.cpp:51-217)
+// -> Cp2 on creation (FrictMat.cpp:20-44 / Hertz.cpp:9-50) -> Law2 (IdealElPl.cpp:12-122 /
+// Hertz.cpp:58-182) -> global force on pA (Contact::getForceTorqueBranch, Contact.cpp:24-34).
+__global__ void __launch_bounds__(128) k_contact_fp64(DevNodes N, DevParticles P, DevContacts C, const double4_32a* __restrict__ mats,
+                                                     const ScenePar* __restrict__ spp, const long long* __restrict__ dStep,
+                                                     int* __restrict__ dErr) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= C.n) return;
+    const ScenePar& sp = *spp;
+    uint32_t fl = C.flags[c];
+    const uint32_t ty = ctype(fl);
+    if (ty == CT_NONE) return;
+    fl &= ~C_PENDING;
+    const uint64_t key = C.key[c];
+    const int lo = (int)(key >> 32), hi = (int)(key & 0xffffffffu);
+    const int A = (fl & C_SWAP) ? hi : lo, B = (fl & C_SWAP) ? lo : hi;
+    const bool real = fl & C_REAL;
+    const long long step = *dStep;
+    const double dt = sp.dt;
+    D3 shift2{0, 0, 0}, shiftVel2{0, 0, 0};
+    if (sp.periodic) {
+        int a, b, cc;
+        unpackCellDist(C.cdist[c], a, b, cc);
+        if (fl & C_SWAP) { a = -a; b = -b; cc = -cc; }
+        const D3 cd{(double)a, (double)b, (double)cc};
+        shift2 = mul(ldm(sp.hSize), cd);
+        shiftVel2 = mul(ldm(sp.shiftVelMat), cd);
+    }
+    Geo g;
+    bool touch;
+    if (ty == CT_SS) touch = geomSS(N, A, B, shift2, real, sp.ssDistFactor, g);
+    else if (ty == CT_WS) touch = geomWS(N, P, C, c, A, B, shift2, real, g);
+    else touch = geomFS(N, P, A, B, shift2, real, g, dErr);
+    if (!touch) {
+        C.flags[c] = fl;
+        return;
+    }
+    D3 c0, c1, c2;
+    D3 lvel{0, 0, 0};
+    double ph0, ph1, ph2, ph3 = 0, ph4 = 0;
+    double fn, ft1 = 0, ft2 = 0;
+    if (!real) {
+        // new geometry: L6Geom::setInitialLocalCoords pkg/dem/L6Geom.cpp:27-38 and :53-71
+        const D3 locX = g.normal;
+        const D3 ref = (fabs(locX.y) < fabs(locX.z)) ? D3{0, 1, 0} : D3{0, 0, 1};
+        D3 locY = cross(locX, ref);
+        locY = locY - locX * dot(locY, locX);
+        locY = normalized(locY);
+        c0 = locX;
+        c1 = locY;
+        c2 = cross(locX, locY);
+        double lens0 = fabs(g.r1) + g.uN / 2, lens1 = fabs(g.r2) + g.uN / 2;
+        if (lens0 < 0) lens0 = lens1;
+        if (lens1 < 0) lens1 = lens0;
+        const double rr = (g.r1 > 0 && g.r2 > 0) ? smin(g.r1, g.r2) : (g.r1 > 0 ? g.r1 : g.r2);
+        const double contA = 3.14159265358979323846 * (rr * rr);
+        const double4_32a m1 = mats[P.mat[A]], m2 = mats[P.mat[B]];  // density young tanPhi ktDivKn
+        if (sp.phys == 0) {
+            // Cp2_FrictMat_FrictPhys::updateFrictPhys, pkg/dem/FrictMat.cpp:20-44
+            ph0 = 1 / (1 / (m1.y * contA / lens0) + 1 / (m2.y * contA / lens1));
+            ph1 = .5 * (m1.w + m2.w) * ph0;
+            ph2 = smin(m1.z, m2.z);
+        } else {
+            // Cp2_FrictMat_HertzPhys::go, pkg/dem/Hertz.cpp:9-50 (kn0 = K*sqrt(R) is stored)
+            const double nu1 = sp.hzPoisson, nu2 = sp.hzPoisson;
+            const double E1 = m1.y, E2 = m2.y;
+            const double K = (4 / 3.) * 1. / ((1 - nu1 * nu1) / E1 + (1 - nu2 * nu2) / E2);
+            const double R = 1. / (1. / lens0 + 1. / lens1);
+            const double kn0 = K * sqrt(R);
+            const double G1 = E1 / (2 * (1 + nu1)), G2 = E2 / (2 * (1 + nu2));
+            const double G = .5 * (G1 + G2);
+            const double nu = .5 * (nu1 + nu2);
+            ph0 = kn0;
+            ph1 = 2 * sqrt(4 * R) * G / (2 - nu);
+            ph2 = smin(m1.z, m2.z);
+            ph4 = R;
+            if (sp.hzViscOn) {
+                const double ma = N.minert[P.shape[A] == WG_SHAPE_FACET ? P.aux[A].x : A].w;
+                const double mb = N.minert[B].w;
+                const double mbar = (ma <= 0 && mb > 0) ? mb : ((ma > 0 && mb <= 0) ? ma : (ma * mb) / (ma + mb));
+                ph3 = smax(0., sp.hzViscConst * sqrt(mbar * kn0));
+            } else ph3 = 0.0;
+        }
+        C.col[CC_P0][c] = ph0;
+        C.col[CC_P1][c] = ph1;
+        C.col[CC_P2][c] = ph2;
+        C.col[CC_P3][c] = ph3;
+        C.col[CC_P4][c] = ph4;
+        C.step0[c] = (int32_t)step;
+    } else {
+        // existing geometry: update branch, pkg/dem/L6Geom.cpp:79-216
+        const int am = sp.approxMask;
+        const D3 currNormal = g.normal;
+        const D3 prevNormal{C.col[CC_T0X][c], C.col[CC_T0Y][c], C.col[CC_T0Z][c]};
+        const D3 prevC1{C.col[CC_T1X][c], C.col[CC_T1Y][c], C.col[CC_T1Z][c]};
+        const D3 prevContPt{C.col[CC_CPX][c], C.col[CC_CPY][c], C.col[CC_CPZ][c]};
+        const D3 normRotVec = cross(prevNormal, currNormal);
+        D3 midNormal = (am & 1) ? prevNormal : .5 * (prevNormal + currNormal);
+        if (sqrt(sqn(midNormal)) == 0) midNormal = currNormal;
+        else if (!(am & 2) && !(am & 1)) midNormal = normalized(midNormal);
+        const D3 normTwistVec = ((midNormal * dt) * .5) * dot(midNormal, g.angVel1 + g.angVel2);
+        const D3 rt = normRotVec + normTwistVec;
+        D3 m0, m1v;
+        if (am & 4) {
+            m0 = prevNormal;
+            m1v = prevC1;
+        } else {
+            m0 = midNormal;
+            m1v = prevC1 - cross(prevC1, rt) / 2.;
+        }
+        const D3 m2v = cross(m0, m1v);
+        c0 = currNormal;
+        c1 = prevC1 - cross(m1v, rt);
+        c2 = cross(c0, c1);
+        if (sp.trsfRenorm > 0 && (step % sp.trsfRenorm) == 0) {
+            c0 = normalized(c0);
+            c1 = c1 - c0 * dot(c1, c0);
+            c1 = normalized(c1);
+            c2 = cross(c0, c1);
+        }
+        D3 midContPt, midPos1, midPos2;
+        if (am & 8) {
+            midContPt = g.contPt;
+            midPos1 = g.pos1;
+            midPos2 = g.pos2;
+        } else {
+            midContPt = .5 * (prevContPt + g.contPt);
+            midPos1 = g.pos1 - (dt / 2.) * g.vel1;
+            midPos2 = g.pos2 - (dt / 2.) * (g.vel2 + shiftVel2);
+        }
+        const D3 c1x = (sp.noRatch && g.r1 > 0) ? g.r1 * midNormal : midContPt - midPos1;
+        const D3 c2x = (sp.noRatch && g.r2 > 0) ? (-g.r2) * midNormal : midContPt - midPos2;
+        const D3 relVel = ((g.vel2 + shiftVel2) + cross(g.angVel2, c2x)) - (g.vel1 + cross(g.angVel1, c1x));
+        lvel = D3{dot(m0, relVel), dot(m1v, relVel), dot(m2v, relVel)};
+        ph0 = C.col[CC_P0][c];
+        ph1 = C.col[CC_P1][c];
+        ph2 = C.col[CC_P2][c];
+        ph3 = C.col[CC_P3][c];
+        ph4 = C.col[CC_P4][c];
+        ft1 = C.col[CC_FT1][c];
+        ft2 = C.col[CC_FT2][c];
+    }
+    const double uN = g.uN;
+    bool keep = true;
+    if (sp.law == 0) {
+        // Law2_L6Geom_FrictPhys_IdealElPl::go, pkg/dem/IdealElPl.cpp:18-81 (kn kt tanPhi = ph0 ph1 ph2)
+        if (uN > 0 && !sp.noBreak) keep = false;
+        else {
+            fn = ph0 * uN;
+            if (sp.noFrict || ph2 == 0.) {
+                ft1 = 0;
+                ft2 = 0;
+            } else {
+                ft1 = ft1 + (dt * ph1) * lvel.y;
+                ft2 = ft2 + (dt * ph1) * lvel.z;
+                const double maxFt = fabs(fn) * ph2;
+                if ((ft1 * ft1 + ft2 * ft2) > maxFt * maxFt && !sp.noSlip) {
+                    const double FtNorm = sqrt(ft1 * ft1 + ft2 * ft2);
+                    double ratio = maxFt / FtNorm;
+                    if (FtNorm == 0.) ratio = 0.;
+                    ft1 = ft1 * ratio;
+                    ft2 = ft2 * ratio;
+                }
+                if (isnan(fn) || isnan(ft1) || isnan(ft2)) atomicCAS(dErr, 0, 101);  // "NaN force in contact"
+            }
+        }
+    } else {
+        // Law2_L6Geom_HertzPhys_DMT::go, DMT branch, pkg/dem/Hertz.cpp:58-87,143-172 (kn0 kt0 tanPhi alpha_sqrtMK R)
+        if (uN > 0) keep = false;
+        else {
+            const double su = sqrt(-uN);
+            const double Fne = -ph0 * (su * su * su);
+            const double Fna = 4 * 3.14159265358979323846 * ph4 * sp.hzGamma;
+            const double eta = (ph3 > 0 ? ph3 * sqrt(sqrt(smax(-uN, 0.))) : 0.);
+            double Fnv = eta * lvel.x;
+            if (sp.noAttraction && Fne + Fnv > 0) Fnv = -Fne;
+            fn = (Fne + Fna) + Fnv;
+            const double kt = ph1 * sqrt(uN < 0 ? -uN : 0);
+            ft1 = (dt * kt) * lvel.y;
+            ft2 = (dt * kt) * lvel.z;
+            const double maxFt = smax(0., fn) * ph2;
+            if ((ft1 * ft1 + ft2 * ft2) > maxFt * maxFt) {
+                const double FtNorm = sqrt(ft1 * ft1 + ft2 * ft2);
+                const double ratio = maxFt / FtNorm;
+                ft1 = ft1 * ratio;
+                ft2 = ft2 * ratio;
+            } else {
+                ft1 = ft1 + eta * lvel.y;
+                ft2 = ft2 + eta * lvel.z;
+            }
+        }
+    }
+    if (!keep) {
+        // ContactContainer::requestRemoval: geom and phys reset, contact pending for the collider
+        C.flags[c] = (fl & ~C_REAL) | C_PENDING;
+        return;
+    }
+    const DQ ori = quatFromCols(c0, c1, c2);
+    const D3 Fg = qrot(ori, D3{fn, ft1, ft2});
+    C.col[CC_T0X][c] = c0.x;
+    C.col[CC_T0Y][c] = c0.y;
+    C.col[CC_T0Z][c] = c0.z;
+    C.col[CC_T1X][c] = c1.x;
+    C.col[CC_T1Y][c] = c1.y;
+    C.col[CC_T1Z][c] = c1.z;
+    C.col[CC_CPX][c] = g.contPt.x;
+    C.col[CC_CPY][c] = g.contPt.y;
+    C.col[CC_CPZ][c] = g.contPt.z;
+    C.col[CC_FN][c] = fn;
+    C.col[CC_FT1][c] = ft1;
+    C.col[CC_FT2][c] = ft2;
+    C.col[CC_FGX][c] = Fg.x;
+    C.col[CC_FGY][c] = Fg.y;
+    C.col[CC_FGZ][c] = Fg.z;
+    C.flags[c] = fl | C_REAL;
+}
+
+void launch_contact_fp64(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C, const double4_32a* mats,
+                         const ScenePar* sp, const long long* dStep, int* dErr) {
+    if (C.n == 0) return;
+    const int bs = 128;
+    k_contact_fp64<<<(unsigned)((C.n + bs - 1) / bs), bs, 0, st>>>(N, P, C, mats, sp, dStep, dErr);
+}
+
+// ---------------------------------------------------------------------------------- force sum
+// Per-particle sum replacing ContactLoop::applyForceUninodal + DemData::addForceTorque
+// (pkg/dem/ContactLoop.cpp:261-267, Contact.cpp:24-34, Particle.hpp:221) and the force reset
+// of Leapfrog (Leapfrog.cpp:240-245). Contributions are added in ascending order of the
+// other particle's id, which is the order of the reference's deterministic serial pass over
+// contacts sorted by (lo,hi) (ContactLoop.cpp:250-257).
+__device__ __forceinline__ void addContribution(const DevNodes& N, const DevContacts& C, const ScenePar& sp, int64_t c, int p,
+                                                D3 pos, D3& F, D3& T) {
+    const uint32_t fl = C.flags[c];
+    if (!(fl & C_REAL)) return;
+    const uint64_t key = C.key[c];
+    const int lo = (int)(key >> 32);
+    const int A = (fl & C_SWAP) ? (int)(key & 0xffffffffu) : lo;
+    const bool isPA = (A == p);
+    const double sign = isPA ? 1 : -1;
+    const D3 Fp = D3{C.col[CC_FGX][c], C.col[CC_FGY][c], C.col[CC_FGZ][c]} * sign;
+    D3 shift{0, 0, 0};
+    if (!isPA && sp.periodic) {
+        int a, b, cc;
+        unpackCellDist(C.cdist[c], a, b, cc);
+        if (fl & C_SWAP) { a = -a; b = -b; cc = -cc; }
+        shift = mul(ldm(sp.hSize), D3{(double)a, (double)b, (double)cc});
+    }
+    const D3 xc = D3{C.col[CC_CPX][c], C.col[CC_CPY][c], C.col[CC_CPZ][c]} - (pos + shift);
+    const D3 tq = cross(xc, Fp) + D3{0, 0, 0};
+    F = F + Fp;
+    T = T + tq;
+}
+
+__global__ void k_reduce(DevNodes N, DevParticles P, DevContacts C, DevIncidence I, const ScenePar* __restrict__ spp,
+                         int heavyThreshold) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P.n) return;
+    const int sh = P.shape[p];
+    if (sh == WG_SHAPE_FACET) return;
+    const ScenePar& sp = *spp;
+    const uint32_t flags = N.flags[p];
+    const double mass = N.minert[p].w;
+    D3 F{0, 0, 0}, T{0, 0, 0};
+    if (sp.hasGravity && !(flags & F_GRAVITY_SKIP)) F = mass * D3{sp.g[0], sp.g[1], sp.g[2]};
+    if (sp.applyForces) {
+        const int h0 = I.hiStart[p], h1 = I.hiStart[p + 1], l0 = I.loStart[p], l1 = I.loStart[p + 1];
+        if ((h1 - h0) + (l1 - l0) > heavyThreshold) return;  // summed by k_reduce_heavy
+        const D3 pos = ld3(N.posr[p]);
+        for (int k = h0; k < h1; k++) addContribution(N, C, sp, I.hiList[k], p, pos, F, T);
+        for (int k = l0; k < l1; k++) addContribution(N, C, sp, k, p, pos, F, T);
+    }
+    N.force[p] = st4(F, 0.);
+    N.torque[p] = st4(T, 0.);
+}
+
+// Particles with many contacts (walls): one block each, fixed-shape tree sum (deterministic,
+// same result on every run; rounding differs from the serial order only for these particles,
+// whose DOFs are blocked in every supported scene).
+__global__ void k_reduce_heavy(DevNodes N, DevParticles P, DevContacts C, DevIncidence I, const ScenePar* __restrict__ spp) {
+    const int p = I.heavy[blockIdx.x];
+    const ScenePar& sp = *spp;
+    const int h0 = I.hiStart[p], h1 = I.hiStart[p + 1], l0 = I.loStart[p], l1 = I.loStart[p + 1];
+    const int nh = h1 - h0, n = nh + (l1 - l0);
+    const D3 pos = ld3(N.posr[p]);
+    D3 F{0, 0, 0}, T{0, 0, 0};
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const int64_t c = (k < nh) ? (int64_t)I.hiList[h0 + k] : (int64_t)(l0 + (k - nh));
+        addContribution(N, C, sp, c, p, pos, F, T);
+    }
+    __shared__ double sh[6][256];
+    sh[0][threadIdx.x] = F.x; sh[1][threadIdx.x] = F.y; sh[2][threadIdx.x] = F.z;
+    sh[3][threadIdx.x] = T.x; sh[4][threadIdx.x] = T.y; sh[5][threadIdx.x] = T.z;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s)
+            for (int q = 0; q < 6; q++) sh[q][threadIdx.x] = sh[q][threadIdx.x] + sh[q][threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const uint32_t flags = N.flags[p];
+        const double mass = N.minert[p].w;
+        D3 G{0, 0, 0};
+        if (sp.hasGravity && !(flags & F_GRAVITY_SKIP)) G = mass * D3{sp.g[0], sp.g[1], sp.g[2]};
+        N.force[p] = st4(G + D3{sh[0][0], sh[1][0], sh[2][0]}, 0.);
+        N.torque[p] = st4(D3{sh[3][0], sh[4][0], sh[5][0]}, 0.);
+    }
+}
+
+__global__ void k_step_advance(long long* dStep) { *dStep += 1; }
+
+static const int kHeavyThreshold = 64;
+
+void launch_reduce(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C, const DevIncidence& I,
+                   const ScenePar* sp, long long* dStep) {
+    if (P.n > 0) {
+        k_reduce<<<(P.n + 255) / 256, 256, 0, st>>>(N, P, C, I, sp, kHeavyThreshold);
+        if (I.nHeavy > 0) k_reduce_heavy<<<I.nHeavy, 256, 0, st>>>(N, P, C, I, sp);
+    }
+    k_step_advance<<<1, 1, 0, st>>>(dStep);
+}
+
+}  // namespace wg

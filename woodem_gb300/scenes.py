@@ -1,0 +1,118 @@
+"""Seeded synthetic scenes of the benchmark configurations.
+
+Each builder returns a ready-to-run Scene assembled through the Woo-style API
+(utils.wallBox, triangulated.cylinder, utils.defaultEngines, utils.pWaveDt); the
+particle positions come from numpy's PCG64 generator or the seeded random
+sequential insertion of libwoogpu (wg_pack_rsa). Boundary particles are added
+before the spheres, so walls and facets take the lowest ids.
+"""
+import math
+
+import numpy as np
+
+from . import utils, triangulated, _native
+from .core import Scene
+from .dem import DemField, FrictMat, Cp2_FrictMat_HertzPhys, Law2_L6Geom_HertzPhys_DMT
+
+
+def pack_rsa(radii, lo, hi, region=0, params=(0, 0, 0, 0), seed=0, max_attempts=2000):
+    """Seeded random sequential insertion (largest spheres first). Returns centers in input order."""
+    radii = np.ascontiguousarray(radii, dtype=float)
+    order = np.argsort(-radii, kind="stable")
+    r_sorted = np.ascontiguousarray(radii[order])
+    out = np.zeros((len(radii), 3))
+    lo = np.ascontiguousarray(lo, dtype=float)
+    hi = np.ascontiguousarray(hi, dtype=float)
+    pr = np.ascontiguousarray(params, dtype=float)
+    n = _native.lib().wg_pack_rsa(len(radii), _native.ptr(r_sorted), _native.ptr(lo), _native.ptr(hi), int(region),
+                                  _native.ptr(pr), int(seed), int(max_attempts), _native.ptr(out))
+    if n != len(radii):
+        raise RuntimeError("random insertion placed only %d of %d spheres; enlarge the region" % (n, len(radii)))
+    res = np.empty_like(out)
+    res[order] = out
+    return res
+
+
+def box_settle(n=10000, seed=0, radius=5e-3, pitch=12e-3, dims=(22, 22, 21), box=((0, 0, 0), (0.3, 0.3, 0.6)), density=3000.0,
+               young=1e7, ktDivKn=0.2, tanPhi=0.5, damping=0.2, verletRel=0.1, jitter=1e-3, precision="fp64"):
+    """Box settle: spheres on a jittered cubic lattice (x fastest, first ``n`` sites), lattice
+    centred in x and y and starting one pitch above z=0, six inward-facing walls, gravity
+    (0,0,-9.81), dt = 0.3*pWaveDt, Leapfrog damping 0.2, verletDist = 0.1*radius, IdealElPl."""
+    nx, ny, nz = dims
+    if n > nx * ny * nz:
+        raise ValueError("lattice too small")
+    lo, hi = np.asarray(box[0], float), np.asarray(box[1], float)
+    x0 = lo[0] + ((hi[0] - lo[0]) - (nx - 1) * pitch) / 2
+    y0 = lo[1] + ((hi[1] - lo[1]) - (ny - 1) * pitch) / 2
+    z0 = lo[2] + pitch
+    i = np.arange(n)
+    centers = np.stack([x0 + (i % nx) * pitch, y0 + ((i // nx) % ny) * pitch, z0 + (i // (nx * ny)) * pitch], axis=1)
+    rng = np.random.default_rng(seed)
+    centers = centers + rng.uniform(-jitter, jitter, size=(n, 3))
+    S = Scene(fields=[DemField(gravity=(0, 0, -9.81))])
+    S.gpu.precision = precision
+    mat = FrictMat(density=density, young=young, ktDivKn=ktDivKn, tanPhi=tanPhi)
+    S.dem.par.add(utils.wallBox((lo, hi), mat=mat))
+    S.dem.par.addSpheres(centers, radius, mat)
+    S.engines = utils.defaultEngines(damping=damping, verletDist=-verletRel, dynDtPeriod=0)
+    S.dt = 0.3 * utils.pWaveDt(S)
+    return S
+
+
+def box_settle_small(n=1500, seed=0, precision="fp64", **kw):
+    """The box-settle configuration on a smaller lattice (tests)."""
+    side = int(math.ceil((n / 2.0) ** (1 / 3.0)))
+    dims = (side, side, int(math.ceil(n / float(side * side))))
+    pitch = kw.pop("pitch", 12e-3)
+    w = (dims[0] + 3) * pitch
+    h = 2 * (dims[2] + 3) * pitch
+    return box_settle(n=n, seed=seed, pitch=pitch, dims=dims, box=((0, 0, 0), (w, w, h)), precision=precision, **kw)
+
+
+def lognormal_radii(n, seed, median=3e-3, sigma=0.25, rmin=1.5e-3, rmax=6e-3):
+    rng = np.random.default_rng(seed)
+    return np.clip(median * np.exp(sigma * rng.standard_normal(n)), rmin, rmax)
+
+
+def _segment_height(R, area):
+    """Height z (relative to the axis) below which a circle of radius R has the given area."""
+    lo, hi = -R, R
+    for _ in range(100):
+        z = 0.5 * (lo + hi)
+        a = R * R * math.acos(-z / R) + z * math.sqrt(max(R * R - z * z, 0.0))
+        if a < area:
+            lo = z
+        else:
+            hi = z
+    return 0.5 * (lo + hi)
+
+
+def hertz_drum(n=1_000_000, seed=0, diameter=1.2, length=0.6, div=201, axDiv=50, fill_fraction=0.35, density=2500.0,
+               young=1e8, poisson=0.25, en=0.6, tanPhi=0.5, omega=1.0, verletRel=0.1, precision="fp64",
+               median=3e-3, sigma=0.25, rmin=1.5e-3, rmax=6e-3):
+    """Rotating drum: x-axis cylinder (diameter x length) meshed into 2*(div-1)*axDiv facets with
+    outward normals and fakeVel for angular velocity ``omega``, two rotating Wall end caps,
+    lognormal radii, Hertz contacts with viscous damping (en), gravity (0,0,-9.81),
+    dt = 0.3*pWaveDt, verletDist = 0.1*min radius. Spheres are placed by seeded random
+    sequential insertion (solid fraction ``fill_fraction``) in the lower part of the drum whose
+    height is chosen to hold them."""
+    R = diameter / 2.0
+    S = Scene(fields=[DemField(gravity=(0, 0, -9.81))])
+    S.gpu.precision = precision
+    mat = FrictMat(density=density, young=young, tanPhi=tanPhi)
+    drum = triangulated.cylinder((0, 0, 0), (length, 0, 0), R, div=div, axDiv=axDiv, capA=True, capB=True, wallCaps=True,
+                                 angVel=omega, mat=mat)
+    S.dem.par.add(drum)
+    radii = lognormal_radii(n, seed, median, sigma, rmin, rmax)
+    vol = float(np.sum((4 / 3.0) * math.pi * radii ** 3))
+    margin = 1e-4
+    usable = length - 2 * margin
+    area = vol / fill_fraction / usable
+    Ri = R - margin
+    zf = _segment_height(Ri, min(area, 0.97 * math.pi * Ri * Ri))
+    centers = pack_rsa(radii, (margin, -Ri, -Ri), (length - margin, Ri, zf), region=1, params=(0.0, 0.0, Ri, zf), seed=seed + 7)
+    S.dem.par.addSpheres(centers, radii, mat)
+    S.engines = utils.defaultEngines(cp2=Cp2_FrictMat_HertzPhys(poisson=poisson, en=en, gamma=0.0, alpha=0.0),
+                                     law=Law2_L6Geom_HertzPhys_DMT(), verletDist=-verletRel, dynDtPeriod=0, damping=0.0)
+    S.dt = 0.3 * utils.pWaveDt(S)
+    return S
