@@ -15,7 +15,8 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libwoogpu.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-diag-suppress", "177,550"]
+# host code of the library (cell matrices, contact listing) is also compiled without contraction
+COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-diag-suppress", "177,550"]
 # translation unit -> extra flags
 UNITS = {
     "wg_step.cu": ["--fmad=false"],
