@@ -151,6 +151,24 @@ void wg_host_free(void* p);
    number of kernel launches. */
 int wg_get_timing(wg_scene* s, double* total_ms, double* phase_ms4, int64_t* launches);
 
+/* Allocation-free broad phase (no counterpart in the reference): for callers that must not
+   allocate device memory (memory owned by another runtime's pool, code running during CUDA
+   graph capture, loops that cannot take the synchronisation of cudaMalloc/cudaFree).
+   Given n sphere boxes in host memory (mn, mx: 3 doubles each; mask: Particle.mask) it
+   returns in host memory the overlapping pairs -- closed 3-axis box overlap and the mask test
+   of Collider::mayCollide with lone_mask -- sorted by (id_lo, id_hi), *n_pairs of them.
+   All device scratch is one static __device__ array (about 13 MB, held by every GPU that
+   loads the library until the process exits); n above 32768 or more than 262144 pairs is
+   rejected with WG_ERR_CAPACITY, as is a pair count above cap (*n_pairs is still set).
+   The first call on a device resolves the scratch address (cudaGetSymbolAddress) and should
+   come before any stream capture. Calls share the scratch: calls that overlap on the GPU
+   (concurrent host threads on one device) race. It runs on the current device and the
+   legacy default stream and returns after the result is in host memory. */
+int wg_broadphase_noalloc(int32_t n, const double* mn, const double* mx, const uint32_t* mask, uint32_t lone_mask,
+                          int64_t cap, int32_t* id_lo, int32_t* id_hi, int64_t* n_pairs);
+/* Message of the last failed wg_broadphase_noalloc call on this thread. */
+const char* wg_broadphase_noalloc_error(void);
+
 /* Scene generation (host only): seeded random sequential insertion of n non-overlapping
    spheres, the role of SpherePack::makeCloud (lib/sphere-pack/SpherePack.hpp:75).
    region_kind 0: box lo..hi; 1: x-axis cylinder through (params[0],params[1]) of radius

@@ -23,6 +23,7 @@ UNITS = {
     "wg_collide.cu": ["--fmad=false"],
     "wg_api.cu": ["--fmad=false"],
     "wg_step32.cu": ["--fmad=true"],
+    "wg_noalloc.cu": ["--fmad=false"],
     "wg_pack.cpp": [],
 }
 

@@ -87,6 +87,8 @@ def lib():
         "wg_get_timing": (C.c_int, [C.c_void_p, P_D, P_D, P_I64]),
         "wg_host_alloc": (C.c_void_p, [C.c_int64]),
         "wg_host_free": (None, [C.c_void_p]),
+        "wg_broadphase_noalloc": (C.c_int, [C.c_int32, P_D, P_D, P_U32, C.c_uint32, C.c_int64, P_I32, P_I32, P_I64]),
+        "wg_broadphase_noalloc_error": (C.c_char_p, []),
         "wg_pack_rsa": (C.c_int64, [C.c_int64, P_D, P_D, P_D, C.c_int32, P_D, C.c_uint64, C.c_int64, P_D]),
     }
     for name, (res, args) in sig.items():
