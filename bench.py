@@ -87,11 +87,29 @@ class Clocks:
 
 
 def build_scene(args, seed, n=None, precision=None):
+    """The drum, filled by seeded random insertion and compacted into a resting bed on the GPU."""
     from woodem_gb300 import scenes
     n = n or args.spheres
     scale = (n / 1e6) ** (1 / 3.0)
-    return scenes.hertz_drum(n=n, seed=seed, diameter=1.2 * scale, length=0.6 * scale, div=201, axDiv=50,
-                             precision=precision or args.precision)
+    t = time.time()
+    S = scenes.hertz_drum(n=n, seed=seed, diameter=1.2 * scale, length=0.6 * scale, div=201, axDiv=50,
+                          precision=precision or args.precision, settle_steps=args.settle)
+    log("scene of %d spheres built and settled (%d steps) in %.1fs" % (n, args.settle, time.time() - t))
+    return S
+
+
+def snapshot(S):
+    nd = S.dem._nodes.soa
+    return {k: nd.col(k).copy() for k in ("pos", "ori", "vel", "angVel", "force", "torque")}
+
+
+def restore(S, st):
+    S.close()
+    nd = S.dem._nodes.soa
+    for k, v in st.items():
+        nd.col(k)[:] = v
+    S.step = 0
+    S.time = 0.0
 
 
 # Algorithmic bytes of the FP64 / FP32 contact kernel and of a whole step (see DESIGN.md):
@@ -104,9 +122,12 @@ BYTES = {
 }
 
 
-def measure_gpu(args, rank, world):
+def measure_gpu(args, rank, world, S=None, prec=None, e2e=True):
     from woodem_gb300 import _native
-    S = build_scene(args, seed=args.seed + rank)
+    if S is None:
+        S = build_scene(args, seed=args.seed + rank)
+    if prec:
+        S.gpu.precision = prec
     t0 = time.time()
     S.run(args.warmup)
     sim = S._sim
@@ -118,9 +139,13 @@ def measure_gpu(args, rank, world):
     if clocks:
         clocks.start()
     barrier(world)
+    if args.profile:
+        L.wg_profiler(1)
     t1 = time.perf_counter()
     S.run(args.steps)
     t2 = time.perf_counter()
+    if args.profile:
+        L.wg_profiler(0)
     ck = clocks.stop() if clocks else None
     tot, ph, nl = sim.timing()
     st1 = sim.stats()
@@ -128,7 +153,7 @@ def measure_gpu(args, rank, world):
     res = dict(ms=tot, wall=(t2 - t1) * 1e3, phases=ph.tolist(), launches=nl, st0=st0, st1=st1, clocks=ck,
                n_nodes=S._sim.A.n_nodes, n_par=S._sim.A.n_particles, n_spheres=n_spheres)
     # e2e through wg_run_host with page-locked host buffers
-    if not args.no_e2e:
+    if e2e and not args.no_e2e:
         na = S._sim.A.n_nodes
         nbytes = 19 * 8 * na
         p = L.wg_host_alloc(nbytes)
@@ -148,7 +173,6 @@ def measure_gpu(args, rank, world):
         te = time.perf_counter() - te
         L.wg_host_free(p)
         res["e2e"] = dict(seconds=te, steps=ne, h2d=(3 + 4 + 3 + 3 + 3 + 3) * 8 * na, d2h=(3 + 4 + 3 + 3 + 3 + 3) * 8 * na)
-    S.close()
     return res
 
 
@@ -175,6 +199,7 @@ def cpu_sample(args, seconds, threads):
     from oracle.oracle import Oracle
     n = args.cpu_spheres
     S = build_scene(args, seed=args.seed, n=n, precision="fp64")
+    S.close()
     A = _plan.compile_scene(S)
     O = Oracle(A, threads=threads, deterministic=False)
     O.run(2)  # initial sort and first contacts outside the timed sample
@@ -205,7 +230,10 @@ def main():
     ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=30)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--precision", default="fp32", choices=["fp64", "fp32"])
+    ap.add_argument("--settle", type=int, default=12000, help="steps compacting the random fill into a resting bed")
+    ap.add_argument("--no-other", action="store_true", help="skip timing the other precision mode")
+    ap.add_argument("--profile", action="store_true", help="bracket the timed steps with cudaProfilerStart/Stop")
     ap.add_argument("--spheres", type=int, default=1_000_000)
     ap.add_argument("--cpu-spheres", type=int, default=100_000)
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
@@ -216,7 +244,7 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = env_rank()
-    cfg = {"workload": "hertz-drum-1M", "spheres": args.spheres, "facets": 20000, "walls": 2,
+    cfg = {"workload": "hertz-drum-1M", "spheres": args.spheres, "facets": 20000, "walls": 2, "settle_steps": args.settle,
            "law": "Cp2_FrictMat_HertzPhys+Law2_L6Geom_HertzPhys_DMT", "precision": args.precision,
            "l2": "inputs larger than L2 (device state > 1 GB)", "replicas": world}
     if args.impl == "reference":
@@ -251,7 +279,16 @@ def main():
     # each rank drives its own GPU (replicas)
     if world > 1:
         from woodem_gb300 import core  # noqa
-    res = measure_gpu(args, rank, world)
+    S = build_scene(args, seed=args.seed + rank)
+    st0 = snapshot(S)
+    res = measure_gpu(args, rank, world, S=S, prec=args.precision)
+    other = None
+    if not args.no_other:
+        restore(S, st0)
+        oprec = "fp64" if args.precision == "fp32" else "fp32"
+        other = measure_gpu(args, rank, world, S=S, prec=oprec, e2e=False)
+        other["prec"] = oprec
+    S.close()
     ms = allreduce_max(res["ms"], world)
     st0, st1 = res["st0"], res["st1"]
     n_sph = res["n_spheres"]
@@ -275,6 +312,12 @@ def main():
             "step": {"contacts": P, "real": R, "full_runs": nfull, "phase_ms": [x / args.steps for x in res["phases"]],
                      "algorithmic_bytes": step_bytes, "achieved_gbs": step_bytes / (ms / args.steps / 1e3) / 1e9},
             "gpu_launches": int(res["launches"]), "clocks": res["clocks"]}
+    if other is not None:
+        oms = allreduce_max(other["ms"], world)
+        ost0, ost1 = other["st0"], other["st1"]
+        line["other_precision"] = {"precision": other["prec"], "value": world * n_sph * args.steps / (oms / 1e3),
+                                   "ms_per_step": oms / args.steps, "phase_ms": [x / args.steps for x in other["phases"]],
+                                   "real": 0.5 * (ost0.n_real + ost1.n_real), "contacts": 0.5 * (ost0.n_contacts + ost1.n_contacts)}
     if "e2e" in res:
         e = res["e2e"]
         es = allreduce_max(e["seconds"], world)

@@ -141,6 +141,9 @@ int wg_get_aabbs(wg_scene* s, double* mn, double* mx);
 /* Run only the broad phase on the current positions (full run), no stepping. */
 int wg_collide_only(wg_scene* s);
 
+/* Mark the region a profiler started with "profile from start off" captures (1 = start, 0 = stop). */
+int wg_profiler(int on);
+
 /* Page-locked host memory for wg_run_host buffers (cudaMallocHost); NULL on failure. */
 void* wg_host_alloc(int64_t bytes);
 void wg_host_free(void* p);

@@ -22,7 +22,7 @@ UNITS = {
     "wg_step.cu": ["--fmad=false"],
     "wg_collide.cu": ["--fmad=false"],
     "wg_api.cu": ["--fmad=false"],
-    "wg_step32.cu": ["--fmad=true"],
+    "wg_step32.cu": ["--fmad=true", "-Xcompiler", "-ffp-contract=fast"],
     "wg_noalloc.cu": ["--fmad=false"],
     "wg_pack.cpp": [],
 }

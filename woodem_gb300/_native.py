@@ -85,6 +85,7 @@ def lib():
         "wg_collide_only": (C.c_int, [C.c_void_p]),
         "wg_get_aabbs": (C.c_int, [C.c_void_p, P_D, P_D]),
         "wg_get_timing": (C.c_int, [C.c_void_p, P_D, P_D, P_I64]),
+        "wg_profiler": (C.c_int, [C.c_int]),
         "wg_host_alloc": (C.c_void_p, [C.c_int64]),
         "wg_host_free": (None, [C.c_void_p]),
         "wg_broadphase_noalloc": (C.c_int, [C.c_int32, P_D, P_D, P_U32, C.c_uint32, C.c_int64, P_I32, P_I32, P_I64]),

@@ -203,6 +203,7 @@ class Scene(Object):
             self._sim.pull()
 
     def close(self):
+        """Pull the device state into the host containers and release the device simulation."""
         self._invalidate()
 
     def __del__(self):

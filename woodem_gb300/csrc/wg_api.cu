@@ -1,6 +1,8 @@
 // Host side of the GB300 DEM hot path: scene upload, the per-step loop of
 // Scene::doOneStep (core/Scene.cpp:319-389) for the engine list
 // [Leapfrog(reset=True), InsertionSortCollider, ContactLoop], and the C ABI of include/woo_gpu.h.
+#include <cuda_profiler_api.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -179,13 +181,23 @@ int Sim::ensureContactCapacity(int64_t need) {
     if (need <= cCap && C.key) return 0;
     int64_t cap = std::max<int64_t>(need + need / 2, std::max<int64_t>(1024, 2 * cCap));
     DevContacts nc{}, nb{};
+    // FP64 plain: every FP64 column. FP32-force: the FP32 columns plus the FP64 shear force
+    // (IdealElPl) and contact point (facet and wall contacts).
+    auto needD = [&](int q) { return prec == WG_PREC_FP64 || q == CC_FT1 || q == CC_FT2 || q == CC_CPX || q == CC_CPY || q == CC_CPZ; };
     for (DevContacts* d : {&nc, &nb}) {
         d->key = (uint64_t*)dalloc(sizeof(uint64_t) * cap);
         d->flags = (uint32_t*)dalloc(sizeof(uint32_t) * cap);
         d->step0 = (int32_t*)dalloc(sizeof(int32_t) * cap);
         d->cdist = (int32_t*)dalloc(sizeof(int32_t) * cap);
-        for (int q = 0; q < CC_NCOL; q++) d->col[q] = (double*)dalloc(sizeof(double) * cap);
-        if (!d->col[CC_NCOL - 1]) return fail(WG_ERR_CUDA, "out of device memory (contacts)");
+        if (!d->cdist) return fail(WG_ERR_CUDA, "out of device memory (contacts)");
+        for (int q = 0; q < CC_NCOL; q++) {
+            d->col[q] = needD(q) ? (double*)dalloc(sizeof(double) * cap) : nullptr;
+            if (needD(q) && !d->col[q]) return fail(WG_ERR_CUDA, "out of device memory (contacts)");
+        }
+        for (int q = 0; q < CF_NCOL; q++) {
+            d->fcol[q] = (prec == WG_PREC_FP32) ? (float*)dalloc(sizeof(float) * cap) : nullptr;
+            if (prec == WG_PREC_FP32 && !d->fcol[q]) return fail(WG_ERR_CUDA, "out of device memory (contacts)");
+        }
     }
     if (C.key && C.n > 0) {
         WG_CUDA_TRY(cudaMemcpyAsync(nc.key, C.key, sizeof(uint64_t) * C.n, cudaMemcpyDeviceToDevice, stream));
@@ -193,7 +205,9 @@ int Sim::ensureContactCapacity(int64_t need) {
         WG_CUDA_TRY(cudaMemcpyAsync(nc.step0, C.step0, sizeof(int32_t) * C.n, cudaMemcpyDeviceToDevice, stream));
         WG_CUDA_TRY(cudaMemcpyAsync(nc.cdist, C.cdist, sizeof(int32_t) * C.n, cudaMemcpyDeviceToDevice, stream));
         for (int q = 0; q < CC_NCOL; q++)
-            WG_CUDA_TRY(cudaMemcpyAsync(nc.col[q], C.col[q], sizeof(double) * C.n, cudaMemcpyDeviceToDevice, stream));
+            if (nc.col[q]) WG_CUDA_TRY(cudaMemcpyAsync(nc.col[q], C.col[q], sizeof(double) * C.n, cudaMemcpyDeviceToDevice, stream));
+        for (int q = 0; q < CF_NCOL; q++)
+            if (nc.fcol[q]) WG_CUDA_TRY(cudaMemcpyAsync(nc.fcol[q], C.fcol[q], sizeof(float) * C.n, cudaMemcpyDeviceToDevice, stream));
     }
     WG_CUDA_TRY(cudaStreamSynchronize(stream));
     nc.n = C.n;
@@ -201,6 +215,7 @@ int Sim::ensureContactCapacity(int64_t need) {
         if (!d->key) continue;
         dfree(d->key); dfree(d->flags); dfree(d->step0); dfree(d->cdist);
         for (int q = 0; q < CC_NCOL; q++) dfree(d->col[q]);
+        for (int q = 0; q < CF_NCOL; q++) dfree(d->fcol[q]);
     }
     C = nc;
     Cb = nb;
@@ -302,7 +317,10 @@ int Sim::upload() {
     if (!((cfg.phys == 0 && cfg.law == 0) || (cfg.phys == 1 && cfg.law == 1)))
         return fail(WG_ERR_UNSUPPORTED, "unsupported Cp2/Law2 combination (FrictPhys+IdealElPl or HertzPhys+HertzPhys_DMT)");
     if (cfg.law == 1 && cfg.hz_alpha != 0) return fail(WG_ERR_UNSUPPORTED, "Law2_L6Geom_HertzPhys_DMT with Cp2_FrictMat_HertzPhys.alpha!=0 (Schwarz model) is not supported");
-    if (cfg.precision != WG_PREC_FP64) return fail(WG_ERR_UNSUPPORTED, "precision mode not available in this build");
+    if (cfg.precision != WG_PREC_FP64 && cfg.precision != WG_PREC_FP32) return fail(WG_ERR_ARG, "unknown precision mode");
+    prec = cfg.precision;
+    if (prec == WG_PREC_FP32 && cfg.law == 1 && cfg.hz_gamma != 0)
+        return fail(WG_ERR_UNSUPPORTED, "FP32-force mode: Cp2_FrictMat_HertzPhys.gamma (DMT adhesion) must be 0; use precision fp64");
     if (cfg.periodic) return fail(WG_ERR_UNSUPPORTED, "periodic cells are not available in this build");
     for (int64_t i = 0; i < nPar; i++) {
         if (hMat[i] < 0 || hMat[i] >= (int)hDensity.size()) return fail(WG_ERR_ARG, "particle material index out of range");
@@ -421,6 +439,16 @@ int Sim::upload() {
     WG_CUDA_TRY(cudaMemcpy(X.dApiMap, map.data(), sizeof(int32_t) * na, cudaMemcpyHostToDevice));
     WG_CUDA_TRY(cudaMemcpy(X.dStage, hApi.data(), sizeof(double) * 19 * na, cudaMemcpyHostToDevice));
     X.hApiMap = map;
+    if (prec == WG_PREC_FP32) {
+        std::vector<double4_32a> inv(nSlots);
+        for (int64_t q = 0; q < nSlots; q++) {
+            const double4_32a m = minert[q];
+            inv[q] = make_double4_32a(m.x != 0 ? 1. / m.x : 0., m.y != 0 ? 1. / m.y : 0., m.z != 0 ? 1. / m.z : 0., m.w != 0 ? 1. / m.w : 0.);
+        }
+        dInvM = (double4_32a*)dalloc(sizeof(double4_32a) * nSlots);
+        if (!dInvM) return fail(WG_ERR_CUDA, "out of device memory (scene)");
+        WG_CUDA_TRY(cudaMemcpy(dInvM, inv.data(), sizeof(double4_32a) * nSlots, cudaMemcpyHostToDevice));
+    }
     long long st0 = cfg.step;
     step = cfg.step;
     WG_CUDA_TRY(cudaMemcpy(dStep, &st0, sizeof(long long), cudaMemcpyHostToDevice));
@@ -478,7 +506,8 @@ int Sim::run(int64_t n) {
         }
         WG_CUDA_TRY(cudaEventRecord(ev[0], stream));
         WG_CUDA_TRY(cudaMemsetAsync(dFlags, 0, sizeof(int), stream));
-        launch_leapfrog(stream, N, P, dPar, dFlags);
+        if (prec == WG_PREC_FP32) launch_leapfrog32(stream, N, P, dInvM, dPar, dFlags);
+        else launch_leapfrog(stream, N, P, dPar, dFlags);
         launches++;
         WG_CUDA_TRY(cudaEventRecord(ev[1], stream));
         WG_CUDA_TRY(cudaMemcpyAsync(hFlags, dFlags, sizeof(int), cudaMemcpyDeviceToHost, stream));
@@ -492,9 +521,11 @@ int Sim::run(int64_t n) {
             launches += 12;
         }
         WG_CUDA_TRY(cudaEventRecord(ev[3], stream));
-        launch_contact_fp64(stream, N, P, C, dMats, dPar, dStep, dFlags + 1);
+        if (prec == WG_PREC_FP32) launch_contact_fp32(stream, N, P, C, I, dMats, dPar, dStep, dFlags + 1);
+        else launch_contact_fp64(stream, N, P, C, I, dMats, dPar, dStep, dFlags + 1);
         WG_CUDA_TRY(cudaEventRecord(ev[4], stream));
-        launch_reduce(stream, N, P, C, I, dPar, dStep);
+        if (prec == WG_PREC_FP32) launch_reduce32(stream, N, P, C, I, dPar, dStep);
+        else launch_reduce(stream, N, P, C, I, dPar, dStep);
         launches += 3 + (I.nHeavy > 0);
         WG_CUDA_TRY(cudaEventRecord(ev[5], stream));
         WG_CUDA_TRY(cudaGetLastError());
@@ -752,12 +783,68 @@ static int collectContacts(Sim& S, std::vector<int64_t>& keep, std::vector<uint6
                            std::vector<int32_t>& cd, std::vector<std::vector<double>>& cols) {
     const int64_t n = S.C.n;
     key.resize(n); fl.resize(n); cd.resize(n);
-    cols.assign(CC_NCOL, std::vector<double>(n));
+    cols.assign(CC_NCOL + 3, std::vector<double>(n, 0.));  // + global force on pA
+    if (n > 0) {
+        // global force on pA from the end slots (pB's slot negated where pA is a facet)
+        std::vector<int32_t> sLo(n), sHi(n);
+        WG_CUDA_TRY(cudaMemcpy(sLo.data(), S.I.slotLo, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+        WG_CUDA_TRY(cudaMemcpy(sHi.data(), S.I.slotHi, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+        std::vector<uint32_t> flc(n);
+        std::vector<uint64_t> kc(n);
+        WG_CUDA_TRY(cudaMemcpy(flc.data(), S.C.flags, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
+        WG_CUDA_TRY(cudaMemcpy(kc.data(), S.C.key, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost));
+        const int64_t ne = 2 * n;
+        std::vector<double> ef(4 * ne);
+        if (S.prec == WG_PREC_FP32) {
+            std::vector<float> tmp(4 * ne);
+            WG_CUDA_TRY(cudaMemcpy(tmp.data(), S.I.endFf, sizeof(float4) * ne, cudaMemcpyDeviceToHost));
+            for (int64_t q = 0; q < 4 * ne; q++) ef[q] = tmp[q];
+        } else {
+            WG_CUDA_TRY(cudaMemcpy(ef.data(), S.I.endF, sizeof(double4_32a) * ne, cudaMemcpyDeviceToHost));
+        }
+        for (int64_t c = 0; c < n; c++) {
+            const bool aIsLo = !(flc[c] & C_SWAP);
+            const bool facetA = ctype(flc[c]) == CT_FS;
+            const int32_t slot = facetA ? (aIsLo ? sHi[c] : sLo[c]) : (aIsLo ? sLo[c] : sHi[c]);
+            const double sg = facetA ? -1.0 : 1.0;
+            for (int k = 0; k < 3; k++) cols[CC_NCOL + k][c] = sg * ef[4 * slot + k] + 0.0;
+        }
+    }
     if (n > 0) {
         WG_CUDA_TRY(cudaMemcpy(key.data(), S.C.key, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost));
         WG_CUDA_TRY(cudaMemcpy(fl.data(), S.C.flags, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
         WG_CUDA_TRY(cudaMemcpy(cd.data(), S.C.cdist, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
-        for (int q = 0; q < CC_NCOL; q++) WG_CUDA_TRY(cudaMemcpy(cols[q].data(), S.C.col[q], sizeof(double) * n, cudaMemcpyDeviceToHost));
+        if (S.prec == WG_PREC_FP64) {
+            for (int q = 0; q < CC_NCOL; q++) WG_CUDA_TRY(cudaMemcpy(cols[q].data(), S.C.col[q], sizeof(double) * n, cudaMemcpyDeviceToHost));
+        } else {
+            // FP32-force mode: map the FP32 columns onto the FP64 listing layout
+            std::vector<std::vector<float>> fc(CF_NCOL, std::vector<float>(n));
+            for (int q = 0; q < CF_NCOL; q++) WG_CUDA_TRY(cudaMemcpy(fc[q].data(), S.C.fcol[q], sizeof(float) * n, cudaMemcpyDeviceToHost));
+            std::vector<double> cp[3];
+            for (int k = 0; k < 3; k++) {
+                cp[k].resize(n);
+                WG_CUDA_TRY(cudaMemcpy(cp[k].data(), S.C.col[CC_CPX + k], sizeof(double) * n, cudaMemcpyDeviceToHost));
+            }
+            std::vector<double4_32a> pos(S.nPar);
+            WG_CUDA_TRY(cudaMemcpy(pos.data(), S.N.posr, sizeof(double4_32a) * S.nPar, cudaMemcpyDeviceToHost));
+            for (int64_t c = 0; c < n; c++) {
+                const int map[] = {CF_T0X, CF_T0Y, CF_T0Z, CF_T1X, CF_T1Y, CF_T1Z};
+                for (int q = 0; q < 6; q++) cols[CC_T0X + q][c] = fc[map[q]][c];
+                cols[CC_FN][c] = fc[CF_FN][c];
+                cols[CC_FT1][c] = fc[CF_FT1][c];
+                cols[CC_FT2][c] = fc[CF_FT2][c];
+                if (ctype(fl[c]) == CT_SS) {
+                    // contact point = x_A + (r_A + uN/2) n (Sphere.cpp:103)
+                    const int a = (fl[c] & C_SWAP) ? (int)(key[c] & 0xffffffffu) : (int)(key[c] >> 32);
+                    const double s = pos[a].w + 0.5 * (double)fc[CF_UN][c];
+                    cols[CC_CPX][c] = pos[a].x + s * fc[CF_T0X][c];
+                    cols[CC_CPY][c] = pos[a].y + s * fc[CF_T0Y][c];
+                    cols[CC_CPZ][c] = pos[a].z + s * fc[CF_T0Z][c];
+                } else {
+                    for (int k = 0; k < 3; k++) cols[CC_CPX + k][c] = cp[k][c];
+                }
+            }
+        }
     }
     std::vector<double4_32a> mn(S.nPar), mx(S.nPar);
     if (S.nPar > 0) {
@@ -812,7 +899,7 @@ int wg_get_contacts(wg_scene* s, int32_t* id_lo, int32_t* id_hi, int32_t* id_a, 
         unpackCellDist(cd[c], a, b, cc);
         if (cell_dist) { cell_dist[3 * i] = a; cell_dist[3 * i + 1] = b; cell_dist[3 * i + 2] = cc; }
         for (int k = 0; k < 3; k++) {
-            if (fglob) fglob[3 * i + k] = isReal ? cols[CC_FGX + k][c] : 0.;
+            if (fglob) fglob[3 * i + k] = isReal ? cols[CC_NCOL + k][c] : 0.;
             if (local) local[3 * i + k] = isReal ? cols[CC_FN + k][c] : 0.;
             if (cpt) cpt[3 * i + k] = isReal ? cols[CC_CPX + k][c] : 0.;
         }
@@ -839,6 +926,11 @@ int wg_get_aabbs(wg_scene* s, double* mn, double* mx) {
         mx[3 * i] = b[i].x; mx[3 * i + 1] = b[i].y; mx[3 * i + 2] = b[i].z;
     }
     return WG_OK;
+}
+
+int wg_profiler(int on) {
+    cudaError_t e = on ? cudaProfilerStart() : cudaProfilerStop();
+    return e == cudaSuccess ? WG_OK : WG_ERR_CUDA;
 }
 
 void* wg_host_alloc(int64_t bytes) {

@@ -60,7 +60,7 @@ struct CollideWork {
     uint64_t* orphKey = nullptr;
     int32_t* orphSrc = nullptr;
     int32_t* src = nullptr;
-    int64_t mergeCap = 0;
+    int64_t mergeCap = 0, orphCap = 0, srcCap = 0;
     uint32_t* hiKeys = nullptr;
     uint32_t* hiKeysSorted = nullptr;
     int32_t* hiVals = nullptr;
@@ -392,7 +392,11 @@ __global__ void k_gather(DevContacts Cold, DevContacts Cnew, const int32_t* __re
         Cnew.step0[i] = Cold.step0[s];
         Cnew.cdist[i] = Cold.cdist[s];
 #pragma unroll
-        for (int q = 0; q < CC_NCOL; q++) Cnew.col[q][i] = Cold.col[q][s];
+        for (int q = 0; q < CC_NCOL; q++)
+            if (Cnew.col[q]) Cnew.col[q][i] = Cold.col[q][s];
+#pragma unroll
+        for (int q = 0; q < CF_NCOL; q++)
+            if (Cnew.fcol[q]) Cnew.fcol[q][i] = Cold.fcol[q][s];
     } else {
         const uint64_t k = Cnew.key[i];
         const int lo = (int)(k >> 32), hi = (int)(k & 0xffffffffu);
@@ -411,7 +415,11 @@ __global__ void k_gather(DevContacts Cold, DevContacts Cnew, const int32_t* __re
         Cnew.step0[i] = (int32_t)(*dStep);
         Cnew.cdist[i] = packCellDist(0, 0, 0);
 #pragma unroll
-        for (int q = 0; q < CC_NCOL; q++) Cnew.col[q][i] = 0.;
+        for (int q = 0; q < CC_NCOL; q++)
+            if (Cnew.col[q]) Cnew.col[q][i] = 0.;
+#pragma unroll
+        for (int q = 0; q < CF_NCOL; q++)
+            if (Cnew.fcol[q]) Cnew.fcol[q][i] = 0.f;
     }
 }
 
@@ -432,6 +440,18 @@ __global__ void k_hi_start(const uint32_t* __restrict__ hks, int64_t n, int nPar
     if (p > nPar) return;
     hiStart[p] = (int32_t)lowerBound32(hks, n, (uint32_t)p);
 }
+// end slots: contact c with hi==p sits at loStart[p] + (its index k in hiList); with lo==p at
+// hiStart[p+1] + c (see DevIncidence)
+__global__ void k_slots(const uint64_t* __restrict__ key, int64_t n, DevIncidence I) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int32_t ch = I.hiList[k];
+    const int hiP = (int)(key[ch] & 0xffffffffu);
+    I.slotHi[ch] = I.loStart[hiP] + (int32_t)k;
+    const int loP = (int)(key[k] >> 32);
+    I.slotLo[k] = I.hiStart[loP + 1] + (int32_t)k;
+}
+
 __global__ void k_heavy(DevIncidence I, DevParticles P, int threshold, int32_t* __restrict__ count) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= P.n) return;
@@ -667,11 +687,13 @@ int collide_full_run(Sim& S) {
         WG_CUDA_TRY(cudaStreamSynchronize(st));
         nOrph = (int64_t)last[0] + last[1];
         if (nOrph > 0) {
-            int64_t c1 = 0, c2 = 0;
-            if (W.orphKey) S.dfree(W.orphKey);
-            if (W.orphSrc) S.dfree(W.orphSrc);
-            W.orphKey = grow(S, (uint64_t*)nullptr, c1, nOrph);
-            W.orphSrc = grow(S, (int32_t*)nullptr, c2, nOrph);
+            if (nOrph > W.orphCap) {
+                int64_t c1 = W.orphCap, c2 = W.orphCap;
+                W.orphKey = grow(S, W.orphKey, c1, nOrph);
+                W.orphSrc = grow(S, W.orphSrc, c2, nOrph);
+                W.orphCap = c1;
+                if (!W.orphKey || !W.orphSrc) return S.fail(WG_ERR_CUDA, "out of device memory (merge)");
+            }
             k_compact_orphans<<<(unsigned)((nOld + BS - 1) / BS), BS, 0, st>>>(S.C, flagsArr, scanArr, W.orphKey, W.orphSrc);
         }
     }
@@ -679,9 +701,8 @@ int collide_full_run(Sim& S) {
     const int64_t nOut = nNew + nOrph;
     int r = S.ensureContactCapacity(nOut);
     if (r) return r;
-    int64_t srcCap = 0;
-    if (W.src) S.dfree(W.src);
-    W.src = grow(S, (int32_t*)nullptr, srcCap, std::max<int64_t>(nOut, 1));
+    W.src = grow(S, W.src, W.srcCap, std::max<int64_t>(nOut, 1));
+    if (!W.src) return S.fail(WG_ERR_CUDA, "out of device memory (merge)");
     S.Cb.n = nOut;
     if (nNew > 0)
         k_place_new<<<(unsigned)((nNew + BS - 1) / BS), BS, 0, st>>>(W.pairsSorted, nNew, W.orphKey, nOrph, S.C.key, nOld, S.Cb.key,
@@ -695,13 +716,33 @@ int collide_full_run(Sim& S) {
     const int64_t n = S.C.n;
     k_lo_start<<<(unsigned)((S.nPar + 1 + BS - 1) / BS), BS, 0, st>>>(S.C.key, n, (int)S.nPar, S.I.loStart);
     if (W.hiCap < std::max<int64_t>(n, 1)) {
-        if (W.hiKeys) { S.dfree(W.hiKeys); S.dfree(W.hiKeysSorted); S.dfree(W.hiVals); S.dfree(S.I.hiList); }
+        if (W.hiKeys) {
+            S.dfree(W.hiKeys); S.dfree(W.hiKeysSorted); S.dfree(W.hiVals); S.dfree(S.I.hiList);
+            S.dfree(S.I.slotLo); S.dfree(S.I.slotHi);
+        }
         W.hiCap = std::max<int64_t>(n, 1) * 3 / 2 + 1024;
         W.hiKeys = (uint32_t*)S.dalloc(sizeof(uint32_t) * W.hiCap);
         W.hiKeysSorted = (uint32_t*)S.dalloc(sizeof(uint32_t) * W.hiCap);
         W.hiVals = (int32_t*)S.dalloc(sizeof(int32_t) * W.hiCap);
         S.I.hiList = (int32_t*)S.dalloc(sizeof(int32_t) * W.hiCap);
-        if (!S.I.hiList) return S.fail(WG_ERR_CUDA, "out of device memory (incidence)");
+        S.I.slotLo = (int32_t*)S.dalloc(sizeof(int32_t) * W.hiCap);
+        S.I.slotHi = (int32_t*)S.dalloc(sizeof(int32_t) * W.hiCap);
+        if (!S.I.slotHi) return S.fail(WG_ERR_CUDA, "out of device memory (incidence)");
+    }
+    if (S.I.endCap < 2 * std::max<int64_t>(n, 1)) {
+        if (S.I.endF) { S.dfree(S.I.endF); S.dfree(S.I.endT); }
+        if (S.I.endFf) { S.dfree(S.I.endFf); S.dfree(S.I.endTf); }
+        S.I.endF = nullptr; S.I.endT = nullptr; S.I.endFf = nullptr; S.I.endTf = nullptr;
+        S.I.endCap = 2 * std::max<int64_t>(n, 1) * 3 / 2 + 2048;
+        if (S.prec == WG_PREC_FP32) {
+            S.I.endFf = (float4*)S.dalloc(sizeof(float4) * S.I.endCap);
+            S.I.endTf = (float4*)S.dalloc(sizeof(float4) * S.I.endCap);
+            if (!S.I.endTf) return S.fail(WG_ERR_CUDA, "out of device memory (contact ends)");
+        } else {
+            S.I.endF = (double4_32a*)S.dalloc(sizeof(double4_32a) * S.I.endCap);
+            S.I.endT = (double4_32a*)S.dalloc(sizeof(double4_32a) * S.I.endCap);
+            if (!S.I.endT) return S.fail(WG_ERR_CUDA, "out of device memory (contact ends)");
+        }
     }
     if (n > 0) {
         k_hi_keys<<<(unsigned)((n + BS - 1) / BS), BS, 0, st>>>(S.C.key, n, W.hiKeys, W.hiVals);
@@ -712,6 +753,10 @@ int collide_full_run(Sim& S) {
         WG_CUDA_TRY(cub::DeviceRadixSort::SortPairs(W.cubTmp, tb, W.hiKeys, W.hiKeysSorted, W.hiVals, S.I.hiList, n, 0, idBits, st));
     }
     k_hi_start<<<(unsigned)((S.nPar + 1 + BS - 1) / BS), BS, 0, st>>>(W.hiKeysSorted, n, (int)S.nPar, S.I.hiStart);
+    if (n > 0) k_slots<<<(unsigned)((n + BS - 1) / BS), BS, 0, st>>>(S.C.key, n, S.I);
+    // every end starts without a contribution; the contact kernel fills the real ones this step
+    if (S.prec == WG_PREC_FP32) WG_CUDA_TRY(cudaMemsetAsync(S.I.endFf, 0, sizeof(float4) * 2 * std::max<int64_t>(n, 1), st));
+    else WG_CUDA_TRY(cudaMemsetAsync(S.I.endF, 0, sizeof(double4_32a) * 2 * std::max<int64_t>(n, 1), st));
     // heavy particles
     if (!W.heavyCount) {
         W.heavyCount = (int32_t*)S.dalloc(sizeof(int32_t));

@@ -75,8 +75,16 @@ enum {
     CC_CPX, CC_CPY, CC_CPZ,                          // L6Geom node position (contact point)
     CC_P0, CC_P1, CC_P2, CC_P3, CC_P4,               // FrictPhys kn kt tanPhi | HertzPhys kn0 kt0 tanPhi alpha_sqrtMK R
     CC_FN, CC_FT1, CC_FT2,                           // phys.force (local)
-    CC_FGX, CC_FGY, CC_FGZ,                          // force on pA in global coordinates
     CC_NCOL
+};
+// FP32-force mode columns (the FP64 columns CC_FT1/CC_FT2 keep the IdealElPl shear force and
+// CC_CPX..Z the contact point of facet and wall contacts in that mode)
+enum {
+    CF_T0X, CF_T0Y, CF_T0Z, CF_T1X, CF_T1Y, CF_T1Z,  // trsf columns 0 and 1
+    CF_UN,                                           // L6Geom.uN of the last step
+    CF_P0, CF_P1, CF_P2, CF_P3,                      // FrictPhys kn kt tanPhi | HertzPhys kn0 kt0 tanPhi alpha_sqrtMK
+    CF_FN, CF_FT1, CF_FT2,                           // phys.force (local), for reporting
+    CF_NCOL
 };
 struct DevContacts {
     int64_t n;
@@ -84,13 +92,26 @@ struct DevContacts {
     uint32_t* flags;
     int32_t* step0;   // Contact.stepCreated
     int32_t* cdist;   // Contact.cellDist for (lo,hi), packed 3x10 bits
-    double* col[CC_NCOL];
+    double* col[CC_NCOL];   // columns not used by the precision mode are null
+    float* fcol[CF_NCOL];
 };
-// CSR incidence for the deterministic per-particle force sum
+// CSR incidence for the deterministic per-particle force sum.
+// Particle p owns the end slots [hiStart[p]+loStart[p], hiStart[p+1]+loStart[p+1]): first its
+// contacts with lower-id partners (ascending), then those with higher-id partners (ascending),
+// i.e. the order in which the reference's deterministic pass over key-sorted contacts adds them
+// (ContactLoop.cpp:250-257). The contact kernel stores each end's force and torque in its slot;
+// the force sum reads each particle's slots as one contiguous run.
 struct DevIncidence {
     int32_t* loStart;  // nPar+1: contacts with lo==p are [loStart[p], loStart[p+1])
     int32_t* hiStart;  // nPar+1: hiList[hiStart[p] .. hiStart[p+1]) are contacts with hi==p, ascending
     int32_t* hiList;
+    int32_t* slotLo;   // per contact: end slot of its lo particle
+    int32_t* slotHi;   // per contact: end slot of its hi particle
+    double4_32a* endF; // FP64 mode: force on the particle (xyz) and a contribution flag (w)
+    double4_32a* endT; // FP64 mode: torque on the particle about its node
+    float4* endFf;     // FP32-force mode: the same in FP32
+    float4* endTf;
+    int64_t endCap;
     int32_t* heavy;    // particles whose degree exceeds the serial threshold
     int32_t nHeavy;
 };
@@ -107,9 +128,16 @@ __host__ __device__ inline void unpackCellDist(int32_t p, int& a, int& b, int& c
 // ------------------------------------------------------------------ launchers (wg_step.cu)
 void launch_leapfrog(cudaStream_t st, const DevNodes& N, const DevParticles& P, const ScenePar* sp, int* dFull);
 void launch_contact_fp64(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C,
-                         const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dErr);
+                         const DevIncidence& I, const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dErr);
 void launch_reduce(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C,
                    const DevIncidence& I, const ScenePar* sp, long long* dStep);
+// FP32-force mode (wg_step32.cu)
+void launch_leapfrog32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const double4_32a* invm, const ScenePar* sp,
+                       int* dFull);
+void launch_contact_fp32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C,
+                         const DevIncidence& I, const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dErr);
+void launch_reduce32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C,
+                     const DevIncidence& I, const ScenePar* sp, long long* dStep);
 
 // ------------------------------------------------------------------ broad phase (wg_collide.cu)
 struct Grid {
@@ -153,6 +181,8 @@ struct Sim {
     DevIncidence I{};
     int64_t cCap = 0;
     double4_32a* dMats = nullptr;
+    double4_32a* dInvM = nullptr;  // 1/Ix 1/Iy 1/Iz 1/m per node slot (FP32-force mode)
+    int prec = 0;                  // WG_PREC_*
     ScenePar hPar{};
     ScenePar* dPar = nullptr;
     long long* dStep = nullptr;

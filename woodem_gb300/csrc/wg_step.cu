@@ -4,12 +4,9 @@
 // Compiled with --fmad=false: every floating-point result is the correctly rounded
 // value of the operation sequence written here, which is the operation sequence of
 // the reference expression cited beside it.
-#include "wg_internal.h"
-#include "wg_math.cuh"
+#include "wg_geom.cuh"
 
 namespace wg {
-
-__device__ __forceinline__ D3 ld3(const double4_32a& v) { return D3{v.x, v.y, v.z}; }
 __device__ __forceinline__ double4_32a st4(D3 a, double w) { return make_double4_32a(a.x, a.y, a.z, w); }
 __device__ __forceinline__ DM3 ldm(const double* m) {
     DM3 r;
@@ -134,150 +131,20 @@ void launch_leapfrog(cudaStream_t st, const DevNodes& N, const DevParticles& P, 
 }
 
 // ---------------------------------------------------------------------------------- ContactLoop
-struct Geo {
-    D3 pos1, vel1, angVel1, pos2, vel2, angVel2, normal, contPt;
-    double uN, r1, r2;
-};
-
-// Cg2_Sphere_Sphere_L6Geom::go, pkg/dem/Sphere.cpp:88-109
-__device__ __forceinline__ bool geomSS(const DevNodes& N, int A, int B, D3 shift2, bool real, double ssDf, Geo& g) {
-    const double4_32a pa = N.posr[A], pb = N.posr[B];
-    const double r1 = pa.w, r2 = pb.w;
-    const D3 p1 = ld3(pa), p2 = ld3(pb);
-    const D3 relPos = (p2 + shift2) - p1;
-    const double dfr = fabs(ssDf) * (r1 + r2);
-    const double unDistSq = sqn(relPos) - dfr * dfr;
-    if (unDistSq > 0 && !real) return false;
-    const double dist = sqrt(sqn(relPos));
-    g.uN = dist - (r1 + r2);
-    g.normal = relPos / dist;
-    g.contPt = p1 + (r1 + 0.5 * g.uN) * g.normal;
-    g.pos1 = p1;
-    g.vel1 = ld3(N.vel[A]);
-    g.angVel1 = ld3(N.angv[A]);
-    g.pos2 = p2 + shift2;
-    g.vel2 = ld3(N.vel[B]);
-    g.angVel2 = ld3(N.angv[B]);
-    g.r1 = r1;
-    g.r2 = r2;
-    return true;
-}
-
-// Cg2_Wall_Sphere_L6Geom::go, pkg/dem/Wall.cpp:45-79
-__device__ __forceinline__ bool geomWS(const DevNodes& N, const DevParticles& P, const DevContacts& C, int64_t c, int A,
-                                       int B, D3 shift2, bool real, Geo& g) {
-    const int4 aux = P.aux[A];
-    const int ax = aux.x, sense = aux.y;
-    const double4_32a pw = N.posr[A], ps = N.posr[B];
-    const double radius = ps.w;
-    const D3 wallPos = ld3(pw);
-    const D3 spherePos = ld3(ps) + shift2;
-    const double dist = comp(spherePos, ax) - comp(wallPos, ax);
-    if (!real && fabs(dist) > radius) return false;
-    D3 contPt = spherePos;
-    setComp(contPt, ax, comp(wallPos, ax));
-    D3 normal{0, 0, 0};
-    if (sense == 0) {
-        if (!real) setComp(normal, ax, dist > 0 ? 1. : -1.);
-        else setComp(normal, ax, C.col[CC_T0X + ax][c]);
-    } else setComp(normal, ax, sense == 1 ? 1. : -1);
-    g.uN = comp(normal, ax) * dist - radius;
-    g.normal = normal;
-    g.contPt = contPt;
-    g.pos1 = wallPos;
-    g.vel1 = ld3(N.vel[A]);
-    g.angVel1 = ld3(N.angv[A]);
-    g.pos2 = spherePos;
-    g.vel2 = ld3(N.vel[B]);
-    g.angVel2 = ld3(N.angv[B]);
-    g.r1 = -radius;
-    g.r2 = radius;
-    return true;
-}
-
-// CompUtils::closestSegmentPt, lib/base/CompUtils.cpp:57-63
-__device__ __forceinline__ D3 closestSegmentPt(D3 P, D3 A, D3 B) {
-    const D3 BA = B - A;
-    if (sqn(BA) == 0.) return A;
-    const double u = (dot(P, BA) - dot(A, BA)) / sqn(BA);
-    return A + smin(1., smax(0., u)) * BA;
-}
-
-// Cg2_Facet_Sphere_L6Geom::go, pkg/dem/Facet.cpp:235-288 with Facet::interpolatePtLinAngVel :158-174
-// and CompUtils::triangleBarycentrics lib/base/CompUtils.cpp:92-110
-__device__ __forceinline__ bool geomFS(const DevNodes& N, const DevParticles& P, int A, int B, D3 shift2, bool real, Geo& g,
-                                       int* dErr) {
-    const int4 fn = P.aux[A];
-    const double4_32a fd = P.facet[A];
-    const double halfThick = fd.w;
-    const D3 fakeVel{fd.x, fd.y, fd.z};
-    const double4_32a ps = N.posr[B];
-    const double radius = ps.w;
-    const D3 sC = ld3(ps) + shift2;
-    const D3 p0 = ld3(N.posr[fn.x]), p1 = ld3(N.posr[fn.y]), p2 = ld3(N.posr[fn.z]);
-    const D3 nn = cross(p1 - p0, p2 - p0);
-    const D3 fNormal = normalized(nn);
-    const double planeDist = dot(sC - p0, fNormal);
-    if (fabs(planeDist) > (radius + halfThick) && !real) return false;
-    const D3 fC = sC - planeDist * fNormal;
-    const double l0 = dot(cross(p1 - p0, nn), fC - p0);
-    const double l1 = dot(cross(p2 - p1, nn), fC - p1);
-    const double l2 = dot(cross(p0 - p2, nn), fC - p2);
-    const int w = (l0 > 0 ? 1 : 0) + (l1 > 0 ? 2 : 0) + (l2 > 0 ? 4 : 0);
-    D3 contPt;
-    switch (w) {
-        case 0: contPt = fC; break;
-        case 1: contPt = closestSegmentPt(fC, p0, p1); break;
-        case 2: contPt = closestSegmentPt(fC, p1, p2); break;
-        case 4: contPt = closestSegmentPt(fC, p2, p0); break;
-        case 3: contPt = p1; break;
-        case 5: contPt = p0; break;
-        case 6: contPt = p2; break;
-        default: atomicCAS(dErr, 0, 100); return false;  // "Impossible sphere-facet intersection"
-    }
-    D3 normal = sC - contPt;
-    const double rh = radius + halfThick;
-    if (sqn(normal) > rh * rh && !real) return false;
-    const double dist = sqrt(sqn(normal));
-    normal = normal / dist;
-    if (halfThick > 0) contPt = contPt + normal * halfThick;
-    g.uN = (dist - radius) - halfThick;
-    // barycentric interpolation of the facet node velocities at contPt
-    const D3 vB = p1 - p0, vC = p2 - p0, vX = contPt - p0;
-    const double m00 = dot(vB, vB), m01 = dot(vC, vB), m10 = dot(vB, vC), m11 = dot(vC, vC);
-    const double det = m00 * m11 - m10 * m01;
-    const double invdet = 1. / det;
-    const double i00 = m11 * invdet, i10 = -m10 * invdet, i01 = -m01 * invdet, i11 = m00 * invdet;
-    const double b0 = dot(vX, vB), b1 = dot(vX, vC);
-    const double u = i00 * b0 + i01 * b1, v = i10 * b0 + i11 * b1;
-    const double a0 = (1 - u) - v;
-    const D3 v0 = ld3(N.vel[fn.x]), v1 = ld3(N.vel[fn.y]), v2 = ld3(N.vel[fn.z]);
-    D3 linVel = (a0 * v0 + u * v1) + v * v2;
-    const D3 angVel = (cross(p0 - contPt, v0) + cross(p1 - contPt, v1)) + cross(p2 - contPt, v2);
-    if (!isZero(fakeVel)) {
-        if (!isnan(fakeVel.x)) linVel = linVel + fakeVel;
-        else linVel = dot(linVel, fNormal) * fNormal;
-    }
-    g.normal = normal;
-    g.contPt = contPt;
-    g.pos1 = contPt;
-    g.vel1 = linVel;
-    g.angVel1 = angVel;
-    g.pos2 = sC;
-    g.vel2 = ld3(N.vel[B]);
-    g.angVel2 = ld3(N.angv[B]);
-    g.r1 = smax(halfThick, radius);
-    g.r2 = radius;
-    return true;
-}
-
 // Fused ContactLoop body (pkg/dem/ContactLoop.cpp:135-224) for one contact:
 // Cg2 (above) -> Cg2_Any_Any_L6Geom__Base::handleSpheresLikeContact (pkg/dem/L6Geom.cpp:51-217)
 // -> Cp2 on creation (FrictMat.cpp:20-44 / Hertz.cpp:9-50) -> Law2 (IdealElPl.cpp:12-122 /
 // Hertz.cpp:58-182) -> global force on pA (Contact::getForceTorqueBranch, Contact.cpp:24-34).
-__global__ void __launch_bounds__(128) k_contact_fp64(DevNodes N, DevParticles P, DevContacts C, const double4_32a* __restrict__ mats,
-                                                     const ScenePar* __restrict__ spp, const long long* __restrict__ dStep,
-                                                     int* __restrict__ dErr) {
+// Clear the end slots of a contact that stops being real (its last contribution must vanish).
+__device__ __forceinline__ void clearEnds(const DevIncidence& I, int64_t c) {
+    const double4_32a z = make_double4_32a(0., 0., 0., 0.);
+    I.endF[I.slotLo[c]] = z;
+    I.endF[I.slotHi[c]] = z;
+}
+
+__global__ void __launch_bounds__(128) k_contact_fp64(DevNodes N, DevParticles P, DevContacts C, DevIncidence I,
+                                                     const double4_32a* __restrict__ mats, const ScenePar* __restrict__ spp,
+                                                     const long long* __restrict__ dStep, int* __restrict__ dErr) {
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= C.n) return;
     const ScenePar& sp = *spp;
@@ -303,7 +170,7 @@ __global__ void __launch_bounds__(128) k_contact_fp64(DevNodes N, DevParticles P
     Geo g;
     bool touch;
     if (ty == CT_SS) touch = geomSS(N, A, B, shift2, real, sp.ssDistFactor, g);
-    else if (ty == CT_WS) touch = geomWS(N, P, C, c, A, B, shift2, real, g);
+    else if (ty == CT_WS) touch = geomWS(N, P, real ? C.col[CC_T0X + P.aux[A].x][c] : 0., A, B, shift2, real, g);
     else touch = geomFS(N, P, A, B, shift2, real, g, dErr);
     if (!touch) {
         C.flags[c] = fl;
@@ -467,10 +334,30 @@ __global__ void __launch_bounds__(128) k_contact_fp64(DevNodes N, DevParticles P
     if (!keep) {
         // ContactContainer::requestRemoval: geom and phys reset, contact pending for the collider
         C.flags[c] = (fl & ~C_REAL) | C_PENDING;
+        if (real) clearEnds(I, c);
         return;
     }
     const DQ ori = quatFromCols(c0, c1, c2);
     const D3 Fg = qrot(ori, D3{fn, ft1, ft2});
+    // Contact::getForceTorqueBranch + applyForceUninodal (Contact.cpp:24-34, ContactLoop.cpp:261-267):
+    // F = ori*force*sign, torque = xc x F + T with xc = contact point - (node + shift for pB)
+    {
+        const bool aIsLo = !(fl & C_SWAP);
+        if (ty != CT_FS) {  // facets are multinodal: no force is applied to them here
+            const D3 FA = Fg * 1.0;
+            const D3 xcA = g.contPt - ld3(N.posr[A]);
+            const D3 TA = cross(xcA, FA) + D3{0, 0, 0};
+            const int sA = aIsLo ? I.slotLo[c] : I.slotHi[c];
+            I.endF[sA] = make_double4_32a(FA.x, FA.y, FA.z, 1.);
+            I.endT[sA] = make_double4_32a(TA.x, TA.y, TA.z, 0.);
+        }
+        const D3 FB = Fg * -1.0;
+        const D3 xcB = g.contPt - (ld3(N.posr[B]) + (sp.periodic ? shift2 : D3{0, 0, 0}));
+        const D3 TB = cross(xcB, FB) + D3{0, 0, 0};
+        const int sB = aIsLo ? I.slotHi[c] : I.slotLo[c];
+        I.endF[sB] = make_double4_32a(FB.x, FB.y, FB.z, 1.);
+        I.endT[sB] = make_double4_32a(TB.x, TB.y, TB.z, 0.);
+    }
     C.col[CC_T0X][c] = c0.x;
     C.col[CC_T0Y][c] = c0.y;
     C.col[CC_T0Z][c] = c0.z;
@@ -483,50 +370,22 @@ __global__ void __launch_bounds__(128) k_contact_fp64(DevNodes N, DevParticles P
     C.col[CC_FN][c] = fn;
     C.col[CC_FT1][c] = ft1;
     C.col[CC_FT2][c] = ft2;
-    C.col[CC_FGX][c] = Fg.x;
-    C.col[CC_FGY][c] = Fg.y;
-    C.col[CC_FGZ][c] = Fg.z;
     C.flags[c] = fl | C_REAL;
 }
 
-void launch_contact_fp64(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C, const double4_32a* mats,
-                         const ScenePar* sp, const long long* dStep, int* dErr) {
+void launch_contact_fp64(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C, const DevIncidence& I,
+                         const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dErr) {
     if (C.n == 0) return;
     const int bs = 128;
-    k_contact_fp64<<<(unsigned)((C.n + bs - 1) / bs), bs, 0, st>>>(N, P, C, mats, sp, dStep, dErr);
+    k_contact_fp64<<<(unsigned)((C.n + bs - 1) / bs), bs, 0, st>>>(N, P, C, I, mats, sp, dStep, dErr);
 }
 
 // ---------------------------------------------------------------------------------- force sum
-// Per-particle sum replacing ContactLoop::applyForceUninodal + DemData::addForceTorque
-// (pkg/dem/ContactLoop.cpp:261-267, Contact.cpp:24-34, Particle.hpp:221) and the force reset
-// of Leapfrog (Leapfrog.cpp:240-245). Contributions are added in ascending order of the
-// other particle's id, which is the order of the reference's deterministic serial pass over
-// contacts sorted by (lo,hi) (ContactLoop.cpp:250-257).
-__device__ __forceinline__ void addContribution(const DevNodes& N, const DevContacts& C, const ScenePar& sp, int64_t c, int p,
-                                                D3 pos, D3& F, D3& T) {
-    const uint32_t fl = C.flags[c];
-    if (!(fl & C_REAL)) return;
-    const uint64_t key = C.key[c];
-    const int lo = (int)(key >> 32);
-    const int A = (fl & C_SWAP) ? (int)(key & 0xffffffffu) : lo;
-    const bool isPA = (A == p);
-    const double sign = isPA ? 1 : -1;
-    const D3 Fp = D3{C.col[CC_FGX][c], C.col[CC_FGY][c], C.col[CC_FGZ][c]} * sign;
-    D3 shift{0, 0, 0};
-    if (!isPA && sp.periodic) {
-        int a, b, cc;
-        unpackCellDist(C.cdist[c], a, b, cc);
-        if (fl & C_SWAP) { a = -a; b = -b; cc = -cc; }
-        shift = mul(ldm(sp.hSize), D3{(double)a, (double)b, (double)cc});
-    }
-    const D3 xc = D3{C.col[CC_CPX][c], C.col[CC_CPY][c], C.col[CC_CPZ][c]} - (pos + shift);
-    const D3 tq = cross(xc, Fp) + D3{0, 0, 0};
-    F = F + Fp;
-    T = T + tq;
-}
-
-__global__ void k_reduce(DevNodes N, DevParticles P, DevContacts C, DevIncidence I, const ScenePar* __restrict__ spp,
-                         int heavyThreshold) {
+// Per-particle sum replacing DemData::addForceTorque (pkg/dem/Particle.hpp:221) in the serial
+// deterministic pass (ContactLoop.cpp:250-257), with the force reset of Leapfrog
+// (Leapfrog.cpp:240-245): F = m*g, T = 0, then every contributing end slot of the particle in
+// slot order (ascending id of the other particle).
+__global__ void k_reduce(DevNodes N, DevParticles P, DevIncidence I, const ScenePar* __restrict__ spp, int heavyThreshold) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= P.n) return;
     const int sh = P.shape[p];
@@ -537,11 +396,15 @@ __global__ void k_reduce(DevNodes N, DevParticles P, DevContacts C, DevIncidence
     D3 F{0, 0, 0}, T{0, 0, 0};
     if (sp.hasGravity && !(flags & F_GRAVITY_SKIP)) F = mass * D3{sp.g[0], sp.g[1], sp.g[2]};
     if (sp.applyForces) {
-        const int h0 = I.hiStart[p], h1 = I.hiStart[p + 1], l0 = I.loStart[p], l1 = I.loStart[p + 1];
-        if ((h1 - h0) + (l1 - l0) > heavyThreshold) return;  // summed by k_reduce_heavy
-        const D3 pos = ld3(N.posr[p]);
-        for (int k = h0; k < h1; k++) addContribution(N, C, sp, I.hiList[k], p, pos, F, T);
-        for (int k = l0; k < l1; k++) addContribution(N, C, sp, k, p, pos, F, T);
+        const int e0 = I.hiStart[p] + I.loStart[p], e1 = I.hiStart[p + 1] + I.loStart[p + 1];
+        if (e1 - e0 > heavyThreshold) return;  // summed by k_reduce_heavy
+        for (int e = e0; e < e1; e++) {
+            const double4_32a f = I.endF[e];
+            if (f.w == 0.) continue;
+            const double4_32a t = I.endT[e];
+            F = F + D3{f.x, f.y, f.z};
+            T = T + D3{t.x, t.y, t.z};
+        }
     }
     N.force[p] = st4(F, 0.);
     N.torque[p] = st4(T, 0.);
@@ -550,16 +413,17 @@ __global__ void k_reduce(DevNodes N, DevParticles P, DevContacts C, DevIncidence
 // Particles with many contacts (walls): one block each, fixed-shape tree sum (deterministic,
 // same result on every run; rounding differs from the serial order only for these particles,
 // whose DOFs are blocked in every supported scene).
-__global__ void k_reduce_heavy(DevNodes N, DevParticles P, DevContacts C, DevIncidence I, const ScenePar* __restrict__ spp) {
+__global__ void k_reduce_heavy(DevNodes N, DevIncidence I, const ScenePar* __restrict__ spp) {
     const int p = I.heavy[blockIdx.x];
     const ScenePar& sp = *spp;
-    const int h0 = I.hiStart[p], h1 = I.hiStart[p + 1], l0 = I.loStart[p], l1 = I.loStart[p + 1];
-    const int nh = h1 - h0, n = nh + (l1 - l0);
-    const D3 pos = ld3(N.posr[p]);
+    const int e0 = I.hiStart[p] + I.loStart[p], e1 = I.hiStart[p + 1] + I.loStart[p + 1];
     D3 F{0, 0, 0}, T{0, 0, 0};
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
-        const int64_t c = (k < nh) ? (int64_t)I.hiList[h0 + k] : (int64_t)(l0 + (k - nh));
-        addContribution(N, C, sp, c, p, pos, F, T);
+    for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+        const double4_32a f = I.endF[e];
+        if (f.w == 0.) continue;
+        const double4_32a t = I.endT[e];
+        F = F + D3{f.x, f.y, f.z};
+        T = T + D3{t.x, t.y, t.z};
     }
     __shared__ double sh[6][256];
     sh[0][threadIdx.x] = F.x; sh[1][threadIdx.x] = F.y; sh[2][threadIdx.x] = F.z;
@@ -587,8 +451,8 @@ static const int kHeavyThreshold = 64;
 void launch_reduce(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C, const DevIncidence& I,
                    const ScenePar* sp, long long* dStep) {
     if (P.n > 0) {
-        k_reduce<<<(P.n + 255) / 256, 256, 0, st>>>(N, P, C, I, sp, kHeavyThreshold);
-        if (I.nHeavy > 0) k_reduce_heavy<<<I.nHeavy, 256, 0, st>>>(N, P, C, I, sp);
+        k_reduce<<<(P.n + 255) / 256, 256, 0, st>>>(N, P, I, sp, kHeavyThreshold);
+        if (I.nHeavy > 0) k_reduce_heavy<<<I.nHeavy, 256, 0, st>>>(N, I, sp);
     }
     k_step_advance<<<1, 1, 0, st>>>(dStep);
 }

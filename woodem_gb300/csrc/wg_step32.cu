@@ -1,0 +1,467 @@
+// FP32-force mode: contact geometry and force laws in FP32; FP64 kept for the steps where
+// FP32 would lose the result -- the relative position of the two particles and the normal
+// overlap (a difference of nearly equal lengths), the relative velocity, the incremental
+// shear force of IdealElPl, the Leapfrog position/velocity update and the per-particle force
+// sum. The physics and its order of evaluation are those of the FP64 path (wg_step.cu), with
+// the sphere-sphere branch vectors written relative to the particle centres:
+//   contact point - x_A = (r1 + uN/2) n,   contact point - x_B' = -(r2 + uN/2) n
+// which is Cg2_Sphere_Sphere_L6Geom's contPt = x1 + (r1 + uN/2) n (pkg/dem/Sphere.cpp:103), so the
+// mid-step branches of L6Geom.cpp:156-160 need only the previous normal and uN.
+//
+// Compiled with --fmad=true (results are compared to the FP64 oracle within a tolerance).
+#include "wg_geom.cuh"
+
+namespace wg {
+
+struct F3 {
+    float x, y, z;
+};
+__device__ __forceinline__ F3 f3(float x, float y, float z) { return F3{x, y, z}; }
+__device__ __forceinline__ F3 toF(D3 a) { return F3{(float)a.x, (float)a.y, (float)a.z}; }
+__device__ __forceinline__ F3 operator+(F3 a, F3 b) { return F3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ F3 operator-(F3 a, F3 b) { return F3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ F3 operator-(F3 a) { return F3{-a.x, -a.y, -a.z}; }
+__device__ __forceinline__ F3 operator*(F3 a, float s) { return F3{a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ F3 operator*(float s, F3 a) { return F3{s * a.x, s * a.y, s * a.z}; }
+__device__ __forceinline__ float fdot(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ F3 fcross(F3 a, F3 b) { return F3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+__device__ __forceinline__ F3 fnormalized(F3 a) {
+    const float z = fdot(a, a);
+    return z > 0.f ? a * rsqrtf(z) : a;
+}
+
+// ---------------------------------------------------------------------------------- Leapfrog
+// Leapfrog::run (pkg/dem/Leapfrog.cpp:103-255) with precomputed 1/m and 1/I; the node
+// orientation (which no force of the supported shapes depends on) is advanced in FP32.
+__global__ void k_leapfrog32(DevNodes N, const double4_32a* __restrict__ invm, const int32_t* __restrict__ pshape, int nPar,
+                             const ScenePar* __restrict__ spp, int* __restrict__ dFull) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N.n) return;
+    const ScenePar& sp = *spp;
+    const uint32_t flags = N.flags[i];
+    if (flags & F_CLUMPED) return;
+    const double dt = sp.dt;
+    const double damping = sp.damping;
+    const bool damp = (damping != 0. && !(flags & F_DAMPING_SKIP));
+    const double4_32a pr = N.posr[i];
+    D3 pos = ld3(pr);
+    D3 vel = ld3(N.vel[i]);
+    D3 angVel = ld3(N.angv[i]);
+    const double4_32a iv = invm[i];
+    const double mass = N.minert[i].w;
+    const D3 f = ld3(N.force[i]);
+    const D3 t = ld3(N.torque[i]);
+    const bool blockedAll = (flags & F_DOF_ALL) == F_DOF_ALL;
+    const int homoDeform = sp.periodic ? sp.homoDeform : -1;
+    D3 linAccel{0, 0, 0};
+    if (!blockedAll) {
+        linAccel = D3{(flags & 1u) ? 0. : f.x * iv.w, (flags & 2u) ? 0. : f.y * iv.w, (flags & 4u) ? 0. : f.z * iv.w};
+        D3 pvf = vel, pva = angVel;
+        if (sp.periodic) {
+            if (homoDeform == 2 || homoDeform == 3) pvf = vel - mul(*(const DM3*)sp.gradV, pos);
+            else if (homoDeform == 4) pvf = vel - mul(*(const DM3*)sp.gradV, pos - (dt / 2) * vel);
+            if (homoDeform == 4) pva = angVel - D3{sp.spinVec[0], sp.spinVec[1], sp.spinVec[2]};
+        }
+        if (damp) {
+            linAccel.x *= 1 - damping * ((f.x * (pvf.x + 0.5 * dt * linAccel.x)) > 0 ? 1 : ((f.x * (pvf.x + 0.5 * dt * linAccel.x)) < 0 ? -1 : 0));
+            linAccel.y *= 1 - damping * ((f.y * (pvf.y + 0.5 * dt * linAccel.y)) > 0 ? 1 : ((f.y * (pvf.y + 0.5 * dt * linAccel.y)) < 0 ? -1 : 0));
+            linAccel.z *= 1 - damping * ((f.z * (pvf.z + 0.5 * dt * linAccel.z)) > 0 ? 1 : ((f.z * (pvf.z + 0.5 * dt * linAccel.z)) < 0 ? -1 : 0));
+        }
+        if (homoDeform == 4)
+            vel = mul(*(const DM3*)sp.ImLL4hInv, (mul(*(const DM3*)sp.LmL, pos) + mul(*(const DM3*)sp.IpLL4h, vel)) + linAccel * dt);
+        else
+            vel = vel + dt * linAccel;
+        if (iv.x != 0 || iv.y != 0 || iv.z != 0) {
+            D3 angAccel{(flags & 8u) ? 0. : t.x * iv.x, (flags & 16u) ? 0. : t.y * iv.y, (flags & 32u) ? 0. : t.z * iv.z};
+            if (damp) {
+                angAccel.x *= 1 - damping * ((t.x * (pva.x + 0.5 * dt * angAccel.x)) > 0 ? 1 : ((t.x * (pva.x + 0.5 * dt * angAccel.x)) < 0 ? -1 : 0));
+                angAccel.y *= 1 - damping * ((t.y * (pva.y + 0.5 * dt * angAccel.y)) > 0 ? 1 : ((t.y * (pva.y + 0.5 * dt * angAccel.y)) < 0 ? -1 : 0));
+                angAccel.z *= 1 - damping * ((t.z * (pva.z + 0.5 * dt * angAccel.z)) > 0 ? 1 : ((t.z * (pva.z + 0.5 * dt * angAccel.z)) < 0 ? -1 : 0));
+            }
+            angVel = angVel + dt * angAccel;
+            if (homoDeform == 4) angVel = angVel - D3{sp.deltaSpinVec[0], sp.deltaSpinVec[1], sp.deltaSpinVec[2]};
+        }
+    } else {
+        if (homoDeform == 4) vel = mul(*(const DM3*)sp.ImLL4hInv, mul(*(const DM3*)sp.LmL, pos) + mul(*(const DM3*)sp.IpLL4h, vel));
+    }
+    if (homoDeform >= 0 && homoDeform != 4) {
+        if (homoDeform == 2 || homoDeform == 3) {
+            if (homoDeform == 3) vel = vel + mul(*(const DM3*)sp.midGradV, vel - (dt / 2.) * linAccel) * dt;
+            vel = vel + mul(*(const DM3*)sp.dGradV, pos);
+        } else if (homoDeform == 1) {
+            pos = pos + mul(*(const DM3*)sp.nextGradV, pos) * dt;
+        }
+    }
+    pos = pos + vel * dt;
+    N.posr[i] = make_double4_32a(pos.x, pos.y, pos.z, pr.w);
+    N.vel[i] = make_double4_32a(vel.x, vel.y, vel.z, 0.);
+    N.angv[i] = make_double4_32a(angVel.x, angVel.y, angVel.z, 0.);
+    if (angVel.x != 0 || angVel.y != 0 || angVel.z != 0) {
+        const double4_32a o = N.ori[i];
+        const F3 w = toF(angVel);
+        const float ang = sqrtf(fdot(w, w));
+        if (ang > 0.f) {
+            float s, c;
+            sincosf(0.5f * ang * (float)dt, &s, &c);
+            const F3 ax = w * (1.f / ang);
+            const float qw = c, qx = s * ax.x, qy = s * ax.y, qz = s * ax.z;
+            const float ow = (float)o.x, ox = (float)o.y, oy = (float)o.z, oz = (float)o.w;
+            float rw = qw * ow - qx * ox - qy * oy - qz * oz;
+            float rx = qw * ox + qx * ow + qy * oz - qz * oy;
+            float ry = qw * oy + qy * ow + qz * ox - qx * oz;
+            float rz = qw * oz + qz * ow + qx * oy - qy * ox;
+            const float inv = rsqrtf(rw * rw + rx * rx + ry * ry + rz * rz);
+            N.ori[i] = make_double4_32a(rw * inv, rx * inv, ry * inv, rz * inv);
+        }
+    }
+    if (sp.reset && (i >= nPar || pshape[i] == WG_SHAPE_FACET)) {
+        D3 G{0, 0, 0};
+        if (sp.hasGravity && !(flags & F_GRAVITY_SKIP)) G = mass * D3{sp.g[0], sp.g[1], sp.g[2]};
+        N.force[i] = make_double4_32a(G.x, G.y, G.z, 0.);
+        N.torque[i] = make_double4_32a(0., 0., 0., 0.);
+    }
+    const D3 lp = ld3(N.lastPos[i]);
+    if (sqn(lp - pos) > sp.maxD2) atomicOr(dFull, 1);
+}
+
+void launch_leapfrog32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const double4_32a* invm, const ScenePar* sp,
+                       int* dFull) {
+    if (N.n == 0) return;
+    k_leapfrog32<<<(N.n + 255) / 256, 256, 0, st>>>(N, invm, P.shape, P.n, sp, dFull);
+}
+
+// ---------------------------------------------------------------------------------- ContactLoop
+struct Frame {
+    F3 c0, c1, c2;
+};
+
+// L6Geom update of the frame (pkg/dem/L6Geom.cpp:80-137) for approxMask==0; returns the
+// mid-step frame in m and writes the current frame to f.
+__device__ __forceinline__ void frameUpdate(F3 prevN, F3 prevC1, F3 n, F3 w1, F3 w2, float dt, bool renorm, Frame& f, Frame& m) {
+    const F3 normRotVec = fcross(prevN, n);
+    F3 midN = 0.5f * (prevN + n);
+    const float mn2 = fdot(midN, midN);
+    midN = (mn2 == 0.f) ? n : midN * rsqrtf(mn2);
+    const F3 twist = midN * (dt * 0.5f * fdot(midN, w1 + w2));
+    const F3 rt = normRotVec + twist;
+    m.c0 = midN;
+    m.c1 = prevC1 - 0.5f * fcross(prevC1, rt);
+    m.c2 = fcross(m.c0, m.c1);
+    f.c0 = n;
+    f.c1 = prevC1 - fcross(m.c1, rt);
+    if (renorm) {
+        f.c0 = fnormalized(f.c0);
+        f.c1 = f.c1 - f.c0 * fdot(f.c1, f.c0);
+        f.c1 = fnormalized(f.c1);
+    }
+    f.c2 = fcross(f.c0, f.c1);
+}
+// L6Geom::setInitialLocalCoords, pkg/dem/L6Geom.cpp:27-38
+__device__ __forceinline__ void frameInit(F3 n, Frame& f) {
+    const F3 ref = (fabsf(n.y) < fabsf(n.z)) ? F3{0, 1, 0} : F3{0, 0, 1};
+    F3 y = fcross(n, ref);
+    y = fnormalized(y - n * fdot(y, n));
+    f.c0 = n;
+    f.c1 = y;
+    f.c2 = fcross(n, y);
+}
+
+__global__ void __launch_bounds__(256) k_contact_fp32(DevNodes N, DevParticles P, DevContacts C, DevIncidence I,
+                                                     const double4_32a* __restrict__ mats, const ScenePar* __restrict__ spp,
+                                                     const long long* __restrict__ dStep, int* __restrict__ dErr) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= C.n) return;
+    const ScenePar& sp = *spp;
+    uint32_t fl = C.flags[c];
+    const uint32_t ty = ctype(fl);
+    if (ty == CT_NONE) return;
+    fl &= ~C_PENDING;
+    const uint64_t key = C.key[c];
+    const int lo = (int)(key >> 32), hi = (int)(key & 0xffffffffu);
+    const int A = (fl & C_SWAP) ? hi : lo, B = (fl & C_SWAP) ? lo : hi;
+    const bool real = fl & C_REAL;
+    const long long step = *dStep;
+    const double dt = sp.dt;
+    const float dtf = (float)dt;
+    D3 shift2{0, 0, 0}, shiftVel2{0, 0, 0};
+    if (sp.periodic) {
+        int a, b, cc;
+        unpackCellDist(C.cdist[c], a, b, cc);
+        if (fl & C_SWAP) { a = -a; b = -b; cc = -cc; }
+        const D3 cd{(double)a, (double)b, (double)cc};
+        shift2 = mul(*(const DM3*)sp.hSize, cd);
+        shiftVel2 = mul(*(const DM3*)sp.shiftVelMat, cd);
+    }
+    // n: normal; armA/armB: contact point minus the nodes of pA/pB (torque arms, Contact.cpp:32);
+    // c1x/c2x: mid-step branch vectors of L6Geom.cpp:156-160; dv: relative velocity of the centres
+    F3 n, armA, armB, c1x, c2x, dv, w1, w2;
+    float uN, r1, r2;
+    if (ty == CT_SS) {
+        const double4_32a pa = N.posr[A], pb = N.posr[B];
+        const D3 dx = (ld3(pb) + shift2) - ld3(pa);
+        const double d2 = sqn(dx);
+        const double R = pa.w + pb.w;
+        const double num = d2 - R * R;  // |dx|^2 - (r1+r2)^2, exact enough in FP64
+        if (num > 0 && !real) {
+            C.flags[c] = fl;
+            return;
+        }
+        const float distf = sqrtf((float)d2);
+        uN = (float)num / (distf + (float)R);  // |dx| - (r1+r2) without the cancellation
+        n = toF(dx) * (1.f / distf);
+        r1 = (float)pa.w;
+        r2 = (float)pb.w;
+        armA = (r1 + 0.5f * uN) * n;
+        armB = -(r2 + 0.5f * uN) * n;
+        if (real) {
+            const F3 pn{C.fcol[CF_T0X][c], C.fcol[CF_T0Y][c], C.fcol[CF_T0Z][c]};
+            const float up = C.fcol[CF_UN][c];
+            c1x = 0.5f * ((r1 + 0.5f * up) * pn + armA);
+            c2x = 0.5f * (-(r2 + 0.5f * up) * pn + armB);
+        }
+        dv = toF((ld3(N.vel[B]) + shiftVel2) - ld3(N.vel[A]));
+        w1 = toF(ld3(N.angv[A]));
+        w2 = toF(ld3(N.angv[B]));
+    } else {
+        Geo g;
+        bool touch;
+        if (ty == CT_WS) touch = geomWS(N, P, real ? (double)C.fcol[CF_T0X + P.aux[A].x][c] : 0., A, B, shift2, real, g);
+        else touch = geomFS(N, P, A, B, shift2, real, g, dErr);
+        if (!touch) {
+            C.flags[c] = fl;
+            return;
+        }
+        n = toF(g.normal);
+        uN = (float)g.uN;
+        r1 = (float)g.r1;
+        r2 = (float)g.r2;
+        // walls are uninodal (their node is pos1); facets take no force here
+        armA = (ty == CT_WS) ? toF(g.contPt - g.pos1) : F3{0.f, 0.f, 0.f};
+        armB = toF(g.contPt - g.pos2);
+        if (real) {
+            const D3 prevCp{C.col[CC_CPX][c], C.col[CC_CPY][c], C.col[CC_CPZ][c]};
+            const D3 mc = .5 * (prevCp + g.contPt);
+            c1x = toF(mc - (g.pos1 - (dt / 2.) * g.vel1));
+            c2x = toF(mc - (g.pos2 - (dt / 2.) * (g.vel2 + shiftVel2)));
+        }
+        dv = toF((g.vel2 + shiftVel2) - g.vel1);
+        w1 = toF(g.angVel1);
+        w2 = toF(g.angVel2);
+        C.col[CC_CPX][c] = g.contPt.x;
+        C.col[CC_CPY][c] = g.contPt.y;
+        C.col[CC_CPZ][c] = g.contPt.z;
+    }
+    Frame f, m;
+    F3 lvel{0, 0, 0};
+    float ph0, ph1, ph2, ph3 = 0.f;
+    if (!real) {
+        frameInit(n, f);
+        // Cp2 on creation (FrictMat.cpp:20-44 / Hertz.cpp:9-50), evaluated in FP64
+        double lens0 = fabs((double)r1) + (double)uN / 2, lens1 = fabs((double)r2) + (double)uN / 2;
+        if (lens0 < 0) lens0 = lens1;
+        if (lens1 < 0) lens1 = lens0;
+        const double rr = (r1 > 0 && r2 > 0) ? fmin((double)r1, (double)r2) : (r1 > 0 ? (double)r1 : (double)r2);
+        const double contA = 3.14159265358979323846 * (rr * rr);
+        const double4_32a m1 = mats[P.mat[A]], m2 = mats[P.mat[B]];
+        if (sp.phys == 0) {
+            const double kn = 1 / (1 / (m1.y * contA / lens0) + 1 / (m2.y * contA / lens1));
+            ph0 = (float)kn;
+            ph1 = (float)(.5 * (m1.w + m2.w) * kn);
+            ph2 = (float)fmin(m1.z, m2.z);
+        } else {
+            const double nu = sp.hzPoisson;
+            const double K = (4 / 3.) / ((1 - nu * nu) / m1.y + (1 - nu * nu) / m2.y);
+            const double R = 1. / (1. / lens0 + 1. / lens1);
+            const double kn0 = K * sqrt(R);
+            const double G = .5 * (m1.y / (2 * (1 + nu)) + m2.y / (2 * (1 + nu)));
+            ph0 = (float)kn0;
+            ph1 = (float)(2 * sqrt(4 * R) * G / (2 - nu));
+            ph2 = (float)fmin(m1.z, m2.z);
+            if (sp.hzViscOn) {
+                const double ma = N.minert[P.shape[A] == WG_SHAPE_FACET ? P.aux[A].x : A].w, mb = N.minert[B].w;
+                const double mbar = (ma <= 0 && mb > 0) ? mb : ((ma > 0 && mb <= 0) ? ma : (ma * mb) / (ma + mb));
+                ph3 = (float)fmax(0., sp.hzViscConst * sqrt(mbar * kn0));
+            }
+        }
+        C.fcol[CF_P0][c] = ph0;
+        C.fcol[CF_P1][c] = ph1;
+        C.fcol[CF_P2][c] = ph2;
+        C.fcol[CF_P3][c] = ph3;
+        C.step0[c] = (int32_t)step;
+        if (sp.law == 0) {
+            C.col[CC_FT1][c] = 0.;
+            C.col[CC_FT2][c] = 0.;
+        }
+    } else {
+        const F3 pn{C.fcol[CF_T0X][c], C.fcol[CF_T0Y][c], C.fcol[CF_T0Z][c]};
+        const F3 pc1{C.fcol[CF_T1X][c], C.fcol[CF_T1Y][c], C.fcol[CF_T1Z][c]};
+        frameUpdate(pn, pc1, n, w1, w2, dtf, sp.trsfRenorm > 0 && (step % sp.trsfRenorm) == 0, f, m);
+        const F3 relVel = (dv + fcross(w2, c2x)) - fcross(w1, c1x);
+        lvel = F3{fdot(m.c0, relVel), fdot(m.c1, relVel), fdot(m.c2, relVel)};
+        ph0 = C.fcol[CF_P0][c];
+        ph1 = C.fcol[CF_P1][c];
+        ph2 = C.fcol[CF_P2][c];
+        ph3 = C.fcol[CF_P3][c];
+    }
+    float fn, ft1 = 0.f, ft2 = 0.f;
+    bool keep = true;
+    if (sp.law == 0) {
+        // Law2_L6Geom_FrictPhys_IdealElPl (IdealElPl.cpp:18-81), shear force accumulated in FP64
+        if (uN > 0 && !sp.noBreak) keep = false;
+        else {
+            fn = ph0 * uN;
+            if (sp.noFrict || ph2 == 0.f) {
+                if (real) { C.col[CC_FT1][c] = 0.; C.col[CC_FT2][c] = 0.; }
+            } else {
+                double t1 = real ? C.col[CC_FT1][c] : 0., t2 = real ? C.col[CC_FT2][c] : 0.;
+                t1 += (double)(dtf * ph1 * lvel.y);
+                t2 += (double)(dtf * ph1 * lvel.z);
+                const double maxFt = (double)(fabsf(fn) * ph2);
+                const double q = t1 * t1 + t2 * t2;
+                if (q > maxFt * maxFt && !sp.noSlip) {
+                    const double ratio = (q > 0) ? maxFt * rsqrt(q) : 0.;
+                    t1 *= ratio;
+                    t2 *= ratio;
+                }
+                C.col[CC_FT1][c] = t1;
+                C.col[CC_FT2][c] = t2;
+                ft1 = (float)t1;
+                ft2 = (float)t2;
+                if (isnan(fn) || isnan(t1) || isnan(t2)) atomicCAS(dErr, 0, 101);
+            }
+        }
+    } else {
+        // Law2_L6Geom_HertzPhys_DMT, DMT branch (Hertz.cpp:58-87,143-172)
+        if (uN > 0) keep = false;
+        else {
+            const float su = sqrtf(-uN);
+            const float Fne = -ph0 * (su * su * su);
+            const float eta = (ph3 > 0.f) ? ph3 * sqrtf(su) : 0.f;
+            float Fnv = eta * lvel.x;
+            if (sp.noAttraction && Fne + Fnv > 0.f) Fnv = -Fne;
+            fn = Fne + Fnv;  // the adhesion term 4 pi R gamma is zero (gamma = 0 is required in this mode)
+            const float kt = ph1 * su;
+            ft1 = dtf * kt * lvel.y;
+            ft2 = dtf * kt * lvel.z;
+            const float maxFt = fmaxf(0.f, fn) * ph2;
+            const float q = ft1 * ft1 + ft2 * ft2;
+            if (q > maxFt * maxFt) {
+                const float ratio = maxFt * rsqrtf(q);
+                ft1 *= ratio;
+                ft2 *= ratio;
+            } else {
+                ft1 += eta * lvel.y;
+                ft2 += eta * lvel.z;
+            }
+        }
+    }
+    const bool aIsLo = !(fl & C_SWAP);
+    if (!keep) {
+        C.flags[c] = (fl & ~C_REAL) | C_PENDING;
+        if (real) {
+            I.endFf[I.slotLo[c]] = make_float4(0.f, 0.f, 0.f, 0.f);
+            I.endFf[I.slotHi[c]] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        return;
+    }
+    // force on pA in global coordinates: trsf * (Fn, Ft1, Ft2); torques about the nodes
+    const F3 F = fn * f.c0 + ft1 * f.c1 + ft2 * f.c2;
+    const F3 TA = fcross(armA, F), TB = fcross(armB, -F);
+    {
+        const int sA = aIsLo ? I.slotLo[c] : I.slotHi[c], sB = aIsLo ? I.slotHi[c] : I.slotLo[c];
+        if (ty != CT_FS) {
+            I.endFf[sA] = make_float4(F.x, F.y, F.z, 1.f);
+            I.endTf[sA] = make_float4(TA.x, TA.y, TA.z, 0.f);
+        }
+        I.endFf[sB] = make_float4(-F.x, -F.y, -F.z, 1.f);
+        I.endTf[sB] = make_float4(TB.x, TB.y, TB.z, 0.f);
+    }
+    C.fcol[CF_T0X][c] = f.c0.x;
+    C.fcol[CF_T0Y][c] = f.c0.y;
+    C.fcol[CF_T0Z][c] = f.c0.z;
+    C.fcol[CF_T1X][c] = f.c1.x;
+    C.fcol[CF_T1Y][c] = f.c1.y;
+    C.fcol[CF_T1Z][c] = f.c1.z;
+    C.fcol[CF_UN][c] = uN;
+    C.fcol[CF_FN][c] = fn;
+    C.fcol[CF_FT1][c] = ft1;
+    C.fcol[CF_FT2][c] = ft2;
+    C.flags[c] = fl | C_REAL;
+}
+
+void launch_contact_fp32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C, const DevIncidence& I,
+                         const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dErr) {
+    if (C.n == 0) return;
+    k_contact_fp32<<<(unsigned)((C.n + 255) / 256), 256, 0, st>>>(N, P, C, I, mats, sp, dStep, dErr);
+}
+
+// ---------------------------------------------------------------------------------- force sum
+// Per-particle FP64 sum of the FP32 end slots in slot order (ascending id of the other particle,
+// the order of ContactLoop.cpp:250-257 over key-sorted contacts).
+__global__ void k_reduce32(DevNodes N, DevParticles P, DevIncidence I, const ScenePar* __restrict__ spp, int heavyThreshold) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P.n) return;
+    if (P.shape[p] == WG_SHAPE_FACET) return;
+    const ScenePar& sp = *spp;
+    const uint32_t flags = N.flags[p];
+    const double mass = N.minert[p].w;
+    D3 F{0, 0, 0}, T{0, 0, 0};
+    if (sp.hasGravity && !(flags & F_GRAVITY_SKIP)) F = mass * D3{sp.g[0], sp.g[1], sp.g[2]};
+    if (sp.applyForces) {
+        const int e0 = I.hiStart[p] + I.loStart[p], e1 = I.hiStart[p + 1] + I.loStart[p + 1];
+        if (e1 - e0 > heavyThreshold) return;
+        for (int e = e0; e < e1; e++) {
+            const float4 f = I.endFf[e];
+            if (f.w == 0.f) continue;
+            const float4 t = I.endTf[e];
+            F = F + D3{(double)f.x, (double)f.y, (double)f.z};
+            T = T + D3{(double)t.x, (double)t.y, (double)t.z};
+        }
+    }
+    N.force[p] = make_double4_32a(F.x, F.y, F.z, 0.);
+    N.torque[p] = make_double4_32a(T.x, T.y, T.z, 0.);
+}
+
+__global__ void k_reduce32_heavy(DevNodes N, DevIncidence I, const ScenePar* __restrict__ spp) {
+    const int p = I.heavy[blockIdx.x];
+    const ScenePar& sp = *spp;
+    const int e0 = I.hiStart[p] + I.loStart[p], e1 = I.hiStart[p + 1] + I.loStart[p + 1];
+    D3 F{0, 0, 0}, T{0, 0, 0};
+    for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+        const float4 f = I.endFf[e];
+        if (f.w == 0.f) continue;
+        const float4 t = I.endTf[e];
+        F = F + D3{(double)f.x, (double)f.y, (double)f.z};
+        T = T + D3{(double)t.x, (double)t.y, (double)t.z};
+    }
+    __shared__ double sh[6][256];
+    sh[0][threadIdx.x] = F.x; sh[1][threadIdx.x] = F.y; sh[2][threadIdx.x] = F.z;
+    sh[3][threadIdx.x] = T.x; sh[4][threadIdx.x] = T.y; sh[5][threadIdx.x] = T.z;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s)
+            for (int q = 0; q < 6; q++) sh[q][threadIdx.x] += sh[q][threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const uint32_t flags = N.flags[p];
+        const double mass = N.minert[p].w;
+        D3 G{0, 0, 0};
+        if (sp.hasGravity && !(flags & F_GRAVITY_SKIP)) G = mass * D3{sp.g[0], sp.g[1], sp.g[2]};
+        N.force[p] = make_double4_32a(G.x + sh[0][0], G.y + sh[1][0], G.z + sh[2][0], 0.);
+        N.torque[p] = make_double4_32a(sh[3][0], sh[4][0], sh[5][0], 0.);
+    }
+}
+
+__global__ void k_step_advance32(long long* dStep) { *dStep += 1; }
+
+void launch_reduce32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C, const DevIncidence& I,
+                     const ScenePar* sp, long long* dStep) {
+    if (P.n > 0) {
+        k_reduce32<<<(P.n + 255) / 256, 256, 0, st>>>(N, P, I, sp, 64);
+        if (I.nHeavy > 0) k_reduce32_heavy<<<I.nHeavy, 256, 0, st>>>(N, I, sp);
+    }
+    k_step_advance32<<<1, 1, 0, st>>>(dStep);
+}
+
+}  // namespace wg

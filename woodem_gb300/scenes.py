@@ -87,15 +87,42 @@ def _segment_height(R, area):
     return 0.5 * (lo + hi)
 
 
+def settle(S, steps, g_factor=30.0, damping=0.3, precision="fp32"):
+    """Compact a loose packing into a resting bed on the GPU: run ``steps`` steps under gravity
+    multiplied by ``g_factor`` with Leapfrog damping ``damping``, then restore the scene's gravity,
+    damping and precision, zero the velocities, forces and torques of the free nodes, and reset
+    Scene.step/time. The contact history is dropped (the next run starts from the positions)."""
+    lf = S.engines[0]
+    g0 = np.array(S.dem.gravity, dtype=float)
+    d0, p0 = lf.damping, S.gpu.precision
+    S.close()
+    S.dem.gravity = g0 * g_factor
+    lf.damping = damping
+    S.gpu.precision = precision
+    S.run(steps)
+    S.close()
+    S.dem.gravity = g0
+    lf.damping = d0
+    S.gpu.precision = p0
+    nd = S.dem._nodes.soa
+    free = (nd.col("flags") & 63) != 63
+    for k in ("vel", "angVel", "force", "torque"):
+        nd.col(k)[free] = 0.0
+    S.step = 0
+    S.time = 0.0
+    return S
+
+
 def hertz_drum(n=1_000_000, seed=0, diameter=1.2, length=0.6, div=201, axDiv=50, fill_fraction=0.35, density=2500.0,
                young=1e8, poisson=0.25, en=0.6, tanPhi=0.5, omega=1.0, verletRel=0.1, precision="fp64",
-               median=3e-3, sigma=0.25, rmin=1.5e-3, rmax=6e-3):
+               median=3e-3, sigma=0.25, rmin=1.5e-3, rmax=6e-3, settle_steps=0):
     """Rotating drum: x-axis cylinder (diameter x length) meshed into 2*(div-1)*axDiv facets with
     outward normals and fakeVel for angular velocity ``omega``, two rotating Wall end caps,
     lognormal radii, Hertz contacts with viscous damping (en), gravity (0,0,-9.81),
     dt = 0.3*pWaveDt, verletDist = 0.1*min radius. Spheres are placed by seeded random
     sequential insertion (solid fraction ``fill_fraction``) in the lower part of the drum whose
-    height is chosen to hold them."""
+    height is chosen to hold them; with ``settle_steps`` the fill is then compacted into a resting
+    bed on the GPU (see ``settle``)."""
     R = diameter / 2.0
     S = Scene(fields=[DemField(gravity=(0, 0, -9.81))])
     S.gpu.precision = precision
@@ -115,4 +142,6 @@ def hertz_drum(n=1_000_000, seed=0, diameter=1.2, length=0.6, div=201, axDiv=50,
     S.engines = utils.defaultEngines(cp2=Cp2_FrictMat_HertzPhys(poisson=poisson, en=en, gamma=0.0, alpha=0.0),
                                      law=Law2_L6Geom_HertzPhys_DMT(), verletDist=-verletRel, dynDtPeriod=0, damping=0.0)
     S.dt = 0.3 * utils.pWaveDt(S)
+    if settle_steps:
+        settle(S, settle_steps)
     return S
