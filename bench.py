@@ -93,9 +93,20 @@ def build_scene(args, seed, n=None, precision=None):
     scale = (n / 1e6) ** (1 / 3.0)
     t = time.time()
     S = scenes.hertz_drum(n=n, seed=seed, diameter=1.2 * scale, length=0.6 * scale, div=201, axDiv=50,
-                          precision=precision or args.precision, settle_steps=args.settle)
-    log("scene of %d spheres built and settled (%d steps) in %.1fs" % (n, args.settle, time.time() - t))
+                          precision=precision or args.precision, settle_steps=args.settle, settle_g=args.settle_g)
+    log("scene of %d spheres built and settled (%d steps at %g g) in %.1fs" % (n, args.settle, args.settle_g, time.time() - t))
     return S
+
+
+def bed_stats(S, radius):
+    """Where the settled bed sits: the 99.5th percentile and the mean of the sphere heights, in drum
+    radii from the axis (a bed filling 40% of the drum has its free surface at z = -0.16 R)."""
+    from woodem_gb300 import _plan
+    A = _plan.compile_scene(S)
+    nd = S.dem._nodes.soa
+    sph = A.particles["shape"] == 0
+    z = nd.col("pos")[A.particles["nodes"][sph, 0], 2]
+    return {"top_z_over_R": round(float(np.percentile(z, 99.5)) / radius, 4), "mean_z_over_R": round(float(z.mean()) / radius, 4)}
 
 
 def snapshot(S):
@@ -112,14 +123,14 @@ def restore(S, st):
     S.time = 0.0
 
 
-# Algorithmic bytes of the FP64 / FP32 contact kernel and of a whole step:
-#   contact kernel: per real contact read+write of the persistent contact state, per potential
-#   contact its key and flags, per particle one read of the gathered state (pos, vel, angVel).
-#   step: + Leapfrog per node, + force sum per contact end and per particle, collider amortised.
-BYTES = {
-    "fp64": dict(real=124 + 124, pot=16, part=96, lf=388, red_end=60, red_part=64 + 16),
-    "fp32": dict(real=76 + 72, pot=16, part=96, lf=388, red_end=48, red_part=64 + 16),
-}
+# Algorithmic bytes per unit of work: the compulsory DRAM traffic of an ideal one-pass step,
+# counted from stored widths (the per-unit figures of the reference path's cost model):
+#   particle-step (Leapfrog)          b_p = 156 read + 104 written = 260 B
+#   real contact (contact kernel)     b_r = 192 B FP64 Hertz, 124 B FP32-force mode
+#   potential, not real contact       b_v = 16 B
+#   facet-step (vertices + fakeVel)   96 B
+#   collider full run                 104 B per particle + 8 B per potential contact
+BYTES = {"b_p": 260, "b_r": {"fp64": 192, "fp32": 124}, "b_v": 16, "b_f": 96, "coll_p": 104, "coll_c": 8}
 
 
 def measure_gpu(args, rank, world, S=None, prec=None, e2e=True):
@@ -150,8 +161,10 @@ def measure_gpu(args, rank, world, S=None, prec=None, e2e=True):
     tot, ph, nl = sim.timing()
     st1 = sim.stats()
     n_spheres = args.spheres
+    A = S._sim.A
     res = dict(ms=tot, wall=(t2 - t1) * 1e3, phases=ph.tolist(), launches=nl, st0=st0, st1=st1, clocks=ck,
-               n_nodes=S._sim.A.n_nodes, n_par=S._sim.A.n_particles, n_spheres=n_spheres)
+               n_nodes=A.n_nodes, n_par=A.n_particles, n_spheres=n_spheres,
+               n_facets=int(np.count_nonzero(A.particles["shape"] == 2)))
     # e2e through wg_run_host with page-locked host buffers
     if e2e and not args.no_e2e:
         na = S._sim.A.n_nodes
@@ -215,6 +228,17 @@ def cpu_sample(args, seconds, threads):
     return n * steps / el, steps, n, el
 
 
+def traffic_per_launch(kern, R, P, nF, n):
+    """DRAM bytes (read + write) per launch of the kernel, from the committed ncu capture summary
+    (bytes per unit of that capture scaled to this launch's units), or None."""
+    try:
+        with open(os.path.join(HERE, "profiles", "dram_per_unit.json")) as f:
+            d = json.load(f)[kern]
+    except Exception:
+        return None
+    return d.get("per_real", 0.0) * R + d.get("per_potential", 0.0) * (P - R) + d.get("per_sphere", 0.0) * n
+
+
 def peaks():
     try:
         with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
@@ -231,7 +255,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=30)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--precision", default="fp32", choices=["fp64", "fp32"])
-    ap.add_argument("--settle", type=int, default=12000, help="steps compacting the random fill into a resting bed")
+    ap.add_argument("--settle", type=int, default=20000, help="steps compacting the random fill into a resting bed")
+    ap.add_argument("--settle-g", type=float, default=40.0, help="gravity multiplier while compacting")
     ap.add_argument("--no-other", action="store_true", help="skip timing the other precision mode")
     ap.add_argument("--profile", action="store_true", help="bracket the timed steps with cudaProfilerStart/Stop")
     ap.add_argument("--spheres", type=int, default=1_000_000)
@@ -245,6 +270,7 @@ def main():
     args.warmup = max(args.warmup, 3)
     rank, world, local = env_rank()
     cfg = {"workload": "hertz-drum-1M", "spheres": args.spheres, "facets": 20000, "walls": 2, "settle_steps": args.settle,
+           "settle_g": args.settle_g, "sphere_order": "Morton curve of the settled positions",
            "law": "Cp2_FrictMat_HertzPhys+Law2_L6Geom_HertzPhys_DMT", "precision": args.precision,
            "l2": "inputs larger than L2 (device state > 1 GB)", "replicas": world}
     if args.impl == "reference":
@@ -280,8 +306,11 @@ def main():
     if world > 1:
         from woodem_gb300 import core  # noqa
     S = build_scene(args, seed=args.seed + rank)
+    bed = bed_stats(S, 0.6 * (args.spheres / 1e6) ** (1 / 3.0))
+    log("bed: %s" % bed)
     st0 = snapshot(S)
     res = measure_gpu(args, rank, world, S=S, prec=args.precision)
+    res["bed"] = bed
     other = None
     if not args.no_other:
         restore(S, st0)
@@ -294,29 +323,41 @@ def main():
     n_sph = res["n_spheres"]
     value = world * n_sph * args.steps / (ms / 1e3)
     hbm, src = peaks()
-    B = BYTES[args.precision]
     R = 0.5 * (st0.n_real + st1.n_real)
     P = 0.5 * (st0.n_contacts + st1.n_contacts)
-    Np = res["n_par"]
-    kern_ms = res["phases"][1] / args.steps
-    kbytes = R * B["real"] + (P - R) * B["pot"] + Np * B["part"]
-    achieved = kbytes / (kern_ms / 1e3) / 1e9 if kern_ms > 0 else 0.0
+    nF = res["n_facets"]
     nfull = st1.n_full_runs - st0.n_full_runs
-    step_bytes = (res["n_nodes"] * B["lf"] + kbytes + 2 * R * B["red_end"] + Np * B["red_part"])
+    # per-launch algorithmic bytes of the two per-step kernels, and of the whole step
+    contact_bytes = R * BYTES["b_r"][args.precision] + (P - R) * BYTES["b_v"] + nF * BYTES["b_f"]
+    leapfrog_bytes = res["n_spheres"] * BYTES["b_p"]
+    coll_bytes = (BYTES["coll_p"] * res["n_par"] + BYTES["coll_c"] * P) * nfull / args.steps
+    step_bytes = leapfrog_bytes + contact_bytes + coll_bytes
+    ph = [x / args.steps for x in res["phases"]]
+    if ph[1] >= ph[0]:
+        kern, kbytes, kern_ms = "k_contact_%s" % args.precision, contact_bytes, ph[1]
+    else:
+        kern, kbytes, kern_ms = "k_leapfrog%s" % ("32" if args.precision == "fp32" else ""), leapfrog_bytes, ph[0]
+    achieved = kbytes / (kern_ms / 1e3) / 1e9 if kern_ms > 0 else 0.0
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if args.precision == "fp64" else "f32+f64", "data": "synthetic", "config": cfg,
-            "roofline": {"bound": "hbm", "kernel": "k_contact_%s" % args.precision, "achieved": achieved, "peak": hbm,
-                         "unit": "GB/s", "frac": achieved / hbm, "traffic": None, "peak_source": src,
-                         "bytes_per_launch": kbytes, "launch_ms": kern_ms},
-            "step": {"contacts": P, "real": R, "full_runs": nfull, "phase_ms": [x / args.steps for x in res["phases"]],
-                     "algorithmic_bytes": step_bytes, "achieved_gbs": step_bytes / (ms / args.steps / 1e3) / 1e9},
+            "roofline": {"bound": "hbm", "kernel": kern, "achieved": achieved, "peak": hbm,
+                         "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic_per_launch(kern, R, P, nF, res["n_spheres"]),
+                         "peak_source": src, "bytes_per_launch": kbytes, "launch_ms": kern_ms},
+            "step": {"contacts": P, "real": R, "real_per_sphere": R / n_sph, "full_runs": nfull,
+                     "phase_ms": {"leapfrog": ph[0], "contact": ph[1], "collider": ph[3]},
+                     "algorithmic_bytes": step_bytes, "achieved_gbs": step_bytes / (ms / args.steps / 1e3) / 1e9,
+                     "frac": step_bytes / (ms / args.steps / 1e3) / 1e9 / hbm},
             "gpu_launches": int(res["launches"]), "clocks": res["clocks"]}
+    if "bed" in res:
+        cfg["bed"] = res["bed"]
     if other is not None:
         oms = allreduce_max(other["ms"], world)
         ost0, ost1 = other["st0"], other["st1"]
+        oph = [x / args.steps for x in other["phases"]]
         line["other_precision"] = {"precision": other["prec"], "value": world * n_sph * args.steps / (oms / 1e3),
-                                   "ms_per_step": oms / args.steps, "phase_ms": [x / args.steps for x in other["phases"]],
+                                   "ms_per_step": oms / args.steps,
+                                   "phase_ms": {"leapfrog": oph[0], "contact": oph[1], "collider": oph[3]},
                                    "real": 0.5 * (ost0.n_real + ost1.n_real), "contacts": 0.5 * (ost0.n_contacts + ost1.n_contacts)}
     if "e2e" in res:
         e = res["e2e"]

@@ -147,3 +147,36 @@ def test_errors_are_raised(gpu_lib):
     S.dem.par[10].pos = (float("nan"), 0, 0)
     with pytest.raises(RuntimeError):
         S.run(2)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_call_granularity_is_invisible(prec):
+    """The step loop queues steps in chunks and resumes after each collider run; running 400 steps
+    in one call, in calls of 1 and 37 steps, or one step at a time through wg_run_host (state
+    copied out and back in every step) gives bitwise the same state."""
+    out = []
+    for mode in ("one", "steps", "host"):
+        S = scenes.box_settle_small(n=1200, seed=5, precision=prec)
+        if mode == "one":
+            S.run(400)
+        elif mode == "steps":
+            S.run(1)
+            for _ in range(10):
+                S.run(37)
+            for _ in range(29):
+                S.run(1)
+        else:
+            S.run(1)
+            sim = S._sim
+            L, h = sim.H.L, sim.H.h
+            na = sim.A.n_nodes
+            parts = [np.zeros(w * na) for w in (3, 4, 3, 3, 3, 3)]
+            sim.H.check(L.wg_get_nodes(h, *[_native.ptr(x) for x in parts]), "get_nodes")
+            for _ in range(399):
+                sim.H.check(L.wg_run_host(h, 1, *[_native.ptr(x) for x in parts]), "run_host")
+        g = _gpu_nodes(S)
+        S.close()
+        out.append(g)
+    for k in ("pos", "vel", "angVel", "force", "torque"):
+        assert np.array_equal(out[0][k], out[1][k]), "%s: one call vs many" % k
+        assert np.array_equal(out[0][k], out[2][k]), "%s: one call vs host round trips" % k

@@ -42,6 +42,7 @@ Sim::~Sim() {
     if (hFlags) cudaFreeHost(hFlags);
     for (int i = 0; i < 8; i++)
         if (ev[i]) cudaEventDestroy(ev[i]);
+    for (cudaEvent_t e : evPool) cudaEventDestroy(e);
     if (stream) cudaStreamDestroy(stream);
 }
 
@@ -410,7 +411,8 @@ int Sim::upload() {
     P.mx = (double4_32a*)dalloc(sizeof(double4_32a) * nPar);
     I.loStart = (int32_t*)dalloc(sizeof(int32_t) * (nPar + 1));
     I.hiStart = (int32_t*)dalloc(sizeof(int32_t) * (nPar + 1));
-    I.heavy = (int32_t*)dalloc(sizeof(int32_t) * nPar);
+    I.heavy = (int32_t*)dalloc(sizeof(int32_t) * 2 * std::max<int64_t>(1, nPar));
+    I.heavyFree = I.heavy + std::max<int64_t>(1, nPar);
     dMats = (double4_32a*)dalloc(sizeof(double4_32a) * std::max<size_t>(1, hDensity.size()));
     dPar = (ScenePar*)dalloc(sizeof(ScenePar));
     dStep = (long long*)dalloc(sizeof(long long));
@@ -418,7 +420,7 @@ int Sim::upload() {
     X.dApiMap = (int32_t*)dalloc(sizeof(int32_t) * std::max<int64_t>(1, na));
     X.dStage = (double*)dalloc(sizeof(double) * 19 * std::max<int64_t>(1, na));
     if (!X.dStage) return fail(WG_ERR_CUDA, "out of device memory (scene)");
-    WG_CUDA_TRY(cudaMallocHost(&hFlags, sizeof(int) * 4));
+    WG_CUDA_TRY(cudaMallocHost(&hFlags, sizeof(int) * 4 + sizeof(long long)));
     std::vector<double4_32a> mats(hDensity.size());
     for (size_t m = 0; m < hDensity.size(); m++) mats[m] = make_double4_32a(hDensity[m], hYoung[m], hTanPhi[m], hKtDivKn[m]);
     WG_CUDA_TRY(cudaMemcpy(N.posr, posr.data(), sizeof(double4_32a) * nSlots, cudaMemcpyHostToDevice));
@@ -446,7 +448,17 @@ int Sim::upload() {
             inv[q] = make_double4_32a(m.x != 0 ? 1. / m.x : 0., m.y != 0 ? 1. / m.y : 0., m.z != 0 ? 1. / m.z : 0., m.w != 0 ? 1. / m.w : 0.);
         }
         dInvM = (double4_32a*)dalloc(sizeof(double4_32a) * nSlots);
-        if (!dInvM) return fail(WG_ERR_CUDA, "out of device memory (scene)");
+        N.ph = (float4*)dalloc(sizeof(float4) * nSlots);
+        N.pl = (float4*)dalloc(sizeof(float4) * nSlots);
+        N.vh = (float4*)dalloc(sizeof(float4) * nSlots);
+        N.vl = (float4*)dalloc(sizeof(float4) * nSlots);
+        N.wz = (float*)dalloc(sizeof(float) * nSlots);
+        if (!dInvM || !N.wz) return fail(WG_ERR_CUDA, "out of device memory (scene)");
+        WG_CUDA_TRY(cudaMemset(N.ph, 0, sizeof(float4) * nSlots));
+        WG_CUDA_TRY(cudaMemset(N.pl, 0, sizeof(float4) * nSlots));
+        WG_CUDA_TRY(cudaMemset(N.vh, 0, sizeof(float4) * nSlots));
+        WG_CUDA_TRY(cudaMemset(N.vl, 0, sizeof(float4) * nSlots));
+        WG_CUDA_TRY(cudaMemset(N.wz, 0, sizeof(float) * nSlots));
         WG_CUDA_TRY(cudaMemcpy(dInvM, inv.data(), sizeof(double4_32a) * nSlots, cudaMemcpyHostToDevice));
     }
     long long st0 = cfg.step;
@@ -487,6 +499,17 @@ int Sim::checkErr() {
     return 0;
 }
 
+// Clears the step-loop flags (an error code is kept) and optionally requests a full collider run.
+__global__ void k_set_flags(int* f, int full) {
+    f[FL_FULL] = full;
+    f[FL_HALT] = 0;
+}
+
+// Scene::doOneStep (core/Scene.cpp:319-389) for n steps. Steps are queued on the stream in
+// chunks without waiting for the verlet test of each one: every per-step kernel checks the
+// device flag words, and once Leapfrog of step s finds a node past verletDist, the contact
+// kernel of step s raises FL_HALT and everything queued after it does nothing. The host then
+// reads the step counter, runs the collider for step s, finishes its contact loop and goes on.
 int Sim::run(int64_t n) {
     Sim& S = *this;
     SimEx& X = static_cast<SimEx&>(*this);
@@ -497,50 +520,105 @@ int Sim::run(int64_t n) {
     WG_CUDA_TRY(cudaSetDevice(device));
     double ph[4] = {0, 0, 0, 0};
     int64_t launches = 0;
+    const int64_t maxChunk = (cfg.periodic || hPar.verletDist == 0) ? 1 : 32;
+    if ((int64_t)evPool.size() < 3 * maxChunk + 2) {
+        for (int64_t q = (int64_t)evPool.size(); q < 3 * maxChunk + 2; q++) {
+            cudaEvent_t e;
+            WG_CUDA_TRY(cudaEventCreate(&e));
+            evPool.push_back(e);
+        }
+    }
+    cudaEvent_t* E = evPool.data();
+    long long* hStepPin = (long long*)(hFlags + 4);
+    const bool fp32 = prec == WG_PREC_FP32;
+    auto stepLeapfrog = [&](int fromEndsArg) {
+        if (fromEndsArg) {
+            if (fp32) launch_forces32(stream, N, P, I, dPar, dFlags, true);
+            else launch_forces(stream, N, P, I, dPar, dFlags, true);
+            launches += I.nHeavyFree > 0;
+        }
+        if (fp32) launch_leapfrog32(stream, N, P, I, dInvM, dPar, dFlags, fromEndsArg);
+        else launch_leapfrog(stream, N, P, I, dPar, dFlags, fromEndsArg);
+        launches++;
+    };
+    auto stepContact = [&]() {
+        if (fp32) launch_contact_fp32(stream, N, P, C, I, dMats, dPar, dStep, dFlags);
+        else launch_contact_fp64(stream, N, P, C, I, dMats, dPar, dStep, dFlags);
+        launch_advance(stream, dStep, dFlags);
+        launches += 2;
+    };
+    WG_CUDA_TRY(cudaMemsetAsync(dFlags, 0, sizeof(int) * 4, stream));
     WG_CUDA_TRY(cudaEventRecord(ev[6], stream));
-    for (int64_t i = 0; i < n; i++) {
+    int64_t done = 0;
+    while (done < n) {
+        const int64_t k = std::min<int64_t>(n - done, maxChunk);
+        const bool needFull = !initialized || hPar.verletDist == 0;
+        k_set_flags<<<1, 1, 0, stream>>>(dFlags, needFull ? 1 : 0);
         if (cfg.periodic) {
             X.cell.integrateAndUpdate(cfg.dt);
             fillCellPar(X);
             WG_CUDA_TRY(cudaMemcpyAsync(dPar, &hPar, sizeof(ScenePar), cudaMemcpyHostToDevice, stream));
         }
-        WG_CUDA_TRY(cudaEventRecord(ev[0], stream));
-        WG_CUDA_TRY(cudaMemsetAsync(dFlags, 0, sizeof(int), stream));
-        if (prec == WG_PREC_FP32) launch_leapfrog32(stream, N, P, dInvM, dPar, dFlags);
-        else launch_leapfrog(stream, N, P, dPar, dFlags);
-        launches++;
-        WG_CUDA_TRY(cudaEventRecord(ev[1], stream));
-        WG_CUDA_TRY(cudaMemcpyAsync(hFlags, dFlags, sizeof(int), cudaMemcpyDeviceToHost, stream));
+        const int64_t s0 = step;
+        for (int64_t j = 0; j < k; j++) {
+            WG_CUDA_TRY(cudaEventRecord(E[3 * j], stream));
+            stepLeapfrog(j == 0 ? (fromEnds ? 1 : 0) : 1);
+            WG_CUDA_TRY(cudaEventRecord(E[3 * j + 1], stream));
+            stepContact();
+            WG_CUDA_TRY(cudaEventRecord(E[3 * j + 2], stream));
+        }
+        WG_CUDA_TRY(cudaGetLastError());
+        WG_CUDA_TRY(cudaMemcpyAsync(hFlags, dFlags, sizeof(int) * 4, cudaMemcpyDeviceToHost, stream));
+        WG_CUDA_TRY(cudaMemcpyAsync(hStepPin, dStep, sizeof(long long), cudaMemcpyDeviceToHost, stream));
         WG_CUDA_TRY(cudaStreamSynchronize(stream));
-        bool full = !initialized || hFlags[0] != 0 || hPar.verletDist == 0;
-        WG_CUDA_TRY(cudaEventRecord(ev[2], stream));
-        if (full) {
+        if (hFlags[FL_ERR]) break;
+        int64_t ds = (int64_t)*hStepPin - s0;
+        if (ds < 0 || ds > k) return fail(WG_ERR_STATE, "device step counter out of sequence");
+        float a;
+        for (int64_t j = 0; j < ds; j++) {
+            cudaEventElapsedTime(&a, E[3 * j], E[3 * j + 1]); ph[0] += a;
+            cudaEventElapsedTime(&a, E[3 * j + 1], E[3 * j + 2]); ph[1] += a;
+        }
+        if (ds < k || hFlags[FL_FULL]) {
+            // Leapfrog of step s0+ds ran, its contact loop waits for the collider
+            if (!hFlags[FL_FULL]) return fail(WG_ERR_STATE, "queued steps halted without a collider request");
+            cudaEventElapsedTime(&a, E[3 * ds], E[3 * ds + 1]); ph[0] += a;
+            WG_CUDA_TRY(cudaEventRecord(E[3 * maxChunk], stream));
             int r = collide_full_run(*this);
             if (r) return r;
             initialized = true;
             launches += 12;
+            WG_CUDA_TRY(cudaEventRecord(E[3 * maxChunk + 1], stream));
+            k_set_flags<<<1, 1, 0, stream>>>(dFlags, 0);
+            WG_CUDA_TRY(cudaEventRecord(E[0], stream));
+            stepContact();
+            WG_CUDA_TRY(cudaEventRecord(E[1], stream));
+            WG_CUDA_TRY(cudaMemcpyAsync(hFlags, dFlags, sizeof(int) * 4, cudaMemcpyDeviceToHost, stream));
+            WG_CUDA_TRY(cudaStreamSynchronize(stream));
+            cudaEventElapsedTime(&a, E[3 * maxChunk], E[3 * maxChunk + 1]); ph[3] += a;
+            cudaEventElapsedTime(&a, E[0], E[1]); ph[1] += a;
+            if (hFlags[FL_ERR]) {
+                step += ds;
+                time += ds * cfg.dt;
+                break;
+            }
+            ds += 1;
         }
-        WG_CUDA_TRY(cudaEventRecord(ev[3], stream));
-        if (prec == WG_PREC_FP32) launch_contact_fp32(stream, N, P, C, I, dMats, dPar, dStep, dFlags + 1);
-        else launch_contact_fp64(stream, N, P, C, I, dMats, dPar, dStep, dFlags + 1);
-        WG_CUDA_TRY(cudaEventRecord(ev[4], stream));
-        if (prec == WG_PREC_FP32) launch_reduce32(stream, N, P, C, I, dPar, dStep);
-        else launch_reduce(stream, N, P, C, I, dPar, dStep);
-        launches += 3 + (I.nHeavy > 0);
-        WG_CUDA_TRY(cudaEventRecord(ev[5], stream));
-        WG_CUDA_TRY(cudaGetLastError());
-        WG_CUDA_TRY(cudaEventSynchronize(ev[5]));
-        float a;
-        cudaEventElapsedTime(&a, ev[0], ev[1]); ph[0] += a;
-        cudaEventElapsedTime(&a, ev[3], ev[4]); ph[1] += a;
-        cudaEventElapsedTime(&a, ev[4], ev[5]); ph[2] += a;
-        cudaEventElapsedTime(&a, ev[2], ev[3]); ph[3] += a;
+        fromEnds = true;
         if (cfg.periodic) X.cell.setNextGradV();
-        step++;
-        time += cfg.dt;
+        step += ds;
+        time += ds * cfg.dt;
+        done += ds;
+    }
+    // DemData.force/torque of the last contact loop, for the host and for the next run
+    if (fromEnds) {
+        if (fp32) launch_forces32(stream, N, P, I, dPar, nullptr, false);
+        else launch_forces(stream, N, P, I, dPar, nullptr, false);
+        launches += 1 + (I.nHeavy > 0);
     }
     WG_CUDA_TRY(cudaEventRecord(ev[7], stream));
     WG_CUDA_TRY(cudaEventSynchronize(ev[7]));
+    WG_CUDA_TRY(cudaGetLastError());
     float tot = 0;
     cudaEventElapsedTime(&tot, ev[6], ev[7]);
     lastTotalMs = tot;
@@ -671,6 +749,7 @@ int wg_collide_only(wg_scene* s) {
     int r = collide_full_run(S);
     if (r) return r;
     S.initialized = true;
+    S.fromEnds = false;  // the new incidence starts empty; the next step takes the stored forces
     WG_CUDA_TRY(cudaStreamSynchronize(S.stream));
     return WG_OK;
 }
@@ -701,6 +780,7 @@ int wg_put_state(wg_scene* s, const double* pos, const double* ori, const double
     for (int q = 0; q < 6; q++)
         if (src[q]) WG_CUDA_TRY(cudaMemcpyAsync(X.dStage + off[q] * na, src[q], sizeof(double) * w[q] * na, cudaMemcpyHostToDevice, S.stream));
     k_put_state<<<(unsigned)((na + 255) / 256), 256, 0, S.stream>>>(S.N, X.dApiMap, na, X.dStage);
+    S.fromEnds = false;  // the next step starts from the forces written here
     WG_CUDA_TRY(cudaGetLastError());
     WG_CUDA_TRY(cudaStreamSynchronize(S.stream));
     return WG_OK;
@@ -797,10 +877,10 @@ static int collectContacts(Sim& S, std::vector<int64_t>& keep, std::vector<uint6
         std::vector<double> ef(4 * ne);
         if (S.prec == WG_PREC_FP32) {
             std::vector<float> tmp(4 * ne);
-            WG_CUDA_TRY(cudaMemcpy(tmp.data(), S.I.endFf, sizeof(float4) * ne, cudaMemcpyDeviceToHost));
+            WG_CUDA_TRY(cudaMemcpy(tmp.data(), S.I.endAf, sizeof(float4) * ne, cudaMemcpyDeviceToHost));
             for (int64_t q = 0; q < 4 * ne; q++) ef[q] = tmp[q];
         } else {
-            WG_CUDA_TRY(cudaMemcpy(ef.data(), S.I.endF, sizeof(double4_32a) * ne, cudaMemcpyDeviceToHost));
+            WG_CUDA_TRY(cudaMemcpy(ef.data(), S.I.endA, sizeof(double4_32a) * ne, cudaMemcpyDeviceToHost));
         }
         for (int64_t c = 0; c < n; c++) {
             const bool aIsLo = !(flc[c] & C_SWAP);
@@ -830,9 +910,14 @@ static int collectContacts(Sim& S, std::vector<int64_t>& keep, std::vector<uint6
             for (int64_t c = 0; c < n; c++) {
                 const int map[] = {CF_T0X, CF_T0Y, CF_T0Z, CF_T1X, CF_T1Y, CF_T1Z};
                 for (int q = 0; q < 6; q++) cols[CC_T0X + q][c] = fc[map[q]][c];
-                cols[CC_FN][c] = fc[CF_FN][c];
-                cols[CC_FT1][c] = fc[CF_FT1][c];
-                cols[CC_FT2][c] = fc[CF_FT2][c];
+                // phys.force (local) = trsf^T * (global force on pA), trsf = (c0, c1, c0 x c1)
+                const double t0[3] = {fc[CF_T0X][c], fc[CF_T0Y][c], fc[CF_T0Z][c]};
+                const double t1[3] = {fc[CF_T1X][c], fc[CF_T1Y][c], fc[CF_T1Z][c]};
+                const double t2[3] = {t0[1] * t1[2] - t0[2] * t1[1], t0[2] * t1[0] - t0[0] * t1[2], t0[0] * t1[1] - t0[1] * t1[0]};
+                const double F[3] = {cols[CC_NCOL][c], cols[CC_NCOL + 1][c], cols[CC_NCOL + 2][c]};
+                cols[CC_FN][c] = t0[0] * F[0] + t0[1] * F[1] + t0[2] * F[2];
+                cols[CC_FT1][c] = t1[0] * F[0] + t1[1] * F[1] + t1[2] * F[2];
+                cols[CC_FT2][c] = t2[0] * F[0] + t2[1] * F[1] + t2[2] * F[2];
                 if (ctype(fl[c]) == CT_SS) {
                     // contact point = x_A + (r_A + uN/2) n (Sphere.cpp:103)
                     const int a = (fl[c] & C_SWAP) ? (int)(key[c] & 0xffffffffu) : (int)(key[c] >> 32);

@@ -452,7 +452,10 @@ __global__ void k_slots(const uint64_t* __restrict__ key, int64_t n, DevIncidenc
     I.slotLo[k] = I.hiStart[loP + 1] + (int32_t)k;
 }
 
-__global__ void k_heavy(DevIncidence I, DevParticles P, int threshold, int32_t* __restrict__ count) {
+// Particles summed by the block tree; the ones whose node has a free DOF are also summed before
+// every Leapfrog (the others only when the forces are reported).
+__global__ void k_heavy(DevIncidence I, DevParticles P, const uint32_t* __restrict__ nodeFlags, int threshold,
+                        int32_t* __restrict__ count) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= P.n) return;
     if (P.shape[p] == WG_SHAPE_FACET) return;
@@ -460,6 +463,7 @@ __global__ void k_heavy(DevIncidence I, DevParticles P, int threshold, int32_t* 
     if (d > threshold) {
         const int q = atomicAdd(count, 1);
         I.heavy[q] = p;
+        if ((nodeFlags[p] & F_DOF_ALL) != F_DOF_ALL) I.heavyFree[atomicAdd(count + 1, 1)] = p;
     }
 }
 
@@ -730,18 +734,18 @@ int collide_full_run(Sim& S) {
         if (!S.I.slotHi) return S.fail(WG_ERR_CUDA, "out of device memory (incidence)");
     }
     if (S.I.endCap < 2 * std::max<int64_t>(n, 1)) {
-        if (S.I.endF) { S.dfree(S.I.endF); S.dfree(S.I.endT); }
-        if (S.I.endFf) { S.dfree(S.I.endFf); S.dfree(S.I.endTf); }
-        S.I.endF = nullptr; S.I.endT = nullptr; S.I.endFf = nullptr; S.I.endTf = nullptr;
+        if (S.I.endA) { S.dfree(S.I.endA); S.dfree(S.I.endB); }
+        if (S.I.endAf) { S.dfree(S.I.endAf); S.dfree(S.I.endBf); }
+        S.I.endA = nullptr; S.I.endB = nullptr; S.I.endAf = nullptr; S.I.endBf = nullptr;
         S.I.endCap = 2 * std::max<int64_t>(n, 1) * 3 / 2 + 2048;
         if (S.prec == WG_PREC_FP32) {
-            S.I.endFf = (float4*)S.dalloc(sizeof(float4) * S.I.endCap);
-            S.I.endTf = (float4*)S.dalloc(sizeof(float4) * S.I.endCap);
-            if (!S.I.endTf) return S.fail(WG_ERR_CUDA, "out of device memory (contact ends)");
+            S.I.endAf = (float4*)S.dalloc(sizeof(float4) * S.I.endCap);
+            S.I.endBf = (float2*)S.dalloc(sizeof(float2) * S.I.endCap);
+            if (!S.I.endAf || !S.I.endBf) return S.fail(WG_ERR_CUDA, "out of device memory (contact ends)");
         } else {
-            S.I.endF = (double4_32a*)S.dalloc(sizeof(double4_32a) * S.I.endCap);
-            S.I.endT = (double4_32a*)S.dalloc(sizeof(double4_32a) * S.I.endCap);
-            if (!S.I.endT) return S.fail(WG_ERR_CUDA, "out of device memory (contact ends)");
+            S.I.endA = (double4_32a*)S.dalloc(sizeof(double4_32a) * S.I.endCap);
+            S.I.endB = (double2*)S.dalloc(sizeof(double2) * S.I.endCap);
+            if (!S.I.endA || !S.I.endB) return S.fail(WG_ERR_CUDA, "out of device memory (contact ends)");
         }
     }
     if (n > 0) {
@@ -755,18 +759,25 @@ int collide_full_run(Sim& S) {
     k_hi_start<<<(unsigned)((S.nPar + 1 + BS - 1) / BS), BS, 0, st>>>(W.hiKeysSorted, n, (int)S.nPar, S.I.hiStart);
     if (n > 0) k_slots<<<(unsigned)((n + BS - 1) / BS), BS, 0, st>>>(S.C.key, n, S.I);
     // every end starts without a contribution; the contact kernel fills the real ones this step
-    if (S.prec == WG_PREC_FP32) WG_CUDA_TRY(cudaMemsetAsync(S.I.endFf, 0, sizeof(float4) * 2 * std::max<int64_t>(n, 1), st));
-    else WG_CUDA_TRY(cudaMemsetAsync(S.I.endF, 0, sizeof(double4_32a) * 2 * std::max<int64_t>(n, 1), st));
+    const int64_t ne = 2 * std::max<int64_t>(n, 1);
+    if (S.prec == WG_PREC_FP32) {
+        WG_CUDA_TRY(cudaMemsetAsync(S.I.endAf, 0, sizeof(float4) * ne, st));
+        WG_CUDA_TRY(cudaMemsetAsync(S.I.endBf, 0, sizeof(float2) * ne, st));
+    } else {
+        WG_CUDA_TRY(cudaMemsetAsync(S.I.endA, 0, sizeof(double4_32a) * ne, st));
+        WG_CUDA_TRY(cudaMemsetAsync(S.I.endB, 0, sizeof(double2) * ne, st));
+    }
     // heavy particles
     if (!W.heavyCount) {
-        W.heavyCount = (int32_t*)S.dalloc(sizeof(int32_t));
-        WG_CUDA_TRY(cudaMallocHost(&W.hHeavy, sizeof(int32_t)));
+        W.heavyCount = (int32_t*)S.dalloc(sizeof(int32_t) * 2);
+        WG_CUDA_TRY(cudaMallocHost(&W.hHeavy, sizeof(int32_t) * 2));
     }
-    WG_CUDA_TRY(cudaMemsetAsync(W.heavyCount, 0, sizeof(int32_t), st));
-    k_heavy<<<(unsigned)((S.nPar + BS - 1) / BS), BS, 0, st>>>(S.I, S.P, 64, W.heavyCount);
-    WG_CUDA_TRY(cudaMemcpyAsync(W.hHeavy, W.heavyCount, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    WG_CUDA_TRY(cudaMemsetAsync(W.heavyCount, 0, sizeof(int32_t) * 2, st));
+    k_heavy<<<(unsigned)((S.nPar + BS - 1) / BS), BS, 0, st>>>(S.I, S.P, S.N.flags, kHeavyThreshold, W.heavyCount);
+    WG_CUDA_TRY(cudaMemcpyAsync(W.hHeavy, W.heavyCount, sizeof(int32_t) * 2, cudaMemcpyDeviceToHost, st));
     WG_CUDA_TRY(cudaStreamSynchronize(st));
-    S.I.nHeavy = S.cfg.apply_forces ? *W.hHeavy : 0;
+    S.I.nHeavy = S.cfg.apply_forces ? W.hHeavy[0] : 0;
+    S.I.nHeavyFree = S.cfg.apply_forces ? W.hHeavy[1] : 0;
     WG_CUDA_TRY(cudaGetLastError());
     S.nFullRuns++;
     return 0;

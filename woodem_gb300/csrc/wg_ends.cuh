@@ -1,0 +1,111 @@
+// Per-particle force/torque sum over the end slots of the contact incidence (DevIncidence),
+// shared by the Leapfrog kernels (which fuse the sum into the integration) and by the
+// reporting kernels that write DemData.force/torque.
+//
+// A warp handles 32 consecutive particles, whose end slots form one contiguous run of the end
+// arrays. The warp stages that run through shared memory in chunks with coalesced loads; each
+// lane then adds its own particle's slots in slot order (ascending id of the other particle),
+// so every lane's sum is the serial sum of the reference's deterministic pass
+// (pkg/dem/ContactLoop.cpp:250-257): F = m*g, then each end in order, T = 0, then each end.
+// Lanes that take no part (facets, particles past the end, particles whose degree exceeds
+// kHeavyThreshold and which are summed by the block tree instead) are left out of the staged
+// range, so a wall with thousands of contacts does not stall the warp of its neighbours.
+#pragma once
+#include "wg_internal.h"
+#include "wg_math.cuh"
+
+namespace wg {
+
+template <typename EA, typename EB, int CH>
+struct EndStage {
+    EA a[CH];
+    EB b[CH];
+};
+
+// FP64 accumulation (FP64 ends): F and T start from the reset value and take each end in turn.
+struct SumD {
+    D3 F, T;
+    __device__ __forceinline__ void add(const double4_32a& x, const double2& y) {
+        F = F + D3{x.x, x.y, x.z};
+        T = T + D3{x.w, y.x, y.y};
+    }
+};
+
+// Knuth's TwoSum: s + e == a + b exactly (round-to-nearest FP32; the intrinsics are never
+// contracted or reassociated).
+__device__ __forceinline__ void twoSum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// Compensated accumulation of FP32 ends (FP32-force mode): each component is carried as an
+// unevaluated FP32 pair hi + lo with the rounding error of every addition captured exactly by
+// TwoSum, which keeps ~48 significant bits, and is converted to FP64 once per particle. On
+// GB300 the FP64 pipe issues at 1/64 of the FP32 rate, and a per-end FP64 add (with the
+// conversion of each addend) would cost more than the whole contact evaluation.
+struct DF6 {
+    float h[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, l[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    __device__ __forceinline__ void add1(int k, float v) {
+        float s, e;
+        twoSum(h[k], v, s, e);
+        h[k] = s;
+        l[k] = __fadd_rn(l[k], e);
+    }
+    __device__ __forceinline__ void add(const float4& x, const float2& y) {
+        add1(0, x.x); add1(1, x.y); add1(2, x.z);
+        add1(3, x.w); add1(4, y.x); add1(5, y.y);
+    }
+    __device__ __forceinline__ double val(int k) const { return (double)h[k] + (double)l[k]; }
+    // F = G + sum of forces, T = sum of torques
+    __device__ __forceinline__ void result(const D3& G, D3& F, D3& T) const {
+        F = G + D3{val(0), val(1), val(2)};
+        T = D3{val(3), val(4), val(5)};
+    }
+};
+
+// Adds the end slots [e0, e1) of every lane with take==true to acc. Must be called by all
+// 32 lanes of the warp (warp-uniform control flow inside).
+template <typename EA, typename EB, int CH, typename Acc>
+__device__ __forceinline__ void warpSumEnds(const EA* __restrict__ endA, const EB* __restrict__ endB, bool take, int e0, int e1,
+                                            EndStage<EA, EB, CH>& st, Acc& acc) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    if (!take) { e0 = 0; e1 = 0; }
+    const unsigned skip = __ballot_sync(FULL, !take || e1 <= e0);
+    int g = 0;
+    while (g < 32) {
+        const unsigned cand = ~skip & (FULL << g);
+        if (!cand) break;
+        const int s = __ffs(cand) - 1;                       // first lane of a group of takers
+        const unsigned after = skip & (FULL << s);
+        const int e = after ? __ffs(after) - 1 : 32;         // one past its last lane
+        const int lo = __shfl_sync(FULL, e0, s), hi = __shfl_sync(FULL, e1, e - 1);
+        for (int base = lo; base < hi; base += CH) {
+            const int cnt = min(CH, hi - base);
+            for (int q = lane; q < cnt; q += 32) {
+                st.a[q] = endA[base + q];
+                st.b[q] = endB[base + q];
+            }
+            __syncwarp();
+            if (lane >= s && lane < e) {
+                const int a = max(e0, base), b = min(e1, base + cnt);
+                for (int q = a; q < b; q++) acc.add(st.a[q - base], st.b[q - base]);
+            }
+            __syncwarp();
+        }
+        g = e;
+    }
+}
+
+// Degree of particle p in the incidence and the first of its end slots.
+__device__ __forceinline__ void endRange(const DevIncidence& I, int p, int& e0, int& e1) {
+    e0 = I.hiStart[p] + I.loStart[p];
+    e1 = I.hiStart[p + 1] + I.loStart[p + 1];
+}
+
+// Step-loop guard: a kernel of a step does nothing once a full collider run is pending, an
+// error was raised, or an earlier step halted the queued steps.
+__device__ __forceinline__ bool halted(const int* f) { return f[FL_HALT] != 0 || f[FL_ERR] != 0; }
+
+}  // namespace wg

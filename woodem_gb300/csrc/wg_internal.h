@@ -59,6 +59,10 @@ struct DevNodes {
     double4_32a* minert;  // ix iy iz mass
     double4_32a* lastPos; // verlet reference position
     uint32_t* flags;
+    // FP32-force mode: double-float mirrors written by Leapfrog for the sphere-sphere contacts
+    // (x = hi + lo): ph/pl = position and radius, vh/vl = velocity with angVel.x/.y in w, wz = angVel.z
+    float4 *ph, *pl, *vh, *vl;
+    float* wz;
 };
 struct DevParticles {
     int32_t n;
@@ -83,7 +87,6 @@ enum {
     CF_T0X, CF_T0Y, CF_T0Z, CF_T1X, CF_T1Y, CF_T1Z,  // trsf columns 0 and 1
     CF_UN,                                           // L6Geom.uN of the last step
     CF_P0, CF_P1, CF_P2, CF_P3,                      // FrictPhys kn kt tanPhi | HertzPhys kn0 kt0 tanPhi alpha_sqrtMK
-    CF_FN, CF_FT1, CF_FT2,                           // phys.force (local), for reporting
     CF_NCOL
 };
 struct DevContacts {
@@ -99,22 +102,30 @@ struct DevContacts {
 // Particle p owns the end slots [hiStart[p]+loStart[p], hiStart[p+1]+loStart[p+1]): first its
 // contacts with lower-id partners (ascending), then those with higher-id partners (ascending),
 // i.e. the order in which the reference's deterministic pass over key-sorted contacts adds them
-// (ContactLoop.cpp:250-257). The contact kernel stores each end's force and torque in its slot;
-// the force sum reads each particle's slots as one contiguous run.
+// (ContactLoop.cpp:250-257). The contact kernel stores each end's force and torque in its slot
+// (zero while the contact is not real); the force sum reads each particle's slots as one
+// contiguous run.
 struct DevIncidence {
     int32_t* loStart;  // nPar+1: contacts with lo==p are [loStart[p], loStart[p+1])
     int32_t* hiStart;  // nPar+1: hiList[hiStart[p] .. hiStart[p+1]) are contacts with hi==p, ascending
     int32_t* hiList;
     int32_t* slotLo;   // per contact: end slot of its lo particle
     int32_t* slotHi;   // per contact: end slot of its hi particle
-    double4_32a* endF; // FP64 mode: force on the particle (xyz) and a contribution flag (w)
-    double4_32a* endT; // FP64 mode: torque on the particle about its node
-    float4* endFf;     // FP32-force mode: the same in FP32
-    float4* endTf;
+    double4_32a* endA; // FP64 mode: (Fx, Fy, Fz, Tx) on the particle, torque about its node
+    double2* endB;     // FP64 mode: (Ty, Tz)
+    float4* endAf;     // FP32-force mode: the same in FP32
+    float2* endBf;
     int64_t endCap;
-    int32_t* heavy;    // particles whose degree exceeds the serial threshold
-    int32_t nHeavy;
+    int32_t* heavy;      // [0, nHeavy): particles whose degree exceeds kHeavyThreshold
+    int32_t* heavyFree;  // [0, nHeavyFree): those of them whose node has a free DOF
+    int32_t nHeavy, nHeavyFree;
 };
+// Particles with more end slots than this are summed by a block tree instead of one lane.
+constexpr int kHeavyThreshold = 64;
+// Step-loop flag words (device int[3]).
+enum { FL_FULL = 0,   // set by Leapfrog: a node moved farther than verletDist, a full collider run is due
+       FL_ERR = 1,    // error code raised by a kernel
+       FL_HALT = 2 }; // set by the contact kernel of a step that found FL_FULL: later queued steps do nothing
 
 __host__ __device__ inline int32_t packCellDist(int a, int b, int c) {
     return (int32_t)(((uint32_t)(a + 512) & 1023u) | (((uint32_t)(b + 512) & 1023u) << 10) | (((uint32_t)(c + 512) & 1023u) << 20));
@@ -126,18 +137,27 @@ __host__ __device__ inline void unpackCellDist(int32_t p, int& a, int& b, int& c
 }
 
 // ------------------------------------------------------------------ launchers (wg_step.cu)
-void launch_leapfrog(cudaStream_t st, const DevNodes& N, const DevParticles& P, const ScenePar* sp, int* dFull);
+// One step is: [heavy sums] -> Leapfrog (with the force sum of the other particles fused in)
+// -> (collider full run, host-driven) -> contact kernel -> step counter. Every per-step kernel
+// takes the flag words and does nothing once FL_HALT or FL_ERR is set, so the host can queue
+// several steps without waiting for each verlet test.
+// fromEnds = 0: take DemData.force/torque as stored (first step after the host wrote the state).
+void launch_leapfrog(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const ScenePar* sp,
+                     int* dFlags, int fromEnds);
 void launch_contact_fp64(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C,
-                         const DevIncidence& I, const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dErr);
-void launch_reduce(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C,
-                   const DevIncidence& I, const ScenePar* sp, long long* dStep);
+                         const DevIncidence& I, const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dFlags);
+// perStep: only the heavy particles with a free DOF (guarded by the flags), before Leapfrog;
+// otherwise every particle's DemData.force/torque (reporting at the end of a run).
+void launch_forces(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const ScenePar* sp,
+                   const int* dFlags, bool perStep);
+void launch_advance(cudaStream_t st, long long* dStep, const int* dFlags);
 // FP32-force mode (wg_step32.cu)
-void launch_leapfrog32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const double4_32a* invm, const ScenePar* sp,
-                       int* dFull);
+void launch_leapfrog32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const double4_32a* invm,
+                       const ScenePar* sp, int* dFlags, int fromEnds);
 void launch_contact_fp32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C,
-                         const DevIncidence& I, const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dErr);
-void launch_reduce32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C,
-                     const DevIncidence& I, const ScenePar* sp, long long* dStep);
+                         const DevIncidence& I, const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dFlags);
+void launch_forces32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const ScenePar* sp,
+                     const int* dFlags, bool perStep);
 
 // ------------------------------------------------------------------ broad phase (wg_collide.cu)
 struct Grid {
@@ -194,7 +214,9 @@ struct Sim {
     int64_t step = 0;
     double time = 0;
     int64_t nFullRuns = 0;
+    bool fromEnds = false;   // the end slots hold the forces of the last contact loop
     // timing
+    std::vector<cudaEvent_t> evPool;  // per queued step: before Leapfrog, before contacts, after
     cudaEvent_t ev[8];
     double lastTotalMs = 0, phaseMs[4] = {0, 0, 0, 0};
     int64_t lastLaunches = 0;

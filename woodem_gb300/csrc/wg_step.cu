@@ -4,6 +4,9 @@
 // Compiled with --fmad=false: every floating-point result is the correctly rounded
 // value of the operation sequence written here, which is the operation sequence of
 // the reference expression cited beside it.
+#include <algorithm>
+
+#include "wg_ends.cuh"
 #include "wg_geom.cuh"
 
 namespace wg {
@@ -22,13 +25,43 @@ __device__ __forceinline__ double sgn(double s) { return s < 0 ? -1 : (s > 0 ? 1
 // applyPeriodicCorrections :258-272, leapfrogTranslate :275-278, leapfrogSphericalRotate :280-288,
 // and the verlet-distance test of InsertionSortCollider::updateBboxes_doFullRun
 // pkg/dem/InsertionSortCollider.cpp:339-350 on the new positions.
-__global__ void k_leapfrog(DevNodes N, const int32_t* __restrict__ pshape, int nPar, const ScenePar* __restrict__ spp,
-                           int* __restrict__ dFull) {
+__global__ void __launch_bounds__(256) k_leapfrog(DevNodes N, DevParticles P, DevIncidence I, const ScenePar* __restrict__ spp,
+                                                  int* __restrict__ dFlags, int fromEnds) {
+    __shared__ EndStage<double4_32a, double2, 32> stage[8];
+    if (halted(dFlags)) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= N.n) return;
+    const bool valid = i < N.n;
     const ScenePar& sp = *spp;
-    const uint32_t flags = N.flags[i];
-    if (flags & F_CLUMPED) return;
+    const int nPar = P.n;
+    const uint32_t flags = valid ? N.flags[i] : 0u;
+    const double4_32a mi = valid ? N.minert[i] : make_double4_32a(0., 0., 0., 0.);
+    const double mass = mi.w;
+    // DemData.force/torque of this step: m*g plus the end slots written by the last contact
+    // loop (the force reset of Leapfrog.cpp:240-245 followed by the deterministic sum of
+    // ContactLoop.cpp:250-257), or the stored value
+    const bool uni = valid && i < nPar && P.shape[i] != WG_SHAPE_FACET;
+    int e0 = 0, e1 = 0;
+    bool take = false;
+    D3 f{0, 0, 0}, t{0, 0, 0};
+    if (fromEnds && uni) {
+        if (sp.hasGravity && !(flags & F_GRAVITY_SKIP)) f = mass * D3{sp.g[0], sp.g[1], sp.g[2]};
+        if (sp.applyForces) {
+            endRange(I, i, e0, e1);
+            take = (e1 - e0) <= kHeavyThreshold;
+            if (!take) {  // summed by the block tree before this kernel
+                f = ld3(N.force[i]);
+                t = ld3(N.torque[i]);
+            }
+        }
+    } else if (valid) {
+        f = ld3(N.force[i]);
+        t = ld3(N.torque[i]);
+    }
+    SumD acc{f, t};
+    warpSumEnds(I.endA, I.endB, take, e0, e1, stage[threadIdx.x >> 5], acc);
+    f = acc.F;
+    t = acc.T;
+    if (!valid || (flags & F_CLUMPED)) return;
     const double dt = sp.dt;
     const double damping = sp.damping;
     const bool damp = (damping != 0. && !(flags & F_DAMPING_SKIP));
@@ -36,11 +69,7 @@ __global__ void k_leapfrog(DevNodes N, const int32_t* __restrict__ pshape, int n
     D3 pos = ld3(pr);
     D3 vel = ld3(N.vel[i]);
     D3 angVel = ld3(N.angv[i]);
-    const double4_32a mi = N.minert[i];
     const D3 inertia{mi.x, mi.y, mi.z};
-    const double mass = mi.w;
-    const D3 f = ld3(N.force[i]);
-    const D3 t = ld3(N.torque[i]);
     const bool blockedAll = (flags & F_DOF_ALL) == F_DOF_ALL;
     const int homoDeform = sp.periodic ? sp.homoDeform : -1;
     D3 linAccel{0, 0, 0};
@@ -113,7 +142,7 @@ __global__ void k_leapfrog(DevNodes N, const int32_t* __restrict__ pshape, int n
     N.ori[i] = make_double4_32a(ori.w, ori.x, ori.y, ori.z);
     // Leapfrog(reset=True) for nodes whose force is not rebuilt by the contact sum
     // (facet vertices): force = mass*gravity, torque = 0 (Leapfrog.cpp:240-245)
-    if (sp.reset && (i >= nPar || pshape[i] == WG_SHAPE_FACET)) {
+    if (sp.reset && !uni) {
         D3 G{0, 0, 0};
         if (sp.hasGravity && !(flags & F_GRAVITY_SKIP)) G = mass * D3{sp.g[0], sp.g[1], sp.g[2]};
         N.force[i] = st4(G, 0.);
@@ -122,12 +151,13 @@ __global__ void k_leapfrog(DevNodes N, const int32_t* __restrict__ pshape, int n
     // verlet test (d2 + moveDueToRot2 > maxD2 with no rotation term for spheres, walls, facets)
     const D3 lp = ld3(N.lastPos[i]);
     const double d2 = sqn(lp - pos);
-    if (d2 + 0. > sp.maxD2) atomicOr(dFull, 1);
+    if (d2 + 0. > sp.maxD2) atomicOr(dFlags + FL_FULL, 1);
 }
 
-void launch_leapfrog(cudaStream_t st, const DevNodes& N, const DevParticles& P, const ScenePar* sp, int* dFull) {
+void launch_leapfrog(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const ScenePar* sp,
+                     int* dFlags, int fromEnds) {
     if (N.n == 0) return;
-    k_leapfrog<<<(N.n + 255) / 256, 256, 0, st>>>(N, P.shape, P.n, sp, dFull);
+    k_leapfrog<<<(N.n + 255) / 256, 256, 0, st>>>(N, P, I, sp, dFlags, fromEnds);
 }
 
 // ---------------------------------------------------------------------------------- ContactLoop
@@ -138,13 +168,23 @@ void launch_leapfrog(cudaStream_t st, const DevNodes& N, const DevParticles& P, 
 // Clear the end slots of a contact that stops being real (its last contribution must vanish).
 __device__ __forceinline__ void clearEnds(const DevIncidence& I, int64_t c) {
     const double4_32a z = make_double4_32a(0., 0., 0., 0.);
-    I.endF[I.slotLo[c]] = z;
-    I.endF[I.slotHi[c]] = z;
+    const double2 z2 = make_double2(0., 0.);
+    const int32_t sl = I.slotLo[c], sh = I.slotHi[c];
+    I.endA[sl] = z;
+    I.endB[sl] = z2;
+    I.endA[sh] = z;
+    I.endB[sh] = z2;
 }
 
 __global__ void __launch_bounds__(128) k_contact_fp64(DevNodes N, DevParticles P, DevContacts C, DevIncidence I,
                                                      const double4_32a* __restrict__ mats, const ScenePar* __restrict__ spp,
-                                                     const long long* __restrict__ dStep, int* __restrict__ dErr) {
+                                                     const long long* __restrict__ dStep, int* __restrict__ dFlags) {
+    if (dFlags[FL_FULL] || halted(dFlags)) {
+        // the collider runs before this step's contacts; the steps queued after it wait
+        if (blockIdx.x == 0 && threadIdx.x == 0) dFlags[FL_HALT] = 1;
+        return;
+    }
+    int* dErr = dFlags + FL_ERR;
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= C.n) return;
     const ScenePar& sp = *spp;
@@ -348,15 +388,15 @@ __global__ void __launch_bounds__(128) k_contact_fp64(DevNodes N, DevParticles P
             const D3 xcA = g.contPt - ld3(N.posr[A]);
             const D3 TA = cross(xcA, FA) + D3{0, 0, 0};
             const int sA = aIsLo ? I.slotLo[c] : I.slotHi[c];
-            I.endF[sA] = make_double4_32a(FA.x, FA.y, FA.z, 1.);
-            I.endT[sA] = make_double4_32a(TA.x, TA.y, TA.z, 0.);
+            I.endA[sA] = make_double4_32a(FA.x, FA.y, FA.z, TA.x);
+            I.endB[sA] = make_double2(TA.y, TA.z);
         }
         const D3 FB = Fg * -1.0;
         const D3 xcB = g.contPt - (ld3(N.posr[B]) + (sp.periodic ? shift2 : D3{0, 0, 0}));
         const D3 TB = cross(xcB, FB) + D3{0, 0, 0};
         const int sB = aIsLo ? I.slotHi[c] : I.slotLo[c];
-        I.endF[sB] = make_double4_32a(FB.x, FB.y, FB.z, 1.);
-        I.endT[sB] = make_double4_32a(TB.x, TB.y, TB.z, 0.);
+        I.endA[sB] = make_double4_32a(FB.x, FB.y, FB.z, TB.x);
+        I.endB[sB] = make_double2(TB.y, TB.z);
     }
     C.col[CC_T0X][c] = c0.x;
     C.col[CC_T0Y][c] = c0.y;
@@ -374,56 +414,56 @@ __global__ void __launch_bounds__(128) k_contact_fp64(DevNodes N, DevParticles P
 }
 
 void launch_contact_fp64(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C, const DevIncidence& I,
-                         const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dErr) {
-    if (C.n == 0) return;
+                         const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dFlags) {
     const int bs = 128;
-    k_contact_fp64<<<(unsigned)((C.n + bs - 1) / bs), bs, 0, st>>>(N, P, C, I, mats, sp, dStep, dErr);
+    // launched even without contacts: it raises FL_HALT when a full run is due
+    k_contact_fp64<<<(unsigned)std::max<int64_t>(1, (C.n + bs - 1) / bs), bs, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags);
 }
 
 // ---------------------------------------------------------------------------------- force sum
-// Per-particle sum replacing DemData::addForceTorque (pkg/dem/Particle.hpp:221) in the serial
-// deterministic pass (ContactLoop.cpp:250-257), with the force reset of Leapfrog
-// (Leapfrog.cpp:240-245): F = m*g, T = 0, then every contributing end slot of the particle in
-// slot order (ascending id of the other particle).
-__global__ void k_reduce(DevNodes N, DevParticles P, DevIncidence I, const ScenePar* __restrict__ spp, int heavyThreshold) {
+// DemData.force/torque for reporting after a run: the sum of the Leapfrog kernel (m*g, then every
+// end slot of the particle in slot order) written to the node, for every particle whose degree
+// is at most kHeavyThreshold.
+__global__ void __launch_bounds__(256) k_forces(DevNodes N, DevParticles P, DevIncidence I, const ScenePar* __restrict__ spp) {
+    __shared__ EndStage<double4_32a, double2, 32> stage[8];
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= P.n) return;
-    const int sh = P.shape[p];
-    if (sh == WG_SHAPE_FACET) return;
     const ScenePar& sp = *spp;
-    const uint32_t flags = N.flags[p];
-    const double mass = N.minert[p].w;
+    const bool uni = p < P.n && P.shape[p] != WG_SHAPE_FACET;
+    int e0 = 0, e1 = 0;
+    bool take = false;
     D3 F{0, 0, 0}, T{0, 0, 0};
-    if (sp.hasGravity && !(flags & F_GRAVITY_SKIP)) F = mass * D3{sp.g[0], sp.g[1], sp.g[2]};
-    if (sp.applyForces) {
-        const int e0 = I.hiStart[p] + I.loStart[p], e1 = I.hiStart[p + 1] + I.loStart[p + 1];
-        if (e1 - e0 > heavyThreshold) return;  // summed by k_reduce_heavy
-        for (int e = e0; e < e1; e++) {
-            const double4_32a f = I.endF[e];
-            if (f.w == 0.) continue;
-            const double4_32a t = I.endT[e];
-            F = F + D3{f.x, f.y, f.z};
-            T = T + D3{t.x, t.y, t.z};
+    if (uni) {
+        const uint32_t flags = N.flags[p];
+        const double mass = N.minert[p].w;
+        if (sp.hasGravity && !(flags & F_GRAVITY_SKIP)) F = mass * D3{sp.g[0], sp.g[1], sp.g[2]};
+        if (sp.applyForces) {
+            endRange(I, p, e0, e1);
+            take = (e1 - e0) <= kHeavyThreshold;
         }
     }
-    N.force[p] = st4(F, 0.);
-    N.torque[p] = st4(T, 0.);
+    SumD acc{F, T};
+    warpSumEnds(I.endA, I.endB, take, e0, e1, stage[threadIdx.x >> 5], acc);
+    if (uni && (take || !sp.applyForces)) {
+        N.force[p] = st4(acc.F, 0.);
+        N.torque[p] = st4(acc.T, 0.);
+    }
 }
 
 // Particles with many contacts (walls): one block each, fixed-shape tree sum (deterministic,
-// same result on every run; rounding differs from the serial order only for these particles,
-// whose DOFs are blocked in every supported scene).
-__global__ void k_reduce_heavy(DevNodes N, DevIncidence I, const ScenePar* __restrict__ spp) {
-    const int p = I.heavy[blockIdx.x];
+// same result on every run; rounding differs from the serial order only for these particles).
+__global__ void k_forces_heavy(DevNodes N, DevIncidence I, const int32_t* __restrict__ list, const ScenePar* __restrict__ spp,
+                               const int* __restrict__ dFlags) {
+    if (dFlags && halted(dFlags)) return;
+    const int p = list[blockIdx.x];
     const ScenePar& sp = *spp;
-    const int e0 = I.hiStart[p] + I.loStart[p], e1 = I.hiStart[p + 1] + I.loStart[p + 1];
+    int e0, e1;
+    endRange(I, p, e0, e1);
     D3 F{0, 0, 0}, T{0, 0, 0};
     for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-        const double4_32a f = I.endF[e];
-        if (f.w == 0.) continue;
-        const double4_32a t = I.endT[e];
-        F = F + D3{f.x, f.y, f.z};
-        T = T + D3{t.x, t.y, t.z};
+        const double4_32a a = I.endA[e];
+        const double2 b = I.endB[e];
+        F = F + D3{a.x, a.y, a.z};
+        T = T + D3{a.w, b.x, b.y};
     }
     __shared__ double sh[6][256];
     sh[0][threadIdx.x] = F.x; sh[1][threadIdx.x] = F.y; sh[2][threadIdx.x] = F.z;
@@ -444,17 +484,23 @@ __global__ void k_reduce_heavy(DevNodes N, DevIncidence I, const ScenePar* __res
     }
 }
 
-__global__ void k_step_advance(long long* dStep) { *dStep += 1; }
-
-static const int kHeavyThreshold = 64;
-
-void launch_reduce(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C, const DevIncidence& I,
-                   const ScenePar* sp, long long* dStep) {
-    if (P.n > 0) {
-        k_reduce<<<(P.n + 255) / 256, 256, 0, st>>>(N, P, I, sp, kHeavyThreshold);
-        if (I.nHeavy > 0) k_reduce_heavy<<<I.nHeavy, 256, 0, st>>>(N, I, sp);
-    }
-    k_step_advance<<<1, 1, 0, st>>>(dStep);
+// Scene::doOneStep's step counter (core/Scene.cpp:386), advanced only by a step that completed.
+__global__ void k_step_advance(long long* dStep, const int* __restrict__ dFlags) {
+    if (dFlags[FL_FULL] || halted(dFlags)) return;
+    *dStep += 1;
 }
+
+void launch_forces(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const ScenePar* sp,
+                   const int* dFlags, bool perStep) {
+    if (P.n == 0) return;
+    if (perStep) {
+        if (I.nHeavyFree > 0) k_forces_heavy<<<I.nHeavyFree, 256, 0, st>>>(N, I, I.heavyFree, sp, dFlags);
+        return;
+    }
+    k_forces<<<(P.n + 255) / 256, 256, 0, st>>>(N, P, I, sp);
+    if (I.nHeavy > 0) k_forces_heavy<<<I.nHeavy, 256, 0, st>>>(N, I, I.heavy, sp, nullptr);
+}
+
+void launch_advance(cudaStream_t st, long long* dStep, const int* dFlags) { k_step_advance<<<1, 1, 0, st>>>(dStep, dFlags); }
 
 }  // namespace wg

@@ -9,6 +9,9 @@
 // mid-step branches of L6Geom.cpp:156-160 need only the previous normal and uN.
 //
 // Compiled with --fmad=true (results are compared to the FP64 oracle within a tolerance).
+#include <algorithm>
+
+#include "wg_ends.cuh"
 #include "wg_geom.cuh"
 
 namespace wg {
@@ -25,6 +28,11 @@ __device__ __forceinline__ F3 operator*(F3 a, float s) { return F3{a.x * s, a.y 
 __device__ __forceinline__ F3 operator*(float s, F3 a) { return F3{s * a.x, s * a.y, s * a.z}; }
 __device__ __forceinline__ float fdot(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 __device__ __forceinline__ F3 fcross(F3 a, F3 b) { return F3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+// x = h + l with h = fl32(x) and l = fl32(x - h); |x - (h + l)| <= 2^-48 |x| (x - h is exact in FP64)
+__device__ __forceinline__ void splitDF(double x, float& h, float& l) {
+    h = __double2float_rn(x);
+    l = __double2float_rn(x - (double)h);
+}
 __device__ __forceinline__ F3 fnormalized(F3 a) {
     const float z = fdot(a, a);
     return z > 0.f ? a * rsqrtf(z) : a;
@@ -33,13 +41,42 @@ __device__ __forceinline__ F3 fnormalized(F3 a) {
 // ---------------------------------------------------------------------------------- Leapfrog
 // Leapfrog::run (pkg/dem/Leapfrog.cpp:103-255) with precomputed 1/m and 1/I; the node
 // orientation (which no force of the supported shapes depends on) is advanced in FP32.
-__global__ void k_leapfrog32(DevNodes N, const double4_32a* __restrict__ invm, const int32_t* __restrict__ pshape, int nPar,
-                             const ScenePar* __restrict__ spp, int* __restrict__ dFull) {
+__global__ void __launch_bounds__(256) k_leapfrog32(DevNodes N, DevParticles P, DevIncidence I, const double4_32a* __restrict__ invm,
+                                                    const ScenePar* __restrict__ spp, int* __restrict__ dFlags, int fromEnds) {
+    __shared__ EndStage<float4, float2, 64> stage[8];
+    if (halted(dFlags)) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= N.n) return;
+    const bool valid = i < N.n;
     const ScenePar& sp = *spp;
-    const uint32_t flags = N.flags[i];
-    if (flags & F_CLUMPED) return;
+    const uint32_t flags = valid ? N.flags[i] : 0u;
+    const double mass = valid ? N.minert[i].w : 0.;
+    // DemData.force/torque: m*g plus the compensated sum of the FP32 end slots of the last
+    // contact loop (see DF6), or the stored value
+    const bool uni = valid && i < P.n && P.shape[i] != WG_SHAPE_FACET;
+    int e0 = 0, e1 = 0;
+    bool take = false;
+    D3 f{0, 0, 0}, t{0, 0, 0};
+    if (fromEnds && uni) {
+        if (sp.hasGravity && !(flags & F_GRAVITY_SKIP)) f = mass * D3{sp.g[0], sp.g[1], sp.g[2]};
+        if (sp.applyForces) {
+            endRange(I, i, e0, e1);
+            take = (e1 - e0) <= kHeavyThreshold;
+            if (!take) {
+                f = ld3(N.force[i]);
+                t = ld3(N.torque[i]);
+            }
+        }
+    } else if (valid) {
+        f = ld3(N.force[i]);
+        t = ld3(N.torque[i]);
+    }
+    DF6 acc;
+    warpSumEnds(I.endAf, I.endBf, take, e0, e1, stage[threadIdx.x >> 5], acc);
+    if (take) {
+        const D3 G = f;
+        acc.result(G, f, t);
+    }
+    if (!valid || (flags & F_CLUMPED)) return;
     const double dt = sp.dt;
     const double damping = sp.damping;
     const bool damp = (damping != 0. && !(flags & F_DAMPING_SKIP));
@@ -48,9 +85,6 @@ __global__ void k_leapfrog32(DevNodes N, const double4_32a* __restrict__ invm, c
     D3 vel = ld3(N.vel[i]);
     D3 angVel = ld3(N.angv[i]);
     const double4_32a iv = invm[i];
-    const double mass = N.minert[i].w;
-    const D3 f = ld3(N.force[i]);
-    const D3 t = ld3(N.torque[i]);
     const bool blockedAll = (flags & F_DOF_ALL) == F_DOF_ALL;
     const int homoDeform = sp.periodic ? sp.homoDeform : -1;
     D3 linAccel{0, 0, 0};
@@ -96,6 +130,24 @@ __global__ void k_leapfrog32(DevNodes N, const double4_32a* __restrict__ invm, c
     N.posr[i] = make_double4_32a(pos.x, pos.y, pos.z, pr.w);
     N.vel[i] = make_double4_32a(vel.x, vel.y, vel.z, 0.);
     N.angv[i] = make_double4_32a(angVel.x, angVel.y, angVel.z, 0.);
+    {
+        // double-float mirrors read by the sphere-sphere contact geometry
+        float4 h, l;
+        splitDF(pos.x, h.x, l.x);
+        splitDF(pos.y, h.y, l.y);
+        splitDF(pos.z, h.z, l.z);
+        splitDF(pr.w, h.w, l.w);
+        N.ph[i] = h;
+        N.pl[i] = l;
+        splitDF(vel.x, h.x, l.x);
+        splitDF(vel.y, h.y, l.y);
+        splitDF(vel.z, h.z, l.z);
+        h.w = (float)angVel.x;
+        l.w = (float)angVel.y;
+        N.vh[i] = h;
+        N.vl[i] = l;
+        N.wz[i] = (float)angVel.z;
+    }
     if (angVel.x != 0 || angVel.y != 0 || angVel.z != 0) {
         const double4_32a o = N.ori[i];
         const F3 w = toF(angVel);
@@ -114,20 +166,20 @@ __global__ void k_leapfrog32(DevNodes N, const double4_32a* __restrict__ invm, c
             N.ori[i] = make_double4_32a(rw * inv, rx * inv, ry * inv, rz * inv);
         }
     }
-    if (sp.reset && (i >= nPar || pshape[i] == WG_SHAPE_FACET)) {
+    if (sp.reset && !uni) {
         D3 G{0, 0, 0};
         if (sp.hasGravity && !(flags & F_GRAVITY_SKIP)) G = mass * D3{sp.g[0], sp.g[1], sp.g[2]};
         N.force[i] = make_double4_32a(G.x, G.y, G.z, 0.);
         N.torque[i] = make_double4_32a(0., 0., 0., 0.);
     }
     const D3 lp = ld3(N.lastPos[i]);
-    if (sqn(lp - pos) > sp.maxD2) atomicOr(dFull, 1);
+    if (sqn(lp - pos) > sp.maxD2) atomicOr(dFlags + FL_FULL, 1);
 }
 
-void launch_leapfrog32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const double4_32a* invm, const ScenePar* sp,
-                       int* dFull) {
+void launch_leapfrog32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const double4_32a* invm,
+                       const ScenePar* sp, int* dFlags, int fromEnds) {
     if (N.n == 0) return;
-    k_leapfrog32<<<(N.n + 255) / 256, 256, 0, st>>>(N, invm, P.shape, P.n, sp, dFull);
+    k_leapfrog32<<<(N.n + 255) / 256, 256, 0, st>>>(N, P, I, invm, sp, dFlags, fromEnds);
 }
 
 // ---------------------------------------------------------------------------------- ContactLoop
@@ -166,9 +218,97 @@ __device__ __forceinline__ void frameInit(F3 n, Frame& f) {
     f.c2 = fcross(n, y);
 }
 
+// ---- double-float arithmetic for the sphere-sphere geometry (FP32 pipe only)
+// (hB + lB) - (hA + lA) as s + t with |t| << |s|: s + e = hB - hA exactly, t = e + (lB - lA).
+__device__ __forceinline__ void dfDiff(float hA, float lA, float hB, float lB, float& s, float& t) {
+    float e;
+    twoSum(hB, -hA, s, e);
+    t = e + (lB - lA);
+}
+// (s + t)^2 as p + c: p = fl(s*s), c = the FMA residual of s*s plus t*(2s + t).
+__device__ __forceinline__ void dfSquare(float s, float t, float& p, float& c) {
+    p = s * s;
+    c = fmaf(s, s, -p) + t * (2.f * s + t);
+}
+
+// Sphere-sphere overlap test and normal overlap without FP64 arithmetic. Positions, velocities
+// and radii are read from the double-float mirrors written by Leapfrog (x = hi + lo, both FP32,
+// |x - (hi + lo)| <= 2^-48 |x|), so the relative position carries ~47 bits and
+//   num = |dx|^2 - (r1 + r2)^2
+// is formed with error-free products and sums: its error is ~2^-46 |dx|^2, i.e. about
+// 1e-9 relative for an overlap of 1e-3 radius, far below the FP32 rounding of the force.
+// uN = num / (|dx| + r1 + r2) is then the overlap of Cg2_Sphere_Sphere_L6Geom
+// (pkg/dem/Sphere.cpp:97-101) without the cancellation of |dx| - (r1 + r2).
+struct SSGeo {
+    F3 n, dv, w1, w2;
+    float uN, r1, r2;
+};
+__device__ __forceinline__ bool geomSS32(const DevNodes& N, int A, int B, float dfAbs, bool real, SSGeo& g) {
+    const float4 ha = N.ph[A], la = N.pl[A], hb = N.ph[B], lb = N.pl[B];
+    float sx, tx, sy, ty, sz, tz;
+    dfDiff(ha.x, la.x, hb.x, lb.x, sx, tx);
+    dfDiff(ha.y, la.y, hb.y, lb.y, sy, ty);
+    dfDiff(ha.z, la.z, hb.z, lb.z, sz, tz);
+    float px, cx, py, cy, pz, cz;
+    dfSquare(sx, tx, px, cx);
+    dfSquare(sy, ty, py, cy);
+    dfSquare(sz, tz, pz, cz);
+    float Rs, Re;
+    twoSum(ha.w, hb.w, Rs, Re);
+    const float Rt = Re + (la.w + lb.w);
+    float a1, e1, a2, e2;
+    twoSum(px, py, a1, e1);
+    twoSum(a1, pz, a2, e2);
+    const float csum = (e1 + e2) + (cx + cy + cz);
+    // creation test of Sphere.cpp:94-96 against (|distFactor| (r1 + r2))^2
+    float Ds = Rs, Dt = Rt;
+    if (dfAbs != 1.f) {
+        float pe;
+        Ds = dfAbs * Rs;
+        pe = fmaf(dfAbs, Rs, -Ds);
+        Dt = pe + dfAbs * Rt;
+    }
+    float Dp, Dc;
+    dfSquare(Ds, Dt, Dp, Dc);
+    float b3, e3;
+    twoSum(a2, -Dp, b3, e3);
+    const float unDist = b3 + (e3 + (csum - Dc));
+    if (unDist > 0.f && !real) return false;
+    float num = unDist;
+    if (dfAbs != 1.f) {
+        float Rp, Rc;
+        dfSquare(Rs, Rt, Rp, Rc);
+        twoSum(a2, -Rp, b3, e3);
+        num = b3 + (e3 + (csum - Rc));
+    }
+    const F3 dx{sx + tx, sy + ty, sz + tz};
+    const float dist = sqrtf(a2 + csum);
+    const float R = Rs + Rt;
+    g.uN = num / (dist + R);
+    g.n = dx * (1.f / dist);
+    g.r1 = ha.w + la.w;
+    g.r2 = hb.w + lb.w;
+    const float4 vha = N.vh[A], vla = N.vl[A], vhb = N.vh[B], vlb = N.vl[B];
+    float s, t;
+    dfDiff(vha.x, vla.x, vhb.x, vlb.x, s, t);
+    g.dv.x = s + t;
+    dfDiff(vha.y, vla.y, vhb.y, vlb.y, s, t);
+    g.dv.y = s + t;
+    dfDiff(vha.z, vla.z, vhb.z, vlb.z, s, t);
+    g.dv.z = s + t;
+    g.w1 = F3{vha.w, vla.w, N.wz[A]};
+    g.w2 = F3{vhb.w, vlb.w, N.wz[B]};
+    return true;
+}
+
 __global__ void __launch_bounds__(256) k_contact_fp32(DevNodes N, DevParticles P, DevContacts C, DevIncidence I,
                                                      const double4_32a* __restrict__ mats, const ScenePar* __restrict__ spp,
-                                                     const long long* __restrict__ dStep, int* __restrict__ dErr) {
+                                                     const long long* __restrict__ dStep, int* __restrict__ dFlags) {
+    if (dFlags[FL_FULL] || halted(dFlags)) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) dFlags[FL_HALT] = 1;
+        return;
+    }
+    int* dErr = dFlags + FL_ERR;
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= C.n) return;
     const ScenePar& sp = *spp;
@@ -183,34 +323,58 @@ __global__ void __launch_bounds__(256) k_contact_fp32(DevNodes N, DevParticles P
     const long long step = *dStep;
     const double dt = sp.dt;
     const float dtf = (float)dt;
+    bool shifted = false;
     D3 shift2{0, 0, 0}, shiftVel2{0, 0, 0};
     if (sp.periodic) {
         int a, b, cc;
         unpackCellDist(C.cdist[c], a, b, cc);
         if (fl & C_SWAP) { a = -a; b = -b; cc = -cc; }
-        const D3 cd{(double)a, (double)b, (double)cc};
-        shift2 = mul(*(const DM3*)sp.hSize, cd);
-        shiftVel2 = mul(*(const DM3*)sp.shiftVelMat, cd);
+        shifted = (a | b | cc) != 0;
+        if (shifted) {
+            const D3 cd{(double)a, (double)b, (double)cc};
+            shift2 = mul(*(const DM3*)sp.hSize, cd);
+            shiftVel2 = mul(*(const DM3*)sp.shiftVelMat, cd);
+        }
     }
     // n: normal; armA/armB: contact point minus the nodes of pA/pB (torque arms, Contact.cpp:32);
     // c1x/c2x: mid-step branch vectors of L6Geom.cpp:156-160; dv: relative velocity of the centres
     F3 n, armA, armB, c1x, c2x, dv, w1, w2;
     float uN, r1, r2;
-    if (ty == CT_SS) {
+    if (ty == CT_SS && !shifted) {
+        SSGeo g;
+        if (!geomSS32(N, A, B, (float)fabs(sp.ssDistFactor), real, g)) {
+            C.flags[c] = fl;
+            return;
+        }
+        n = g.n;
+        uN = g.uN;
+        r1 = g.r1;
+        r2 = g.r2;
+        dv = g.dv;
+        w1 = g.w1;
+        w2 = g.w2;
+    } else if (ty == CT_SS) {
+        // a pair across the periodic boundary: FP64 relative position with the cell shift
         const double4_32a pa = N.posr[A], pb = N.posr[B];
         const D3 dx = (ld3(pb) + shift2) - ld3(pa);
         const double d2 = sqn(dx);
         const double R = pa.w + pb.w;
-        const double num = d2 - R * R;  // |dx|^2 - (r1+r2)^2, exact enough in FP64
-        if (num > 0 && !real) {
+        const double dfr = fabs(sp.ssDistFactor) * R;
+        if (d2 - dfr * dfr > 0 && !real) {
             C.flags[c] = fl;
             return;
         }
         const float distf = sqrtf((float)d2);
-        uN = (float)num / (distf + (float)R);  // |dx| - (r1+r2) without the cancellation
+        uN = (float)(d2 - R * R) / (distf + (float)R);
         n = toF(dx) * (1.f / distf);
         r1 = (float)pa.w;
         r2 = (float)pb.w;
+        dv = toF((ld3(N.vel[B]) + shiftVel2) - ld3(N.vel[A]));
+        w1 = toF(ld3(N.angv[A]));
+        w2 = toF(ld3(N.angv[B]));
+    }
+    if (ty == CT_SS) {
+        // contPt = x1 + (r1 + uN/2) n (Sphere.cpp:103), written relative to both centres
         armA = (r1 + 0.5f * uN) * n;
         armB = -(r2 + 0.5f * uN) * n;
         if (real) {
@@ -219,9 +383,6 @@ __global__ void __launch_bounds__(256) k_contact_fp32(DevNodes N, DevParticles P
             c1x = 0.5f * ((r1 + 0.5f * up) * pn + armA);
             c2x = 0.5f * (-(r2 + 0.5f * up) * pn + armB);
         }
-        dv = toF((ld3(N.vel[B]) + shiftVel2) - ld3(N.vel[A]));
-        w1 = toF(ld3(N.angv[A]));
-        w2 = toF(ld3(N.angv[B]));
     } else {
         Geo g;
         bool touch;
@@ -359,8 +520,11 @@ __global__ void __launch_bounds__(256) k_contact_fp32(DevNodes N, DevParticles P
     if (!keep) {
         C.flags[c] = (fl & ~C_REAL) | C_PENDING;
         if (real) {
-            I.endFf[I.slotLo[c]] = make_float4(0.f, 0.f, 0.f, 0.f);
-            I.endFf[I.slotHi[c]] = make_float4(0.f, 0.f, 0.f, 0.f);
+            const int32_t sl = I.slotLo[c], sh = I.slotHi[c];
+            I.endAf[sl] = make_float4(0.f, 0.f, 0.f, 0.f);
+            I.endBf[sl] = make_float2(0.f, 0.f);
+            I.endAf[sh] = make_float4(0.f, 0.f, 0.f, 0.f);
+            I.endBf[sh] = make_float2(0.f, 0.f);
         }
         return;
     }
@@ -370,11 +534,11 @@ __global__ void __launch_bounds__(256) k_contact_fp32(DevNodes N, DevParticles P
     {
         const int sA = aIsLo ? I.slotLo[c] : I.slotHi[c], sB = aIsLo ? I.slotHi[c] : I.slotLo[c];
         if (ty != CT_FS) {
-            I.endFf[sA] = make_float4(F.x, F.y, F.z, 1.f);
-            I.endTf[sA] = make_float4(TA.x, TA.y, TA.z, 0.f);
+            I.endAf[sA] = make_float4(F.x, F.y, F.z, TA.x);
+            I.endBf[sA] = make_float2(TA.y, TA.z);
         }
-        I.endFf[sB] = make_float4(-F.x, -F.y, -F.z, 1.f);
-        I.endTf[sB] = make_float4(TB.x, TB.y, TB.z, 0.f);
+        I.endAf[sB] = make_float4(-F.x, -F.y, -F.z, TB.x);
+        I.endBf[sB] = make_float2(TB.y, TB.z);
     }
     C.fcol[CF_T0X][c] = f.c0.x;
     C.fcol[CF_T0Y][c] = f.c0.y;
@@ -383,56 +547,57 @@ __global__ void __launch_bounds__(256) k_contact_fp32(DevNodes N, DevParticles P
     C.fcol[CF_T1Y][c] = f.c1.y;
     C.fcol[CF_T1Z][c] = f.c1.z;
     C.fcol[CF_UN][c] = uN;
-    C.fcol[CF_FN][c] = fn;
-    C.fcol[CF_FT1][c] = ft1;
-    C.fcol[CF_FT2][c] = ft2;
     C.flags[c] = fl | C_REAL;
 }
 
 void launch_contact_fp32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C, const DevIncidence& I,
-                         const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dErr) {
-    if (C.n == 0) return;
-    k_contact_fp32<<<(unsigned)((C.n + 255) / 256), 256, 0, st>>>(N, P, C, I, mats, sp, dStep, dErr);
+                         const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dFlags) {
+    k_contact_fp32<<<(unsigned)std::max<int64_t>(1, (C.n + 255) / 256), 256, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags);
 }
 
 // ---------------------------------------------------------------------------------- force sum
-// Per-particle FP64 sum of the FP32 end slots in slot order (ascending id of the other particle,
-// the order of ContactLoop.cpp:250-257 over key-sorted contacts).
-__global__ void k_reduce32(DevNodes N, DevParticles P, DevIncidence I, const ScenePar* __restrict__ spp, int heavyThreshold) {
+// DemData.force/torque for reporting after a run: the same sum as k_leapfrog32 (m*g plus the
+// compensated sum of the particle's FP32 end slots, in slot order), written to the node.
+__global__ void __launch_bounds__(256) k_forces32(DevNodes N, DevParticles P, DevIncidence I, const ScenePar* __restrict__ spp) {
+    __shared__ EndStage<float4, float2, 64> stage[8];
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= P.n) return;
-    if (P.shape[p] == WG_SHAPE_FACET) return;
     const ScenePar& sp = *spp;
-    const uint32_t flags = N.flags[p];
-    const double mass = N.minert[p].w;
-    D3 F{0, 0, 0}, T{0, 0, 0};
-    if (sp.hasGravity && !(flags & F_GRAVITY_SKIP)) F = mass * D3{sp.g[0], sp.g[1], sp.g[2]};
-    if (sp.applyForces) {
-        const int e0 = I.hiStart[p] + I.loStart[p], e1 = I.hiStart[p + 1] + I.loStart[p + 1];
-        if (e1 - e0 > heavyThreshold) return;
-        for (int e = e0; e < e1; e++) {
-            const float4 f = I.endFf[e];
-            if (f.w == 0.f) continue;
-            const float4 t = I.endTf[e];
-            F = F + D3{(double)f.x, (double)f.y, (double)f.z};
-            T = T + D3{(double)t.x, (double)t.y, (double)t.z};
+    const bool uni = p < P.n && P.shape[p] != WG_SHAPE_FACET;
+    int e0 = 0, e1 = 0;
+    bool take = false;
+    D3 G{0, 0, 0};
+    if (uni) {
+        const uint32_t flags = N.flags[p];
+        const double mass = N.minert[p].w;
+        if (sp.hasGravity && !(flags & F_GRAVITY_SKIP)) G = mass * D3{sp.g[0], sp.g[1], sp.g[2]};
+        if (sp.applyForces) {
+            endRange(I, p, e0, e1);
+            take = (e1 - e0) <= kHeavyThreshold;
         }
     }
-    N.force[p] = make_double4_32a(F.x, F.y, F.z, 0.);
-    N.torque[p] = make_double4_32a(T.x, T.y, T.z, 0.);
+    DF6 acc;
+    warpSumEnds(I.endAf, I.endBf, take, e0, e1, stage[threadIdx.x >> 5], acc);
+    if (uni && (take || !sp.applyForces)) {
+        D3 F, T;
+        acc.result(G, F, T);
+        N.force[p] = make_double4_32a(F.x, F.y, F.z, 0.);
+        N.torque[p] = make_double4_32a(T.x, T.y, T.z, 0.);
+    }
 }
 
-__global__ void k_reduce32_heavy(DevNodes N, DevIncidence I, const ScenePar* __restrict__ spp) {
-    const int p = I.heavy[blockIdx.x];
+__global__ void k_forces32_heavy(DevNodes N, DevIncidence I, const int32_t* __restrict__ list, const ScenePar* __restrict__ spp,
+                                 const int* __restrict__ dFlags) {
+    if (dFlags && halted(dFlags)) return;
+    const int p = list[blockIdx.x];
     const ScenePar& sp = *spp;
-    const int e0 = I.hiStart[p] + I.loStart[p], e1 = I.hiStart[p + 1] + I.loStart[p + 1];
+    int e0, e1;
+    endRange(I, p, e0, e1);
     D3 F{0, 0, 0}, T{0, 0, 0};
     for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-        const float4 f = I.endFf[e];
-        if (f.w == 0.f) continue;
-        const float4 t = I.endTf[e];
-        F = F + D3{(double)f.x, (double)f.y, (double)f.z};
-        T = T + D3{(double)t.x, (double)t.y, (double)t.z};
+        const float4 a = I.endAf[e];
+        const float2 b = I.endBf[e];
+        F = F + D3{(double)a.x, (double)a.y, (double)a.z};
+        T = T + D3{(double)a.w, (double)b.x, (double)b.y};
     }
     __shared__ double sh[6][256];
     sh[0][threadIdx.x] = F.x; sh[1][threadIdx.x] = F.y; sh[2][threadIdx.x] = F.z;
@@ -453,15 +618,15 @@ __global__ void k_reduce32_heavy(DevNodes N, DevIncidence I, const ScenePar* __r
     }
 }
 
-__global__ void k_step_advance32(long long* dStep) { *dStep += 1; }
-
-void launch_reduce32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C, const DevIncidence& I,
-                     const ScenePar* sp, long long* dStep) {
-    if (P.n > 0) {
-        k_reduce32<<<(P.n + 255) / 256, 256, 0, st>>>(N, P, I, sp, 64);
-        if (I.nHeavy > 0) k_reduce32_heavy<<<I.nHeavy, 256, 0, st>>>(N, I, sp);
+void launch_forces32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const ScenePar* sp,
+                     const int* dFlags, bool perStep) {
+    if (P.n == 0) return;
+    if (perStep) {
+        if (I.nHeavyFree > 0) k_forces32_heavy<<<I.nHeavyFree, 256, 0, st>>>(N, I, I.heavyFree, sp, dFlags);
+        return;
     }
-    k_step_advance32<<<1, 1, 0, st>>>(dStep);
+    k_forces32<<<(P.n + 255) / 256, 256, 0, st>>>(N, P, I, sp);
+    if (I.nHeavy > 0) k_forces32_heavy<<<I.nHeavy, 256, 0, st>>>(N, I, I.heavy, sp, nullptr);
 }
 
 }  // namespace wg

@@ -87,10 +87,33 @@ def _segment_height(R, area):
     return 0.5 * (lo + hi)
 
 
-def settle(S, steps, g_factor=30.0, damping=0.3, precision="fp32"):
+def spatial_order(points, cell):
+    """Permutation that lists ``points`` along a Morton (Z-order) curve over a grid of cubes of
+    side ``cell`` (up to 2^21 cells per axis), so that particles close in space get close ids."""
+    pts = np.asarray(points, dtype=float)
+    if len(pts) == 0:
+        return np.zeros(0, dtype=np.int64)
+    q = np.floor((pts - pts.min(axis=0)) / float(cell)).astype(np.uint64)
+    q = np.minimum(q, np.uint64((1 << 21) - 1))
+
+    def spread(v):
+        v = v & np.uint64(0x1FFFFF)
+        v = (v | (v << np.uint64(32))) & np.uint64(0x1F00000000FFFF)
+        v = (v | (v << np.uint64(16))) & np.uint64(0x1F0000FF0000FF)
+        v = (v | (v << np.uint64(8))) & np.uint64(0x100F00F00F00F00F)
+        v = (v | (v << np.uint64(4))) & np.uint64(0x10C30C30C30C30C3)
+        v = (v | (v << np.uint64(2))) & np.uint64(0x1249249249249249)
+        return v
+
+    code = spread(q[:, 0]) | (spread(q[:, 1]) << np.uint64(1)) | (spread(q[:, 2]) << np.uint64(2))
+    return np.argsort(code, kind="stable")
+
+
+def settle(S, steps, g_factor=30.0, damping=0.3, precision="fp32", relax_steps=0, relax_damping=0.5):
     """Compact a loose packing into a resting bed on the GPU: run ``steps`` steps under gravity
-    multiplied by ``g_factor`` with Leapfrog damping ``damping``, then restore the scene's gravity,
-    damping and precision, zero the velocities, forces and torques of the free nodes, and reset
+    multiplied by ``g_factor`` with Leapfrog damping ``damping``, then ``relax_steps`` steps under
+    the scene's own gravity with damping ``relax_damping``; restore the scene's gravity, damping and
+    precision, zero the velocities, forces and torques of the free nodes, and reset
     Scene.step/time. The contact history is dropped (the next run starts from the positions)."""
     lf = S.engines[0]
     g0 = np.array(S.dem.gravity, dtype=float)
@@ -100,6 +123,11 @@ def settle(S, steps, g_factor=30.0, damping=0.3, precision="fp32"):
     lf.damping = damping
     S.gpu.precision = precision
     S.run(steps)
+    if relax_steps:
+        S.close()
+        S.dem.gravity = g0
+        lf.damping = relax_damping
+        S.run(relax_steps)
     S.close()
     S.dem.gravity = g0
     lf.damping = d0
@@ -113,16 +141,7 @@ def settle(S, steps, g_factor=30.0, damping=0.3, precision="fp32"):
     return S
 
 
-def hertz_drum(n=1_000_000, seed=0, diameter=1.2, length=0.6, div=201, axDiv=50, fill_fraction=0.35, density=2500.0,
-               young=1e8, poisson=0.25, en=0.6, tanPhi=0.5, omega=1.0, verletRel=0.1, precision="fp64",
-               median=3e-3, sigma=0.25, rmin=1.5e-3, rmax=6e-3, settle_steps=0):
-    """Rotating drum: x-axis cylinder (diameter x length) meshed into 2*(div-1)*axDiv facets with
-    outward normals and fakeVel for angular velocity ``omega``, two rotating Wall end caps,
-    lognormal radii, Hertz contacts with viscous damping (en), gravity (0,0,-9.81),
-    dt = 0.3*pWaveDt, verletDist = 0.1*min radius. Spheres are placed by seeded random
-    sequential insertion (solid fraction ``fill_fraction``) in the lower part of the drum whose
-    height is chosen to hold them; with ``settle_steps`` the fill is then compacted into a resting
-    bed on the GPU (see ``settle``)."""
+def _drum_scene(centers, radii, diameter, length, div, axDiv, density, young, poisson, en, tanPhi, omega, verletRel, precision):
     R = diameter / 2.0
     S = Scene(fields=[DemField(gravity=(0, 0, -9.81))])
     S.gpu.precision = precision
@@ -130,6 +149,27 @@ def hertz_drum(n=1_000_000, seed=0, diameter=1.2, length=0.6, div=201, axDiv=50,
     drum = triangulated.cylinder((0, 0, 0), (length, 0, 0), R, div=div, axDiv=axDiv, capA=True, capB=True, wallCaps=True,
                                  angVel=omega, mat=mat)
     S.dem.par.add(drum)
+    S.dem.par.addSpheres(centers, radii, mat)
+    S.engines = utils.defaultEngines(cp2=Cp2_FrictMat_HertzPhys(poisson=poisson, en=en, gamma=0.0, alpha=0.0),
+                                     law=Law2_L6Geom_HertzPhys_DMT(), verletDist=-verletRel, dynDtPeriod=0, damping=0.0)
+    S.dt = 0.3 * utils.pWaveDt(S)
+    return S
+
+
+def hertz_drum(n=1_000_000, seed=0, diameter=1.2, length=0.6, div=201, axDiv=50, fill_fraction=0.40, density=2500.0,
+               young=1e8, poisson=0.25, en=0.6, tanPhi=0.5, omega=1.0, verletRel=0.1, precision="fp64",
+               median=3e-3, sigma=0.25, rmin=1.5e-3, rmax=6e-3, settle_steps=0, settle_g=40.0, relax_steps=None, order=True):
+    """Rotating drum: x-axis cylinder (diameter x length) meshed into 2*(div-1)*axDiv facets with
+    outward normals and fakeVel for angular velocity ``omega``, two rotating Wall end caps,
+    lognormal radii, Hertz contacts with viscous damping (en), gravity (0,0,-9.81),
+    dt = 0.3*pWaveDt, verletDist = 0.1*min radius. Spheres are placed by seeded random
+    sequential insertion (solid fraction ``fill_fraction``) in the lower part of the drum whose
+    height is chosen to hold them. With ``settle_steps`` the fill is compacted into a resting bed
+    on the GPU (``settle``: ``settle_g`` times gravity, then ``relax_steps`` steps at 1 g) and the
+    scene is rebuilt from the settled positions. With ``order`` the spheres are numbered along a
+    Morton curve of their positions (cells of one largest diameter), so that spheres in contact
+    have nearby ids; walls and facets keep the lowest ids."""
+    R = diameter / 2.0
     radii = lognormal_radii(n, seed, median, sigma, rmin, rmax)
     vol = float(np.sum((4 / 3.0) * math.pi * radii ** 3))
     margin = 1e-4
@@ -138,10 +178,23 @@ def hertz_drum(n=1_000_000, seed=0, diameter=1.2, length=0.6, div=201, axDiv=50,
     Ri = R - margin
     zf = _segment_height(Ri, min(area, 0.97 * math.pi * Ri * Ri))
     centers = pack_rsa(radii, (margin, -Ri, -Ri), (length - margin, Ri, zf), region=1, params=(0.0, 0.0, Ri, zf), seed=seed + 7)
-    S.dem.par.addSpheres(centers, radii, mat)
-    S.engines = utils.defaultEngines(cp2=Cp2_FrictMat_HertzPhys(poisson=poisson, en=en, gamma=0.0, alpha=0.0),
-                                     law=Law2_L6Geom_HertzPhys_DMT(), verletDist=-verletRel, dynDtPeriod=0, damping=0.0)
-    S.dt = 0.3 * utils.pWaveDt(S)
+    args = (diameter, length, div, axDiv, density, young, poisson, en, tanPhi, omega, verletRel)
     if settle_steps:
-        settle(S, settle_steps)
-    return S
+        S0 = _drum_scene(centers, radii, *args, precision)
+        settle(S0, settle_steps, g_factor=settle_g, relax_steps=settle_steps // 6 if relax_steps is None else relax_steps)
+        A = _native_positions(S0)
+        centers = A
+        S0 = None
+    if order:
+        perm = spatial_order(centers, 2 * rmax)
+        centers, radii = centers[perm], radii[perm]
+    return _drum_scene(centers, radii, *args, precision)
+
+
+def _native_positions(S):
+    """Sphere centres of a scene whose spheres were added after its boundary particles."""
+    nd = S.dem._nodes.soa
+    from . import _plan
+    A = _plan.compile_scene(S)
+    sph = A.particles["shape"] == 0
+    return nd.col("pos")[A.particles["nodes"][sph, 0]].copy()
