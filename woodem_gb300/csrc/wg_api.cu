@@ -43,6 +43,10 @@ Sim::~Sim() {
     for (int i = 0; i < 8; i++)
         if (ev[i]) cudaEventDestroy(ev[i]);
     for (cudaEvent_t e : evPool) cudaEventDestroy(e);
+    if (side.st) cudaStreamSynchronize(side.st);
+    if (side.fork) cudaEventDestroy(side.fork);
+    if (side.join) cudaEventDestroy(side.join);
+    if (side.st) cudaStreamDestroy(side.st);
     if (stream) cudaStreamDestroy(stream);
 }
 
@@ -152,6 +156,31 @@ __global__ void k_put_state(DevNodes N, const int32_t* __restrict__ map, int64_t
     const double r = N.posr[s].w;
     N.posr[s] = make_double4_32a(pos[3 * a], pos[3 * a + 1], pos[3 * a + 2], r);
     N.ori[s] = make_double4_32a(ori[4 * a], ori[4 * a + 1], ori[4 * a + 2], ori[4 * a + 3]);
+    if (N.orif) N.orif[s] = make_float4((float)ori[4 * a], (float)ori[4 * a + 1], (float)ori[4 * a + 2], (float)ori[4 * a + 3]);
+    if (N.ph) {
+        // the double-float mirrors of the FP32-force mode follow the written state
+        auto split = [](double x, float& h, float& l) {
+            h = __double2float_rn(x);
+            l = __double2float_rn(x - (double)h);
+        };
+        float4 h, l;
+        const float2 rs = N.rsplit[s];
+        split(pos[3 * a], h.x, l.x);
+        split(pos[3 * a + 1], h.y, l.y);
+        split(pos[3 * a + 2], h.z, l.z);
+        h.w = rs.x;
+        l.w = rs.y;
+        N.ph[s] = h;
+        N.pl[s] = l;
+        split(vel[3 * a], h.x, l.x);
+        split(vel[3 * a + 1], h.y, l.y);
+        split(vel[3 * a + 2], h.z, l.z);
+        h.w = (float)av[3 * a];
+        l.w = (float)av[3 * a + 1];
+        N.vh[s] = h;
+        N.vl[s] = l;
+        N.wz[s] = (float)av[3 * a + 2];
+    }
     N.vel[s] = make_double4_32a(vel[3 * a], vel[3 * a + 1], vel[3 * a + 2], 0.);
     N.angv[s] = make_double4_32a(av[3 * a], av[3 * a + 1], av[3 * a + 2], 0.);
     N.force[s] = make_double4_32a(f[3 * a], f[3 * a + 1], f[3 * a + 2], 0.);
@@ -168,7 +197,12 @@ __global__ void k_get_state(DevNodes N, const int32_t* __restrict__ map, int64_t
     double* av = st + 10 * na;
     double* f = st + 13 * na;
     double* t = st + 16 * na;
-    const double4_32a p = N.posr[s], o = N.ori[s], v = N.vel[s], w = N.angv[s], ff = N.force[s], tt = N.torque[s];
+    const double4_32a p = N.posr[s], v = N.vel[s], w = N.angv[s], ff = N.force[s], tt = N.torque[s];
+    double4_32a o;
+    if (N.orif) {
+        const float4 q = N.orif[s];
+        o = make_double4_32a(q.x, q.y, q.z, q.w);
+    } else o = N.ori[s];
     pos[3 * a] = p.x; pos[3 * a + 1] = p.y; pos[3 * a + 2] = p.z;
     ori[4 * a] = o.x; ori[4 * a + 1] = o.y; ori[4 * a + 2] = o.z; ori[4 * a + 3] = o.w;
     vel[3 * a] = v.x; vel[3 * a + 1] = v.y; vel[3 * a + 2] = v.z;
@@ -234,6 +268,13 @@ int Sim::prepareParams() {
     p.hasGravity = (cfg.gravity[0] != 0 || cfg.gravity[1] != 0 || cfg.gravity[2] != 0);
     p.damping = cfg.damping;
     p.ssDistFactor = cfg.cg2_ss_dist_factor;
+    p.dtF = (float)cfg.dt;
+    p.ssDfAbsF = (float)std::fabs(cfg.cg2_ss_dist_factor);
+    p.dampingF = (float)cfg.damping;
+    for (int i = 0; i < 3; i++) {
+        p.gH[i] = (float)cfg.gravity[i];
+        p.gL[i] = (float)(cfg.gravity[i] - (double)p.gH[i]);
+    }
     p.bo1DistFactor = cfg.bo1_sphere_dist_factor;
     p.law = cfg.law;
     p.phys = cfg.phys;
@@ -272,6 +313,8 @@ int Sim::prepareParams() {
     }
     p.verletDist = vd;
     p.maxD2 = vd * vd;
+    // FP32 verlet test: a hair below maxD2 so that rounding can only trigger a full run early
+    p.maxD2F = (float)(p.maxD2 * (1 - 1e-6));
     (void)X;
     (void)S;
     return 0;
@@ -379,6 +422,7 @@ int Sim::upload() {
         mask[p] = hMask[p];
         aux[p] = make_int4(0, 0, 0, 0);
         facet[p] = make_double4_32a(0, 0, 0, 0);
+        if (hShape[p] != WG_SHAPE_SPHERE) maxBoundaryId = (int32_t)p;
         if (hShape[p] == WG_SHAPE_SPHERE) {
             posr[p].w = hRadius[p];
             nSpheres++;
@@ -442,24 +486,61 @@ int Sim::upload() {
     WG_CUDA_TRY(cudaMemcpy(X.dStage, hApi.data(), sizeof(double) * 19 * na, cudaMemcpyHostToDevice));
     X.hApiMap = map;
     if (prec == WG_PREC_FP32) {
-        std::vector<double4_32a> inv(nSlots);
+        std::vector<NodeConst32> nc(nSlots);
         for (int64_t q = 0; q < nSlots; q++) {
             const double4_32a m = minert[q];
-            inv[q] = make_double4_32a(m.x != 0 ? 1. / m.x : 0., m.y != 0 ? 1. / m.y : 0., m.z != 0 ? 1. / m.z : 0., m.w != 0 ? 1. / m.w : 0.);
+            nc[q].invMass = m.w != 0 ? (float)(1. / m.w) : 0.f;
+            nc[q].invI[0] = m.x != 0 ? (float)(1. / m.x) : 0.f;
+            nc[q].invI[1] = m.y != 0 ? (float)(1. / m.y) : 0.f;
+            nc[q].invI[2] = m.z != 0 ? (float)(1. / m.z) : 0.f;
+            nc[q].mh = (float)m.w;
+            nc[q].ml = (float)(m.w - (double)nc[q].mh);
+            nc[q].flags = flags[q];
+            nc[q]._pad = 0;
         }
-        dInvM = (double4_32a*)dalloc(sizeof(double4_32a) * nSlots);
+        std::vector<float4> orf(nSlots);
+        std::vector<float2> rsp(nSlots);
+        for (int64_t q = 0; q < nSlots; q++) {
+            orf[q] = make_float4((float)ori[q].x, (float)ori[q].y, (float)ori[q].z, (float)ori[q].w);
+            const float rh = (float)posr[q].w;
+            rsp[q] = make_float2(rh, (float)(posr[q].w - (double)rh));
+        }
+        dNodeC = (NodeConst32*)dalloc(sizeof(NodeConst32) * nSlots);
         N.ph = (float4*)dalloc(sizeof(float4) * nSlots);
         N.pl = (float4*)dalloc(sizeof(float4) * nSlots);
         N.vh = (float4*)dalloc(sizeof(float4) * nSlots);
         N.vl = (float4*)dalloc(sizeof(float4) * nSlots);
         N.wz = (float*)dalloc(sizeof(float) * nSlots);
-        if (!dInvM || !N.wz) return fail(WG_ERR_CUDA, "out of device memory (scene)");
-        WG_CUDA_TRY(cudaMemset(N.ph, 0, sizeof(float4) * nSlots));
-        WG_CUDA_TRY(cudaMemset(N.pl, 0, sizeof(float4) * nSlots));
-        WG_CUDA_TRY(cudaMemset(N.vh, 0, sizeof(float4) * nSlots));
-        WG_CUDA_TRY(cudaMemset(N.vl, 0, sizeof(float4) * nSlots));
-        WG_CUDA_TRY(cudaMemset(N.wz, 0, sizeof(float) * nSlots));
-        WG_CUDA_TRY(cudaMemcpy(dInvM, inv.data(), sizeof(double4_32a) * nSlots, cudaMemcpyHostToDevice));
+        N.orif = (float4*)dalloc(sizeof(float4) * nSlots);
+        N.rsplit = (float2*)dalloc(sizeof(float2) * nSlots);
+        if (!dNodeC || !N.wz || !N.orif || !N.rsplit) return fail(WG_ERR_CUDA, "out of device memory (scene)");
+        WG_CUDA_TRY(cudaMemcpy(N.orif, orf.data(), sizeof(float4) * nSlots, cudaMemcpyHostToDevice));
+        WG_CUDA_TRY(cudaMemcpy(N.rsplit, rsp.data(), sizeof(float2) * nSlots, cudaMemcpyHostToDevice));
+        // double-float mirrors of the initial state (x = hi + lo)
+        std::vector<float4> hph(nSlots), hpl(nSlots), hvh(nSlots), hvl(nSlots);
+        std::vector<float> hwz(nSlots);
+        auto split = [](double x, float& h, float& l) {
+            h = (float)x;
+            l = (float)(x - (double)h);
+        };
+        for (int64_t q = 0; q < nSlots; q++) {
+            split(posr[q].x, hph[q].x, hpl[q].x);
+            split(posr[q].y, hph[q].y, hpl[q].y);
+            split(posr[q].z, hph[q].z, hpl[q].z);
+            split(posr[q].w, hph[q].w, hpl[q].w);
+            split(vel[q].x, hvh[q].x, hvl[q].x);
+            split(vel[q].y, hvh[q].y, hvl[q].y);
+            split(vel[q].z, hvh[q].z, hvl[q].z);
+            hvh[q].w = (float)angv[q].x;
+            hvl[q].w = (float)angv[q].y;
+            hwz[q] = (float)angv[q].z;
+        }
+        WG_CUDA_TRY(cudaMemcpy(N.ph, hph.data(), sizeof(float4) * nSlots, cudaMemcpyHostToDevice));
+        WG_CUDA_TRY(cudaMemcpy(N.pl, hpl.data(), sizeof(float4) * nSlots, cudaMemcpyHostToDevice));
+        WG_CUDA_TRY(cudaMemcpy(N.vh, hvh.data(), sizeof(float4) * nSlots, cudaMemcpyHostToDevice));
+        WG_CUDA_TRY(cudaMemcpy(N.vl, hvl.data(), sizeof(float4) * nSlots, cudaMemcpyHostToDevice));
+        WG_CUDA_TRY(cudaMemcpy(N.wz, hwz.data(), sizeof(float) * nSlots, cudaMemcpyHostToDevice));
+        WG_CUDA_TRY(cudaMemcpy(dNodeC, nc.data(), sizeof(NodeConst32) * nSlots, cudaMemcpyHostToDevice));
     }
     long long st0 = cfg.step;
     step = cfg.step;
@@ -533,16 +614,16 @@ int Sim::run(int64_t n) {
     const bool fp32 = prec == WG_PREC_FP32;
     auto stepLeapfrog = [&](int fromEndsArg) {
         if (fromEndsArg) {
-            if (fp32) launch_forces32(stream, N, P, I, dPar, dFlags, true);
+            if (fp32) launch_forces32(stream, N, P, I, dNodeC, dPar, dFlags, true);
             else launch_forces(stream, N, P, I, dPar, dFlags, true);
             launches += I.nHeavyFree > 0;
         }
-        if (fp32) launch_leapfrog32(stream, N, P, I, dInvM, dPar, dFlags, fromEndsArg);
+        if (fp32) launch_leapfrog32(stream, N, P, I, dNodeC, dPar, dFlags, fromEndsArg);
         else launch_leapfrog(stream, N, P, I, dPar, dFlags, fromEndsArg);
         launches++;
     };
     auto stepContact = [&]() {
-        if (fp32) launch_contact_fp32(stream, N, P, C, I, dMats, dPar, dStep, dFlags);
+        if (fp32) launch_contact_fp32(stream, side, N, P, C, I, dMats, dPar, dStep, dFlags, nMixed, cfg.periodic != 0);
         else launch_contact_fp64(stream, N, P, C, I, dMats, dPar, dStep, dFlags);
         launch_advance(stream, dStep, dFlags);
         launches += 2;
@@ -612,7 +693,7 @@ int Sim::run(int64_t n) {
     }
     // DemData.force/torque of the last contact loop, for the host and for the next run
     if (fromEnds) {
-        if (fp32) launch_forces32(stream, N, P, I, dPar, nullptr, false);
+        if (fp32) launch_forces32(stream, N, P, I, dNodeC, dPar, nullptr, false);
         else launch_forces(stream, N, P, I, dPar, nullptr, false);
         launches += 1 + (I.nHeavy > 0);
     }
@@ -652,7 +733,10 @@ int wg_create(wg_scene** out, int device) {
     SimEx* s = new SimEx();
     s->device = device;
     for (int i = 0; i < 8; i++) s->ev[i] = nullptr;
-    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&s->side.st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->side.fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->side.join, cudaEventDisableTiming) != cudaSuccess) {
         g_createError = "cudaStreamCreate failed";
         delete s;
         return WG_ERR_CUDA;
@@ -873,7 +957,7 @@ static int collectContacts(Sim& S, std::vector<int64_t>& keep, std::vector<uint6
         std::vector<uint64_t> kc(n);
         WG_CUDA_TRY(cudaMemcpy(flc.data(), S.C.flags, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
         WG_CUDA_TRY(cudaMemcpy(kc.data(), S.C.key, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost));
-        const int64_t ne = 2 * n;
+        const int64_t ne = 2 * std::max<int64_t>(S.nActive, 1);
         std::vector<double> ef(4 * ne);
         if (S.prec == WG_PREC_FP32) {
             std::vector<float> tmp(4 * ne);
@@ -887,7 +971,8 @@ static int collectContacts(Sim& S, std::vector<int64_t>& keep, std::vector<uint6
             const bool facetA = ctype(flc[c]) == CT_FS;
             const int32_t slot = facetA ? (aIsLo ? sHi[c] : sLo[c]) : (aIsLo ? sLo[c] : sHi[c]);
             const double sg = facetA ? -1.0 : 1.0;
-            for (int k = 0; k < 3; k++) cols[CC_NCOL + k][c] = sg * ef[4 * slot + k] + 0.0;
+            if (slot >= 0)
+                for (int k = 0; k < 3; k++) cols[CC_NCOL + k][c] = sg * ef[4 * slot + k] + 0.0;
         }
     }
     if (n > 0) {

@@ -19,11 +19,14 @@
 //   6. CSR incidence for the deterministic force sum              (k_lo_start, hi sort, k_hi_start)
 #include <cub/cub.cuh>
 
+
 #include <algorithm>
 #include <cmath>
 
 #include "wg_internal.h"
 #include "wg_math.cuh"
+#include "wg_ends.cuh"
+#include "wg_geom.cuh"
 
 namespace wg {
 
@@ -45,6 +48,8 @@ struct CollideWork {
     double4_32a* smn = nullptr;
     double4_32a* smx = nullptr;
     uint32_t* smask = nullptr;
+    float4* smnf = nullptr;       // box min rounded down, mask in w
+    float4* smxf = nullptr;       // box max rounded up, particle id in w
     int32_t* cellOff = nullptr;
     int64_t cellOffCap = 0;
     double* red = nullptr;        // reduction partials
@@ -61,6 +66,7 @@ struct CollideWork {
     int32_t* orphSrc = nullptr;
     int32_t* src = nullptr;
     int64_t mergeCap = 0, orphCap = 0, srcCap = 0;
+    int32_t* act = nullptr;       // exclusive scan of the active contacts
     uint32_t* hiKeys = nullptr;
     uint32_t* hiKeysSorted = nullptr;
     int32_t* hiVals = nullptr;
@@ -220,13 +226,18 @@ __global__ void k_cell_off(const uint32_t* __restrict__ skey, int n, int64_t nce
 }
 
 __global__ void k_gather_sorted(DevParticles P, const int32_t* __restrict__ sid, int n, double4_32a* __restrict__ smn,
-                                double4_32a* __restrict__ smx, uint32_t* __restrict__ smask) {
+                                double4_32a* __restrict__ smx, uint32_t* __restrict__ smask, float4* __restrict__ smnf,
+                                float4* __restrict__ smxf) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int p = sid[i];
-    smn[i] = P.mn[p];
-    smx[i] = P.mx[p];
-    smask[i] = P.mask[p];
+    const double4_32a a = P.mn[p], b = P.mx[p];
+    const uint32_t m = P.mask[p];
+    smn[i] = a;
+    smx[i] = b;
+    smask[i] = m;
+    smnf[i] = make_float4(__double2float_rd(a.x), __double2float_rd(a.y), __double2float_rd(a.z), __uint_as_float(m));
+    smxf[i] = make_float4(__double2float_ru(b.x), __double2float_ru(b.y), __double2float_ru(b.z), __int_as_float(p));
 }
 
 // closed-interval 3-axis overlap, InsertionSortCollider::spatialOverlap :52-58
@@ -242,66 +253,142 @@ __device__ __forceinline__ void emitPair(int a, int b, uint64_t* pairs, int64_t 
     if ((int64_t)idx < cap) pairs[idx] = ((uint64_t)(uint32_t)lo << 32) | (uint32_t)hi;
 }
 
+// Outward-rounded FP32 boxes overlap whenever the FP64 boxes do, so the FP32 test rejects most
+// candidates exactly and the FP64 test (InsertionSortCollider::spatialOverlap) decides the rest.
+__device__ __forceinline__ bool overlapF(const float4& mn1, const float4& mx1, const float4& mn2, const float4& mx2) {
+    return (mn1.x <= mx2.x) && (mx1.x >= mn2.x) && (mn1.y <= mx2.y) && (mx1.y >= mn2.y) && (mn1.z <= mx2.z) && (mx1.z >= mn2.z);
+}
+
+// Pairs found by the lanes of a warp are written with one atomic per warp: each lane keeps up to
+// kPairBuf pairs in registers, the warp reserves room for all of them at once (the single counter
+// would otherwise serialise millions of atomics in L2), and a lane whose buffer fills flushes it
+// the same way. Must be called by all lanes of the warp together.
+constexpr int kPairBuf = 8;
+__device__ __forceinline__ void flushPairs(uint64_t (&buf)[kPairBuf], int& nb, uint64_t* pairs, int64_t cap,
+                                           unsigned long long* counter) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    int incl = nb;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += v;
+    }
+    const int total = __shfl_sync(FULL, incl, 31);
+    unsigned long long base = 0;
+    if (lane == 31 && total > 0) base = atomicAdd(counter, (unsigned long long)total);
+    base = __shfl_sync(FULL, base, 31);
+    const unsigned long long at = base + (unsigned long long)(incl - nb);
+#pragma unroll
+    for (int q = 0; q < kPairBuf; q++)
+        if (q < nb && (int64_t)(at + q) < cap) pairs[at + q] = buf[q];
+    nb = 0;
+}
+__device__ __forceinline__ uint64_t pairKey(int a, int b) {
+    const int lo = a < b ? a : b, hi = a < b ? b : a;
+    return ((uint64_t)(uint32_t)lo << 32) | (uint32_t)hi;
+}
+
 // Half-shell sweep: particle i tests the rest of its own cell, the next cell in x, and the
 // three-cell x-runs of the rows (dy,dz) in {(1,0),(-1,1),(0,1),(1,1)}; each pair is met once.
-__global__ void k_pairs_ss(const int32_t* __restrict__ sid, const uint32_t* __restrict__ skey, const double4_32a* __restrict__ smn,
-                           const double4_32a* __restrict__ smx, const uint32_t* __restrict__ smask, int n, Grid G,
-                           const int32_t* __restrict__ off, uint32_t lone, uint64_t* __restrict__ pairs, int64_t cap,
+// The candidate ranges of a lane are walked as one sequence so that the warp can flush together.
+__global__ void k_pairs_ss(const uint32_t* __restrict__ skey, const double4_32a* __restrict__ smn,
+                           const double4_32a* __restrict__ smx, const float4* __restrict__ smnf, const float4* __restrict__ smxf,
+                           int n, Grid G, const int32_t* __restrict__ off, uint32_t lone, uint64_t* __restrict__ pairs, int64_t cap,
                            unsigned long long* __restrict__ counter) {
+    const unsigned FULL = 0xffffffffu;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const uint32_t k = skey[i];
-    const int cx = (int)(k % (uint32_t)G.nx);
-    const int cy = (int)((k / (uint32_t)G.nx) % (uint32_t)G.ny);
-    const int cz = (int)(k / ((uint32_t)G.nx * (uint32_t)G.ny));
-    const double4_32a mn1 = smn[i], mx1 = smx[i];
-    const uint32_t m1 = smask[i];
-    const int pi = sid[i];
-    // own row: rest of own cell + cell cx+1
-    {
+    const bool valid = i < n;
+    // up to 5 ranges [beg, end) of sorted indices
+    int rb[5], re[5];
+    float4 fn1 = make_float4(0.f, 0.f, 0.f, 0.f), fx1 = fn1;
+    uint32_t m1 = 0;
+    int pi = 0;
+#pragma unroll
+    for (int r = 0; r < 5; r++) rb[r] = re[r] = 0;
+    if (valid) {
+        const uint32_t k = skey[i];
+        const int cx = (int)(k % (uint32_t)G.nx);
+        const int cy = (int)((k / (uint32_t)G.nx) % (uint32_t)G.ny);
+        const int cz = (int)(k / ((uint32_t)G.nx * (uint32_t)G.ny));
+        fn1 = smnf[i];
+        fx1 = smxf[i];
+        m1 = __float_as_uint(fn1.w);
+        pi = __float_as_int(fx1.w);
         const int cx1 = cx + 1 < G.nx ? cx + 1 : cx;
-        const int64_t kEnd = ((int64_t)cz * G.ny + cy) * G.nx + cx1;
-        const int end = off[kEnd + 1];
-        for (int j = i + 1; j < end; j++) {
-            if (overlap3(mn1, mx1, smn[j], smx[j]) && maskOk(m1, smask[j], lone)) emitPair(pi, sid[j], pairs, cap, counter);
+        rb[0] = i + 1;
+        re[0] = off[((int64_t)cz * G.ny + cy) * G.nx + cx1 + 1];
+        const int DY[4] = {1, -1, 0, 1}, DZ[4] = {0, 1, 1, 1};
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            const int y = cy + DY[r], z = cz + DZ[r];
+            if (y < 0 || y >= G.ny || z >= G.nz) continue;
+            const int x0 = cx > 0 ? cx - 1 : 0;
+            const int64_t rowBase = ((int64_t)z * G.ny + y) * G.nx;
+            rb[r + 1] = off[rowBase + x0];
+            re[r + 1] = off[rowBase + cx1 + 1];
         }
     }
-    const int DY[4] = {1, -1, 0, 1}, DZ[4] = {0, 1, 1, 1};
-    for (int r = 0; r < 4; r++) {
-        const int y = cy + DY[r], z = cz + DZ[r];
-        if (y < 0 || y >= G.ny || z >= G.nz) continue;
-        const int x0 = cx > 0 ? cx - 1 : 0, x1 = cx + 1 < G.nx ? cx + 1 : cx;
-        const int64_t rowBase = ((int64_t)z * G.ny + y) * G.nx;
-        const int beg = off[rowBase + x0], end = off[rowBase + x1 + 1];
-        for (int j = beg; j < end; j++) {
-            if (overlap3(mn1, mx1, smn[j], smx[j]) && maskOk(m1, smask[j], lone)) emitPair(pi, sid[j], pairs, cap, counter);
+    uint64_t buf[kPairBuf];
+    int nb = 0;
+    int r = 0, j = rb[0];
+    for (;;) {
+        // advance to the next candidate of this lane
+        while (r < 5 && j >= re[r]) {
+            r++;
+            if (r < 5) j = rb[r];
         }
+        const bool has = r < 5;
+        if (!__any_sync(FULL, has)) break;
+        if (has) {
+            const float4 fn2 = smnf[j], fx2 = smxf[j];
+            if (overlapF(fn1, fx1, fn2, fx2) && maskOk(m1, __float_as_uint(fn2.w), lone) && overlap3(smn[i], smx[i], smn[j], smx[j]))
+                buf[nb++] = pairKey(pi, __float_as_int(fx2.w));
+            j++;
+        }
+        if (__any_sync(FULL, nb == kPairBuf)) flushPairs(buf, nb, pairs, cap, counter);
     }
+    flushPairs(buf, nb, pairs, cap, counter);
 }
 
 // A facet (finite box) against the spheres of the cells its box can reach: a sphere j that
-// overlaps it has mn_j in [mn_f - h, mx_f] on every axis.
-__global__ void k_pairs_local(DevParticles P, const int32_t* __restrict__ lids, int nl, const int32_t* __restrict__ sid,
-                              const double4_32a* __restrict__ smn, const double4_32a* __restrict__ smx, const uint32_t* __restrict__ smask,
+// overlaps it has mn_j in [mn_f - h, mx_f] on every axis. One warp per facet; its lanes split
+// each x-run of cells.
+__global__ void k_pairs_local(DevParticles P, const int32_t* __restrict__ lids, int nl, const double4_32a* __restrict__ smn,
+                              const double4_32a* __restrict__ smx, const float4* __restrict__ smnf, const float4* __restrict__ smxf,
                               Grid G, const int32_t* __restrict__ off, uint32_t lone, uint64_t* __restrict__ pairs, int64_t cap,
                               unsigned long long* __restrict__ counter) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nl) return;
+    const unsigned FULL = 0xffffffffu;
+    const int t = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (t >= nl) return;  // warp-uniform
     const int p = lids[t];
     const double4_32a mn1 = P.mn[p], mx1 = P.mx[p];
+    const float4 fn1 = make_float4(__double2float_rd(mn1.x), __double2float_rd(mn1.y), __double2float_rd(mn1.z), 0.f);
+    const float4 fx1 = make_float4(__double2float_ru(mx1.x), __double2float_ru(mx1.y), __double2float_ru(mx1.z), 0.f);
     const uint32_t m1 = P.mask[p];
     const int x0 = cellCoord(mn1.x - G.h, G.ox, G.h, G.nx), x1 = cellCoord(mx1.x, G.ox, G.h, G.nx);
     const int y0 = cellCoord(mn1.y - G.h, G.oy, G.h, G.ny), y1 = cellCoord(mx1.y, G.oy, G.h, G.ny);
     const int z0 = cellCoord(mn1.z - G.h, G.oz, G.h, G.nz), z1 = cellCoord(mx1.z, G.oz, G.h, G.nz);
+    uint64_t buf[kPairBuf];
+    int nb = 0;
     for (int z = z0; z <= z1; z++)
         for (int y = y0; y <= y1; y++) {
             const int64_t rowBase = ((int64_t)z * G.ny + y) * G.nx;
             const int beg = off[rowBase + x0], end = off[rowBase + x1 + 1];
-            for (int j = beg; j < end; j++) {
-                if (sid[j] == p) continue;
-                if (overlap3(mn1, mx1, smn[j], smx[j]) && maskOk(m1, smask[j], lone)) emitPair(p, sid[j], pairs, cap, counter);
+            for (int j0 = beg; j0 < end; j0 += 32) {
+                const int j = j0 + lane;
+                if (j < end) {
+                    const float4 fn2 = smnf[j], fx2 = smxf[j];
+                    const int q = __float_as_int(fx2.w);
+                    if (q != p && overlapF(fn1, fx1, fn2, fx2) && maskOk(m1, __float_as_uint(fn2.w), lone) &&
+                        overlap3(mn1, mx1, smn[j], smx[j]))
+                        buf[nb++] = pairKey(p, q);
+                }
+                if (__any_sync(FULL, nb == kPairBuf)) flushPairs(buf, nb, pairs, cap, counter);
             }
         }
+    flushPairs(buf, nb, pairs, cap, counter);
 }
 
 // Walls (and any box too large for the grid) against every sphere.
@@ -388,7 +475,7 @@ __global__ void k_gather(DevContacts Cold, DevContacts Cnew, const int32_t* __re
     if (i >= Cnew.n) return;
     const int32_t s = src[i];
     if (s >= 0) {
-        Cnew.flags[i] = Cold.flags[s] & ~C_PENDING;
+        Cnew.flags[i] = Cold.flags[s] & ~(C_PENDING | C_DORMANT);
         Cnew.step0[i] = Cold.step0[s];
         Cnew.cdist[i] = Cold.cdist[s];
 #pragma unroll
@@ -423,16 +510,101 @@ __global__ void k_gather(DevContacts Cold, DevContacts Cnew, const int32_t* __re
     }
 }
 
-// ---------------------------------------------------------------- CSR incidence
-__global__ void k_lo_start(const uint64_t* __restrict__ key, int64_t n, int nPar, int32_t* __restrict__ loStart) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p > nPar) return;
-    loStart[p] = (int32_t)lowerBound64(key, n, (uint64_t)(uint32_t)p << 32);
+// Dormant contacts. Between two full runs no node moves farther than verletDist from the position
+// it had at the first of them (the verlet test of Leapfrog triggers the next full run before that),
+// so a pair that is not real and whose surfaces are more than 2*verletDist apart now cannot touch
+// before the next full run: the geometry functor would reject it at every step until then. Such
+// contacts stay in the container (they are potential contacts of the reference) but the contact
+// kernels skip them. The bounds are taken with a relative margin of 1e-9, and only for aperiodic
+// scenes (a periodic cell moves the images of the particles by itself).
+__global__ void k_dormant(DevContacts C, DevNodes N, DevParticles P, const ScenePar* __restrict__ spp) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= C.n) return;
+    const ScenePar& sp = *spp;
+    const uint32_t fl = C.flags[c];
+    if (fl & C_REAL) return;
+    const uint32_t ty = ctype(fl);
+    if (ty == CT_NONE) return;
+    const uint64_t key = C.key[c];
+    const int lo = (int)(key >> 32), hi = (int)(key & 0xffffffffu);
+    const int A = (fl & C_SWAP) ? hi : lo, B = (fl & C_SWAP) ? lo : hi;
+    const double m2 = 2 * sp.verletDist;
+    bool far;
+    const double4_32a pb = N.posr[B];
+    if (ty == CT_SS && N.ph) {
+        // FP32-force mode: the double-float mirrors of the positions, FP32 arithmetic; the
+        // relative position carries ~47 bits and the squares and sums ~2^-22 relative error
+        const float4 ha = N.ph[A], la = N.pl[A], hb = N.ph[B], lb = N.pl[B];
+        float sx, tx, sy, ty_, sz, tz;
+        dfDiff(ha.x, la.x, hb.x, lb.x, sx, tx);
+        dfDiff(ha.y, la.y, hb.y, lb.y, sy, ty_);
+        dfDiff(ha.z, la.z, hb.z, lb.z, sz, tz);
+        const float dx = sx + tx, dy = sy + ty_, dz = sz + tz;
+        const float reach = (sp.ssDfAbsF * (ha.w + hb.w) + (float)m2) * (1.f + 1e-5f);
+        far = dx * dx + dy * dy + dz * dz > reach * reach;
+    } else if (ty == CT_SS) {
+        const double4_32a pa = N.posr[A];
+        const double dx = pb.x - pa.x, dy = pb.y - pa.y, dz = pb.z - pa.z;
+        const double reach = (fabs(sp.ssDistFactor) * (pa.w + pb.w) + m2) * (1 + 1e-9);
+        far = dx * dx + dy * dy + dz * dz > reach * reach;
+    } else if (ty == CT_WS) {
+        const int4 ax = P.aux[A];
+        const double4_32a pw = N.posr[A];
+        const double d = (ax.x == 0 ? pb.x - pw.x : (ax.x == 1 ? pb.y - pw.y : pb.z - pw.z));
+        far = fabs(d) > (pb.w + m2) * (1 + 1e-9);
+    } else {
+        // distance from the sphere centre to the triangle: to its plane when the projection falls
+        // inside, else to the nearest edge; it bounds from below the distance the functor tests
+        // (Facet.cpp:247-259), and every point of the triangle moves at most verletDist since its
+        // vertices do
+        const int4 nd = P.aux[A];
+        const D3 p0 = ld3(N.posr[nd.x]), p1 = ld3(N.posr[nd.y]), p2 = ld3(N.posr[nd.z]);
+        const D3 sC = ld3(pb);
+        const D3 nn = cross(p1 - p0, p2 - p0);
+        const double nl = sqrt(sqn(nn));
+        far = false;
+        if (nl > 0) {
+            const D3 fN = nn / nl;
+            const double planeDist = dot(sC - p0, fN);
+            const D3 fC = sC - planeDist * fN;
+            const bool inside = dot(cross(p1 - p0, nn), fC - p0) <= 0 && dot(cross(p2 - p1, nn), fC - p1) <= 0 &&
+                                dot(cross(p0 - p2, nn), fC - p2) <= 0;
+            double d2;
+            if (inside) d2 = planeDist * planeDist;
+            else {
+                d2 = sqn(sC - closestSegmentPt(sC, p0, p1));
+                d2 = fmin(d2, sqn(sC - closestSegmentPt(sC, p1, p2)));
+                d2 = fmin(d2, sqn(sC - closestSegmentPt(sC, p2, p0)));
+            }
+            const double reach = (pb.w + P.facet[A].w + m2) * (1 + 1e-9);
+            far = d2 > reach * reach;
+        }
+    }
+    if (far) C.flags[c] = fl | C_DORMANT;
 }
-__global__ void k_hi_keys(const uint64_t* __restrict__ key, int64_t n, uint32_t* __restrict__ hk, int32_t* __restrict__ hv) {
+
+// ---------------------------------------------------------------- CSR incidence
+// Only active contacts (a functor applies and the pair is not dormant) own end slots; act is
+// their exclusive scan over the key-sorted contacts, act[n] = number of active contacts.
+__device__ __forceinline__ bool activeContact(uint32_t fl) { return ctype(fl) != CT_NONE && !(fl & C_DORMANT); }
+__global__ void k_active(const uint32_t* __restrict__ flags, int64_t n, int32_t* __restrict__ act) {
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= n) return;
-    hk[c] = (uint32_t)(key[c] & 0xffffffffu);
+    act[c] = activeContact(flags[c]) ? 1 : 0;
+}
+// loStart[p] = active contacts with lo < p
+__global__ void k_lo_start(const uint64_t* __restrict__ key, int64_t n, int nPar, const int32_t* __restrict__ act,
+                           int32_t* __restrict__ loStart) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p > nPar) return;
+    loStart[p] = act[lowerBound64(key, n, (uint64_t)(uint32_t)p << 32)];
+}
+// hi id of the active contacts, nPar for the others (sorted past every particle)
+__global__ void k_hi_keys(const uint64_t* __restrict__ key, const uint32_t* __restrict__ flags, int64_t n, uint32_t nPar,
+                          uint32_t* __restrict__ hk, int32_t* __restrict__ hv) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    hk[c] = activeContact(flags[c]) ? (uint32_t)(key[c] & 0xffffffffu) : nPar;
     hv[c] = (int32_t)c;
 }
 __global__ void k_hi_start(const uint32_t* __restrict__ hks, int64_t n, int nPar, int32_t* __restrict__ hiStart) {
@@ -440,16 +612,29 @@ __global__ void k_hi_start(const uint32_t* __restrict__ hks, int64_t n, int nPar
     if (p > nPar) return;
     hiStart[p] = (int32_t)lowerBound32(hks, n, (uint32_t)p);
 }
-// end slots: contact c with hi==p sits at loStart[p] + (its index k in hiList); with lo==p at
-// hiStart[p+1] + c (see DevIncidence)
-__global__ void k_slots(const uint64_t* __restrict__ key, int64_t n, DevIncidence I) {
+// end slots: active contact c with hi==p sits at loStart[p] + (its index k in hiList); with lo==p
+// at hiStart[p+1] + act[c] (see DevIncidence); inactive contacts have no slot (-1)
+__global__ void k_slots(const uint64_t* __restrict__ key, const uint32_t* __restrict__ flags, int64_t n, int64_t nAct,
+                        const int32_t* __restrict__ act, DevIncidence I) {
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
-    const int32_t ch = I.hiList[k];
-    const int hiP = (int)(key[ch] & 0xffffffffu);
-    I.slotHi[ch] = I.loStart[hiP] + (int32_t)k;
-    const int loP = (int)(key[k] >> 32);
-    I.slotLo[k] = I.hiStart[loP + 1] + (int32_t)k;
+    if (k < nAct) {
+        const int32_t ch = I.hiList[k];
+        const int hiP = (int)(key[ch] & 0xffffffffu);
+        I.slotHi[ch] = I.loStart[hiP] + (int32_t)k;
+    }
+    if (activeContact(flags[k])) {
+        const int loP = (int)(key[k] >> 32);
+        I.slotLo[k] = I.hiStart[loP + 1] + act[k];
+    } else {
+        I.slotLo[k] = -1;
+        I.slotHi[k] = -1;
+    }
+}
+
+// index of the first contact whose lo id is above every boundary particle
+__global__ void k_first_ss(const uint64_t* __restrict__ key, int64_t n, int firstId, int32_t* __restrict__ out) {
+    *out = (int32_t)lowerBound64(key, n, (uint64_t)(uint32_t)firstId << 32);
 }
 
 // Particles summed by the block tree; the ones whose node has a free DOF are also summed before
@@ -575,7 +760,9 @@ int collide_full_run(Sim& S) {
             W.smn = (double4_32a*)S.dalloc(sizeof(double4_32a) * ns);
             W.smx = (double4_32a*)S.dalloc(sizeof(double4_32a) * ns);
             W.smask = (uint32_t*)S.dalloc(sizeof(uint32_t) * ns);
-            if (!W.smask) return S.fail(WG_ERR_CUDA, "out of device memory (grid)");
+            W.smnf = (float4*)S.dalloc(sizeof(float4) * ns);
+            W.smxf = (float4*)S.dalloc(sizeof(float4) * ns);
+            if (!W.smask || !W.smxf) return S.fail(WG_ERR_CUDA, "out of device memory (grid)");
         }
         W.cellOff = grow(S, W.cellOff, W.cellOffCap, G.ncell + 1);
         k_cellkey<<<(ns + BS - 1) / BS, BS, 0, st>>>(S.P, W.sphereIds, ns, G, W.cellKey, W.cellVal);
@@ -587,7 +774,7 @@ int collide_full_run(Sim& S) {
         tb = W.cubBytes;
         WG_CUDA_TRY(cub::DeviceRadixSort::SortPairs(W.cubTmp, tb, W.cellKey, W.cellKeySorted, W.cellVal, W.sid, ns, 0, endBit, st));
         k_cell_off<<<(unsigned)((G.ncell + 1 + BS - 1) / BS), BS, 0, st>>>(W.cellKeySorted, ns, G.ncell, W.cellOff);
-        k_gather_sorted<<<(ns + BS - 1) / BS, BS, 0, st>>>(S.P, W.sid, ns, W.smn, W.smx, W.smask);
+        k_gather_sorted<<<(ns + BS - 1) / BS, BS, 0, st>>>(S.P, W.sid, ns, W.smn, W.smx, W.smask, W.smnf, W.smxf);
     }
     // lists of large particles: facets with boxes spanning a few cells use the grid, the rest are global
     {
@@ -625,11 +812,11 @@ int collide_full_run(Sim& S) {
     for (int attempt = 0; attempt < 3; attempt++) {
         WG_CUDA_TRY(cudaMemsetAsync(W.counter, 0, sizeof(unsigned long long), st));
         if (ns > 0) {
-            k_pairs_ss<<<(ns + BS - 1) / BS, BS, 0, st>>>(W.sid, W.cellKeySorted, W.smn, W.smx, W.smask, ns, G, W.cellOff, lone,
+            k_pairs_ss<<<(ns + BS - 1) / BS, BS, 0, st>>>(W.cellKeySorted, W.smn, W.smx, W.smnf, W.smxf, ns, G, W.cellOff, lone,
                                                         W.pairs, W.pairCap, W.counter);
             if (W.nLarge > 0)
-                k_pairs_local<<<(W.nLarge + 63) / 64, 64, 0, st>>>(S.P, W.largeIds, W.nLarge, W.sid, W.smn, W.smx, W.smask, G,
-                                                                W.cellOff, lone, W.pairs, W.pairCap, W.counter);
+                k_pairs_local<<<(unsigned)(((int64_t)W.nLarge * 32 + BS - 1) / BS), BS, 0, st>>>(
+                    S.P, W.largeIds, W.nLarge, W.smn, W.smx, W.smnf, W.smxf, G, W.cellOff, lone, W.pairs, W.pairCap, W.counter);
             if (W.nGlobal > 0)
                 k_pairs_global<<<(ns + BS - 1) / BS, BS, 0, st>>>(S.P, W.globalIds, W.nGlobal, W.sphereIds, ns, lone, W.pairs,
                                                                 W.pairCap, W.counter);
@@ -716,13 +903,14 @@ int collide_full_run(Sim& S) {
                                                                       W.src);
     if (nOut > 0) k_gather<<<(unsigned)((nOut + BS - 1) / BS), BS, 0, st>>>(S.C, S.Cb, W.src, S.P, S.dStep);
     std::swap(S.C, S.Cb);
-    // 6. CSR incidence
+    if (nOut > 0 && !S.cfg.periodic)
+        k_dormant<<<(unsigned)((nOut + BS - 1) / BS), BS, 0, st>>>(S.C, S.N, S.P, S.dPar);
+    // 6. CSR incidence over the active contacts
     const int64_t n = S.C.n;
-    k_lo_start<<<(unsigned)((S.nPar + 1 + BS - 1) / BS), BS, 0, st>>>(S.C.key, n, (int)S.nPar, S.I.loStart);
     if (W.hiCap < std::max<int64_t>(n, 1)) {
         if (W.hiKeys) {
             S.dfree(W.hiKeys); S.dfree(W.hiKeysSorted); S.dfree(W.hiVals); S.dfree(S.I.hiList);
-            S.dfree(S.I.slotLo); S.dfree(S.I.slotHi);
+            S.dfree(S.I.slotLo); S.dfree(S.I.slotHi); S.dfree(W.act);
         }
         W.hiCap = std::max<int64_t>(n, 1) * 3 / 2 + 1024;
         W.hiKeys = (uint32_t*)S.dalloc(sizeof(uint32_t) * W.hiCap);
@@ -731,13 +919,31 @@ int collide_full_run(Sim& S) {
         S.I.hiList = (int32_t*)S.dalloc(sizeof(int32_t) * W.hiCap);
         S.I.slotLo = (int32_t*)S.dalloc(sizeof(int32_t) * W.hiCap);
         S.I.slotHi = (int32_t*)S.dalloc(sizeof(int32_t) * W.hiCap);
-        if (!S.I.slotHi) return S.fail(WG_ERR_CUDA, "out of device memory (incidence)");
+        W.act = (int32_t*)S.dalloc(sizeof(int32_t) * (W.hiCap + 1));
+        if (!S.I.slotHi || !W.act) return S.fail(WG_ERR_CUDA, "out of device memory (incidence)");
     }
-    if (S.I.endCap < 2 * std::max<int64_t>(n, 1)) {
+    int64_t nAct = 0;
+    {
+        WG_CUDA_TRY(cudaMemsetAsync(W.act, 0, sizeof(int32_t) * (n + 1), st));
+        if (n > 0) {
+            k_active<<<(unsigned)((n + BS - 1) / BS), BS, 0, st>>>(S.C.flags, n, W.act);
+            size_t tb = 0;
+            cub::DeviceScan::ExclusiveSum(nullptr, tb, W.act, W.act, (int)(n + 1), st);
+            if (ensureCub(S, tb)) return WG_ERR_CUDA;
+            tb = W.cubBytes;
+            WG_CUDA_TRY(cub::DeviceScan::ExclusiveSum(W.cubTmp, tb, W.act, W.act, (int)(n + 1), st));
+        }
+        int32_t h = 0;
+        WG_CUDA_TRY(cudaMemcpyAsync(&h, W.act + n, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+        WG_CUDA_TRY(cudaStreamSynchronize(st));
+        nAct = h;
+    }
+    k_lo_start<<<(unsigned)((S.nPar + 1 + BS - 1) / BS), BS, 0, st>>>(S.C.key, n, (int)S.nPar, W.act, S.I.loStart);
+    if (S.I.endCap < 2 * std::max<int64_t>(nAct, 1)) {
         if (S.I.endA) { S.dfree(S.I.endA); S.dfree(S.I.endB); }
         if (S.I.endAf) { S.dfree(S.I.endAf); S.dfree(S.I.endBf); }
         S.I.endA = nullptr; S.I.endB = nullptr; S.I.endAf = nullptr; S.I.endBf = nullptr;
-        S.I.endCap = 2 * std::max<int64_t>(n, 1) * 3 / 2 + 2048;
+        S.I.endCap = 2 * std::max<int64_t>(nAct, 1) * 3 / 2 + 2048;
         if (S.prec == WG_PREC_FP32) {
             S.I.endAf = (float4*)S.dalloc(sizeof(float4) * S.I.endCap);
             S.I.endBf = (float2*)S.dalloc(sizeof(float2) * S.I.endCap);
@@ -748,18 +954,21 @@ int collide_full_run(Sim& S) {
             if (!S.I.endA || !S.I.endB) return S.fail(WG_ERR_CUDA, "out of device memory (contact ends)");
         }
     }
+    int hiBits = 1;  // bits of the largest hi key, nPar
+    while ((int64_t(1) << hiBits) <= S.nPar) hiBits++;
     if (n > 0) {
-        k_hi_keys<<<(unsigned)((n + BS - 1) / BS), BS, 0, st>>>(S.C.key, n, W.hiKeys, W.hiVals);
+        k_hi_keys<<<(unsigned)((n + BS - 1) / BS), BS, 0, st>>>(S.C.key, S.C.flags, n, (uint32_t)S.nPar, W.hiKeys, W.hiVals);
         size_t tb = 0;
-        cub::DeviceRadixSort::SortPairs(nullptr, tb, W.hiKeys, W.hiKeysSorted, W.hiVals, S.I.hiList, n, 0, idBits, st);
+        cub::DeviceRadixSort::SortPairs(nullptr, tb, W.hiKeys, W.hiKeysSorted, W.hiVals, S.I.hiList, n, 0, hiBits, st);
         if (ensureCub(S, tb)) return WG_ERR_CUDA;
         tb = W.cubBytes;
-        WG_CUDA_TRY(cub::DeviceRadixSort::SortPairs(W.cubTmp, tb, W.hiKeys, W.hiKeysSorted, W.hiVals, S.I.hiList, n, 0, idBits, st));
+        WG_CUDA_TRY(cub::DeviceRadixSort::SortPairs(W.cubTmp, tb, W.hiKeys, W.hiKeysSorted, W.hiVals, S.I.hiList, n, 0, hiBits, st));
     }
     k_hi_start<<<(unsigned)((S.nPar + 1 + BS - 1) / BS), BS, 0, st>>>(W.hiKeysSorted, n, (int)S.nPar, S.I.hiStart);
-    if (n > 0) k_slots<<<(unsigned)((n + BS - 1) / BS), BS, 0, st>>>(S.C.key, n, S.I);
+    if (n > 0) k_slots<<<(unsigned)((n + BS - 1) / BS), BS, 0, st>>>(S.C.key, S.C.flags, n, nAct, W.act, S.I);
+    S.nActive = nAct;
     // every end starts without a contribution; the contact kernel fills the real ones this step
-    const int64_t ne = 2 * std::max<int64_t>(n, 1);
+    const int64_t ne = 2 * std::max<int64_t>(nAct, 1);
     if (S.prec == WG_PREC_FP32) {
         WG_CUDA_TRY(cudaMemsetAsync(S.I.endAf, 0, sizeof(float4) * ne, st));
         WG_CUDA_TRY(cudaMemsetAsync(S.I.endBf, 0, sizeof(float2) * ne, st));
@@ -769,13 +978,16 @@ int collide_full_run(Sim& S) {
     }
     // heavy particles
     if (!W.heavyCount) {
-        W.heavyCount = (int32_t*)S.dalloc(sizeof(int32_t) * 2);
-        WG_CUDA_TRY(cudaMallocHost(&W.hHeavy, sizeof(int32_t) * 2));
+        W.heavyCount = (int32_t*)S.dalloc(sizeof(int32_t) * 3);
+        WG_CUDA_TRY(cudaMallocHost(&W.hHeavy, sizeof(int32_t) * 3));
     }
-    WG_CUDA_TRY(cudaMemsetAsync(W.heavyCount, 0, sizeof(int32_t) * 2, st));
+    WG_CUDA_TRY(cudaMemsetAsync(W.heavyCount, 0, sizeof(int32_t) * 3, st));
     k_heavy<<<(unsigned)((S.nPar + BS - 1) / BS), BS, 0, st>>>(S.I, S.P, S.N.flags, kHeavyThreshold, W.heavyCount);
-    WG_CUDA_TRY(cudaMemcpyAsync(W.hHeavy, W.heavyCount, sizeof(int32_t) * 2, cudaMemcpyDeviceToHost, st));
+    // contacts whose lo id is above every boundary particle join two spheres
+    if (S.maxBoundaryId >= 0) k_first_ss<<<1, 1, 0, st>>>(S.C.key, n, S.maxBoundaryId + 1, W.heavyCount + 2);
+    WG_CUDA_TRY(cudaMemcpyAsync(W.hHeavy, W.heavyCount, sizeof(int32_t) * 3, cudaMemcpyDeviceToHost, st));
     WG_CUDA_TRY(cudaStreamSynchronize(st));
+    S.nMixed = W.hHeavy[2];
     S.I.nHeavy = S.cfg.apply_forces ? W.hHeavy[0] : 0;
     S.I.nHeavyFree = S.cfg.apply_forces ? W.hHeavy[1] : 0;
     WG_CUDA_TRY(cudaGetLastError());

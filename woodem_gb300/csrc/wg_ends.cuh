@@ -39,6 +39,18 @@ __device__ __forceinline__ void twoSum(float a, float b, float& s, float& e) {
     e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 
+// (hB + lB) - (hA + lA) as s + t with |t| << |s|: s + e = hB - hA exactly, t = e + (lB - lA).
+__device__ __forceinline__ void dfDiff(float hA, float lA, float hB, float lB, float& s, float& t) {
+    float e;
+    twoSum(hB, -hA, s, e);
+    t = e + (lB - lA);
+}
+// (s + t)^2 as p + c: p = fl(s*s), c = the FMA residual of s*s plus t*(2s + t).
+__device__ __forceinline__ void dfSquare(float s, float t, float& p, float& c) {
+    p = s * s;
+    c = fmaf(s, s, -p) + t * (2.f * s + t);
+}
+
 // Compensated accumulation of FP32 ends (FP32-force mode): each component is carried as an
 // unevaluated FP32 pair hi + lo with the rounding error of every addition captured exactly by
 // TwoSum, which keeps ~48 significant bits, and is converted to FP64 once per particle. On
@@ -56,12 +68,18 @@ struct DF6 {
         add1(0, x.x); add1(1, x.y); add1(2, x.z);
         add1(3, x.w); add1(4, y.x); add1(5, y.y);
     }
-    __device__ __forceinline__ double val(int k) const { return (double)h[k] + (double)l[k]; }
-    // F = G + sum of forces, T = sum of torques
-    __device__ __forceinline__ void result(const D3& G, D3& F, D3& T) const {
-        F = G + D3{val(0), val(1), val(2)};
-        T = D3{val(3), val(4), val(5)};
+    // start the force from m*g, both given as double-float pairs: the exact product of the high
+    // parts (FMA residual) plus the cross terms
+    __device__ __forceinline__ void initGravity(float mh, float ml, const float* gh, const float* gl) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const float p = mh * gh[k];
+            h[k] = p;
+            l[k] = fmaf(mh, gh[k], -p) + (mh * gl[k] + ml * gh[k]);
+        }
     }
+    __device__ __forceinline__ double val(int k) const { return (double)h[k] + (double)l[k]; }
+    __device__ __forceinline__ float net(int k) const { return __fadd_rn(h[k], l[k]); }
 };
 
 // Adds the end slots [e0, e1) of every lane with take==true to acc. Must be called by all

@@ -18,7 +18,8 @@ enum : uint32_t {
 enum : uint32_t {
     C_REAL = 1u,     // geom && phys exist
     C_SWAP = 2u,     // pA is the hi id (functor order Facet/Wall first)
-    C_PENDING = 16u  // law requested removal in the last ContactLoop
+    C_PENDING = 16u, // law requested removal in the last ContactLoop
+    C_DORMANT = 32u  // not real and too far apart to touch before the next full collider run
 };
 enum { CT_SS = 0, CT_FS = 1, CT_WS = 2, CT_NONE = 3 };
 __host__ __device__ inline uint32_t ctype(uint32_t fl) { return (fl >> 2) & 3u; }
@@ -39,7 +40,9 @@ struct ScenePar {
     int32_t trsfRenorm, approxMask, noRatch, noSlip, noBreak, noFrict, noAttraction, hzViscOn;
     int32_t periodic, homoDeform, hasGravity, evalStress;
     uint32_t loneMask;
-    int32_t _pad;
+    float dtF, ssDfAbsF;  // FP32 copies read by the FP32-force kernels
+    float gH[3], gL[3];   // gravity as double-float pairs (g = gH + gL)
+    float dampingF, maxD2F;
     // periodic cell, integrated on the host each step (core/Cell.cpp:81-120)
     double hSize[9], pprevHsize[9], gradV[9], nextGradV[9], dGradV[9], midGradV[9], shiftVelMat[9];
     double ImLL4hInv[9], IpLL4h[9], LmL[9], unshear[9];
@@ -63,6 +66,8 @@ struct DevNodes {
     // (x = hi + lo): ph/pl = position and radius, vh/vl = velocity with angVel.x/.y in w, wz = angVel.z
     float4 *ph, *pl, *vh, *vl;
     float* wz;
+    float4* orif;   // FP32-force mode: the orientation (w x y z), in place of ori
+    float2* rsplit; // FP32-force mode: the radius as a double-float pair (constant)
 };
 struct DevParticles {
     int32_t n;
@@ -109,7 +114,7 @@ struct DevIncidence {
     int32_t* loStart;  // nPar+1: contacts with lo==p are [loStart[p], loStart[p+1])
     int32_t* hiStart;  // nPar+1: hiList[hiStart[p] .. hiStart[p+1]) are contacts with hi==p, ascending
     int32_t* hiList;
-    int32_t* slotLo;   // per contact: end slot of its lo particle
+    int32_t* slotLo;   // per contact: end slot of its lo particle (-1: no slot, the contact is inactive)
     int32_t* slotHi;   // per contact: end slot of its hi particle
     double4_32a* endA; // FP64 mode: (Fx, Fy, Fz, Tx) on the particle, torque about its node
     double2* endB;     // FP64 mode: (Ty, Tz)
@@ -119,6 +124,16 @@ struct DevIncidence {
     int32_t* heavy;      // [0, nHeavy): particles whose degree exceeds kHeavyThreshold
     int32_t* heavyFree;  // [0, nHeavyFree): those of them whose node has a free DOF
     int32_t nHeavy, nHeavyFree;
+};
+// FP32-force mode per-node constants, one 32-byte record read by Leapfrog instead of the
+// inertia/mass and flag arrays: 1/m and 1/I per axis in FP32, the mass as a double-float pair
+// (mass = mh + ml), the DemData flags.
+struct NodeConst32 {
+    float invMass;
+    float invI[3];
+    float mh, ml;
+    uint32_t flags;
+    uint32_t _pad;
 };
 // Particles with more end slots than this are summed by a block tree instead of one lane.
 constexpr int kHeavyThreshold = 64;
@@ -152,12 +167,20 @@ void launch_forces(cudaStream_t st, const DevNodes& N, const DevParticles& P, co
                    const int* dFlags, bool perStep);
 void launch_advance(cudaStream_t st, long long* dStep, const int* dFlags);
 // FP32-force mode (wg_step32.cu)
-void launch_leapfrog32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const double4_32a* invm,
+void launch_leapfrog32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const NodeConst32* nc,
                        const ScenePar* sp, int* dFlags, int fromEnds);
-void launch_contact_fp32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C,
-                         const DevIncidence& I, const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dFlags);
-void launch_forces32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const ScenePar* sp,
-                     const int* dFlags, bool perStep);
+// Contacts [0, nMixed) may be of any type; [nMixed, C.n) join two spheres (both ids above every
+// boundary particle) and, in an aperiodic scene, go to a sphere-sphere-only kernel.
+// With a side stream the mixed range runs beside the sphere-sphere range (joined on st).
+struct SideStream {
+    cudaStream_t st = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+};
+void launch_contact_fp32(cudaStream_t st, const SideStream& side, const DevNodes& N, const DevParticles& P, const DevContacts& C,
+                         const DevIncidence& I, const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dFlags,
+                         int64_t nMixed, bool periodic);
+void launch_forces32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const NodeConst32* nc,
+                     const ScenePar* sp, const int* dFlags, bool perStep);
 
 // ------------------------------------------------------------------ broad phase (wg_collide.cu)
 struct Grid {
@@ -178,6 +201,7 @@ struct DevBuf {
 struct Sim {
     int device = 0;
     cudaStream_t stream = nullptr;
+    SideStream side;
     std::string err;
     wg_config cfg{};
     bool haveCfg = false;
@@ -200,8 +224,11 @@ struct Sim {
     DevContacts C{}, Cb{};  // current and spare (merge target)
     DevIncidence I{};
     int64_t cCap = 0;
+    int64_t nMixed = 0;   // contacts [0, nMixed) may involve a boundary particle (see launch_contact_fp32)
+    int64_t nActive = 0;  // contacts with end slots (a functor applies and the pair is not dormant)
+    int32_t maxBoundaryId = -1;  // largest id of a non-sphere particle
     double4_32a* dMats = nullptr;
-    double4_32a* dInvM = nullptr;  // 1/Ix 1/Iy 1/Iz 1/m per node slot (FP32-force mode)
+    NodeConst32* dNodeC = nullptr;  // per node slot (FP32-force mode)
     int prec = 0;                  // WG_PREC_*
     ScenePar hPar{};
     ScenePar* dPar = nullptr;

@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(128) k_contact_fp64(DevNodes N, DevParticles P
     const ScenePar& sp = *spp;
     uint32_t fl = C.flags[c];
     const uint32_t ty = ctype(fl);
-    if (ty == CT_NONE) return;
+    if (ty == CT_NONE || (fl & C_DORMANT)) return;
     fl &= ~C_PENDING;
     const uint64_t key = C.key[c];
     const int lo = (int)(key >> 32), hi = (int)(key & 0xffffffffu);

@@ -39,88 +39,106 @@ __device__ __forceinline__ F3 fnormalized(F3 a) {
 }
 
 // ---------------------------------------------------------------------------------- Leapfrog
-// Leapfrog::run (pkg/dem/Leapfrog.cpp:103-255) with precomputed 1/m and 1/I; the node
-// orientation (which no force of the supported shapes depends on) is advanced in FP32.
-__global__ void __launch_bounds__(256) k_leapfrog32(DevNodes N, DevParticles P, DevIncidence I, const double4_32a* __restrict__ invm,
+__device__ __forceinline__ float fsgn(float s) { return s < 0.f ? -1.f : (s > 0.f ? 1.f : 0.f); }
+
+// Leapfrog::run (pkg/dem/Leapfrog.cpp:103-255), FP32-force mode. The force and torque of the step
+// (m*g plus the compensated sum of the particle's FP32 end slots) give the accelerations in FP32;
+// the velocity, angular velocity and position are accumulated in FP64:
+//   vel += fl64(dt*a),  angVel += fl64(dt*alpha),  pos += vel*dt.
+// The orientation, which no force of the supported shapes depends on, is advanced in FP32.
+// Writes the double-float mirrors of position and velocity used by the contact kernel.
+// The node state is loaded before the end-slot sum so that its loads overlap the staging.
+__global__ void __launch_bounds__(256) k_leapfrog32(DevNodes N, DevParticles P, DevIncidence I, const NodeConst32* __restrict__ ncs,
                                                     const ScenePar* __restrict__ spp, int* __restrict__ dFlags, int fromEnds) {
-    __shared__ EndStage<float4, float2, 64> stage[8];
+    __shared__ EndStage<float4, float2, 128> stage[8];
     if (halted(dFlags)) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < N.n;
     const ScenePar& sp = *spp;
-    const uint32_t flags = valid ? N.flags[i] : 0u;
-    const double mass = valid ? N.minert[i].w : 0.;
-    // DemData.force/torque: m*g plus the compensated sum of the FP32 end slots of the last
-    // contact loop (see DF6), or the stored value
+    NodeConst32 nc{0.f, {0.f, 0.f, 0.f}, 0.f, 0.f, 0u, 0u};
+    double4_32a pr = make_double4_32a(0., 0., 0., 0.), v4 = pr, w4 = pr, lp4 = pr;
+    if (valid) {
+        nc = ncs[i];
+        pr = N.posr[i];
+        v4 = N.vel[i];
+        w4 = N.angv[i];
+        lp4 = N.lastPos[i];
+    }
+    const uint32_t flags = nc.flags;
+    // DemData.force/torque of this step
     const bool uni = valid && i < P.n && P.shape[i] != WG_SHAPE_FACET;
     int e0 = 0, e1 = 0;
-    bool take = false;
-    D3 f{0, 0, 0}, t{0, 0, 0};
+    bool take = false, summed = false;
+    DF6 acc;
     if (fromEnds && uni) {
-        if (sp.hasGravity && !(flags & F_GRAVITY_SKIP)) f = mass * D3{sp.g[0], sp.g[1], sp.g[2]};
+        if (sp.hasGravity && !(flags & F_GRAVITY_SKIP)) acc.initGravity(nc.mh, nc.ml, sp.gH, sp.gL);
+        summed = true;
         if (sp.applyForces) {
             endRange(I, i, e0, e1);
             take = (e1 - e0) <= kHeavyThreshold;
-            if (!take) {
-                f = ld3(N.force[i]);
-                t = ld3(N.torque[i]);
-            }
+            summed = take;
         }
-    } else if (valid) {
-        f = ld3(N.force[i]);
-        t = ld3(N.torque[i]);
     }
-    DF6 acc;
     warpSumEnds(I.endAf, I.endBf, take, e0, e1, stage[threadIdx.x >> 5], acc);
-    if (take) {
-        const D3 G = f;
-        acc.result(G, f, t);
-    }
     if (!valid || (flags & F_CLUMPED)) return;
+    F3 f, t;
+    if (summed) {
+        f = F3{acc.net(0), acc.net(1), acc.net(2)};
+        t = F3{acc.net(3), acc.net(4), acc.net(5)};
+    } else {  // the stored value: first step after the host wrote the state, or a heavy particle
+        f = toF(ld3(N.force[i]));
+        t = toF(ld3(N.torque[i]));
+    }
     const double dt = sp.dt;
-    const double damping = sp.damping;
-    const bool damp = (damping != 0. && !(flags & F_DAMPING_SKIP));
-    const double4_32a pr = N.posr[i];
+    const float dtf = sp.dtF;
+    const bool damp = (sp.damping != 0. && !(flags & F_DAMPING_SKIP));
     D3 pos = ld3(pr);
-    D3 vel = ld3(N.vel[i]);
-    D3 angVel = ld3(N.angv[i]);
-    const double4_32a iv = invm[i];
+    D3 vel = ld3(v4);
+    D3 angVel = ld3(w4);
     const bool blockedAll = (flags & F_DOF_ALL) == F_DOF_ALL;
     const int homoDeform = sp.periodic ? sp.homoDeform : -1;
-    D3 linAccel{0, 0, 0};
+    F3 la{0.f, 0.f, 0.f};
     if (!blockedAll) {
-        linAccel = D3{(flags & 1u) ? 0. : f.x * iv.w, (flags & 2u) ? 0. : f.y * iv.w, (flags & 4u) ? 0. : f.z * iv.w};
-        D3 pvf = vel, pva = angVel;
-        if (sp.periodic) {
-            if (homoDeform == 2 || homoDeform == 3) pvf = vel - mul(*(const DM3*)sp.gradV, pos);
-            else if (homoDeform == 4) pvf = vel - mul(*(const DM3*)sp.gradV, pos - (dt / 2) * vel);
-            if (homoDeform == 4) pva = angVel - D3{sp.spinVec[0], sp.spinVec[1], sp.spinVec[2]};
-        }
+        la = F3{(flags & 1u) ? 0.f : f.x * nc.invMass, (flags & 2u) ? 0.f : f.y * nc.invMass, (flags & 4u) ? 0.f : f.z * nc.invMass};
+        F3 pvf{0.f, 0.f, 0.f}, pva{0.f, 0.f, 0.f};
         if (damp) {
-            linAccel.x *= 1 - damping * ((f.x * (pvf.x + 0.5 * dt * linAccel.x)) > 0 ? 1 : ((f.x * (pvf.x + 0.5 * dt * linAccel.x)) < 0 ? -1 : 0));
-            linAccel.y *= 1 - damping * ((f.y * (pvf.y + 0.5 * dt * linAccel.y)) > 0 ? 1 : ((f.y * (pvf.y + 0.5 * dt * linAccel.y)) < 0 ? -1 : 0));
-            linAccel.z *= 1 - damping * ((f.z * (pvf.z + 0.5 * dt * linAccel.z)) > 0 ? 1 : ((f.z * (pvf.z + 0.5 * dt * linAccel.z)) < 0 ? -1 : 0));
+            // nonviscDamp2nd (Leapfrog.cpp:32-34) on the fluctuation velocity (Cell.cpp:36-57)
+            D3 v = vel, w = angVel;
+            if (sp.periodic) {
+                if (homoDeform == 2 || homoDeform == 3) v = vel - mul(*(const DM3*)sp.gradV, pos);
+                else if (homoDeform == 4) v = vel - mul(*(const DM3*)sp.gradV, pos - (dt / 2) * vel);
+                if (homoDeform == 4) w = angVel - D3{sp.spinVec[0], sp.spinVec[1], sp.spinVec[2]};
+            }
+            pvf = toF(v);
+            pva = toF(w);
+            const float d = sp.dampingF;
+            la.x *= 1.f - d * fsgn(f.x * (pvf.x + 0.5f * dtf * la.x));
+            la.y *= 1.f - d * fsgn(f.y * (pvf.y + 0.5f * dtf * la.y));
+            la.z *= 1.f - d * fsgn(f.z * (pvf.z + 0.5f * dtf * la.z));
         }
         if (homoDeform == 4)
-            vel = mul(*(const DM3*)sp.ImLL4hInv, (mul(*(const DM3*)sp.LmL, pos) + mul(*(const DM3*)sp.IpLL4h, vel)) + linAccel * dt);
+            vel = mul(*(const DM3*)sp.ImLL4hInv, (mul(*(const DM3*)sp.LmL, pos) + mul(*(const DM3*)sp.IpLL4h, vel)) +
+                                                   D3{(double)la.x, (double)la.y, (double)la.z} * dt);
         else
-            vel = vel + dt * linAccel;
-        if (iv.x != 0 || iv.y != 0 || iv.z != 0) {
-            D3 angAccel{(flags & 8u) ? 0. : t.x * iv.x, (flags & 16u) ? 0. : t.y * iv.y, (flags & 32u) ? 0. : t.z * iv.z};
+            vel = vel + D3{(double)(dtf * la.x), (double)(dtf * la.y), (double)(dtf * la.z)};
+        if (nc.invI[0] != 0.f || nc.invI[1] != 0.f || nc.invI[2] != 0.f) {
+            F3 aa{(flags & 8u) ? 0.f : t.x * nc.invI[0], (flags & 16u) ? 0.f : t.y * nc.invI[1], (flags & 32u) ? 0.f : t.z * nc.invI[2]};
             if (damp) {
-                angAccel.x *= 1 - damping * ((t.x * (pva.x + 0.5 * dt * angAccel.x)) > 0 ? 1 : ((t.x * (pva.x + 0.5 * dt * angAccel.x)) < 0 ? -1 : 0));
-                angAccel.y *= 1 - damping * ((t.y * (pva.y + 0.5 * dt * angAccel.y)) > 0 ? 1 : ((t.y * (pva.y + 0.5 * dt * angAccel.y)) < 0 ? -1 : 0));
-                angAccel.z *= 1 - damping * ((t.z * (pva.z + 0.5 * dt * angAccel.z)) > 0 ? 1 : ((t.z * (pva.z + 0.5 * dt * angAccel.z)) < 0 ? -1 : 0));
+                const float d = sp.dampingF;
+                aa.x *= 1.f - d * fsgn(t.x * (pva.x + 0.5f * dtf * aa.x));
+                aa.y *= 1.f - d * fsgn(t.y * (pva.y + 0.5f * dtf * aa.y));
+                aa.z *= 1.f - d * fsgn(t.z * (pva.z + 0.5f * dtf * aa.z));
             }
-            angVel = angVel + dt * angAccel;
+            angVel = angVel + D3{(double)(dtf * aa.x), (double)(dtf * aa.y), (double)(dtf * aa.z)};
             if (homoDeform == 4) angVel = angVel - D3{sp.deltaSpinVec[0], sp.deltaSpinVec[1], sp.deltaSpinVec[2]};
         }
     } else {
         if (homoDeform == 4) vel = mul(*(const DM3*)sp.ImLL4hInv, mul(*(const DM3*)sp.LmL, pos) + mul(*(const DM3*)sp.IpLL4h, vel));
     }
     if (homoDeform >= 0 && homoDeform != 4) {
+        const D3 lad{(double)la.x, (double)la.y, (double)la.z};
         if (homoDeform == 2 || homoDeform == 3) {
-            if (homoDeform == 3) vel = vel + mul(*(const DM3*)sp.midGradV, vel - (dt / 2.) * linAccel) * dt;
+            if (homoDeform == 3) vel = vel + mul(*(const DM3*)sp.midGradV, vel - (dt / 2.) * lad) * dt;
             vel = vel + mul(*(const DM3*)sp.dGradV, pos);
         } else if (homoDeform == 1) {
             pos = pos + mul(*(const DM3*)sp.nextGradV, pos) * dt;
@@ -130,56 +148,59 @@ __global__ void __launch_bounds__(256) k_leapfrog32(DevNodes N, DevParticles P, 
     N.posr[i] = make_double4_32a(pos.x, pos.y, pos.z, pr.w);
     N.vel[i] = make_double4_32a(vel.x, vel.y, vel.z, 0.);
     N.angv[i] = make_double4_32a(angVel.x, angVel.y, angVel.z, 0.);
+    const F3 w = toF(angVel);
     {
         // double-float mirrors read by the sphere-sphere contact geometry
+        const float2 rs = N.rsplit[i];
         float4 h, l;
         splitDF(pos.x, h.x, l.x);
         splitDF(pos.y, h.y, l.y);
         splitDF(pos.z, h.z, l.z);
-        splitDF(pr.w, h.w, l.w);
+        h.w = rs.x;
+        l.w = rs.y;
         N.ph[i] = h;
         N.pl[i] = l;
         splitDF(vel.x, h.x, l.x);
         splitDF(vel.y, h.y, l.y);
         splitDF(vel.z, h.z, l.z);
-        h.w = (float)angVel.x;
-        l.w = (float)angVel.y;
+        h.w = w.x;
+        l.w = w.y;
         N.vh[i] = h;
         N.vl[i] = l;
-        N.wz[i] = (float)angVel.z;
+        N.wz[i] = w.z;
     }
-    if (angVel.x != 0 || angVel.y != 0 || angVel.z != 0) {
-        const double4_32a o = N.ori[i];
-        const F3 w = toF(angVel);
-        const float ang = sqrtf(fdot(w, w));
-        if (ang > 0.f) {
-            float s, c;
-            sincosf(0.5f * ang * (float)dt, &s, &c);
-            const F3 ax = w * (1.f / ang);
-            const float qw = c, qx = s * ax.x, qy = s * ax.y, qz = s * ax.z;
-            const float ow = (float)o.x, ox = (float)o.y, oy = (float)o.z, oz = (float)o.w;
-            float rw = qw * ow - qx * ox - qy * oy - qz * oz;
-            float rx = qw * ox + qx * ow + qy * oz - qz * oy;
-            float ry = qw * oy + qy * ow + qz * ox - qx * oz;
-            float rz = qw * oz + qz * ow + qx * oy - qy * ox;
-            const float inv = rsqrtf(rw * rw + rx * rx + ry * ry + rz * rz);
-            N.ori[i] = make_double4_32a(rw * inv, rx * inv, ry * inv, rz * inv);
-        }
+    const float ang = sqrtf(fdot(w, w));
+    if (ang > 0.f) {
+        // leapfrogSphericalRotate (Leapfrog.cpp:280-288) in FP32
+        const float4 o = N.orif[i];
+        float s, c;
+        sincosf(0.5f * ang * dtf, &s, &c);
+        const F3 ax = w * (1.f / ang);
+        const float qw = c, qx = s * ax.x, qy = s * ax.y, qz = s * ax.z;
+        const float ow = o.x, ox = o.y, oy = o.z, oz = o.w;
+        float rw = qw * ow - qx * ox - qy * oy - qz * oz;
+        float rx = qw * ox + qx * ow + qy * oz - qz * oy;
+        float ry = qw * oy + qy * ow + qz * ox - qx * oz;
+        float rz = qw * oz + qz * ow + qx * oy - qy * ox;
+        const float inv = rsqrtf(rw * rw + rx * rx + ry * ry + rz * rz);
+        N.orif[i] = make_float4(rw * inv, rx * inv, ry * inv, rz * inv);
     }
     if (sp.reset && !uni) {
+        // force reset of nodes whose force is not rebuilt by the contact sum (facet vertices)
         D3 G{0, 0, 0};
-        if (sp.hasGravity && !(flags & F_GRAVITY_SKIP)) G = mass * D3{sp.g[0], sp.g[1], sp.g[2]};
+        if (sp.hasGravity && !(flags & F_GRAVITY_SKIP)) G = ((double)nc.mh + (double)nc.ml) * D3{sp.g[0], sp.g[1], sp.g[2]};
         N.force[i] = make_double4_32a(G.x, G.y, G.z, 0.);
         N.torque[i] = make_double4_32a(0., 0., 0., 0.);
     }
-    const D3 lp = ld3(N.lastPos[i]);
-    if (sqn(lp - pos) > sp.maxD2) atomicOr(dFlags + FL_FULL, 1);
+    // verlet test (InsertionSortCollider.cpp:339-350) on the FP64 displacement rounded to FP32
+    const F3 dd = toF(ld3(lp4) - pos);
+    if (fdot(dd, dd) > sp.maxD2F) atomicOr(dFlags + FL_FULL, 1);
 }
 
-void launch_leapfrog32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const double4_32a* invm,
+void launch_leapfrog32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const NodeConst32* nc,
                        const ScenePar* sp, int* dFlags, int fromEnds) {
     if (N.n == 0) return;
-    k_leapfrog32<<<(N.n + 255) / 256, 256, 0, st>>>(N, P, I, invm, sp, dFlags, fromEnds);
+    k_leapfrog32<<<(N.n + 255) / 256, 256, 0, st>>>(N, P, I, nc, sp, dFlags, fromEnds);
 }
 
 // ---------------------------------------------------------------------------------- ContactLoop
@@ -219,18 +240,6 @@ __device__ __forceinline__ void frameInit(F3 n, Frame& f) {
 }
 
 // ---- double-float arithmetic for the sphere-sphere geometry (FP32 pipe only)
-// (hB + lB) - (hA + lA) as s + t with |t| << |s|: s + e = hB - hA exactly, t = e + (lB - lA).
-__device__ __forceinline__ void dfDiff(float hA, float lA, float hB, float lB, float& s, float& t) {
-    float e;
-    twoSum(hB, -hA, s, e);
-    t = e + (lB - lA);
-}
-// (s + t)^2 as p + c: p = fl(s*s), c = the FMA residual of s*s plus t*(2s + t).
-__device__ __forceinline__ void dfSquare(float s, float t, float& p, float& c) {
-    p = s * s;
-    c = fmaf(s, s, -p) + t * (2.f * s + t);
-}
-
 // Sphere-sphere overlap test and normal overlap without FP64 arithmetic. Positions, velocities
 // and radii are read from the double-float mirrors written by Leapfrog (x = hi + lo, both FP32,
 // |x - (hi + lo)| <= 2^-48 |x|), so the relative position carries ~47 bits and
@@ -301,20 +310,24 @@ __device__ __forceinline__ bool geomSS32(const DevNodes& N, int A, int B, float 
     return true;
 }
 
+// SSONLY: every contact of [c0, c1) joins two spheres of an aperiodic scene (no FP64 on the
+// evaluation path except contact creation).
+template <bool SSONLY>
 __global__ void __launch_bounds__(256) k_contact_fp32(DevNodes N, DevParticles P, DevContacts C, DevIncidence I,
                                                      const double4_32a* __restrict__ mats, const ScenePar* __restrict__ spp,
-                                                     const long long* __restrict__ dStep, int* __restrict__ dFlags) {
+                                                     const long long* __restrict__ dStep, int* __restrict__ dFlags, int64_t c0,
+                                                     int64_t c1, int haltBlock) {
     if (dFlags[FL_FULL] || halted(dFlags)) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) dFlags[FL_HALT] = 1;
+        if (haltBlock && blockIdx.x == 0 && threadIdx.x == 0) dFlags[FL_HALT] = 1;
         return;
     }
     int* dErr = dFlags + FL_ERR;
-    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= C.n) return;
+    const int64_t c = c0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= c1) return;
     const ScenePar& sp = *spp;
     uint32_t fl = C.flags[c];
     const uint32_t ty = ctype(fl);
-    if (ty == CT_NONE) return;
+    if (ty == CT_NONE || (fl & C_DORMANT)) return;
     fl &= ~C_PENDING;
     const uint64_t key = C.key[c];
     const int lo = (int)(key >> 32), hi = (int)(key & 0xffffffffu);
@@ -322,10 +335,10 @@ __global__ void __launch_bounds__(256) k_contact_fp32(DevNodes N, DevParticles P
     const bool real = fl & C_REAL;
     const long long step = *dStep;
     const double dt = sp.dt;
-    const float dtf = (float)dt;
+    const float dtf = sp.dtF;
     bool shifted = false;
     D3 shift2{0, 0, 0}, shiftVel2{0, 0, 0};
-    if (sp.periodic) {
+    if (!SSONLY && sp.periodic) {
         int a, b, cc;
         unpackCellDist(C.cdist[c], a, b, cc);
         if (fl & C_SWAP) { a = -a; b = -b; cc = -cc; }
@@ -340,9 +353,9 @@ __global__ void __launch_bounds__(256) k_contact_fp32(DevNodes N, DevParticles P
     // c1x/c2x: mid-step branch vectors of L6Geom.cpp:156-160; dv: relative velocity of the centres
     F3 n, armA, armB, c1x, c2x, dv, w1, w2;
     float uN, r1, r2;
-    if (ty == CT_SS && !shifted) {
+    if (SSONLY || (ty == CT_SS && !shifted)) {
         SSGeo g;
-        if (!geomSS32(N, A, B, (float)fabs(sp.ssDistFactor), real, g)) {
+        if (!geomSS32(N, A, B, sp.ssDfAbsF, real, g)) {
             C.flags[c] = fl;
             return;
         }
@@ -373,7 +386,7 @@ __global__ void __launch_bounds__(256) k_contact_fp32(DevNodes N, DevParticles P
         w1 = toF(ld3(N.angv[A]));
         w2 = toF(ld3(N.angv[B]));
     }
-    if (ty == CT_SS) {
+    if (SSONLY || ty == CT_SS) {
         // contPt = x1 + (r1 + uN/2) n (Sphere.cpp:103), written relative to both centres
         armA = (r1 + 0.5f * uN) * n;
         armB = -(r2 + 0.5f * uN) * n;
@@ -383,7 +396,7 @@ __global__ void __launch_bounds__(256) k_contact_fp32(DevNodes N, DevParticles P
             c1x = 0.5f * ((r1 + 0.5f * up) * pn + armA);
             c2x = 0.5f * (-(r2 + 0.5f * up) * pn + armB);
         }
-    } else {
+    } else if (!SSONLY) {
         Geo g;
         bool touch;
         if (ty == CT_WS) touch = geomWS(N, P, real ? (double)C.fcol[CF_T0X + P.aux[A].x][c] : 0., A, B, shift2, real, g);
@@ -550,38 +563,54 @@ __global__ void __launch_bounds__(256) k_contact_fp32(DevNodes N, DevParticles P
     C.flags[c] = fl | C_REAL;
 }
 
-void launch_contact_fp32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C, const DevIncidence& I,
-                         const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dFlags) {
-    k_contact_fp32<<<(unsigned)std::max<int64_t>(1, (C.n + 255) / 256), 256, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags);
+void launch_contact_fp32(cudaStream_t st, const SideStream& side, const DevNodes& N, const DevParticles& P, const DevContacts& C,
+                         const DevIncidence& I, const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dFlags,
+                         int64_t nMixed, bool periodic) {
+    const int64_t nm = periodic ? C.n : std::min<int64_t>(nMixed, C.n);
+    const int64_t ns = C.n - nm;
+    if (ns > 0 && nm > 0 && side.st) {
+        // the mixed range (facets and walls, FP64 geometry) beside the sphere-sphere range; the
+        // sphere-sphere launch raises FL_HALT when a full run is due
+        cudaEventRecord(side.fork, st);
+        cudaStreamWaitEvent(side.st, side.fork, 0);
+        k_contact_fp32<false><<<(unsigned)((nm + 255) / 256), 256, 0, side.st>>>(N, P, C, I, mats, sp, dStep, dFlags, 0, nm, 0);
+        k_contact_fp32<true><<<(unsigned)((ns + 255) / 256), 256, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags, nm, C.n, 1);
+        cudaEventRecord(side.join, side.st);
+        cudaStreamWaitEvent(st, side.join, 0);
+        return;
+    }
+    // the first launch also raises FL_HALT when a full run is due (it always runs)
+    k_contact_fp32<false><<<(unsigned)std::max<int64_t>(1, (nm + 255) / 256), 256, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags,
+                                                                                          0, nm, 1);
+    if (ns > 0)
+        k_contact_fp32<true><<<(unsigned)((ns + 255) / 256), 256, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags, nm, C.n, 0);
 }
 
 // ---------------------------------------------------------------------------------- force sum
-// DemData.force/torque for reporting after a run: the same sum as k_leapfrog32 (m*g plus the
-// compensated sum of the particle's FP32 end slots, in slot order), written to the node.
-__global__ void __launch_bounds__(256) k_forces32(DevNodes N, DevParticles P, DevIncidence I, const ScenePar* __restrict__ spp) {
-    __shared__ EndStage<float4, float2, 64> stage[8];
+// DemData.force/torque for reporting after a run: the sum of k_leapfrog32 (m*g and the
+// particle's FP32 end slots, compensated, in slot order) converted to FP64, for every particle
+// whose degree is at most kHeavyThreshold. Its FP32 rounding is the force k_leapfrog32 uses.
+__global__ void __launch_bounds__(256) k_forces32(DevNodes N, DevParticles P, DevIncidence I, const NodeConst32* __restrict__ ncs,
+                                                  const ScenePar* __restrict__ spp) {
+    __shared__ EndStage<float4, float2, 128> stage[8];
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     const ScenePar& sp = *spp;
     const bool uni = p < P.n && P.shape[p] != WG_SHAPE_FACET;
     int e0 = 0, e1 = 0;
     bool take = false;
-    D3 G{0, 0, 0};
+    DF6 acc;
     if (uni) {
-        const uint32_t flags = N.flags[p];
-        const double mass = N.minert[p].w;
-        if (sp.hasGravity && !(flags & F_GRAVITY_SKIP)) G = mass * D3{sp.g[0], sp.g[1], sp.g[2]};
+        const NodeConst32 nc = ncs[p];
+        if (sp.hasGravity && !(nc.flags & F_GRAVITY_SKIP)) acc.initGravity(nc.mh, nc.ml, sp.gH, sp.gL);
         if (sp.applyForces) {
             endRange(I, p, e0, e1);
             take = (e1 - e0) <= kHeavyThreshold;
         }
     }
-    DF6 acc;
     warpSumEnds(I.endAf, I.endBf, take, e0, e1, stage[threadIdx.x >> 5], acc);
     if (uni && (take || !sp.applyForces)) {
-        D3 F, T;
-        acc.result(G, F, T);
-        N.force[p] = make_double4_32a(F.x, F.y, F.z, 0.);
-        N.torque[p] = make_double4_32a(T.x, T.y, T.z, 0.);
+        N.force[p] = make_double4_32a(acc.val(0), acc.val(1), acc.val(2), 0.);
+        N.torque[p] = make_double4_32a(acc.val(3), acc.val(4), acc.val(5), 0.);
     }
 }
 
@@ -618,14 +647,14 @@ __global__ void k_forces32_heavy(DevNodes N, DevIncidence I, const int32_t* __re
     }
 }
 
-void launch_forces32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const ScenePar* sp,
-                     const int* dFlags, bool perStep) {
+void launch_forces32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const NodeConst32* nc,
+                     const ScenePar* sp, const int* dFlags, bool perStep) {
     if (P.n == 0) return;
     if (perStep) {
         if (I.nHeavyFree > 0) k_forces32_heavy<<<I.nHeavyFree, 256, 0, st>>>(N, I, I.heavyFree, sp, dFlags);
         return;
     }
-    k_forces32<<<(P.n + 255) / 256, 256, 0, st>>>(N, P, I, sp);
+    k_forces32<<<(P.n + 255) / 256, 256, 0, st>>>(N, P, I, nc, sp);
     if (I.nHeavy > 0) k_forces32_heavy<<<I.nHeavy, 256, 0, st>>>(N, I, I.heavy, sp, nullptr);
 }
 

@@ -109,12 +109,15 @@ def spatial_order(points, cell):
     return np.argsort(code, kind="stable")
 
 
-def settle(S, steps, g_factor=30.0, damping=0.3, precision="fp32", relax_steps=0, relax_damping=0.5):
+def settle(S, steps, g_factor=30.0, damping=0.3, precision="fp32", relax_steps=0, relax_damping=0.3, zero=True, relax_stages=4):
     """Compact a loose packing into a resting bed on the GPU: run ``steps`` steps under gravity
-    multiplied by ``g_factor`` with Leapfrog damping ``damping``, then ``relax_steps`` steps under
-    the scene's own gravity with damping ``relax_damping``; restore the scene's gravity, damping and
-    precision, zero the velocities, forces and torques of the free nodes, and reset
-    Scene.step/time. The contact history is dropped (the next run starts from the positions)."""
+    multiplied by ``g_factor`` with Leapfrog damping ``damping``, then bring gravity back to the
+    scene's own in ``relax_stages`` geometric stages (g_factor^(3/4), ^(1/2), ^(1/4), 1 for four)
+    of ``relax_steps/relax_stages`` steps each with damping ``relax_damping``, so that the elastic
+    energy stored under the high gravity leaves the bed gradually instead of launching it. Then
+    restore the scene's gravity, damping and precision, zero the forces and torques (and with
+    ``zero`` the velocities) of the free nodes, and reset Scene.step/time. The contact history is
+    dropped (the next run starts from the positions)."""
     lf = S.engines[0]
     g0 = np.array(S.dem.gravity, dtype=float)
     d0, p0 = lf.damping, S.gpu.precision
@@ -124,17 +127,18 @@ def settle(S, steps, g_factor=30.0, damping=0.3, precision="fp32", relax_steps=0
     S.gpu.precision = precision
     S.run(steps)
     if relax_steps:
-        S.close()
-        S.dem.gravity = g0
-        lf.damping = relax_damping
-        S.run(relax_steps)
+        for k in range(1, relax_stages + 1):
+            S.close()
+            S.dem.gravity = g0 * g_factor ** ((relax_stages - k) / float(relax_stages))
+            lf.damping = relax_damping
+            S.run(max(1, relax_steps // relax_stages))
     S.close()
     S.dem.gravity = g0
     lf.damping = d0
     S.gpu.precision = p0
     nd = S.dem._nodes.soa
     free = (nd.col("flags") & 63) != 63
-    for k in ("vel", "angVel", "force", "torque"):
+    for k in (("vel", "angVel", "force", "torque") if zero else ("force", "torque")):
         nd.col(k)[free] = 0.0
     S.step = 0
     S.time = 0.0
@@ -165,7 +169,7 @@ def hertz_drum(n=1_000_000, seed=0, diameter=1.2, length=0.6, div=201, axDiv=50,
     dt = 0.3*pWaveDt, verletDist = 0.1*min radius. Spheres are placed by seeded random
     sequential insertion (solid fraction ``fill_fraction``) in the lower part of the drum whose
     height is chosen to hold them. With ``settle_steps`` the fill is compacted into a resting bed
-    on the GPU (``settle``: ``settle_g`` times gravity, then ``relax_steps`` steps at 1 g) and the
+    on the GPU (``settle``: ``settle_g`` times gravity, then ``relax_steps`` steps easing back to 1 g) and the
     scene is rebuilt from the settled positions. With ``order`` the spheres are numbered along a
     Morton curve of their positions (cells of one largest diameter), so that spheres in contact
     have nearby ids; walls and facets keep the lowest ids."""
@@ -179,22 +183,32 @@ def hertz_drum(n=1_000_000, seed=0, diameter=1.2, length=0.6, div=201, axDiv=50,
     zf = _segment_height(Ri, min(area, 0.97 * math.pi * Ri * Ri))
     centers = pack_rsa(radii, (margin, -Ri, -Ri), (length - margin, Ri, zf), region=1, params=(0.0, 0.0, Ri, zf), seed=seed + 7)
     args = (diameter, length, div, axDiv, density, young, poisson, en, tanPhi, omega, verletRel)
+    vel = angVel = None
     if settle_steps:
         S0 = _drum_scene(centers, radii, *args, precision)
-        settle(S0, settle_steps, g_factor=settle_g, relax_steps=settle_steps // 6 if relax_steps is None else relax_steps)
-        A = _native_positions(S0)
-        centers = A
+        settle(S0, settle_steps, g_factor=settle_g, relax_steps=(3 * settle_steps) // 4 if relax_steps is None else relax_steps,
+               relax_damping=0.8, zero=True)
+        centers, vel, angVel = (_sphere_nodes(S0, k) for k in ("pos", "vel", "angVel"))
         S0 = None
     if order:
         perm = spatial_order(centers, 2 * rmax)
         centers, radii = centers[perm], radii[perm]
-    return _drum_scene(centers, radii, *args, precision)
+        if vel is not None:
+            vel, angVel = vel[perm], angVel[perm]
+    S = _drum_scene(centers, radii, *args, precision)
+    if vel is not None:
+        # the bed starts from the state it settled to
+        _sphere_nodes(S, "vel", vel)
+        _sphere_nodes(S, "angVel", angVel)
+    return S
 
 
-def _native_positions(S):
-    """Sphere centres of a scene whose spheres were added after its boundary particles."""
-    nd = S.dem._nodes.soa
+def _sphere_nodes(S, col, value=None):
+    """Read (or write) a node column for the spheres of a scene, in sphere order."""
     from . import _plan
+    nd = S.dem._nodes.soa
     A = _plan.compile_scene(S)
-    sph = A.particles["shape"] == 0
-    return nd.col("pos")[A.particles["nodes"][sph, 0]].copy()
+    nodes = A.particles["nodes"][A.particles["shape"] == 0, 0]
+    if value is None:
+        return nd.col(col)[nodes].copy()
+    nd.col(col)[nodes] = value
