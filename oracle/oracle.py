@@ -42,6 +42,7 @@ def lib():
         "wo_get_contacts": (C.c_int, [C.c_void_p, P_I32, P_I32, P_I32, P_I32, P_I32, P_D, P_D, P_D, P_D]),
         "wo_kinetic_energy": (C.c_int, [C.c_void_p, P_D]),
         "wo_get_aabbs": (C.c_int, [C.c_void_p, P_D, P_D]),
+        "wo_get_cell": (C.c_int, [C.c_void_p, P_D, P_D, P_D]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -106,6 +107,11 @@ class Oracle:
         mn, mx = np.empty((n, 3)), np.empty((n, 3))
         self.L.wo_get_aabbs(self.h, _native.ptr(mn), _native.ptr(mx))
         return mn, mx
+
+    def cell(self):
+        hs, tr, gv = np.zeros(9), np.zeros(9), np.zeros(9)
+        self.L.wo_get_cell(self.h, _native.ptr(hs), _native.ptr(tr), _native.ptr(gv))
+        return hs.reshape(3, 3), tr.reshape(3, 3), gv.reshape(3, 3)
 
     def close(self):
         if self.h:

@@ -1237,6 +1237,15 @@ int wo_get_stats(void* sp, wo_stats* o) {
     for (int i = 0; i < 9; i++) o->stress[i] = s->stress.m[i / 3][i % 3];
     return 0;
 }
+int wo_get_cell(void* sp, double* hsize, double* trsf, double* gradv) {
+    Scene* s = (Scene*)sp;
+    for (int i = 0; i < 9; i++) {
+        if (hsize) hsize[i] = s->cell.hSize.m[i / 3][i % 3];
+        if (trsf) trsf[i] = s->cell.trsf.m[i / 3][i % 3];
+        if (gradv) gradv[i] = s->cell.gradV.m[i / 3][i % 3];
+    }
+    return 0;
+}
 int64_t wo_num_contacts(void* s) { return (int64_t)((Scene*)s)->linView.size(); }
 int wo_get_contacts(void* sp, int32_t* id_lo, int32_t* id_hi, int32_t* id_a, int32_t* real, int32_t* cell_dist, double* fglob,
                     double* local, double* cpt, double* trsf) {

@@ -108,6 +108,8 @@ int wo_get_contacts(void* s, int32_t* id_lo, int32_t* id_hi, int32_t* id_a, int3
                     int32_t* cell_dist, double* fglob, double* local, double* cpt, double* trsf);
 /* Run only the broad phase (full run) on the current positions, without stepping. */
 int wo_collide_only(void* s);
+/* periodic cell: hSize, trsf, gradV (row-major 3x3) */
+int wo_get_cell(void* s, double* hsize, double* trsf, double* gradv);
 /* Per-particle force/torque as applied by the last ContactLoop (the node arrays). */
 int wo_kinetic_energy(void* s, double* ek);
 /* Aabb.min/max of every particle as computed at the last full run (verletDist included). */

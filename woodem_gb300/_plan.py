@@ -232,6 +232,10 @@ class Simulation:
     def run(self, n):
         self.push()
         L, h = self.H.L, self.H.h
+        if self.S.isPeriodic:
+            # Cell.nextGradV set between runs takes effect at the next step (core/Cell.hpp:152)
+            g = np.ascontiguousarray(np.asarray(self.S.cell.nextGradV, dtype=float).reshape(9))
+            self.H.check(L.wg_set_next_gradv(h, _native.ptr(g)), "set_next_gradv")
         self.H.check(L.wg_run(h, int(n)), "run")
         self.host_stale = True
         self._contacts = None
@@ -252,6 +256,10 @@ class Simulation:
             self.S.cell.hSize = hs.reshape(3, 3)
             self.S.cell.trsf = tr.reshape(3, 3)
             self.S.cell._gradV = gv.reshape(3, 3)
+            from .dem import ContactLoop
+            for e in self.S.engines:
+                if isinstance(e, ContactLoop):
+                    e.stress = np.array(st.stress).reshape(3, 3)
 
     def stats(self):
         st = _native.wg_stats()

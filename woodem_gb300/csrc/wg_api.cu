@@ -365,7 +365,10 @@ int Sim::upload() {
     prec = cfg.precision;
     if (prec == WG_PREC_FP32 && cfg.law == 1 && cfg.hz_gamma != 0)
         return fail(WG_ERR_UNSUPPORTED, "FP32-force mode: Cp2_FrictMat_HertzPhys.gamma (DMT adhesion) must be 0; use precision fp64");
-    if (cfg.periodic) return fail(WG_ERR_UNSUPPORTED, "periodic cells are not available in this build");
+    if (cfg.periodic)
+        for (int64_t i = 0; i < nPar; i++)
+            if (hShape[i] == WG_SHAPE_FACET)
+                return fail(WG_ERR_UNSUPPORTED, "facets in a periodic cell are outside the GPU path");
     for (int64_t i = 0; i < nPar; i++) {
         if (hMat[i] < 0 || hMat[i] >= (int)hDensity.size()) return fail(WG_ERR_ARG, "particle material index out of range");
     }
@@ -513,6 +516,9 @@ int Sim::upload() {
         N.wz = (float*)dalloc(sizeof(float) * nSlots);
         N.orif = (float4*)dalloc(sizeof(float4) * nSlots);
         N.rsplit = (float2*)dalloc(sizeof(float2) * nSlots);
+        N.lh = (float4*)dalloc(sizeof(float4) * nSlots);
+        N.ll = (float4*)dalloc(sizeof(float4) * nSlots);
+        if (!N.ll) return fail(WG_ERR_CUDA, "out of device memory (scene)");
         if (!dNodeC || !N.wz || !N.orif || !N.rsplit) return fail(WG_ERR_CUDA, "out of device memory (scene)");
         WG_CUDA_TRY(cudaMemcpy(N.orif, orf.data(), sizeof(float4) * nSlots, cudaMemcpyHostToDevice));
         WG_CUDA_TRY(cudaMemcpy(N.rsplit, rsp.data(), sizeof(float2) * nSlots, cudaMemcpyHostToDevice));
@@ -540,6 +546,8 @@ int Sim::upload() {
         WG_CUDA_TRY(cudaMemcpy(N.vh, hvh.data(), sizeof(float4) * nSlots, cudaMemcpyHostToDevice));
         WG_CUDA_TRY(cudaMemcpy(N.vl, hvl.data(), sizeof(float4) * nSlots, cudaMemcpyHostToDevice));
         WG_CUDA_TRY(cudaMemcpy(N.wz, hwz.data(), sizeof(float) * nSlots, cudaMemcpyHostToDevice));
+        WG_CUDA_TRY(cudaMemcpy(N.lh, hph.data(), sizeof(float4) * nSlots, cudaMemcpyHostToDevice));
+        WG_CUDA_TRY(cudaMemcpy(N.ll, hpl.data(), sizeof(float4) * nSlots, cudaMemcpyHostToDevice));
         WG_CUDA_TRY(cudaMemcpy(dNodeC, nc.data(), sizeof(NodeConst32) * nSlots, cudaMemcpyHostToDevice));
     }
     long long st0 = cfg.step;
@@ -563,6 +571,7 @@ int Sim::upload() {
         X.cell.integrateAndUpdate(0);
     }
     prepareParams();
+    if (cfg.periodic) fillCellPar(X);
     WG_CUDA_TRY(cudaMemcpy(dPar, &hPar, sizeof(ScenePar), cudaMemcpyHostToDevice));
     uploaded = true;
     initialized = false;
@@ -575,6 +584,7 @@ int Sim::checkErr() {
     WG_CUDA_TRY(cudaStreamSynchronize(stream));
     if (hFlags[1] == 101) return fail(WG_ERR_NAN, "NaN force in contact (message above)?!");
     if (hFlags[1] == 102) return fail(WG_ERR_NAN, "InsertionSortCollider: NaN in a particle bounding box (NaN position)");
+    if (hFlags[1] == 103) return fail(WG_ERR_PERIODIC, "InsertionSortCollider: Particle larger than half of the cell size encountered.");
     if (hFlags[1] == 100) return fail(WG_ERR_ARG, "Cg2_Facet_Sphere_L3Geom: Impossible sphere-facet intersection (all points are outside the edges). (please report bug)");
     if (hFlags[1] != 0) return fail(WG_ERR_STATE, "device error code " + std::to_string(hFlags[1]));
     return 0;
@@ -690,6 +700,23 @@ int Sim::run(int64_t n) {
         step += ds;
         time += ds * cfg.dt;
         done += ds;
+    }
+    // ContactLoop.stress of the last step (periodic cells with evalStress)
+    if (cfg.periodic && cfg.eval_stress && fromEnds && done > 0) {
+        const int64_t need = 9 * (std::max<int64_t>(1, (I.nAct + 255) / 256) + 1);
+        if (stressCap < need) {
+            if (dStress) dfree(dStress);
+            stressCap = need + need / 2;
+            dStress = (double*)dalloc(sizeof(double) * stressCap);
+            if (!dStress) return fail(WG_ERR_CUDA, "out of device memory (stress)");
+        }
+        if (launch_stress(stream, N, P, C, I, dPar, dStress + 9, stressCap - 9, dStress))
+            return fail(WG_ERR_STATE, "stress scratch too small");
+        double sum[9];
+        WG_CUDA_TRY(cudaMemcpyAsync(sum, dStress, sizeof(double) * 9, cudaMemcpyDeviceToHost, stream));
+        WG_CUDA_TRY(cudaStreamSynchronize(stream));
+        const double det = hdet(X.cell.hSize);
+        for (int q = 0; q < 9; q++) stress[q] = sum[q] / det;
     }
     // DemData.force/torque of the last contact loop, for the host and for the next run
     if (fromEnds) {
@@ -907,6 +934,7 @@ int wg_get_stats(wg_scene* s, wg_stats* o) {
     o->n_full_runs = S.nFullRuns;
     o->n_contacts = S.uploaded ? S.C.n : 0;
     o->verlet_dist = S.hPar.verletDist;
+    for (int q = 0; q < 9; q++) o->stress[q] = S.stress[q];
     if (S.uploaded && S.C.n > 0) {
         std::vector<uint32_t> fl(S.C.n);
         WG_CUDA_TRY(cudaMemcpy(fl.data(), S.C.flags, sizeof(uint32_t) * S.C.n, cudaMemcpyDeviceToHost));
@@ -941,8 +969,7 @@ int wg_get_cell(wg_scene* s, double* hsize, double* trsf, double* gradv) {
     return WG_OK;
 }
 
-// Contacts listed the way the reference's container holds them after a step: every contact
-// that is real, was removed by the law in the last step (pending), or whose boxes overlap.
+// Contacts listed the way the reference's container holds them after a step.
 static int collectContacts(Sim& S, std::vector<int64_t>& keep, std::vector<uint64_t>& key, std::vector<uint32_t>& fl,
                            std::vector<int32_t>& cd, std::vector<std::vector<double>>& cols) {
     const int64_t n = S.C.n;
@@ -957,7 +984,7 @@ static int collectContacts(Sim& S, std::vector<int64_t>& keep, std::vector<uint6
         std::vector<uint64_t> kc(n);
         WG_CUDA_TRY(cudaMemcpy(flc.data(), S.C.flags, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
         WG_CUDA_TRY(cudaMemcpy(kc.data(), S.C.key, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost));
-        const int64_t ne = 2 * std::max<int64_t>(S.nActive, 1);
+        const int64_t ne = 2 * std::max<int64_t>(S.I.nAct, 1);
         std::vector<double> ef(4 * ne);
         if (S.prec == WG_PREC_FP32) {
             std::vector<float> tmp(4 * ne);
@@ -1016,18 +1043,11 @@ static int collectContacts(Sim& S, std::vector<int64_t>& keep, std::vector<uint6
             }
         }
     }
-    std::vector<double4_32a> mn(S.nPar), mx(S.nPar);
-    if (S.nPar > 0) {
-        WG_CUDA_TRY(cudaMemcpy(mn.data(), S.P.mn, sizeof(double4_32a) * S.nPar, cudaMemcpyDeviceToHost));
-        WG_CUDA_TRY(cudaMemcpy(mx.data(), S.P.mx, sizeof(double4_32a) * S.nPar, cudaMemcpyDeviceToHost));
-    }
+    // every contact but those removed by the collider since the last full run (pending contacts
+    // whose boxes stopped overlapping)
     keep.clear();
-    for (int64_t c = 0; c < n; c++) {
-        if (fl[c] & (C_REAL | C_PENDING)) { keep.push_back(c); continue; }
-        const int a = (int)(key[c] >> 32), b = (int)(key[c] & 0xffffffffu);
-        const double4_32a &m1 = mn[a], &x1 = mx[a], &m2 = mn[b], &x2 = mx[b];
-        if ((m1.x <= x2.x) && (x1.x >= m2.x) && (m1.y <= x2.y) && (x1.y >= m2.y) && (m1.z <= x2.z) && (x1.z >= m2.z)) keep.push_back(c);
-    }
+    for (int64_t c = 0; c < n; c++)
+        if (!(fl[c] & C_REMOVED)) keep.push_back(c);
     return 0;
 }
 

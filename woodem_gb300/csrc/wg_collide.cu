@@ -58,6 +58,11 @@ struct CollideWork {
     uint64_t* pairs = nullptr;
     uint64_t* pairsSorted = nullptr;
     int64_t pairCap = 0;
+    int32_t* pairCd = nullptr;        // periodic: cell distance of each new pair
+    int32_t* pairCdSorted = nullptr;
+    int64_t pairCdCap = 0;
+    int32_t* newCd = nullptr;         // periodic: cell distance per merged contact
+    int64_t newCdCap = 0;
     unsigned long long* counter = nullptr;
     unsigned long long* hCounter = nullptr;
     // merge scratch
@@ -114,6 +119,10 @@ __global__ void k_aabb(DevNodes N, DevParticles P, const ScenePar* __restrict__ 
             mx = u + h;
         }
         N.lastPos[p] = make_double4_32a(pr.x, pr.y, pr.z, 0.);
+        if (N.lh) {
+            N.lh[p] = N.ph[p];
+            N.ll[p] = N.pl[p];
+        }
     } else if (sh == WG_SHAPE_WALL) {
         const int ax = P.aux[p].x;
         const double4_32a pr = N.posr[p];
@@ -122,6 +131,10 @@ __global__ void k_aabb(DevNodes N, DevParticles P, const ScenePar* __restrict__ 
         setComp(mn, ax, comp(D3{pr.x, pr.y, pr.z}, ax));
         setComp(mx, ax, comp(D3{pr.x, pr.y, pr.z}, ax));
         N.lastPos[p] = make_double4_32a(pr.x, pr.y, pr.z, 0.);
+        if (N.lh) {
+            N.lh[p] = N.ph[p];
+            N.ll[p] = N.pl[p];
+        }
     } else {
         const int4 fn = P.aux[p];
         const double ht = P.facet[p].w;
@@ -144,8 +157,16 @@ __global__ void k_aabb(DevNodes N, DevParticles P, const ScenePar* __restrict__ 
                 mx = D3{smax(mx.x, b.x), smax(mx.y, b.y), smax(mx.z, b.z)};
             }
             N.lastPos[nn[k]] = make_double4_32a(pr.x, pr.y, pr.z, 0.);
+            if (N.lh) {
+                N.lh[nn[k]] = N.ph[nn[k]];
+                N.ll[nn[k]] = N.pl[nn[k]];
+            }
         }
         N.lastPos[p] = N.posr[p];
+        if (N.lh) {
+            N.lh[p] = N.ph[p];
+            N.ll[p] = N.pl[p];
+        }
     }
     if (sp.verletDist > 0) {
         const D3 vd{sp.verletDist, sp.verletDist, sp.verletDist};
@@ -240,10 +261,6 @@ __global__ void k_gather_sorted(DevParticles P, const int32_t* __restrict__ sid,
     smxf[i] = make_float4(__double2float_ru(b.x), __double2float_ru(b.y), __double2float_ru(b.z), __int_as_float(p));
 }
 
-// closed-interval 3-axis overlap, InsertionSortCollider::spatialOverlap :52-58
-__device__ __forceinline__ bool overlap3(const double4_32a& mn1, const double4_32a& mx1, const double4_32a& mn2, const double4_32a& mx2) {
-    return (mn1.x <= mx2.x) && (mx1.x >= mn2.x) && (mn1.y <= mx2.y) && (mx1.y >= mn2.y) && (mn1.z <= mx2.z) && (mx1.z >= mn2.z);
-}
 // Collider::mayCollide pkg/dem/Collision.cpp:19-41 for particles that share no nodes
 __device__ __forceinline__ bool maskOk(uint32_t a, uint32_t b, uint32_t lone) { return (a & b) != 0 && (a & b & lone) == 0; }
 
@@ -391,6 +408,132 @@ __global__ void k_pairs_local(DevParticles P, const int32_t* __restrict__ lids, 
     flushPairs(buf, nb, pairs, cap, counter);
 }
 
+// ---------------------------------------------------------------- periodic cell
+__global__ void k_cellkey_peri(DevParticles P, const int32_t* __restrict__ ids, int n, Grid G, const ScenePar* __restrict__ spp,
+                               uint32_t* __restrict__ key, int32_t* __restrict__ val) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const ScenePar& sp = *spp;
+    const int p = ids[i];
+    const double4_32a a = P.mn[p];
+    const double w[3] = {cellWrapRelD(a.x, 0., sp.cellSize[0]), cellWrapRelD(a.y, 0., sp.cellSize[1]),
+                         cellWrapRelD(a.z, 0., sp.cellSize[2])};
+    const int nn[3] = {G.nx, G.ny, G.nz};
+    int c[3];
+    for (int k = 0; k < 3; k++) {
+        const int ci = (int)floor(w[k] / (sp.cellSize[k] / nn[k]));
+        c[k] = ci < 0 ? 0 : (ci >= nn[k] ? nn[k] - 1 : ci);
+    }
+    key[i] = (uint32_t)(((int64_t)c[2] * G.ny + c[1]) * G.nx + c[0]);
+    val[i] = p;
+}
+// Pairs emitted with their cell distance (periods of the lo particle minus those of the hi one).
+__device__ __forceinline__ void flushPairsCd(uint64_t (&buf)[kPairBuf], int32_t (&cbuf)[kPairBuf], int& nb, uint64_t* pairs,
+                                             int32_t* cds, int64_t cap, unsigned long long* counter) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    int incl = nb;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += v;
+    }
+    const int total = __shfl_sync(FULL, incl, 31);
+    unsigned long long base = 0;
+    if (lane == 31 && total > 0) base = atomicAdd(counter, (unsigned long long)total);
+    base = __shfl_sync(FULL, base, 31);
+    const unsigned long long at = base + (unsigned long long)(incl - nb);
+#pragma unroll
+    for (int q = 0; q < kPairBuf; q++)
+        if (q < nb && (int64_t)(at + q) < cap) {
+            pairs[at + q] = buf[q];
+            cds[at + q] = cbuf[q];
+        }
+    nb = 0;
+}
+// Periodic sweep: particle i tests the spheres of higher id in the (up to 27, wrapped, distinct)
+// cells around its own with the periodic overlap test; each pair is met once, from its lo id.
+__global__ void k_pairs_ss_peri(const uint32_t* __restrict__ skey, const int32_t* __restrict__ sid, const double4_32a* __restrict__ smn,
+                                const double4_32a* __restrict__ smx, const uint32_t* __restrict__ smask, int n, Grid G,
+                                const int32_t* __restrict__ off, uint32_t lone, const ScenePar* __restrict__ spp,
+                                uint64_t* __restrict__ pairs, int32_t* __restrict__ cds, int64_t cap,
+                                unsigned long long* __restrict__ counter, int* __restrict__ dErr) {
+    const unsigned FULL = 0xffffffffu;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = i < n;
+    const ScenePar& sp = *spp;
+    int cx = 0, cy = 0, cz = 0, pi = 0;
+    uint32_t m1 = 0;
+    double4_32a mn1 = make_double4_32a(0., 0., 0., 0.), mx1 = mn1;
+    if (valid) {
+        const uint32_t k = skey[i];
+        cx = (int)(k % (uint32_t)G.nx);
+        cy = (int)((k / (uint32_t)G.nx) % (uint32_t)G.ny);
+        cz = (int)(k / ((uint32_t)G.nx * (uint32_t)G.ny));
+        pi = sid[i];
+        m1 = smask[i];
+        mn1 = smn[i];
+        mx1 = smx[i];
+    }
+    const int nx = G.nx, ny = G.ny, nz = G.nz;
+    // distinct wrapped offsets per axis
+    const int ox = nx >= 3 ? 3 : nx, oy = ny >= 3 ? 3 : ny, oz = nz >= 3 ? 3 : nz;
+    uint64_t buf[kPairBuf];
+    int32_t cbuf[kPairBuf];
+    int nb = 0;
+    for (int q = 0; q < ox * oy * oz; q++) {
+        const int dx = q % ox - (ox == 3 ? 1 : 0), dy = (q / ox) % oy - (oy == 3 ? 1 : 0), dz = q / (ox * oy) - (oz == 3 ? 1 : 0);
+        const int x = ((cx + dx) % nx + nx) % nx, y = ((cy + dy) % ny + ny) % ny, z = ((cz + dz) % nz + nz) % nz;
+        const int64_t cell = ((int64_t)z * ny + y) * nx + x;
+        const int beg = valid ? off[cell] : 0, end = valid ? off[cell + 1] : 0;
+        int j = beg;
+        for (;;) {
+            const bool has = j < end;
+            if (!__any_sync(FULL, has)) break;
+            if (has) {
+                const int pj = sid[j];
+                if (pj > pi && maskOk(m1, smask[j], lone)) {
+                    int per[3];
+                    const int r = overlapPeri(mn1, mx1, smn[j], smx[j], sp.cellSize, per);
+                    if (r < 0) atomicCAS(dErr, 0, 103);
+                    else if (r > 0) {
+                        buf[nb] = pairKey(pi, pj);
+                        cbuf[nb] = packCellDist(per[0], per[1], per[2]);
+                        nb++;
+                    }
+                }
+                j++;
+            }
+            if (__any_sync(FULL, nb == kPairBuf)) flushPairsCd(buf, cbuf, nb, pairs, cds, cap, counter);
+        }
+    }
+    flushPairsCd(buf, cbuf, nb, pairs, cds, cap, counter);
+}
+// Walls against every sphere with the periodic overlap test (pair oriented lo, hi).
+__global__ void k_pairs_global_peri(DevParticles P, const int32_t* __restrict__ gids, int ng, const int32_t* __restrict__ sph, int ns,
+                                    uint32_t lone, const ScenePar* __restrict__ spp, uint64_t* __restrict__ pairs,
+                                    int32_t* __restrict__ cds, int64_t cap, unsigned long long* __restrict__ counter,
+                                    int* __restrict__ dErr) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ns) return;
+    const int s = sph[i];
+    for (int g = 0; g < ng; g++) {
+        const int w = gids[g];
+        if (w == s || !maskOk(P.mask[s], P.mask[w], lone)) continue;
+        const int lo = s < w ? s : w, hi = s < w ? w : s;
+        int per[3];
+        const int r = overlapPeri(P.mn[lo], P.mx[lo], P.mn[hi], P.mx[hi], spp->cellSize, per);
+        if (r < 0) atomicCAS(dErr, 0, 103);
+        else if (r > 0) {
+            const unsigned long long idx = atomicAdd(counter, 1ull);
+            if ((int64_t)idx < cap) {
+                pairs[idx] = pairKey(lo, hi);
+                cds[idx] = packCellDist(per[0], per[1], per[2]);
+            }
+        }
+    }
+}
+
 // Walls (and any box too large for the grid) against every sphere.
 __global__ void k_pairs_global(DevParticles P, const int32_t* __restrict__ gids, int ng, const int32_t* __restrict__ sph, int ns,
                                uint32_t lone, uint64_t* __restrict__ pairs, int64_t cap, unsigned long long* __restrict__ counter) {
@@ -449,7 +592,7 @@ __global__ void k_compact_orphans(DevContacts C, const int32_t* __restrict__ orp
 }
 __global__ void k_place_new(const uint64_t* __restrict__ nk, int64_t nn, const uint64_t* __restrict__ okey, int64_t no,
                             const uint64_t* __restrict__ oldKey, int64_t nOld, uint64_t* __restrict__ outKey,
-                            int32_t* __restrict__ src) {
+                            int32_t* __restrict__ src, const int32_t* __restrict__ nkCd, int32_t* __restrict__ outCd) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nn) return;
     const uint64_t k = nk[i];
@@ -457,6 +600,7 @@ __global__ void k_place_new(const uint64_t* __restrict__ nk, int64_t nn, const u
     const int64_t pos = lowerBound64(oldKey, nOld, k);
     outKey[out] = k;
     src[out] = (pos < nOld && oldKey[pos] == k) ? (int32_t)pos : -1;
+    if (nkCd) outCd[out] = nkCd[i];
 }
 __global__ void k_place_orph(const uint64_t* __restrict__ nk, int64_t nn, const uint64_t* __restrict__ okey,
                              const int32_t* __restrict__ osrc, int64_t no, uint64_t* __restrict__ outKey, int32_t* __restrict__ src) {
@@ -470,10 +614,12 @@ __global__ void k_place_orph(const uint64_t* __restrict__ nk, int64_t nn, const 
 // carry persistent state of surviving contacts; new contacts get their functor type and orientation
 // (CGeomDispatcher functor order: Facet/Wall first, ContactLoop.cpp:145-152)
 __global__ void k_gather(DevContacts Cold, DevContacts Cnew, const int32_t* __restrict__ src, DevParticles P,
-                         const long long* __restrict__ dStep) {
+                         const long long* __restrict__ dStep, const int32_t* __restrict__ newCd) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= Cnew.n) return;
-    const int32_t s = src[i];
+    const int32_t s0 = src[i];
+    // a contact removed since the last full run comes back as a new one
+    const int32_t s = (s0 >= 0 && (Cold.flags[s0] & C_REMOVED)) ? -1 : s0;
     if (s >= 0) {
         Cnew.flags[i] = Cold.flags[s] & ~(C_PENDING | C_DORMANT);
         Cnew.step0[i] = Cold.step0[s];
@@ -500,7 +646,7 @@ __global__ void k_gather(DevContacts Cold, DevContacts Cnew, const int32_t* __re
         fl |= ty << 2;
         Cnew.flags[i] = fl;
         Cnew.step0[i] = (int32_t)(*dStep);
-        Cnew.cdist[i] = packCellDist(0, 0, 0);
+        Cnew.cdist[i] = newCd ? newCd[i] : packCellDist(0, 0, 0);
 #pragma unroll
         for (int q = 0; q < CC_NCOL; q++)
             if (Cnew.col[q]) Cnew.col[q][i] = 0.;
@@ -626,6 +772,9 @@ __global__ void k_slots(const uint64_t* __restrict__ key, const uint32_t* __rest
     if (activeContact(flags[k])) {
         const int loP = (int)(key[k] >> 32);
         I.slotLo[k] = I.hiStart[loP + 1] + act[k];
+        const uint32_t fl = flags[k];
+        const int hiP = (int)(key[k] & 0xffffffffu);
+        I.work[act[k]] = (fl & C_SWAP) ? make_int4((int)k, hiP, loP, (int)(fl & 0xeu)) : make_int4((int)k, loP, hiP, (int)(fl & 0xeu));
     } else {
         I.slotLo[k] = -1;
         I.slotHi[k] = -1;
@@ -633,8 +782,9 @@ __global__ void k_slots(const uint64_t* __restrict__ key, const uint32_t* __rest
 }
 
 // index of the first contact whose lo id is above every boundary particle
-__global__ void k_first_ss(const uint64_t* __restrict__ key, int64_t n, int firstId, int32_t* __restrict__ out) {
-    *out = (int32_t)lowerBound64(key, n, (uint64_t)(uint32_t)firstId << 32);
+__global__ void k_first_ss(const uint64_t* __restrict__ key, int64_t n, int firstId, const int32_t* __restrict__ act,
+                           int32_t* __restrict__ out) {
+    *out = act[lowerBound64(key, n, (uint64_t)(uint32_t)firstId << 32)];  // its active rank
 }
 
 // Particles summed by the block tree; the ones whose node has a free DOF are also summed before
@@ -715,6 +865,8 @@ int collide_full_run(Sim& S) {
     }
     CollideWork& W = *S.cw;
     const uint32_t lone = S.cfg.lone_mask;
+    if (S.cfg.periodic && S.hPar.hasShear && !W.hGlobal.empty())
+        return S.fail(WG_ERR_UNSUPPORTED, "Walls not supported in skewed (Scene.cell.trsf is not diagonal) periodic boundary conditions.");
     // 1. boxes
     if (S.nPar > 0) k_aabb<<<(unsigned)((S.nPar + BS - 1) / BS), BS, 0, st>>>(S.N, S.P, S.dPar, S.dFlags + 1);
     // lastPos for node slots not owned by a particle box computation (dummy slots) stays stale:
@@ -742,11 +894,21 @@ int collide_full_run(Sim& S) {
         double h = v[6] * (1 + 1e-9) + 1e-300;
         double ext[3] = {v[3] - v[0], v[4] - v[1], v[5] - v[2]};
         int64_t dims[3];
-        for (;;) {
-            for (int q = 0; q < 3; q++) dims[q] = (int64_t)std::floor(ext[q] / h) + 1;
-            int64_t nc = dims[0] * dims[1] * dims[2];
-            if (nc <= std::max<int64_t>(8 * (int64_t)ns, 1 << 16) && nc < (int64_t(1) << 31)) break;
-            h *= 1.25;
+        if (S.cfg.periodic) {
+            // the periodic cell [0, size) per axis (unsheared coordinates) in whole cells no narrower than h
+            for (;;) {
+                for (int q = 0; q < 3; q++) dims[q] = std::max<int64_t>(1, (int64_t)std::floor(S.hPar.cellSize[q] / h));
+                int64_t nc = dims[0] * dims[1] * dims[2];
+                if (nc <= std::max<int64_t>(8 * (int64_t)ns, 1 << 16) && nc < (int64_t(1) << 31)) break;
+                h *= 1.25;
+            }
+        } else {
+            for (;;) {
+                for (int q = 0; q < 3; q++) dims[q] = (int64_t)std::floor(ext[q] / h) + 1;
+                int64_t nc = dims[0] * dims[1] * dims[2];
+                if (nc <= std::max<int64_t>(8 * (int64_t)ns, 1 << 16) && nc < (int64_t(1) << 31)) break;
+                h *= 1.25;
+            }
         }
         G.ox = v[0]; G.oy = v[1]; G.oz = v[2]; G.h = h;
         G.nx = (int32_t)dims[0]; G.ny = (int32_t)dims[1]; G.nz = (int32_t)dims[2];
@@ -765,7 +927,8 @@ int collide_full_run(Sim& S) {
             if (!W.smask || !W.smxf) return S.fail(WG_ERR_CUDA, "out of device memory (grid)");
         }
         W.cellOff = grow(S, W.cellOff, W.cellOffCap, G.ncell + 1);
-        k_cellkey<<<(ns + BS - 1) / BS, BS, 0, st>>>(S.P, W.sphereIds, ns, G, W.cellKey, W.cellVal);
+        if (S.cfg.periodic) k_cellkey_peri<<<(ns + BS - 1) / BS, BS, 0, st>>>(S.P, W.sphereIds, ns, G, S.dPar, W.cellKey, W.cellVal);
+        else k_cellkey<<<(ns + BS - 1) / BS, BS, 0, st>>>(S.P, W.sphereIds, ns, G, W.cellKey, W.cellVal);
         int endBit = 1;
         while ((int64_t(1) << endBit) < G.ncell) endBit++;
         size_t tb = 0;
@@ -808,10 +971,24 @@ int collide_full_run(Sim& S) {
         int64_t cap2 = 0;
         W.pairsSorted = grow(S, W.pairsSorted, cap2, W.pairCap);
     }
+    const bool peri = S.cfg.periodic != 0;
     int64_t nNew = 0;
     for (int attempt = 0; attempt < 3; attempt++) {
         WG_CUDA_TRY(cudaMemsetAsync(W.counter, 0, sizeof(unsigned long long), st));
-        if (ns > 0) {
+        if (peri) {
+            if (W.pairCdCap < W.pairCap) {
+                int64_t c2 = W.pairCdCap;
+                W.pairCd = grow(S, W.pairCd, W.pairCdCap, W.pairCap);
+                W.pairCdSorted = grow(S, W.pairCdSorted, c2, W.pairCap);
+                if (!W.pairCd || !W.pairCdSorted) return S.fail(WG_ERR_CUDA, "out of device memory (pairs)");
+            }
+            if (ns > 0)
+                k_pairs_ss_peri<<<(ns + BS - 1) / BS, BS, 0, st>>>(W.cellKeySorted, W.sid, W.smn, W.smx, W.smask, ns, G, W.cellOff, lone,
+                                                                 S.dPar, W.pairs, W.pairCd, W.pairCap, W.counter, S.dFlags + FL_ERR);
+            if (ns > 0 && W.nGlobal > 0)
+                k_pairs_global_peri<<<(ns + BS - 1) / BS, BS, 0, st>>>(S.P, W.globalIds, W.nGlobal, W.sphereIds, ns, lone, S.dPar,
+                                                                     W.pairs, W.pairCd, W.pairCap, W.counter, S.dFlags + FL_ERR);
+        } else if (ns > 0) {
             k_pairs_ss<<<(ns + BS - 1) / BS, BS, 0, st>>>(W.cellKeySorted, W.smn, W.smx, W.smnf, W.smxf, ns, G, W.cellOff, lone,
                                                         W.pairs, W.pairCap, W.counter);
             if (W.nLarge > 0)
@@ -821,7 +998,7 @@ int collide_full_run(Sim& S) {
                 k_pairs_global<<<(ns + BS - 1) / BS, BS, 0, st>>>(S.P, W.globalIds, W.nGlobal, W.sphereIds, ns, lone, W.pairs,
                                                                 W.pairCap, W.counter);
         }
-        if (W.largeLargePossible) {
+        if (W.largeLargePossible && !peri) {
             // all non-spheres against each other
             int nn = W.nLarge + W.nGlobal;
             std::vector<int32_t> all;
@@ -846,7 +1023,14 @@ int collide_full_run(Sim& S) {
     // sort new pair keys
     int idBits = 1;
     while ((int64_t(1) << idBits) < S.nPar) idBits++;
-    if (nNew > 0) {
+    if (nNew > 0 && peri) {
+        size_t tb = 0;
+        cub::DeviceRadixSort::SortPairs(nullptr, tb, W.pairs, W.pairsSorted, W.pairCd, W.pairCdSorted, nNew, 0, 32 + idBits, st);
+        if (ensureCub(S, tb)) return WG_ERR_CUDA;
+        tb = W.cubBytes;
+        WG_CUDA_TRY(cub::DeviceRadixSort::SortPairs(W.cubTmp, tb, W.pairs, W.pairsSorted, W.pairCd, W.pairCdSorted, nNew, 0,
+                                                    32 + idBits, st));
+    } else if (nNew > 0) {
         size_t tb = 0;
         cub::DeviceRadixSort::SortKeys(nullptr, tb, W.pairs, W.pairsSorted, nNew, 0, 32 + idBits, st);
         if (ensureCub(S, tb)) return WG_ERR_CUDA;
@@ -895,13 +1079,17 @@ int collide_full_run(Sim& S) {
     W.src = grow(S, W.src, W.srcCap, std::max<int64_t>(nOut, 1));
     if (!W.src) return S.fail(WG_ERR_CUDA, "out of device memory (merge)");
     S.Cb.n = nOut;
+    if (peri) {
+        W.newCd = grow(S, W.newCd, W.newCdCap, std::max<int64_t>(nOut, 1));
+        if (!W.newCd) return S.fail(WG_ERR_CUDA, "out of device memory (merge)");
+    }
     if (nNew > 0)
         k_place_new<<<(unsigned)((nNew + BS - 1) / BS), BS, 0, st>>>(W.pairsSorted, nNew, W.orphKey, nOrph, S.C.key, nOld, S.Cb.key,
-                                                                    W.src);
+                                                                    W.src, peri ? W.pairCdSorted : nullptr, W.newCd);
     if (nOrph > 0)
         k_place_orph<<<(unsigned)((nOrph + BS - 1) / BS), BS, 0, st>>>(W.pairsSorted, nNew, W.orphKey, W.orphSrc, nOrph, S.Cb.key,
                                                                       W.src);
-    if (nOut > 0) k_gather<<<(unsigned)((nOut + BS - 1) / BS), BS, 0, st>>>(S.C, S.Cb, W.src, S.P, S.dStep);
+    if (nOut > 0) k_gather<<<(unsigned)((nOut + BS - 1) / BS), BS, 0, st>>>(S.C, S.Cb, W.src, S.P, S.dStep, peri ? W.newCd : nullptr);
     std::swap(S.C, S.Cb);
     if (nOut > 0 && !S.cfg.periodic)
         k_dormant<<<(unsigned)((nOut + BS - 1) / BS), BS, 0, st>>>(S.C, S.N, S.P, S.dPar);
@@ -910,7 +1098,7 @@ int collide_full_run(Sim& S) {
     if (W.hiCap < std::max<int64_t>(n, 1)) {
         if (W.hiKeys) {
             S.dfree(W.hiKeys); S.dfree(W.hiKeysSorted); S.dfree(W.hiVals); S.dfree(S.I.hiList);
-            S.dfree(S.I.slotLo); S.dfree(S.I.slotHi); S.dfree(W.act);
+            S.dfree(S.I.slotLo); S.dfree(S.I.slotHi); S.dfree(W.act); S.dfree(S.I.work);
         }
         W.hiCap = std::max<int64_t>(n, 1) * 3 / 2 + 1024;
         W.hiKeys = (uint32_t*)S.dalloc(sizeof(uint32_t) * W.hiCap);
@@ -920,7 +1108,8 @@ int collide_full_run(Sim& S) {
         S.I.slotLo = (int32_t*)S.dalloc(sizeof(int32_t) * W.hiCap);
         S.I.slotHi = (int32_t*)S.dalloc(sizeof(int32_t) * W.hiCap);
         W.act = (int32_t*)S.dalloc(sizeof(int32_t) * (W.hiCap + 1));
-        if (!S.I.slotHi || !W.act) return S.fail(WG_ERR_CUDA, "out of device memory (incidence)");
+        S.I.work = (int4*)S.dalloc(sizeof(int4) * W.hiCap);
+        if (!S.I.slotHi || !W.act || !S.I.work) return S.fail(WG_ERR_CUDA, "out of device memory (incidence)");
     }
     int64_t nAct = 0;
     {
@@ -966,7 +1155,7 @@ int collide_full_run(Sim& S) {
     }
     k_hi_start<<<(unsigned)((S.nPar + 1 + BS - 1) / BS), BS, 0, st>>>(W.hiKeysSorted, n, (int)S.nPar, S.I.hiStart);
     if (n > 0) k_slots<<<(unsigned)((n + BS - 1) / BS), BS, 0, st>>>(S.C.key, S.C.flags, n, nAct, W.act, S.I);
-    S.nActive = nAct;
+    S.I.nAct = nAct;
     // every end starts without a contribution; the contact kernel fills the real ones this step
     const int64_t ne = 2 * std::max<int64_t>(nAct, 1);
     if (S.prec == WG_PREC_FP32) {
@@ -984,7 +1173,7 @@ int collide_full_run(Sim& S) {
     WG_CUDA_TRY(cudaMemsetAsync(W.heavyCount, 0, sizeof(int32_t) * 3, st));
     k_heavy<<<(unsigned)((S.nPar + BS - 1) / BS), BS, 0, st>>>(S.I, S.P, S.N.flags, kHeavyThreshold, W.heavyCount);
     // contacts whose lo id is above every boundary particle join two spheres
-    if (S.maxBoundaryId >= 0) k_first_ss<<<1, 1, 0, st>>>(S.C.key, n, S.maxBoundaryId + 1, W.heavyCount + 2);
+    if (S.maxBoundaryId >= 0) k_first_ss<<<1, 1, 0, st>>>(S.C.key, n, S.maxBoundaryId + 1, W.act, W.heavyCount + 2);
     WG_CUDA_TRY(cudaMemcpyAsync(W.hHeavy, W.heavyCount, sizeof(int32_t) * 3, cudaMemcpyDeviceToHost, st));
     WG_CUDA_TRY(cudaStreamSynchronize(st));
     S.nMixed = W.hHeavy[2];

@@ -13,6 +13,58 @@ struct Geo {
     double uN, r1, r2;
 };
 
+// closed-interval 3-axis overlap, InsertionSortCollider::spatialOverlap :52-58
+__device__ __forceinline__ bool overlap3(const double4_32a& mn1, const double4_32a& mx1, const double4_32a& mn2, const double4_32a& mx2) {
+    return (mn1.x <= mx2.x) && (mx1.x >= mn2.x) && (mn1.y <= mx2.y) && (mx1.y >= mn2.y) && (mn1.z <= mx2.z) && (mx1.z >= mn2.z);
+}
+// cellWrap / cellWrapRel, pkg/dem/InsertionSortCollider.cpp:650-660
+// (rounded intrinsics: no contraction in the translation units compiled with --fmad=true)
+__device__ __forceinline__ double cellWrapD(double x, double x0, double x1, int& period) {
+    const double xNorm = __ddiv_rn(__dsub_rn(x, x0), __dsub_rn(x1, x0));
+    period = (int)floor(xNorm);
+    return __dadd_rn(x0, __dmul_rn(__dsub_rn(xNorm, (double)period), __dsub_rn(x1, x0)));
+}
+__device__ __forceinline__ double cellWrapRelD(double x, double x0, double x1) {
+    const double xNorm = __ddiv_rn(__dsub_rn(x, x0), __dsub_rn(x1, x0));
+    return __dmul_rn(__dsub_rn(xNorm, floor(xNorm)), __dsub_rn(x1, x0));
+}
+// InsertionSortCollider::spatialOverlapPeri, pkg/dem/InsertionSortCollider.cpp:903-957, for the
+// pair (id1, id2); periods[] = pmn1 - pmn2 per axis. Returns 1 on overlap, 0 without, -1 when a
+// box spans more than one period ("Particle larger than half of the cell size").
+__device__ __forceinline__ int overlapPeri(const double4_32a& mn1, const double4_32a& mx1, const double4_32a& mn2,
+                                          const double4_32a& mx2, const double* size, int periods[3]) {
+    const double m1a[3] = {mn1.x, mn1.y, mn1.z}, x1a[3] = {mx1.x, mx1.y, mx1.z};
+    const double m2a[3] = {mn2.x, mn2.y, mn2.z}, x2a[3] = {mx2.x, mx2.y, mx2.z};
+    int res = 1;
+    for (int axis = 0; axis < 3; axis++) {
+        const double dim = size[axis];
+        const double m1 = m1a[axis], m2 = m2a[axis];
+        if (isinf(m1) || isinf(m2)) {
+            periods[axis] = 0;
+            continue;
+        }
+        const double wMn = (cellWrapRelD(m1, m2, m2 + dim) < cellWrapRelD(m2, m1, m1 + dim)) ? m2 : m1;
+        int pmn1, pmx1, pmn2, pmx2;
+        const double a1 = cellWrapD(m1, wMn, wMn + dim, pmn1), b1 = cellWrapD(x1a[axis], wMn, wMn + dim, pmx1);
+        const double a2 = cellWrapD(m2, wMn, wMn + dim, pmn2), b2 = cellWrapD(x2a[axis], wMn, wMn + dim, pmx2);
+        if ((pmn1 != pmx1) || (pmn2 != pmx2)) return -1;
+        periods[axis] = pmn1 - pmn2;
+        if (!(a1 <= b2 && b1 >= a2)) res = 0;
+    }
+    return res;
+}
+// ContactContainer::removePending (pkg/dem/ContactContainer.hpp:78-93 with
+// InsertionSortCollider::shouldBeRemoved, InsertionSortCollider.hpp:209-214): a contact that the
+// law removed in the last step leaves the container at the next collider run unless the boxes of
+// its particles (those of the last full run) still overlap.
+__device__ __forceinline__ bool pendingStays(const DevParticles& P, int A, int B, bool periodic, const double* cellSize, int* dErr) {
+    const int lo = A < B ? A : B, hi = A < B ? B : A;
+    if (!periodic) return overlap3(P.mn[lo], P.mx[lo], P.mn[hi], P.mx[hi]);
+    int per[3];
+    const int r = overlapPeri(P.mn[lo], P.mx[lo], P.mn[hi], P.mx[hi], cellSize, per);
+    if (r < 0) atomicCAS(dErr, 0, 103);
+    return r > 0;
+}
 // Cg2_Sphere_Sphere_L6Geom::go, pkg/dem/Sphere.cpp:88-109
 __device__ __forceinline__ bool geomSS(const DevNodes& N, int A, int B, D3 shift2, bool real, double ssDf, Geo& g) {
     const double4_32a pa = N.posr[A], pb = N.posr[B];

@@ -19,7 +19,8 @@ enum : uint32_t {
     C_REAL = 1u,     // geom && phys exist
     C_SWAP = 2u,     // pA is the hi id (functor order Facet/Wall first)
     C_PENDING = 16u, // law requested removal in the last ContactLoop
-    C_DORMANT = 32u  // not real and too far apart to touch before the next full collider run
+    C_DORMANT = 32u, // not real and too far apart to touch before the next full collider run
+    C_REMOVED = 64u  // pending contact whose boxes no longer overlapped at the next collider run
 };
 enum { CT_SS = 0, CT_FS = 1, CT_WS = 2, CT_NONE = 3 };
 __host__ __device__ inline uint32_t ctype(uint32_t fl) { return (fl >> 2) & 3u; }
@@ -68,6 +69,7 @@ struct DevNodes {
     float* wz;
     float4* orif;   // FP32-force mode: the orientation (w x y z), in place of ori
     float2* rsplit; // FP32-force mode: the radius as a double-float pair (constant)
+    float4 *lh, *ll; // FP32-force mode: the position mirror at the last full run (verlet reference)
 };
 struct DevParticles {
     int32_t n;
@@ -114,6 +116,8 @@ struct DevIncidence {
     int32_t* loStart;  // nPar+1: contacts with lo==p are [loStart[p], loStart[p+1])
     int32_t* hiStart;  // nPar+1: hiList[hiStart[p] .. hiStart[p+1]) are contacts with hi==p, ascending
     int32_t* hiList;
+    int4* work;        // active contacts in ascending index order: (contact, pA, pB, type|swap flag bits)
+    int64_t nAct;
     int32_t* slotLo;   // per contact: end slot of its lo particle (-1: no slot, the contact is inactive)
     int32_t* slotHi;   // per contact: end slot of its hi particle
     double4_32a* endA; // FP64 mode: (Fx, Fy, Fz, Tx) on the particle, torque about its node
@@ -166,11 +170,16 @@ void launch_contact_fp64(cudaStream_t st, const DevNodes& N, const DevParticles&
 void launch_forces(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const ScenePar* sp,
                    const int* dFlags, bool perStep);
 void launch_advance(cudaStream_t st, long long* dStep, const int* dFlags);
+// sum over real contacts of F_A (x) branch into out[9] (not divided by the volume); scratch holds
+// 9 doubles per 256 active contacts; returns -1 when it is too small
+int launch_stress(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C, const DevIncidence& I,
+                  const ScenePar* sp, double* scratch, int64_t scratchDoubles, double* out);
 // FP32-force mode (wg_step32.cu)
 void launch_leapfrog32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const NodeConst32* nc,
                        const ScenePar* sp, int* dFlags, int fromEnds);
-// Contacts [0, nMixed) may be of any type; [nMixed, C.n) join two spheres (both ids above every
-// boundary particle) and, in an aperiodic scene, go to a sphere-sphere-only kernel.
+// The kernels walk the active contacts I.work[0, I.nAct). Ranks [0, nMixed) may be of any type;
+// [nMixed, I.nAct) join two spheres (both ids above every boundary particle) and, in an aperiodic
+// scene, go to a sphere-sphere-only kernel.
 // With a side stream the mixed range runs beside the sphere-sphere range (joined on st).
 struct SideStream {
     cudaStream_t st = nullptr;
@@ -224,8 +233,7 @@ struct Sim {
     DevContacts C{}, Cb{};  // current and spare (merge target)
     DevIncidence I{};
     int64_t cCap = 0;
-    int64_t nMixed = 0;   // contacts [0, nMixed) may involve a boundary particle (see launch_contact_fp32)
-    int64_t nActive = 0;  // contacts with end slots (a functor applies and the pair is not dormant)
+    int64_t nMixed = 0;   // active ranks [0, nMixed) may involve a boundary particle (see launch_contact_fp32)
     int32_t maxBoundaryId = -1;  // largest id of a non-sphere particle
     double4_32a* dMats = nullptr;
     NodeConst32* dNodeC = nullptr;  // per node slot (FP32-force mode)
@@ -242,6 +250,9 @@ struct Sim {
     double time = 0;
     int64_t nFullRuns = 0;
     bool fromEnds = false;   // the end slots hold the forces of the last contact loop
+    double* dStress = nullptr;       // 9 doubles + per-block partials
+    int64_t stressCap = 0;
+    double stress[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // ContactLoop.stress of the last step
     // timing
     std::vector<cudaEvent_t> evPool;  // per queued step: before Leapfrog, before contacts, after
     cudaEvent_t ev[8];

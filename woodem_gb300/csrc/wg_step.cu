@@ -185,16 +185,21 @@ __global__ void __launch_bounds__(128) k_contact_fp64(DevNodes N, DevParticles P
         return;
     }
     int* dErr = dFlags + FL_ERR;
-    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= C.n) return;
+    const int64_t rk = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (rk >= I.nAct) return;
+    // work item: contact index, pA, pB and the static flag bits (type, swap) fixed at the full run
+    const int4 wk = I.work[rk];
+    const int64_t c = wk.x;
+    const int A = wk.y, B = wk.z;
     const ScenePar& sp = *spp;
     uint32_t fl = C.flags[c];
-    const uint32_t ty = ctype(fl);
-    if (ty == CT_NONE || (fl & C_DORMANT)) return;
+    if (fl & C_REMOVED) return;
+    if ((fl & C_PENDING) && !pendingStays(P, A, B, sp.periodic, sp.cellSize, dErr)) {
+        C.flags[c] = (fl & ~C_PENDING) | C_REMOVED;
+        return;
+    }
     fl &= ~C_PENDING;
-    const uint64_t key = C.key[c];
-    const int lo = (int)(key >> 32), hi = (int)(key & 0xffffffffu);
-    const int A = (fl & C_SWAP) ? hi : lo, B = (fl & C_SWAP) ? lo : hi;
+    const uint32_t ty = ctype((uint32_t)wk.w);
     const bool real = fl & C_REAL;
     const long long step = *dStep;
     const double dt = sp.dt;
@@ -417,7 +422,7 @@ void launch_contact_fp64(cudaStream_t st, const DevNodes& N, const DevParticles&
                          const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dFlags) {
     const int bs = 128;
     // launched even without contacts: it raises FL_HALT when a full run is due
-    k_contact_fp64<<<(unsigned)std::max<int64_t>(1, (C.n + bs - 1) / bs), bs, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags);
+    k_contact_fp64<<<(unsigned)std::max<int64_t>(1, (I.nAct + bs - 1) / bs), bs, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags);
 }
 
 // ---------------------------------------------------------------------------------- force sum
@@ -482,6 +487,61 @@ __global__ void k_forces_heavy(DevNodes N, DevIncidence I, const int32_t* __rest
         N.force[p] = st4(G + D3{sh[0][0], sh[1][0], sh[2][0]}, 0.);
         N.torque[p] = st4(D3{sh[3][0], sh[4][0], sh[5][0]}, 0.);
     }
+}
+
+// ContactLoop.stress for periodic scenes (ContactLoop.cpp:211-247): sum over real contacts of
+// F_A (x) (x_B + shift - x_A), divided by the cell volume on the host. Per-block partial sums in a
+// fixed tree, then one block adds the partials in block order.
+__global__ void k_stress_partial(DevNodes N, DevParticles P, DevContacts C, DevIncidence I, const ScenePar* __restrict__ spp,
+                                 double* __restrict__ partial) {
+    __shared__ double sh[9][256];
+    const int64_t rk = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    if (rk < I.nAct) {
+        const int4 wk = I.work[rk];
+        const int64_t c = wk.x;
+        const uint32_t fl = C.flags[c];
+        if (fl & C_REAL) {
+            const int A = wk.y, B = wk.z;
+            const bool aIsLo = !(fl & C_SWAP);
+            const int sA = aIsLo ? I.slotLo[c] : I.slotHi[c];
+            D3 F;
+            if (I.endA) F = D3{I.endA[sA].x, I.endA[sA].y, I.endA[sA].z};
+            else F = D3{(double)I.endAf[sA].x, (double)I.endAf[sA].y, (double)I.endAf[sA].z};
+            const int nA = (P.shape[A] == WG_SHAPE_FACET) ? P.aux[A].x : A;
+            D3 branch = D3{N.posr[B].x, N.posr[B].y, N.posr[B].z} - D3{N.posr[nA].x, N.posr[nA].y, N.posr[nA].z};
+            int a, b, cc;
+            unpackCellDist(C.cdist[c], a, b, cc);
+            if (fl & C_SWAP) { a = -a; b = -b; cc = -cc; }
+            if (a != 0 || b != 0 || cc != 0) branch = branch + mul(ldm(spp->hSize), D3{(double)a, (double)b, (double)cc});
+            const double Fa[3] = {F.x, F.y, F.z}, Ba[3] = {branch.x, branch.y, branch.z};
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++) v[3 * i + j] = Fa[i] * Ba[j];
+        }
+    }
+    for (int q = 0; q < 9; q++) sh[q][threadIdx.x] = v[q];
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s)
+            for (int q = 0; q < 9; q++) sh[q][threadIdx.x] = sh[q][threadIdx.x] + sh[q][threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int q = 0; q < 9; q++) partial[9 * blockIdx.x + q] = sh[q][0];
+}
+__global__ void k_stress_final(const double* __restrict__ partial, int nb, double* __restrict__ out) {
+    if (threadIdx.x >= 9) return;
+    double acc = 0;
+    for (int b = 0; b < nb; b++) acc = acc + partial[9 * b + threadIdx.x];
+    out[threadIdx.x] = acc;
+}
+int launch_stress(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C, const DevIncidence& I,
+                  const ScenePar* sp, double* scratch, int64_t scratchDoubles, double* out) {
+    const int64_t nb = std::max<int64_t>(1, (I.nAct + 255) / 256);
+    if (9 * nb > scratchDoubles) return -1;
+    k_stress_partial<<<(unsigned)nb, 256, 0, st>>>(N, P, C, I, sp, scratch);
+    k_stress_final<<<1, 32, 0, st>>>(scratch, (int)nb, out);
+    return 0;
 }
 
 // Scene::doOneStep's step counter (core/Scene.cpp:386), advanced only by a step that completed.

@@ -28,10 +28,46 @@ __device__ __forceinline__ F3 operator*(F3 a, float s) { return F3{a.x * s, a.y 
 __device__ __forceinline__ F3 operator*(float s, F3 a) { return F3{s * a.x, s * a.y, s * a.z}; }
 __device__ __forceinline__ float fdot(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 __device__ __forceinline__ F3 fcross(F3 a, F3 b) { return F3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
-// x = h + l with h = fl32(x) and l = fl32(x - h); |x - (h + l)| <= 2^-48 |x| (x - h is exact in FP64)
+// x = h + l from the bits of x with integer operations only (FP64 arithmetic and conversions
+// issue at 1/64 of the FP32 rate on GB300): h is x truncated to 24 significant bits, l the
+// remaining 29 mantissa bits truncated to 24, so |x - (h + l)| < 2^-47 |x|. Zero, |x| < 2^-74
+// and |x| >= 2^127 take the FP64 route (h = fl32(x), l = fl32(x - h)).
 __device__ __forceinline__ void splitDF(double x, float& h, float& l) {
-    h = __double2float_rn(x);
-    l = __double2float_rn(x - (double)h);
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned top = (unsigned)(b >> 32);
+    const unsigned sign = top & 0x80000000u;
+    const int e = (int)((top >> 20) & 0x7ffu);
+    if (e < 949 || e > 1150) {
+        h = __double2float_rn(x);
+        l = __double2float_rn(x - (double)h);
+        return;
+    }
+    const unsigned long long m = b & 0x000FFFFFFFFFFFFFull;
+    h = __uint_as_float(sign | ((unsigned)(e - 896) << 23) | (unsigned)(m >> 29));
+    const unsigned r = (unsigned)(m & 0x1FFFFFFFull);
+    if (r == 0) {
+        l = 0.f;
+        return;
+    }
+    const int p = 31 - __clz((int)r);  // r = 1.f * 2^p, 0 <= p <= 28
+    const unsigned frac = (p >= 23) ? (r >> (p - 23)) : (r << (23 - p));
+    l = __uint_as_float(sign | ((unsigned)(p + e - 948) << 23) | (frac & 0x7FFFFFu));
+}
+// (double)f from the bits of f with integer operations (exact for normal numbers; FP32 subnormals,
+// below 1.2e-38, become zero; infinities and NaN take the FP64 route).
+__device__ __forceinline__ double f2d(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xffu;
+    const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+    if (e == 0) return __longlong_as_double((long long)sign);
+    if (e == 0xffu) return (double)f;
+    return __longlong_as_double((long long)(sign | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29)));
+}
+// x rounded toward zero to FP32 (the h of splitDF)
+__device__ __forceinline__ float truncF(double x) {
+    float h, l;
+    splitDF(x, h, l);
+    return h;
 }
 __device__ __forceinline__ F3 fnormalized(F3 a) {
     const float z = fdot(a, a);
@@ -56,13 +92,15 @@ __global__ void __launch_bounds__(256) k_leapfrog32(DevNodes N, DevParticles P, 
     const bool valid = i < N.n;
     const ScenePar& sp = *spp;
     NodeConst32 nc{0.f, {0.f, 0.f, 0.f}, 0.f, 0.f, 0u, 0u};
-    double4_32a pr = make_double4_32a(0., 0., 0., 0.), v4 = pr, w4 = pr, lp4 = pr;
+    double4_32a pr = make_double4_32a(0., 0., 0., 0.), v4 = pr, w4 = pr;
+    float4 lh = make_float4(0.f, 0.f, 0.f, 0.f), ll = lh;
     if (valid) {
         nc = ncs[i];
         pr = N.posr[i];
         v4 = N.vel[i];
         w4 = N.angv[i];
-        lp4 = N.lastPos[i];
+        lh = N.lh[i];
+        ll = N.ll[i];
     }
     const uint32_t flags = nc.flags;
     // DemData.force/torque of this step
@@ -91,7 +129,7 @@ __global__ void __launch_bounds__(256) k_leapfrog32(DevNodes N, DevParticles P, 
     }
     const double dt = sp.dt;
     const float dtf = sp.dtF;
-    const bool damp = (sp.damping != 0. && !(flags & F_DAMPING_SKIP));
+    const bool damp = (sp.dampingF != 0.f && !(flags & F_DAMPING_SKIP));
     D3 pos = ld3(pr);
     D3 vel = ld3(v4);
     D3 angVel = ld3(w4);
@@ -120,7 +158,7 @@ __global__ void __launch_bounds__(256) k_leapfrog32(DevNodes N, DevParticles P, 
             vel = mul(*(const DM3*)sp.ImLL4hInv, (mul(*(const DM3*)sp.LmL, pos) + mul(*(const DM3*)sp.IpLL4h, vel)) +
                                                    D3{(double)la.x, (double)la.y, (double)la.z} * dt);
         else
-            vel = vel + D3{(double)(dtf * la.x), (double)(dtf * la.y), (double)(dtf * la.z)};
+            vel = vel + D3{f2d(dtf * la.x), f2d(dtf * la.y), f2d(dtf * la.z)};
         if (nc.invI[0] != 0.f || nc.invI[1] != 0.f || nc.invI[2] != 0.f) {
             F3 aa{(flags & 8u) ? 0.f : t.x * nc.invI[0], (flags & 16u) ? 0.f : t.y * nc.invI[1], (flags & 32u) ? 0.f : t.z * nc.invI[2]};
             if (damp) {
@@ -129,7 +167,7 @@ __global__ void __launch_bounds__(256) k_leapfrog32(DevNodes N, DevParticles P, 
                 aa.y *= 1.f - d * fsgn(t.y * (pva.y + 0.5f * dtf * aa.y));
                 aa.z *= 1.f - d * fsgn(t.z * (pva.z + 0.5f * dtf * aa.z));
             }
-            angVel = angVel + D3{(double)(dtf * aa.x), (double)(dtf * aa.y), (double)(dtf * aa.z)};
+            angVel = angVel + D3{f2d(dtf * aa.x), f2d(dtf * aa.y), f2d(dtf * aa.z)};
             if (homoDeform == 4) angVel = angVel - D3{sp.deltaSpinVec[0], sp.deltaSpinVec[1], sp.deltaSpinVec[2]};
         }
     } else {
@@ -148,7 +186,7 @@ __global__ void __launch_bounds__(256) k_leapfrog32(DevNodes N, DevParticles P, 
     N.posr[i] = make_double4_32a(pos.x, pos.y, pos.z, pr.w);
     N.vel[i] = make_double4_32a(vel.x, vel.y, vel.z, 0.);
     N.angv[i] = make_double4_32a(angVel.x, angVel.y, angVel.z, 0.);
-    const F3 w = toF(angVel);
+    const F3 w{truncF(angVel.x), truncF(angVel.y), truncF(angVel.z)};
     {
         // double-float mirrors read by the sphere-sphere contact geometry
         const float2 rs = N.rsplit[i];
@@ -160,6 +198,10 @@ __global__ void __launch_bounds__(256) k_leapfrog32(DevNodes N, DevParticles P, 
         l.w = rs.y;
         N.ph[i] = h;
         N.pl[i] = l;
+        // verlet test (InsertionSortCollider.cpp:339-350): displacement since the last full run
+        // from the double-float mirrors, in FP32
+        const float dx = (h.x - lh.x) + (l.x - ll.x), dy = (h.y - lh.y) + (l.y - ll.y), dz = (h.z - lh.z) + (l.z - ll.z);
+        if (dx * dx + dy * dy + dz * dz > sp.maxD2F) atomicOr(dFlags + FL_FULL, 1);
         splitDF(vel.x, h.x, l.x);
         splitDF(vel.y, h.y, l.y);
         splitDF(vel.z, h.z, l.z);
@@ -192,9 +234,6 @@ __global__ void __launch_bounds__(256) k_leapfrog32(DevNodes N, DevParticles P, 
         N.force[i] = make_double4_32a(G.x, G.y, G.z, 0.);
         N.torque[i] = make_double4_32a(0., 0., 0., 0.);
     }
-    // verlet test (InsertionSortCollider.cpp:339-350) on the FP64 displacement rounded to FP32
-    const F3 dd = toF(ld3(lp4) - pos);
-    if (fdot(dd, dd) > sp.maxD2F) atomicOr(dFlags + FL_FULL, 1);
 }
 
 void launch_leapfrog32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const NodeConst32* nc,
@@ -313,7 +352,7 @@ __device__ __forceinline__ bool geomSS32(const DevNodes& N, int A, int B, float 
 // SSONLY: every contact of [c0, c1) joins two spheres of an aperiodic scene (no FP64 on the
 // evaluation path except contact creation).
 template <bool SSONLY>
-__global__ void __launch_bounds__(256) k_contact_fp32(DevNodes N, DevParticles P, DevContacts C, DevIncidence I,
+__global__ void __launch_bounds__(256, SSONLY ? 4 : 1) k_contact_fp32(DevNodes N, DevParticles P, DevContacts C, DevIncidence I,
                                                      const double4_32a* __restrict__ mats, const ScenePar* __restrict__ spp,
                                                      const long long* __restrict__ dStep, int* __restrict__ dFlags, int64_t c0,
                                                      int64_t c1, int haltBlock) {
@@ -322,16 +361,21 @@ __global__ void __launch_bounds__(256) k_contact_fp32(DevNodes N, DevParticles P
         return;
     }
     int* dErr = dFlags + FL_ERR;
-    const int64_t c = c0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= c1) return;
+    const int64_t rk = c0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (rk >= c1) return;
+    // work item: contact index, pA, pB and the static flag bits (type, swap) fixed at the full run
+    const int4 wk = I.work[rk];
+    const int64_t c = wk.x;
+    const int A = wk.y, B = wk.z;
     const ScenePar& sp = *spp;
     uint32_t fl = C.flags[c];
-    const uint32_t ty = ctype(fl);
-    if (ty == CT_NONE || (fl & C_DORMANT)) return;
+    if (fl & C_REMOVED) return;
+    if ((fl & C_PENDING) && !pendingStays(P, A, B, sp.periodic, sp.cellSize, dErr)) {
+        C.flags[c] = (fl & ~C_PENDING) | C_REMOVED;
+        return;
+    }
     fl &= ~C_PENDING;
-    const uint64_t key = C.key[c];
-    const int lo = (int)(key >> 32), hi = (int)(key & 0xffffffffu);
-    const int A = (fl & C_SWAP) ? hi : lo, B = (fl & C_SWAP) ? lo : hi;
+    const uint32_t ty = ctype((uint32_t)wk.w);
     const bool real = fl & C_REAL;
     const long long step = *dStep;
     const double dt = sp.dt;
@@ -566,15 +610,15 @@ __global__ void __launch_bounds__(256) k_contact_fp32(DevNodes N, DevParticles P
 void launch_contact_fp32(cudaStream_t st, const SideStream& side, const DevNodes& N, const DevParticles& P, const DevContacts& C,
                          const DevIncidence& I, const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dFlags,
                          int64_t nMixed, bool periodic) {
-    const int64_t nm = periodic ? C.n : std::min<int64_t>(nMixed, C.n);
-    const int64_t ns = C.n - nm;
+    const int64_t nm = periodic ? I.nAct : std::min<int64_t>(nMixed, I.nAct);
+    const int64_t ns = I.nAct - nm;
     if (ns > 0 && nm > 0 && side.st) {
         // the mixed range (facets and walls, FP64 geometry) beside the sphere-sphere range; the
         // sphere-sphere launch raises FL_HALT when a full run is due
         cudaEventRecord(side.fork, st);
         cudaStreamWaitEvent(side.st, side.fork, 0);
         k_contact_fp32<false><<<(unsigned)((nm + 255) / 256), 256, 0, side.st>>>(N, P, C, I, mats, sp, dStep, dFlags, 0, nm, 0);
-        k_contact_fp32<true><<<(unsigned)((ns + 255) / 256), 256, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags, nm, C.n, 1);
+        k_contact_fp32<true><<<(unsigned)((ns + 255) / 256), 256, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags, nm, I.nAct, 1);
         cudaEventRecord(side.join, side.st);
         cudaStreamWaitEvent(st, side.join, 0);
         return;
@@ -583,7 +627,7 @@ void launch_contact_fp32(cudaStream_t st, const SideStream& side, const DevNodes
     k_contact_fp32<false><<<(unsigned)std::max<int64_t>(1, (nm + 255) / 256), 256, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags,
                                                                                           0, nm, 1);
     if (ns > 0)
-        k_contact_fp32<true><<<(unsigned)((ns + 255) / 256), 256, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags, nm, C.n, 0);
+        k_contact_fp32<true><<<(unsigned)((ns + 255) / 256), 256, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags, nm, I.nAct, 0);
 }
 
 // ---------------------------------------------------------------------------------- force sum

@@ -212,3 +212,39 @@ def _sphere_nodes(S, col, value=None):
     if value is None:
         return nd.col(col)[nodes].copy()
     nd.col(col)[nodes] = value
+
+
+def periodic_shear(n=200_000, seed=0, rmin=2e-3, rmax=4e-3, density=2600.0, young=5e7, tanPhi=0.4, ktDivKn=0.2,
+                   fill_fraction=0.35, shear_rate=1.0, damping=0.2, verletRel=0.1, precision="fp64", compress_steps=0,
+                   compress_rate=None):
+    """Periodic simple shear: ``n`` spheres with radii uniform in [rmin, rmax] placed by seeded random
+    sequential insertion in a periodic cube sized to solid fraction ``fill_fraction``; IdealElPl
+    contacts, Leapfrog damping ``damping``, dt = 0.3*pWaveDt, verletDist = 0.1*rmin,
+    Cell.homoDeform = HomoGradV2. With ``compress_steps`` the cell is first compressed isotropically
+    (nextGradV = -compress_rate*I, by default the rate that brings the fill to 0.55 in that many
+    steps); then nextGradV is set to the simple shear with xz component ``shear_rate``."""
+    from .core import Cell
+    rng = np.random.default_rng(seed)
+    radii = rng.uniform(rmin, rmax, n)
+    vol = float(np.sum((4 / 3.0) * math.pi * radii ** 3))
+    side = (vol / fill_fraction) ** (1 / 3.0)
+    centers = pack_rsa(radii, (0, 0, 0), (side, side, side), region=2, seed=seed + 11)
+    S = Scene(fields=[DemField(gravity=(0, 0, 0))])
+    S.gpu.precision = precision
+    S.periodic = True
+    S.cell.setBox(side, side, side)
+    S.cell.homoDeform = Cell.HomoGradV2
+    mat = FrictMat(density=density, young=young, tanPhi=tanPhi, ktDivKn=ktDivKn)
+    S.dem.par.addSpheres(centers, radii, mat)
+    S.engines = utils.defaultEngines(damping=damping, verletDist=-verletRel, dynDtPeriod=0)
+    S.dt = 0.3 * utils.pWaveDt(S)
+    if compress_steps:
+        rate = compress_rate
+        if rate is None:
+            rate = math.log((0.55 / fill_fraction) ** (1 / 3.0)) / (compress_steps * S.dt)
+        S.cell.nextGradV = -rate * np.eye(3)
+        S.run(compress_steps)
+    g = np.zeros((3, 3))
+    g[0, 2] = shear_rate
+    S.cell.nextGradV = g
+    return S
