@@ -245,6 +245,54 @@ def traffic_per_launch(kern, R, P, nF, n):
     return d.get("per_real", 0.0) * R + d.get("per_potential", 0.0) * (P - R) + d.get("per_sphere", 0.0) * n
 
 
+def measure_batch(args):
+    """Parametric batch of independent box settles (sphere counts log-uniform in [1k, 50k], per-scene
+    radius, tanPhi, young, damping): scene-steps/s of the one-scene-at-a-time GPU path (each scene
+    its own simulation, run in turn) against the batch in one simulation, with the default launch
+    shape and with the autotuned one (CUDA-graph chunks among the candidates), both precisions."""
+    from woodem_gb300 import scenes, tune
+    from woodem_gb300.batch import Batch
+    K, W, T = args.batch_scenes, 20, args.batch_steps
+    out = {"scenes": K, "steps": T, "warmup": W, "scene_kind": "box settle (lattice, 6 walls, FrictPhys+IdealElPl)"}
+
+    def build(prec):
+        ss, tab = scenes.batch_study(n_scenes=K, seed=args.seed + 1, precision=prec)
+        out["spheres"] = int(tab["n"].sum())
+        return ss
+
+    # one scene at a time
+    ss = build("fp64")
+    tot_ms = 0.0
+    for S in ss:
+        S.run(W)
+        S.run(T)
+        tot_ms += S._sim.timing()[0]
+        S.close()
+    out["one_at_a_time_fp64"] = {"scene_steps_per_s": K * T / (tot_ms / 1e3), "ms": tot_ms}
+    log("batch: one at a time %.1f ms for %d scene-steps" % (tot_ms, K * T))
+    for prec in ("fp64", "fp32"):
+        for tuned in (False, True):
+            ss = build(prec)
+            B = Batch(ss)
+            B.run(W)
+            best = None
+            if tuned:
+                best, med = tune.autotune(B, trial_steps=16, rounds=1)
+            B.run(T)
+            ms = B.timing()[0]
+            key = "batched_%s_%s" % (prec, "tuned" if tuned else "default")
+            out[key] = {"scene_steps_per_s": K * T / (ms / 1e3), "ms": ms}
+            if best:
+                out[key]["launch"] = {"contact_block": best[0], "chunk_steps": best[1], "cuda_graph": bool(best[2])}
+            log("batch: %s %.1f ms" % (key, ms))
+            B.close()
+    base = out["one_at_a_time_fp64"]["scene_steps_per_s"]
+    out["speedup_fp64_tuned"] = out["batched_fp64_tuned"]["scene_steps_per_s"] / base
+    out["speedup_fp32_tuned"] = out["batched_fp32_tuned"]["scene_steps_per_s"] / base
+    out["jobs_per_s_fp32_tuned"] = out["batched_fp32_tuned"]["scene_steps_per_s"] / 10000.0
+    return out
+
+
 def peaks():
     try:
         with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
@@ -273,6 +321,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--batch-scenes", type=int, default=256)
+    ap.add_argument("--batch-steps", type=int, default=200)
+    ap.add_argument("--no-batch", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = env_rank()
@@ -372,6 +423,8 @@ def main():
         line["e2e"] = {"value": world * n_sph * e["steps"] / es, "unit": UNIT, "h2d_bytes_per_step": e["h2d"],
                        "d2h_bytes_per_step": e["d2h"], "steps": e["steps"],
                        "call": "wg_run_host(1 step) with page-locked host state"}
+    if rank == 0 and not args.no_batch:
+        line["batch"] = measure_batch(args)
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
         v, steps, n, el = cpu_sample(args, args.cpu_seconds, threads)

@@ -104,6 +104,20 @@ const char* wg_last_error(const wg_scene* s);
    nodes3: 3 node indices per particle (-1 unused); wall_axis/wall_sense: Wall.axis/sense;
    half_thick/fake_vel: Facet.halfThick/fakeVel; radius: Sphere.radius. */
 int wg_set_config(wg_scene* s, const wg_config* c);
+/* Batch of independent scenes in one simulation (no counterpart in the reference, where each
+   Scene is its own object; a batch runs many Scene.run loops at once). Scene k owns the particles
+   [particle_start[k], particle_start[k+1]) (and the nodes they use) and has its own configuration
+   cfgs[k] (dt, gravity, damping, verletDist, laws, Scene.step); particles of different scenes never
+   interact. All scenes share the precision mode, loneMask and applyForces; periodic scenes are not
+   batched. Replaces wg_set_config; call before the first run. */
+int wg_set_scenes(wg_scene* s, int32_t n_scenes, const wg_config* cfgs, const int64_t* particle_start);
+/* Launch shape (no counterpart in the reference): threads per block of the contact kernels
+   (0 = default, 64, 128, 256), steps queued per host check of the collider request (1..1024),
+   and use_graph != 0 to replay each such chunk of steps as one CUDA graph. Results do not depend
+   on these; only the speed does. */
+int wg_set_launch(wg_scene* s, int32_t contact_block, int32_t chunk_steps, int32_t use_graph);
+/* Scene.step, Scene.time and the contacts (counted by their lower particle id) of scene k. */
+int wg_get_scene_stats(wg_scene* s, int32_t k, wg_stats* out);
 int wg_set_materials(wg_scene* s, int32_t n, const double* density, const double* young,
                      const double* tan_phi, const double* kt_div_kn);
 int wg_set_nodes(wg_scene* s, int64_t n, const double* pos, const double* ori, const double* vel,

@@ -79,6 +79,9 @@ def lib():
         "wg_get_nodes": (C.c_int, [C.c_void_p, P_D, P_D, P_D, P_D, P_D, P_D]),
         "wg_get_stats": (C.c_int, [C.c_void_p, C.POINTER(wg_stats)]),
         "wg_set_next_gradv": (C.c_int, [C.c_void_p, P_D]),
+        "wg_set_scenes": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.POINTER(C.c_int64)]),
+        "wg_get_scene_stats": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+        "wg_set_launch": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
         "wg_get_cell": (C.c_int, [C.c_void_p, P_D, P_D, P_D]),
         "wg_num_contacts": (C.c_int64, [C.c_void_p]),
         "wg_get_contacts": (C.c_int, [C.c_void_p, P_I32, P_I32, P_I32, P_I32, P_I32, P_D, P_D, P_D, P_D]),

@@ -43,6 +43,7 @@ Sim::~Sim() {
     for (int i = 0; i < 8; i++)
         if (ev[i]) cudaEventDestroy(ev[i]);
     for (cudaEvent_t e : evPool) cudaEventDestroy(e);
+    if (graphExec) cudaGraphExecDestroy(graphExec);
     if (side.st) cudaStreamSynchronize(side.st);
     if (side.fork) cudaEventDestroy(side.fork);
     if (side.join) cudaEventDestroy(side.join);
@@ -259,10 +260,19 @@ int Sim::ensureContactCapacity(int64_t need) {
 }
 
 int Sim::prepareParams() {
+    if (nScenes <= 1) return prepareParamsFor(cfg, 0, nPar, hPar);
+    hPars.resize(nScenes);
+    for (int k = 0; k < nScenes; k++) prepareParamsFor(cfgs[k], sceneStart[k], sceneStart[k + 1], hPars[k]);
+    hPar = hPars[0];
+    return 0;
+}
+
+// ScenePar of one scene (configuration cfg, particles [p0, p1))
+int Sim::prepareParamsFor(const wg_config& cfg, int64_t p0, int64_t p1, ScenePar& p) {
     Sim& S = *this;
     SimEx& X = static_cast<SimEx&>(*this);
-    ScenePar& p = hPar;
     std::memset(&p, 0, sizeof(p));
+    p.stepBase = 0;
     p.dt = cfg.dt;
     for (int i = 0; i < 3; i++) p.g[i] = cfg.gravity[i];
     p.hasGravity = (cfg.gravity[0] != 0 || cfg.gravity[1] != 0 || cfg.gravity[2] != 0);
@@ -307,7 +317,7 @@ int Sim::prepareParams() {
     if (vd < 0) {
         double minR = std::numeric_limits<double>::infinity();
         // radius of spheres is in posr.w; read back from the host description
-        for (int64_t i = 0; i < nPar; i++)
+        for (int64_t i = p0; i < p1; i++)
             if (hShape[i] == WG_SHAPE_SPHERE) minR = std::min(minR, hRadius[i]);
         vd = std::isinf(minR) ? 0 : std::abs(vd) * minR;
     }
@@ -357,14 +367,23 @@ int Sim::upload() {
     SimEx& X = static_cast<SimEx&>(*this);
     if (!haveCfg) return fail(WG_ERR_STATE, "wg_set_config must be called before running");
     if (nPar == 0) return fail(WG_ERR_STATE, "no particles");
-    if (!cfg.reset) return fail(WG_ERR_UNSUPPORTED, "Leapfrog.reset=False: the GPU path integrates the engine list [Leapfrog(reset=True), InsertionSortCollider, ContactLoop]");
-    if (!((cfg.phys == 0 && cfg.law == 0) || (cfg.phys == 1 && cfg.law == 1)))
-        return fail(WG_ERR_UNSUPPORTED, "unsupported Cp2/Law2 combination (FrictPhys+IdealElPl or HertzPhys+HertzPhys_DMT)");
-    if (cfg.law == 1 && cfg.hz_alpha != 0) return fail(WG_ERR_UNSUPPORTED, "Law2_L6Geom_HertzPhys_DMT with Cp2_FrictMat_HertzPhys.alpha!=0 (Schwarz model) is not supported");
-    if (cfg.precision != WG_PREC_FP64 && cfg.precision != WG_PREC_FP32) return fail(WG_ERR_ARG, "unknown precision mode");
+    if (nScenes > 1 && (int64_t)sceneStart.size() == nScenes + 1 && sceneStart[nScenes] != nPar)
+        return fail(WG_ERR_ARG, "the scenes of the batch do not cover the particles");
+    for (int k = 0; k < nScenes; k++) {
+        const wg_config& c = nScenes > 1 ? cfgs[k] : cfg;
+        if (!c.reset) return fail(WG_ERR_UNSUPPORTED, "Leapfrog.reset=False: the GPU path integrates the engine list [Leapfrog(reset=True), InsertionSortCollider, ContactLoop]");
+        if (!((c.phys == 0 && c.law == 0) || (c.phys == 1 && c.law == 1)))
+            return fail(WG_ERR_UNSUPPORTED, "unsupported Cp2/Law2 combination (FrictPhys+IdealElPl or HertzPhys+HertzPhys_DMT)");
+        if (c.law == 1 && c.hz_alpha != 0) return fail(WG_ERR_UNSUPPORTED, "Law2_L6Geom_HertzPhys_DMT with Cp2_FrictMat_HertzPhys.alpha!=0 (Schwarz model) is not supported");
+        if (c.precision != WG_PREC_FP64 && c.precision != WG_PREC_FP32) return fail(WG_ERR_ARG, "unknown precision mode");
+        if (c.precision != cfg.precision) return fail(WG_ERR_UNSUPPORTED, "the scenes of a batch share one precision mode");
+        if (c.precision == WG_PREC_FP32 && c.law == 1 && c.hz_gamma != 0)
+            return fail(WG_ERR_UNSUPPORTED, "FP32-force mode: Cp2_FrictMat_HertzPhys.gamma (DMT adhesion) must be 0; use precision fp64");
+        if (nScenes > 1 && c.periodic) return fail(WG_ERR_UNSUPPORTED, "periodic scenes run one per simulation, not in a batch");
+        if (nScenes > 1 && (c.lone_mask != cfg.lone_mask || c.apply_forces != cfg.apply_forces))
+            return fail(WG_ERR_UNSUPPORTED, "the scenes of a batch share loneMask and ContactLoop.applyForces");
+    }
     prec = cfg.precision;
-    if (prec == WG_PREC_FP32 && cfg.law == 1 && cfg.hz_gamma != 0)
-        return fail(WG_ERR_UNSUPPORTED, "FP32-force mode: Cp2_FrictMat_HertzPhys.gamma (DMT adhesion) must be 0; use precision fp64");
     if (cfg.periodic)
         for (int64_t i = 0; i < nPar; i++)
             if (hShape[i] == WG_SHAPE_FACET)
@@ -425,7 +444,6 @@ int Sim::upload() {
         mask[p] = hMask[p];
         aux[p] = make_int4(0, 0, 0, 0);
         facet[p] = make_double4_32a(0, 0, 0, 0);
-        if (hShape[p] != WG_SHAPE_SPHERE) maxBoundaryId = (int32_t)p;
         if (hShape[p] == WG_SHAPE_SPHERE) {
             posr[p].w = hRadius[p];
             nSpheres++;
@@ -461,7 +479,24 @@ int Sim::upload() {
     I.heavy = (int32_t*)dalloc(sizeof(int32_t) * 2 * std::max<int64_t>(1, nPar));
     I.heavyFree = I.heavy + std::max<int64_t>(1, nPar);
     dMats = (double4_32a*)dalloc(sizeof(double4_32a) * std::max<size_t>(1, hDensity.size()));
-    dPar = (ScenePar*)dalloc(sizeof(ScenePar));
+    dPar = (ScenePar*)dalloc(sizeof(ScenePar) * nScenes);
+    if (nScenes > 1) {
+        // scene of each particle and node slot
+        hSceneOfPar.assign(nPar, 0);
+        std::vector<int32_t> nsc(nSlots, 0);
+        for (int k = 0; k < nScenes; k++)
+            for (int64_t p = sceneStart[k]; p < sceneStart[k + 1]; p++) {
+                hSceneOfPar[p] = k;
+                if (hShape[p] == WG_SHAPE_FACET) {
+                    for (int q = 0; q < 3; q++) nsc[map[hNodes3[3 * p + q]]] = k;
+                } else nsc[p] = k;
+            }
+        P.scene = (int32_t*)dalloc(sizeof(int32_t) * nPar);
+        N.scene = (int32_t*)dalloc(sizeof(int32_t) * nSlots);
+        if (!N.scene) return fail(WG_ERR_CUDA, "out of device memory (scene)");
+        WG_CUDA_TRY(cudaMemcpy(P.scene, hSceneOfPar.data(), sizeof(int32_t) * nPar, cudaMemcpyHostToDevice));
+        WG_CUDA_TRY(cudaMemcpy(N.scene, nsc.data(), sizeof(int32_t) * nSlots, cudaMemcpyHostToDevice));
+    }
     dStep = (long long*)dalloc(sizeof(long long));
     dFlags = (int*)dalloc(sizeof(int) * 4);
     X.dApiMap = (int32_t*)dalloc(sizeof(int32_t) * std::max<int64_t>(1, na));
@@ -572,7 +607,11 @@ int Sim::upload() {
     }
     prepareParams();
     if (cfg.periodic) fillCellPar(X);
-    WG_CUDA_TRY(cudaMemcpy(dPar, &hPar, sizeof(ScenePar), cudaMemcpyHostToDevice));
+    if (nScenes > 1) {
+        for (int k = 0; k < nScenes; k++) hPars[k].stepBase = (long long)cfg.step - (long long)cfgs[k].step;
+        WG_CUDA_TRY(cudaMemcpy(dPar, hPars.data(), sizeof(ScenePar) * nScenes, cudaMemcpyHostToDevice));
+    } else
+        WG_CUDA_TRY(cudaMemcpy(dPar, &hPar, sizeof(ScenePar), cudaMemcpyHostToDevice));
     uploaded = true;
     initialized = false;
     return 0;
@@ -611,7 +650,9 @@ int Sim::run(int64_t n) {
     WG_CUDA_TRY(cudaSetDevice(device));
     double ph[4] = {0, 0, 0, 0};
     int64_t launches = 0;
-    const int64_t maxChunk = (cfg.periodic || hPar.verletDist == 0) ? 1 : 32;
+    bool anyZeroVd = hPar.verletDist == 0;
+    for (const ScenePar& q : hPars) anyZeroVd = anyZeroVd || q.verletDist == 0;
+    const int64_t maxChunk = (cfg.periodic || anyZeroVd) ? 1 : std::max<int64_t>(1, std::min<int64_t>(chunkSteps, 1024));
     if ((int64_t)evPool.size() < 3 * maxChunk + 2) {
         for (int64_t q = (int64_t)evPool.size(); q < 3 * maxChunk + 2; q++) {
             cudaEvent_t e;
@@ -633,8 +674,10 @@ int Sim::run(int64_t n) {
         launches++;
     };
     auto stepContact = [&]() {
-        if (fp32) launch_contact_fp32(stream, side, N, P, C, I, dMats, dPar, dStep, dFlags, nMixed, cfg.periodic != 0);
-        else launch_contact_fp64(stream, N, P, C, I, dMats, dPar, dStep, dFlags);
+        if (fp32) launch_contact_fp32(stream, side, N, P, C, I, dMats, dPar, dStep, dFlags, nMixed, cfg.periodic != 0,
+                                      contactBlock > 0 ? contactBlock : 256);
+        else launch_contact_fp64(stream, N, P, C, I, dMats, dPar, dStep, dFlags,
+                                 (contactBlock > 0 && contactBlock <= 128) ? contactBlock : 128);  // launch bounds 128
         launch_advance(stream, dStep, dFlags);
         launches += 2;
     };
@@ -643,7 +686,7 @@ int Sim::run(int64_t n) {
     int64_t done = 0;
     while (done < n) {
         const int64_t k = std::min<int64_t>(n - done, maxChunk);
-        const bool needFull = !initialized || hPar.verletDist == 0;
+        const bool needFull = !initialized || anyZeroVd;
         k_set_flags<<<1, 1, 0, stream>>>(dFlags, needFull ? 1 : 0);
         if (cfg.periodic) {
             X.cell.integrateAndUpdate(cfg.dt);
@@ -651,12 +694,40 @@ int Sim::run(int64_t n) {
             WG_CUDA_TRY(cudaMemcpyAsync(dPar, &hPar, sizeof(ScenePar), cudaMemcpyHostToDevice, stream));
         }
         const int64_t s0 = step;
-        for (int64_t j = 0; j < k; j++) {
-            WG_CUDA_TRY(cudaEventRecord(E[3 * j], stream));
-            stepLeapfrog(j == 0 ? (fromEnds ? 1 : 0) : 1);
-            WG_CUDA_TRY(cudaEventRecord(E[3 * j + 1], stream));
-            stepContact();
-            WG_CUDA_TRY(cudaEventRecord(E[3 * j + 2], stream));
+        // a chunk that starts from the end slots and is not due for a full run is replayed as a
+        // CUDA graph (re-captured after every full run, whose contact arrays it refers to)
+        const bool graphChunk = useGraph && fromEnds && !needFull && k == maxChunk && !cfg.periodic;
+        if (graphChunk) {
+            if (!graphExec || graphSteps != k || graphEpoch != nFullRuns) {
+                if (graphExec) cudaGraphExecDestroy(graphExec);
+                graphExec = nullptr;
+                cudaGraph_t g = nullptr;
+                WG_CUDA_TRY(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+                const int64_t l0 = launches;
+                for (int64_t j = 0; j < k; j++) {
+                    stepLeapfrog(1);
+                    stepContact();
+                }
+                graphLaunches = launches - l0;
+                launches = l0;
+                WG_CUDA_TRY(cudaStreamEndCapture(stream, &g));
+                WG_CUDA_TRY(cudaGraphInstantiate(&graphExec, g, 0));
+                cudaGraphDestroy(g);
+                graphSteps = k;
+                graphEpoch = nFullRuns;
+            }
+            WG_CUDA_TRY(cudaEventRecord(E[0], stream));
+            WG_CUDA_TRY(cudaGraphLaunch(graphExec, stream));
+            WG_CUDA_TRY(cudaEventRecord(E[1], stream));
+            launches += graphLaunches;
+        } else {
+            for (int64_t j = 0; j < k; j++) {
+                WG_CUDA_TRY(cudaEventRecord(E[3 * j], stream));
+                stepLeapfrog(j == 0 ? (fromEnds ? 1 : 0) : 1);
+                WG_CUDA_TRY(cudaEventRecord(E[3 * j + 1], stream));
+                stepContact();
+                WG_CUDA_TRY(cudaEventRecord(E[3 * j + 2], stream));
+            }
         }
         WG_CUDA_TRY(cudaGetLastError());
         WG_CUDA_TRY(cudaMemcpyAsync(hFlags, dFlags, sizeof(int) * 4, cudaMemcpyDeviceToHost, stream));
@@ -666,14 +737,21 @@ int Sim::run(int64_t n) {
         int64_t ds = (int64_t)*hStepPin - s0;
         if (ds < 0 || ds > k) return fail(WG_ERR_STATE, "device step counter out of sequence");
         float a;
-        for (int64_t j = 0; j < ds; j++) {
-            cudaEventElapsedTime(&a, E[3 * j], E[3 * j + 1]); ph[0] += a;
-            cudaEventElapsedTime(&a, E[3 * j + 1], E[3 * j + 2]); ph[1] += a;
-        }
+        if (graphChunk) {
+            cudaEventElapsedTime(&a, E[0], E[1]);
+            ph[2] += a;  // whole steps replayed as a graph
+        } else
+            for (int64_t j = 0; j < ds; j++) {
+                cudaEventElapsedTime(&a, E[3 * j], E[3 * j + 1]); ph[0] += a;
+                cudaEventElapsedTime(&a, E[3 * j + 1], E[3 * j + 2]); ph[1] += a;
+            }
         if (ds < k || hFlags[FL_FULL]) {
             // Leapfrog of step s0+ds ran, its contact loop waits for the collider
             if (!hFlags[FL_FULL]) return fail(WG_ERR_STATE, "queued steps halted without a collider request");
-            cudaEventElapsedTime(&a, E[3 * ds], E[3 * ds + 1]); ph[0] += a;
+            if (!graphChunk) {
+                cudaEventElapsedTime(&a, E[3 * ds], E[3 * ds + 1]);
+                ph[0] += a;
+            }
             WG_CUDA_TRY(cudaEventRecord(E[3 * maxChunk], stream));
             int r = collide_full_run(*this);
             if (r) return r;
@@ -790,6 +868,64 @@ int wg_set_config(wg_scene* s, const wg_config* c) {
     if (!(c->dt > 0) || !std::isfinite(c->dt)) return S.fail(WG_ERR_ARG, "Scene.dt must be positive and finite");
     S.cfg = *c;
     S.haveCfg = true;
+    return WG_OK;
+}
+
+int wg_set_scenes(wg_scene* s, int32_t n_scenes, const wg_config* cfgs, const int64_t* particle_start) {
+    if (!s || n_scenes < 1 || !cfgs || !particle_start) return WG_ERR_ARG;
+    Sim& S = *SIM(s);
+    if (S.uploaded) return S.fail(WG_ERR_STATE, "scenes are fixed once the simulation runs; create a new one");
+    if (particle_start[0] != 0) return S.fail(WG_ERR_ARG, "particle_start[0] must be 0");
+    for (int k = 0; k < n_scenes; k++) {
+        if (particle_start[k + 1] < particle_start[k]) return S.fail(WG_ERR_ARG, "particle_start must be non-decreasing");
+        if (!(cfgs[k].dt > 0) || !std::isfinite(cfgs[k].dt)) return S.fail(WG_ERR_ARG, "Scene.dt must be positive and finite");
+    }
+    S.nScenes = n_scenes;
+    S.cfgs.assign(cfgs, cfgs + n_scenes);
+    S.sceneStart.assign(particle_start, particle_start + n_scenes + 1);
+    S.sceneTime0.assign(n_scenes, 0.0);
+    S.cfg = cfgs[0];
+    S.haveCfg = true;
+    return WG_OK;
+}
+
+int wg_set_launch(wg_scene* s, int32_t contact_block, int32_t chunk_steps, int32_t use_graph) {
+    if (!s) return WG_ERR_ARG;
+    Sim& S = *SIM(s);
+    if (contact_block != 0 && contact_block != 64 && contact_block != 128 && contact_block != 256)
+        return S.fail(WG_ERR_ARG, "contact_block must be 0, 64, 128 or 256");
+    if (chunk_steps < 1 || chunk_steps > 1024) return S.fail(WG_ERR_ARG, "chunk_steps must be in [1, 1024]");
+    S.contactBlock = contact_block;
+    S.chunkSteps = chunk_steps;
+    S.useGraph = use_graph != 0;
+    return WG_OK;
+}
+
+int wg_get_scene_stats(wg_scene* s, int32_t k, wg_stats* o) {
+    if (!s || !o) return WG_ERR_ARG;
+    Sim& S = *SIM(s);
+    if (k < 0 || k >= S.nScenes) return S.fail(WG_ERR_ARG, "scene index out of range");
+    std::memset(o, 0, sizeof(*o));
+    const wg_config& c = S.nScenes > 1 ? S.cfgs[k] : S.cfg;
+    const int64_t done = S.step - S.cfg.step;
+    o->step = c.step + done;
+    o->time = S.nScenes > 1 ? S.sceneTime0[k] + done * c.dt : S.time;
+    o->n_full_runs = S.nFullRuns;
+    o->verlet_dist = S.nScenes > 1 && S.uploaded ? S.hPars[k].verletDist : S.hPar.verletDist;
+    if (S.uploaded && S.C.n > 0) {
+        const int64_t n = S.C.n;
+        std::vector<uint32_t> fl(n);
+        std::vector<uint64_t> key(n);
+        WG_CUDA_TRY(cudaMemcpy(fl.data(), S.C.flags, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
+        WG_CUDA_TRY(cudaMemcpy(key.data(), S.C.key, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost));
+        const int64_t p0 = S.nScenes > 1 ? S.sceneStart[k] : 0, p1 = S.nScenes > 1 ? S.sceneStart[k + 1] : S.nPar;
+        for (int64_t c2 = 0; c2 < n; c2++) {
+            const int64_t lo = (int64_t)(key[c2] >> 32);
+            if (lo < p0 || lo >= p1 || (fl[c2] & C_REMOVED)) continue;
+            o->n_contacts++;
+            if (fl[c2] & C_REAL) o->n_real++;
+        }
+    }
     return WG_OK;
 }
 

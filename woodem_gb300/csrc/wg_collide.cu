@@ -54,6 +54,12 @@ struct CollideWork {
     int64_t cellOffCap = 0;
     double* red = nullptr;        // reduction partials
     double* hRed = nullptr;       // pinned
+    std::vector<int32_t> hChunk;      // grid-reduction chunks of sphereIds (never across scenes)
+    std::vector<int32_t> hSceneChunk; // chunks of scene k: [hSceneChunk[k], hSceneChunk[k+1])
+    std::vector<int64_t> hSceneSph;   // spheres of scene k: sphereIds[hSceneSph[k] .. hSceneSph[k+1])
+    int32_t* dChunk = nullptr;
+    Grid* dGrids = nullptr;
+    int32_t* gStart = nullptr;        // walls of scene k in globalIds (batches)
     // pairs
     uint64_t* pairs = nullptr;
     uint64_t* pairsSorted = nullptr;
@@ -72,6 +78,7 @@ struct CollideWork {
     int32_t* src = nullptr;
     int64_t mergeCap = 0, orphCap = 0, srcCap = 0;
     int32_t* act = nullptr;       // exclusive scan of the active contacts
+    int32_t* actSS = nullptr;     // exclusive scan of the active sphere-sphere contacts
     uint32_t* hiKeys = nullptr;
     uint32_t* hiKeysSorted = nullptr;
     int32_t* hiVals = nullptr;
@@ -91,7 +98,7 @@ static const int BS = 256;
 __global__ void k_aabb(DevNodes N, DevParticles P, const ScenePar* __restrict__ spp, int* __restrict__ dErr) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= P.n) return;
-    const ScenePar& sp = *spp;
+    const ScenePar& sp = spp[sceneOfP(P, p)];
     const int sh = P.shape[p];
     D3 mn, mx;
     const double inf = __longlong_as_double(0x7ff0000000000000LL);
@@ -180,12 +187,14 @@ __global__ void k_aabb(DevNodes N, DevParticles P, const ScenePar* __restrict__ 
 }
 
 // ---------------------------------------------------------------- grid bounds over spheres
-// partial[b] = {min mn.x, min mn.y, min mn.z, max mn.x, max mn.y, max mn.z, max extent}
-__global__ void k_grid_reduce(DevParticles P, const int32_t* __restrict__ ids, int n, double* __restrict__ partial) {
+// partial[b] = {min mn.x, min mn.y, min mn.z, max mn.x, max mn.y, max mn.z, max extent} over the
+// spheres ids[chunk[b] .. chunk[b+1]) (chunks never span two scenes of a batch)
+__global__ void k_grid_reduce(DevParticles P, const int32_t* __restrict__ ids, const int32_t* __restrict__ chunk,
+                              double* __restrict__ partial) {
     __shared__ double s[7][BS];
     const double inf = __longlong_as_double(0x7ff0000000000000LL);
     double v[7] = {inf, inf, inf, -inf, -inf, -inf, 0.};
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (int i = chunk[blockIdx.x] + threadIdx.x; i < chunk[blockIdx.x + 1]; i += blockDim.x) {
         const int p = ids[i];
         const double4_32a a = P.mn[p], b = P.mx[p];
         v[0] = fmin(v[0], a.x); v[1] = fmin(v[1], a.y); v[2] = fmin(v[2], a.z);
@@ -211,14 +220,15 @@ __device__ __forceinline__ int cellCoord(double v, double o, double h, int n) {
     return ci < 0 ? 0 : (ci >= n ? n - 1 : ci);
 }
 
-__global__ void k_cellkey(DevParticles P, const int32_t* __restrict__ ids, int n, Grid G, uint32_t* __restrict__ key,
-                          int32_t* __restrict__ val) {
+__global__ void k_cellkey(DevParticles P, const int32_t* __restrict__ ids, int n, const Grid* __restrict__ Gs,
+                          uint32_t* __restrict__ key, int32_t* __restrict__ val) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int p = ids[i];
+    const Grid G = Gs[sceneOfP(P, p)];
     const double4_32a a = P.mn[p];
     const int cx = cellCoord(a.x, G.ox, G.h, G.nx), cy = cellCoord(a.y, G.oy, G.h, G.ny), cz = cellCoord(a.z, G.oz, G.h, G.nz);
-    key[i] = (uint32_t)(((int64_t)cz * G.ny + cy) * G.nx + cx);
+    key[i] = (uint32_t)(G.base + ((int64_t)cz * G.ny + cy) * G.nx + cx);
     val[i] = p;
 }
 
@@ -311,8 +321,8 @@ __device__ __forceinline__ uint64_t pairKey(int a, int b) {
 // The candidate ranges of a lane are walked as one sequence so that the warp can flush together.
 __global__ void k_pairs_ss(const uint32_t* __restrict__ skey, const double4_32a* __restrict__ smn,
                            const double4_32a* __restrict__ smx, const float4* __restrict__ smnf, const float4* __restrict__ smxf,
-                           int n, Grid G, const int32_t* __restrict__ off, uint32_t lone, uint64_t* __restrict__ pairs, int64_t cap,
-                           unsigned long long* __restrict__ counter) {
+                           int n, const Grid* __restrict__ Gs, const int32_t* __restrict__ pscene, const int32_t* __restrict__ off,
+                           uint32_t lone, uint64_t* __restrict__ pairs, int64_t cap, unsigned long long* __restrict__ counter) {
     const unsigned FULL = 0xffffffffu;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < n;
@@ -324,24 +334,25 @@ __global__ void k_pairs_ss(const uint32_t* __restrict__ skey, const double4_32a*
 #pragma unroll
     for (int r = 0; r < 5; r++) rb[r] = re[r] = 0;
     if (valid) {
-        const uint32_t k = skey[i];
-        const int cx = (int)(k % (uint32_t)G.nx);
-        const int cy = (int)((k / (uint32_t)G.nx) % (uint32_t)G.ny);
-        const int cz = (int)(k / ((uint32_t)G.nx * (uint32_t)G.ny));
         fn1 = smnf[i];
         fx1 = smxf[i];
         m1 = __float_as_uint(fn1.w);
         pi = __float_as_int(fx1.w);
+        const Grid G = Gs[pscene ? pscene[pi] : 0];
+        const uint32_t k = (uint32_t)((int64_t)skey[i] - G.base);
+        const int cx = (int)(k % (uint32_t)G.nx);
+        const int cy = (int)((k / (uint32_t)G.nx) % (uint32_t)G.ny);
+        const int cz = (int)(k / ((uint32_t)G.nx * (uint32_t)G.ny));
         const int cx1 = cx + 1 < G.nx ? cx + 1 : cx;
         rb[0] = i + 1;
-        re[0] = off[((int64_t)cz * G.ny + cy) * G.nx + cx1 + 1];
+        re[0] = off[G.base + ((int64_t)cz * G.ny + cy) * G.nx + cx1 + 1];
         const int DY[4] = {1, -1, 0, 1}, DZ[4] = {0, 1, 1, 1};
 #pragma unroll
         for (int r = 0; r < 4; r++) {
             const int y = cy + DY[r], z = cz + DZ[r];
             if (y < 0 || y >= G.ny || z >= G.nz) continue;
             const int x0 = cx > 0 ? cx - 1 : 0;
-            const int64_t rowBase = ((int64_t)z * G.ny + y) * G.nx;
+            const int64_t rowBase = G.base + ((int64_t)z * G.ny + y) * G.nx;
             rb[r + 1] = off[rowBase + x0];
             re[r + 1] = off[rowBase + cx1 + 1];
         }
@@ -373,13 +384,14 @@ __global__ void k_pairs_ss(const uint32_t* __restrict__ skey, const double4_32a*
 // each x-run of cells.
 __global__ void k_pairs_local(DevParticles P, const int32_t* __restrict__ lids, int nl, const double4_32a* __restrict__ smn,
                               const double4_32a* __restrict__ smx, const float4* __restrict__ smnf, const float4* __restrict__ smxf,
-                              Grid G, const int32_t* __restrict__ off, uint32_t lone, uint64_t* __restrict__ pairs, int64_t cap,
-                              unsigned long long* __restrict__ counter) {
+                              const Grid* __restrict__ Gs, const int32_t* __restrict__ off, uint32_t lone, uint64_t* __restrict__ pairs,
+                              int64_t cap, unsigned long long* __restrict__ counter) {
     const unsigned FULL = 0xffffffffu;
     const int t = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (t >= nl) return;  // warp-uniform
     const int p = lids[t];
+    const Grid G = Gs[sceneOfP(P, p)];
     const double4_32a mn1 = P.mn[p], mx1 = P.mx[p];
     const float4 fn1 = make_float4(__double2float_rd(mn1.x), __double2float_rd(mn1.y), __double2float_rd(mn1.z), 0.f);
     const float4 fx1 = make_float4(__double2float_ru(mx1.x), __double2float_ru(mx1.y), __double2float_ru(mx1.z), 0.f);
@@ -391,7 +403,7 @@ __global__ void k_pairs_local(DevParticles P, const int32_t* __restrict__ lids, 
     int nb = 0;
     for (int z = z0; z <= z1; z++)
         for (int y = y0; y <= y1; y++) {
-            const int64_t rowBase = ((int64_t)z * G.ny + y) * G.nx;
+            const int64_t rowBase = G.base + ((int64_t)z * G.ny + y) * G.nx;
             const int beg = off[rowBase + x0], end = off[rowBase + x1 + 1];
             for (int j0 = beg; j0 < end; j0 += 32) {
                 const int j = j0 + lane;
@@ -535,14 +547,19 @@ __global__ void k_pairs_global_peri(DevParticles P, const int32_t* __restrict__ 
 }
 
 // Walls (and any box too large for the grid) against every sphere.
-__global__ void k_pairs_global(DevParticles P, const int32_t* __restrict__ gids, int ng, const int32_t* __restrict__ sph, int ns,
-                               uint32_t lone, uint64_t* __restrict__ pairs, int64_t cap, unsigned long long* __restrict__ counter) {
+// gids are grouped by scene: the walls of scene k are gids[gStart[k] .. gStart[k+1]) (gStart null:
+// one scene, all of gids)
+__global__ void k_pairs_global(DevParticles P, const int32_t* __restrict__ gids, int ng, const int32_t* __restrict__ gStart,
+                               const int32_t* __restrict__ sph, int ns, uint32_t lone, uint64_t* __restrict__ pairs, int64_t cap,
+                               unsigned long long* __restrict__ counter) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= ns) return;
     const int s = sph[i];
     const double4_32a mn1 = P.mn[s], mx1 = P.mx[s];
     const uint32_t m1 = P.mask[s];
-    for (int g = 0; g < ng; g++) {
+    const int sc = sceneOfP(P, s);
+    const int g0 = gStart ? gStart[sc] : 0, g1 = gStart ? gStart[sc + 1] : ng;
+    for (int g = g0; g < g1; g++) {
         const int w = gids[g];
         if (w == s) continue;
         if (overlap3(mn1, mx1, P.mn[w], P.mx[w]) && maskOk(m1, P.mask[w], lone)) emitPair(s, w, pairs, cap, counter);
@@ -557,6 +574,7 @@ __global__ void k_pairs_large_large(DevParticles P, const int32_t* __restrict__ 
     const int a = (int)(t / n), b = (int)(t % n);
     if (b <= a) return;
     const int pa = ids[a], pb = ids[b];
+    if (sceneOfP(P, pa) != sceneOfP(P, pb)) return;  // the scenes of a batch never interact
     // facets sharing a node may not collide (Collision.cpp:27-31)
     if (P.shape[pa] == WG_SHAPE_FACET && P.shape[pb] == WG_SHAPE_FACET) {
         const int4 x = P.aux[pa], y = P.aux[pb];
@@ -666,7 +684,6 @@ __global__ void k_gather(DevContacts Cold, DevContacts Cnew, const int32_t* __re
 __global__ void k_dormant(DevContacts C, DevNodes N, DevParticles P, const ScenePar* __restrict__ spp) {
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= C.n) return;
-    const ScenePar& sp = *spp;
     const uint32_t fl = C.flags[c];
     if (fl & C_REAL) return;
     const uint32_t ty = ctype(fl);
@@ -674,6 +691,7 @@ __global__ void k_dormant(DevContacts C, DevNodes N, DevParticles P, const Scene
     const uint64_t key = C.key[c];
     const int lo = (int)(key >> 32), hi = (int)(key & 0xffffffffu);
     const int A = (fl & C_SWAP) ? hi : lo, B = (fl & C_SWAP) ? lo : hi;
+    const ScenePar& sp = spp[sceneOfP(P, B)];
     const double m2 = 2 * sp.verletDist;
     bool far;
     const double4_32a pb = N.posr[B];
@@ -733,10 +751,13 @@ __global__ void k_dormant(DevContacts C, DevNodes N, DevParticles P, const Scene
 // Only active contacts (a functor applies and the pair is not dormant) own end slots; act is
 // their exclusive scan over the key-sorted contacts, act[n] = number of active contacts.
 __device__ __forceinline__ bool activeContact(uint32_t fl) { return ctype(fl) != CT_NONE && !(fl & C_DORMANT); }
-__global__ void k_active(const uint32_t* __restrict__ flags, int64_t n, int32_t* __restrict__ act) {
+__global__ void k_active(const uint32_t* __restrict__ flags, int64_t n, int32_t* __restrict__ act, int32_t* __restrict__ actSS) {
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= n) return;
-    act[c] = activeContact(flags[c]) ? 1 : 0;
+    const uint32_t fl = flags[c];
+    const bool a = activeContact(fl);
+    act[c] = a ? 1 : 0;
+    actSS[c] = (a && ctype(fl) == CT_SS) ? 1 : 0;
 }
 // loStart[p] = active contacts with lo < p
 __global__ void k_lo_start(const uint64_t* __restrict__ key, int64_t n, int nPar, const int32_t* __restrict__ act,
@@ -760,8 +781,11 @@ __global__ void k_hi_start(const uint32_t* __restrict__ hks, int64_t n, int nPar
 }
 // end slots: active contact c with hi==p sits at loStart[p] + (its index k in hiList); with lo==p
 // at hiStart[p+1] + act[c] (see DevIncidence); inactive contacts have no slot (-1)
+// The work list holds the active contacts other than sphere-sphere first, then the sphere-sphere
+// ones, each group in ascending contact order (actSS: exclusive scan of the active sphere-sphere
+// contacts; nOther = active contacts that are not sphere-sphere).
 __global__ void k_slots(const uint64_t* __restrict__ key, const uint32_t* __restrict__ flags, int64_t n, int64_t nAct,
-                        const int32_t* __restrict__ act, DevIncidence I) {
+                        const int32_t* __restrict__ act, const int32_t* __restrict__ actSS, int64_t nOther, DevIncidence I) {
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     if (k < nAct) {
@@ -774,17 +798,12 @@ __global__ void k_slots(const uint64_t* __restrict__ key, const uint32_t* __rest
         I.slotLo[k] = I.hiStart[loP + 1] + act[k];
         const uint32_t fl = flags[k];
         const int hiP = (int)(key[k] & 0xffffffffu);
-        I.work[act[k]] = (fl & C_SWAP) ? make_int4((int)k, hiP, loP, (int)(fl & 0xeu)) : make_int4((int)k, loP, hiP, (int)(fl & 0xeu));
+        const int64_t w = (ctype(fl) == CT_SS) ? nOther + actSS[k] : act[k] - actSS[k];
+        I.work[w] = (fl & C_SWAP) ? make_int4((int)k, hiP, loP, (int)(fl & 0xeu)) : make_int4((int)k, loP, hiP, (int)(fl & 0xeu));
     } else {
         I.slotLo[k] = -1;
         I.slotHi[k] = -1;
     }
-}
-
-// index of the first contact whose lo id is above every boundary particle
-__global__ void k_first_ss(const uint64_t* __restrict__ key, int64_t n, int firstId, const int32_t* __restrict__ act,
-                           int32_t* __restrict__ out) {
-    *out = act[lowerBound64(key, n, (uint64_t)(uint32_t)firstId << 32)];  // its active rank
 }
 
 // Particles summed by the block tree; the ones whose node has a free DOF are also summed before
@@ -829,6 +848,18 @@ static int buildLists(Sim& S) {
         else large.push_back((int32_t)p);
     }
     W.nSph = (int)sph.size();
+    // per-scene sphere ranges and grid-reduction chunks (particles of a batch are grouped by scene)
+    const int K = S.nScenes;
+    W.hSceneSph.assign(K + 1, 0);
+    for (int32_t p : sph) W.hSceneSph[(S.hSceneOfPar.empty() ? 0 : S.hSceneOfPar[p]) + 1]++;
+    for (int k = 0; k < K; k++) W.hSceneSph[k + 1] += W.hSceneSph[k];
+    W.hChunk.assign(1, 0);
+    W.hSceneChunk.assign(1, 0);
+    const int64_t CH = 4096;
+    for (int k = 0; k < K; k++) {
+        for (int64_t b = W.hSceneSph[k]; b < W.hSceneSph[k + 1]; b += CH) W.hChunk.push_back((int32_t)std::min(b + CH, W.hSceneSph[k + 1]));
+        W.hSceneChunk.push_back((int32_t)W.hChunk.size() - 1);
+    }
     W.hLarge = large;
     W.hGlobal = glob;
     W.sphereIds = (int32_t*)S.dalloc(sizeof(int32_t) * std::max<size_t>(1, sph.size()));
@@ -871,48 +902,59 @@ int collide_full_run(Sim& S) {
     if (S.nPar > 0) k_aabb<<<(unsigned)((S.nPar + BS - 1) / BS), BS, 0, st>>>(S.N, S.P, S.dPar, S.dFlags + 1);
     // lastPos for node slots not owned by a particle box computation (dummy slots) stays stale:
     // they never move (blocked, zero velocity) and are never tested against a stale reference.
-    // 2. grid over spheres
-    Grid G{0, 0, 0, 1, 1, 1, 1, 1};
+    // 2. grid over spheres, one per scene of a batch (keys of scene k start at its grid's base)
+    const int K = S.nScenes;
+    std::vector<Grid> hG(K, Grid{0, 0, 0, 1, 1, 1, 1, 1, 0});
+    Grid G = hG[0];
     const int ns = W.nSph;
     if (ns > 0) {
-        const int nb = std::min(1024, (ns + BS - 1) / BS);
+        const int nb = (int)W.hChunk.size() - 1;
         if (!W.red) {
-            W.red = (double*)S.dalloc(sizeof(double) * 7 * 1024);
-            WG_CUDA_TRY(cudaMallocHost(&W.hRed, sizeof(double) * 7 * 1024));
+            W.red = (double*)S.dalloc(sizeof(double) * 7 * std::max(nb, 1));
+            W.dChunk = (int32_t*)S.dalloc(sizeof(int32_t) * (nb + 1));
+            WG_CUDA_TRY(cudaMallocHost(&W.hRed, sizeof(double) * 7 * std::max(nb, 1)));
+            WG_CUDA_TRY(cudaMemcpy(W.dChunk, W.hChunk.data(), sizeof(int32_t) * (nb + 1), cudaMemcpyHostToDevice));
+            W.dGrids = (Grid*)S.dalloc(sizeof(Grid) * K);
+            if (!W.dGrids) return S.fail(WG_ERR_CUDA, "out of device memory (grid)");
         }
-        k_grid_reduce<<<nb, BS, 0, st>>>(S.P, W.sphereIds, ns, W.red);
+        k_grid_reduce<<<nb, BS, 0, st>>>(S.P, W.sphereIds, W.dChunk, W.red);
         WG_CUDA_TRY(cudaMemcpyAsync(W.hRed, W.red, sizeof(double) * 7 * nb, cudaMemcpyDeviceToHost, st));
         WG_CUDA_TRY(cudaStreamSynchronize(st));
-        double v[7] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY, 0.};
-        for (int b = 0; b < nb; b++) {
-            for (int q = 0; q < 3; q++) v[q] = std::min(v[q], W.hRed[7 * b + q]);
-            for (int q = 3; q < 7; q++) v[q] = std::max(v[q], W.hRed[7 * b + q]);
-        }
-        if (!(std::isfinite(v[0]) && std::isfinite(v[3]) && std::isfinite(v[6])))
-            return S.fail(WG_ERR_NAN, "InsertionSortCollider: non-finite sphere bounding box (NaN or infinite position)");
-        // cell edge slightly above the largest sphere box, so boxes that overlap sit in adjacent cells
-        double h = v[6] * (1 + 1e-9) + 1e-300;
-        double ext[3] = {v[3] - v[0], v[4] - v[1], v[5] - v[2]};
-        int64_t dims[3];
-        if (S.cfg.periodic) {
-            // the periodic cell [0, size) per axis (unsheared coordinates) in whole cells no narrower than h
+        int64_t base = 0;
+        for (int k = 0; k < K; k++) {
+            double v[7] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY, 0.};
+            for (int b = W.hSceneChunk[k]; b < W.hSceneChunk[k + 1]; b++) {
+                for (int q = 0; q < 3; q++) v[q] = std::min(v[q], W.hRed[7 * b + q]);
+                for (int q = 3; q < 7; q++) v[q] = std::max(v[q], W.hRed[7 * b + q]);
+            }
+            Grid& g = hG[k];
+            g.base = base;
+            if (W.hSceneChunk[k] == W.hSceneChunk[k + 1]) continue;  // a scene without spheres
+            if (!(std::isfinite(v[0]) && std::isfinite(v[3]) && std::isfinite(v[6])))
+                return S.fail(WG_ERR_NAN, "InsertionSortCollider: non-finite sphere bounding box (NaN or infinite position)");
+            const int64_t nsk = W.hSceneSph[k + 1] - W.hSceneSph[k];
+            // cell edge slightly above the largest sphere box, so boxes that overlap sit in adjacent cells
+            double h = v[6] * (1 + 1e-9) + 1e-300;
+            double ext[3] = {v[3] - v[0], v[4] - v[1], v[5] - v[2]};
+            int64_t dims[3];
             for (;;) {
-                for (int q = 0; q < 3; q++) dims[q] = std::max<int64_t>(1, (int64_t)std::floor(S.hPar.cellSize[q] / h));
+                if (S.cfg.periodic)  // the periodic cell [0, size) per axis (unsheared coordinates)
+                    for (int q = 0; q < 3; q++) dims[q] = std::max<int64_t>(1, (int64_t)std::floor(S.hPar.cellSize[q] / h));
+                else
+                    for (int q = 0; q < 3; q++) dims[q] = (int64_t)std::floor(ext[q] / h) + 1;
                 int64_t nc = dims[0] * dims[1] * dims[2];
-                if (nc <= std::max<int64_t>(8 * (int64_t)ns, 1 << 16) && nc < (int64_t(1) << 31)) break;
+                if (nc <= std::max<int64_t>(8 * nsk, K > 1 ? 64 : (1 << 16)) && nc < (int64_t(1) << 31)) break;
                 h *= 1.25;
             }
-        } else {
-            for (;;) {
-                for (int q = 0; q < 3; q++) dims[q] = (int64_t)std::floor(ext[q] / h) + 1;
-                int64_t nc = dims[0] * dims[1] * dims[2];
-                if (nc <= std::max<int64_t>(8 * (int64_t)ns, 1 << 16) && nc < (int64_t(1) << 31)) break;
-                h *= 1.25;
-            }
+            g.ox = v[0]; g.oy = v[1]; g.oz = v[2]; g.h = h;
+            g.nx = (int32_t)dims[0]; g.ny = (int32_t)dims[1]; g.nz = (int32_t)dims[2];
+            g.ncell = dims[0] * dims[1] * dims[2];
+            base += g.ncell;
         }
-        G.ox = v[0]; G.oy = v[1]; G.oz = v[2]; G.h = h;
-        G.nx = (int32_t)dims[0]; G.ny = (int32_t)dims[1]; G.nz = (int32_t)dims[2];
-        G.ncell = dims[0] * dims[1] * dims[2];
+        if (base >= (int64_t(1) << 32) - 1) return S.fail(WG_ERR_CAPACITY, "too many broad-phase cells in the batch");
+        const int64_t ncellAll = base;
+        G = hG[0];
+        WG_CUDA_TRY(cudaMemcpyAsync(W.dGrids, hG.data(), sizeof(Grid) * K, cudaMemcpyHostToDevice, st));
         // sort spheres by cell
         if (!W.cellKey) {
             W.cellKey = (uint32_t*)S.dalloc(sizeof(uint32_t) * ns);
@@ -926,17 +968,17 @@ int collide_full_run(Sim& S) {
             W.smxf = (float4*)S.dalloc(sizeof(float4) * ns);
             if (!W.smask || !W.smxf) return S.fail(WG_ERR_CUDA, "out of device memory (grid)");
         }
-        W.cellOff = grow(S, W.cellOff, W.cellOffCap, G.ncell + 1);
+        W.cellOff = grow(S, W.cellOff, W.cellOffCap, ncellAll + 1);
         if (S.cfg.periodic) k_cellkey_peri<<<(ns + BS - 1) / BS, BS, 0, st>>>(S.P, W.sphereIds, ns, G, S.dPar, W.cellKey, W.cellVal);
-        else k_cellkey<<<(ns + BS - 1) / BS, BS, 0, st>>>(S.P, W.sphereIds, ns, G, W.cellKey, W.cellVal);
+        else k_cellkey<<<(ns + BS - 1) / BS, BS, 0, st>>>(S.P, W.sphereIds, ns, W.dGrids, W.cellKey, W.cellVal);
         int endBit = 1;
-        while ((int64_t(1) << endBit) < G.ncell) endBit++;
+        while ((int64_t(1) << endBit) < ncellAll) endBit++;
         size_t tb = 0;
         cub::DeviceRadixSort::SortPairs(nullptr, tb, W.cellKey, W.cellKeySorted, W.cellVal, W.sid, ns, 0, endBit, st);
         if (ensureCub(S, tb)) return WG_ERR_CUDA;
         tb = W.cubBytes;
         WG_CUDA_TRY(cub::DeviceRadixSort::SortPairs(W.cubTmp, tb, W.cellKey, W.cellKeySorted, W.cellVal, W.sid, ns, 0, endBit, st));
-        k_cell_off<<<(unsigned)((G.ncell + 1 + BS - 1) / BS), BS, 0, st>>>(W.cellKeySorted, ns, G.ncell, W.cellOff);
+        k_cell_off<<<(unsigned)((ncellAll + 1 + BS - 1) / BS), BS, 0, st>>>(W.cellKeySorted, ns, ncellAll, W.cellOff);
         k_gather_sorted<<<(ns + BS - 1) / BS, BS, 0, st>>>(S.P, W.sid, ns, W.smn, W.smx, W.smask, W.smnf, W.smxf);
     }
     // lists of large particles: facets with boxes spanning a few cells use the grid, the rest are global
@@ -951,13 +993,23 @@ int collide_full_run(Sim& S) {
             std::vector<int32_t> loc, glo = W.hGlobal;
             for (int32_t p : W.hLarge) {
                 double e = std::max({mx[p].x - mn[p].x, mx[p].y - mn[p].y, mx[p].z - mn[p].z});
-                if (ns > 0 && std::isfinite(e) && e <= 8 * G.h) loc.push_back(p);
+                const double hk = hG[S.hSceneOfPar.empty() ? 0 : S.hSceneOfPar[p]].h;
+                if (ns > 0 && std::isfinite(e) && e <= 8 * hk) loc.push_back(p);
                 else glo.push_back(p);
             }
+            std::sort(glo.begin(), glo.end());  // grouped by scene (particles of a batch are)
             W.nLarge = (int)loc.size();
             W.nGlobal = (int)glo.size();
             if (W.nLarge) WG_CUDA_TRY(cudaMemcpy(W.largeIds, loc.data(), sizeof(int32_t) * loc.size(), cudaMemcpyHostToDevice));
             if (W.nGlobal) WG_CUDA_TRY(cudaMemcpy(W.globalIds, glo.data(), sizeof(int32_t) * glo.size(), cudaMemcpyHostToDevice));
+            if (K > 1) {
+                std::vector<int32_t> gs(K + 1, 0);
+                for (int32_t p : glo) gs[S.hSceneOfPar[p] + 1]++;
+                for (int k = 0; k < K; k++) gs[k + 1] += gs[k];
+                W.gStart = (int32_t*)S.dalloc(sizeof(int32_t) * (K + 1));
+                if (!W.gStart) return S.fail(WG_ERR_CUDA, "out of device memory (grid)");
+                WG_CUDA_TRY(cudaMemcpy(W.gStart, gs.data(), sizeof(int32_t) * (K + 1), cudaMemcpyHostToDevice));
+            }
         }
     }
     // 3-4. pair generation with a capacity retry
@@ -989,14 +1041,14 @@ int collide_full_run(Sim& S) {
                 k_pairs_global_peri<<<(ns + BS - 1) / BS, BS, 0, st>>>(S.P, W.globalIds, W.nGlobal, W.sphereIds, ns, lone, S.dPar,
                                                                      W.pairs, W.pairCd, W.pairCap, W.counter, S.dFlags + FL_ERR);
         } else if (ns > 0) {
-            k_pairs_ss<<<(ns + BS - 1) / BS, BS, 0, st>>>(W.cellKeySorted, W.smn, W.smx, W.smnf, W.smxf, ns, G, W.cellOff, lone,
-                                                        W.pairs, W.pairCap, W.counter);
+            k_pairs_ss<<<(ns + BS - 1) / BS, BS, 0, st>>>(W.cellKeySorted, W.smn, W.smx, W.smnf, W.smxf, ns, W.dGrids, S.P.scene,
+                                                        W.cellOff, lone, W.pairs, W.pairCap, W.counter);
             if (W.nLarge > 0)
                 k_pairs_local<<<(unsigned)(((int64_t)W.nLarge * 32 + BS - 1) / BS), BS, 0, st>>>(
-                    S.P, W.largeIds, W.nLarge, W.smn, W.smx, W.smnf, W.smxf, G, W.cellOff, lone, W.pairs, W.pairCap, W.counter);
+                    S.P, W.largeIds, W.nLarge, W.smn, W.smx, W.smnf, W.smxf, W.dGrids, W.cellOff, lone, W.pairs, W.pairCap, W.counter);
             if (W.nGlobal > 0)
-                k_pairs_global<<<(ns + BS - 1) / BS, BS, 0, st>>>(S.P, W.globalIds, W.nGlobal, W.sphereIds, ns, lone, W.pairs,
-                                                                W.pairCap, W.counter);
+                k_pairs_global<<<(ns + BS - 1) / BS, BS, 0, st>>>(S.P, W.globalIds, W.nGlobal, W.gStart, W.sphereIds, ns, lone,
+                                                                W.pairs, W.pairCap, W.counter);
         }
         if (W.largeLargePossible && !peri) {
             // all non-spheres against each other
@@ -1098,7 +1150,7 @@ int collide_full_run(Sim& S) {
     if (W.hiCap < std::max<int64_t>(n, 1)) {
         if (W.hiKeys) {
             S.dfree(W.hiKeys); S.dfree(W.hiKeysSorted); S.dfree(W.hiVals); S.dfree(S.I.hiList);
-            S.dfree(S.I.slotLo); S.dfree(S.I.slotHi); S.dfree(W.act); S.dfree(S.I.work);
+            S.dfree(S.I.slotLo); S.dfree(S.I.slotHi); S.dfree(W.act); S.dfree(W.actSS); S.dfree(S.I.work);
         }
         W.hiCap = std::max<int64_t>(n, 1) * 3 / 2 + 1024;
         W.hiKeys = (uint32_t*)S.dalloc(sizeof(uint32_t) * W.hiCap);
@@ -1108,24 +1160,30 @@ int collide_full_run(Sim& S) {
         S.I.slotLo = (int32_t*)S.dalloc(sizeof(int32_t) * W.hiCap);
         S.I.slotHi = (int32_t*)S.dalloc(sizeof(int32_t) * W.hiCap);
         W.act = (int32_t*)S.dalloc(sizeof(int32_t) * (W.hiCap + 1));
+        W.actSS = (int32_t*)S.dalloc(sizeof(int32_t) * (W.hiCap + 1));
         S.I.work = (int4*)S.dalloc(sizeof(int4) * W.hiCap);
         if (!S.I.slotHi || !W.act || !S.I.work) return S.fail(WG_ERR_CUDA, "out of device memory (incidence)");
     }
-    int64_t nAct = 0;
+    int64_t nAct = 0, nSS = 0;
     {
         WG_CUDA_TRY(cudaMemsetAsync(W.act, 0, sizeof(int32_t) * (n + 1), st));
+        WG_CUDA_TRY(cudaMemsetAsync(W.actSS, 0, sizeof(int32_t) * (n + 1), st));
         if (n > 0) {
-            k_active<<<(unsigned)((n + BS - 1) / BS), BS, 0, st>>>(S.C.flags, n, W.act);
+            k_active<<<(unsigned)((n + BS - 1) / BS), BS, 0, st>>>(S.C.flags, n, W.act, W.actSS);
             size_t tb = 0;
             cub::DeviceScan::ExclusiveSum(nullptr, tb, W.act, W.act, (int)(n + 1), st);
             if (ensureCub(S, tb)) return WG_ERR_CUDA;
             tb = W.cubBytes;
             WG_CUDA_TRY(cub::DeviceScan::ExclusiveSum(W.cubTmp, tb, W.act, W.act, (int)(n + 1), st));
+            tb = W.cubBytes;
+            WG_CUDA_TRY(cub::DeviceScan::ExclusiveSum(W.cubTmp, tb, W.actSS, W.actSS, (int)(n + 1), st));
         }
-        int32_t h = 0;
-        WG_CUDA_TRY(cudaMemcpyAsync(&h, W.act + n, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+        int32_t h[2] = {0, 0};
+        WG_CUDA_TRY(cudaMemcpyAsync(&h[0], W.act + n, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+        WG_CUDA_TRY(cudaMemcpyAsync(&h[1], W.actSS + n, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
         WG_CUDA_TRY(cudaStreamSynchronize(st));
-        nAct = h;
+        nAct = h[0];
+        nSS = h[1];
     }
     k_lo_start<<<(unsigned)((S.nPar + 1 + BS - 1) / BS), BS, 0, st>>>(S.C.key, n, (int)S.nPar, W.act, S.I.loStart);
     if (S.I.endCap < 2 * std::max<int64_t>(nAct, 1)) {
@@ -1154,8 +1212,9 @@ int collide_full_run(Sim& S) {
         WG_CUDA_TRY(cub::DeviceRadixSort::SortPairs(W.cubTmp, tb, W.hiKeys, W.hiKeysSorted, W.hiVals, S.I.hiList, n, 0, hiBits, st));
     }
     k_hi_start<<<(unsigned)((S.nPar + 1 + BS - 1) / BS), BS, 0, st>>>(W.hiKeysSorted, n, (int)S.nPar, S.I.hiStart);
-    if (n > 0) k_slots<<<(unsigned)((n + BS - 1) / BS), BS, 0, st>>>(S.C.key, S.C.flags, n, nAct, W.act, S.I);
+    if (n > 0) k_slots<<<(unsigned)((n + BS - 1) / BS), BS, 0, st>>>(S.C.key, S.C.flags, n, nAct, W.act, W.actSS, nAct - nSS, S.I);
     S.I.nAct = nAct;
+    S.nMixed = nAct - nSS;
     // every end starts without a contribution; the contact kernel fills the real ones this step
     const int64_t ne = 2 * std::max<int64_t>(nAct, 1);
     if (S.prec == WG_PREC_FP32) {
@@ -1172,11 +1231,8 @@ int collide_full_run(Sim& S) {
     }
     WG_CUDA_TRY(cudaMemsetAsync(W.heavyCount, 0, sizeof(int32_t) * 3, st));
     k_heavy<<<(unsigned)((S.nPar + BS - 1) / BS), BS, 0, st>>>(S.I, S.P, S.N.flags, kHeavyThreshold, W.heavyCount);
-    // contacts whose lo id is above every boundary particle join two spheres
-    if (S.maxBoundaryId >= 0) k_first_ss<<<1, 1, 0, st>>>(S.C.key, n, S.maxBoundaryId + 1, W.act, W.heavyCount + 2);
     WG_CUDA_TRY(cudaMemcpyAsync(W.hHeavy, W.heavyCount, sizeof(int32_t) * 3, cudaMemcpyDeviceToHost, st));
     WG_CUDA_TRY(cudaStreamSynchronize(st));
-    S.nMixed = W.hHeavy[2];
     S.I.nHeavy = S.cfg.apply_forces ? W.hHeavy[0] : 0;
     S.I.nHeavyFree = S.cfg.apply_forces ? W.hHeavy[1] : 0;
     WG_CUDA_TRY(cudaGetLastError());

@@ -44,6 +44,7 @@ struct ScenePar {
     float dtF, ssDfAbsF;  // FP32 copies read by the FP32-force kernels
     float gH[3], gL[3];   // gravity as double-float pairs (g = gH + gL)
     float dampingF, maxD2F;
+    long long stepBase;   // Scene.step of this scene = device step counter - stepBase
     // periodic cell, integrated on the host each step (core/Cell.cpp:81-120)
     double hSize[9], pprevHsize[9], gradV[9], nextGradV[9], dGradV[9], midGradV[9], shiftVelMat[9];
     double ImLL4hInv[9], IpLL4h[9], LmL[9], unshear[9];
@@ -70,6 +71,7 @@ struct DevNodes {
     float4* orif;   // FP32-force mode: the orientation (w x y z), in place of ori
     float2* rsplit; // FP32-force mode: the radius as a double-float pair (constant)
     float4 *lh, *ll; // FP32-force mode: the position mirror at the last full run (verlet reference)
+    int32_t* scene;  // batch of scenes: scene of each node slot (null: one scene)
 };
 struct DevParticles {
     int32_t n;
@@ -80,7 +82,11 @@ struct DevParticles {
     uint32_t* mask;
     double4_32a* mn;      // Aabb.min (verletDist included)
     double4_32a* mx;      // Aabb.max
+    int32_t* scene;       // batch of scenes: scene of each particle (null: one scene)
 };
+// the parameters of the scene a node or particle belongs to
+__device__ __forceinline__ int sceneOfP(const DevParticles& P, int p) { return P.scene ? P.scene[p] : 0; }
+__device__ __forceinline__ int sceneOfN(const DevNodes& N, int i) { return N.scene ? N.scene[i] : 0; }
 enum {
     CC_T0X, CC_T0Y, CC_T0Z, CC_T1X, CC_T1Y, CC_T1Z,  // L6Geom.trsf columns 0 and 1 (column 2 = c0 x c1)
     CC_CPX, CC_CPY, CC_CPZ,                          // L6Geom node position (contact point)
@@ -116,7 +122,8 @@ struct DevIncidence {
     int32_t* loStart;  // nPar+1: contacts with lo==p are [loStart[p], loStart[p+1])
     int32_t* hiStart;  // nPar+1: hiList[hiStart[p] .. hiStart[p+1]) are contacts with hi==p, ascending
     int32_t* hiList;
-    int4* work;        // active contacts in ascending index order: (contact, pA, pB, type|swap flag bits)
+    int4* work;        // active contacts (contact, pA, pB, type|swap flag bits): those that are not
+                       // sphere-sphere first, then the sphere-sphere ones, each in ascending order
     int64_t nAct;
     int32_t* slotLo;   // per contact: end slot of its lo particle (-1: no slot, the contact is inactive)
     int32_t* slotHi;   // per contact: end slot of its hi particle
@@ -164,7 +171,8 @@ __host__ __device__ inline void unpackCellDist(int32_t p, int& a, int& b, int& c
 void launch_leapfrog(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const ScenePar* sp,
                      int* dFlags, int fromEnds);
 void launch_contact_fp64(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C,
-                         const DevIncidence& I, const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dFlags);
+                         const DevIncidence& I, const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dFlags,
+                         int block = 128);
 // perStep: only the heavy particles with a free DOF (guarded by the flags), before Leapfrog;
 // otherwise every particle's DemData.force/torque (reporting at the end of a run).
 void launch_forces(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const ScenePar* sp,
@@ -177,9 +185,9 @@ int launch_stress(cudaStream_t st, const DevNodes& N, const DevParticles& P, con
 // FP32-force mode (wg_step32.cu)
 void launch_leapfrog32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const NodeConst32* nc,
                        const ScenePar* sp, int* dFlags, int fromEnds);
-// The kernels walk the active contacts I.work[0, I.nAct). Ranks [0, nMixed) may be of any type;
-// [nMixed, I.nAct) join two spheres (both ids above every boundary particle) and, in an aperiodic
-// scene, go to a sphere-sphere-only kernel.
+// The kernels walk the active contacts I.work[0, I.nAct). Items [0, nMixed) are facet and wall
+// contacts; [nMixed, I.nAct) join two spheres and, in an aperiodic scene, go to a
+// sphere-sphere-only kernel.
 // With a side stream the mixed range runs beside the sphere-sphere range (joined on st).
 struct SideStream {
     cudaStream_t st = nullptr;
@@ -187,7 +195,7 @@ struct SideStream {
 };
 void launch_contact_fp32(cudaStream_t st, const SideStream& side, const DevNodes& N, const DevParticles& P, const DevContacts& C,
                          const DevIncidence& I, const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dFlags,
-                         int64_t nMixed, bool periodic);
+                         int64_t nMixed, bool periodic, int block = 256);
 void launch_forces32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const NodeConst32* nc,
                      const ScenePar* sp, const int* dFlags, bool perStep);
 
@@ -196,6 +204,7 @@ struct Grid {
     double ox, oy, oz, h;
     int32_t nx, ny, nz;
     int64_t ncell;
+    int64_t base;  // first cell key of this grid (a batch of scenes has one grid per scene)
 };
 struct CollideWork;  // scratch owned by the simulation
 struct Sim;
@@ -233,13 +242,19 @@ struct Sim {
     DevContacts C{}, Cb{};  // current and spare (merge target)
     DevIncidence I{};
     int64_t cCap = 0;
-    int64_t nMixed = 0;   // active ranks [0, nMixed) may involve a boundary particle (see launch_contact_fp32)
-    int32_t maxBoundaryId = -1;  // largest id of a non-sphere particle
+    int64_t nMixed = 0;   // work items [0, nMixed) are not sphere-sphere (see launch_contact_fp32)
     double4_32a* dMats = nullptr;
     NodeConst32* dNodeC = nullptr;  // per node slot (FP32-force mode)
     int prec = 0;                  // WG_PREC_*
     ScenePar hPar{};
-    ScenePar* dPar = nullptr;
+    ScenePar* dPar = nullptr;  // one per scene
+    // batch of independent scenes: scene k owns particles [sceneStart[k], sceneStart[k+1])
+    int nScenes = 1;
+    std::vector<wg_config> cfgs;
+    std::vector<int64_t> sceneStart;
+    std::vector<int32_t> hSceneOfPar;  // empty for one scene
+    std::vector<ScenePar> hPars;
+    std::vector<double> sceneTime0;    // Scene.time of each scene at upload
     long long* dStep = nullptr;
     int* dFlags = nullptr;   // [0] full run requested, [1] error code
     int* hFlags = nullptr;   // pinned mirror
@@ -250,6 +265,15 @@ struct Sim {
     double time = 0;
     int64_t nFullRuns = 0;
     bool fromEnds = false;   // the end slots hold the forces of the last contact loop
+    // launch shape (wg_set_launch): threads per block of the contact kernels, steps queued per host
+    // check, and whether a chunk of steps is replayed as a CUDA graph
+    int contactBlock = 0;    // 0: default (256 FP32, 128 FP64)
+    int chunkSteps = 32;
+    bool useGraph = false;
+    cudaGraphExec_t graphExec = nullptr;
+    int64_t graphSteps = 0;  // steps in the captured chunk, 0: none valid
+    int64_t graphEpoch = -1; // nFullRuns when it was captured
+    int64_t graphLaunches = 0;
     double* dStress = nullptr;       // 9 doubles + per-block partials
     int64_t stressCap = 0;
     double stress[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // ContactLoop.stress of the last step
@@ -265,6 +289,7 @@ struct Sim {
     int fail(int code, const std::string& m) { err = m; return code; }
     int upload();
     int prepareParams();
+    int prepareParamsFor(const wg_config& c, int64_t p0, int64_t p1, ScenePar& out);
     int run(int64_t n);
     int checkErr();
     int ensureContactCapacity(int64_t need);

@@ -31,7 +31,7 @@ __global__ void __launch_bounds__(256) k_leapfrog(DevNodes N, DevParticles P, De
     if (halted(dFlags)) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < N.n;
-    const ScenePar& sp = *spp;
+    const ScenePar& sp = spp[valid ? sceneOfN(N, i) : 0];
     const int nPar = P.n;
     const uint32_t flags = valid ? N.flags[i] : 0u;
     const double4_32a mi = valid ? N.minert[i] : make_double4_32a(0., 0., 0., 0.);
@@ -191,7 +191,7 @@ __global__ void __launch_bounds__(128) k_contact_fp64(DevNodes N, DevParticles P
     const int4 wk = I.work[rk];
     const int64_t c = wk.x;
     const int A = wk.y, B = wk.z;
-    const ScenePar& sp = *spp;
+    const ScenePar& sp = spp[sceneOfP(P, B)];
     uint32_t fl = C.flags[c];
     if (fl & C_REMOVED) return;
     if ((fl & C_PENDING) && !pendingStays(P, A, B, sp.periodic, sp.cellSize, dErr)) {
@@ -201,7 +201,7 @@ __global__ void __launch_bounds__(128) k_contact_fp64(DevNodes N, DevParticles P
     fl &= ~C_PENDING;
     const uint32_t ty = ctype((uint32_t)wk.w);
     const bool real = fl & C_REAL;
-    const long long step = *dStep;
+    const long long step = *dStep - sp.stepBase;
     const double dt = sp.dt;
     D3 shift2{0, 0, 0}, shiftVel2{0, 0, 0};
     if (sp.periodic) {
@@ -419,8 +419,8 @@ __global__ void __launch_bounds__(128) k_contact_fp64(DevNodes N, DevParticles P
 }
 
 void launch_contact_fp64(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C, const DevIncidence& I,
-                         const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dFlags) {
-    const int bs = 128;
+                         const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dFlags, int block) {
+    const int bs = block;
     // launched even without contacts: it raises FL_HALT when a full run is due
     k_contact_fp64<<<(unsigned)std::max<int64_t>(1, (I.nAct + bs - 1) / bs), bs, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags);
 }
@@ -432,7 +432,7 @@ void launch_contact_fp64(cudaStream_t st, const DevNodes& N, const DevParticles&
 __global__ void __launch_bounds__(256) k_forces(DevNodes N, DevParticles P, DevIncidence I, const ScenePar* __restrict__ spp) {
     __shared__ EndStage<double4_32a, double2, 32> stage[8];
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    const ScenePar& sp = *spp;
+    const ScenePar& sp = spp[p < P.n ? sceneOfP(P, p) : 0];
     const bool uni = p < P.n && P.shape[p] != WG_SHAPE_FACET;
     int e0 = 0, e1 = 0;
     bool take = false;
@@ -460,7 +460,7 @@ __global__ void k_forces_heavy(DevNodes N, DevIncidence I, const int32_t* __rest
                                const int* __restrict__ dFlags) {
     if (dFlags && halted(dFlags)) return;
     const int p = list[blockIdx.x];
-    const ScenePar& sp = *spp;
+    const ScenePar& sp = spp[sceneOfN(N, p)];
     int e0, e1;
     endRange(I, p, e0, e1);
     D3 F{0, 0, 0}, T{0, 0, 0};

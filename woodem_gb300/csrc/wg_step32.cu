@@ -90,7 +90,7 @@ __global__ void __launch_bounds__(256) k_leapfrog32(DevNodes N, DevParticles P, 
     if (halted(dFlags)) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < N.n;
-    const ScenePar& sp = *spp;
+    const ScenePar& sp = spp[valid ? sceneOfN(N, i) : 0];
     NodeConst32 nc{0.f, {0.f, 0.f, 0.f}, 0.f, 0.f, 0u, 0u};
     double4_32a pr = make_double4_32a(0., 0., 0., 0.), v4 = pr, w4 = pr;
     float4 lh = make_float4(0.f, 0.f, 0.f, 0.f), ll = lh;
@@ -367,7 +367,7 @@ __global__ void __launch_bounds__(256, SSONLY ? 4 : 1) k_contact_fp32(DevNodes N
     const int4 wk = I.work[rk];
     const int64_t c = wk.x;
     const int A = wk.y, B = wk.z;
-    const ScenePar& sp = *spp;
+    const ScenePar& sp = spp[sceneOfP(P, B)];
     uint32_t fl = C.flags[c];
     if (fl & C_REMOVED) return;
     if ((fl & C_PENDING) && !pendingStays(P, A, B, sp.periodic, sp.cellSize, dErr)) {
@@ -377,7 +377,7 @@ __global__ void __launch_bounds__(256, SSONLY ? 4 : 1) k_contact_fp32(DevNodes N
     fl &= ~C_PENDING;
     const uint32_t ty = ctype((uint32_t)wk.w);
     const bool real = fl & C_REAL;
-    const long long step = *dStep;
+    const long long step = *dStep - sp.stepBase;
     const double dt = sp.dt;
     const float dtf = sp.dtF;
     bool shifted = false;
@@ -609,16 +609,17 @@ __global__ void __launch_bounds__(256, SSONLY ? 4 : 1) k_contact_fp32(DevNodes N
 
 void launch_contact_fp32(cudaStream_t st, const SideStream& side, const DevNodes& N, const DevParticles& P, const DevContacts& C,
                          const DevIncidence& I, const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dFlags,
-                         int64_t nMixed, bool periodic) {
+                         int64_t nMixed, bool periodic, int block) {
     const int64_t nm = periodic ? I.nAct : std::min<int64_t>(nMixed, I.nAct);
     const int64_t ns = I.nAct - nm;
+    const int64_t bs = block;
     if (ns > 0 && nm > 0 && side.st) {
         // the mixed range (facets and walls, FP64 geometry) beside the sphere-sphere range; the
         // sphere-sphere launch raises FL_HALT when a full run is due
         cudaEventRecord(side.fork, st);
         cudaStreamWaitEvent(side.st, side.fork, 0);
         k_contact_fp32<false><<<(unsigned)((nm + 255) / 256), 256, 0, side.st>>>(N, P, C, I, mats, sp, dStep, dFlags, 0, nm, 0);
-        k_contact_fp32<true><<<(unsigned)((ns + 255) / 256), 256, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags, nm, I.nAct, 1);
+        k_contact_fp32<true><<<(unsigned)((ns + bs - 1) / bs), (unsigned)bs, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags, nm, I.nAct, 1);
         cudaEventRecord(side.join, side.st);
         cudaStreamWaitEvent(st, side.join, 0);
         return;
@@ -627,7 +628,7 @@ void launch_contact_fp32(cudaStream_t st, const SideStream& side, const DevNodes
     k_contact_fp32<false><<<(unsigned)std::max<int64_t>(1, (nm + 255) / 256), 256, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags,
                                                                                           0, nm, 1);
     if (ns > 0)
-        k_contact_fp32<true><<<(unsigned)((ns + 255) / 256), 256, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags, nm, I.nAct, 0);
+        k_contact_fp32<true><<<(unsigned)((ns + bs - 1) / bs), (unsigned)bs, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags, nm, I.nAct, 0);
 }
 
 // ---------------------------------------------------------------------------------- force sum
@@ -638,7 +639,7 @@ __global__ void __launch_bounds__(256) k_forces32(DevNodes N, DevParticles P, De
                                                   const ScenePar* __restrict__ spp) {
     __shared__ EndStage<float4, float2, 128> stage[8];
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    const ScenePar& sp = *spp;
+    const ScenePar& sp = spp[p < P.n ? sceneOfP(P, p) : 0];
     const bool uni = p < P.n && P.shape[p] != WG_SHAPE_FACET;
     int e0 = 0, e1 = 0;
     bool take = false;
@@ -662,7 +663,7 @@ __global__ void k_forces32_heavy(DevNodes N, DevIncidence I, const int32_t* __re
                                  const int* __restrict__ dFlags) {
     if (dFlags && halted(dFlags)) return;
     const int p = list[blockIdx.x];
-    const ScenePar& sp = *spp;
+    const ScenePar& sp = spp[sceneOfN(N, p)];
     int e0, e1;
     endRange(I, p, e0, e1);
     D3 F{0, 0, 0}, T{0, 0, 0};

@@ -248,3 +248,35 @@ def periodic_shear(n=200_000, seed=0, rmin=2e-3, rmax=4e-3, density=2600.0, youn
     g[0, 2] = shear_rate
     S.cell.nextGradV = g
     return S
+
+
+def box_settle_scaled(n, radius, seed=0, density=3000.0, young=1e7, tanPhi=0.5, ktDivKn=0.2, damping=0.2, verletRel=0.1,
+                      precision="fp64"):
+    """A box settle of ``n`` spheres of one ``radius``: the lattice of the 10k-sphere box settle (pitch
+    2.4 radius, jitter 0.2 radius, two stacked layers per column of the square footprint) in a box
+    with a free column of three pitches around it and twice the lattice height."""
+    pitch = 2.4 * radius
+    side = int(math.ceil((n / 2.0) ** (1 / 3.0)))
+    dims = (side, side, int(math.ceil(n / float(side * side))))
+    w = (dims[0] + 3) * pitch
+    h = 2 * (dims[2] + 3) * pitch
+    return box_settle(n=n, seed=seed, radius=radius, pitch=pitch, dims=dims, box=((0, 0, 0), (w, w, h)), density=density,
+                      young=young, ktDivKn=ktDivKn, tanPhi=tanPhi, damping=damping, verletRel=verletRel, jitter=0.2 * radius,
+                      precision=precision)
+
+
+def batch_study(n_scenes=256, seed=0, nmin=1000, nmax=50000, rmin=3e-3, rmax=6e-3, precision="fp64"):
+    """Parametric study of independent box settles: sphere counts log-uniform in [nmin, nmax], one
+    radius per scene uniform in [rmin, rmax], tanPhi log-uniform in [0.2, 0.8], young log-uniform in
+    [1e6, 1e8] Pa, Leapfrog damping uniform in [0, 0.4]; each scene is a ``box_settle_scaled``.
+    Returns the list of scenes and the table of their parameters."""
+    rng = np.random.default_rng(seed)
+    n = np.exp(rng.uniform(math.log(nmin), math.log(nmax), n_scenes)).astype(int)
+    r = rng.uniform(rmin, rmax, n_scenes)
+    tp = np.exp(rng.uniform(math.log(0.2), math.log(0.8), n_scenes))
+    E = np.exp(rng.uniform(math.log(1e6), math.log(1e8), n_scenes))
+    d = rng.uniform(0.0, 0.4, n_scenes)
+    scenes = [box_settle_scaled(int(n[k]), float(r[k]), seed=seed * 1000 + k, young=float(E[k]), tanPhi=float(tp[k]),
+                                damping=float(d[k]), precision=precision) for k in range(n_scenes)]
+    table = {"n": n, "radius": r, "tanPhi": tp, "young": E, "damping": d}
+    return scenes, table

@@ -1,0 +1,55 @@
+"""Autotuner of the launch shape of a device simulation.
+
+The results of a simulation do not depend on the launch shape (threads per block of the contact
+kernels, steps queued per host check of the collider request, CUDA-graph replay of such a chunk of
+steps): every contact and every particle is updated by the same operations in the same order.
+The tuner therefore measures candidate shapes on real steps of the simulation it tunes (the steps
+count as part of the run) and keeps the fastest.
+"""
+import ctypes as C
+
+import numpy as np
+
+DEFAULT_CANDIDATES = (
+    # (contact threads per block, steps per chunk, CUDA graph)
+    (256, 32, False),
+    (128, 32, False),
+    (256, 8, True),
+    (256, 32, True),
+    (128, 32, True),
+    (256, 64, True),
+)
+
+
+def _handle(sim):
+    return sim.H.L, sim.H.h
+
+
+def set_launch(sim, block=0, chunk=32, graph=False):
+    L, h = _handle(sim)
+    sim.H.check(L.wg_set_launch(h, int(block), int(chunk), int(bool(graph))), "set_launch")
+
+
+def _run_ms(sim, steps):
+    sim.run(steps)
+    L, h = _handle(sim)
+    tot = C.c_double()
+    ph = np.zeros(4)
+    nl = C.c_int64()
+    L.wg_get_timing(h, C.byref(tot), ph.ctypes.data_as(C.POINTER(C.c_double)), C.byref(nl))
+    return tot.value
+
+
+def autotune(sim, trial_steps=64, candidates=DEFAULT_CANDIDATES, rounds=2):
+    """Time ``trial_steps`` steps of ``sim`` (a Simulation or a Batch) with each candidate launch
+    shape, ``rounds`` times in turn (the median counts), set the fastest and return
+    (best, {candidate: ms per step})."""
+    times = {c: [] for c in candidates}
+    for _ in range(rounds):
+        for c in candidates:
+            set_launch(sim, *c)
+            times[c].append(_run_ms(sim, trial_steps) / trial_steps)
+    med = {c: float(np.median(v)) for c, v in times.items()}
+    best = min(med, key=med.get)
+    set_launch(sim, *best)
+    return best, med
