@@ -293,6 +293,67 @@ def measure_batch(args):
     return out
 
 
+def measure_serving(args):
+    """Serving loop on a seeded Poisson stream of jobs (box settles and periodic shears with
+    probability 0.5, sizes log-uniform, step counts uniform; sizes and step counts scaled down from
+    the 10-minute stream so that the run stays within the benchmark's time): continuous batching
+    (SlotPool + periodic jobs on their own streams) against the same stream served one job at a
+    time, each with the same arrival times; p50/p99 latency (queueing included), jobs/s,
+    particle-steps/s."""
+    from woodem_gb300 import scenes, _plan, serve
+    prec = "fp32"
+    rate, horizon = args.serve_rate, args.serve_seconds
+    nmin, nmax, smin, smax = 2000, 30000, 2000, 5000
+
+    def make_box(n, seed):
+        r = 3e-3 + 3e-3 * ((seed % 1000) / 1000.0)
+        return scenes.box_settle_scaled(n, r, seed=seed % 100000, precision=prec)
+
+    def make_peri(n, seed):
+        S = scenes.periodic_shear(n=n, seed=seed % 100000, fill_fraction=0.4, shear_rate=1.0, precision=prec)
+        return S
+
+    def stream():
+        return serve.poisson_jobs(rate, horizon, args.seed + 5, make_box, make_peri, nmin, nmax, smin, smax)
+
+    out = {"arrival_rate_jobs_per_s": rate, "arrivals_seconds": horizon, "sizes": [nmin, nmax], "steps": [smin, smax],
+           "precision": prec, "stream": "seeded Poisson, p(periodic shear)=0.5, p(box settle)=0.5"}
+    template = _plan.compile_scene(make_box(2000, 1))
+    caps = [32000] * 4 + [12000] * 8 + [4000] * 8
+    pool = serve.SlotPool(caps, precision=prec, template=template)
+    srv = serve.Server(pool, hbm_budget=150e9, tick=250, max_periodic=4, clock="wall")
+    jobs = stream()
+    done = srv.run(jobs, horizon=horizon * 3)
+    pool.close()
+    el = srv.elapsed
+    out["continuous_batching"] = dict(serve.latency_stats(done), jobs=len(jobs), finished=len(done), seconds=el,
+                                      jobs_per_s=len(done) / el, particle_steps_per_s=srv.particle_steps / el,
+                                      slots=len(caps), slot_capacities=sorted(set(caps)))
+    log("serving: batched %d/%d jobs in %.1fs" % (len(done), len(jobs), el))
+    # one job at a time, same arrivals, FIFO
+    jobs = stream()
+    t0 = time.perf_counter()
+    fin, psteps = [], 0.0
+    for j in jobs:
+        now = time.perf_counter() - t0
+        if now < j.arrival:
+            time.sleep(j.arrival - now)
+        if time.perf_counter() - t0 > horizon * 3:
+            break
+        S = j.build()
+        S.run(j.steps)
+        S.sync()
+        S.close()
+        j.end = time.perf_counter() - t0
+        fin.append(j)
+        psteps += j.n * j.steps
+    el = time.perf_counter() - t0
+    out["one_at_a_time"] = dict(serve.latency_stats(fin), jobs=len(jobs), finished=len(fin), seconds=el, jobs_per_s=len(fin) / el,
+                                particle_steps_per_s=psteps / el)
+    log("serving: one at a time %d/%d jobs in %.1fs" % (len(fin), len(jobs), el))
+    return out
+
+
 def peaks():
     try:
         with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
@@ -324,6 +385,9 @@ def main():
     ap.add_argument("--batch-scenes", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=200)
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--serve-rate", type=float, default=8.0, help="serving: job arrivals per second")
+    ap.add_argument("--serve-seconds", type=float, default=15.0, help="serving: arrivals over this many seconds")
+    ap.add_argument("--no-serve", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = env_rank()
@@ -425,6 +489,8 @@ def main():
                        "call": "wg_run_host(1 step) with page-locked host state"}
     if rank == 0 and not args.no_batch:
         line["batch"] = measure_batch(args)
+    if rank == 0 and not args.no_serve:
+        line["serving"] = measure_serving(args)
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
         v, steps, n, el = cpu_sample(args, args.cpu_seconds, threads)

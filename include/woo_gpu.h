@@ -116,6 +116,23 @@ int wg_set_scenes(wg_scene* s, int32_t n_scenes, const wg_config* cfgs, const in
    and use_graph != 0 to replay each such chunk of steps as one CUDA graph. Results do not depend
    on these; only the speed does. */
 int wg_set_launch(wg_scene* s, int32_t contact_block, int32_t chunk_steps, int32_t use_graph);
+/* Serving slots (no counterpart in the reference): the scenes of a batch (wg_set_scenes) are slots
+   whose particle ranges bound the jobs they can hold. wg_slot_load puts a job (an aperiodic scene
+   of n spheres and walls, its configuration, its n_mat materials indexed 0..n_mat-1, its step
+   count) into slot k in place of whatever the slot held: the other slots keep running and keep
+   their contacts; the job runs n_steps steps from the next one on and then stays frozen.
+   wg_slot_clear empties slot k. wg_slot_status reports the steps a slot's job has done.
+   wg_get_slot_nodes copies the state of the first n nodes of slot k. */
+int wg_slot_load(wg_scene* s, int32_t k, const wg_config* cfg, int64_t n, const double* pos, const double* ori,
+                 const double* vel, const double* ang_vel, const double* mass, const double* inertia,
+                 const uint32_t* flags, const int32_t* shape, const double* radius, const int32_t* wall_axis,
+                 const int32_t* wall_sense, const int32_t* mat, const uint32_t* mask, int32_t n_mat,
+                 const double* density, const double* young, const double* tan_phi, const double* kt_div_kn,
+                 int64_t n_steps);
+int wg_slot_clear(wg_scene* s, int32_t k);
+int wg_slot_status(wg_scene* s, int32_t k, int64_t* steps_done, int64_t* steps_end);
+int wg_get_slot_nodes(wg_scene* s, int32_t k, int64_t n, double* pos, double* ori, double* vel, double* ang_vel,
+                      double* force, double* torque);
 /* Scene.step, Scene.time and the contacts (counted by their lower particle id) of scene k. */
 int wg_get_scene_stats(wg_scene* s, int32_t k, wg_stats* out);
 int wg_set_materials(wg_scene* s, int32_t n, const double* density, const double* young,

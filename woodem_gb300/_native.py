@@ -82,6 +82,11 @@ def lib():
         "wg_set_scenes": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.POINTER(C.c_int64)]),
         "wg_get_scene_stats": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
         "wg_set_launch": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
+        "wg_slot_load": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64, P_D, P_D, P_D, P_D, P_D, P_D, P_U32, P_I32, P_D,
+                                   P_I32, P_I32, P_I32, P_U32, C.c_int32, P_D, P_D, P_D, P_D, C.c_int64]),
+        "wg_slot_clear": (C.c_int, [C.c_void_p, C.c_int32]),
+        "wg_slot_status": (C.c_int, [C.c_void_p, C.c_int32, P_I64, P_I64]),
+        "wg_get_slot_nodes": (C.c_int, [C.c_void_p, C.c_int32, C.c_int64, P_D, P_D, P_D, P_D, P_D, P_D]),
         "wg_get_cell": (C.c_int, [C.c_void_p, P_D, P_D, P_D]),
         "wg_num_contacts": (C.c_int64, [C.c_void_p]),
         "wg_get_contacts": (C.c_int, [C.c_void_p, P_I32, P_I32, P_I32, P_I32, P_I32, P_D, P_D, P_D, P_D]),

@@ -260,7 +260,15 @@ int Sim::ensureContactCapacity(int64_t need) {
 }
 
 int Sim::prepareParams() {
-    if (nScenes <= 1) return prepareParamsFor(cfg, 0, nPar, hPar);
+    if (nScenes <= 1) {
+        // a single scene is also a batch of one (serving slots address it as scene 0)
+        int r = prepareParamsFor(cfg, 0, nPar, hPar);
+        hPars.assign(1, hPar);
+        cfgs.assign(1, cfg);
+        sceneStart = {0, nPar};
+        sceneTime0.assign(1, 0.0);
+        return r;
+    }
     hPars.resize(nScenes);
     for (int k = 0; k < nScenes; k++) prepareParamsFor(cfgs[k], sceneStart[k], sceneStart[k + 1], hPars[k]);
     hPar = hPars[0];
@@ -273,6 +281,7 @@ int Sim::prepareParamsFor(const wg_config& cfg, int64_t p0, int64_t p1, ScenePar
     SimEx& X = static_cast<SimEx&>(*this);
     std::memset(&p, 0, sizeof(p));
     p.stepBase = 0;
+    p.stepEnd = (long long)1 << 62;
     p.dt = cfg.dt;
     for (int i = 0; i < 3; i++) p.g[i] = cfg.gravity[i];
     p.hasGravity = (cfg.gravity[0] != 0 || cfg.gravity[1] != 0 || cfg.gravity[2] != 0);
@@ -669,8 +678,8 @@ int Sim::run(int64_t n) {
             else launch_forces(stream, N, P, I, dPar, dFlags, true);
             launches += I.nHeavyFree > 0;
         }
-        if (fp32) launch_leapfrog32(stream, N, P, I, dNodeC, dPar, dFlags, fromEndsArg);
-        else launch_leapfrog(stream, N, P, I, dPar, dFlags, fromEndsArg);
+        if (fp32) launch_leapfrog32(stream, N, P, I, dNodeC, dPar, dFlags, fromEndsArg, dStep);
+        else launch_leapfrog(stream, N, P, I, dPar, dFlags, fromEndsArg, dStep);
         launches++;
     };
     auto stepContact = [&]() {
@@ -686,7 +695,7 @@ int Sim::run(int64_t n) {
     int64_t done = 0;
     while (done < n) {
         const int64_t k = std::min<int64_t>(n - done, maxChunk);
-        const bool needFull = !initialized || anyZeroVd;
+        const bool needFull = !initialized || anyZeroVd || forceFull;
         k_set_flags<<<1, 1, 0, stream>>>(dFlags, needFull ? 1 : 0);
         if (cfg.periodic) {
             X.cell.integrateAndUpdate(cfg.dt);
@@ -756,6 +765,7 @@ int Sim::run(int64_t n) {
             int r = collide_full_run(*this);
             if (r) return r;
             initialized = true;
+            forceFull = false;
             launches += 12;
             WG_CUDA_TRY(cudaEventRecord(E[3 * maxChunk + 1], stream));
             k_set_flags<<<1, 1, 0, stream>>>(dFlags, 0);
@@ -886,6 +896,240 @@ int wg_set_scenes(wg_scene* s, int32_t n_scenes, const wg_config* cfgs, const in
     S.sceneTime0.assign(n_scenes, 0.0);
     S.cfg = cfgs[0];
     S.haveCfg = true;
+    return WG_OK;
+}
+
+// ------------------------------------------------------------------ serving slots
+namespace wg {
+// Writes particles [p0, p0 + cap) of a slot (uninodal: node slot = particle): the first n from the
+// job's arrays, the rest parked (blocked, at rest, left out of the collider).
+static int writeSlot(Sim& S, int64_t p0, int64_t cap, int64_t n, const double* pos, const double* ori, const double* vel,
+                     const double* angv, const double* mass, const double* inertia, const uint32_t* flags, const int32_t* shape,
+                     const double* radius, const int32_t* axis, const int32_t* sense, const int32_t* mat, int32_t matBase,
+                     const uint32_t* mask) {
+    std::vector<double4_32a> posr(cap), v4(cap), w4(cap), o4(cap), zero(cap), mi(cap);
+    std::vector<uint32_t> fl(cap), mk(cap);
+    std::vector<int32_t> sh(cap), mt(cap);
+    std::vector<int4> aux(cap);
+    std::vector<double4_32a> fac(cap);
+    for (int64_t q = 0; q < cap; q++) {
+        const int64_t p = p0 + q;
+        zero[q] = make_double4_32a(0, 0, 0, 0);
+        fac[q] = zero[q];
+        aux[q] = make_int4(0, 0, 0, 0);
+        if (q < n) {
+            sh[q] = shape[q];
+            const double r = shape[q] == WG_SHAPE_SPHERE ? radius[q] : 0.;
+            posr[q] = make_double4_32a(pos[3 * q], pos[3 * q + 1], pos[3 * q + 2], r);
+            v4[q] = make_double4_32a(vel[3 * q], vel[3 * q + 1], vel[3 * q + 2], 0);
+            w4[q] = make_double4_32a(angv[3 * q], angv[3 * q + 1], angv[3 * q + 2], 0);
+            o4[q] = make_double4_32a(ori[4 * q], ori[4 * q + 1], ori[4 * q + 2], ori[4 * q + 3]);
+            mi[q] = make_double4_32a(inertia[3 * q], inertia[3 * q + 1], inertia[3 * q + 2], mass[q]);
+            fl[q] = flags[q];
+            mt[q] = matBase + mat[q];
+            mk[q] = mask[q];
+            if (shape[q] == WG_SHAPE_WALL) aux[q] = make_int4(axis[q], sense[q], 0, 0);
+        } else {
+            sh[q] = WG_SHAPE_SPHERE;
+            posr[q] = make_double4_32a(0, 0, 0, 0);
+            v4[q] = w4[q] = zero[q];
+            o4[q] = make_double4_32a(1, 0, 0, 0);
+            mi[q] = make_double4_32a(1, 1, 1, 1);
+            fl[q] = F_DOF_ALL;
+            mt[q] = matBase;
+            mk[q] = 0;
+        }
+        S.hShape[p] = sh[q];
+        S.hRadius[p] = posr[q].w;
+        S.hAxis[p] = aux[q].x;
+        S.hSense[p] = aux[q].y;
+        S.hMat[p] = mt[q];
+        S.hMask[p] = mk[q];
+        S.hParked[p] = q < n ? 0 : 1;
+    }
+    auto put = [&](void* dst, const void* src, size_t bytes) -> int {
+        return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, S.stream) == cudaSuccess ? 0 : -1;
+    };
+    const size_t d4 = sizeof(double4_32a);
+    if (put(S.N.posr + p0, posr.data(), d4 * cap) || put(S.N.vel + p0, v4.data(), d4 * cap) || put(S.N.angv + p0, w4.data(), d4 * cap) ||
+        put(S.N.ori + p0, o4.data(), d4 * cap) || put(S.N.force + p0, zero.data(), d4 * cap) || put(S.N.torque + p0, zero.data(), d4 * cap) ||
+        put(S.N.minert + p0, mi.data(), d4 * cap) || put(S.N.lastPos + p0, posr.data(), d4 * cap) ||
+        put(S.N.flags + p0, fl.data(), sizeof(uint32_t) * cap) || put(S.P.shape + p0, sh.data(), sizeof(int32_t) * cap) ||
+        put(S.P.aux + p0, aux.data(), sizeof(int4) * cap) || put(S.P.facet + p0, fac.data(), d4 * cap) ||
+        put(S.P.mat + p0, mt.data(), sizeof(int32_t) * cap) || put(S.P.mask + p0, mk.data(), sizeof(uint32_t) * cap))
+        return S.fail(WG_ERR_CUDA, "slot upload failed");
+    if (S.prec == WG_PREC_FP32) {
+        std::vector<NodeConst32> nc(cap);
+        std::vector<float4> ph(cap), pl(cap), vh(cap), vl(cap), of(cap);
+        std::vector<float> wz(cap);
+        std::vector<float2> rs(cap);
+        auto split = [](double x, float& h, float& l) {
+            h = (float)x;
+            l = (float)(x - (double)h);
+        };
+        for (int64_t q = 0; q < cap; q++) {
+            const double4_32a m = mi[q];
+            nc[q].invMass = m.w != 0 ? (float)(1. / m.w) : 0.f;
+            nc[q].invI[0] = m.x != 0 ? (float)(1. / m.x) : 0.f;
+            nc[q].invI[1] = m.y != 0 ? (float)(1. / m.y) : 0.f;
+            nc[q].invI[2] = m.z != 0 ? (float)(1. / m.z) : 0.f;
+            nc[q].mh = (float)m.w;
+            nc[q].ml = (float)(m.w - (double)nc[q].mh);
+            nc[q].flags = fl[q];
+            nc[q]._pad = 0;
+            split(posr[q].x, ph[q].x, pl[q].x);
+            split(posr[q].y, ph[q].y, pl[q].y);
+            split(posr[q].z, ph[q].z, pl[q].z);
+            split(posr[q].w, ph[q].w, pl[q].w);
+            split(v4[q].x, vh[q].x, vl[q].x);
+            split(v4[q].y, vh[q].y, vl[q].y);
+            split(v4[q].z, vh[q].z, vl[q].z);
+            vh[q].w = (float)w4[q].x;
+            vl[q].w = (float)w4[q].y;
+            wz[q] = (float)w4[q].z;
+            of[q] = make_float4((float)o4[q].x, (float)o4[q].y, (float)o4[q].z, (float)o4[q].w);
+            rs[q] = make_float2(ph[q].w, pl[q].w);
+        }
+        if (put(S.dNodeC + p0, nc.data(), sizeof(NodeConst32) * cap) || put(S.N.ph + p0, ph.data(), sizeof(float4) * cap) ||
+            put(S.N.pl + p0, pl.data(), sizeof(float4) * cap) || put(S.N.vh + p0, vh.data(), sizeof(float4) * cap) ||
+            put(S.N.vl + p0, vl.data(), sizeof(float4) * cap) || put(S.N.wz + p0, wz.data(), sizeof(float) * cap) ||
+            put(S.N.orif + p0, of.data(), sizeof(float4) * cap) || put(S.N.rsplit + p0, rs.data(), sizeof(float2) * cap) ||
+            put(S.N.lh + p0, ph.data(), sizeof(float4) * cap) || put(S.N.ll + p0, pl.data(), sizeof(float4) * cap))
+            return S.fail(WG_ERR_CUDA, "slot upload failed");
+    }
+    // the slot's contacts end at the next full run; its nodes take their stored force first
+    if (cudaMemsetAsync(S.P.fresh + p0, 1, cap, S.stream) != cudaSuccess || cudaMemsetAsync(S.N.fresh + p0, 1, cap, S.stream) != cudaSuccess)
+        return S.fail(WG_ERR_CUDA, "slot upload failed");
+    if (cudaStreamSynchronize(S.stream) != cudaSuccess) return S.fail(WG_ERR_CUDA, "slot upload failed");
+    S.listsDirty = true;
+    S.forceFull = true;
+    return 0;
+}
+
+static int slotCheck(Sim& S, int32_t k) {
+    if (S.nScenes < 1 || k < 0 || k >= S.nScenes || (int64_t)S.sceneStart.size() != S.nScenes + 1)
+        return S.fail(WG_ERR_ARG, "slot index out of range");
+    if (!S.uploaded) {
+        int r = S.upload();
+        if (r) return r;
+    }
+    if (S.cfg.periodic) return S.fail(WG_ERR_UNSUPPORTED, "serving slots hold aperiodic scenes");
+    for (int64_t p = S.sceneStart[k]; p < S.sceneStart[k + 1]; p++)
+        if (S.hShape[p] == WG_SHAPE_FACET) return S.fail(WG_ERR_UNSUPPORTED, "serving slots hold spheres and walls");
+    if (!S.P.fresh) {
+        S.P.fresh = (uint8_t*)S.dalloc(S.nPar);
+        S.N.fresh = (uint8_t*)S.dalloc(S.N.n);
+        if (!S.N.fresh) return S.fail(WG_ERR_CUDA, "out of device memory (slots)");
+        WG_CUDA_TRY(cudaMemset(S.P.fresh, 0, S.nPar));
+        WG_CUDA_TRY(cudaMemset(S.N.fresh, 0, S.N.n));
+    }
+    if (S.hParked.empty()) S.hParked.assign(S.nPar, 0);
+    return 0;
+}
+}  // namespace wg
+
+int wg_slot_load(wg_scene* s, int32_t k, const wg_config* c, int64_t n, const double* pos, const double* ori, const double* vel,
+                 const double* ang_vel, const double* mass, const double* inertia, const uint32_t* flags, const int32_t* shape,
+                 const double* radius, const int32_t* wall_axis, const int32_t* wall_sense, const int32_t* mat, const uint32_t* mask,
+                 int32_t n_mat, const double* density, const double* young, const double* tan_phi, const double* kt_div_kn,
+                 int64_t n_steps) {
+    if (!s || !c || n < 0 || n_steps < 0 || n_mat < 1) return WG_ERR_ARG;
+    Sim& S = *SIM(s);
+    int r = slotCheck(S, k);
+    if (r) return r;
+    const int64_t p0 = S.sceneStart[k], cap = S.sceneStart[k + 1] - p0;
+    if (n > cap) return S.fail(WG_ERR_CAPACITY, "job larger than the slot");
+    const int32_t matCap = (int32_t)(S.hDensity.size() / S.nScenes);
+    if (n_mat > matCap) return S.fail(WG_ERR_CAPACITY, "job has more materials than the slot");
+    if (c->precision != S.cfg.precision || c->periodic || c->lone_mask != S.cfg.lone_mask || c->apply_forces != S.cfg.apply_forces ||
+        !c->reset || !((c->phys == 0 && c->law == 0) || (c->phys == 1 && c->law == 1)) || (c->law == 1 && c->hz_alpha != 0) ||
+        !(c->dt > 0))
+        return S.fail(WG_ERR_UNSUPPORTED, "job configuration does not fit the serving batch");
+    for (int64_t q = 0; q < n; q++) {
+        if (shape[q] != WG_SHAPE_SPHERE && shape[q] != WG_SHAPE_WALL) return S.fail(WG_ERR_UNSUPPORTED, "serving slots hold spheres and walls");
+        if (mat[q] < 0 || mat[q] >= n_mat) return S.fail(WG_ERR_ARG, "particle material index out of range");
+    }
+    WG_CUDA_TRY(cudaSetDevice(S.device));
+    const int32_t matBase = k * matCap;
+    std::vector<double4_32a> mats(n_mat);
+    for (int m = 0; m < n_mat; m++) {
+        mats[m] = make_double4_32a(density[m], young[m], tan_phi[m], kt_div_kn[m]);
+        S.hDensity[matBase + m] = density[m];
+        S.hYoung[matBase + m] = young[m];
+        S.hTanPhi[matBase + m] = tan_phi[m];
+        S.hKtDivKn[matBase + m] = kt_div_kn[m];
+    }
+    WG_CUDA_TRY(cudaMemcpy(S.dMats + matBase, mats.data(), sizeof(double4_32a) * n_mat, cudaMemcpyHostToDevice));
+    r = writeSlot(S, p0, cap, n, pos, ori, vel, ang_vel, mass, inertia, flags, shape, radius, wall_axis, wall_sense, mat, matBase, mask);
+    if (r) return r;
+    S.cfgs[k] = *c;
+    S.prepareParamsFor(*c, p0, p0 + n, S.hPars[k]);
+    S.hPars[k].stepBase = (long long)S.step - (long long)c->step;
+    S.hPars[k].stepEnd = (long long)c->step + (long long)n_steps;
+    S.sceneTime0[k] = 0.;
+    if (k == 0) S.hPar = S.hPars[0];
+    WG_CUDA_TRY(cudaMemcpy(S.dPar + k, &S.hPars[k], sizeof(ScenePar), cudaMemcpyHostToDevice));
+    return WG_OK;
+}
+
+int wg_slot_clear(wg_scene* s, int32_t k) {
+    if (!s) return WG_ERR_ARG;
+    Sim& S = *SIM(s);
+    int r = slotCheck(S, k);
+    if (r) return r;
+    const int64_t p0 = S.sceneStart[k], cap = S.sceneStart[k + 1] - p0;
+    for (int64_t p = p0; p < p0 + cap; p++) S.hParked[p] = 1;
+    WG_CUDA_TRY(cudaMemset(S.P.fresh + p0, 1, cap));
+    S.hPars[k].stepEnd = -((long long)1 << 62);  // frozen
+    if (k == 0) S.hPar = S.hPars[0];
+    WG_CUDA_TRY(cudaMemcpy(S.dPar + k, &S.hPars[k], sizeof(ScenePar), cudaMemcpyHostToDevice));
+    S.listsDirty = true;
+    S.forceFull = true;
+    return WG_OK;
+}
+
+int wg_slot_status(wg_scene* s, int32_t k, int64_t* steps_done, int64_t* steps_end) {
+    if (!s) return WG_ERR_ARG;
+    Sim& S = *SIM(s);
+    if (k < 0 || k >= S.nScenes || (int64_t)S.hPars.size() != S.nScenes) return S.fail(WG_ERR_ARG, "slot index out of range");
+    const ScenePar& q = S.hPars[k];
+    const long long done = (long long)S.step - q.stepBase;
+    if (steps_done) *steps_done = std::min<long long>(done, std::max<long long>(q.stepEnd, 0));
+    if (steps_end) *steps_end = q.stepEnd;
+    return WG_OK;
+}
+
+int wg_get_slot_nodes(wg_scene* s, int32_t k, int64_t n, double* pos, double* ori, double* vel, double* ang_vel, double* force,
+                      double* torque) {
+    if (!s || n < 0) return WG_ERR_ARG;
+    Sim& S = *SIM(s);
+    if (k < 0 || k >= S.nScenes || !S.uploaded) return S.fail(WG_ERR_ARG, "slot index out of range");
+    const int64_t p0 = S.sceneStart[k];
+    if (n > S.sceneStart[k + 1] - p0) return S.fail(WG_ERR_ARG, "more nodes than the slot holds");
+    WG_CUDA_TRY(cudaStreamSynchronize(S.stream));
+    std::vector<double4_32a> a(n);
+    auto get = [&](const double4_32a* src, double* dst, int w) -> int {
+        if (!dst) return 0;
+        if (cudaMemcpy(a.data(), src + p0, sizeof(double4_32a) * n, cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+        for (int64_t q = 0; q < n; q++) {
+            const double v[4] = {a[q].x, a[q].y, a[q].z, a[q].w};
+            for (int j = 0; j < w; j++) dst[w * q + j] = v[j];
+        }
+        return 0;
+    };
+    if (get(S.N.posr, pos, 3) || get(S.N.vel, vel, 3) || get(S.N.angv, ang_vel, 3) || get(S.N.force, force, 3) ||
+        get(S.N.torque, torque, 3))
+        return S.fail(WG_ERR_CUDA, "slot download failed");
+    if (ori) {
+        if (S.N.orif) {
+            std::vector<float4> f(n);
+            WG_CUDA_TRY(cudaMemcpy(f.data(), S.N.orif + p0, sizeof(float4) * n, cudaMemcpyDeviceToHost));
+            for (int64_t q = 0; q < n; q++) {
+                ori[4 * q] = f[q].x; ori[4 * q + 1] = f[q].y; ori[4 * q + 2] = f[q].z; ori[4 * q + 3] = f[q].w;
+            }
+        } else if (get(S.N.ori, ori, 4))
+            return S.fail(WG_ERR_CUDA, "slot download failed");
+    }
     return WG_OK;
 }
 

@@ -59,6 +59,7 @@ struct CollideWork {
     std::vector<int64_t> hSceneSph;   // spheres of scene k: sphereIds[hSceneSph[k] .. hSceneSph[k+1])
     int32_t* dChunk = nullptr;
     Grid* dGrids = nullptr;
+    bool chunksDirty = true;
     int32_t* gStart = nullptr;        // walls of scene k in globalIds (batches)
     // pairs
     uint64_t* pairs = nullptr;
@@ -587,11 +588,16 @@ __global__ void k_pairs_large_large(DevParticles P, const int32_t* __restrict__ 
 }
 
 // ---------------------------------------------------------------- merge with previous contacts
-__global__ void k_mark_orphans(DevContacts C, const uint64_t* __restrict__ nk, int64_t nn, int32_t* __restrict__ orph) {
+// a contact of a particle that was (re)loaded or parked since the last full run does not survive
+__device__ __forceinline__ bool freshPair(const uint8_t* fresh, uint64_t k) {
+    return fresh && (fresh[(int)(k >> 32)] || fresh[(int)(k & 0xffffffffu)]);
+}
+__global__ void k_mark_orphans(DevContacts C, const uint64_t* __restrict__ nk, int64_t nn, int32_t* __restrict__ orph,
+                               const uint8_t* __restrict__ fresh) {
     const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= C.n) return;
     int32_t o = 0;
-    if (C.flags[j] & C_REAL) {
+    if ((C.flags[j] & C_REAL) && !freshPair(fresh, C.key[j])) {
         const uint64_t k = C.key[j];
         const int64_t pos = lowerBound64(nk, nn, k);
         o = (pos < nn && nk[pos] == k) ? 0 : 1;
@@ -610,14 +616,15 @@ __global__ void k_compact_orphans(DevContacts C, const int32_t* __restrict__ orp
 }
 __global__ void k_place_new(const uint64_t* __restrict__ nk, int64_t nn, const uint64_t* __restrict__ okey, int64_t no,
                             const uint64_t* __restrict__ oldKey, int64_t nOld, uint64_t* __restrict__ outKey,
-                            int32_t* __restrict__ src, const int32_t* __restrict__ nkCd, int32_t* __restrict__ outCd) {
+                            int32_t* __restrict__ src, const int32_t* __restrict__ nkCd, int32_t* __restrict__ outCd,
+                            const uint8_t* __restrict__ fresh) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nn) return;
     const uint64_t k = nk[i];
     const int64_t out = i + lowerBound64(okey, no, k);
     const int64_t pos = lowerBound64(oldKey, nOld, k);
     outKey[out] = k;
-    src[out] = (pos < nOld && oldKey[pos] == k) ? (int32_t)pos : -1;
+    src[out] = (pos < nOld && oldKey[pos] == k && !freshPair(fresh, k)) ? (int32_t)pos : -1;
     if (nkCd) outCd[out] = nkCd[i];
 }
 __global__ void k_place_orph(const uint64_t* __restrict__ nk, int64_t nn, const uint64_t* __restrict__ okey,
@@ -843,6 +850,7 @@ static int buildLists(Sim& S) {
     CollideWork& W = *S.cw;
     std::vector<int32_t> sph, large, glob;
     for (int64_t p = 0; p < S.nPar; p++) {
+        if (!S.hParked.empty() && S.hParked[p]) continue;  // empty part of a serving slot
         if (S.hShape[p] == WG_SHAPE_SPHERE) sph.push_back((int32_t)p);
         else if (S.hShape[p] == WG_SHAPE_WALL) glob.push_back((int32_t)p);
         else large.push_back((int32_t)p);
@@ -853,6 +861,7 @@ static int buildLists(Sim& S) {
     W.hSceneSph.assign(K + 1, 0);
     for (int32_t p : sph) W.hSceneSph[(S.hSceneOfPar.empty() ? 0 : S.hSceneOfPar[p]) + 1]++;
     for (int k = 0; k < K; k++) W.hSceneSph[k + 1] += W.hSceneSph[k];
+    W.chunksDirty = true;
     W.hChunk.assign(1, 0);
     W.hSceneChunk.assign(1, 0);
     const int64_t CH = 4096;
@@ -862,11 +871,16 @@ static int buildLists(Sim& S) {
     }
     W.hLarge = large;
     W.hGlobal = glob;
-    W.sphereIds = (int32_t*)S.dalloc(sizeof(int32_t) * std::max<size_t>(1, sph.size()));
-    W.largeIds = (int32_t*)S.dalloc(sizeof(int32_t) * std::max<size_t>(1, large.size() + glob.size()));
-    W.globalIds = (int32_t*)S.dalloc(sizeof(int32_t) * std::max<size_t>(1, large.size() + glob.size()));
-    if (!W.sphereIds || !W.largeIds || !W.globalIds) return S.fail(WG_ERR_CUDA, "out of device memory");
-    WG_CUDA_TRY(cudaMemcpy(W.sphereIds, sph.data(), sizeof(int32_t) * sph.size(), cudaMemcpyHostToDevice));
+    // capacity for every particle: the lists are rebuilt when serving slots change
+    if (!W.sphereIds) {
+        W.sphereIds = (int32_t*)S.dalloc(sizeof(int32_t) * std::max<int64_t>(1, S.nPar));
+        W.largeIds = (int32_t*)S.dalloc(sizeof(int32_t) * std::max<int64_t>(1, S.nPar));
+        W.globalIds = (int32_t*)S.dalloc(sizeof(int32_t) * std::max<int64_t>(1, S.nPar));
+        W.gStart = (int32_t*)S.dalloc(sizeof(int32_t) * (S.nScenes + 1));
+        if (!W.sphereIds || !W.largeIds || !W.globalIds || !W.gStart) return S.fail(WG_ERR_CUDA, "out of device memory");
+    }
+    W.nLarge = W.nGlobal = 0;
+    if (!sph.empty()) WG_CUDA_TRY(cudaMemcpy(W.sphereIds, sph.data(), sizeof(int32_t) * sph.size(), cudaMemcpyHostToDevice));
     // non-sphere pairs are possible only if some pair of them shares a mask bit outside loneMask
     bool ll = false;
     std::vector<int32_t> nonSph(large);
@@ -891,8 +905,12 @@ int collide_full_run(Sim& S) {
     cudaStream_t st = S.stream;
     if (!S.cw) {
         S.cw = new CollideWork();
+        S.listsDirty = true;
+    }
+    if (S.listsDirty) {
         int r = buildLists(S);
         if (r) return r;
+        S.listsDirty = false;
     }
     CollideWork& W = *S.cw;
     const uint32_t lone = S.cfg.lone_mask;
@@ -909,13 +927,18 @@ int collide_full_run(Sim& S) {
     const int ns = W.nSph;
     if (ns > 0) {
         const int nb = (int)W.hChunk.size() - 1;
-        if (!W.red) {
-            W.red = (double*)S.dalloc(sizeof(double) * 7 * std::max(nb, 1));
-            W.dChunk = (int32_t*)S.dalloc(sizeof(int32_t) * (nb + 1));
-            WG_CUDA_TRY(cudaMallocHost(&W.hRed, sizeof(double) * 7 * std::max(nb, 1)));
-            WG_CUDA_TRY(cudaMemcpy(W.dChunk, W.hChunk.data(), sizeof(int32_t) * (nb + 1), cudaMemcpyHostToDevice));
+        if (!W.dGrids) {
+            // capacity for the most chunks the particles can form (one per scene plus one per 4096 spheres)
+            const int cap = (int)(S.nPar / 4096 + S.nScenes + 2);
+            W.red = (double*)S.dalloc(sizeof(double) * 7 * cap);
+            W.dChunk = (int32_t*)S.dalloc(sizeof(int32_t) * (cap + 1));
+            WG_CUDA_TRY(cudaMallocHost(&W.hRed, sizeof(double) * 7 * cap));
             W.dGrids = (Grid*)S.dalloc(sizeof(Grid) * K);
-            if (!W.dGrids) return S.fail(WG_ERR_CUDA, "out of device memory (grid)");
+            if (!W.dGrids || !W.dChunk) return S.fail(WG_ERR_CUDA, "out of device memory (grid)");
+        }
+        if (W.chunksDirty) {
+            WG_CUDA_TRY(cudaMemcpy(W.dChunk, W.hChunk.data(), sizeof(int32_t) * (nb + 1), cudaMemcpyHostToDevice));
+            W.chunksDirty = false;
         }
         k_grid_reduce<<<nb, BS, 0, st>>>(S.P, W.sphereIds, W.dChunk, W.red);
         WG_CUDA_TRY(cudaMemcpyAsync(W.hRed, W.red, sizeof(double) * 7 * nb, cudaMemcpyDeviceToHost, st));
@@ -957,15 +980,16 @@ int collide_full_run(Sim& S) {
         WG_CUDA_TRY(cudaMemcpyAsync(W.dGrids, hG.data(), sizeof(Grid) * K, cudaMemcpyHostToDevice, st));
         // sort spheres by cell
         if (!W.cellKey) {
-            W.cellKey = (uint32_t*)S.dalloc(sizeof(uint32_t) * ns);
-            W.cellKeySorted = (uint32_t*)S.dalloc(sizeof(uint32_t) * ns);
-            W.cellVal = (int32_t*)S.dalloc(sizeof(int32_t) * ns);
-            W.sid = (int32_t*)S.dalloc(sizeof(int32_t) * ns);
-            W.smn = (double4_32a*)S.dalloc(sizeof(double4_32a) * ns);
-            W.smx = (double4_32a*)S.dalloc(sizeof(double4_32a) * ns);
-            W.smask = (uint32_t*)S.dalloc(sizeof(uint32_t) * ns);
-            W.smnf = (float4*)S.dalloc(sizeof(float4) * ns);
-            W.smxf = (float4*)S.dalloc(sizeof(float4) * ns);
+            const int64_t cap = S.nPar;  // every particle could be an active sphere
+            W.cellKey = (uint32_t*)S.dalloc(sizeof(uint32_t) * cap);
+            W.cellKeySorted = (uint32_t*)S.dalloc(sizeof(uint32_t) * cap);
+            W.cellVal = (int32_t*)S.dalloc(sizeof(int32_t) * cap);
+            W.sid = (int32_t*)S.dalloc(sizeof(int32_t) * cap);
+            W.smn = (double4_32a*)S.dalloc(sizeof(double4_32a) * cap);
+            W.smx = (double4_32a*)S.dalloc(sizeof(double4_32a) * cap);
+            W.smask = (uint32_t*)S.dalloc(sizeof(uint32_t) * cap);
+            W.smnf = (float4*)S.dalloc(sizeof(float4) * cap);
+            W.smxf = (float4*)S.dalloc(sizeof(float4) * cap);
             if (!W.smask || !W.smxf) return S.fail(WG_ERR_CUDA, "out of device memory (grid)");
         }
         W.cellOff = grow(S, W.cellOff, W.cellOffCap, ncellAll + 1);
@@ -1006,8 +1030,6 @@ int collide_full_run(Sim& S) {
                 std::vector<int32_t> gs(K + 1, 0);
                 for (int32_t p : glo) gs[S.hSceneOfPar[p] + 1]++;
                 for (int k = 0; k < K; k++) gs[k + 1] += gs[k];
-                W.gStart = (int32_t*)S.dalloc(sizeof(int32_t) * (K + 1));
-                if (!W.gStart) return S.fail(WG_ERR_CUDA, "out of device memory (grid)");
                 WG_CUDA_TRY(cudaMemcpy(W.gStart, gs.data(), sizeof(int32_t) * (K + 1), cudaMemcpyHostToDevice));
             }
         }
@@ -1047,7 +1069,7 @@ int collide_full_run(Sim& S) {
                 k_pairs_local<<<(unsigned)(((int64_t)W.nLarge * 32 + BS - 1) / BS), BS, 0, st>>>(
                     S.P, W.largeIds, W.nLarge, W.smn, W.smx, W.smnf, W.smxf, W.dGrids, W.cellOff, lone, W.pairs, W.pairCap, W.counter);
             if (W.nGlobal > 0)
-                k_pairs_global<<<(ns + BS - 1) / BS, BS, 0, st>>>(S.P, W.globalIds, W.nGlobal, W.gStart, W.sphereIds, ns, lone,
+                k_pairs_global<<<(ns + BS - 1) / BS, BS, 0, st>>>(S.P, W.globalIds, W.nGlobal, K > 1 ? W.gStart : nullptr, W.sphereIds, ns, lone,
                                                                 W.pairs, W.pairCap, W.counter);
         }
         if (W.largeLargePossible && !peri) {
@@ -1102,7 +1124,7 @@ int collide_full_run(Sim& S) {
     if (nOld > 0) {
         int32_t* flagsArr = W.orph;
         int32_t* scanArr = W.orph + (std::max<int64_t>(nOld, 1) + 1);
-        k_mark_orphans<<<(unsigned)((nOld + BS - 1) / BS), BS, 0, st>>>(S.C, W.pairsSorted, nNew, flagsArr);
+        k_mark_orphans<<<(unsigned)((nOld + BS - 1) / BS), BS, 0, st>>>(S.C, W.pairsSorted, nNew, flagsArr, S.P.fresh);
         size_t tb = 0;
         cub::DeviceScan::ExclusiveSum(nullptr, tb, flagsArr, scanArr, (int)nOld, st);
         if (ensureCub(S, tb)) return WG_ERR_CUDA;
@@ -1137,7 +1159,7 @@ int collide_full_run(Sim& S) {
     }
     if (nNew > 0)
         k_place_new<<<(unsigned)((nNew + BS - 1) / BS), BS, 0, st>>>(W.pairsSorted, nNew, W.orphKey, nOrph, S.C.key, nOld, S.Cb.key,
-                                                                    W.src, peri ? W.pairCdSorted : nullptr, W.newCd);
+                                                                    W.src, peri ? W.pairCdSorted : nullptr, W.newCd, S.P.fresh);
     if (nOrph > 0)
         k_place_orph<<<(unsigned)((nOrph + BS - 1) / BS), BS, 0, st>>>(W.pairsSorted, nNew, W.orphKey, W.orphSrc, nOrph, S.Cb.key,
                                                                       W.src);
@@ -1235,6 +1257,7 @@ int collide_full_run(Sim& S) {
     WG_CUDA_TRY(cudaStreamSynchronize(st));
     S.I.nHeavy = S.cfg.apply_forces ? W.hHeavy[0] : 0;
     S.I.nHeavyFree = S.cfg.apply_forces ? W.hHeavy[1] : 0;
+    if (S.P.fresh) WG_CUDA_TRY(cudaMemsetAsync(S.P.fresh, 0, S.nPar, st));
     WG_CUDA_TRY(cudaGetLastError());
     S.nFullRuns++;
     return 0;

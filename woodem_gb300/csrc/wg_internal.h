@@ -45,6 +45,7 @@ struct ScenePar {
     float gH[3], gL[3];   // gravity as double-float pairs (g = gH + gL)
     float dampingF, maxD2F;
     long long stepBase;   // Scene.step of this scene = device step counter - stepBase
+    long long stepEnd;    // the scene is frozen once Scene.step reaches stepEnd (serving slots)
     // periodic cell, integrated on the host each step (core/Cell.cpp:81-120)
     double hSize[9], pprevHsize[9], gradV[9], nextGradV[9], dGradV[9], midGradV[9], shiftVelMat[9];
     double ImLL4hInv[9], IpLL4h[9], LmL[9], unshear[9];
@@ -72,6 +73,7 @@ struct DevNodes {
     float2* rsplit; // FP32-force mode: the radius as a double-float pair (constant)
     float4 *lh, *ll; // FP32-force mode: the position mirror at the last full run (verlet reference)
     int32_t* scene;  // batch of scenes: scene of each node slot (null: one scene)
+    uint8_t* fresh;  // serving slots: node (re)loaded since its last step; Leapfrog takes its stored force
 };
 struct DevParticles {
     int32_t n;
@@ -83,6 +85,8 @@ struct DevParticles {
     double4_32a* mn;      // Aabb.min (verletDist included)
     double4_32a* mx;      // Aabb.max
     int32_t* scene;       // batch of scenes: scene of each particle (null: one scene)
+    uint8_t* fresh;       // serving slots: particle (re)loaded or parked since the last full run; its
+                          // contacts do not survive that run
 };
 // the parameters of the scene a node or particle belongs to
 __device__ __forceinline__ int sceneOfP(const DevParticles& P, int p) { return P.scene ? P.scene[p] : 0; }
@@ -169,7 +173,7 @@ __host__ __device__ inline void unpackCellDist(int32_t p, int& a, int& b, int& c
 // several steps without waiting for each verlet test.
 // fromEnds = 0: take DemData.force/torque as stored (first step after the host wrote the state).
 void launch_leapfrog(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const ScenePar* sp,
-                     int* dFlags, int fromEnds);
+                     int* dFlags, int fromEnds, const long long* dStep);
 void launch_contact_fp64(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C,
                          const DevIncidence& I, const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dFlags,
                          int block = 128);
@@ -184,7 +188,7 @@ int launch_stress(cudaStream_t st, const DevNodes& N, const DevParticles& P, con
                   const ScenePar* sp, double* scratch, int64_t scratchDoubles, double* out);
 // FP32-force mode (wg_step32.cu)
 void launch_leapfrog32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const NodeConst32* nc,
-                       const ScenePar* sp, int* dFlags, int fromEnds);
+                       const ScenePar* sp, int* dFlags, int fromEnds, const long long* dStep);
 // The kernels walk the active contacts I.work[0, I.nAct). Items [0, nMixed) are facet and wall
 // contacts; [nMixed, I.nAct) join two spheres and, in an aperiodic scene, go to a
 // sphere-sphere-only kernel.
@@ -255,6 +259,9 @@ struct Sim {
     std::vector<int32_t> hSceneOfPar;  // empty for one scene
     std::vector<ScenePar> hPars;
     std::vector<double> sceneTime0;    // Scene.time of each scene at upload
+    std::vector<uint8_t> hParked;      // serving slots: particle holds no job (left out of the collider)
+    bool listsDirty = true;            // particle lists of the collider to be rebuilt at the next full run
+    bool forceFull = false;            // next step starts with a full collider run
     long long* dStep = nullptr;
     int* dFlags = nullptr;   // [0] full run requested, [1] error code
     int* hFlags = nullptr;   // pinned mirror

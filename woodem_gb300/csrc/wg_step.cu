@@ -26,7 +26,7 @@ __device__ __forceinline__ double sgn(double s) { return s < 0 ? -1 : (s > 0 ? 1
 // and the verlet-distance test of InsertionSortCollider::updateBboxes_doFullRun
 // pkg/dem/InsertionSortCollider.cpp:339-350 on the new positions.
 __global__ void __launch_bounds__(256) k_leapfrog(DevNodes N, DevParticles P, DevIncidence I, const ScenePar* __restrict__ spp,
-                                                  int* __restrict__ dFlags, int fromEnds) {
+                                                  int* __restrict__ dFlags, int fromEnds, const long long* __restrict__ dStepC) {
     __shared__ EndStage<double4_32a, double2, 32> stage[8];
     if (halted(dFlags)) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -40,10 +40,13 @@ __global__ void __launch_bounds__(256) k_leapfrog(DevNodes N, DevParticles P, De
     // loop (the force reset of Leapfrog.cpp:240-245 followed by the deterministic sum of
     // ContactLoop.cpp:250-257), or the stored value
     const bool uni = valid && i < nPar && P.shape[i] != WG_SHAPE_FACET;
+    // a scene past its last step (serving slot) is frozen; a node just (re)loaded takes its stored force
+    const bool frozen = valid && (*dStepC - sp.stepBase) >= sp.stepEnd;
+    const bool fresh = valid && N.fresh && N.fresh[i];
     int e0 = 0, e1 = 0;
     bool take = false;
     D3 f{0, 0, 0}, t{0, 0, 0};
-    if (fromEnds && uni) {
+    if (fromEnds && uni && !fresh && !frozen) {
         if (sp.hasGravity && !(flags & F_GRAVITY_SKIP)) f = mass * D3{sp.g[0], sp.g[1], sp.g[2]};
         if (sp.applyForces) {
             endRange(I, i, e0, e1);
@@ -61,7 +64,8 @@ __global__ void __launch_bounds__(256) k_leapfrog(DevNodes N, DevParticles P, De
     warpSumEnds(I.endA, I.endB, take, e0, e1, stage[threadIdx.x >> 5], acc);
     f = acc.F;
     t = acc.T;
-    if (!valid || (flags & F_CLUMPED)) return;
+    if (!valid || (flags & F_CLUMPED) || frozen) return;
+    if (fresh) N.fresh[i] = 0;
     const double dt = sp.dt;
     const double damping = sp.damping;
     const bool damp = (damping != 0. && !(flags & F_DAMPING_SKIP));
@@ -155,9 +159,9 @@ __global__ void __launch_bounds__(256) k_leapfrog(DevNodes N, DevParticles P, De
 }
 
 void launch_leapfrog(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const ScenePar* sp,
-                     int* dFlags, int fromEnds) {
+                     int* dFlags, int fromEnds, const long long* dStep) {
     if (N.n == 0) return;
-    k_leapfrog<<<(N.n + 255) / 256, 256, 0, st>>>(N, P, I, sp, dFlags, fromEnds);
+    k_leapfrog<<<(N.n + 255) / 256, 256, 0, st>>>(N, P, I, sp, dFlags, fromEnds, dStep);
 }
 
 // ---------------------------------------------------------------------------------- ContactLoop
@@ -192,6 +196,7 @@ __global__ void __launch_bounds__(128) k_contact_fp64(DevNodes N, DevParticles P
     const int64_t c = wk.x;
     const int A = wk.y, B = wk.z;
     const ScenePar& sp = spp[sceneOfP(P, B)];
+    if (*dStep - sp.stepBase >= sp.stepEnd) return;  // frozen scene (serving slot past its last step)
     uint32_t fl = C.flags[c];
     if (fl & C_REMOVED) return;
     if ((fl & C_PENDING) && !pendingStays(P, A, B, sp.periodic, sp.cellSize, dErr)) {

@@ -85,7 +85,8 @@ __device__ __forceinline__ float fsgn(float s) { return s < 0.f ? -1.f : (s > 0.
 // Writes the double-float mirrors of position and velocity used by the contact kernel.
 // The node state is loaded before the end-slot sum so that its loads overlap the staging.
 __global__ void __launch_bounds__(256) k_leapfrog32(DevNodes N, DevParticles P, DevIncidence I, const NodeConst32* __restrict__ ncs,
-                                                    const ScenePar* __restrict__ spp, int* __restrict__ dFlags, int fromEnds) {
+                                                    const ScenePar* __restrict__ spp, int* __restrict__ dFlags, int fromEnds,
+                                                    const long long* __restrict__ dStepC) {
     __shared__ EndStage<float4, float2, 128> stage[8];
     if (halted(dFlags)) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -105,10 +106,13 @@ __global__ void __launch_bounds__(256) k_leapfrog32(DevNodes N, DevParticles P, 
     const uint32_t flags = nc.flags;
     // DemData.force/torque of this step
     const bool uni = valid && i < P.n && P.shape[i] != WG_SHAPE_FACET;
+    // a scene past its last step (serving slot) is frozen; a node just (re)loaded takes its stored force
+    const bool frozen = valid && (*dStepC - sp.stepBase) >= sp.stepEnd;
+    const bool fresh = valid && N.fresh && N.fresh[i];
     int e0 = 0, e1 = 0;
     bool take = false, summed = false;
     DF6 acc;
-    if (fromEnds && uni) {
+    if (fromEnds && uni && !fresh && !frozen) {
         if (sp.hasGravity && !(flags & F_GRAVITY_SKIP)) acc.initGravity(nc.mh, nc.ml, sp.gH, sp.gL);
         summed = true;
         if (sp.applyForces) {
@@ -118,7 +122,8 @@ __global__ void __launch_bounds__(256) k_leapfrog32(DevNodes N, DevParticles P, 
         }
     }
     warpSumEnds(I.endAf, I.endBf, take, e0, e1, stage[threadIdx.x >> 5], acc);
-    if (!valid || (flags & F_CLUMPED)) return;
+    if (!valid || (flags & F_CLUMPED) || frozen) return;
+    if (fresh) N.fresh[i] = 0;
     F3 f, t;
     if (summed) {
         f = F3{acc.net(0), acc.net(1), acc.net(2)};
@@ -237,9 +242,9 @@ __global__ void __launch_bounds__(256) k_leapfrog32(DevNodes N, DevParticles P, 
 }
 
 void launch_leapfrog32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const NodeConst32* nc,
-                       const ScenePar* sp, int* dFlags, int fromEnds) {
+                       const ScenePar* sp, int* dFlags, int fromEnds, const long long* dStep) {
     if (N.n == 0) return;
-    k_leapfrog32<<<(N.n + 255) / 256, 256, 0, st>>>(N, P, I, nc, sp, dFlags, fromEnds);
+    k_leapfrog32<<<(N.n + 255) / 256, 256, 0, st>>>(N, P, I, nc, sp, dFlags, fromEnds, dStep);
 }
 
 // ---------------------------------------------------------------------------------- ContactLoop
@@ -368,6 +373,7 @@ __global__ void __launch_bounds__(256, SSONLY ? 4 : 1) k_contact_fp32(DevNodes N
     const int64_t c = wk.x;
     const int A = wk.y, B = wk.z;
     const ScenePar& sp = spp[sceneOfP(P, B)];
+    if (*dStep - sp.stepBase >= sp.stepEnd) return;  // frozen scene (serving slot past its last step)
     uint32_t fl = C.flags[c];
     if (fl & C_REMOVED) return;
     if ((fl & C_PENDING) && !pendingStays(P, A, B, sp.periodic, sp.cellSize, dErr)) {
