@@ -158,7 +158,7 @@ __global__ void k_put_state(DevNodes N, const int32_t* __restrict__ map, int64_t
     N.posr[s] = make_double4_32a(pos[3 * a], pos[3 * a + 1], pos[3 * a + 2], r);
     N.ori[s] = make_double4_32a(ori[4 * a], ori[4 * a + 1], ori[4 * a + 2], ori[4 * a + 3]);
     if (N.orif) N.orif[s] = make_float4((float)ori[4 * a], (float)ori[4 * a + 1], (float)ori[4 * a + 2], (float)ori[4 * a + 3]);
-    if (N.ph) {
+    if (N.mir) {
         // the double-float mirrors of the FP32-force mode follow the written state
         auto split = [](double x, float& h, float& l) {
             h = __double2float_rn(x);
@@ -171,15 +171,17 @@ __global__ void k_put_state(DevNodes N, const int32_t* __restrict__ map, int64_t
         split(pos[3 * a + 2], h.z, l.z);
         h.w = rs.x;
         l.w = rs.y;
-        N.ph[s] = h;
-        N.pl[s] = l;
+        Mirror m;
+        m.ph = h;
+        m.pl = l;
         split(vel[3 * a], h.x, l.x);
         split(vel[3 * a + 1], h.y, l.y);
         split(vel[3 * a + 2], h.z, l.z);
         h.w = (float)av[3 * a];
         l.w = (float)av[3 * a + 1];
-        N.vh[s] = h;
-        N.vl[s] = l;
+        m.vh = h;
+        m.vl = l;
+        N.mir[s] = m;
         N.wz[s] = (float)av[3 * a + 2];
     }
     N.vel[s] = make_double4_32a(vel[3 * a], vel[3 * a + 1], vel[3 * a + 2], 0.);
@@ -553,17 +555,14 @@ int Sim::upload() {
             rsp[q] = make_float2(rh, (float)(posr[q].w - (double)rh));
         }
         dNodeC = (NodeConst32*)dalloc(sizeof(NodeConst32) * nSlots);
-        N.ph = (float4*)dalloc(sizeof(float4) * nSlots);
-        N.pl = (float4*)dalloc(sizeof(float4) * nSlots);
-        N.vh = (float4*)dalloc(sizeof(float4) * nSlots);
-        N.vl = (float4*)dalloc(sizeof(float4) * nSlots);
+        N.mir = (Mirror*)dalloc(sizeof(Mirror) * nSlots);
         N.wz = (float*)dalloc(sizeof(float) * nSlots);
         N.orif = (float4*)dalloc(sizeof(float4) * nSlots);
         N.rsplit = (float2*)dalloc(sizeof(float2) * nSlots);
         N.lh = (float4*)dalloc(sizeof(float4) * nSlots);
         N.ll = (float4*)dalloc(sizeof(float4) * nSlots);
         if (!N.ll) return fail(WG_ERR_CUDA, "out of device memory (scene)");
-        if (!dNodeC || !N.wz || !N.orif || !N.rsplit) return fail(WG_ERR_CUDA, "out of device memory (scene)");
+        if (!dNodeC || !N.mir || !N.wz || !N.orif || !N.rsplit) return fail(WG_ERR_CUDA, "out of device memory (scene)");
         WG_CUDA_TRY(cudaMemcpy(N.orif, orf.data(), sizeof(float4) * nSlots, cudaMemcpyHostToDevice));
         WG_CUDA_TRY(cudaMemcpy(N.rsplit, rsp.data(), sizeof(float2) * nSlots, cudaMemcpyHostToDevice));
         // double-float mirrors of the initial state (x = hi + lo)
@@ -585,10 +584,9 @@ int Sim::upload() {
             hvl[q].w = (float)angv[q].y;
             hwz[q] = (float)angv[q].z;
         }
-        WG_CUDA_TRY(cudaMemcpy(N.ph, hph.data(), sizeof(float4) * nSlots, cudaMemcpyHostToDevice));
-        WG_CUDA_TRY(cudaMemcpy(N.pl, hpl.data(), sizeof(float4) * nSlots, cudaMemcpyHostToDevice));
-        WG_CUDA_TRY(cudaMemcpy(N.vh, hvh.data(), sizeof(float4) * nSlots, cudaMemcpyHostToDevice));
-        WG_CUDA_TRY(cudaMemcpy(N.vl, hvl.data(), sizeof(float4) * nSlots, cudaMemcpyHostToDevice));
+        std::vector<Mirror> hm(nSlots);
+        for (int64_t q = 0; q < nSlots; q++) hm[q] = Mirror{hph[q], hpl[q], hvh[q], hvl[q]};
+        WG_CUDA_TRY(cudaMemcpy(N.mir, hm.data(), sizeof(Mirror) * nSlots, cudaMemcpyHostToDevice));
         WG_CUDA_TRY(cudaMemcpy(N.wz, hwz.data(), sizeof(float) * nSlots, cudaMemcpyHostToDevice));
         WG_CUDA_TRY(cudaMemcpy(N.lh, hph.data(), sizeof(float4) * nSlots, cudaMemcpyHostToDevice));
         WG_CUDA_TRY(cudaMemcpy(N.ll, hpl.data(), sizeof(float4) * nSlots, cudaMemcpyHostToDevice));
@@ -601,6 +599,8 @@ int Sim::upload() {
     int r = ensureContactCapacity(std::max<int64_t>(1024, 4 * nPar));
     if (r) return r;
     C.n = 0;
+    K.n = 0;
+    packDirty = false;
     if (cfg.periodic) {
         X.cell.trsf = fromRow(cfg.cell_trsf);
         X.cell.hSize = fromRow(cfg.cell_hsize);
@@ -649,6 +649,18 @@ __global__ void k_set_flags(int* f, int full) {
 // device flag words, and once Leapfrog of step s finds a node past verletDist, the contact
 // kernel of step s raises FL_HALT and everything queued after it does nothing. The host then
 // reads the step counter, runs the collider for step s, finishes its contact loop and goes on.
+int Sim::syncContacts() {
+    Sim& S = *this;
+    if (packDirty && K.n > 0) {
+        WG_CUDA_TRY(cudaSetDevice(device));
+        launch_unpack_ss(stream, C, I, K, nMixed);
+        WG_CUDA_TRY(cudaGetLastError());
+        WG_CUDA_TRY(cudaStreamSynchronize(stream));
+    }
+    packDirty = false;
+    return 0;
+}
+
 int Sim::run(int64_t n) {
     Sim& S = *this;
     SimEx& X = static_cast<SimEx&>(*this);
@@ -672,6 +684,8 @@ int Sim::run(int64_t n) {
     cudaEvent_t* E = evPool.data();
     long long* hStepPin = (long long*)(hFlags + 4);
     const bool fp32 = prec == WG_PREC_FP32;
+    bool anyLaw0 = cfg.law == 0;
+    for (const wg_config& c : cfgs) anyLaw0 = anyLaw0 || c.law == 0;
     auto stepLeapfrog = [&](int fromEndsArg) {
         if (fromEndsArg) {
             if (fp32) launch_forces32(stream, N, P, I, dNodeC, dPar, dFlags, true);
@@ -683,7 +697,7 @@ int Sim::run(int64_t n) {
         launches++;
     };
     auto stepContact = [&]() {
-        if (fp32) launch_contact_fp32(stream, side, N, P, C, I, dMats, dPar, dStep, dFlags, nMixed, cfg.periodic != 0,
+        if (fp32) launch_contact_fp32(stream, side, N, P, C, I, K, dMats, dPar, dStep, dFlags, nMixed, cfg.periodic != 0, anyLaw0,
                                       contactBlock > 0 ? contactBlock : 256);
         else launch_contact_fp64(stream, N, P, C, I, dMats, dPar, dStep, dFlags,
                                  (contactBlock > 0 && contactBlock <= 128) ? contactBlock : 128);  // launch bounds 128
@@ -694,6 +708,8 @@ int Sim::run(int64_t n) {
     WG_CUDA_TRY(cudaEventRecord(ev[6], stream));
     int64_t done = 0;
     while (done < n) {
+        // the sphere-sphere kernel updates the packed state from here on
+        if (K.n > 0) packDirty = true;
         const int64_t k = std::min<int64_t>(n - done, maxChunk);
         const bool needFull = !initialized || anyZeroVd || forceFull;
         k_set_flags<<<1, 1, 0, stream>>>(dFlags, needFull ? 1 : 0);
@@ -769,6 +785,7 @@ int Sim::run(int64_t n) {
             launches += 12;
             WG_CUDA_TRY(cudaEventRecord(E[3 * maxChunk + 1], stream));
             k_set_flags<<<1, 1, 0, stream>>>(dFlags, 0);
+            if (K.n > 0) packDirty = true;
             WG_CUDA_TRY(cudaEventRecord(E[0], stream));
             stepContact();
             WG_CUDA_TRY(cudaEventRecord(E[1], stream));
@@ -798,6 +815,8 @@ int Sim::run(int64_t n) {
             dStress = (double*)dalloc(sizeof(double) * stressCap);
             if (!dStress) return fail(WG_ERR_CUDA, "out of device memory (stress)");
         }
+        int r = syncContacts();
+        if (r) return r;
         if (launch_stress(stream, N, P, C, I, dPar, dStress + 9, stressCap - 9, dStress))
             return fail(WG_ERR_STATE, "stress scratch too small");
         double sum[9];
@@ -990,9 +1009,10 @@ static int writeSlot(Sim& S, int64_t p0, int64_t cap, int64_t n, const double* p
             of[q] = make_float4((float)o4[q].x, (float)o4[q].y, (float)o4[q].z, (float)o4[q].w);
             rs[q] = make_float2(ph[q].w, pl[q].w);
         }
-        if (put(S.dNodeC + p0, nc.data(), sizeof(NodeConst32) * cap) || put(S.N.ph + p0, ph.data(), sizeof(float4) * cap) ||
-            put(S.N.pl + p0, pl.data(), sizeof(float4) * cap) || put(S.N.vh + p0, vh.data(), sizeof(float4) * cap) ||
-            put(S.N.vl + p0, vl.data(), sizeof(float4) * cap) || put(S.N.wz + p0, wz.data(), sizeof(float) * cap) ||
+        std::vector<Mirror> mr(cap);
+        for (int64_t q = 0; q < cap; q++) mr[q] = Mirror{ph[q], pl[q], vh[q], vl[q]};
+        if (put(S.dNodeC + p0, nc.data(), sizeof(NodeConst32) * cap) || put(S.N.mir + p0, mr.data(), sizeof(Mirror) * cap) ||
+            put(S.N.wz + p0, wz.data(), sizeof(float) * cap) ||
             put(S.N.orif + p0, of.data(), sizeof(float4) * cap) || put(S.N.rsplit + p0, rs.data(), sizeof(float2) * cap) ||
             put(S.N.lh + p0, ph.data(), sizeof(float4) * cap) || put(S.N.ll + p0, pl.data(), sizeof(float4) * cap))
             return S.fail(WG_ERR_CUDA, "slot upload failed");
@@ -1149,6 +1169,8 @@ int wg_get_scene_stats(wg_scene* s, int32_t k, wg_stats* o) {
     if (!s || !o) return WG_ERR_ARG;
     Sim& S = *SIM(s);
     if (k < 0 || k >= S.nScenes) return S.fail(WG_ERR_ARG, "scene index out of range");
+    int r = S.syncContacts();
+    if (r) return r;
     std::memset(o, 0, sizeof(*o));
     const wg_config& c = S.nScenes > 1 ? S.cfgs[k] : S.cfg;
     const int64_t done = S.step - S.cfg.step;
@@ -1308,6 +1330,8 @@ int wg_run_host(wg_scene* s, int64_t n_steps, double* pos, double* ori, double* 
 int wg_get_stats(wg_scene* s, wg_stats* o) {
     if (!s || !o) return WG_ERR_ARG;
     Sim& S = *SIM(s);
+    int r = S.syncContacts();
+    if (r) return r;
     std::memset(o, 0, sizeof(*o));
     o->step = S.step;
     o->time = S.time;
@@ -1352,6 +1376,8 @@ int wg_get_cell(wg_scene* s, double* hsize, double* trsf, double* gradv) {
 // Contacts listed the way the reference's container holds them after a step.
 static int collectContacts(Sim& S, std::vector<int64_t>& keep, std::vector<uint64_t>& key, std::vector<uint32_t>& fl,
                            std::vector<int32_t>& cd, std::vector<std::vector<double>>& cols) {
+    int r = S.syncContacts();
+    if (r) return r;
     const int64_t n = S.C.n;
     key.resize(n); fl.resize(n); cd.resize(n);
     cols.assign(CC_NCOL + 3, std::vector<double>(n, 0.));  // + global force on pA

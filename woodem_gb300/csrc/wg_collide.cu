@@ -128,8 +128,8 @@ __global__ void k_aabb(DevNodes N, DevParticles P, const ScenePar* __restrict__ 
         }
         N.lastPos[p] = make_double4_32a(pr.x, pr.y, pr.z, 0.);
         if (N.lh) {
-            N.lh[p] = N.ph[p];
-            N.ll[p] = N.pl[p];
+            N.lh[p] = N.mir[p].ph;
+            N.ll[p] = N.mir[p].pl;
         }
     } else if (sh == WG_SHAPE_WALL) {
         const int ax = P.aux[p].x;
@@ -140,8 +140,8 @@ __global__ void k_aabb(DevNodes N, DevParticles P, const ScenePar* __restrict__ 
         setComp(mx, ax, comp(D3{pr.x, pr.y, pr.z}, ax));
         N.lastPos[p] = make_double4_32a(pr.x, pr.y, pr.z, 0.);
         if (N.lh) {
-            N.lh[p] = N.ph[p];
-            N.ll[p] = N.pl[p];
+            N.lh[p] = N.mir[p].ph;
+            N.ll[p] = N.mir[p].pl;
         }
     } else {
         const int4 fn = P.aux[p];
@@ -166,14 +166,14 @@ __global__ void k_aabb(DevNodes N, DevParticles P, const ScenePar* __restrict__ 
             }
             N.lastPos[nn[k]] = make_double4_32a(pr.x, pr.y, pr.z, 0.);
             if (N.lh) {
-                N.lh[nn[k]] = N.ph[nn[k]];
-                N.ll[nn[k]] = N.pl[nn[k]];
+                N.lh[nn[k]] = N.mir[nn[k]].ph;
+                N.ll[nn[k]] = N.mir[nn[k]].pl;
             }
         }
         N.lastPos[p] = N.posr[p];
         if (N.lh) {
-            N.lh[p] = N.ph[p];
-            N.ll[p] = N.pl[p];
+            N.lh[p] = N.mir[p].ph;
+            N.ll[p] = N.mir[p].pl;
         }
     }
     if (sp.verletDist > 0) {
@@ -702,10 +702,10 @@ __global__ void k_dormant(DevContacts C, DevNodes N, DevParticles P, const Scene
     const double m2 = 2 * sp.verletDist;
     bool far;
     const double4_32a pb = N.posr[B];
-    if (ty == CT_SS && N.ph) {
+    if (ty == CT_SS && N.mir) {
         // FP32-force mode: the double-float mirrors of the positions, FP32 arithmetic; the
         // relative position carries ~47 bits and the squares and sums ~2^-22 relative error
-        const float4 ha = N.ph[A], la = N.pl[A], hb = N.ph[B], lb = N.pl[B];
+        const float4 ha = N.mir[A].ph, la = N.mir[A].pl, hb = N.mir[B].ph, lb = N.mir[B].pl;
         float sx, tx, sy, ty_, sz, tz;
         dfDiff(ha.x, la.x, hb.x, lb.x, sx, tx);
         dfDiff(ha.y, la.y, hb.y, lb.y, sy, ty_);
@@ -903,6 +903,12 @@ static int buildLists(Sim& S) {
 
 int collide_full_run(Sim& S) {
     cudaStream_t st = S.stream;
+    // the contact arrays take back the packed sphere-sphere state before they are merged
+    {
+        int r = S.syncContacts();
+        if (r) return r;
+        S.K.n = 0;
+    }
     if (!S.cw) {
         S.cw = new CollideWork();
         S.listsDirty = true;
@@ -1246,6 +1252,35 @@ int collide_full_run(Sim& S) {
         WG_CUDA_TRY(cudaMemsetAsync(S.I.endA, 0, sizeof(double4_32a) * ne, st));
         WG_CUDA_TRY(cudaMemsetAsync(S.I.endB, 0, sizeof(double2) * ne, st));
     }
+    // FP32-force mode, aperiodic scenes: the sphere-sphere contacts' state in work-list order
+    if (S.prec == WG_PREC_FP32 && !S.cfg.periodic && nSS > 0) {
+        DevPackedSS& K = S.K;
+        if (K.cap < nSS) {
+            S.dfree(K.item); S.dfree(K.flags);
+            for (int q = 0; q < CF_NCOL; q++) S.dfree(K.col[q]);
+            S.dfree(K.ft[0]); S.dfree(K.ft[1]);
+            K = DevPackedSS{};
+            K.cap = nSS * 5 / 4 + 4096;
+            K.item = (int4*)S.dalloc(sizeof(int4) * K.cap);
+            K.flags = (uint32_t*)S.dalloc(sizeof(uint32_t) * K.cap);
+            bool ok = K.item && K.flags;
+            for (int q = 0; q < CF_NCOL; q++) {
+                K.col[q] = (float*)S.dalloc(sizeof(float) * K.cap);
+                ok = ok && K.col[q];
+            }
+            // the IdealElPl shear force (a serving slot may take a job with that law at any time)
+            K.ft[0] = (double*)S.dalloc(sizeof(double) * K.cap);
+            K.ft[1] = (double*)S.dalloc(sizeof(double) * K.cap);
+            ok = ok && K.ft[0] && K.ft[1];
+            if (!ok) {
+                K.cap = 0;
+                return S.fail(WG_ERR_CUDA, "out of device memory (packed contacts)");
+            }
+        }
+        K.n = nSS;
+        launch_pack_ss(st, S.C, S.I, S.P, K, S.nMixed);
+    }
+    S.packDirty = false;
     // heavy particles
     if (!W.heavyCount) {
         W.heavyCount = (int32_t*)S.dalloc(sizeof(int32_t) * 3);

@@ -82,8 +82,26 @@ struct DF6 {
     __device__ __forceinline__ float net(int k) const { return __fadd_rn(h[k], l[k]); }
 };
 
+// Asynchronous global -> shared copy of one element of 8, 16 or 32 bytes (cp.async: the copies of
+// a lane are in flight together and hold no registers).
+template <int BYTES>
+__device__ __forceinline__ void cpAsync(void* dst, const void* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    if constexpr (BYTES == 8) {
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+    } else if constexpr (BYTES == 16) {
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+    } else {
+        static_assert(BYTES == 32, "8, 16 or 32 bytes");
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d + 16u), "l"((const char*)src + 16) : "memory");
+    }
+}
+__device__ __forceinline__ void cpAsyncWaitAll() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 // Adds the end slots [e0, e1) of every lane with take==true to acc. Must be called by all
-// 32 lanes of the warp (warp-uniform control flow inside).
+// 32 lanes of the warp (warp-uniform control flow inside). Each chunk of the warp's run of slots
+// is copied to shared memory with cp.async, all of a lane's copies in flight at once.
 template <typename EA, typename EB, int CH, typename Acc>
 __device__ __forceinline__ void warpSumEnds(const EA* __restrict__ endA, const EB* __restrict__ endB, bool take, int e0, int e1,
                                             EndStage<EA, EB, CH>& st, Acc& acc) {
@@ -101,10 +119,15 @@ __device__ __forceinline__ void warpSumEnds(const EA* __restrict__ endA, const E
         const int lo = __shfl_sync(FULL, e0, s), hi = __shfl_sync(FULL, e1, e - 1);
         for (int base = lo; base < hi; base += CH) {
             const int cnt = min(CH, hi - base);
-            for (int q = lane; q < cnt; q += 32) {
-                st.a[q] = endA[base + q];
-                st.b[q] = endB[base + q];
+#pragma unroll
+            for (int u = 0; u < CH / 32; u++) {
+                const int q = lane + 32 * u;
+                if (q < cnt) {
+                    cpAsync<sizeof(EA)>(&st.a[q], &endA[base + q]);
+                    cpAsync<sizeof(EB)>(&st.b[q], &endB[base + q]);
+                }
             }
+            cpAsyncWaitAll();
             __syncwarp();
             if (lane >= s && lane < e) {
                 const int a = max(e0, base), b = min(e1, base + cnt);

@@ -53,6 +53,11 @@ struct ScenePar {
     int32_t hasShear, _pad2;
 };
 
+// Double-float mirror of a node: ph/pl = position and radius, vh/vl = velocity with angVel.x/.y
+// in w (x = hi + lo).
+struct __align__(64) Mirror {
+    float4 ph, pl, vh, vl;
+};
 // Node-slot arrays (uninodal particle p owns slot p; facet vertices follow the particles).
 struct DevNodes {
     int32_t n;
@@ -66,8 +71,9 @@ struct DevNodes {
     double4_32a* lastPos; // verlet reference position
     uint32_t* flags;
     // FP32-force mode: double-float mirrors written by Leapfrog for the sphere-sphere contacts
-    // (x = hi + lo): ph/pl = position and radius, vh/vl = velocity with angVel.x/.y in w, wz = angVel.z
-    float4 *ph, *pl, *vh, *vl;
+    // (x = hi + lo), one 64-byte record per node so that a contact gathers two adjacent sectors
+    // per particle; wz = angVel.z
+    Mirror* mir;
     float* wz;
     float4* orif;   // FP32-force mode: the orientation (w x y z), in place of ori
     float2* rsplit; // FP32-force mode: the radius as a double-float pair (constant)
@@ -152,6 +158,22 @@ struct NodeConst32 {
 };
 // Particles with more end slots than this are summed by a block tree instead of one lane.
 constexpr int kHeavyThreshold = 64;
+// End slots a warp of the FP32 Leapfrog stages per chunk (32 particles of ~6 contacts each fit
+// one chunk; 8 warps x 256 x 24 bytes = 48 KB of shared memory per block).
+constexpr int kLeapfrogChunk32 = 256;
+
+// FP32-force mode, aperiodic scenes: the state of the active sphere-sphere contacts (work items
+// [nMixed, nAct)) held in work-list order, so that the per-step kernel loads and stores it
+// coalesced, with the particle ids and end slots beside it. Filled from the contact arrays at
+// each full collider run and written back before the next one and before the host reads the
+// contacts; the contact arrays hold the state of those contacts only after such a write-back.
+struct DevPackedSS {
+    int64_t n = 0, cap = 0;
+    int4* item = nullptr;      // (pA, pB, end slot of pA, end slot of pB)
+    uint32_t* flags = nullptr; // contact flags | scene << 8
+    float* col[CF_NCOL] = {};
+    double* ft[2] = {};        // IdealElPl shear force
+};
 // Step-loop flag words (device int[3]).
 enum { FL_FULL = 0,   // set by Leapfrog: a node moved farther than verletDist, a full collider run is due
        FL_ERR = 1,    // error code raised by a kernel
@@ -198,8 +220,12 @@ struct SideStream {
     cudaEvent_t fork = nullptr, join = nullptr;
 };
 void launch_contact_fp32(cudaStream_t st, const SideStream& side, const DevNodes& N, const DevParticles& P, const DevContacts& C,
-                         const DevIncidence& I, const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dFlags,
-                         int64_t nMixed, bool periodic, int block = 256);
+                         const DevIncidence& I, const DevPackedSS& K, const double4_32a* mats, const ScenePar* sp,
+                         const long long* dStep, int* dFlags, int64_t nMixed, bool periodic, bool anyLaw0, int block = 256);
+// copy the packed sphere-sphere state from (pack) / back to (unpack) the contact arrays
+void launch_pack_ss(cudaStream_t st, const DevContacts& C, const DevIncidence& I, const DevParticles& P, const DevPackedSS& K,
+                    int64_t nMixed);
+void launch_unpack_ss(cudaStream_t st, const DevContacts& C, const DevIncidence& I, const DevPackedSS& K, int64_t nMixed);
 void launch_forces32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const NodeConst32* nc,
                      const ScenePar* sp, const int* dFlags, bool perStep);
 
@@ -247,6 +273,8 @@ struct Sim {
     DevIncidence I{};
     int64_t cCap = 0;
     int64_t nMixed = 0;   // work items [0, nMixed) are not sphere-sphere (see launch_contact_fp32)
+    DevPackedSS K{};      // FP32-force mode: packed state of the active sphere-sphere contacts
+    bool packDirty = false;  // K changed since it was last written back to the contact arrays
     double4_32a* dMats = nullptr;
     NodeConst32* dNodeC = nullptr;  // per node slot (FP32-force mode)
     int prec = 0;                  // WG_PREC_*
@@ -300,6 +328,7 @@ struct Sim {
     int run(int64_t n);
     int checkErr();
     int ensureContactCapacity(int64_t need);
+    int syncContacts();  // write the packed sphere-sphere state back to the contact arrays if needed
 };
 
 #define WG_CUDA_TRY(expr)                                                                  \

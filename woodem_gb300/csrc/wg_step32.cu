@@ -87,28 +87,36 @@ __device__ __forceinline__ float fsgn(float s) { return s < 0.f ? -1.f : (s > 0.
 __global__ void __launch_bounds__(256) k_leapfrog32(DevNodes N, DevParticles P, DevIncidence I, const NodeConst32* __restrict__ ncs,
                                                     const ScenePar* __restrict__ spp, int* __restrict__ dFlags, int fromEnds,
                                                     const long long* __restrict__ dStepC) {
-    __shared__ EndStage<float4, float2, 128> stage[8];
-    if (halted(dFlags)) return;
+    __shared__ EndStage<float4, float2, kLeapfrogChunk32> stage[8];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < N.n;
-    const ScenePar& sp = spp[valid ? sceneOfN(N, i) : 0];
-    NodeConst32 nc{0.f, {0.f, 0.f, 0.f}, 0.f, 0.f, 0u, 0u};
-    double4_32a pr = make_double4_32a(0., 0., 0., 0.), v4 = pr, w4 = pr;
-    float4 lh = make_float4(0.f, 0.f, 0.f, 0.f), ll = lh;
-    if (valid) {
-        nc = ncs[i];
-        pr = N.posr[i];
-        v4 = N.vel[i];
-        w4 = N.angv[i];
-        lh = N.lh[i];
-        ll = N.ll[i];
+    // every load of the node is issued before the step guard (nothing is written before it), so
+    // that they are in flight together
+    const int ii = valid ? i : 0;
+    const NodeConst32 nc = ncs[ii];
+    const double4_32a pr = N.posr[ii], v4 = N.vel[ii], w4 = N.angv[ii];
+    const float4 lh = N.lh[ii], ll = N.ll[ii], o = N.orif[ii];
+    const float2 rs = N.rsplit[ii];
+    const int pi = ii < P.n ? ii : 0;
+    const int shape = P.shape[pi];
+    const bool freshLd = N.fresh && N.fresh[ii];
+    int hs0 = 0, hs1 = 0, ls0 = 0, ls1 = 0;
+    if (fromEnds) {
+        hs0 = I.hiStart[pi];
+        hs1 = I.hiStart[pi + 1];
+        ls0 = I.loStart[pi];
+        ls1 = I.loStart[pi + 1];
     }
+    const long long stepAbs = *dStepC;
+    const int scene = valid ? sceneOfN(N, i) : 0;
+    if (halted(dFlags)) return;
+    const ScenePar& sp = spp[scene];
     const uint32_t flags = nc.flags;
     // DemData.force/torque of this step
-    const bool uni = valid && i < P.n && P.shape[i] != WG_SHAPE_FACET;
+    const bool uni = valid && i < P.n && shape != WG_SHAPE_FACET;
     // a scene past its last step (serving slot) is frozen; a node just (re)loaded takes its stored force
-    const bool frozen = valid && (*dStepC - sp.stepBase) >= sp.stepEnd;
-    const bool fresh = valid && N.fresh && N.fresh[i];
+    const bool frozen = valid && (stepAbs - sp.stepBase) >= sp.stepEnd;
+    const bool fresh = valid && freshLd;
     int e0 = 0, e1 = 0;
     bool take = false, summed = false;
     DF6 acc;
@@ -116,7 +124,8 @@ __global__ void __launch_bounds__(256) k_leapfrog32(DevNodes N, DevParticles P, 
         if (sp.hasGravity && !(flags & F_GRAVITY_SKIP)) acc.initGravity(nc.mh, nc.ml, sp.gH, sp.gL);
         summed = true;
         if (sp.applyForces) {
-            endRange(I, i, e0, e1);
+            e0 = hs0 + ls0;
+            e1 = hs1 + ls1;
             take = (e1 - e0) <= kHeavyThreshold;
             summed = take;
         }
@@ -194,32 +203,28 @@ __global__ void __launch_bounds__(256) k_leapfrog32(DevNodes N, DevParticles P, 
     const F3 w{truncF(angVel.x), truncF(angVel.y), truncF(angVel.z)};
     {
         // double-float mirrors read by the sphere-sphere contact geometry
-        const float2 rs = N.rsplit[i];
-        float4 h, l;
-        splitDF(pos.x, h.x, l.x);
-        splitDF(pos.y, h.y, l.y);
-        splitDF(pos.z, h.z, l.z);
-        h.w = rs.x;
-        l.w = rs.y;
-        N.ph[i] = h;
-        N.pl[i] = l;
+        Mirror m;
+        splitDF(pos.x, m.ph.x, m.pl.x);
+        splitDF(pos.y, m.ph.y, m.pl.y);
+        splitDF(pos.z, m.ph.z, m.pl.z);
+        m.ph.w = rs.x;
+        m.pl.w = rs.y;
         // verlet test (InsertionSortCollider.cpp:339-350): displacement since the last full run
         // from the double-float mirrors, in FP32
-        const float dx = (h.x - lh.x) + (l.x - ll.x), dy = (h.y - lh.y) + (l.y - ll.y), dz = (h.z - lh.z) + (l.z - ll.z);
+        const float dx = (m.ph.x - lh.x) + (m.pl.x - ll.x), dy = (m.ph.y - lh.y) + (m.pl.y - ll.y),
+                    dz = (m.ph.z - lh.z) + (m.pl.z - ll.z);
         if (dx * dx + dy * dy + dz * dz > sp.maxD2F) atomicOr(dFlags + FL_FULL, 1);
-        splitDF(vel.x, h.x, l.x);
-        splitDF(vel.y, h.y, l.y);
-        splitDF(vel.z, h.z, l.z);
-        h.w = w.x;
-        l.w = w.y;
-        N.vh[i] = h;
-        N.vl[i] = l;
+        splitDF(vel.x, m.vh.x, m.vl.x);
+        splitDF(vel.y, m.vh.y, m.vl.y);
+        splitDF(vel.z, m.vh.z, m.vl.z);
+        m.vh.w = w.x;
+        m.vl.w = w.y;
+        N.mir[i] = m;
         N.wz[i] = w.z;
     }
     const float ang = sqrtf(fdot(w, w));
     if (ang > 0.f) {
         // leapfrogSphericalRotate (Leapfrog.cpp:280-288) in FP32
-        const float4 o = N.orif[i];
         float s, c;
         sincosf(0.5f * ang * dtf, &s, &c);
         const F3 ax = w * (1.f / ang);
@@ -296,8 +301,8 @@ struct SSGeo {
     F3 n, dv, w1, w2;
     float uN, r1, r2;
 };
-__device__ __forceinline__ bool geomSS32(const DevNodes& N, int A, int B, float dfAbs, bool real, SSGeo& g) {
-    const float4 ha = N.ph[A], la = N.pl[A], hb = N.ph[B], lb = N.pl[B];
+__device__ __forceinline__ bool geomSS32(const Mirror& ma, const Mirror& mb, float wza, float wzb, float dfAbs, bool real, SSGeo& g) {
+    const float4 ha = ma.ph, la = ma.pl, hb = mb.ph, lb = mb.pl;
     float sx, tx, sy, ty, sz, tz;
     dfDiff(ha.x, la.x, hb.x, lb.x, sx, tx);
     dfDiff(ha.y, la.y, hb.y, lb.y, sy, ty);
@@ -341,7 +346,7 @@ __device__ __forceinline__ bool geomSS32(const DevNodes& N, int A, int B, float 
     g.n = dx * (1.f / dist);
     g.r1 = ha.w + la.w;
     g.r2 = hb.w + lb.w;
-    const float4 vha = N.vh[A], vla = N.vl[A], vhb = N.vh[B], vlb = N.vl[B];
+    const float4 vha = ma.vh, vla = ma.vl, vhb = mb.vh, vlb = mb.vl;
     float s, t;
     dfDiff(vha.x, vla.x, vhb.x, vlb.x, s, t);
     g.dv.x = s + t;
@@ -349,15 +354,260 @@ __device__ __forceinline__ bool geomSS32(const DevNodes& N, int A, int B, float 
     g.dv.y = s + t;
     dfDiff(vha.z, vla.z, vhb.z, vlb.z, s, t);
     g.dv.z = s + t;
-    g.w1 = F3{vha.w, vla.w, N.wz[A]};
-    g.w2 = F3{vhb.w, vlb.w, N.wz[B]};
+    g.w1 = F3{vha.w, vla.w, wza};
+    g.w2 = F3{vhb.w, vlb.w, wzb};
     return true;
 }
 
-// SSONLY: every contact of [c0, c1) joins two spheres of an aperiodic scene (no FP64 on the
-// evaluation path except contact creation).
-template <bool SSONLY>
-__global__ void __launch_bounds__(256, SSONLY ? 4 : 1) k_contact_fp32(DevNodes N, DevParticles P, DevContacts C, DevIncidence I,
+// L6Geom::trsf renormalisation step (L6Geom.cpp:129-135): every trsfRenorm-th step
+__device__ __forceinline__ bool renormStep(long long step, int every) {
+    if (every <= 0) return false;
+    if (step >= 0 && step < 0x7fffffffLL) return ((unsigned)step % (unsigned)every) == 0u;
+    return (step % every) == 0;
+}
+
+// Cp2_FrictMat_FrictPhys / Cp2_FrictMat_HertzPhys on contact creation (FrictMat.cpp:20-44,
+// Hertz.cpp:9-50), evaluated in FP64 from the FP32 geometry; ma/mb: the two nodes' mass.
+__device__ __forceinline__ void physCreate(const ScenePar& sp, float r1, float r2, float uN, const double4_32a& m1,
+                                           const double4_32a& m2, double ma, double mb, float& ph0, float& ph1, float& ph2,
+                                           float& ph3) {
+    double lens0 = fabs((double)r1) + (double)uN / 2, lens1 = fabs((double)r2) + (double)uN / 2;
+    if (lens0 < 0) lens0 = lens1;
+    if (lens1 < 0) lens1 = lens0;
+    const double rr = (r1 > 0 && r2 > 0) ? fmin((double)r1, (double)r2) : (r1 > 0 ? (double)r1 : (double)r2);
+    const double contA = 3.14159265358979323846 * (rr * rr);
+    ph3 = 0.f;
+    if (sp.phys == 0) {
+        const double kn = 1 / (1 / (m1.y * contA / lens0) + 1 / (m2.y * contA / lens1));
+        ph0 = (float)kn;
+        ph1 = (float)(.5 * (m1.w + m2.w) * kn);
+        ph2 = (float)fmin(m1.z, m2.z);
+    } else {
+        const double nu = sp.hzPoisson;
+        const double K = (4 / 3.) / ((1 - nu * nu) / m1.y + (1 - nu * nu) / m2.y);
+        const double R = 1. / (1. / lens0 + 1. / lens1);
+        const double kn0 = K * sqrt(R);
+        const double G = .5 * (m1.y / (2 * (1 + nu)) + m2.y / (2 * (1 + nu)));
+        ph0 = (float)kn0;
+        ph1 = (float)(2 * sqrt(4 * R) * G / (2 - nu));
+        ph2 = (float)fmin(m1.z, m2.z);
+        if (sp.hzViscOn) {
+            const double mbar = (ma <= 0 && mb > 0) ? mb : ((ma > 0 && mb <= 0) ? ma : (ma * mb) / (ma + mb));
+            ph3 = (float)fmax(0., sp.hzViscConst * sqrt(mbar * kn0));
+        }
+    }
+}
+
+// Sphere-sphere contacts of aperiodic scenes (work items [nMixed, nAct)), from the packed state:
+// item, flags and state are read at the contact's position in the work list (coalesced), the two
+// particles' mirror records are gathered; every load is issued before the step guard and the
+// branches, so a contact waits for two memory round trips. FP32 arithmetic throughout except
+// the IdealElPl shear accumulation (FP64) and contact creation.
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB) k_contact_ss32(DevNodes N, DevParticles P, DevContacts C, DevIncidence I, DevPackedSS K,
+                                                            const double4_32a* __restrict__ mats, const ScenePar* __restrict__ spp,
+                                                            const long long* __restrict__ dStep, int* __restrict__ dFlags, int64_t nm,
+                                                            int haltBlock, int loadFt) {
+    const int64_t j0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool in = j0 < K.n;
+    const int64_t j = in ? j0 : 0;
+    const int4 it = K.item[j];
+    const uint32_t pf = K.flags[j];
+    float st[CF_NCOL];
+#pragma unroll
+    for (int q = 0; q < CF_NCOL; q++) st[q] = K.col[q][j];
+    double ft1o = 0., ft2o = 0.;
+    if (loadFt) {  // some scene uses IdealElPl
+        ft1o = K.ft[0][j];
+        ft2o = K.ft[1][j];
+    }
+    const Mirror ma = N.mir[it.x], mb = N.mir[it.y];
+    const float wza = N.wz[it.x], wzb = N.wz[it.y];
+    const long long stepAbs = *dStep;
+    if (dFlags[FL_FULL] || halted(dFlags)) {
+        if (haltBlock && blockIdx.x == 0 && threadIdx.x == 0) dFlags[FL_HALT] = 1;
+        return;
+    }
+    if (!in) return;
+    int* dErr = dFlags + FL_ERR;
+    const int A = it.x, B = it.y;
+    const ScenePar& sp = spp[pf >> 8];
+    const long long step = stepAbs - sp.stepBase;
+    if (step >= sp.stepEnd) return;  // frozen scene (serving slot past its last step)
+    const uint32_t fl0 = pf & 0xffu, hiBits = pf & ~0xffu;
+    uint32_t fl = fl0;
+    if (fl & C_REMOVED) return;
+    if ((fl & C_PENDING) && !pendingStays(P, A, B, false, nullptr, dErr)) {
+        K.flags[j] = ((fl & ~C_PENDING) | C_REMOVED) | hiBits;
+        return;
+    }
+    fl &= ~C_PENDING;
+    const bool real = fl & C_REAL;
+    SSGeo g;
+    if (!geomSS32(ma, mb, wza, wzb, sp.ssDfAbsF, real, g)) {
+        if (fl != fl0) K.flags[j] = fl | hiBits;
+        return;
+    }
+    const float dtf = sp.dtF;
+    const F3 n = g.n;
+    const float uN = g.uN, r1 = g.r1, r2 = g.r2;
+    // contPt = x1 + (r1 + uN/2) n (Sphere.cpp:103), written relative to both centres
+    const F3 armA = (r1 + 0.5f * uN) * n;
+    const F3 armB = -(r2 + 0.5f * uN) * n;
+    Frame f, m;
+    F3 lvel{0, 0, 0};
+    float ph0, ph1, ph2, ph3;
+    if (!real) {
+        frameInit(n, f);
+        physCreate(sp, r1, r2, uN, mats[P.mat[A]], mats[P.mat[B]], N.minert[A].w, N.minert[B].w, ph0, ph1, ph2, ph3);
+        K.col[CF_P0][j] = ph0;
+        K.col[CF_P1][j] = ph1;
+        K.col[CF_P2][j] = ph2;
+        K.col[CF_P3][j] = ph3;
+        C.step0[I.work[nm + j].x] = (int32_t)step;
+        ft1o = 0.;
+        ft2o = 0.;
+        if (sp.law == 0) {
+            K.ft[0][j] = 0.;
+            K.ft[1][j] = 0.;
+        }
+    } else {
+        const F3 pn{st[CF_T0X], st[CF_T0Y], st[CF_T0Z]};
+        const F3 pc1{st[CF_T1X], st[CF_T1Y], st[CF_T1Z]};
+        const float up = st[CF_UN];
+        // mid-step branch vectors (L6Geom.cpp:156-160)
+        const F3 c1x = 0.5f * ((r1 + 0.5f * up) * pn + armA);
+        const F3 c2x = 0.5f * (-(r2 + 0.5f * up) * pn + armB);
+        frameUpdate(pn, pc1, n, g.w1, g.w2, dtf, renormStep(step, sp.trsfRenorm), f, m);
+        const F3 relVel = (g.dv + fcross(g.w2, c2x)) - fcross(g.w1, c1x);
+        lvel = F3{fdot(m.c0, relVel), fdot(m.c1, relVel), fdot(m.c2, relVel)};
+        ph0 = st[CF_P0];
+        ph1 = st[CF_P1];
+        ph2 = st[CF_P2];
+        ph3 = st[CF_P3];
+    }
+    float fn, ft1 = 0.f, ft2 = 0.f;
+    bool keep = true;
+    if (sp.law == 0) {
+        // Law2_L6Geom_FrictPhys_IdealElPl (IdealElPl.cpp:18-81), shear force accumulated in FP64
+        if (uN > 0 && !sp.noBreak) keep = false;
+        else {
+            fn = ph0 * uN;
+            if (sp.noFrict || ph2 == 0.f) {
+                K.ft[0][j] = 0.;
+                K.ft[1][j] = 0.;
+            } else {
+                double t1 = ft1o, t2 = ft2o;
+                t1 += (double)(dtf * ph1 * lvel.y);
+                t2 += (double)(dtf * ph1 * lvel.z);
+                const double maxFt = (double)(fabsf(fn) * ph2);
+                const double q = t1 * t1 + t2 * t2;
+                if (q > maxFt * maxFt && !sp.noSlip) {
+                    const double ratio = (q > 0) ? maxFt * rsqrt(q) : 0.;
+                    t1 *= ratio;
+                    t2 *= ratio;
+                }
+                K.ft[0][j] = t1;
+                K.ft[1][j] = t2;
+                ft1 = (float)t1;
+                ft2 = (float)t2;
+                if (isnan(fn) || isnan(t1) || isnan(t2)) atomicCAS(dErr, 0, 101);
+            }
+        }
+    } else {
+        // Law2_L6Geom_HertzPhys_DMT, DMT branch (Hertz.cpp:58-87,143-172)
+        if (uN > 0) keep = false;
+        else {
+            const float su = sqrtf(-uN);
+            const float Fne = -ph0 * (su * su * su);
+            const float eta = (ph3 > 0.f) ? ph3 * sqrtf(su) : 0.f;
+            float Fnv = eta * lvel.x;
+            if (sp.noAttraction && Fne + Fnv > 0.f) Fnv = -Fne;
+            fn = Fne + Fnv;  // the adhesion term 4 pi R gamma is zero (gamma = 0 is required in this mode)
+            const float kt = ph1 * su;
+            ft1 = dtf * kt * lvel.y;
+            ft2 = dtf * kt * lvel.z;
+            const float maxFt = fmaxf(0.f, fn) * ph2;
+            const float q = ft1 * ft1 + ft2 * ft2;
+            if (q > maxFt * maxFt) {
+                const float ratio = maxFt * rsqrtf(q);
+                ft1 *= ratio;
+                ft2 *= ratio;
+            } else {
+                ft1 += eta * lvel.y;
+                ft2 += eta * lvel.z;
+            }
+        }
+    }
+    if (!keep) {
+        K.flags[j] = ((fl & ~C_REAL) | C_PENDING) | hiBits;
+        if (real) {
+            I.endAf[it.z] = make_float4(0.f, 0.f, 0.f, 0.f);
+            I.endBf[it.z] = make_float2(0.f, 0.f);
+            I.endAf[it.w] = make_float4(0.f, 0.f, 0.f, 0.f);
+            I.endBf[it.w] = make_float2(0.f, 0.f);
+        }
+        return;
+    }
+    // force on pA in global coordinates: trsf * (Fn, Ft1, Ft2); torques about the nodes
+    const F3 F = fn * f.c0 + ft1 * f.c1 + ft2 * f.c2;
+    const F3 TA = fcross(armA, F), TB = fcross(armB, -F);
+    I.endAf[it.z] = make_float4(F.x, F.y, F.z, TA.x);
+    I.endBf[it.z] = make_float2(TA.y, TA.z);
+    I.endAf[it.w] = make_float4(-F.x, -F.y, -F.z, TB.x);
+    I.endBf[it.w] = make_float2(TB.y, TB.z);
+    K.col[CF_T0X][j] = f.c0.x;
+    K.col[CF_T0Y][j] = f.c0.y;
+    K.col[CF_T0Z][j] = f.c0.z;
+    K.col[CF_T1X][j] = f.c1.x;
+    K.col[CF_T1Y][j] = f.c1.y;
+    K.col[CF_T1Z][j] = f.c1.z;
+    K.col[CF_UN][j] = uN;
+    if ((fl | C_REAL) != fl0) K.flags[j] = (fl | C_REAL) | hiBits;
+}
+
+__global__ void k_pack_ss(DevContacts C, DevIncidence I, DevParticles P, DevPackedSS K, int64_t nm) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= K.n) return;
+    const int4 wk = I.work[nm + j];
+    const int64_t c = wk.x;
+    const uint32_t fl = C.flags[c];
+    const int32_t sl = I.slotLo[c], sh = I.slotHi[c];
+    const bool swap = fl & C_SWAP;
+    K.item[j] = make_int4(wk.y, wk.z, swap ? sh : sl, swap ? sl : sh);
+    K.flags[j] = fl | ((uint32_t)sceneOfP(P, wk.z) << 8);
+#pragma unroll
+    for (int q = 0; q < CF_NCOL; q++) K.col[q][j] = C.fcol[q][c];
+    if (K.ft[0]) {
+        K.ft[0][j] = C.col[CC_FT1][c];
+        K.ft[1][j] = C.col[CC_FT2][c];
+    }
+}
+
+__global__ void k_unpack_ss(DevContacts C, DevIncidence I, DevPackedSS K, int64_t nm) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= K.n) return;
+    const int64_t c = I.work[nm + j].x;
+    C.flags[c] = K.flags[j] & 0xffu;
+#pragma unroll
+    for (int q = 0; q < CF_NCOL; q++) C.fcol[q][c] = K.col[q][j];
+    if (K.ft[0]) {
+        C.col[CC_FT1][c] = K.ft[0][j];
+        C.col[CC_FT2][c] = K.ft[1][j];
+    }
+}
+
+void launch_pack_ss(cudaStream_t st, const DevContacts& C, const DevIncidence& I, const DevParticles& P, const DevPackedSS& K,
+                    int64_t nMixed) {
+    if (K.n > 0) k_pack_ss<<<(unsigned)((K.n + 255) / 256), 256, 0, st>>>(C, I, P, K, nMixed);
+}
+void launch_unpack_ss(cudaStream_t st, const DevContacts& C, const DevIncidence& I, const DevPackedSS& K, int64_t nMixed) {
+    if (K.n > 0) k_unpack_ss<<<(unsigned)((K.n + 255) / 256), 256, 0, st>>>(C, I, K, nMixed);
+}
+
+// Work items [c0, c1): facet and wall contacts, and every contact of a periodic scene (cell shifts,
+// FP64 geometry of the shifted pairs); the state is read and written in the contact arrays.
+__global__ void __launch_bounds__(256, 1) k_contact_fp32(DevNodes N, DevParticles P, DevContacts C, DevIncidence I,
                                                      const double4_32a* __restrict__ mats, const ScenePar* __restrict__ spp,
                                                      const long long* __restrict__ dStep, int* __restrict__ dFlags, int64_t c0,
                                                      int64_t c1, int haltBlock) {
@@ -388,7 +638,7 @@ __global__ void __launch_bounds__(256, SSONLY ? 4 : 1) k_contact_fp32(DevNodes N
     const float dtf = sp.dtF;
     bool shifted = false;
     D3 shift2{0, 0, 0}, shiftVel2{0, 0, 0};
-    if (!SSONLY && sp.periodic) {
+    if (sp.periodic) {
         int a, b, cc;
         unpackCellDist(C.cdist[c], a, b, cc);
         if (fl & C_SWAP) { a = -a; b = -b; cc = -cc; }
@@ -403,9 +653,9 @@ __global__ void __launch_bounds__(256, SSONLY ? 4 : 1) k_contact_fp32(DevNodes N
     // c1x/c2x: mid-step branch vectors of L6Geom.cpp:156-160; dv: relative velocity of the centres
     F3 n, armA, armB, c1x, c2x, dv, w1, w2;
     float uN, r1, r2;
-    if (SSONLY || (ty == CT_SS && !shifted)) {
+    if (ty == CT_SS && !shifted) {
         SSGeo g;
-        if (!geomSS32(N, A, B, sp.ssDfAbsF, real, g)) {
+        if (!geomSS32(N.mir[A], N.mir[B], N.wz[A], N.wz[B], sp.ssDfAbsF, real, g)) {
             C.flags[c] = fl;
             return;
         }
@@ -436,7 +686,7 @@ __global__ void __launch_bounds__(256, SSONLY ? 4 : 1) k_contact_fp32(DevNodes N
         w1 = toF(ld3(N.angv[A]));
         w2 = toF(ld3(N.angv[B]));
     }
-    if (SSONLY || ty == CT_SS) {
+    if (ty == CT_SS) {
         // contPt = x1 + (r1 + uN/2) n (Sphere.cpp:103), written relative to both centres
         armA = (r1 + 0.5f * uN) * n;
         armB = -(r2 + 0.5f * uN) * n;
@@ -446,7 +696,7 @@ __global__ void __launch_bounds__(256, SSONLY ? 4 : 1) k_contact_fp32(DevNodes N
             c1x = 0.5f * ((r1 + 0.5f * up) * pn + armA);
             c2x = 0.5f * (-(r2 + 0.5f * up) * pn + armB);
         }
-    } else if (!SSONLY) {
+    } else {
         Geo g;
         bool touch;
         if (ty == CT_WS) touch = geomWS(N, P, real ? (double)C.fcol[CF_T0X + P.aux[A].x][c] : 0., A, B, shift2, real, g);
@@ -480,33 +730,8 @@ __global__ void __launch_bounds__(256, SSONLY ? 4 : 1) k_contact_fp32(DevNodes N
     float ph0, ph1, ph2, ph3 = 0.f;
     if (!real) {
         frameInit(n, f);
-        // Cp2 on creation (FrictMat.cpp:20-44 / Hertz.cpp:9-50), evaluated in FP64
-        double lens0 = fabs((double)r1) + (double)uN / 2, lens1 = fabs((double)r2) + (double)uN / 2;
-        if (lens0 < 0) lens0 = lens1;
-        if (lens1 < 0) lens1 = lens0;
-        const double rr = (r1 > 0 && r2 > 0) ? fmin((double)r1, (double)r2) : (r1 > 0 ? (double)r1 : (double)r2);
-        const double contA = 3.14159265358979323846 * (rr * rr);
-        const double4_32a m1 = mats[P.mat[A]], m2 = mats[P.mat[B]];
-        if (sp.phys == 0) {
-            const double kn = 1 / (1 / (m1.y * contA / lens0) + 1 / (m2.y * contA / lens1));
-            ph0 = (float)kn;
-            ph1 = (float)(.5 * (m1.w + m2.w) * kn);
-            ph2 = (float)fmin(m1.z, m2.z);
-        } else {
-            const double nu = sp.hzPoisson;
-            const double K = (4 / 3.) / ((1 - nu * nu) / m1.y + (1 - nu * nu) / m2.y);
-            const double R = 1. / (1. / lens0 + 1. / lens1);
-            const double kn0 = K * sqrt(R);
-            const double G = .5 * (m1.y / (2 * (1 + nu)) + m2.y / (2 * (1 + nu)));
-            ph0 = (float)kn0;
-            ph1 = (float)(2 * sqrt(4 * R) * G / (2 - nu));
-            ph2 = (float)fmin(m1.z, m2.z);
-            if (sp.hzViscOn) {
-                const double ma = N.minert[P.shape[A] == WG_SHAPE_FACET ? P.aux[A].x : A].w, mb = N.minert[B].w;
-                const double mbar = (ma <= 0 && mb > 0) ? mb : ((ma > 0 && mb <= 0) ? ma : (ma * mb) / (ma + mb));
-                ph3 = (float)fmax(0., sp.hzViscConst * sqrt(mbar * kn0));
-            }
-        }
+        const double ma = N.minert[P.shape[A] == WG_SHAPE_FACET ? P.aux[A].x : A].w, mb = N.minert[B].w;
+        physCreate(sp, r1, r2, uN, mats[P.mat[A]], mats[P.mat[B]], ma, mb, ph0, ph1, ph2, ph3);
         C.fcol[CF_P0][c] = ph0;
         C.fcol[CF_P1][c] = ph1;
         C.fcol[CF_P2][c] = ph2;
@@ -519,7 +744,7 @@ __global__ void __launch_bounds__(256, SSONLY ? 4 : 1) k_contact_fp32(DevNodes N
     } else {
         const F3 pn{C.fcol[CF_T0X][c], C.fcol[CF_T0Y][c], C.fcol[CF_T0Z][c]};
         const F3 pc1{C.fcol[CF_T1X][c], C.fcol[CF_T1Y][c], C.fcol[CF_T1Z][c]};
-        frameUpdate(pn, pc1, n, w1, w2, dtf, sp.trsfRenorm > 0 && (step % sp.trsfRenorm) == 0, f, m);
+        frameUpdate(pn, pc1, n, w1, w2, dtf, renormStep(step, sp.trsfRenorm), f, m);
         const F3 relVel = (dv + fcross(w2, c2x)) - fcross(w1, c1x);
         lvel = F3{fdot(m.c0, relVel), fdot(m.c1, relVel), fdot(m.c2, relVel)};
         ph0 = C.fcol[CF_P0][c];
@@ -613,28 +838,32 @@ __global__ void __launch_bounds__(256, SSONLY ? 4 : 1) k_contact_fp32(DevNodes N
     C.flags[c] = fl | C_REAL;
 }
 
+// minimum resident blocks per SM the sphere-sphere kernel is compiled for (register budget)
+constexpr int kSSMinBlocks = 3;
+
 void launch_contact_fp32(cudaStream_t st, const SideStream& side, const DevNodes& N, const DevParticles& P, const DevContacts& C,
-                         const DevIncidence& I, const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dFlags,
-                         int64_t nMixed, bool periodic, int block) {
+                         const DevIncidence& I, const DevPackedSS& K, const double4_32a* mats, const ScenePar* sp,
+                         const long long* dStep, int* dFlags, int64_t nMixed, bool periodic, bool anyLaw0, int block) {
     const int64_t nm = periodic ? I.nAct : std::min<int64_t>(nMixed, I.nAct);
-    const int64_t ns = I.nAct - nm;
+    const int64_t ns = periodic ? 0 : K.n;
     const int64_t bs = block;
     if (ns > 0 && nm > 0 && side.st) {
         // the mixed range (facets and walls, FP64 geometry) beside the sphere-sphere range; the
         // sphere-sphere launch raises FL_HALT when a full run is due
         cudaEventRecord(side.fork, st);
         cudaStreamWaitEvent(side.st, side.fork, 0);
-        k_contact_fp32<false><<<(unsigned)((nm + 255) / 256), 256, 0, side.st>>>(N, P, C, I, mats, sp, dStep, dFlags, 0, nm, 0);
-        k_contact_fp32<true><<<(unsigned)((ns + bs - 1) / bs), (unsigned)bs, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags, nm, I.nAct, 1);
+        k_contact_fp32<<<(unsigned)((nm + 255) / 256), 256, 0, side.st>>>(N, P, C, I, mats, sp, dStep, dFlags, 0, nm, 0);
+        k_contact_ss32<kSSMinBlocks><<<(unsigned)((ns + bs - 1) / bs), (unsigned)bs, 0, st>>>(N, P, C, I, K, mats, sp, dStep, dFlags,
+                                                                                             nm, 1, anyLaw0);
         cudaEventRecord(side.join, side.st);
         cudaStreamWaitEvent(st, side.join, 0);
         return;
     }
     // the first launch also raises FL_HALT when a full run is due (it always runs)
-    k_contact_fp32<false><<<(unsigned)std::max<int64_t>(1, (nm + 255) / 256), 256, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags,
-                                                                                          0, nm, 1);
+    k_contact_fp32<<<(unsigned)std::max<int64_t>(1, (nm + 255) / 256), 256, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags, 0, nm, 1);
     if (ns > 0)
-        k_contact_fp32<true><<<(unsigned)((ns + bs - 1) / bs), (unsigned)bs, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags, nm, I.nAct, 0);
+        k_contact_ss32<kSSMinBlocks><<<(unsigned)((ns + bs - 1) / bs), (unsigned)bs, 0, st>>>(N, P, C, I, K, mats, sp, dStep, dFlags,
+                                                                                             nm, 0, anyLaw0);
 }
 
 // ---------------------------------------------------------------------------------- force sum
