@@ -143,6 +143,10 @@ def measure_gpu(args, rank, world, S=None, prec=None, e2e=True):
     S.run(args.warmup)
     sim = S._sim
     L, h = sim.H.L, sim.H.h
+    from woodem_gb300 import tune
+    tune.set_launch(sim, args.contact_block if (prec or args.precision) == "fp32" else 0, args.chunk_steps, False,
+                    args.concurrent_contacts)
+    S.run(3)
     st0 = sim.stats()
     log("[rank %d] warmup %d steps done in %.1fs: %d contacts (%d real), %d full runs" %
         (rank, args.warmup, time.time() - t0, st0.n_contacts, st0.n_real, st0.n_full_runs))
@@ -283,7 +287,8 @@ def measure_batch(args):
             key = "batched_%s_%s" % (prec, "tuned" if tuned else "default")
             out[key] = {"scene_steps_per_s": K * T / (ms / 1e3), "ms": ms}
             if best:
-                out[key]["launch"] = {"contact_block": best[0], "chunk_steps": best[1], "cuda_graph": bool(best[2])}
+                out[key]["launch"] = {"contact_block": best[0], "chunk_steps": best[1], "cuda_graph": bool(best[2]),
+                                      "concurrent_contacts": bool(best[3])}
             log("batch: %s %.1f ms" % (key, ms))
             B.close()
     base = out["one_at_a_time_fp64"]["scene_steps_per_s"]
@@ -388,6 +393,12 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=8.0, help="serving: job arrivals per second")
     ap.add_argument("--serve-seconds", type=float, default=15.0, help="serving: arrivals over this many seconds")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--contact-block", type=int, default=256,
+                    help="launch shape of the contact kernels (wg_set_launch): 128/256 one contact per thread, "
+                         "-128/-256 the persistent staged FP32 sphere-sphere kernel")
+    ap.add_argument("--chunk-steps", type=int, default=32, help="steps queued per host check of the collider request")
+    ap.add_argument("--concurrent-contacts", action="store_true",
+                    help="facet/wall contacts beside the sphere-sphere ones on a second stream (default: after them)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = env_rank()

@@ -112,10 +112,15 @@ int wg_set_config(wg_scene* s, const wg_config* c);
    batched. Replaces wg_set_config; call before the first run. */
 int wg_set_scenes(wg_scene* s, int32_t n_scenes, const wg_config* cfgs, const int64_t* particle_start);
 /* Launch shape (no counterpart in the reference): threads per block of the contact kernels
-   (0 = default, 64, 128, 256), steps queued per host check of the collider request (1..1024),
-   and use_graph != 0 to replay each such chunk of steps as one CUDA graph. Results do not depend
-   on these; only the speed does. */
-int wg_set_launch(wg_scene* s, int32_t contact_block, int32_t chunk_steps, int32_t use_graph);
+   (0 = default, 64, 128, 256; -128 or -256: the FP32 sphere-sphere contacts through a persistent
+   kernel of that many threads per block that stages batches of contacts in shared memory), steps
+   queued per host check of the collider request (1..1024), and flags: WG_LAUNCH_GRAPH replays each
+   such chunk of steps as one CUDA graph, WG_LAUNCH_CONCURRENT runs the facet/wall contacts beside
+   the sphere-sphere ones on a second stream instead of after them. Results do not depend on these;
+   only the speed does. */
+#define WG_LAUNCH_GRAPH 1
+#define WG_LAUNCH_CONCURRENT 2
+int wg_set_launch(wg_scene* s, int32_t contact_block, int32_t chunk_steps, int32_t launch_flags);
 /* Serving slots (no counterpart in the reference): the scenes of a batch (wg_set_scenes) are slots
    whose particle ranges bound the jobs they can hold. wg_slot_load puts a job (an aperiodic scene
    of n spheres and walls, its configuration, its n_mat materials indexed 0..n_mat-1, its step

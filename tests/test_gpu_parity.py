@@ -180,3 +180,26 @@ def test_call_granularity_is_invisible(prec):
     for k in ("pos", "vel", "angVel", "force", "torque"):
         assert np.array_equal(out[0][k], out[1][k]), "%s: one call vs many" % k
         assert np.array_equal(out[0][k], out[2][k]), "%s: one call vs host round trips" % k
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_launch_shape_is_invisible(prec, gpu_lib):
+    """Threads per contact block, the staged persistent sphere-sphere kernel (FP32-force mode),
+    steps per chunk and CUDA-graph replay change only the speed: a box settle (IdealElPl, walls)
+    and a drum (Hertz, facets, rotating walls) end bitwise the same under every launch shape."""
+    from woodem_gb300 import tune
+    shapes = [(0, 32, False, False), (128, 8, False, True), (-256, 32, True, False), (-128, 5, False, True)]
+    for build in (lambda: scenes.box_settle_small(n=1200, seed=5, precision=prec),
+                  lambda: scenes.hertz_drum(n=2500, seed=2, diameter=0.3, length=0.12, div=31, axDiv=6, fill_fraction=0.3,
+                                            precision=prec)):
+        out = []
+        for shape in shapes:
+            S = build()
+            S.run(1)
+            tune.set_launch(S._sim, *shape)
+            S.run(499)
+            out.append(_gpu_nodes(S))
+            S.close()
+        for q in range(1, len(shapes)):
+            for k in ("pos", "vel", "angVel", "force", "torque"):
+                assert np.array_equal(out[0][k], out[q][k]), "%s differs under launch shape %s" % (k, shapes[q])

@@ -449,6 +449,7 @@ int Sim::upload() {
     std::vector<double4_32a> facet(nPar);
     std::vector<uint32_t> mask(nPar);
     nSpheres = 0;
+    std::vector<int32_t> facetIds;
     for (int64_t p = 0; p < nPar; p++) {
         shape[p] = hShape[p];
         mat[p] = hMat[p];
@@ -462,7 +463,8 @@ int Sim::upload() {
             if (hAxis[p] < 0 || hAxis[p] > 2) return fail(WG_ERR_ARG, "Wall.axis must be 0, 1 or 2");
             aux[p] = make_int4(hAxis[p], hSense[p], 0, 0);
         } else if (hShape[p] == WG_SHAPE_FACET) {
-            aux[p] = make_int4(map[hNodes3[3 * p]], map[hNodes3[3 * p + 1]], map[hNodes3[3 * p + 2]], 0);
+            aux[p] = make_int4(map[hNodes3[3 * p]], map[hNodes3[3 * p + 1]], map[hNodes3[3 * p + 2]], (int)facetIds.size());
+            facetIds.push_back((int32_t)p);
             facet[p] = make_double4_32a(hFakeVel[3 * p], hFakeVel[3 * p + 1], hFakeVel[3 * p + 2], hHalfThick[p]);
         } else return fail(WG_ERR_UNSUPPORTED, "unknown shape code");
     }
@@ -527,6 +529,19 @@ int Sim::upload() {
     WG_CUDA_TRY(cudaMemcpy(N.flags, flags.data(), sizeof(uint32_t) * nSlots, cudaMemcpyHostToDevice));
     WG_CUDA_TRY(cudaMemcpy(P.shape, shape.data(), sizeof(int32_t) * nPar, cudaMemcpyHostToDevice));
     WG_CUDA_TRY(cudaMemcpy(P.aux, aux.data(), sizeof(int4) * nPar, cudaMemcpyHostToDevice));
+    P.nFacets = (int32_t)facetIds.size();
+    P.facetIds = nullptr;
+    P.prep = nullptr;
+    if (P.nFacets > 0) {
+        P.facetIds = (int32_t*)dalloc(sizeof(int32_t) * P.nFacets);
+        if (!P.facetIds) return fail(WG_ERR_CUDA, "out of device memory (facets)");
+        WG_CUDA_TRY(cudaMemcpy(P.facetIds, facetIds.data(), sizeof(int32_t) * P.nFacets, cudaMemcpyHostToDevice));
+        if (prec == WG_PREC_FP32) {
+            P.prep = (FacetPrep*)dalloc(sizeof(FacetPrep) * P.nFacets);
+            if (!P.prep) return fail(WG_ERR_CUDA, "out of device memory (facets)");
+            WG_CUDA_TRY(cudaMemset(P.prep, 0xff, sizeof(FacetPrep) * P.nFacets));  // NaN: made at the first step
+        }
+    }
     WG_CUDA_TRY(cudaMemcpy(P.facet, facet.data(), sizeof(double4_32a) * nPar, cudaMemcpyHostToDevice));
     WG_CUDA_TRY(cudaMemcpy(P.mat, mat.data(), sizeof(int32_t) * nPar, cudaMemcpyHostToDevice));
     WG_CUDA_TRY(cudaMemcpy(P.mask, mask.data(), sizeof(uint32_t) * nPar, cudaMemcpyHostToDevice));
@@ -697,8 +712,9 @@ int Sim::run(int64_t n) {
         launches++;
     };
     auto stepContact = [&]() {
-        if (fp32) launch_contact_fp32(stream, side, N, P, C, I, K, dMats, dPar, dStep, dFlags, nMixed, cfg.periodic != 0, anyLaw0,
-                                      contactBlock > 0 ? contactBlock : 256);
+        if (fp32) launch_contact_fp32(stream, concurrentContacts ? side : SideStream{}, N, P, C, I, K, dMats, dPar, dStep, dFlags, nMixed,
+                                      cfg.periodic != 0, anyLaw0,
+                                      contactBlock != 0 ? contactBlock : 256);
         else launch_contact_fp64(stream, N, P, C, I, dMats, dPar, dStep, dFlags,
                                  (contactBlock > 0 && contactBlock <= 128) ? contactBlock : 128);  // launch bounds 128
         launch_advance(stream, dStep, dFlags);
@@ -1153,15 +1169,18 @@ int wg_get_slot_nodes(wg_scene* s, int32_t k, int64_t n, double* pos, double* or
     return WG_OK;
 }
 
-int wg_set_launch(wg_scene* s, int32_t contact_block, int32_t chunk_steps, int32_t use_graph) {
+int wg_set_launch(wg_scene* s, int32_t contact_block, int32_t chunk_steps, int32_t launch_flags) {
     if (!s) return WG_ERR_ARG;
     Sim& S = *SIM(s);
-    if (contact_block != 0 && contact_block != 64 && contact_block != 128 && contact_block != 256)
-        return S.fail(WG_ERR_ARG, "contact_block must be 0, 64, 128 or 256");
+    if (contact_block != 0 && contact_block != 64 && contact_block != 128 && contact_block != 256 && contact_block != -128 &&
+        contact_block != -256)
+        return S.fail(WG_ERR_ARG, "contact_block must be 0, 64, 128, 256, -128 or -256");
     if (chunk_steps < 1 || chunk_steps > 1024) return S.fail(WG_ERR_ARG, "chunk_steps must be in [1, 1024]");
     S.contactBlock = contact_block;
     S.chunkSteps = chunk_steps;
-    S.useGraph = use_graph != 0;
+    if (launch_flags & ~(WG_LAUNCH_GRAPH | WG_LAUNCH_CONCURRENT)) return S.fail(WG_ERR_ARG, "unknown launch flag");
+    S.useGraph = (launch_flags & WG_LAUNCH_GRAPH) != 0;
+    S.concurrentContacts = (launch_flags & WG_LAUNCH_CONCURRENT) != 0;
     return WG_OK;
 }
 

@@ -81,10 +81,21 @@ struct DevNodes {
     int32_t* scene;  // batch of scenes: scene of each node slot (null: one scene)
     uint8_t* fresh;  // serving slots: node (re)loaded since its last step; Leapfrog takes its stored force
 };
+// FP32-force mode: the quantities of Cg2_Facet_Sphere_L6Geom that depend only on a facet's
+// vertices (Facet.cpp:240-246 and the barycentric matrix of CompUtils::triangleBarycentrics),
+// evaluated once per step for every facet instead of once per contact.
+struct FacetPrep {
+    double4_32a p0, p1, p2;  // vertices; w: the inverse barycentric matrix i00, i01, i10
+    double4_32a n;           // unit normal; w: i11
+    double4_32a e0, e1, e2;  // edge normals in the plane: (p1-p0) x nn, (p2-p1) x nn, (p0-p2) x nn
+};
 struct DevParticles {
     int32_t n;
     int32_t* shape;   // WG_SHAPE_*
-    int4* aux;        // facet: node slots n0 n1 n2; wall: axis sense
+    int4* aux;        // facet: node slots n0 n1 n2 and the facet's ordinal; wall: axis sense
+    int32_t nFacets;
+    int32_t* facetIds;  // particle id of each facet ordinal
+    FacetPrep* prep;    // FP32-force mode: per facet ordinal
     double4_32a* facet;   // fakeVel xyz, halfThick
     int32_t* mat;
     uint32_t* mask;
@@ -228,6 +239,8 @@ void launch_pack_ss(cudaStream_t st, const DevContacts& C, const DevIncidence& I
 void launch_unpack_ss(cudaStream_t st, const DevContacts& C, const DevIncidence& I, const DevPackedSS& K, int64_t nMixed);
 void launch_forces32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const NodeConst32* nc,
                      const ScenePar* sp, const int* dFlags, bool perStep);
+// FP32-force mode: P.prep from the current vertex positions (before the contact kernels of a step)
+void launch_facet_prep(cudaStream_t st, const DevNodes& N, const DevParticles& P, const int* dFlags);
 
 // ------------------------------------------------------------------ broad phase (wg_collide.cu)
 struct Grid {
@@ -305,6 +318,7 @@ struct Sim {
     int contactBlock = 0;    // 0: default (256 FP32, 128 FP64)
     int chunkSteps = 32;
     bool useGraph = false;
+    bool concurrentContacts = false;  // facet/wall contacts beside, not after, the sphere-sphere ones
     cudaGraphExec_t graphExec = nullptr;
     int64_t graphSteps = 0;  // steps in the captured chunk, 0: none valid
     int64_t graphEpoch = -1; // nFullRuns when it was captured

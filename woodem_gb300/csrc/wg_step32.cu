@@ -10,6 +10,7 @@
 //
 // Compiled with --fmad=true (results are compared to the FP64 oracle within a tolerance).
 #include <algorithm>
+#include <mutex>
 
 #include "wg_ends.cuh"
 #include "wg_geom.cuh"
@@ -21,6 +22,18 @@ struct F3 {
 };
 __device__ __forceinline__ F3 f3(float x, float y, float z) { return F3{x, y, z}; }
 __device__ __forceinline__ F3 toF(D3 a) { return F3{(float)a.x, (float)a.y, (float)a.z}; }
+// x truncated toward zero to FP32 with 32-bit integer operations on its words (no FP64-pipe
+// conversion): |x| below the FP32 normal range gives a signed zero; |x| >= 2^127, infinities and
+// NaN take the FP64 route.
+__device__ __forceinline__ float d2fT(double x) {
+    const unsigned top = (unsigned)__double2hiint(x), bot = (unsigned)__double2loint(x);
+    const unsigned sign = top & 0x80000000u;
+    const int e = (int)((top >> 20) & 0x7ffu);
+    if (e < 897) return __uint_as_float(sign);
+    if (e > 1150) return __double2float_rz(x);
+    return __uint_as_float(sign | ((unsigned)(e - 896) << 23) | ((top & 0xFFFFFu) << 3) | (bot >> 29));
+}
+__device__ __forceinline__ F3 toFt(D3 a) { return F3{d2fT(a.x), d2fT(a.y), d2fT(a.z)}; }
 __device__ __forceinline__ F3 operator+(F3 a, F3 b) { return F3{a.x + b.x, a.y + b.y, a.z + b.z}; }
 __device__ __forceinline__ F3 operator-(F3 a, F3 b) { return F3{a.x - b.x, a.y - b.y, a.z - b.z}; }
 __device__ __forceinline__ F3 operator-(F3 a) { return F3{-a.x, -a.y, -a.z}; }
@@ -28,13 +41,12 @@ __device__ __forceinline__ F3 operator*(F3 a, float s) { return F3{a.x * s, a.y 
 __device__ __forceinline__ F3 operator*(float s, F3 a) { return F3{s * a.x, s * a.y, s * a.z}; }
 __device__ __forceinline__ float fdot(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 __device__ __forceinline__ F3 fcross(F3 a, F3 b) { return F3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
-// x = h + l from the bits of x with integer operations only (FP64 arithmetic and conversions
-// issue at 1/64 of the FP32 rate on GB300): h is x truncated to 24 significant bits, l the
-// remaining 29 mantissa bits truncated to 24, so |x - (h + l)| < 2^-47 |x|. Zero, |x| < 2^-74
-// and |x| >= 2^127 take the FP64 route (h = fl32(x), l = fl32(x - h)).
+// x = h + l from the bits of x with 32-bit integer operations on its two words (FP64
+// arithmetic and conversions issue at 1/64 of the FP32 rate on GB300): h is x truncated to 24
+// significant bits, l the remaining 29 mantissa bits truncated to 24, so |x - (h + l)| < 2^-47 |x|.
+// Zero, |x| < 2^-74 and |x| >= 2^127 take the FP64 route (h = fl32(x), l = fl32(x - h)).
 __device__ __forceinline__ void splitDF(double x, float& h, float& l) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    const unsigned top = (unsigned)(b >> 32);
+    const unsigned top = (unsigned)__double2hiint(x), bot = (unsigned)__double2loint(x);
     const unsigned sign = top & 0x80000000u;
     const int e = (int)((top >> 20) & 0x7ffu);
     if (e < 949 || e > 1150) {
@@ -42,9 +54,9 @@ __device__ __forceinline__ void splitDF(double x, float& h, float& l) {
         l = __double2float_rn(x - (double)h);
         return;
     }
-    const unsigned long long m = b & 0x000FFFFFFFFFFFFFull;
-    h = __uint_as_float(sign | ((unsigned)(e - 896) << 23) | (unsigned)(m >> 29));
-    const unsigned r = (unsigned)(m & 0x1FFFFFFFull);
+    // the 52 mantissa bits are (top & 0xfffff):bot; h keeps the upper 23
+    h = __uint_as_float(sign | ((unsigned)(e - 896) << 23) | ((top & 0xFFFFFu) << 3) | (bot >> 29));
+    const unsigned r = bot & 0x1FFFFFFFu;
     if (r == 0) {
         l = 0.f;
         return;
@@ -53,15 +65,16 @@ __device__ __forceinline__ void splitDF(double x, float& h, float& l) {
     const unsigned frac = (p >= 23) ? (r >> (p - 23)) : (r << (23 - p));
     l = __uint_as_float(sign | ((unsigned)(p + e - 948) << 23) | (frac & 0x7FFFFFu));
 }
-// (double)f from the bits of f with integer operations (exact for normal numbers; FP32 subnormals,
-// below 1.2e-38, become zero; infinities and NaN take the FP64 route).
+// (double)f from the bits of f with 32-bit integer operations (exact for normal numbers; FP32
+// subnormals, below 1.2e-38, become zero; infinities and NaN take the FP64 route).
 __device__ __forceinline__ double f2d(float f) {
     const unsigned u = __float_as_uint(f);
     const unsigned e = (u >> 23) & 0xffu;
-    const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
-    if (e == 0) return __longlong_as_double((long long)sign);
+    const unsigned sign = u & 0x80000000u;
+    if (e == 0) return __hiloint2double((int)sign, 0);
     if (e == 0xffu) return (double)f;
-    return __longlong_as_double((long long)(sign | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29)));
+    const unsigned mant = u & 0x7fffffu;
+    return __hiloint2double((int)(sign | ((e + 896u) << 20) | (mant >> 3)), (int)(mant << 29));
 }
 // x rounded toward zero to FP32 (the h of splitDF)
 __device__ __forceinline__ float truncF(double x) {
@@ -398,37 +411,27 @@ __device__ __forceinline__ void physCreate(const ScenePar& sp, float r1, float r
     }
 }
 
-// Sphere-sphere contacts of aperiodic scenes (work items [nMixed, nAct)), from the packed state:
-// item, flags and state are read at the contact's position in the work list (coalesced), the two
-// particles' mirror records are gathered; every load is issued before the step guard and the
-// branches, so a contact waits for two memory round trips. FP32 arithmetic throughout except
-// the IdealElPl shear accumulation (FP64) and contact creation.
-template <int MINB>
-__global__ void __launch_bounds__(256, MINB) k_contact_ss32(DevNodes N, DevParticles P, DevContacts C, DevIncidence I, DevPackedSS K,
-                                                            const double4_32a* __restrict__ mats, const ScenePar* __restrict__ spp,
-                                                            const long long* __restrict__ dStep, int* __restrict__ dFlags, int64_t nm,
-                                                            int haltBlock, int loadFt) {
-    const int64_t j0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const bool in = j0 < K.n;
-    const int64_t j = in ? j0 : 0;
-    const int4 it = K.item[j];
-    const uint32_t pf = K.flags[j];
+// The values one sphere-sphere contact is evaluated from: its packed item, flags, state and the
+// two particles' mirror records.
+struct SSIn {
+    int4 it;
+    uint32_t pf;
     float st[CF_NCOL];
-#pragma unroll
-    for (int q = 0; q < CF_NCOL; q++) st[q] = K.col[q][j];
-    double ft1o = 0., ft2o = 0.;
-    if (loadFt) {  // some scene uses IdealElPl
-        ft1o = K.ft[0][j];
-        ft2o = K.ft[1][j];
-    }
-    const Mirror ma = N.mir[it.x], mb = N.mir[it.y];
-    const float wza = N.wz[it.x], wzb = N.wz[it.y];
-    const long long stepAbs = *dStep;
-    if (dFlags[FL_FULL] || halted(dFlags)) {
-        if (haltBlock && blockIdx.x == 0 && threadIdx.x == 0) dFlags[FL_HALT] = 1;
-        return;
-    }
-    if (!in) return;
+    double ft1o, ft2o;
+    Mirror ma, mb;
+    float wza, wzb;
+};
+
+// One sphere-sphere contact of an aperiodic scene (packed position j): Cg2_Sphere_Sphere_L6Geom,
+// Cp2 on creation, Law2, the two end slots and the packed state. FP32 arithmetic throughout
+// except the IdealElPl shear accumulation (FP64) and contact creation.
+__device__ __forceinline__ void ssContact(const SSIn& x, int64_t j, const DevNodes& N, const DevParticles& P, const DevContacts& C,
+                                          const DevIncidence& I, const DevPackedSS& K, const double4_32a* __restrict__ mats,
+                                          const ScenePar* __restrict__ spp, long long stepAbs, int* dFlags, int64_t nm) {
+    const int4 it = x.it;
+    const uint32_t pf = x.pf;
+    const float* st = x.st;
+    double ft1o = x.ft1o, ft2o = x.ft2o;
     int* dErr = dFlags + FL_ERR;
     const int A = it.x, B = it.y;
     const ScenePar& sp = spp[pf >> 8];
@@ -444,7 +447,7 @@ __global__ void __launch_bounds__(256, MINB) k_contact_ss32(DevNodes N, DevParti
     fl &= ~C_PENDING;
     const bool real = fl & C_REAL;
     SSGeo g;
-    if (!geomSS32(ma, mb, wza, wzb, sp.ssDfAbsF, real, g)) {
+    if (!geomSS32(x.ma, x.mb, x.wza, x.wzb, sp.ssDfAbsF, real, g)) {
         if (fl != fl0) K.flags[j] = fl | hiBits;
         return;
     }
@@ -566,6 +569,141 @@ __global__ void __launch_bounds__(256, MINB) k_contact_ss32(DevNodes N, DevParti
     if ((fl | C_REAL) != fl0) K.flags[j] = (fl | C_REAL) | hiBits;
 }
 
+// Sphere-sphere contacts of aperiodic scenes (work items [nMixed, nAct)), one per thread: item,
+// flags and state are read at the contact's position in the work list (coalesced), the two
+// particles' mirror records are gathered; every load is issued before the step guard and the
+// branches, so a contact waits for two memory round trips.
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB) k_contact_ss32(DevNodes N, DevParticles P, DevContacts C, DevIncidence I, DevPackedSS K,
+                                                            const double4_32a* __restrict__ mats, const ScenePar* __restrict__ spp,
+                                                            const long long* __restrict__ dStep, int* __restrict__ dFlags, int64_t nm,
+                                                            int haltBlock, int loadFt) {
+    const int64_t j0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool in = j0 < K.n;
+    const int64_t j = in ? j0 : 0;
+    SSIn x;
+    x.it = K.item[j];
+    x.pf = K.flags[j];
+#pragma unroll
+    for (int q = 0; q < CF_NCOL; q++) x.st[q] = K.col[q][j];
+    x.ft1o = 0.;
+    x.ft2o = 0.;
+    if (loadFt) {  // some scene uses IdealElPl
+        x.ft1o = K.ft[0][j];
+        x.ft2o = K.ft[1][j];
+    }
+    x.ma = N.mir[x.it.x];
+    x.mb = N.mir[x.it.y];
+    x.wza = N.wz[x.it.x];
+    x.wzb = N.wz[x.it.y];
+    const long long stepAbs = *dStep;
+    if (dFlags[FL_FULL] || halted(dFlags)) {
+        if (haltBlock && blockIdx.x == 0 && threadIdx.x == 0) dFlags[FL_HALT] = 1;
+        return;
+    }
+    if (!in) return;
+    ssContact(x, j, N, P, C, I, K, mats, spp, stepAbs, dFlags, nm);
+}
+
+// The same contacts through a persistent, software-pipelined block of T threads: batches of T
+// consecutive packed contacts are staged in shared memory with cp.async (no registers held by
+// loads in flight). While batch k is evaluated from registers, the mirror gathers of batch k+1
+// and the coalesced state loads of batch k+2 are in flight.
+template <int T>
+struct SSStage1 {
+    int4 it[T];
+    uint32_t pf[T];
+    float col[CF_NCOL][T];
+    double ft[2][T];
+};
+template <int T>
+struct SSStage2 {
+    float4 phA[T], plA[T], vhA[T], vlA[T], phB[T], plB[T], vhB[T], vlB[T];
+    float wzA[T], wzB[T];
+};
+template <int T>
+struct SSStaged {
+    SSStage1<T> s1[2];
+    SSStage2<T> s2[2];
+};
+template <int T>
+__device__ __forceinline__ void ssIssue1(SSStage1<T>& s, const DevPackedSS& K, int64_t j, int loadFt) {
+    const int t = threadIdx.x;
+    cpAsync<16>(&s.it[t], &K.item[j]);
+    cpAsyncCa<4>(&s.pf[t], &K.flags[j]);
+#pragma unroll
+    for (int q = 0; q < CF_NCOL; q++) cpAsyncCa<4>(&s.col[q][t], &K.col[q][j]);
+    if (loadFt) {
+        cpAsyncCa<8>(&s.ft[0][t], &K.ft[0][j]);
+        cpAsyncCa<8>(&s.ft[1][t], &K.ft[1][j]);
+    }
+}
+template <int T>
+__device__ __forceinline__ void ssIssue2(SSStage2<T>& s, int4 it, const DevNodes& N) {
+    const int t = threadIdx.x;
+    const Mirror* a = N.mir + it.x;
+    const Mirror* b = N.mir + it.y;
+    cpAsyncCa<16>(&s.phA[t], &a->ph);
+    cpAsyncCa<16>(&s.plA[t], &a->pl);
+    cpAsyncCa<16>(&s.vhA[t], &a->vh);
+    cpAsyncCa<16>(&s.vlA[t], &a->vl);
+    cpAsyncCa<16>(&s.phB[t], &b->ph);
+    cpAsyncCa<16>(&s.plB[t], &b->pl);
+    cpAsyncCa<16>(&s.vhB[t], &b->vh);
+    cpAsyncCa<16>(&s.vlB[t], &b->vl);
+    cpAsyncCa<4>(&s.wzA[t], N.wz + it.x);
+    cpAsyncCa<4>(&s.wzB[t], N.wz + it.y);
+}
+template <int T>
+__global__ void __launch_bounds__(T, 512 / T) k_contact_ss32s(DevNodes N, DevParticles P, DevContacts C, DevIncidence I, DevPackedSS K,
+                                                     const double4_32a* __restrict__ mats, const ScenePar* __restrict__ spp,
+                                                     const long long* __restrict__ dStep, int* __restrict__ dFlags, int64_t nm,
+                                                     int haltBlock, int loadFt) {
+    extern __shared__ __align__(16) unsigned char ssSmem[];
+    SSStaged<T>& S = *reinterpret_cast<SSStaged<T>*>(ssSmem);
+    const long long stepAbs = *dStep;
+    if (dFlags[FL_FULL] || halted(dFlags)) {
+        if (haltBlock && blockIdx.x == 0 && threadIdx.x == 0) dFlags[FL_HALT] = 1;
+        return;
+    }
+    const int t = threadIdx.x;
+    const int64_t nB = (K.n + T - 1) / T, stride = gridDim.x;
+    int64_t b = blockIdx.x;
+    if (b >= nB) return;
+    // prologue: state of batch b, then its gathers and the state of the next batch
+    if (b * T + t < K.n) ssIssue1(S.s1[0], K, b * T + t, loadFt);
+    cpAsyncWaitAll();
+    __syncthreads();
+    if (b * T + t < K.n) ssIssue2(S.s2[0], S.s1[0].it[t], N);
+    if (b + stride < nB && (b + stride) * T + t < K.n) ssIssue1(S.s1[1], K, (b + stride) * T + t, loadFt);
+    for (int k = 0; b < nB; k ^= 1, b += stride) {
+        cpAsyncWaitAll();
+        __syncthreads();
+        const int64_t j = b * T + t;
+        const bool in = j < K.n;
+        SSIn x;
+        if (in) {
+            const SSStage1<T>& a = S.s1[k];
+            const SSStage2<T>& g = S.s2[k];
+            x.it = a.it[t];
+            x.pf = a.pf[t];
+#pragma unroll
+            for (int q = 0; q < CF_NCOL; q++) x.st[q] = a.col[q][t];
+            x.ft1o = loadFt ? a.ft[0][t] : 0.;
+            x.ft2o = loadFt ? a.ft[1][t] : 0.;
+            x.ma = Mirror{g.phA[t], g.plA[t], g.vhA[t], g.vlA[t]};
+            x.mb = Mirror{g.phB[t], g.plB[t], g.vhB[t], g.vlB[t]};
+            x.wza = g.wzA[t];
+            x.wzb = g.wzB[t];
+        }
+        __syncthreads();
+        const int64_t j1 = (b + stride) * T + t, j2 = (b + 2 * stride) * T + t;
+        if (b + stride < nB && j1 < K.n) ssIssue2(S.s2[k ^ 1], S.s1[k ^ 1].it[t], N);
+        if (b + 2 * stride < nB && j2 < K.n) ssIssue1(S.s1[k], K, j2, loadFt);
+        if (in) ssContact(x, j, N, P, C, I, K, mats, spp, stepAbs, dFlags, nm);
+    }
+}
+
 __global__ void k_pack_ss(DevContacts C, DevIncidence I, DevParticles P, DevPackedSS K, int64_t nm) {
     const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= K.n) return;
@@ -605,19 +743,115 @@ void launch_unpack_ss(cudaStream_t st, const DevContacts& C, const DevIncidence&
     if (K.n > 0) k_unpack_ss<<<(unsigned)((K.n + 255) / 256), 256, 0, st>>>(C, I, K, nMixed);
 }
 
+// FacetPrep of every facet (Facet.cpp:240-246: normal; CompUtils.cpp:92-110: the barycentric
+// matrix), from the vertex positions of this step; a facet whose vertices are where they were
+// when its record was made keeps it (the record starts as NaN, which equals nothing).
+__global__ void k_facet_prep(DevNodes N, DevParticles P, const int* __restrict__ dFlags) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= P.nFacets || halted(dFlags)) return;
+    const int4 fn = P.aux[P.facetIds[f]];
+    const D3 p0 = ld3(N.posr[fn.x]), p1 = ld3(N.posr[fn.y]), p2 = ld3(N.posr[fn.z]);
+    {
+        const FacetPrep& F = P.prep[f];
+        const double4_32a o0 = F.p0, o1 = F.p1, o2 = F.p2;
+        if (o0.x == p0.x && o0.y == p0.y && o0.z == p0.z && o1.x == p1.x && o1.y == p1.y && o1.z == p1.z && o2.x == p2.x &&
+            o2.y == p2.y && o2.z == p2.z)
+            return;
+    }
+    const D3 nn = cross(p1 - p0, p2 - p0);
+    const D3 fNormal = normalized(nn);
+    const D3 e0 = cross(p1 - p0, nn), e1 = cross(p2 - p1, nn), e2 = cross(p0 - p2, nn);
+    const D3 vB = p1 - p0, vC = p2 - p0;
+    const double m00 = dot(vB, vB), m01 = dot(vC, vB), m10 = dot(vB, vC), m11 = dot(vC, vC);
+    const double det = m00 * m11 - m10 * m01;
+    const double invdet = 1. / det;
+    FacetPrep& F = P.prep[f];
+    F.p0 = make_double4_32a(p0.x, p0.y, p0.z, m11 * invdet);
+    F.p1 = make_double4_32a(p1.x, p1.y, p1.z, -m01 * invdet);
+    F.p2 = make_double4_32a(p2.x, p2.y, p2.z, -m10 * invdet);
+    F.n = make_double4_32a(fNormal.x, fNormal.y, fNormal.z, m00 * invdet);
+    F.e0 = make_double4_32a(e0.x, e0.y, e0.z, 0.);
+    F.e1 = make_double4_32a(e1.x, e1.y, e1.z, 0.);
+    F.e2 = make_double4_32a(e2.x, e2.y, e2.z, 0.);
+}
+void launch_facet_prep(cudaStream_t st, const DevNodes& N, const DevParticles& P, const int* dFlags) {
+    if (P.nFacets > 0 && P.prep) k_facet_prep<<<(P.nFacets + 63) / 64, 64, 0, st>>>(N, P, dFlags);
+}
+
+// Cg2_Facet_Sphere_L6Geom::go (Facet.cpp:235-288, Facet::interpolatePtLinAngVel :158-174) in FP64
+// from the facet's FacetPrep of this step: the per-contact part of the functor (plane distance,
+// region tests, closest point, barycentric velocity).
+__device__ __forceinline__ bool geomFS32(const DevNodes& N, const DevParticles& P, int A, int B, D3 shift2, bool real, Geo& g, int* dErr) {
+    const int4 fn = P.aux[A];
+    const FacetPrep& F = P.prep[fn.w];
+    const double4_32a fd = P.facet[A];
+    const double halfThick = fd.w;
+    const D3 fakeVel{fd.x, fd.y, fd.z};
+    const double4_32a ps = N.posr[B];
+    const double4_32a q0 = F.p0, q1 = F.p1, q2 = F.p2, qn = F.n;
+    const double radius = ps.w;
+    const D3 sC = ld3(ps) + shift2;
+    const D3 p0 = ld3(q0), p1 = ld3(q1), p2 = ld3(q2);
+    const D3 fNormal = ld3(qn);
+    const double planeDist = dot(sC - p0, fNormal);
+    if (fabs(planeDist) > (radius + halfThick) && !real) return false;
+    const D3 fC = sC - planeDist * fNormal;
+    const double l0 = dot(ld3(F.e0), fC - p0);
+    const double l1 = dot(ld3(F.e1), fC - p1);
+    const double l2 = dot(ld3(F.e2), fC - p2);
+    const int w = (l0 > 0 ? 1 : 0) + (l1 > 0 ? 2 : 0) + (l2 > 0 ? 4 : 0);
+    D3 contPt;
+    switch (w) {
+        case 0: contPt = fC; break;
+        case 1: contPt = closestSegmentPt(fC, p0, p1); break;
+        case 2: contPt = closestSegmentPt(fC, p1, p2); break;
+        case 4: contPt = closestSegmentPt(fC, p2, p0); break;
+        case 3: contPt = p1; break;
+        case 5: contPt = p0; break;
+        case 6: contPt = p2; break;
+        default: atomicCAS(dErr, 0, 100); return false;  // "Impossible sphere-facet intersection"
+    }
+    D3 normal = sC - contPt;
+    const double rh = radius + halfThick;
+    const double d2 = sqn(normal);
+    if (d2 > rh * rh && !real) return false;
+    const double dist = sqrt(d2);
+    normal = normal * (1. / dist);
+    if (halfThick > 0) contPt = contPt + normal * halfThick;
+    g.uN = (dist - radius) - halfThick;
+    // barycentric interpolation of the facet node velocities at contPt
+    const D3 vX = contPt - p0;
+    const double b0 = dot(vX, p1 - p0), b1 = dot(vX, p2 - p0);
+    const double u = q0.w * b0 + q1.w * b1, v = q2.w * b0 + qn.w * b1;
+    const double a0 = (1 - u) - v;
+    const D3 v0 = ld3(N.vel[fn.x]), v1 = ld3(N.vel[fn.y]), v2 = ld3(N.vel[fn.z]);
+    D3 linVel = (a0 * v0 + u * v1) + v * v2;
+    D3 angVel{0, 0, 0};
+    if (!isZero(v0) || !isZero(v1) || !isZero(v2))
+        angVel = (cross(p0 - contPt, v0) + cross(p1 - contPt, v1)) + cross(p2 - contPt, v2);
+    if (!isZero(fakeVel)) {
+        if (!isnan(fakeVel.x)) linVel = linVel + fakeVel;
+        else linVel = dot(linVel, fNormal) * fNormal;
+    }
+    g.normal = normal;
+    g.contPt = contPt;
+    g.pos1 = contPt;
+    g.vel1 = linVel;
+    g.angVel1 = angVel;
+    g.pos2 = sC;
+    g.vel2 = ld3(N.vel[B]);
+    g.angVel2 = ld3(N.angv[B]);
+    g.r1 = smax(halfThick, radius);
+    g.r2 = radius;
+    return true;
+}
+
 // Work items [c0, c1): facet and wall contacts, and every contact of a periodic scene (cell shifts,
 // FP64 geometry of the shifted pairs); the state is read and written in the contact arrays.
-__global__ void __launch_bounds__(256, 1) k_contact_fp32(DevNodes N, DevParticles P, DevContacts C, DevIncidence I,
-                                                     const double4_32a* __restrict__ mats, const ScenePar* __restrict__ spp,
-                                                     const long long* __restrict__ dStep, int* __restrict__ dFlags, int64_t c0,
-                                                     int64_t c1, int haltBlock) {
-    if (dFlags[FL_FULL] || halted(dFlags)) {
-        if (haltBlock && blockIdx.x == 0 && threadIdx.x == 0) dFlags[FL_HALT] = 1;
-        return;
-    }
+__device__ __forceinline__ void mixedContact(int64_t rk, const DevNodes& N, const DevParticles& P, const DevContacts& C,
+                                             const DevIncidence& I, const double4_32a* __restrict__ mats,
+                                             const ScenePar* __restrict__ spp, const long long* __restrict__ dStep, int* dFlags) {
     int* dErr = dFlags + FL_ERR;
-    const int64_t rk = c0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (rk >= c1) return;
     // work item: contact index, pA, pB and the static flag bits (type, swap) fixed at the full run
     const int4 wk = I.work[rk];
     const int64_t c = wk.x;
@@ -700,27 +934,27 @@ __global__ void __launch_bounds__(256, 1) k_contact_fp32(DevNodes N, DevParticle
         Geo g;
         bool touch;
         if (ty == CT_WS) touch = geomWS(N, P, real ? (double)C.fcol[CF_T0X + P.aux[A].x][c] : 0., A, B, shift2, real, g);
-        else touch = geomFS(N, P, A, B, shift2, real, g, dErr);
+        else touch = geomFS32(N, P, A, B, shift2, real, g, dErr);
         if (!touch) {
             C.flags[c] = fl;
             return;
         }
-        n = toF(g.normal);
-        uN = (float)g.uN;
-        r1 = (float)g.r1;
-        r2 = (float)g.r2;
+        n = toFt(g.normal);
+        uN = d2fT(g.uN);
+        r1 = d2fT(g.r1);
+        r2 = d2fT(g.r2);
         // walls are uninodal (their node is pos1); facets take no force here
-        armA = (ty == CT_WS) ? toF(g.contPt - g.pos1) : F3{0.f, 0.f, 0.f};
-        armB = toF(g.contPt - g.pos2);
+        armA = (ty == CT_WS) ? toFt(g.contPt - g.pos1) : F3{0.f, 0.f, 0.f};
+        armB = toFt(g.contPt - g.pos2);
         if (real) {
             const D3 prevCp{C.col[CC_CPX][c], C.col[CC_CPY][c], C.col[CC_CPZ][c]};
             const D3 mc = .5 * (prevCp + g.contPt);
-            c1x = toF(mc - (g.pos1 - (dt / 2.) * g.vel1));
-            c2x = toF(mc - (g.pos2 - (dt / 2.) * (g.vel2 + shiftVel2)));
+            c1x = toFt(mc - (g.pos1 - (dt / 2.) * g.vel1));
+            c2x = toFt(mc - (g.pos2 - (dt / 2.) * (g.vel2 + shiftVel2)));
         }
-        dv = toF((g.vel2 + shiftVel2) - g.vel1);
-        w1 = toF(g.angVel1);
-        w2 = toF(g.angVel2);
+        dv = toFt((g.vel2 + shiftVel2) - g.vel1);
+        w1 = toFt(g.angVel1);
+        w2 = toFt(g.angVel2);
         C.col[CC_CPX][c] = g.contPt.x;
         C.col[CC_CPY][c] = g.contPt.y;
         C.col[CC_CPZ][c] = g.contPt.z;
@@ -838,32 +1072,109 @@ __global__ void __launch_bounds__(256, 1) k_contact_fp32(DevNodes N, DevParticle
     C.flags[c] = fl | C_REAL;
 }
 
-// minimum resident blocks per SM the sphere-sphere kernel is compiled for (register budget)
+// One thread per work item of [c0, c1), looping over the range with the grid's stride (the
+// launch sizes the grid so that its blocks leave room for the sphere-sphere kernel beside it).
+__global__ void __launch_bounds__(128, 4) k_contact_fp32(DevNodes N, DevParticles P, DevContacts C, DevIncidence I,
+                                                       const double4_32a* __restrict__ mats, const ScenePar* __restrict__ spp,
+                                                       const long long* __restrict__ dStep, int* __restrict__ dFlags, int64_t c0,
+                                                       int64_t c1, int haltBlock) {
+    if (dFlags[FL_FULL] || halted(dFlags)) {
+        if (haltBlock && blockIdx.x == 0 && threadIdx.x == 0) dFlags[FL_HALT] = 1;
+        return;
+    }
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t rk = c0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; rk < c1; rk += stride)
+        mixedContact(rk, N, P, C, I, mats, spp, dStep, dFlags);
+}
+
+// minimum resident blocks per SM the one-contact-per-thread kernel is compiled for (register budget)
 constexpr int kSSMinBlocks = 3;
+
+// streaming multiprocessors of the current device
+static int smCount() {
+    static std::mutex mu;
+    static int n[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 1;
+    std::lock_guard<std::mutex> lk(mu);
+    if (!n[dev] && (cudaDeviceGetAttribute(&n[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n[dev] < 1)) n[dev] = 1;
+    return n[dev];
+}
+
+// grid of the persistent staged kernel: resident blocks per SM x SMs, per device (set up once)
+template <int T>
+static int stagedGrid(size_t smem) {
+    static std::mutex mu;
+    static int grid[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
+    std::lock_guard<std::mutex> lk(mu);
+    if (!grid[dev]) {
+        int sms = 0, per = 0;
+        if (cudaFuncSetAttribute(k_contact_ss32s<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_contact_ss32s<T>, T, smem) != cudaSuccess || per < 1)
+            return 0;
+        grid[dev] = per * sms;
+    }
+    return grid[dev];
+}
+
+// sphere-sphere range: block > 0 one contact per thread with that many threads per block; block < 0
+// the persistent staged kernel with -block (128 or 256) threads per block
+static void launchSS(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C, const DevIncidence& I,
+                     const DevPackedSS& K, const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dFlags, int64_t nm,
+                     int halt, int loadFt, int block) {
+    if (block < 0) {
+        const int T = (block == -128) ? 128 : 256;
+        const int64_t nB = (K.n + T - 1) / T;
+        if (T == 128) {
+            const size_t smem = sizeof(SSStaged<128>);
+            const int g = stagedGrid<128>(smem);
+            if (g > 0) {
+                k_contact_ss32s<128><<<(unsigned)std::min<int64_t>(nB, g), 128, smem, st>>>(N, P, C, I, K, mats, sp, dStep, dFlags, nm,
+                                                                                          halt, loadFt);
+                return;
+            }
+        } else {
+            const size_t smem = sizeof(SSStaged<256>);
+            const int g = stagedGrid<256>(smem);
+            if (g > 0) {
+                k_contact_ss32s<256><<<(unsigned)std::min<int64_t>(nB, g), 256, smem, st>>>(N, P, C, I, K, mats, sp, dStep, dFlags, nm,
+                                                                                          halt, loadFt);
+                return;
+            }
+        }
+        block = 256;  // the staged kernel could not be set up on this device
+    }
+    k_contact_ss32<kSSMinBlocks><<<(unsigned)((K.n + block - 1) / block), (unsigned)block, 0, st>>>(N, P, C, I, K, mats, sp, dStep,
+                                                                                                 dFlags, nm, halt, loadFt);
+}
 
 void launch_contact_fp32(cudaStream_t st, const SideStream& side, const DevNodes& N, const DevParticles& P, const DevContacts& C,
                          const DevIncidence& I, const DevPackedSS& K, const double4_32a* mats, const ScenePar* sp,
                          const long long* dStep, int* dFlags, int64_t nMixed, bool periodic, bool anyLaw0, int block) {
     const int64_t nm = periodic ? I.nAct : std::min<int64_t>(nMixed, I.nAct);
     const int64_t ns = periodic ? 0 : K.n;
-    const int64_t bs = block;
     if (ns > 0 && nm > 0 && side.st) {
         // the mixed range (facets and walls, FP64 geometry) beside the sphere-sphere range; the
         // sphere-sphere launch raises FL_HALT when a full run is due
         cudaEventRecord(side.fork, st);
         cudaStreamWaitEvent(side.st, side.fork, 0);
-        k_contact_fp32<<<(unsigned)((nm + 255) / 256), 256, 0, side.st>>>(N, P, C, I, mats, sp, dStep, dFlags, 0, nm, 0);
-        k_contact_ss32<kSSMinBlocks><<<(unsigned)((ns + bs - 1) / bs), (unsigned)bs, 0, st>>>(N, P, C, I, K, mats, sp, dStep, dFlags,
-                                                                                             nm, 1, anyLaw0);
+        launch_facet_prep(side.st, N, P, dFlags);
+        // one block of 128 threads per SM: two blocks of the sphere-sphere kernel still fit beside it
+        k_contact_fp32<<<(unsigned)std::min<int64_t>((nm + 127) / 128, smCount()), 128, 0, side.st>>>(N, P, C, I, mats, sp, dStep,
+                                                                                                     dFlags, 0, nm, 0);
+        launchSS(st, N, P, C, I, K, mats, sp, dStep, dFlags, nm, 1, anyLaw0, block);
         cudaEventRecord(side.join, side.st);
         cudaStreamWaitEvent(st, side.join, 0);
         return;
     }
     // the first launch also raises FL_HALT when a full run is due (it always runs)
-    k_contact_fp32<<<(unsigned)std::max<int64_t>(1, (nm + 255) / 256), 256, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags, 0, nm, 1);
-    if (ns > 0)
-        k_contact_ss32<kSSMinBlocks><<<(unsigned)((ns + bs - 1) / bs), (unsigned)bs, 0, st>>>(N, P, C, I, K, mats, sp, dStep, dFlags,
-                                                                                             nm, 0, anyLaw0);
+    if (nm > 0) launch_facet_prep(st, N, P, dFlags);
+    k_contact_fp32<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>((nm + 127) / 128, 4 * smCount())), 128, 0, st>>>(
+        N, P, C, I, mats, sp, dStep, dFlags, 0, nm, 1);
+    if (ns > 0) launchSS(st, N, P, C, I, K, mats, sp, dStep, dFlags, nm, 0, anyLaw0, block);
 }
 
 // ---------------------------------------------------------------------------------- force sum

@@ -11,13 +11,18 @@ import ctypes as C
 import numpy as np
 
 DEFAULT_CANDIDATES = (
-    # (contact threads per block, steps per chunk, CUDA graph)
-    (256, 32, False),
-    (128, 32, False),
-    (256, 8, True),
-    (256, 32, True),
-    (128, 32, True),
-    (256, 64, True),
+    # (contact threads per block, steps per chunk, CUDA graph, facet/wall contacts on a second
+    # stream beside the sphere-sphere ones); a negative block selects the persistent staged FP32
+    # sphere-sphere kernel with that many threads
+    (256, 32, False, False),
+    (256, 32, False, True),
+    (128, 32, False, False),
+    (-256, 32, False, False),
+    (-128, 32, False, False),
+    (256, 8, True, False),
+    (256, 32, True, False),
+    (256, 32, True, True),
+    (256, 64, True, False),
 )
 
 
@@ -25,9 +30,9 @@ def _handle(sim):
     return sim.H.L, sim.H.h
 
 
-def set_launch(sim, block=0, chunk=32, graph=False):
+def set_launch(sim, block=0, chunk=32, graph=False, concurrent=False):
     L, h = _handle(sim)
-    sim.H.check(L.wg_set_launch(h, int(block), int(chunk), int(bool(graph))), "set_launch")
+    sim.H.check(L.wg_set_launch(h, int(block), int(chunk), (1 if graph else 0) | (2 if concurrent else 0)), "set_launch")
 
 
 def _run_ms(sim, steps):
