@@ -393,9 +393,9 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=8.0, help="serving: job arrivals per second")
     ap.add_argument("--serve-seconds", type=float, default=15.0, help="serving: arrivals over this many seconds")
     ap.add_argument("--no-serve", action="store_true")
-    ap.add_argument("--contact-block", type=int, default=256,
+    ap.add_argument("--contact-block", type=int, default=0,
                     help="launch shape of the contact kernels (wg_set_launch): 128/256 one contact per thread, "
-                         "-128/-256 the persistent staged FP32 sphere-sphere kernel")
+                         "-256 the resident-grid FP32 sphere-sphere kernel with prefetch")
     ap.add_argument("--chunk-steps", type=int, default=32, help="steps queued per host check of the collider request")
     ap.add_argument("--concurrent-contacts", action="store_true",
                     help="facet/wall contacts beside the sphere-sphere ones on a second stream (default: after them)")

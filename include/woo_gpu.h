@@ -112,8 +112,8 @@ int wg_set_config(wg_scene* s, const wg_config* c);
    batched. Replaces wg_set_config; call before the first run. */
 int wg_set_scenes(wg_scene* s, int32_t n_scenes, const wg_config* cfgs, const int64_t* particle_start);
 /* Launch shape (no counterpart in the reference): threads per block of the contact kernels
-   (0 = default, 64, 128, 256; -128 or -256: the FP32 sphere-sphere contacts through a persistent
-   kernel of that many threads per block that stages batches of contacts in shared memory), steps
+   (0 = default, 64, 128, 256; -256: the FP32 sphere-sphere contacts through a resident grid whose
+   threads prefetch their next contact), steps
    queued per host check of the collider request (1..1024), and flags: WG_LAUNCH_GRAPH replays each
    such chunk of steps as one CUDA graph, WG_LAUNCH_CONCURRENT runs the facet/wall contacts beside
    the sphere-sphere ones on a second stream instead of after them. Results do not depend on these;

@@ -184,11 +184,11 @@ def test_call_granularity_is_invisible(prec):
 
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])
 def test_launch_shape_is_invisible(prec, gpu_lib):
-    """Threads per contact block, the staged persistent sphere-sphere kernel (FP32-force mode),
+    """Threads per contact block, the resident-grid sphere-sphere kernel (FP32-force mode),
     steps per chunk and CUDA-graph replay change only the speed: a box settle (IdealElPl, walls)
     and a drum (Hertz, facets, rotating walls) end bitwise the same under every launch shape."""
     from woodem_gb300 import tune
-    shapes = [(0, 32, False, False), (128, 8, False, True), (-256, 32, True, False), (-128, 5, False, True)]
+    shapes = [(0, 32, False, False), (128, 8, False, True), (-256, 32, True, False), (-256, 5, False, True)]
     for build in (lambda: scenes.box_settle_small(n=1200, seed=5, precision=prec),
                   lambda: scenes.hertz_drum(n=2500, seed=2, diameter=0.3, length=0.12, div=31, axDiv=6, fill_fraction=0.3,
                                             precision=prec)):

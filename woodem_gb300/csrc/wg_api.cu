@@ -714,7 +714,7 @@ int Sim::run(int64_t n) {
     auto stepContact = [&]() {
         if (fp32) launch_contact_fp32(stream, concurrentContacts ? side : SideStream{}, N, P, C, I, K, dMats, dPar, dStep, dFlags, nMixed,
                                       cfg.periodic != 0, anyLaw0,
-                                      contactBlock != 0 ? contactBlock : 256);
+                                      contactBlock != 0 ? contactBlock : -256);
         else launch_contact_fp64(stream, N, P, C, I, dMats, dPar, dStep, dFlags,
                                  (contactBlock > 0 && contactBlock <= 128) ? contactBlock : 128);  // launch bounds 128
         launch_advance(stream, dStep, dFlags);
@@ -1172,9 +1172,8 @@ int wg_get_slot_nodes(wg_scene* s, int32_t k, int64_t n, double* pos, double* or
 int wg_set_launch(wg_scene* s, int32_t contact_block, int32_t chunk_steps, int32_t launch_flags) {
     if (!s) return WG_ERR_ARG;
     Sim& S = *SIM(s);
-    if (contact_block != 0 && contact_block != 64 && contact_block != 128 && contact_block != 256 && contact_block != -128 &&
-        contact_block != -256)
-        return S.fail(WG_ERR_ARG, "contact_block must be 0, 64, 128, 256, -128 or -256");
+    if (contact_block != 0 && contact_block != 64 && contact_block != 128 && contact_block != 256 && contact_block != -256)
+        return S.fail(WG_ERR_ARG, "contact_block must be 0, 64, 128, 256 or -256");
     if (chunk_steps < 1 || chunk_steps > 1024) return S.fail(WG_ERR_ARG, "chunk_steps must be in [1, 1024]");
     S.contactBlock = contact_block;
     S.chunkSteps = chunk_steps;

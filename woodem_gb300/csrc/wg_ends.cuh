@@ -97,13 +97,6 @@ __device__ __forceinline__ void cpAsync(void* dst, const void* src) {
         asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d + 16u), "l"((const char*)src + 16) : "memory");
     }
 }
-// the same, cached in L1 (4, 8 or 16 bytes)
-template <int BYTES>
-__device__ __forceinline__ void cpAsyncCa(void* dst, const void* src) {
-    static_assert(BYTES == 4 || BYTES == 8 || BYTES == 16, "4, 8 or 16 bytes");
-    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(d), "l"(src), "n"(BYTES) : "memory");
-}
 __device__ __forceinline__ void cpAsyncWaitAll() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 // Adds the end slots [e0, e1) of every lane with take==true to acc. Must be called by all

@@ -315,7 +315,7 @@ struct Sim {
     bool fromEnds = false;   // the end slots hold the forces of the last contact loop
     // launch shape (wg_set_launch): threads per block of the contact kernels, steps queued per host
     // check, and whether a chunk of steps is replayed as a CUDA graph
-    int contactBlock = 0;    // 0: default (256 FP32, 128 FP64)
+    int contactBlock = 0;    // 0: default (FP32: the resident-grid sphere-sphere kernel; FP64: 128)
     int chunkSteps = 32;
     bool useGraph = false;
     bool concurrentContacts = false;  // facet/wall contacts beside, not after, the sphere-sphere ones

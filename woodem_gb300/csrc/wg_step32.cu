@@ -605,102 +605,41 @@ __global__ void __launch_bounds__(256, MINB) k_contact_ss32(DevNodes N, DevParti
     ssContact(x, j, N, P, C, I, K, mats, spp, stepAbs, dFlags, nm);
 }
 
-// The same contacts through a persistent, software-pipelined block of T threads: batches of T
-// consecutive packed contacts are staged in shared memory with cp.async (no registers held by
-// loads in flight). While batch k is evaluated from registers, the mirror gathers of batch k+1
-// and the coalesced state loads of batch k+2 are in flight.
-template <int T>
-struct SSStage1 {
-    int4 it[T];
-    uint32_t pf[T];
-    float col[CF_NCOL][T];
-    double ft[2][T];
-};
-template <int T>
-struct SSStage2 {
-    float4 phA[T], plA[T], vhA[T], vlA[T], phB[T], plB[T], vhB[T], vlB[T];
-    float wzA[T], wzB[T];
-};
-template <int T>
-struct SSStaged {
-    SSStage1<T> s1[2];
-    SSStage2<T> s2[2];
-};
-template <int T>
-__device__ __forceinline__ void ssIssue1(SSStage1<T>& s, const DevPackedSS& K, int64_t j, int loadFt) {
-    const int t = threadIdx.x;
-    cpAsync<16>(&s.it[t], &K.item[j]);
-    cpAsyncCa<4>(&s.pf[t], &K.flags[j]);
-#pragma unroll
-    for (int q = 0; q < CF_NCOL; q++) cpAsyncCa<4>(&s.col[q][t], &K.col[q][j]);
-    if (loadFt) {
-        cpAsyncCa<8>(&s.ft[0][t], &K.ft[0][j]);
-        cpAsyncCa<8>(&s.ft[1][t], &K.ft[1][j]);
-    }
-}
-template <int T>
-__device__ __forceinline__ void ssIssue2(SSStage2<T>& s, int4 it, const DevNodes& N) {
-    const int t = threadIdx.x;
-    const Mirror* a = N.mir + it.x;
-    const Mirror* b = N.mir + it.y;
-    cpAsyncCa<16>(&s.phA[t], &a->ph);
-    cpAsyncCa<16>(&s.plA[t], &a->pl);
-    cpAsyncCa<16>(&s.vhA[t], &a->vh);
-    cpAsyncCa<16>(&s.vlA[t], &a->vl);
-    cpAsyncCa<16>(&s.phB[t], &b->ph);
-    cpAsyncCa<16>(&s.plB[t], &b->pl);
-    cpAsyncCa<16>(&s.vhB[t], &b->vh);
-    cpAsyncCa<16>(&s.vlB[t], &b->vl);
-    cpAsyncCa<4>(&s.wzA[t], N.wz + it.x);
-    cpAsyncCa<4>(&s.wzB[t], N.wz + it.y);
-}
-template <int T>
-__global__ void __launch_bounds__(T, 512 / T) k_contact_ss32s(DevNodes N, DevParticles P, DevContacts C, DevIncidence I, DevPackedSS K,
-                                                     const double4_32a* __restrict__ mats, const ScenePar* __restrict__ spp,
-                                                     const long long* __restrict__ dStep, int* __restrict__ dFlags, int64_t nm,
-                                                     int haltBlock, int loadFt) {
-    extern __shared__ __align__(16) unsigned char ssSmem[];
-    SSStaged<T>& S = *reinterpret_cast<SSStaged<T>*>(ssSmem);
+// The same contacts through a resident grid, each thread walking the range with the grid's
+// stride: the next contact's packed item is loaded while the current contact's state and mirror
+// records are in flight, so each contact waits for one memory round trip instead of two.
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB) k_contact_ss32p(DevNodes N, DevParticles P, DevContacts C, DevIncidence I, DevPackedSS K,
+                                                             const double4_32a* __restrict__ mats, const ScenePar* __restrict__ spp,
+                                                             const long long* __restrict__ dStep, int* __restrict__ dFlags, int64_t nm,
+                                                             int haltBlock, int loadFt) {
     const long long stepAbs = *dStep;
     if (dFlags[FL_FULL] || halted(dFlags)) {
         if (haltBlock && blockIdx.x == 0 && threadIdx.x == 0) dFlags[FL_HALT] = 1;
         return;
     }
-    const int t = threadIdx.x;
-    const int64_t nB = (K.n + T - 1) / T, stride = gridDim.x;
-    int64_t b = blockIdx.x;
-    if (b >= nB) return;
-    // prologue: state of batch b, then its gathers and the state of the next batch
-    if (b * T + t < K.n) ssIssue1(S.s1[0], K, b * T + t, loadFt);
-    cpAsyncWaitAll();
-    __syncthreads();
-    if (b * T + t < K.n) ssIssue2(S.s2[0], S.s1[0].it[t], N);
-    if (b + stride < nB && (b + stride) * T + t < K.n) ssIssue1(S.s1[1], K, (b + stride) * T + t, loadFt);
-    for (int k = 0; b < nB; k ^= 1, b += stride) {
-        cpAsyncWaitAll();
-        __syncthreads();
-        const int64_t j = b * T + t;
-        const bool in = j < K.n;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= K.n) return;
+    int4 next = K.item[j];
+    for (; j < K.n; j += stride) {
         SSIn x;
-        if (in) {
-            const SSStage1<T>& a = S.s1[k];
-            const SSStage2<T>& g = S.s2[k];
-            x.it = a.it[t];
-            x.pf = a.pf[t];
+        x.it = next;
+        if (j + stride < K.n) next = K.item[j + stride];
+        x.pf = K.flags[j];
 #pragma unroll
-            for (int q = 0; q < CF_NCOL; q++) x.st[q] = a.col[q][t];
-            x.ft1o = loadFt ? a.ft[0][t] : 0.;
-            x.ft2o = loadFt ? a.ft[1][t] : 0.;
-            x.ma = Mirror{g.phA[t], g.plA[t], g.vhA[t], g.vlA[t]};
-            x.mb = Mirror{g.phB[t], g.plB[t], g.vhB[t], g.vlB[t]};
-            x.wza = g.wzA[t];
-            x.wzb = g.wzB[t];
+        for (int q = 0; q < CF_NCOL; q++) x.st[q] = K.col[q][j];
+        x.ft1o = 0.;
+        x.ft2o = 0.;
+        if (loadFt) {
+            x.ft1o = K.ft[0][j];
+            x.ft2o = K.ft[1][j];
         }
-        __syncthreads();
-        const int64_t j1 = (b + stride) * T + t, j2 = (b + 2 * stride) * T + t;
-        if (b + stride < nB && j1 < K.n) ssIssue2(S.s2[k ^ 1], S.s1[k ^ 1].it[t], N);
-        if (b + 2 * stride < nB && j2 < K.n) ssIssue1(S.s1[k], K, j2, loadFt);
-        if (in) ssContact(x, j, N, P, C, I, K, mats, spp, stepAbs, dFlags, nm);
+        x.ma = N.mir[x.it.x];
+        x.mb = N.mir[x.it.y];
+        x.wza = N.wz[x.it.x];
+        x.wzb = N.wz[x.it.y];
+        ssContact(x, j, N, P, C, I, K, mats, spp, stepAbs, dFlags, nm);
     }
 }
 
@@ -1101,51 +1040,15 @@ static int smCount() {
     return n[dev];
 }
 
-// grid of the persistent staged kernel: resident blocks per SM x SMs, per device (set up once)
-template <int T>
-static int stagedGrid(size_t smem) {
-    static std::mutex mu;
-    static int grid[64] = {0};
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
-    std::lock_guard<std::mutex> lk(mu);
-    if (!grid[dev]) {
-        int sms = 0, per = 0;
-        if (cudaFuncSetAttribute(k_contact_ss32s<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_contact_ss32s<T>, T, smem) != cudaSuccess || per < 1)
-            return 0;
-        grid[dev] = per * sms;
-    }
-    return grid[dev];
-}
-
-// sphere-sphere range: block > 0 one contact per thread with that many threads per block; block < 0
-// the persistent staged kernel with -block (128 or 256) threads per block
+// sphere-sphere range: block > 0 one contact per thread with that many threads per block;
+// block < 0 the resident-grid kernel with prefetch (256 threads per block)
 static void launchSS(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C, const DevIncidence& I,
                      const DevPackedSS& K, const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dFlags, int64_t nm,
                      int halt, int loadFt, int block) {
     if (block < 0) {
-        const int T = (block == -128) ? 128 : 256;
-        const int64_t nB = (K.n + T - 1) / T;
-        if (T == 128) {
-            const size_t smem = sizeof(SSStaged<128>);
-            const int g = stagedGrid<128>(smem);
-            if (g > 0) {
-                k_contact_ss32s<128><<<(unsigned)std::min<int64_t>(nB, g), 128, smem, st>>>(N, P, C, I, K, mats, sp, dStep, dFlags, nm,
-                                                                                          halt, loadFt);
-                return;
-            }
-        } else {
-            const size_t smem = sizeof(SSStaged<256>);
-            const int g = stagedGrid<256>(smem);
-            if (g > 0) {
-                k_contact_ss32s<256><<<(unsigned)std::min<int64_t>(nB, g), 256, smem, st>>>(N, P, C, I, K, mats, sp, dStep, dFlags, nm,
-                                                                                          halt, loadFt);
-                return;
-            }
-        }
-        block = 256;  // the staged kernel could not be set up on this device
+        const int64_t g = std::min<int64_t>((K.n + 255) / 256, (int64_t)kSSMinBlocks * smCount());
+        k_contact_ss32p<kSSMinBlocks><<<(unsigned)g, 256, 0, st>>>(N, P, C, I, K, mats, sp, dStep, dFlags, nm, halt, loadFt);
+        return;
     }
     k_contact_ss32<kSSMinBlocks><<<(unsigned)((K.n + block - 1) / block), (unsigned)block, 0, st>>>(N, P, C, I, K, mats, sp, dStep,
                                                                                                  dFlags, nm, halt, loadFt);

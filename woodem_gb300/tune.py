@@ -12,13 +12,12 @@ import numpy as np
 
 DEFAULT_CANDIDATES = (
     # (contact threads per block, steps per chunk, CUDA graph, facet/wall contacts on a second
-    # stream beside the sphere-sphere ones); a negative block selects the persistent staged FP32
-    # sphere-sphere kernel with that many threads
+    # stream beside the sphere-sphere ones); block -256 selects the resident-grid FP32
+    # sphere-sphere kernel whose threads prefetch their next contact
     (256, 32, False, False),
     (256, 32, False, True),
     (128, 32, False, False),
     (-256, 32, False, False),
-    (-128, 32, False, False),
     (256, 8, True, False),
     (256, 32, True, False),
     (256, 32, True, True),
