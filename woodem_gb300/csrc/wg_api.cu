@@ -1464,6 +1464,9 @@ static int collectContacts(Sim& S, std::vector<int64_t>& keep, std::vector<uint6
                 } else {
                     for (int k = 0; k < 3; k++) cols[CC_CPX + k][c] = cp[k][c];
                 }
+                if (!(fl[c] & C_REAL))  // no geometry nor phys: the state arrays hold nothing for it
+                    for (int q : {CC_T0X, CC_T0Y, CC_T0Z, CC_T1X, CC_T1Y, CC_T1Z, CC_FN, CC_FT1, CC_FT2, CC_CPX, CC_CPY, CC_CPZ})
+                        cols[q][c] = 0.;
             }
         }
     }

@@ -50,6 +50,8 @@ struct CollideWork {
     uint32_t* smask = nullptr;
     float4* smnf = nullptr;       // box min rounded down, mask in w
     float4* smxf = nullptr;       // box max rounded up, particle id in w
+    float4* smnfi = nullptr;      // box min rounded up (inward)
+    float4* smxfi = nullptr;      // box max rounded down (inward)
     int32_t* cellOff = nullptr;
     int64_t cellOffCap = 0;
     double* red = nullptr;        // reduction partials
@@ -259,7 +261,7 @@ __global__ void k_cell_off(const uint32_t* __restrict__ skey, int n, int64_t nce
 
 __global__ void k_gather_sorted(DevParticles P, const int32_t* __restrict__ sid, int n, double4_32a* __restrict__ smn,
                                 double4_32a* __restrict__ smx, uint32_t* __restrict__ smask, float4* __restrict__ smnf,
-                                float4* __restrict__ smxf) {
+                                float4* __restrict__ smxf, float4* __restrict__ smnfi, float4* __restrict__ smxfi) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int p = sid[i];
@@ -270,6 +272,8 @@ __global__ void k_gather_sorted(DevParticles P, const int32_t* __restrict__ sid,
     smask[i] = m;
     smnf[i] = make_float4(__double2float_rd(a.x), __double2float_rd(a.y), __double2float_rd(a.z), __uint_as_float(m));
     smxf[i] = make_float4(__double2float_ru(b.x), __double2float_ru(b.y), __double2float_ru(b.z), __int_as_float(p));
+    smnfi[i] = make_float4(__double2float_ru(a.x), __double2float_ru(a.y), __double2float_ru(a.z), 0.f);
+    smxfi[i] = make_float4(__double2float_rd(b.x), __double2float_rd(b.y), __double2float_rd(b.z), 0.f);
 }
 
 // Collider::mayCollide pkg/dem/Collision.cpp:19-41 for particles that share no nodes
@@ -282,9 +286,17 @@ __device__ __forceinline__ void emitPair(int a, int b, uint64_t* pairs, int64_t 
 }
 
 // Outward-rounded FP32 boxes overlap whenever the FP64 boxes do, so the FP32 test rejects most
-// candidates exactly and the FP64 test (InsertionSortCollider::spatialOverlap) decides the rest.
+// candidates exactly; inward-rounded boxes (min up, max down) overlap only if the FP64 boxes do,
+// so they accept most of the rest exactly, and the FP64 test (InsertionSortCollider::spatialOverlap)
+// decides the cases where a bound lies within one FP32 rounding of the other.
 __device__ __forceinline__ bool overlapF(const float4& mn1, const float4& mx1, const float4& mn2, const float4& mx2) {
     return (mn1.x <= mx2.x) && (mx1.x >= mn2.x) && (mn1.y <= mx2.y) && (mx1.y >= mn2.y) && (mn1.z <= mx2.z) && (mx1.z >= mn2.z);
+}
+// the FP64 closed overlap of sorted boxes i and j whose outward-rounded boxes overlap
+__device__ __forceinline__ bool overlapSorted(int i, int j, const double4_32a* __restrict__ smn, const double4_32a* __restrict__ smx,
+                                              const float4* __restrict__ smnfi, const float4* __restrict__ smxfi) {
+    if (overlapF(smnfi[i], smxfi[i], smnfi[j], smxfi[j])) return true;
+    return overlap3(smn[i], smx[i], smn[j], smx[j]);
 }
 
 // Pairs found by the lanes of a warp are written with one atomic per warp: each lane keeps up to
@@ -317,23 +329,33 @@ __device__ __forceinline__ uint64_t pairKey(int a, int b) {
     return ((uint64_t)(uint32_t)lo << 32) | (uint32_t)hi;
 }
 
+// Appends key to the lane's pair buffer (register-resident: the slot is chosen by unrolled
+// comparisons, never by a runtime index).
+__device__ __forceinline__ void pushPair(uint64_t (&buf)[kPairBuf], int& nb, uint64_t key) {
+#pragma unroll
+    for (int q = 0; q < kPairBuf; q++)
+        if (q == nb) buf[q] = key;
+    nb++;
+}
+
 // Half-shell sweep: particle i tests the rest of its own cell, the next cell in x, and the
 // three-cell x-runs of the rows (dy,dz) in {(1,0),(-1,1),(0,1),(1,1)}; each pair is met once.
-// The candidate ranges of a lane are walked as one sequence so that the warp can flush together.
-__global__ void k_pairs_ss(const uint32_t* __restrict__ skey, const double4_32a* __restrict__ smn,
+// The candidate ranges of a lane are walked as one sequence, kSweepBatch candidates at a time
+// (their boxes are loaded together), so that the warp can flush together.
+constexpr int kSweepBatch = 2;
+__global__ void __launch_bounds__(256, 4) k_pairs_ss(const uint32_t* __restrict__ skey, const double4_32a* __restrict__ smn,
                            const double4_32a* __restrict__ smx, const float4* __restrict__ smnf, const float4* __restrict__ smxf,
+                           const float4* __restrict__ smnfi, const float4* __restrict__ smxfi,
                            int n, const Grid* __restrict__ Gs, const int32_t* __restrict__ pscene, const int32_t* __restrict__ off,
                            uint32_t lone, uint64_t* __restrict__ pairs, int64_t cap, unsigned long long* __restrict__ counter) {
     const unsigned FULL = 0xffffffffu;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < n;
-    // up to 5 ranges [beg, end) of sorted indices
-    int rb[5], re[5];
+    // the five ranges [b_r, b_r + len_r) of sorted indices, as starts and cumulative lengths
+    int b0 = 0, b1 = 0, b2 = 0, b3 = 0, b4 = 0, c1 = 0, c2 = 0, c3 = 0, c4 = 0, total = 0;
     float4 fn1 = make_float4(0.f, 0.f, 0.f, 0.f), fx1 = fn1;
     uint32_t m1 = 0;
     int pi = 0;
-#pragma unroll
-    for (int r = 0; r < 5; r++) rb[r] = re[r] = 0;
     if (valid) {
         fn1 = smnf[i];
         fx1 = smxf[i];
@@ -345,37 +367,50 @@ __global__ void k_pairs_ss(const uint32_t* __restrict__ skey, const double4_32a*
         const int cy = (int)((k / (uint32_t)G.nx) % (uint32_t)G.ny);
         const int cz = (int)(k / ((uint32_t)G.nx * (uint32_t)G.ny));
         const int cx1 = cx + 1 < G.nx ? cx + 1 : cx;
-        rb[0] = i + 1;
-        re[0] = off[G.base + ((int64_t)cz * G.ny + cy) * G.nx + cx1 + 1];
+        const int x0 = cx > 0 ? cx - 1 : 0;
+        int rb[4], re[4];
         const int DY[4] = {1, -1, 0, 1}, DZ[4] = {0, 1, 1, 1};
 #pragma unroll
         for (int r = 0; r < 4; r++) {
             const int y = cy + DY[r], z = cz + DZ[r];
+            rb[r] = re[r] = 0;
             if (y < 0 || y >= G.ny || z >= G.nz) continue;
-            const int x0 = cx > 0 ? cx - 1 : 0;
             const int64_t rowBase = G.base + ((int64_t)z * G.ny + y) * G.nx;
-            rb[r + 1] = off[rowBase + x0];
-            re[r + 1] = off[rowBase + cx1 + 1];
+            rb[r] = off[rowBase + x0];
+            re[r] = off[rowBase + cx1 + 1];
         }
+        b0 = i + 1;
+        c1 = off[G.base + ((int64_t)cz * G.ny + cy) * G.nx + cx1 + 1] - b0;
+        b1 = rb[0];
+        c2 = c1 + (re[0] - rb[0]);
+        b2 = rb[1];
+        c3 = c2 + (re[1] - rb[1]);
+        b3 = rb[2];
+        c4 = c3 + (re[2] - rb[2]);
+        b4 = rb[3];
+        total = c4 + (re[3] - rb[3]);
     }
     uint64_t buf[kPairBuf];
     int nb = 0;
-    int r = 0, j = rb[0];
-    for (;;) {
-        // advance to the next candidate of this lane
-        while (r < 5 && j >= re[r]) {
-            r++;
-            if (r < 5) j = rb[r];
+    for (int v0 = 0; __any_sync(FULL, v0 < total); v0 += kSweepBatch) {
+        int jj[kSweepBatch];
+        float4 a[kSweepBatch], c[kSweepBatch];
+#pragma unroll
+        for (int u = 0; u < kSweepBatch; u++) {
+            const int v = v0 + u;
+            jj[u] = v >= total ? -1
+                               : (v < c1 ? b0 + v : (v < c2 ? b1 + (v - c1) : (v < c3 ? b2 + (v - c2) : (v < c4 ? b3 + (v - c3) : b4 + (v - c4)))));
+            if (jj[u] >= 0) {
+                a[u] = smnf[jj[u]];
+                c[u] = smxf[jj[u]];
+            }
         }
-        const bool has = r < 5;
-        if (!__any_sync(FULL, has)) break;
-        if (has) {
-            const float4 fn2 = smnf[j], fx2 = smxf[j];
-            if (overlapF(fn1, fx1, fn2, fx2) && maskOk(m1, __float_as_uint(fn2.w), lone) && overlap3(smn[i], smx[i], smn[j], smx[j]))
-                buf[nb++] = pairKey(pi, __float_as_int(fx2.w));
-            j++;
-        }
-        if (__any_sync(FULL, nb == kPairBuf)) flushPairs(buf, nb, pairs, cap, counter);
+#pragma unroll
+        for (int u = 0; u < kSweepBatch; u++)
+            if (jj[u] >= 0 && overlapF(fn1, fx1, a[u], c[u]) && maskOk(m1, __float_as_uint(a[u].w), lone) &&
+                overlapSorted(i, jj[u], smn, smx, smnfi, smxfi))
+                pushPair(buf, nb, pairKey(pi, __float_as_int(c[u].w)));
+        if (__any_sync(FULL, nb > kPairBuf - kSweepBatch)) flushPairs(buf, nb, pairs, cap, counter);
     }
     flushPairs(buf, nb, pairs, cap, counter);
 }
@@ -385,7 +420,7 @@ __global__ void k_pairs_ss(const uint32_t* __restrict__ skey, const double4_32a*
 // each x-run of cells.
 __global__ void k_pairs_local(DevParticles P, const int32_t* __restrict__ lids, int nl, const double4_32a* __restrict__ smn,
                               const double4_32a* __restrict__ smx, const float4* __restrict__ smnf, const float4* __restrict__ smxf,
-                              const Grid* __restrict__ Gs, const int32_t* __restrict__ off, uint32_t lone, uint64_t* __restrict__ pairs,
+                              const float4* __restrict__ smnfi, const float4* __restrict__ smxfi, const Grid* __restrict__ Gs, const int32_t* __restrict__ off, uint32_t lone, uint64_t* __restrict__ pairs,
                               int64_t cap, unsigned long long* __restrict__ counter) {
     const unsigned FULL = 0xffffffffu;
     const int t = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
@@ -396,6 +431,8 @@ __global__ void k_pairs_local(DevParticles P, const int32_t* __restrict__ lids, 
     const double4_32a mn1 = P.mn[p], mx1 = P.mx[p];
     const float4 fn1 = make_float4(__double2float_rd(mn1.x), __double2float_rd(mn1.y), __double2float_rd(mn1.z), 0.f);
     const float4 fx1 = make_float4(__double2float_ru(mx1.x), __double2float_ru(mx1.y), __double2float_ru(mx1.z), 0.f);
+    const float4 fni1 = make_float4(__double2float_ru(mn1.x), __double2float_ru(mn1.y), __double2float_ru(mn1.z), 0.f);
+    const float4 fxi1 = make_float4(__double2float_rd(mx1.x), __double2float_rd(mx1.y), __double2float_rd(mx1.z), 0.f);
     const uint32_t m1 = P.mask[p];
     const int x0 = cellCoord(mn1.x - G.h, G.ox, G.h, G.nx), x1 = cellCoord(mx1.x, G.ox, G.h, G.nx);
     const int y0 = cellCoord(mn1.y - G.h, G.oy, G.h, G.ny), y1 = cellCoord(mx1.y, G.oy, G.h, G.ny);
@@ -412,8 +449,8 @@ __global__ void k_pairs_local(DevParticles P, const int32_t* __restrict__ lids, 
                     const float4 fn2 = smnf[j], fx2 = smxf[j];
                     const int q = __float_as_int(fx2.w);
                     if (q != p && overlapF(fn1, fx1, fn2, fx2) && maskOk(m1, __float_as_uint(fn2.w), lone) &&
-                        overlap3(mn1, mx1, smn[j], smx[j]))
-                        buf[nb++] = pairKey(p, q);
+                        (overlapF(fni1, fxi1, smnfi[j], smxfi[j]) || overlap3(mn1, mx1, smn[j], smx[j])))
+                        pushPair(buf, nb, pairKey(p, q));
                 }
                 if (__any_sync(FULL, nb == kPairBuf)) flushPairs(buf, nb, pairs, cap, counter);
             }
@@ -510,8 +547,14 @@ __global__ void k_pairs_ss_peri(const uint32_t* __restrict__ skey, const int32_t
                     const int r = overlapPeri(mn1, mx1, smn[j], smx[j], sp.cellSize, per);
                     if (r < 0) atomicCAS(dErr, 0, 103);
                     else if (r > 0) {
-                        buf[nb] = pairKey(pi, pj);
-                        cbuf[nb] = packCellDist(per[0], per[1], per[2]);
+                        const uint64_t key = pairKey(pi, pj);
+                        const int32_t cd = packCellDist(per[0], per[1], per[2]);
+#pragma unroll
+                        for (int q = 0; q < kPairBuf; q++)
+                            if (q == nb) {
+                                buf[q] = key;
+                                cbuf[q] = cd;
+                            }
                         nb++;
                     }
                 }
@@ -645,16 +688,22 @@ __global__ void k_gather(DevContacts Cold, DevContacts Cnew, const int32_t* __re
     const int32_t s0 = src[i];
     // a contact removed since the last full run comes back as a new one
     const int32_t s = (s0 >= 0 && (Cold.flags[s0] & C_REMOVED)) ? -1 : s0;
+    // FP32-force mode carries the state of real contacts only (a contact that is not real has no
+    // state any kernel reads; the listing reports zeros for it)
+    const bool fp32 = Cnew.fcol[0] != nullptr;
     if (s >= 0) {
-        Cnew.flags[i] = Cold.flags[s] & ~(C_PENDING | C_DORMANT);
+        const uint32_t fo = Cold.flags[s];
+        Cnew.flags[i] = fo & ~(C_PENDING | C_DORMANT);
         Cnew.step0[i] = Cold.step0[s];
         Cnew.cdist[i] = Cold.cdist[s];
+        if (!fp32 || (fo & C_REAL)) {
 #pragma unroll
-        for (int q = 0; q < CC_NCOL; q++)
-            if (Cnew.col[q]) Cnew.col[q][i] = Cold.col[q][s];
+            for (int q = 0; q < CC_NCOL; q++)
+                if (Cnew.col[q]) Cnew.col[q][i] = Cold.col[q][s];
 #pragma unroll
-        for (int q = 0; q < CF_NCOL; q++)
-            if (Cnew.fcol[q]) Cnew.fcol[q][i] = Cold.fcol[q][s];
+            for (int q = 0; q < CF_NCOL; q++)
+                if (Cnew.fcol[q]) Cnew.fcol[q][i] = Cold.fcol[q][s];
+        }
     } else {
         const uint64_t k = Cnew.key[i];
         const int lo = (int)(k >> 32), hi = (int)(k & 0xffffffffu);
@@ -672,12 +721,11 @@ __global__ void k_gather(DevContacts Cold, DevContacts Cnew, const int32_t* __re
         Cnew.flags[i] = fl;
         Cnew.step0[i] = (int32_t)(*dStep);
         Cnew.cdist[i] = newCd ? newCd[i] : packCellDist(0, 0, 0);
+        if (!fp32) {
 #pragma unroll
-        for (int q = 0; q < CC_NCOL; q++)
-            if (Cnew.col[q]) Cnew.col[q][i] = 0.;
-#pragma unroll
-        for (int q = 0; q < CF_NCOL; q++)
-            if (Cnew.fcol[q]) Cnew.fcol[q][i] = 0.f;
+            for (int q = 0; q < CC_NCOL; q++)
+                if (Cnew.col[q]) Cnew.col[q][i] = 0.;
+        }
     }
 }
 
@@ -996,7 +1044,9 @@ int collide_full_run(Sim& S) {
             W.smask = (uint32_t*)S.dalloc(sizeof(uint32_t) * cap);
             W.smnf = (float4*)S.dalloc(sizeof(float4) * cap);
             W.smxf = (float4*)S.dalloc(sizeof(float4) * cap);
-            if (!W.smask || !W.smxf) return S.fail(WG_ERR_CUDA, "out of device memory (grid)");
+            W.smnfi = (float4*)S.dalloc(sizeof(float4) * cap);
+            W.smxfi = (float4*)S.dalloc(sizeof(float4) * cap);
+            if (!W.smask || !W.smxf || !W.smxfi) return S.fail(WG_ERR_CUDA, "out of device memory (grid)");
         }
         W.cellOff = grow(S, W.cellOff, W.cellOffCap, ncellAll + 1);
         if (S.cfg.periodic) k_cellkey_peri<<<(ns + BS - 1) / BS, BS, 0, st>>>(S.P, W.sphereIds, ns, G, S.dPar, W.cellKey, W.cellVal);
@@ -1009,7 +1059,7 @@ int collide_full_run(Sim& S) {
         tb = W.cubBytes;
         WG_CUDA_TRY(cub::DeviceRadixSort::SortPairs(W.cubTmp, tb, W.cellKey, W.cellKeySorted, W.cellVal, W.sid, ns, 0, endBit, st));
         k_cell_off<<<(unsigned)((ncellAll + 1 + BS - 1) / BS), BS, 0, st>>>(W.cellKeySorted, ns, ncellAll, W.cellOff);
-        k_gather_sorted<<<(ns + BS - 1) / BS, BS, 0, st>>>(S.P, W.sid, ns, W.smn, W.smx, W.smask, W.smnf, W.smxf);
+        k_gather_sorted<<<(ns + BS - 1) / BS, BS, 0, st>>>(S.P, W.sid, ns, W.smn, W.smx, W.smask, W.smnf, W.smxf, W.smnfi, W.smxfi);
     }
     // lists of large particles: facets with boxes spanning a few cells use the grid, the rest are global
     {
@@ -1069,11 +1119,13 @@ int collide_full_run(Sim& S) {
                 k_pairs_global_peri<<<(ns + BS - 1) / BS, BS, 0, st>>>(S.P, W.globalIds, W.nGlobal, W.sphereIds, ns, lone, S.dPar,
                                                                      W.pairs, W.pairCd, W.pairCap, W.counter, S.dFlags + FL_ERR);
         } else if (ns > 0) {
-            k_pairs_ss<<<(ns + BS - 1) / BS, BS, 0, st>>>(W.cellKeySorted, W.smn, W.smx, W.smnf, W.smxf, ns, W.dGrids, S.P.scene,
+            k_pairs_ss<<<(ns + BS - 1) / BS, BS, 0, st>>>(W.cellKeySorted, W.smn, W.smx, W.smnf, W.smxf, W.smnfi, W.smxfi, ns, W.dGrids,
+                                                        S.P.scene,
                                                         W.cellOff, lone, W.pairs, W.pairCap, W.counter);
             if (W.nLarge > 0)
                 k_pairs_local<<<(unsigned)(((int64_t)W.nLarge * 32 + BS - 1) / BS), BS, 0, st>>>(
-                    S.P, W.largeIds, W.nLarge, W.smn, W.smx, W.smnf, W.smxf, W.dGrids, W.cellOff, lone, W.pairs, W.pairCap, W.counter);
+                    S.P, W.largeIds, W.nLarge, W.smn, W.smx, W.smnf, W.smxf, W.smnfi, W.smxfi, W.dGrids, W.cellOff, lone, W.pairs,
+                    W.pairCap, W.counter);
             if (W.nGlobal > 0)
                 k_pairs_global<<<(ns + BS - 1) / BS, BS, 0, st>>>(S.P, W.globalIds, W.nGlobal, K > 1 ? W.gStart : nullptr, W.sphereIds, ns, lone,
                                                                 W.pairs, W.pairCap, W.counter);
@@ -1278,6 +1330,9 @@ int collide_full_run(Sim& S) {
             }
         }
         K.n = nSS;
+        bool law0 = S.cfg.law == 0;
+        for (const wg_config& c : S.cfgs) law0 = law0 || c.law == 0;
+        K.ftLive = law0;
         launch_pack_ss(st, S.C, S.I, S.P, K, S.nMixed);
     }
     S.packDirty = false;

@@ -184,6 +184,8 @@ struct DevPackedSS {
     uint32_t* flags = nullptr; // contact flags | scene << 8
     float* col[CF_NCOL] = {};
     double* ft[2] = {};        // IdealElPl shear force
+    bool ftLive = false;       // ft is copied (some scene used IdealElPl at the last full run); it is
+                               // read only for contacts of scenes with that law
 };
 // Step-loop flag words (device int[3]).
 enum { FL_FULL = 0,   // set by Leapfrog: a node moved farther than verletDist, a full collider run is due

@@ -643,7 +643,7 @@ __global__ void __launch_bounds__(256, MINB) k_contact_ss32p(DevNodes N, DevPart
     }
 }
 
-__global__ void k_pack_ss(DevContacts C, DevIncidence I, DevParticles P, DevPackedSS K, int64_t nm) {
+__global__ void k_pack_ss(DevContacts C, DevIncidence I, DevParticles P, DevPackedSS K, int64_t nm, int copyFt) {
     const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= K.n) return;
     const int4 wk = I.work[nm + j];
@@ -655,20 +655,20 @@ __global__ void k_pack_ss(DevContacts C, DevIncidence I, DevParticles P, DevPack
     K.flags[j] = fl | ((uint32_t)sceneOfP(P, wk.z) << 8);
 #pragma unroll
     for (int q = 0; q < CF_NCOL; q++) K.col[q][j] = C.fcol[q][c];
-    if (K.ft[0]) {
+    if (copyFt) {
         K.ft[0][j] = C.col[CC_FT1][c];
         K.ft[1][j] = C.col[CC_FT2][c];
     }
 }
 
-__global__ void k_unpack_ss(DevContacts C, DevIncidence I, DevPackedSS K, int64_t nm) {
+__global__ void k_unpack_ss(DevContacts C, DevIncidence I, DevPackedSS K, int64_t nm, int copyFt) {
     const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= K.n) return;
     const int64_t c = I.work[nm + j].x;
     C.flags[c] = K.flags[j] & 0xffu;
 #pragma unroll
     for (int q = 0; q < CF_NCOL; q++) C.fcol[q][c] = K.col[q][j];
-    if (K.ft[0]) {
+    if (copyFt) {
         C.col[CC_FT1][c] = K.ft[0][j];
         C.col[CC_FT2][c] = K.ft[1][j];
     }
@@ -676,10 +676,10 @@ __global__ void k_unpack_ss(DevContacts C, DevIncidence I, DevPackedSS K, int64_
 
 void launch_pack_ss(cudaStream_t st, const DevContacts& C, const DevIncidence& I, const DevParticles& P, const DevPackedSS& K,
                     int64_t nMixed) {
-    if (K.n > 0) k_pack_ss<<<(unsigned)((K.n + 255) / 256), 256, 0, st>>>(C, I, P, K, nMixed);
+    if (K.n > 0) k_pack_ss<<<(unsigned)((K.n + 255) / 256), 256, 0, st>>>(C, I, P, K, nMixed, K.ftLive ? 1 : 0);
 }
 void launch_unpack_ss(cudaStream_t st, const DevContacts& C, const DevIncidence& I, const DevPackedSS& K, int64_t nMixed) {
-    if (K.n > 0) k_unpack_ss<<<(unsigned)((K.n + 255) / 256), 256, 0, st>>>(C, I, K, nMixed);
+    if (K.n > 0) k_unpack_ss<<<(unsigned)((K.n + 255) / 256), 256, 0, st>>>(C, I, K, nMixed, K.ftLive ? 1 : 0);
 }
 
 // FacetPrep of every facet (Facet.cpp:240-246: normal; CompUtils.cpp:92-110: the barycentric
