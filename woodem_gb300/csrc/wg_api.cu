@@ -707,7 +707,7 @@ int Sim::run(int64_t n) {
             else launch_forces(stream, N, P, I, dPar, dFlags, true);
             launches += I.nHeavyFree > 0;
         }
-        if (fp32) launch_leapfrog32(stream, N, P, I, dNodeC, dPar, dFlags, fromEndsArg, dStep);
+        if (fp32) launch_leapfrog32(stream, N, P, I, dNodeC, dPar, dFlags, fromEndsArg, dStep, cfg.periodic != 0);
         else launch_leapfrog(stream, N, P, I, dPar, dFlags, fromEndsArg, dStep);
         launches++;
     };

@@ -223,7 +223,7 @@ int launch_stress(cudaStream_t st, const DevNodes& N, const DevParticles& P, con
                   const ScenePar* sp, double* scratch, int64_t scratchDoubles, double* out);
 // FP32-force mode (wg_step32.cu)
 void launch_leapfrog32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const NodeConst32* nc,
-                       const ScenePar* sp, int* dFlags, int fromEnds, const long long* dStep);
+                       const ScenePar* sp, int* dFlags, int fromEnds, const long long* dStep, bool periodic);
 // The kernels walk the active contacts I.work[0, I.nAct). Items [0, nMixed) are facet and wall
 // contacts; [nMixed, I.nAct) join two spheres and, in an aperiodic scene, go to a
 // sphere-sphere-only kernel.

@@ -23,14 +23,17 @@ struct F3 {
 __device__ __forceinline__ F3 f3(float x, float y, float z) { return F3{x, y, z}; }
 __device__ __forceinline__ F3 toF(D3 a) { return F3{(float)a.x, (float)a.y, (float)a.z}; }
 // x truncated toward zero to FP32 with 32-bit integer operations on its words (no FP64-pipe
-// conversion): |x| below the FP32 normal range gives a signed zero; |x| >= 2^127, infinities and
-// NaN take the FP64 route.
+// conversion on any path): |x| below the FP32 normal range gives a signed zero, finite |x| from
+// 2^128 up the largest FP32 of its sign; infinities and NaN stay what they are.
 __device__ __forceinline__ float d2fT(double x) {
     const unsigned top = (unsigned)__double2hiint(x), bot = (unsigned)__double2loint(x);
     const unsigned sign = top & 0x80000000u;
     const int e = (int)((top >> 20) & 0x7ffu);
     if (e < 897) return __uint_as_float(sign);
-    if (e > 1150) return __double2float_rz(x);
+    if (e > 1150) {
+        if (e < 2047) return __uint_as_float(sign | 0x7F7FFFFFu);
+        return __uint_as_float(sign | 0x7F800000u | ((((top & 0xFFFFFu) | bot) != 0) ? 0x400000u : 0u));
+    }
     return __uint_as_float(sign | ((unsigned)(e - 896) << 23) | ((top & 0xFFFFFu) << 3) | (bot >> 29));
 }
 __device__ __forceinline__ F3 toFt(D3 a) { return F3{d2fT(a.x), d2fT(a.y), d2fT(a.z)}; }
@@ -41,17 +44,26 @@ __device__ __forceinline__ F3 operator*(F3 a, float s) { return F3{a.x * s, a.y 
 __device__ __forceinline__ F3 operator*(float s, F3 a) { return F3{s * a.x, s * a.y, s * a.z}; }
 __device__ __forceinline__ float fdot(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 __device__ __forceinline__ F3 fcross(F3 a, F3 b) { return F3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
-// x = h + l from the bits of x with 32-bit integer operations on its two words (FP64
-// arithmetic and conversions issue at 1/64 of the FP32 rate on GB300): h is x truncated to 24
-// significant bits, l the remaining 29 mantissa bits truncated to 24, so |x - (h + l)| < 2^-47 |x|.
-// Zero, |x| < 2^-74 and |x| >= 2^127 take the FP64 route (h = fl32(x), l = fl32(x - h)).
+// x = h + l from the bits of x with 32-bit integer operations on its two words, on every path:
+// FP64 arithmetic and conversions issue at 1/64 of the FP32 rate on GB300, and the compiler
+// turns a rarely taken branch into predicated instructions that occupy the FP64 pipe in every
+// warp. h is x truncated to 24 significant bits, l the remaining 29 mantissa bits truncated to
+// 24, so |x - (h + l)| < 2^-47 |x|. Below 2^-74 (zero included) l is dropped (h = x truncated,
+// or a signed zero under the FP32 normal range: an absolute error below 2^-97); from 2^127 up h
+// is the signed infinity (NaN stays NaN) and l zero.
 __device__ __forceinline__ void splitDF(double x, float& h, float& l) {
     const unsigned top = (unsigned)__double2hiint(x), bot = (unsigned)__double2loint(x);
     const unsigned sign = top & 0x80000000u;
     const int e = (int)((top >> 20) & 0x7ffu);
-    if (e < 949 || e > 1150) {
-        h = __double2float_rn(x);
-        l = __double2float_rn(x - (double)h);
+    if (e < 949) {
+        h = __uint_as_float(e >= 897 ? (sign | ((unsigned)(e - 896) << 23) | ((top & 0xFFFFFu) << 3) | (bot >> 29)) : sign);
+        l = 0.f;
+        return;
+    }
+    if (e > 1150) {
+        const bool nan = e == 2047 && ((top & 0xFFFFFu) | bot) != 0;
+        h = __uint_as_float(sign | 0x7F800000u | (nan ? 0x400000u : 0u));
+        l = 0.f;
         return;
     }
     // the 52 mantissa bits are (top & 0xfffff):bot; h keeps the upper 23
@@ -65,16 +77,16 @@ __device__ __forceinline__ void splitDF(double x, float& h, float& l) {
     const unsigned frac = (p >= 23) ? (r >> (p - 23)) : (r << (23 - p));
     l = __uint_as_float(sign | ((unsigned)(p + e - 948) << 23) | (frac & 0x7FFFFFu));
 }
-// (double)f from the bits of f with 32-bit integer operations (exact for normal numbers; FP32
-// subnormals, below 1.2e-38, become zero; infinities and NaN take the FP64 route).
+// (double)f from the bits of f with 32-bit integer operations (exact for normal numbers,
+// infinities and NaN; FP32 subnormals, below 1.2e-38, become zero).
 __device__ __forceinline__ double f2d(float f) {
     const unsigned u = __float_as_uint(f);
     const unsigned e = (u >> 23) & 0xffu;
     const unsigned sign = u & 0x80000000u;
     if (e == 0) return __hiloint2double((int)sign, 0);
-    if (e == 0xffu) return (double)f;
     const unsigned mant = u & 0x7fffffu;
-    return __hiloint2double((int)(sign | ((e + 896u) << 20) | (mant >> 3)), (int)(mant << 29));
+    const unsigned ed = (e == 0xffu) ? 0x7ffu : e + 896u;
+    return __hiloint2double((int)(sign | (ed << 20) | (mant >> 3)), (int)(mant << 29));
 }
 // x rounded toward zero to FP32 (the h of splitDF)
 __device__ __forceinline__ float truncF(double x) {
@@ -97,6 +109,20 @@ __device__ __forceinline__ float fsgn(float s) { return s < 0.f ? -1.f : (s > 0.
 // The orientation, which no force of the supported shapes depends on, is advanced in FP32.
 // Writes the double-float mirrors of position and velocity used by the contact kernel.
 // The node state is loaded before the end-slot sum so that its loads overlap the staging.
+// m*g written as the force of a node no contact sum rebuilds (facet vertices): kept out of line so
+// that its FP64 arithmetic is a branch, not predicated instructions in every warp
+__device__ __noinline__ void resetNodeForce(DevNodes N, int i, float mh, float ml, bool gravity, const ScenePar* __restrict__ spp,
+                                            int scene) {
+    const ScenePar& sp = spp[scene];
+    D3 G{0, 0, 0};
+    if (gravity) G = ((double)mh + (double)ml) * D3{sp.g[0], sp.g[1], sp.g[2]};
+    N.force[i] = make_double4_32a(G.x, G.y, G.z, 0.);
+    N.torque[i] = make_double4_32a(0., 0., 0., 0.);
+}
+
+// PERI: the scene is periodic (homothetic corrections of Leapfrog.cpp:103-255 with the cell's
+// velocity gradient); the aperiodic instantiation carries none of that FP64 code.
+template <bool PERI>
 __global__ void __launch_bounds__(256) k_leapfrog32(DevNodes N, DevParticles P, DevIncidence I, const NodeConst32* __restrict__ ncs,
                                                     const ScenePar* __restrict__ spp, int* __restrict__ dFlags, int fromEnds,
                                                     const long long* __restrict__ dStepC) {
@@ -151,8 +177,8 @@ __global__ void __launch_bounds__(256) k_leapfrog32(DevNodes N, DevParticles P, 
         f = F3{acc.net(0), acc.net(1), acc.net(2)};
         t = F3{acc.net(3), acc.net(4), acc.net(5)};
     } else {  // the stored value: first step after the host wrote the state, or a heavy particle
-        f = toF(ld3(N.force[i]));
-        t = toF(ld3(N.torque[i]));
+        f = toFt(ld3(N.force[i]));
+        t = toFt(ld3(N.torque[i]));
     }
     const double dt = sp.dt;
     const float dtf = sp.dtF;
@@ -161,7 +187,7 @@ __global__ void __launch_bounds__(256) k_leapfrog32(DevNodes N, DevParticles P, 
     D3 vel = ld3(v4);
     D3 angVel = ld3(w4);
     const bool blockedAll = (flags & F_DOF_ALL) == F_DOF_ALL;
-    const int homoDeform = sp.periodic ? sp.homoDeform : -1;
+    const int homoDeform = PERI ? sp.homoDeform : -1;
     F3 la{0.f, 0.f, 0.f};
     if (!blockedAll) {
         la = F3{(flags & 1u) ? 0.f : f.x * nc.invMass, (flags & 2u) ? 0.f : f.y * nc.invMass, (flags & 4u) ? 0.f : f.z * nc.invMass};
@@ -169,19 +195,19 @@ __global__ void __launch_bounds__(256) k_leapfrog32(DevNodes N, DevParticles P, 
         if (damp) {
             // nonviscDamp2nd (Leapfrog.cpp:32-34) on the fluctuation velocity (Cell.cpp:36-57)
             D3 v = vel, w = angVel;
-            if (sp.periodic) {
+            if (PERI) {
                 if (homoDeform == 2 || homoDeform == 3) v = vel - mul(*(const DM3*)sp.gradV, pos);
                 else if (homoDeform == 4) v = vel - mul(*(const DM3*)sp.gradV, pos - (dt / 2) * vel);
                 if (homoDeform == 4) w = angVel - D3{sp.spinVec[0], sp.spinVec[1], sp.spinVec[2]};
             }
-            pvf = toF(v);
-            pva = toF(w);
+            pvf = toFt(v);
+            pva = toFt(w);
             const float d = sp.dampingF;
             la.x *= 1.f - d * fsgn(f.x * (pvf.x + 0.5f * dtf * la.x));
             la.y *= 1.f - d * fsgn(f.y * (pvf.y + 0.5f * dtf * la.y));
             la.z *= 1.f - d * fsgn(f.z * (pvf.z + 0.5f * dtf * la.z));
         }
-        if (homoDeform == 4)
+        if (PERI && homoDeform == 4)
             vel = mul(*(const DM3*)sp.ImLL4hInv, (mul(*(const DM3*)sp.LmL, pos) + mul(*(const DM3*)sp.IpLL4h, vel)) +
                                                    D3{(double)la.x, (double)la.y, (double)la.z} * dt);
         else
@@ -195,12 +221,12 @@ __global__ void __launch_bounds__(256) k_leapfrog32(DevNodes N, DevParticles P, 
                 aa.z *= 1.f - d * fsgn(t.z * (pva.z + 0.5f * dtf * aa.z));
             }
             angVel = angVel + D3{f2d(dtf * aa.x), f2d(dtf * aa.y), f2d(dtf * aa.z)};
-            if (homoDeform == 4) angVel = angVel - D3{sp.deltaSpinVec[0], sp.deltaSpinVec[1], sp.deltaSpinVec[2]};
+            if (PERI && homoDeform == 4) angVel = angVel - D3{sp.deltaSpinVec[0], sp.deltaSpinVec[1], sp.deltaSpinVec[2]};
         }
     } else {
-        if (homoDeform == 4) vel = mul(*(const DM3*)sp.ImLL4hInv, mul(*(const DM3*)sp.LmL, pos) + mul(*(const DM3*)sp.IpLL4h, vel));
+        if (PERI && homoDeform == 4) vel = mul(*(const DM3*)sp.ImLL4hInv, mul(*(const DM3*)sp.LmL, pos) + mul(*(const DM3*)sp.IpLL4h, vel));
     }
-    if (homoDeform >= 0 && homoDeform != 4) {
+    if (PERI && homoDeform >= 0 && homoDeform != 4) {
         const D3 lad{(double)la.x, (double)la.y, (double)la.z};
         if (homoDeform == 2 || homoDeform == 3) {
             if (homoDeform == 3) vel = vel + mul(*(const DM3*)sp.midGradV, vel - (dt / 2.) * lad) * dt;
@@ -250,19 +276,15 @@ __global__ void __launch_bounds__(256) k_leapfrog32(DevNodes N, DevParticles P, 
         const float inv = rsqrtf(rw * rw + rx * rx + ry * ry + rz * rz);
         N.orif[i] = make_float4(rw * inv, rx * inv, ry * inv, rz * inv);
     }
-    if (sp.reset && !uni) {
-        // force reset of nodes whose force is not rebuilt by the contact sum (facet vertices)
-        D3 G{0, 0, 0};
-        if (sp.hasGravity && !(flags & F_GRAVITY_SKIP)) G = ((double)nc.mh + (double)nc.ml) * D3{sp.g[0], sp.g[1], sp.g[2]};
-        N.force[i] = make_double4_32a(G.x, G.y, G.z, 0.);
-        N.torque[i] = make_double4_32a(0., 0., 0., 0.);
-    }
+    // force reset of nodes whose force is not rebuilt by the contact sum (facet vertices)
+    if (sp.reset && !uni) resetNodeForce(N, i, nc.mh, nc.ml, sp.hasGravity && !(flags & F_GRAVITY_SKIP), spp, scene);
 }
 
 void launch_leapfrog32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const NodeConst32* nc,
-                       const ScenePar* sp, int* dFlags, int fromEnds, const long long* dStep) {
+                       const ScenePar* sp, int* dFlags, int fromEnds, const long long* dStep, bool periodic) {
     if (N.n == 0) return;
-    k_leapfrog32<<<(N.n + 255) / 256, 256, 0, st>>>(N, P, I, nc, sp, dFlags, fromEnds, dStep);
+    if (periodic) k_leapfrog32<true><<<(N.n + 255) / 256, 256, 0, st>>>(N, P, I, nc, sp, dFlags, fromEnds, dStep);
+    else k_leapfrog32<false><<<(N.n + 255) / 256, 256, 0, st>>>(N, P, I, nc, sp, dFlags, fromEnds, dStep);
 }
 
 // ---------------------------------------------------------------------------------- ContactLoop
