@@ -708,14 +708,14 @@ int Sim::run(int64_t n) {
             launches += I.nHeavyFree > 0;
         }
         if (fp32) launch_leapfrog32(stream, N, P, I, dNodeC, dPar, dFlags, fromEndsArg, dStep, cfg.periodic != 0);
-        else launch_leapfrog(stream, N, P, I, dPar, dFlags, fromEndsArg, dStep);
+        else launch_leapfrog(stream, N, P, I, dPar, dFlags, fromEndsArg, dStep, cfg.periodic != 0);
         launches++;
     };
     auto stepContact = [&]() {
         if (fp32) launch_contact_fp32(stream, concurrentContacts ? side : SideStream{}, N, P, C, I, K, dMats, dPar, dStep, dFlags, nMixed,
                                       cfg.periodic != 0, anyLaw0,
                                       contactBlock != 0 ? contactBlock : -256);
-        else launch_contact_fp64(stream, N, P, C, I, dMats, dPar, dStep, dFlags,
+        else launch_contact_fp64(stream, N, P, C, I, dMats, dPar, dStep, dFlags, cfg.periodic != 0,
                                  (contactBlock > 0 && contactBlock <= 128) ? contactBlock : 128);  // launch bounds 128
         launch_advance(stream, dStep, dFlags);
         launches += 2;

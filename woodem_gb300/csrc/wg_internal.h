@@ -208,10 +208,10 @@ __host__ __device__ inline void unpackCellDist(int32_t p, int& a, int& b, int& c
 // several steps without waiting for each verlet test.
 // fromEnds = 0: take DemData.force/torque as stored (first step after the host wrote the state).
 void launch_leapfrog(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const ScenePar* sp,
-                     int* dFlags, int fromEnds, const long long* dStep);
+                     int* dFlags, int fromEnds, const long long* dStep, bool periodic);
 void launch_contact_fp64(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C,
                          const DevIncidence& I, const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dFlags,
-                         int block = 128);
+                         bool periodic, int block = 128);
 // perStep: only the heavy particles with a free DOF (guarded by the flags), before Leapfrog;
 // otherwise every particle's DemData.force/torque (reporting at the end of a run).
 void launch_forces(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const ScenePar* sp,

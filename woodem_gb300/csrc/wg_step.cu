@@ -25,6 +25,43 @@ __device__ __forceinline__ double sgn(double s) { return s < 0 ? -1 : (s > 0 ? 1
 // applyPeriodicCorrections :258-272, leapfrogTranslate :275-278, leapfrogSphericalRotate :280-288,
 // and the verlet-distance test of InsertionSortCollider::updateBboxes_doFullRun
 // pkg/dem/InsertionSortCollider.cpp:339-350 on the new positions.
+//
+// Paths that few nodes take (partly blocked DOFs, damping, the force reset of facet vertices)
+// are out-of-line functions: inlined, the compiler turns them into predicated FP64 instructions,
+// which occupy the FP64 pipe (1/64 of the FP32 rate on GB300) in every warp. The operations, and
+// so the results, are the same either way. PERI: the periodic corrections (Cell velocity gradient).
+__device__ __noinline__ D3 linAccelPartial(D3 f, double mass, uint32_t flags) {
+    D3 a{0, 0, 0};
+    if (!(flags & 1u)) a.x = 0. + f.x / mass;
+    if (!(flags & 2u)) a.y = 0. + f.y / mass;
+    if (!(flags & 4u)) a.z = 0. + f.z / mass;
+    return a;
+}
+__device__ __noinline__ D3 angAccelPartial(D3 t, D3 inertia, uint32_t flags) {
+    D3 a{0, 0, 0};
+    if (!(flags & 8u)) a.x = 0. + t.x / inertia.x;
+    if (!(flags & 16u)) a.y = 0. + t.y / inertia.y;
+    if (!(flags & 32u)) a.z = 0. + t.z / inertia.z;
+    return a;
+}
+// nonviscDamp2nd (Leapfrog.cpp:32-34) of an acceleration a under force (or torque) f, with the
+// fluctuation velocity v
+__device__ __noinline__ D3 dampAccel(D3 a, D3 f, D3 v, double damping, double dt) {
+    a.x = a.x * (1 - damping * sgn(f.x * (v.x + (0.5 * dt) * a.x)));
+    a.y = a.y * (1 - damping * sgn(f.y * (v.y + (0.5 * dt) * a.y)));
+    a.z = a.z * (1 - damping * sgn(f.z * (v.z + (0.5 * dt) * a.z)));
+    return a;
+}
+// Leapfrog(reset=True) for nodes whose force is not rebuilt by the contact sum (facet vertices):
+// force = mass*gravity, torque = 0 (Leapfrog.cpp:240-245)
+__device__ __noinline__ void resetForce(DevNodes N, int i, double mass, bool gravity, const ScenePar* __restrict__ spp, int scene) {
+    const ScenePar& sp = spp[scene];
+    D3 G{0, 0, 0};
+    if (gravity) G = mass * D3{sp.g[0], sp.g[1], sp.g[2]};
+    N.force[i] = st4(G, 0.);
+    N.torque[i] = make_double4_32a(0., 0., 0., 0.);
+}
+template <bool PERI>
 __global__ void __launch_bounds__(256) k_leapfrog(DevNodes N, DevParticles P, DevIncidence I, const ScenePar* __restrict__ spp,
                                                   int* __restrict__ dFlags, int fromEnds, const long long* __restrict__ dStepC) {
     __shared__ EndStage<double4_32a, double2, 32> stage[8];
@@ -75,51 +112,35 @@ __global__ void __launch_bounds__(256) k_leapfrog(DevNodes N, DevParticles P, De
     D3 angVel = ld3(N.angv[i]);
     const D3 inertia{mi.x, mi.y, mi.z};
     const bool blockedAll = (flags & F_DOF_ALL) == F_DOF_ALL;
-    const int homoDeform = sp.periodic ? sp.homoDeform : -1;
+    const int homoDeform = PERI ? sp.homoDeform : -1;
     D3 linAccel{0, 0, 0};
     if (!blockedAll) {
         if ((flags & F_DOF_ALL) == 0) linAccel = f / mass;
-        else {
-            if (!(flags & 1u)) linAccel.x = 0. + f.x / mass;
-            if (!(flags & 2u)) linAccel.y = 0. + f.y / mass;
-            if (!(flags & 4u)) linAccel.z = 0. + f.z / mass;
-        }
+        else linAccel = linAccelPartial(f, mass, flags);
         D3 pvf = vel, pva = angVel;
-        if (sp.periodic) {
+        if (PERI) {
             // Cell::pprevFluctVel / pprevFluctAngVel, core/Cell.cpp:36-57
             if (homoDeform == 2 || homoDeform == 3) pvf = vel - mul(ldm(sp.gradV), pos);
             else if (homoDeform == 4) pvf = vel - mul(ldm(sp.gradV), pos - (dt / 2) * vel);
             if (homoDeform == 4) pva = angVel - D3{sp.spinVec[0], sp.spinVec[1], sp.spinVec[2]};
         }
-        if (damp) {
-            linAccel.x = linAccel.x * (1 - damping * sgn(f.x * (pvf.x + (0.5 * dt) * linAccel.x)));
-            linAccel.y = linAccel.y * (1 - damping * sgn(f.y * (pvf.y + (0.5 * dt) * linAccel.y)));
-            linAccel.z = linAccel.z * (1 - damping * sgn(f.z * (pvf.z + (0.5 * dt) * linAccel.z)));
-        }
-        if (homoDeform == 4)
+        if (damp) linAccel = dampAccel(linAccel, f, pvf, damping, dt);
+        if (PERI && homoDeform == 4)
             vel = mul(ldm(sp.ImLL4hInv), (mul(ldm(sp.LmL), pos) + mul(ldm(sp.IpLL4h), vel)) + linAccel * dt);
         else
             vel = vel + dt * linAccel;
         if (!isZero(inertia)) {
             D3 angAccel{0, 0, 0};
             if ((flags & F_DOF_ALL) == 0) angAccel = D3{t.x / inertia.x, t.y / inertia.y, t.z / inertia.z};
-            else {
-                if (!(flags & 8u)) angAccel.x = 0. + t.x / inertia.x;
-                if (!(flags & 16u)) angAccel.y = 0. + t.y / inertia.y;
-                if (!(flags & 32u)) angAccel.z = 0. + t.z / inertia.z;
-            }
-            if (damp) {
-                angAccel.x = angAccel.x * (1 - damping * sgn(t.x * (pva.x + (0.5 * dt) * angAccel.x)));
-                angAccel.y = angAccel.y * (1 - damping * sgn(t.y * (pva.y + (0.5 * dt) * angAccel.y)));
-                angAccel.z = angAccel.z * (1 - damping * sgn(t.z * (pva.z + (0.5 * dt) * angAccel.z)));
-            }
+            else angAccel = angAccelPartial(t, inertia, flags);
+            if (damp) angAccel = dampAccel(angAccel, t, pva, damping, dt);
             angVel = angVel + dt * angAccel;
-            if (homoDeform == 4) angVel = angVel - D3{sp.deltaSpinVec[0], sp.deltaSpinVec[1], sp.deltaSpinVec[2]};
+            if (PERI && homoDeform == 4) angVel = angVel - D3{sp.deltaSpinVec[0], sp.deltaSpinVec[1], sp.deltaSpinVec[2]};
         }
     } else {
-        if (homoDeform == 4) vel = mul(ldm(sp.ImLL4hInv), mul(ldm(sp.LmL), pos) + mul(ldm(sp.IpLL4h), vel));
+        if (PERI && homoDeform == 4) vel = mul(ldm(sp.ImLL4hInv), mul(ldm(sp.LmL), pos) + mul(ldm(sp.IpLL4h), vel));
     }
-    if (homoDeform >= 0 && homoDeform != 4) {
+    if (PERI && homoDeform >= 0 && homoDeform != 4) {
         if (homoDeform == 2 || homoDeform == 3) {
             if (homoDeform == 3) vel = vel + mul(ldm(sp.midGradV), vel - (dt / 2.) * linAccel) * dt;
             vel = vel + mul(ldm(sp.dGradV), pos);
@@ -144,14 +165,7 @@ __global__ void __launch_bounds__(256) k_leapfrog(DevNodes N, DevParticles P, De
     N.vel[i] = st4(vel, 0.);
     N.angv[i] = st4(angVel, 0.);
     N.ori[i] = make_double4_32a(ori.w, ori.x, ori.y, ori.z);
-    // Leapfrog(reset=True) for nodes whose force is not rebuilt by the contact sum
-    // (facet vertices): force = mass*gravity, torque = 0 (Leapfrog.cpp:240-245)
-    if (sp.reset && !uni) {
-        D3 G{0, 0, 0};
-        if (sp.hasGravity && !(flags & F_GRAVITY_SKIP)) G = mass * D3{sp.g[0], sp.g[1], sp.g[2]};
-        N.force[i] = st4(G, 0.);
-        N.torque[i] = make_double4_32a(0., 0., 0., 0.);
-    }
+    if (sp.reset && !uni) resetForce(N, i, mass, sp.hasGravity && !(flags & F_GRAVITY_SKIP), spp, valid ? sceneOfN(N, i) : 0);
     // verlet test (d2 + moveDueToRot2 > maxD2 with no rotation term for spheres, walls, facets)
     const D3 lp = ld3(N.lastPos[i]);
     const double d2 = sqn(lp - pos);
@@ -159,9 +173,10 @@ __global__ void __launch_bounds__(256) k_leapfrog(DevNodes N, DevParticles P, De
 }
 
 void launch_leapfrog(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const ScenePar* sp,
-                     int* dFlags, int fromEnds, const long long* dStep) {
+                     int* dFlags, int fromEnds, const long long* dStep, bool periodic) {
     if (N.n == 0) return;
-    k_leapfrog<<<(N.n + 255) / 256, 256, 0, st>>>(N, P, I, sp, dFlags, fromEnds, dStep);
+    if (periodic) k_leapfrog<true><<<(N.n + 255) / 256, 256, 0, st>>>(N, P, I, sp, dFlags, fromEnds, dStep);
+    else k_leapfrog<false><<<(N.n + 255) / 256, 256, 0, st>>>(N, P, I, sp, dFlags, fromEnds, dStep);
 }
 
 // ---------------------------------------------------------------------------------- ContactLoop
@@ -180,6 +195,87 @@ __device__ __forceinline__ void clearEnds(const DevIncidence& I, int64_t c) {
     I.endB[sh] = z2;
 }
 
+// A contact that becomes real: L6Geom::setInitialLocalCoords (pkg/dem/L6Geom.cpp:27-38, :53-71)
+// and Cp2 (FrictMat.cpp:20-44 / Hertz.cpp:9-50). Out of line (see k_leapfrog).
+struct NewContact {
+    D3 c0, c1, c2;
+    double ph[5];
+};
+__device__ __noinline__ NewContact newContact(D3 normal, double r1, double r2, double uN, double4_32a m1, double4_32a m2, double ma,
+                                              double mb, const ScenePar* __restrict__ spp, int scene) {
+    const ScenePar& sp = spp[scene];
+    D3 c0, c1, c2;
+    double ph0, ph1, ph2, ph3 = 0, ph4 = 0;
+    const D3 locX = normal;
+    const D3 ref = (fabs(locX.y) < fabs(locX.z)) ? D3{0, 1, 0} : D3{0, 0, 1};
+    D3 locY = cross(locX, ref);
+    locY = locY - locX * dot(locY, locX);
+    locY = normalized(locY);
+    c0 = locX;
+    c1 = locY;
+    c2 = cross(locX, locY);
+    double lens0 = fabs(r1) + uN / 2, lens1 = fabs(r2) + uN / 2;
+    if (lens0 < 0) lens0 = lens1;
+    if (lens1 < 0) lens1 = lens0;
+    const double rr = (r1 > 0 && r2 > 0) ? smin(r1, r2) : (r1 > 0 ? r1 : r2);
+    const double contA = 3.14159265358979323846 * (rr * rr);
+    // m1, m2: the materials' density young tanPhi ktDivKn; ma, mb: the nodes' masses
+    if (sp.phys == 0) {
+        // Cp2_FrictMat_FrictPhys::updateFrictPhys, pkg/dem/FrictMat.cpp:20-44
+        ph0 = 1 / (1 / (m1.y * contA / lens0) + 1 / (m2.y * contA / lens1));
+        ph1 = .5 * (m1.w + m2.w) * ph0;
+        ph2 = smin(m1.z, m2.z);
+    } else {
+        // Cp2_FrictMat_HertzPhys::go, pkg/dem/Hertz.cpp:9-50 (kn0 = K*sqrt(R) is stored)
+        const double nu1 = sp.hzPoisson, nu2 = sp.hzPoisson;
+        const double E1 = m1.y, E2 = m2.y;
+        const double K = (4 / 3.) * 1. / ((1 - nu1 * nu1) / E1 + (1 - nu2 * nu2) / E2);
+        const double R = 1. / (1. / lens0 + 1. / lens1);
+        const double kn0 = K * sqrt(R);
+        const double G1 = E1 / (2 * (1 + nu1)), G2 = E2 / (2 * (1 + nu2));
+        const double G = .5 * (G1 + G2);
+        const double nu = .5 * (nu1 + nu2);
+        ph0 = kn0;
+        ph1 = 2 * sqrt(4 * R) * G / (2 - nu);
+        ph2 = smin(m1.z, m2.z);
+        ph4 = R;
+        if (sp.hzViscOn) {
+            const double mbar = (ma <= 0 && mb > 0) ? mb : ((ma > 0 && mb <= 0) ? ma : (ma * mb) / (ma + mb));
+            ph3 = smax(0., sp.hzViscConst * sqrt(mbar * kn0));
+        } else ph3 = 0.0;
+    }
+    NewContact r;
+    r.c0 = c0;
+    r.c1 = c1;
+    r.c2 = c2;
+    r.ph[0] = ph0;
+    r.ph[1] = ph1;
+    r.ph[2] = ph2;
+    r.ph[3] = ph3;
+    r.ph[4] = ph4;
+    return r;
+}
+// L6Geom renormalisation of the frame every trsfRenorm steps (L6Geom.cpp:129-135). Out of line.
+struct Frame3 {
+    D3 c0, c1, c2;
+};
+__device__ __noinline__ Frame3 renormFrame(D3 c0, D3 c1) {
+    Frame3 f;
+    f.c0 = normalized(c0);
+    c1 = c1 - f.c0 * dot(c1, f.c0);
+    f.c1 = normalized(c1);
+    f.c2 = cross(f.c0, f.c1);
+    return f;
+}
+// Coulomb cap of the shear force: IdealElPl.cpp:57-63 (zeroIfNull) and Hertz.cpp:160-165. Out of line.
+__device__ __noinline__ double2 capShear(double ft1, double ft2, double maxFt, bool zeroIfNull) {
+    const double FtNorm = sqrt(ft1 * ft1 + ft2 * ft2);
+    double ratio = maxFt / FtNorm;
+    if (zeroIfNull && FtNorm == 0.) ratio = 0.;
+    return make_double2(ft1 * ratio, ft2 * ratio);
+}
+
+template <bool PERI>
 __global__ void __launch_bounds__(128) k_contact_fp64(DevNodes N, DevParticles P, DevContacts C, DevIncidence I,
                                                      const double4_32a* __restrict__ mats, const ScenePar* __restrict__ spp,
                                                      const long long* __restrict__ dStep, int* __restrict__ dFlags) {
@@ -199,7 +295,7 @@ __global__ void __launch_bounds__(128) k_contact_fp64(DevNodes N, DevParticles P
     if (*dStep - sp.stepBase >= sp.stepEnd) return;  // frozen scene (serving slot past its last step)
     uint32_t fl = C.flags[c];
     if (fl & C_REMOVED) return;
-    if ((fl & C_PENDING) && !pendingStays(P, A, B, sp.periodic, sp.cellSize, dErr)) {
+    if ((fl & C_PENDING) && !pendingStays(P, A, B, PERI && sp.periodic, sp.cellSize, dErr)) {
         C.flags[c] = (fl & ~C_PENDING) | C_REMOVED;
         return;
     }
@@ -209,7 +305,7 @@ __global__ void __launch_bounds__(128) k_contact_fp64(DevNodes N, DevParticles P
     const long long step = *dStep - sp.stepBase;
     const double dt = sp.dt;
     D3 shift2{0, 0, 0}, shiftVel2{0, 0, 0};
-    if (sp.periodic) {
+    if (PERI) {
         int a, b, cc;
         unpackCellDist(C.cdist[c], a, b, cc);
         if (fl & C_SWAP) { a = -a; b = -b; cc = -cc; }
@@ -231,47 +327,17 @@ __global__ void __launch_bounds__(128) k_contact_fp64(DevNodes N, DevParticles P
     double ph0, ph1, ph2, ph3 = 0, ph4 = 0;
     double fn, ft1 = 0, ft2 = 0;
     if (!real) {
-        // new geometry: L6Geom::setInitialLocalCoords pkg/dem/L6Geom.cpp:27-38 and :53-71
-        const D3 locX = g.normal;
-        const D3 ref = (fabs(locX.y) < fabs(locX.z)) ? D3{0, 1, 0} : D3{0, 0, 1};
-        D3 locY = cross(locX, ref);
-        locY = locY - locX * dot(locY, locX);
-        locY = normalized(locY);
-        c0 = locX;
-        c1 = locY;
-        c2 = cross(locX, locY);
-        double lens0 = fabs(g.r1) + g.uN / 2, lens1 = fabs(g.r2) + g.uN / 2;
-        if (lens0 < 0) lens0 = lens1;
-        if (lens1 < 0) lens1 = lens0;
-        const double rr = (g.r1 > 0 && g.r2 > 0) ? smin(g.r1, g.r2) : (g.r1 > 0 ? g.r1 : g.r2);
-        const double contA = 3.14159265358979323846 * (rr * rr);
-        const double4_32a m1 = mats[P.mat[A]], m2 = mats[P.mat[B]];  // density young tanPhi ktDivKn
-        if (sp.phys == 0) {
-            // Cp2_FrictMat_FrictPhys::updateFrictPhys, pkg/dem/FrictMat.cpp:20-44
-            ph0 = 1 / (1 / (m1.y * contA / lens0) + 1 / (m2.y * contA / lens1));
-            ph1 = .5 * (m1.w + m2.w) * ph0;
-            ph2 = smin(m1.z, m2.z);
-        } else {
-            // Cp2_FrictMat_HertzPhys::go, pkg/dem/Hertz.cpp:9-50 (kn0 = K*sqrt(R) is stored)
-            const double nu1 = sp.hzPoisson, nu2 = sp.hzPoisson;
-            const double E1 = m1.y, E2 = m2.y;
-            const double K = (4 / 3.) * 1. / ((1 - nu1 * nu1) / E1 + (1 - nu2 * nu2) / E2);
-            const double R = 1. / (1. / lens0 + 1. / lens1);
-            const double kn0 = K * sqrt(R);
-            const double G1 = E1 / (2 * (1 + nu1)), G2 = E2 / (2 * (1 + nu2));
-            const double G = .5 * (G1 + G2);
-            const double nu = .5 * (nu1 + nu2);
-            ph0 = kn0;
-            ph1 = 2 * sqrt(4 * R) * G / (2 - nu);
-            ph2 = smin(m1.z, m2.z);
-            ph4 = R;
-            if (sp.hzViscOn) {
-                const double ma = N.minert[P.shape[A] == WG_SHAPE_FACET ? P.aux[A].x : A].w;
-                const double mb = N.minert[B].w;
-                const double mbar = (ma <= 0 && mb > 0) ? mb : ((ma > 0 && mb <= 0) ? ma : (ma * mb) / (ma + mb));
-                ph3 = smax(0., sp.hzViscConst * sqrt(mbar * kn0));
-            } else ph3 = 0.0;
-        }
+        // new geometry: L6Geom::setInitialLocalCoords pkg/dem/L6Geom.cpp:27-38 and :53-71, Cp2
+        const double ma = N.minert[P.shape[A] == WG_SHAPE_FACET ? P.aux[A].x : A].w, mb = N.minert[B].w;
+        const NewContact nc = newContact(g.normal, g.r1, g.r2, g.uN, mats[P.mat[A]], mats[P.mat[B]], ma, mb, spp, sceneOfP(P, B));
+        c0 = nc.c0;
+        c1 = nc.c1;
+        c2 = nc.c2;
+        ph0 = nc.ph[0];
+        ph1 = nc.ph[1];
+        ph2 = nc.ph[2];
+        ph3 = nc.ph[3];
+        ph4 = nc.ph[4];
         C.col[CC_P0][c] = ph0;
         C.col[CC_P1][c] = ph1;
         C.col[CC_P2][c] = ph2;
@@ -304,10 +370,10 @@ __global__ void __launch_bounds__(128) k_contact_fp64(DevNodes N, DevParticles P
         c1 = prevC1 - cross(m1v, rt);
         c2 = cross(c0, c1);
         if (sp.trsfRenorm > 0 && (step % sp.trsfRenorm) == 0) {
-            c0 = normalized(c0);
-            c1 = c1 - c0 * dot(c1, c0);
-            c1 = normalized(c1);
-            c2 = cross(c0, c1);
+            const Frame3 f = renormFrame(c0, c1);
+            c0 = f.c0;
+            c1 = f.c1;
+            c2 = f.c2;
         }
         D3 midContPt, midPos1, midPos2;
         if (am & 8) {
@@ -346,11 +412,9 @@ __global__ void __launch_bounds__(128) k_contact_fp64(DevNodes N, DevParticles P
                 ft2 = ft2 + (dt * ph1) * lvel.z;
                 const double maxFt = fabs(fn) * ph2;
                 if ((ft1 * ft1 + ft2 * ft2) > maxFt * maxFt && !sp.noSlip) {
-                    const double FtNorm = sqrt(ft1 * ft1 + ft2 * ft2);
-                    double ratio = maxFt / FtNorm;
-                    if (FtNorm == 0.) ratio = 0.;
-                    ft1 = ft1 * ratio;
-                    ft2 = ft2 * ratio;
+                    const double2 q = capShear(ft1, ft2, maxFt, true);
+                    ft1 = q.x;
+                    ft2 = q.y;
                 }
                 if (isnan(fn) || isnan(ft1) || isnan(ft2)) atomicCAS(dErr, 0, 101);  // "NaN force in contact"
             }
@@ -371,10 +435,9 @@ __global__ void __launch_bounds__(128) k_contact_fp64(DevNodes N, DevParticles P
             ft2 = (dt * kt) * lvel.z;
             const double maxFt = smax(0., fn) * ph2;
             if ((ft1 * ft1 + ft2 * ft2) > maxFt * maxFt) {
-                const double FtNorm = sqrt(ft1 * ft1 + ft2 * ft2);
-                const double ratio = maxFt / FtNorm;
-                ft1 = ft1 * ratio;
-                ft2 = ft2 * ratio;
+                const double2 q = capShear(ft1, ft2, maxFt, false);
+                ft1 = q.x;
+                ft2 = q.y;
             } else {
                 ft1 = ft1 + eta * lvel.y;
                 ft2 = ft2 + eta * lvel.z;
@@ -402,7 +465,7 @@ __global__ void __launch_bounds__(128) k_contact_fp64(DevNodes N, DevParticles P
             I.endB[sA] = make_double2(TA.y, TA.z);
         }
         const D3 FB = Fg * -1.0;
-        const D3 xcB = g.contPt - (ld3(N.posr[B]) + (sp.periodic ? shift2 : D3{0, 0, 0}));
+        const D3 xcB = g.contPt - (ld3(N.posr[B]) + (PERI ? shift2 : D3{0, 0, 0}));
         const D3 TB = cross(xcB, FB) + D3{0, 0, 0};
         const int sB = aIsLo ? I.slotHi[c] : I.slotLo[c];
         I.endA[sB] = make_double4_32a(FB.x, FB.y, FB.z, TB.x);
@@ -424,10 +487,12 @@ __global__ void __launch_bounds__(128) k_contact_fp64(DevNodes N, DevParticles P
 }
 
 void launch_contact_fp64(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C, const DevIncidence& I,
-                         const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dFlags, int block) {
+                         const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dFlags, bool periodic, int block) {
     const int bs = block;
     // launched even without contacts: it raises FL_HALT when a full run is due
-    k_contact_fp64<<<(unsigned)std::max<int64_t>(1, (I.nAct + bs - 1) / bs), bs, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags);
+    const unsigned g = (unsigned)std::max<int64_t>(1, (I.nAct + bs - 1) / bs);
+    if (periodic) k_contact_fp64<true><<<g, bs, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags);
+    else k_contact_fp64<false><<<g, bs, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags);
 }
 
 // ---------------------------------------------------------------------------------- force sum

@@ -402,10 +402,16 @@ __device__ __forceinline__ bool renormStep(long long step, int every) {
 }
 
 // Cp2_FrictMat_FrictPhys / Cp2_FrictMat_HertzPhys on contact creation (FrictMat.cpp:20-44,
-// Hertz.cpp:9-50), evaluated in FP64 from the FP32 geometry; ma/mb: the two nodes' mass.
-__device__ __forceinline__ void physCreate(const ScenePar& sp, float r1, float r2, float uN, const double4_32a& m1,
-                                           const double4_32a& m2, double ma, double mb, float& ph0, float& ph1, float& ph2,
-                                           float& ph3) {
+// Hertz.cpp:9-50), evaluated in FP64 from the FP32 geometry; ma/mb: the two nodes' mass. Out of
+// line: its FP64 arithmetic runs only in warps that create a contact (rare paths of FP64 code
+// inlined into a kernel become predicated instructions that occupy the FP64 pipe in every warp).
+struct Phys4 {
+    float p0, p1, p2, p3;
+};
+__device__ __noinline__ Phys4 physCreateFP64(const ScenePar* __restrict__ spp, int scene, float r1, float r2, float uN,
+                                             double4_32a m1, double4_32a m2, double ma, double mb) {
+    const ScenePar& sp = spp[scene];
+    float ph0, ph1, ph2, ph3;
     double lens0 = fabs((double)r1) + (double)uN / 2, lens1 = fabs((double)r2) + (double)uN / 2;
     if (lens0 < 0) lens0 = lens1;
     if (lens1 < 0) lens1 = lens0;
@@ -431,6 +437,16 @@ __device__ __forceinline__ void physCreate(const ScenePar& sp, float r1, float r
             ph3 = (float)fmax(0., sp.hzViscConst * sqrt(mbar * kn0));
         }
     }
+    return Phys4{ph0, ph1, ph2, ph3};
+}
+__device__ __forceinline__ void physCreate(const ScenePar* __restrict__ spp, int scene, float r1, float r2, float uN, const double4_32a& m1,
+                                           const double4_32a& m2, double ma, double mb, float& ph0, float& ph1, float& ph2,
+                                           float& ph3) {
+    const Phys4 q = physCreateFP64(spp, scene, r1, r2, uN, m1, m2, ma, mb);
+    ph0 = q.p0;
+    ph1 = q.p1;
+    ph2 = q.p2;
+    ph3 = q.p3;
 }
 
 // The values one sphere-sphere contact is evaluated from: its packed item, flags, state and the
@@ -484,7 +500,7 @@ __device__ __forceinline__ void ssContact(const SSIn& x, int64_t j, const DevNod
     float ph0, ph1, ph2, ph3;
     if (!real) {
         frameInit(n, f);
-        physCreate(sp, r1, r2, uN, mats[P.mat[A]], mats[P.mat[B]], N.minert[A].w, N.minert[B].w, ph0, ph1, ph2, ph3);
+        physCreate(spp, (int)(pf >> 8), r1, r2, uN, mats[P.mat[A]], mats[P.mat[B]], N.minert[A].w, N.minert[B].w, ph0, ph1, ph2, ph3);
         K.col[CF_P0][j] = ph0;
         K.col[CF_P1][j] = ph1;
         K.col[CF_P2][j] = ph2;
@@ -739,6 +755,13 @@ void launch_facet_prep(cudaStream_t st, const DevNodes& N, const DevParticles& P
     if (P.nFacets > 0 && P.prep) k_facet_prep<<<(P.nFacets + 63) / 64, 64, 0, st>>>(N, P, dFlags);
 }
 
+// rare paths of the facet geometry, out of line (see physCreateFP64)
+__device__ __noinline__ D3 closestSegmentPtOut(D3 P, D3 A, D3 B) { return closestSegmentPt(P, A, B); }
+__device__ __noinline__ D3 facetAngVelOut(D3 p0, D3 p1, D3 p2, D3 c, D3 v0, D3 v1, D3 v2) {
+    return (cross(p0 - c, v0) + cross(p1 - c, v1)) + cross(p2 - c, v2);
+}
+__device__ __noinline__ D3 normalPartOut(D3 v, D3 n) { return dot(v, n) * n; }
+
 // Cg2_Facet_Sphere_L6Geom::go (Facet.cpp:235-288, Facet::interpolatePtLinAngVel :158-174) in FP64
 // from the facet's FacetPrep of this step: the per-contact part of the functor (plane distance,
 // region tests, closest point, barycentric velocity).
@@ -764,9 +787,9 @@ __device__ __forceinline__ bool geomFS32(const DevNodes& N, const DevParticles& 
     D3 contPt;
     switch (w) {
         case 0: contPt = fC; break;
-        case 1: contPt = closestSegmentPt(fC, p0, p1); break;
-        case 2: contPt = closestSegmentPt(fC, p1, p2); break;
-        case 4: contPt = closestSegmentPt(fC, p2, p0); break;
+        case 1: contPt = closestSegmentPtOut(fC, p0, p1); break;
+        case 2: contPt = closestSegmentPtOut(fC, p1, p2); break;
+        case 4: contPt = closestSegmentPtOut(fC, p2, p0); break;
         case 3: contPt = p1; break;
         case 5: contPt = p0; break;
         case 6: contPt = p2; break;
@@ -788,11 +811,10 @@ __device__ __forceinline__ bool geomFS32(const DevNodes& N, const DevParticles& 
     const D3 v0 = ld3(N.vel[fn.x]), v1 = ld3(N.vel[fn.y]), v2 = ld3(N.vel[fn.z]);
     D3 linVel = (a0 * v0 + u * v1) + v * v2;
     D3 angVel{0, 0, 0};
-    if (!isZero(v0) || !isZero(v1) || !isZero(v2))
-        angVel = (cross(p0 - contPt, v0) + cross(p1 - contPt, v1)) + cross(p2 - contPt, v2);
+    if (!isZero(v0) || !isZero(v1) || !isZero(v2)) angVel = facetAngVelOut(p0, p1, p2, contPt, v0, v1, v2);
     if (!isZero(fakeVel)) {
         if (!isnan(fakeVel.x)) linVel = linVel + fakeVel;
-        else linVel = dot(linVel, fNormal) * fNormal;
+        else linVel = normalPartOut(linVel, fNormal);
     }
     g.normal = normal;
     g.contPt = contPt;
@@ -809,6 +831,7 @@ __device__ __forceinline__ bool geomFS32(const DevNodes& N, const DevParticles& 
 
 // Work items [c0, c1): facet and wall contacts, and every contact of a periodic scene (cell shifts,
 // FP64 geometry of the shifted pairs); the state is read and written in the contact arrays.
+template <bool PERI>
 __device__ __forceinline__ void mixedContact(int64_t rk, const DevNodes& N, const DevParticles& P, const DevContacts& C,
                                              const DevIncidence& I, const double4_32a* __restrict__ mats,
                                              const ScenePar* __restrict__ spp, const long long* __restrict__ dStep, int* dFlags) {
@@ -821,7 +844,7 @@ __device__ __forceinline__ void mixedContact(int64_t rk, const DevNodes& N, cons
     if (*dStep - sp.stepBase >= sp.stepEnd) return;  // frozen scene (serving slot past its last step)
     uint32_t fl = C.flags[c];
     if (fl & C_REMOVED) return;
-    if ((fl & C_PENDING) && !pendingStays(P, A, B, sp.periodic, sp.cellSize, dErr)) {
+    if ((fl & C_PENDING) && !pendingStays(P, A, B, PERI && sp.periodic, sp.cellSize, dErr)) {
         C.flags[c] = (fl & ~C_PENDING) | C_REMOVED;
         return;
     }
@@ -833,7 +856,7 @@ __device__ __forceinline__ void mixedContact(int64_t rk, const DevNodes& N, cons
     const float dtf = sp.dtF;
     bool shifted = false;
     D3 shift2{0, 0, 0}, shiftVel2{0, 0, 0};
-    if (sp.periodic) {
+    if (PERI && sp.periodic) {
         int a, b, cc;
         unpackCellDist(C.cdist[c], a, b, cc);
         if (fl & C_SWAP) { a = -a; b = -b; cc = -cc; }
@@ -848,7 +871,7 @@ __device__ __forceinline__ void mixedContact(int64_t rk, const DevNodes& N, cons
     // c1x/c2x: mid-step branch vectors of L6Geom.cpp:156-160; dv: relative velocity of the centres
     F3 n, armA, armB, c1x, c2x, dv, w1, w2;
     float uN, r1, r2;
-    if (ty == CT_SS && !shifted) {
+    if (PERI && ty == CT_SS && !shifted) {
         SSGeo g;
         if (!geomSS32(N.mir[A], N.mir[B], N.wz[A], N.wz[B], sp.ssDfAbsF, real, g)) {
             C.flags[c] = fl;
@@ -861,7 +884,7 @@ __device__ __forceinline__ void mixedContact(int64_t rk, const DevNodes& N, cons
         dv = g.dv;
         w1 = g.w1;
         w2 = g.w2;
-    } else if (ty == CT_SS) {
+    } else if (PERI && ty == CT_SS) {
         // a pair across the periodic boundary: FP64 relative position with the cell shift
         const double4_32a pa = N.posr[A], pb = N.posr[B];
         const D3 dx = (ld3(pb) + shift2) - ld3(pa);
@@ -881,7 +904,7 @@ __device__ __forceinline__ void mixedContact(int64_t rk, const DevNodes& N, cons
         w1 = toF(ld3(N.angv[A]));
         w2 = toF(ld3(N.angv[B]));
     }
-    if (ty == CT_SS) {
+    if (PERI && ty == CT_SS) {
         // contPt = x1 + (r1 + uN/2) n (Sphere.cpp:103), written relative to both centres
         armA = (r1 + 0.5f * uN) * n;
         armB = -(r2 + 0.5f * uN) * n;
@@ -926,7 +949,7 @@ __device__ __forceinline__ void mixedContact(int64_t rk, const DevNodes& N, cons
     if (!real) {
         frameInit(n, f);
         const double ma = N.minert[P.shape[A] == WG_SHAPE_FACET ? P.aux[A].x : A].w, mb = N.minert[B].w;
-        physCreate(sp, r1, r2, uN, mats[P.mat[A]], mats[P.mat[B]], ma, mb, ph0, ph1, ph2, ph3);
+        physCreate(spp, sceneOfP(P, B), r1, r2, uN, mats[P.mat[A]], mats[P.mat[B]], ma, mb, ph0, ph1, ph2, ph3);
         C.fcol[CF_P0][c] = ph0;
         C.fcol[CF_P1][c] = ph1;
         C.fcol[CF_P2][c] = ph2;
@@ -1035,6 +1058,7 @@ __device__ __forceinline__ void mixedContact(int64_t rk, const DevNodes& N, cons
 
 // One thread per work item of [c0, c1), looping over the range with the grid's stride (the
 // launch sizes the grid so that its blocks leave room for the sphere-sphere kernel beside it).
+template <bool PERI>
 __global__ void __launch_bounds__(128, 4) k_contact_fp32(DevNodes N, DevParticles P, DevContacts C, DevIncidence I,
                                                        const double4_32a* __restrict__ mats, const ScenePar* __restrict__ spp,
                                                        const long long* __restrict__ dStep, int* __restrict__ dFlags, int64_t c0,
@@ -1045,7 +1069,7 @@ __global__ void __launch_bounds__(128, 4) k_contact_fp32(DevNodes N, DevParticle
     }
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t rk = c0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; rk < c1; rk += stride)
-        mixedContact(rk, N, P, C, I, mats, spp, dStep, dFlags);
+        mixedContact<PERI>(rk, N, P, C, I, mats, spp, dStep, dFlags);
 }
 
 // minimum resident blocks per SM the one-contact-per-thread kernel is compiled for (register budget)
@@ -1088,8 +1112,8 @@ void launch_contact_fp32(cudaStream_t st, const SideStream& side, const DevNodes
         cudaStreamWaitEvent(side.st, side.fork, 0);
         launch_facet_prep(side.st, N, P, dFlags);
         // one block of 128 threads per SM: two blocks of the sphere-sphere kernel still fit beside it
-        k_contact_fp32<<<(unsigned)std::min<int64_t>((nm + 127) / 128, smCount()), 128, 0, side.st>>>(N, P, C, I, mats, sp, dStep,
-                                                                                                     dFlags, 0, nm, 0);
+        k_contact_fp32<false><<<(unsigned)std::min<int64_t>((nm + 127) / 128, smCount()), 128, 0, side.st>>>(N, P, C, I, mats, sp, dStep,
+                                                                                                            dFlags, 0, nm, 0);
         launchSS(st, N, P, C, I, K, mats, sp, dStep, dFlags, nm, 1, anyLaw0, block);
         cudaEventRecord(side.join, side.st);
         cudaStreamWaitEvent(st, side.join, 0);
@@ -1097,8 +1121,9 @@ void launch_contact_fp32(cudaStream_t st, const SideStream& side, const DevNodes
     }
     // the first launch also raises FL_HALT when a full run is due (it always runs)
     if (nm > 0) launch_facet_prep(st, N, P, dFlags);
-    k_contact_fp32<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>((nm + 127) / 128, 4 * smCount())), 128, 0, st>>>(
-        N, P, C, I, mats, sp, dStep, dFlags, 0, nm, 1);
+    const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((nm + 127) / 128, 4 * smCount()));
+    if (periodic) k_contact_fp32<true><<<g, 128, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags, 0, nm, 1);
+    else k_contact_fp32<false><<<g, 128, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags, 0, nm, 1);
     if (ns > 0) launchSS(st, N, P, C, I, K, mats, sp, dStep, dFlags, nm, 0, anyLaw0, block);
 }
 
