@@ -336,6 +336,7 @@ int Sim::prepareParamsFor(const wg_config& cfg, int64_t p0, int64_t p1, ScenePar
     p.maxD2 = vd * vd;
     // FP32 verlet test: a hair below maxD2 so that rounding can only trigger a full run early
     p.maxD2F = (float)(p.maxD2 * (1 - 1e-6));
+    p.reach2F = (float)(2 * p.verletDist);
     (void)X;
     (void)S;
     return 0;

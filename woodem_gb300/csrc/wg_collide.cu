@@ -50,6 +50,9 @@ struct CollideWork {
     uint32_t* smask = nullptr;
     float4* smnf = nullptr;       // box min rounded down, mask in w
     float4* smxf = nullptr;       // box max rounded up, particle id in w
+    int32_t* newLo = nullptr;     // first index of each lo id in the sorted new pairs (merge)
+    int32_t* oldLo = nullptr;     // the same in the previous contact keys
+    int64_t newLoCap = 0, oldLoCap = 0;
     float4* smnfi = nullptr;      // box min rounded up (inward)
     float4* smxfi = nullptr;      // box max rounded down (inward)
     int32_t* cellOff = nullptr;
@@ -635,16 +638,42 @@ __global__ void k_pairs_large_large(DevParticles P, const int32_t* __restrict__ 
 __device__ __forceinline__ bool freshPair(const uint8_t* fresh, uint64_t k) {
     return fresh && (fresh[(int)(k >> 32)] || fresh[(int)(k & 0xffffffffu)]);
 }
-__global__ void k_mark_orphans(DevContacts C, const uint64_t* __restrict__ nk, int64_t nn, int32_t* __restrict__ orph,
-                               const uint8_t* __restrict__ fresh) {
+// start[p] = first index of key array (sorted ascending, key = lo << 32 | hi) whose lo is >= p,
+// for p in [0, nPar]; one thread per index fills the ids between its lo and its predecessor's.
+__global__ void k_lo_bounds(const uint64_t* __restrict__ key, int64_t n, int nPar, int32_t* __restrict__ start) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > n) return;
+    const int cur = (i < n) ? (int)(key[i] >> 32) : nPar;
+    const int prev = (i > 0) ? (int)(key[i - 1] >> 32) : -1;
+    for (int q = prev + 1; q <= cur && q <= nPar; q++) start[q] = (int32_t)i;
+}
+// position of k in the sorted key array, searched within the range of its lo id (a few entries
+// for a sphere, thousands for a wall), or -1
+__device__ __forceinline__ int64_t findInRange(const uint64_t* __restrict__ key, const int32_t* __restrict__ start, uint64_t k) {
+    const int lo = (int)(k >> 32);
+    int64_t a = start[lo], b = start[lo + 1];
+    while (a < b) {
+        const int64_t m = (a + b) >> 1;
+        if (key[m] < k) a = m + 1;
+        else b = m;
+    }
+    return (a < start[lo + 1] && key[a] == k) ? a : -1;
+}
+// pair keys (lo << 32 | hi) to (lo << bits | hi) for the sort, and back
+__global__ void k_pack_keys(uint64_t* __restrict__ k, int64_t n, int bits) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) k[i] = ((k[i] >> 32) << bits) | (k[i] & 0xffffffffu);
+}
+__global__ void k_unpack_keys(uint64_t* __restrict__ k, int64_t n, int bits) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) k[i] = ((k[i] >> bits) << 32) | (k[i] & ((1ull << bits) - 1));
+}
+__global__ void k_mark_orphans(DevContacts C, const uint64_t* __restrict__ nk, const int32_t* __restrict__ newLo,
+                               int32_t* __restrict__ orph, const uint8_t* __restrict__ fresh) {
     const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= C.n) return;
     int32_t o = 0;
-    if ((C.flags[j] & C_REAL) && !freshPair(fresh, C.key[j])) {
-        const uint64_t k = C.key[j];
-        const int64_t pos = lowerBound64(nk, nn, k);
-        o = (pos < nn && nk[pos] == k) ? 0 : 1;
-    }
+    if ((C.flags[j] & C_REAL) && !freshPair(fresh, C.key[j])) o = findInRange(nk, newLo, C.key[j]) < 0 ? 1 : 0;
     orph[j] = o;
 }
 __global__ void k_compact_orphans(DevContacts C, const int32_t* __restrict__ orphFlag, const int32_t* __restrict__ orphScan,
@@ -658,16 +687,16 @@ __global__ void k_compact_orphans(DevContacts C, const int32_t* __restrict__ orp
     }
 }
 __global__ void k_place_new(const uint64_t* __restrict__ nk, int64_t nn, const uint64_t* __restrict__ okey, int64_t no,
-                            const uint64_t* __restrict__ oldKey, int64_t nOld, uint64_t* __restrict__ outKey,
+                            const uint64_t* __restrict__ oldKey, const int32_t* __restrict__ oldLo, uint64_t* __restrict__ outKey,
                             int32_t* __restrict__ src, const int32_t* __restrict__ nkCd, int32_t* __restrict__ outCd,
                             const uint8_t* __restrict__ fresh) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nn) return;
     const uint64_t k = nk[i];
     const int64_t out = i + lowerBound64(okey, no, k);
-    const int64_t pos = lowerBound64(oldKey, nOld, k);
+    const int64_t pos = oldLo ? findInRange(oldKey, oldLo, k) : -1;
     outKey[out] = k;
-    src[out] = (pos < nOld && oldKey[pos] == k && !freshPair(fresh, k)) ? (int32_t)pos : -1;
+    src[out] = (pos >= 0 && !freshPair(fresh, k)) ? (int32_t)pos : -1;
     if (nkCd) outCd[out] = nkCd[i];
 }
 __global__ void k_place_orph(const uint64_t* __restrict__ nk, int64_t nn, const uint64_t* __restrict__ okey,
@@ -736,32 +765,15 @@ __global__ void k_gather(DevContacts Cold, DevContacts Cnew, const int32_t* __re
 // contacts stay in the container (they are potential contacts of the reference) but the contact
 // kernels skip them. The bounds are taken with a relative margin of 1e-9, and only for aperiodic
 // scenes (a periodic cell moves the images of the particles by itself).
-__global__ void k_dormant(DevContacts C, DevNodes N, DevParticles P, const ScenePar* __restrict__ spp) {
-    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= C.n) return;
-    const uint32_t fl = C.flags[c];
-    if (fl & C_REAL) return;
-    const uint32_t ty = ctype(fl);
-    if (ty == CT_NONE) return;
-    const uint64_t key = C.key[c];
-    const int lo = (int)(key >> 32), hi = (int)(key & 0xffffffffu);
-    const int A = (fl & C_SWAP) ? hi : lo, B = (fl & C_SWAP) ? lo : hi;
-    const ScenePar& sp = spp[sceneOfP(P, B)];
+// The FP64 tests of k_dormant (sphere-sphere without mirrors, wall-sphere, facet-sphere), out of
+// line: inlined, they become predicated FP64 instructions in the warps of mirror-tested pairs.
+__device__ __noinline__ bool dormantFarFP64(const DevNodes& N, const DevParticles& P, const ScenePar* __restrict__ spp, int scene,
+                                            uint32_t ty, int A, int B) {
+    const ScenePar& sp = spp[scene];
     const double m2 = 2 * sp.verletDist;
     bool far;
     const double4_32a pb = N.posr[B];
-    if (ty == CT_SS && N.mir) {
-        // FP32-force mode: the double-float mirrors of the positions, FP32 arithmetic; the
-        // relative position carries ~47 bits and the squares and sums ~2^-22 relative error
-        const float4 ha = N.mir[A].ph, la = N.mir[A].pl, hb = N.mir[B].ph, lb = N.mir[B].pl;
-        float sx, tx, sy, ty_, sz, tz;
-        dfDiff(ha.x, la.x, hb.x, lb.x, sx, tx);
-        dfDiff(ha.y, la.y, hb.y, lb.y, sy, ty_);
-        dfDiff(ha.z, la.z, hb.z, lb.z, sz, tz);
-        const float dx = sx + tx, dy = sy + ty_, dz = sz + tz;
-        const float reach = (sp.ssDfAbsF * (ha.w + hb.w) + (float)m2) * (1.f + 1e-5f);
-        far = dx * dx + dy * dy + dz * dz > reach * reach;
-    } else if (ty == CT_SS) {
+    if (ty == CT_SS) {
         const double4_32a pa = N.posr[A];
         const double dx = pb.x - pa.x, dy = pb.y - pa.y, dz = pb.z - pa.z;
         const double reach = (fabs(sp.ssDistFactor) * (pa.w + pb.w) + m2) * (1 + 1e-9);
@@ -799,6 +811,33 @@ __global__ void k_dormant(DevContacts C, DevNodes N, DevParticles P, const Scene
             far = d2 > reach * reach;
         }
     }
+    return far;
+}
+__global__ void k_dormant(DevContacts C, DevNodes N, DevParticles P, const ScenePar* __restrict__ spp) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= C.n) return;
+    const uint32_t fl = C.flags[c];
+    if (fl & C_REAL) return;
+    const uint32_t ty = ctype(fl);
+    if (ty == CT_NONE) return;
+    const uint64_t key = C.key[c];
+    const int lo = (int)(key >> 32), hi = (int)(key & 0xffffffffu);
+    const int A = (fl & C_SWAP) ? hi : lo, B = (fl & C_SWAP) ? lo : hi;
+    const int scene = sceneOfP(P, B);
+    bool far;
+    if (ty == CT_SS && N.mir) {
+        // FP32-force mode: the double-float mirrors of the positions, FP32 arithmetic; the
+        // relative position carries ~47 bits and the squares and sums ~2^-22 relative error
+        const ScenePar& sp = spp[scene];
+        const float4 ha = N.mir[A].ph, la = N.mir[A].pl, hb = N.mir[B].ph, lb = N.mir[B].pl;
+        float sx, tx, sy, ty_, sz, tz;
+        dfDiff(ha.x, la.x, hb.x, lb.x, sx, tx);
+        dfDiff(ha.y, la.y, hb.y, lb.y, sy, ty_);
+        dfDiff(ha.z, la.z, hb.z, lb.z, sz, tz);
+        const float dx = sx + tx, dy = sy + ty_, dz = sz + tz;
+        const float reach = (sp.ssDfAbsF * (ha.w + hb.w) + sp.reach2F) * (1.f + 1e-5f);
+        far = dx * dx + dy * dy + dz * dz > reach * reach;
+    } else far = dormantFarFP64(N, P, spp, scene, ty, A, B);
     if (far) C.flags[c] = fl | C_DORMANT;
 }
 
@@ -1163,11 +1202,15 @@ int collide_full_run(Sim& S) {
         WG_CUDA_TRY(cub::DeviceRadixSort::SortPairs(W.cubTmp, tb, W.pairs, W.pairsSorted, W.pairCd, W.pairCdSorted, nNew, 0,
                                                     32 + idBits, st));
     } else if (nNew > 0) {
+        // ids take idBits each: sort (lo << idBits | hi), the same order in fewer radix passes
+        const unsigned pb = (unsigned)((nNew + BS - 1) / BS);
+        k_pack_keys<<<pb, BS, 0, st>>>(W.pairs, nNew, idBits);
         size_t tb = 0;
-        cub::DeviceRadixSort::SortKeys(nullptr, tb, W.pairs, W.pairsSorted, nNew, 0, 32 + idBits, st);
+        cub::DeviceRadixSort::SortKeys(nullptr, tb, W.pairs, W.pairsSorted, nNew, 0, 2 * idBits, st);
         if (ensureCub(S, tb)) return WG_ERR_CUDA;
         tb = W.cubBytes;
-        WG_CUDA_TRY(cub::DeviceRadixSort::SortKeys(W.cubTmp, tb, W.pairs, W.pairsSorted, nNew, 0, 32 + idBits, st));
+        WG_CUDA_TRY(cub::DeviceRadixSort::SortKeys(W.cubTmp, tb, W.pairs, W.pairsSorted, nNew, 0, 2 * idBits, st));
+        k_unpack_keys<<<pb, BS, 0, st>>>(W.pairsSorted, nNew, idBits);
     }
     // 5. merge with the previous contact set
     const int64_t nOld = S.C.n;
@@ -1179,10 +1222,16 @@ int collide_full_run(Sim& S) {
         (void)dummy;
     }
     int64_t nOrph = 0;
+    // the first index of every lo id in the new pairs and in the old contacts
+    W.newLo = grow(S, W.newLo, W.newLoCap, S.nPar + 2);
+    W.oldLo = grow(S, W.oldLo, W.oldLoCap, S.nPar + 2);
+    if (!W.newLo || !W.oldLo) return S.fail(WG_ERR_CUDA, "out of device memory (merge)");
+    k_lo_bounds<<<(unsigned)((nNew + 1 + BS - 1) / BS), BS, 0, st>>>(W.pairsSorted, nNew, (int)S.nPar, W.newLo);
+    k_lo_bounds<<<(unsigned)((nOld + 1 + BS - 1) / BS), BS, 0, st>>>(S.C.key, nOld, (int)S.nPar, W.oldLo);
     if (nOld > 0) {
         int32_t* flagsArr = W.orph;
         int32_t* scanArr = W.orph + (std::max<int64_t>(nOld, 1) + 1);
-        k_mark_orphans<<<(unsigned)((nOld + BS - 1) / BS), BS, 0, st>>>(S.C, W.pairsSorted, nNew, flagsArr, S.P.fresh);
+        k_mark_orphans<<<(unsigned)((nOld + BS - 1) / BS), BS, 0, st>>>(S.C, W.pairsSorted, W.newLo, flagsArr, S.P.fresh);
         size_t tb = 0;
         cub::DeviceScan::ExclusiveSum(nullptr, tb, flagsArr, scanArr, (int)nOld, st);
         if (ensureCub(S, tb)) return WG_ERR_CUDA;
@@ -1216,8 +1265,9 @@ int collide_full_run(Sim& S) {
         if (!W.newCd) return S.fail(WG_ERR_CUDA, "out of device memory (merge)");
     }
     if (nNew > 0)
-        k_place_new<<<(unsigned)((nNew + BS - 1) / BS), BS, 0, st>>>(W.pairsSorted, nNew, W.orphKey, nOrph, S.C.key, nOld, S.Cb.key,
-                                                                    W.src, peri ? W.pairCdSorted : nullptr, W.newCd, S.P.fresh);
+        k_place_new<<<(unsigned)((nNew + BS - 1) / BS), BS, 0, st>>>(W.pairsSorted, nNew, W.orphKey, nOrph, S.C.key,
+                                                                    nOld > 0 ? W.oldLo : nullptr, S.Cb.key, W.src,
+                                                                    peri ? W.pairCdSorted : nullptr, W.newCd, S.P.fresh);
     if (nOrph > 0)
         k_place_orph<<<(unsigned)((nOrph + BS - 1) / BS), BS, 0, st>>>(W.pairsSorted, nNew, W.orphKey, W.orphSrc, nOrph, S.Cb.key,
                                                                       W.src);

@@ -44,6 +44,7 @@ struct ScenePar {
     float dtF, ssDfAbsF;  // FP32 copies read by the FP32-force kernels
     float gH[3], gL[3];   // gravity as double-float pairs (g = gH + gL)
     float dampingF, maxD2F;
+    float reach2F;        // 2*verletDist in FP32 (dormant-contact test of the FP32-force mode)
     long long stepBase;   // Scene.step of this scene = device step counter - stepBase
     long long stepEnd;    // the scene is frozen once Scene.step reaches stepEnd (serving slots)
     // periodic cell, integrated on the host each step (core/Cell.cpp:81-120)
