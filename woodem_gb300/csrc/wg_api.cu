@@ -543,6 +543,16 @@ int Sim::upload() {
             WG_CUDA_TRY(cudaMemset(P.prep, 0xff, sizeof(FacetPrep) * P.nFacets));  // NaN: made at the first step
         }
     }
+    // facets whose vertices are all fully blocked and at rest never move: their FacetPrep records
+    // are made once (here and when the host writes the state) instead of at every step
+    facetsStatic = P.nFacets > 0;
+    for (int64_t p = 0; p < nPar && facetsStatic; p++) {
+        if (hShape[p] != WG_SHAPE_FACET) continue;
+        for (int k = 0; k < 3; k++) {
+            const int32_t v = map[hNodes3[3 * p + k]];
+            if ((flags[v] & F_DOF_ALL) != F_DOF_ALL || vel[v].x != 0 || vel[v].y != 0 || vel[v].z != 0) facetsStatic = false;
+        }
+    }
     WG_CUDA_TRY(cudaMemcpy(P.facet, facet.data(), sizeof(double4_32a) * nPar, cudaMemcpyHostToDevice));
     WG_CUDA_TRY(cudaMemcpy(P.mat, mat.data(), sizeof(int32_t) * nPar, cudaMemcpyHostToDevice));
     WG_CUDA_TRY(cudaMemcpy(P.mask, mask.data(), sizeof(uint32_t) * nPar, cudaMemcpyHostToDevice));
@@ -608,6 +618,7 @@ int Sim::upload() {
         WG_CUDA_TRY(cudaMemcpy(N.ll, hpl.data(), sizeof(float4) * nSlots, cudaMemcpyHostToDevice));
         WG_CUDA_TRY(cudaMemcpy(dNodeC, nc.data(), sizeof(NodeConst32) * nSlots, cudaMemcpyHostToDevice));
     }
+    launch_facet_prep(stream, N, P, nullptr);
     long long st0 = cfg.step;
     step = cfg.step;
     WG_CUDA_TRY(cudaMemcpy(dStep, &st0, sizeof(long long), cudaMemcpyHostToDevice));
@@ -713,13 +724,14 @@ int Sim::run(int64_t n) {
         launches++;
     };
     auto stepContact = [&]() {
-        if (fp32) launch_contact_fp32(stream, concurrentContacts ? side : SideStream{}, N, P, C, I, K, dMats, dPar, dStep, dFlags, nMixed,
-                                      cfg.periodic != 0, anyLaw0,
-                                      contactBlock != 0 ? contactBlock : -256);
+        bool advanced = false;  // the last contact kernel advanced the step counter itself
+        if (fp32)
+            advanced = launch_contact_fp32(stream, concurrentContacts ? side : SideStream{}, N, P, C, I, K, dMats, dPar, dStep, dFlags,
+                                           nMixed, cfg.periodic != 0, anyLaw0, !facetsStatic, contactBlock != 0 ? contactBlock : -256);
         else launch_contact_fp64(stream, N, P, C, I, dMats, dPar, dStep, dFlags, cfg.periodic != 0,
                                  (contactBlock > 0 && contactBlock <= 128) ? contactBlock : 128);  // launch bounds 128
-        launch_advance(stream, dStep, dFlags);
-        launches += 2;
+        if (!advanced) launch_advance(stream, dStep, dFlags);
+        launches += advanced ? 1 : 2;
     };
     WG_CUDA_TRY(cudaMemsetAsync(dFlags, 0, sizeof(int) * 4, stream));
     WG_CUDA_TRY(cudaEventRecord(ev[6], stream));
@@ -1313,6 +1325,8 @@ int wg_put_state(wg_scene* s, const double* pos, const double* ori, const double
         if (src[q]) WG_CUDA_TRY(cudaMemcpyAsync(X.dStage + off[q] * na, src[q], sizeof(double) * w[q] * na, cudaMemcpyHostToDevice, S.stream));
     k_put_state<<<(unsigned)((na + 255) / 256), 256, 0, S.stream>>>(S.N, X.dApiMap, na, X.dStage);
     S.fromEnds = false;  // the next step starts from the forces written here
+    if (vel) S.facetsStatic = false;  // facet vertices may have been given a velocity
+    launch_facet_prep(S.stream, S.N, S.P, nullptr);
     WG_CUDA_TRY(cudaGetLastError());
     WG_CUDA_TRY(cudaStreamSynchronize(S.stream));
     return WG_OK;

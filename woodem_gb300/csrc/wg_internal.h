@@ -191,7 +191,8 @@ struct DevPackedSS {
 // Step-loop flag words (device int[3]).
 enum { FL_FULL = 0,   // set by Leapfrog: a node moved farther than verletDist, a full collider run is due
        FL_ERR = 1,    // error code raised by a kernel
-       FL_HALT = 2 }; // set by the contact kernel of a step that found FL_FULL: later queued steps do nothing
+       FL_HALT = 2,   // set by the contact kernel of a step that found FL_FULL: later queued steps do nothing
+       FL_TICKET = 3 }; // blocks of the last contact kernel of a step that have finished (the last advances the step)
 
 __host__ __device__ inline int32_t packCellDist(int a, int b, int c) {
     return (int32_t)(((uint32_t)(a + 512) & 1023u) | (((uint32_t)(b + 512) & 1023u) << 10) | (((uint32_t)(c + 512) & 1023u) << 20));
@@ -233,16 +234,19 @@ struct SideStream {
     cudaStream_t st = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;
 };
-void launch_contact_fp32(cudaStream_t st, const SideStream& side, const DevNodes& N, const DevParticles& P, const DevContacts& C,
+// Returns true when the sphere-sphere kernel, last of the step, also advanced the step counter.
+bool launch_contact_fp32(cudaStream_t st, const SideStream& side, const DevNodes& N, const DevParticles& P, const DevContacts& C,
                          const DevIncidence& I, const DevPackedSS& K, const double4_32a* mats, const ScenePar* sp,
-                         const long long* dStep, int* dFlags, int64_t nMixed, bool periodic, bool anyLaw0, int block = 256);
+                         long long* dStep, int* dFlags, int64_t nMixed, bool periodic, bool anyLaw0, bool prepFacets,
+                         int block = 256);
 // copy the packed sphere-sphere state from (pack) / back to (unpack) the contact arrays
 void launch_pack_ss(cudaStream_t st, const DevContacts& C, const DevIncidence& I, const DevParticles& P, const DevPackedSS& K,
                     int64_t nMixed);
 void launch_unpack_ss(cudaStream_t st, const DevContacts& C, const DevIncidence& I, const DevPackedSS& K, int64_t nMixed);
 void launch_forces32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const NodeConst32* nc,
                      const ScenePar* sp, const int* dFlags, bool perStep);
-// FP32-force mode: P.prep from the current vertex positions (before the contact kernels of a step)
+// FP32-force mode: P.prep from the current vertex positions (before the contact kernels of a step;
+// dFlags null: unconditionally)
 void launch_facet_prep(cudaStream_t st, const DevNodes& N, const DevParticles& P, const int* dFlags);
 
 // ------------------------------------------------------------------ broad phase (wg_collide.cu)
@@ -322,6 +326,7 @@ struct Sim {
     int chunkSteps = 32;
     bool useGraph = false;
     bool concurrentContacts = false;  // facet/wall contacts beside, not after, the sphere-sphere ones
+    bool facetsStatic = false;        // every facet vertex is fully blocked and at rest: FacetPrep is made once
     cudaGraphExec_t graphExec = nullptr;
     int64_t graphSteps = 0;  // steps in the captured chunk, 0: none valid
     int64_t graphEpoch = -1; // nFullRuns when it was captured

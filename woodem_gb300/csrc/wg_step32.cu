@@ -649,17 +649,16 @@ __global__ void __launch_bounds__(256, MINB) k_contact_ss32(DevNodes N, DevParti
 template <int MINB>
 __global__ void __launch_bounds__(256, MINB) k_contact_ss32p(DevNodes N, DevParticles P, DevContacts C, DevIncidence I, DevPackedSS K,
                                                              const double4_32a* __restrict__ mats, const ScenePar* __restrict__ spp,
-                                                             const long long* __restrict__ dStep, int* __restrict__ dFlags, int64_t nm,
-                                                             int haltBlock, int loadFt) {
+                                                             long long* __restrict__ dStep, int* __restrict__ dFlags, int64_t nm,
+                                                             int haltBlock, int loadFt, int advance) {
     const long long stepAbs = *dStep;
-    if (dFlags[FL_FULL] || halted(dFlags)) {
+    if (dFlags[FL_FULL] || halted(dFlags)) {  // the same for every thread of the grid
         if (haltBlock && blockIdx.x == 0 && threadIdx.x == 0) dFlags[FL_HALT] = 1;
         return;
     }
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= K.n) return;
-    int4 next = K.item[j];
+    int4 next = j < K.n ? K.item[j] : make_int4(0, 0, 0, 0);
     for (; j < K.n; j += stride) {
         SSIn x;
         x.it = next;
@@ -678,6 +677,17 @@ __global__ void __launch_bounds__(256, MINB) k_contact_ss32p(DevNodes N, DevPart
         x.wza = N.wz[x.it.x];
         x.wzb = N.wz[x.it.y];
         ssContact(x, j, N, P, C, I, K, mats, spp, stepAbs, dFlags, nm);
+    }
+    if (advance) {
+        // the step counter (k_step_advance) advanced by the last block to finish
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            if (atomicAdd(dFlags + FL_TICKET, 1) == (int)gridDim.x - 1) {
+                dFlags[FL_TICKET] = 0;
+                if (!halted(dFlags)) *dStep += 1;
+            }
+        }
     }
 }
 
@@ -725,7 +735,7 @@ void launch_unpack_ss(cudaStream_t st, const DevContacts& C, const DevIncidence&
 // when its record was made keeps it (the record starts as NaN, which equals nothing).
 __global__ void k_facet_prep(DevNodes N, DevParticles P, const int* __restrict__ dFlags) {
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= P.nFacets || halted(dFlags)) return;
+    if (f >= P.nFacets || (dFlags && halted(dFlags))) return;
     const int4 fn = P.aux[P.facetIds[f]];
     const D3 p0 = ld3(N.posr[fn.x]), p1 = ld3(N.posr[fn.y]), p2 = ld3(N.posr[fn.z]);
     {
@@ -1088,21 +1098,25 @@ static int smCount() {
 
 // sphere-sphere range: block > 0 one contact per thread with that many threads per block;
 // block < 0 the resident-grid kernel with prefetch (256 threads per block)
-static void launchSS(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C, const DevIncidence& I,
-                     const DevPackedSS& K, const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dFlags, int64_t nm,
-                     int halt, int loadFt, int block) {
+// Returns true when the launch also advances the step counter (advance requested and possible).
+static bool launchSS(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C, const DevIncidence& I,
+                     const DevPackedSS& K, const double4_32a* mats, const ScenePar* sp, long long* dStep, int* dFlags, int64_t nm,
+                     int halt, int loadFt, int block, bool advance) {
     if (block < 0) {
         const int64_t g = std::min<int64_t>((K.n + 255) / 256, (int64_t)kSSMinBlocks * smCount());
-        k_contact_ss32p<kSSMinBlocks><<<(unsigned)g, 256, 0, st>>>(N, P, C, I, K, mats, sp, dStep, dFlags, nm, halt, loadFt);
-        return;
+        k_contact_ss32p<kSSMinBlocks><<<(unsigned)g, 256, 0, st>>>(N, P, C, I, K, mats, sp, dStep, dFlags, nm, halt, loadFt,
+                                                                   advance ? 1 : 0);
+        return advance;
     }
     k_contact_ss32<kSSMinBlocks><<<(unsigned)((K.n + block - 1) / block), (unsigned)block, 0, st>>>(N, P, C, I, K, mats, sp, dStep,
                                                                                                  dFlags, nm, halt, loadFt);
+    return false;
 }
 
-void launch_contact_fp32(cudaStream_t st, const SideStream& side, const DevNodes& N, const DevParticles& P, const DevContacts& C,
+bool launch_contact_fp32(cudaStream_t st, const SideStream& side, const DevNodes& N, const DevParticles& P, const DevContacts& C,
                          const DevIncidence& I, const DevPackedSS& K, const double4_32a* mats, const ScenePar* sp,
-                         const long long* dStep, int* dFlags, int64_t nMixed, bool periodic, bool anyLaw0, int block) {
+                         long long* dStep, int* dFlags, int64_t nMixed, bool periodic, bool anyLaw0, bool prepFacets,
+                         int block) {
     const int64_t nm = periodic ? I.nAct : std::min<int64_t>(nMixed, I.nAct);
     const int64_t ns = periodic ? 0 : K.n;
     if (ns > 0 && nm > 0 && side.st) {
@@ -1110,21 +1124,21 @@ void launch_contact_fp32(cudaStream_t st, const SideStream& side, const DevNodes
         // sphere-sphere launch raises FL_HALT when a full run is due
         cudaEventRecord(side.fork, st);
         cudaStreamWaitEvent(side.st, side.fork, 0);
-        launch_facet_prep(side.st, N, P, dFlags);
+        if (prepFacets) launch_facet_prep(side.st, N, P, dFlags);
         // one block of 128 threads per SM: two blocks of the sphere-sphere kernel still fit beside it
         k_contact_fp32<false><<<(unsigned)std::min<int64_t>((nm + 127) / 128, smCount()), 128, 0, side.st>>>(N, P, C, I, mats, sp, dStep,
                                                                                                             dFlags, 0, nm, 0);
-        launchSS(st, N, P, C, I, K, mats, sp, dStep, dFlags, nm, 1, anyLaw0, block);
+        launchSS(st, N, P, C, I, K, mats, sp, dStep, dFlags, nm, 1, anyLaw0, block, false);
         cudaEventRecord(side.join, side.st);
         cudaStreamWaitEvent(st, side.join, 0);
-        return;
+        return false;
     }
     // the first launch also raises FL_HALT when a full run is due (it always runs)
-    if (nm > 0) launch_facet_prep(st, N, P, dFlags);
+    if (nm > 0 && prepFacets) launch_facet_prep(st, N, P, dFlags);
     const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((nm + 127) / 128, 4 * smCount()));
     if (periodic) k_contact_fp32<true><<<g, 128, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags, 0, nm, 1);
     else k_contact_fp32<false><<<g, 128, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags, 0, nm, 1);
-    if (ns > 0) launchSS(st, N, P, C, I, K, mats, sp, dStep, dFlags, nm, 0, anyLaw0, block);
+    return ns > 0 && launchSS(st, N, P, C, I, K, mats, sp, dStep, dFlags, nm, 0, anyLaw0, block, true);
 }
 
 // ---------------------------------------------------------------------------------- force sum
