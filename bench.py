@@ -238,15 +238,22 @@ def cpu_sample(args, seconds, threads):
     return n * steps / el, steps, n, el
 
 
+# the kernels behind each roofline entry (the contact loop of the FP32-force mode is the facet/wall
+# kernel followed by the sphere-sphere kernel, timed together by the phase events)
+KERNELS = {"contact_loop": "k_contact_fp32 (facets, walls) + k_contact_ss32p (sphere-sphere)", "k_contact_fp64": "k_contact_fp64",
+           "k_leapfrog32": "k_leapfrog32", "k_leapfrog": "k_leapfrog"}
+
+
 def traffic_per_launch(kern, R, P, nF, n):
-    """DRAM bytes (read + write) per launch of the kernel, from the committed ncu capture summary
-    (bytes per unit of that capture scaled to this launch's units), or None."""
+    """DRAM bytes (read + write) per launch of the kernel (or per contact loop), from the committed
+    ncu capture summary: bytes per unit of that capture scaled to this launch's units, or None."""
     try:
         with open(os.path.join(HERE, "profiles", "dram_per_unit.json")) as f:
             d = json.load(f)[kern]
     except Exception:
         return None
-    return d.get("per_real", 0.0) * R + d.get("per_potential", 0.0) * (P - R) + d.get("per_sphere", 0.0) * n
+    return (d.get("per_real", 0.0) * R + d.get("per_potential", 0.0) * P + d.get("per_sphere", 0.0) * n +
+            d.get("per_facet", 0.0) * nF)
 
 
 def measure_batch(args):
@@ -467,14 +474,14 @@ def main():
     step_bytes = leapfrog_bytes + contact_bytes + coll_bytes
     ph = [x / args.steps for x in res["phases"]]
     if ph[1] >= ph[0]:
-        kern, kbytes, kern_ms = "k_contact_%s" % args.precision, contact_bytes, ph[1]
+        kern, kbytes, kern_ms = ("contact_loop" if args.precision == "fp32" else "k_contact_fp64"), contact_bytes, ph[1]
     else:
         kern, kbytes, kern_ms = "k_leapfrog%s" % ("32" if args.precision == "fp32" else ""), leapfrog_bytes, ph[0]
     achieved = kbytes / (kern_ms / 1e3) / 1e9 if kern_ms > 0 else 0.0
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if args.precision == "fp64" else "f32+f64", "data": "synthetic", "config": cfg,
-            "roofline": {"bound": "hbm", "kernel": kern, "achieved": achieved, "peak": hbm,
+            "roofline": {"bound": "hbm", "kernel": kern, "kernels": KERNELS.get(kern, kern), "achieved": achieved, "peak": hbm,
                          "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic_per_launch(kern, R, P, nF, res["n_spheres"]),
                          "peak_source": src, "bytes_per_launch": kbytes, "launch_ms": kern_ms},
             "step": {"contacts": P, "real": R, "real_per_sphere": R / n_sph, "full_runs": nfull,
