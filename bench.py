@@ -145,7 +145,7 @@ def measure_gpu(args, rank, world, S=None, prec=None, e2e=True):
     L, h = sim.H.L, sim.H.h
     from woodem_gb300 import tune
     tune.set_launch(sim, args.contact_block if (prec or args.precision) == "fp32" else 0, args.chunk_steps, False,
-                    args.concurrent_contacts)
+                    not args.serial_contacts)
     S.run(3)
     st0 = sim.stats()
     log("[rank %d] warmup %d steps done in %.1fs: %d contacts (%d real), %d full runs" %
@@ -404,8 +404,8 @@ def main():
                     help="launch shape of the contact kernels (wg_set_launch): 128/256 one contact per thread, "
                          "-256 the resident-grid FP32 sphere-sphere kernel with prefetch")
     ap.add_argument("--chunk-steps", type=int, default=32, help="steps queued per host check of the collider request")
-    ap.add_argument("--concurrent-contacts", action="store_true",
-                    help="facet/wall contacts beside the sphere-sphere ones on a second stream (default: after them)")
+    ap.add_argument("--serial-contacts", action="store_true",
+                    help="facet/wall contacts before the sphere-sphere ones (default: beside them on a second stream)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = env_rank()

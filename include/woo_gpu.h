@@ -115,11 +115,11 @@ int wg_set_scenes(wg_scene* s, int32_t n_scenes, const wg_config* cfgs, const in
    (0 = default, 64, 128, 256; -256: the FP32 sphere-sphere contacts through a resident grid whose
    threads prefetch their next contact), steps
    queued per host check of the collider request (1..1024), and flags: WG_LAUNCH_GRAPH replays each
-   such chunk of steps as one CUDA graph, WG_LAUNCH_CONCURRENT runs the facet/wall contacts beside
-   the sphere-sphere ones on a second stream instead of after them. Results do not depend on these;
+   such chunk of steps as one CUDA graph, WG_LAUNCH_SERIAL runs the facet/wall contacts before the
+   sphere-sphere ones instead of beside them on a second stream. Results do not depend on these;
    only the speed does. */
 #define WG_LAUNCH_GRAPH 1
-#define WG_LAUNCH_CONCURRENT 2
+#define WG_LAUNCH_SERIAL 2
 int wg_set_launch(wg_scene* s, int32_t contact_block, int32_t chunk_steps, int32_t launch_flags);
 /* Serving slots (no counterpart in the reference): the scenes of a batch (wg_set_scenes) are slots
    whose particle ranges bound the jobs they can hold. wg_slot_load puts a job (an aperiodic scene

@@ -1190,9 +1190,9 @@ int wg_set_launch(wg_scene* s, int32_t contact_block, int32_t chunk_steps, int32
     if (chunk_steps < 1 || chunk_steps > 1024) return S.fail(WG_ERR_ARG, "chunk_steps must be in [1, 1024]");
     S.contactBlock = contact_block;
     S.chunkSteps = chunk_steps;
-    if (launch_flags & ~(WG_LAUNCH_GRAPH | WG_LAUNCH_CONCURRENT)) return S.fail(WG_ERR_ARG, "unknown launch flag");
+    if (launch_flags & ~(WG_LAUNCH_GRAPH | WG_LAUNCH_SERIAL)) return S.fail(WG_ERR_ARG, "unknown launch flag");
     S.useGraph = (launch_flags & WG_LAUNCH_GRAPH) != 0;
-    S.concurrentContacts = (launch_flags & WG_LAUNCH_CONCURRENT) != 0;
+    S.concurrentContacts = (launch_flags & WG_LAUNCH_SERIAL) == 0;
     return WG_OK;
 }
 

@@ -325,7 +325,7 @@ struct Sim {
     int contactBlock = 0;    // 0: default (FP32: the resident-grid sphere-sphere kernel; FP64: 128)
     int chunkSteps = 32;
     bool useGraph = false;
-    bool concurrentContacts = false;  // facet/wall contacts beside, not after, the sphere-sphere ones
+    bool concurrentContacts = true;   // facet/wall contacts beside, not before, the sphere-sphere ones
     bool facetsStatic = false;        // every facet vertex is fully blocked and at rest: FacetPrep is made once
     cudaGraphExec_t graphExec = nullptr;
     int64_t graphSteps = 0;  // steps in the captured chunk, 0: none valid

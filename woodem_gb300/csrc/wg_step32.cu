@@ -460,6 +460,21 @@ struct SSIn {
     float wza, wzb;
 };
 
+// k_step_advance folded into the last kernel(s) of a step: every block of the `total` blocks of
+// those kernels calls this at its end; the last one to finish advances the step counter (unless
+// the queued steps were halted) and resets the ticket. total <= 0: nothing.
+__device__ __forceinline__ void stepTicket(int* dFlags, long long* dStep, int total) {
+    if (total <= 0) return;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(dFlags + FL_TICKET, 1) == total - 1) {
+            dFlags[FL_TICKET] = 0;
+            if (!halted(dFlags)) *dStep += 1;
+        }
+    }
+}
+
 // One sphere-sphere contact of an aperiodic scene (packed position j): Cg2_Sphere_Sphere_L6Geom,
 // Cp2 on creation, Law2, the two end slots and the packed state. FP32 arithmetic throughout
 // except the IdealElPl shear accumulation (FP64) and contact creation.
@@ -650,7 +665,7 @@ template <int MINB>
 __global__ void __launch_bounds__(256, MINB) k_contact_ss32p(DevNodes N, DevParticles P, DevContacts C, DevIncidence I, DevPackedSS K,
                                                              const double4_32a* __restrict__ mats, const ScenePar* __restrict__ spp,
                                                              long long* __restrict__ dStep, int* __restrict__ dFlags, int64_t nm,
-                                                             int haltBlock, int loadFt, int advance) {
+                                                             int haltBlock, int loadFt, int ticketTotal) {
     const long long stepAbs = *dStep;
     if (dFlags[FL_FULL] || halted(dFlags)) {  // the same for every thread of the grid
         if (haltBlock && blockIdx.x == 0 && threadIdx.x == 0) dFlags[FL_HALT] = 1;
@@ -678,17 +693,7 @@ __global__ void __launch_bounds__(256, MINB) k_contact_ss32p(DevNodes N, DevPart
         x.wzb = N.wz[x.it.y];
         ssContact(x, j, N, P, C, I, K, mats, spp, stepAbs, dFlags, nm);
     }
-    if (advance) {
-        // the step counter (k_step_advance) advanced by the last block to finish
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            __threadfence();
-            if (atomicAdd(dFlags + FL_TICKET, 1) == (int)gridDim.x - 1) {
-                dFlags[FL_TICKET] = 0;
-                if (!halted(dFlags)) *dStep += 1;
-            }
-        }
-    }
+    stepTicket(dFlags, dStep, ticketTotal);
 }
 
 __global__ void k_pack_ss(DevContacts C, DevIncidence I, DevParticles P, DevPackedSS K, int64_t nm, int copyFt) {
@@ -1071,15 +1076,16 @@ __device__ __forceinline__ void mixedContact(int64_t rk, const DevNodes& N, cons
 template <bool PERI>
 __global__ void __launch_bounds__(128, 4) k_contact_fp32(DevNodes N, DevParticles P, DevContacts C, DevIncidence I,
                                                        const double4_32a* __restrict__ mats, const ScenePar* __restrict__ spp,
-                                                       const long long* __restrict__ dStep, int* __restrict__ dFlags, int64_t c0,
-                                                       int64_t c1, int haltBlock) {
-    if (dFlags[FL_FULL] || halted(dFlags)) {
+                                                       long long* __restrict__ dStep, int* __restrict__ dFlags, int64_t c0,
+                                                       int64_t c1, int haltBlock, int ticketTotal) {
+    if (dFlags[FL_FULL] || halted(dFlags)) {  // the same for every thread of the grid
         if (haltBlock && blockIdx.x == 0 && threadIdx.x == 0) dFlags[FL_HALT] = 1;
         return;
     }
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t rk = c0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; rk < c1; rk += stride)
         mixedContact<PERI>(rk, N, P, C, I, mats, spp, dStep, dFlags);
+    stepTicket(dFlags, dStep, ticketTotal);
 }
 
 // minimum resident blocks per SM the one-contact-per-thread kernel is compiled for (register budget)
@@ -1099,18 +1105,20 @@ static int smCount() {
 // sphere-sphere range: block > 0 one contact per thread with that many threads per block;
 // block < 0 the resident-grid kernel with prefetch (256 threads per block)
 // Returns true when the launch also advances the step counter (advance requested and possible).
-static bool launchSS(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C, const DevIncidence& I,
+// grid of the resident sphere-sphere kernel (block < 0), or 0 for the one-contact-per-thread kernel
+static int ssGrid(const DevPackedSS& K, int block, int blocksPerSM) {
+    return block < 0 ? (int)std::min<int64_t>((K.n + 255) / 256, (int64_t)blocksPerSM * smCount()) : 0;
+}
+static void launchSS(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C, const DevIncidence& I,
                      const DevPackedSS& K, const double4_32a* mats, const ScenePar* sp, long long* dStep, int* dFlags, int64_t nm,
-                     int halt, int loadFt, int block, bool advance) {
+                     int halt, int loadFt, int block, int grid, int ticketTotal) {
     if (block < 0) {
-        const int64_t g = std::min<int64_t>((K.n + 255) / 256, (int64_t)kSSMinBlocks * smCount());
-        k_contact_ss32p<kSSMinBlocks><<<(unsigned)g, 256, 0, st>>>(N, P, C, I, K, mats, sp, dStep, dFlags, nm, halt, loadFt,
-                                                                   advance ? 1 : 0);
-        return advance;
+        k_contact_ss32p<kSSMinBlocks><<<(unsigned)grid, 256, 0, st>>>(N, P, C, I, K, mats, sp, dStep, dFlags, nm, halt, loadFt,
+                                                                      ticketTotal);
+        return;
     }
     k_contact_ss32<kSSMinBlocks><<<(unsigned)((K.n + block - 1) / block), (unsigned)block, 0, st>>>(N, P, C, I, K, mats, sp, dStep,
                                                                                                  dFlags, nm, halt, loadFt);
-    return false;
 }
 
 bool launch_contact_fp32(cudaStream_t st, const SideStream& side, const DevNodes& N, const DevParticles& P, const DevContacts& C,
@@ -1120,25 +1128,32 @@ bool launch_contact_fp32(cudaStream_t st, const SideStream& side, const DevNodes
     const int64_t nm = periodic ? I.nAct : std::min<int64_t>(nMixed, I.nAct);
     const int64_t ns = periodic ? 0 : K.n;
     if (ns > 0 && nm > 0 && side.st) {
-        // the mixed range (facets and walls, FP64 geometry) beside the sphere-sphere range; the
-        // sphere-sphere launch raises FL_HALT when a full run is due
+        // the mixed range (facets and walls, FP64 geometry) beside the sphere-sphere range: one block
+        // of 128 threads per SM, and two resident sphere-sphere blocks per SM beside it; the
+        // sphere-sphere launch raises FL_HALT when a full run is due; the last block of either
+        // advances the step counter
+        const int gM = (int)std::min<int64_t>((nm + 127) / 128, smCount());
+        const int gS = ssGrid(K, block, kSSMinBlocks - 1);
+        const int total = gS > 0 ? gM + gS : 0;
         cudaEventRecord(side.fork, st);
         cudaStreamWaitEvent(side.st, side.fork, 0);
         if (prepFacets) launch_facet_prep(side.st, N, P, dFlags);
-        // one block of 128 threads per SM: two blocks of the sphere-sphere kernel still fit beside it
-        k_contact_fp32<false><<<(unsigned)std::min<int64_t>((nm + 127) / 128, smCount()), 128, 0, side.st>>>(N, P, C, I, mats, sp, dStep,
-                                                                                                            dFlags, 0, nm, 0);
-        launchSS(st, N, P, C, I, K, mats, sp, dStep, dFlags, nm, 1, anyLaw0, block, false);
+        k_contact_fp32<false><<<(unsigned)gM, 128, 0, side.st>>>(N, P, C, I, mats, sp, dStep, dFlags, 0, nm, 0, total);
+        launchSS(st, N, P, C, I, K, mats, sp, dStep, dFlags, nm, 1, anyLaw0, block, gS, total);
         cudaEventRecord(side.join, side.st);
         cudaStreamWaitEvent(st, side.join, 0);
-        return false;
+        return total > 0;
     }
-    // the first launch also raises FL_HALT when a full run is due (it always runs)
+    // the first launch also raises FL_HALT when a full run is due (it always runs); the last
+    // kernel of the step advances the step counter
     if (nm > 0 && prepFacets) launch_facet_prep(st, N, P, dFlags);
-    const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((nm + 127) / 128, 4 * smCount()));
-    if (periodic) k_contact_fp32<true><<<g, 128, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags, 0, nm, 1);
-    else k_contact_fp32<false><<<g, 128, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags, 0, nm, 1);
-    return ns > 0 && launchSS(st, N, P, C, I, K, mats, sp, dStep, dFlags, nm, 0, anyLaw0, block, true);
+    const int gS = ns > 0 ? ssGrid(K, block, kSSMinBlocks) : 0;
+    const int gM = (int)std::max<int64_t>(1, std::min<int64_t>((nm + 127) / 128, 4 * smCount()));
+    const int totalM = ns > 0 ? 0 : gM;
+    if (periodic) k_contact_fp32<true><<<(unsigned)gM, 128, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags, 0, nm, 1, totalM);
+    else k_contact_fp32<false><<<(unsigned)gM, 128, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags, 0, nm, 1, totalM);
+    if (ns > 0) launchSS(st, N, P, C, I, K, mats, sp, dStep, dFlags, nm, 0, anyLaw0, block, gS, gS);
+    return totalM > 0 || gS > 0;
 }
 
 // ---------------------------------------------------------------------------------- force sum

@@ -14,14 +14,14 @@ DEFAULT_CANDIDATES = (
     # (contact threads per block, steps per chunk, CUDA graph, facet/wall contacts on a second
     # stream beside the sphere-sphere ones); block -256 selects the resident-grid FP32
     # sphere-sphere kernel whose threads prefetch their next contact
-    (256, 32, False, False),
-    (256, 32, False, True),
-    (128, 32, False, False),
+    (-256, 32, False, True),
     (-256, 32, False, False),
-    (256, 8, True, False),
-    (256, 32, True, False),
-    (256, 32, True, True),
-    (256, 64, True, False),
+    (256, 32, False, True),
+    (128, 32, False, True),
+    (-256, 8, True, True),
+    (-256, 32, True, True),
+    (-256, 32, True, False),
+    (-256, 64, True, True),
 )
 
 
@@ -29,9 +29,9 @@ def _handle(sim):
     return sim.H.L, sim.H.h
 
 
-def set_launch(sim, block=0, chunk=32, graph=False, concurrent=False):
+def set_launch(sim, block=0, chunk=32, graph=False, concurrent=True):
     L, h = _handle(sim)
-    sim.H.check(L.wg_set_launch(h, int(block), int(chunk), (1 if graph else 0) | (2 if concurrent else 0)), "set_launch")
+    sim.H.check(L.wg_set_launch(h, int(block), int(chunk), (1 if graph else 0) | (0 if concurrent else 2)), "set_launch")
 
 
 def _run_ms(sim, steps):
