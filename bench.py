@@ -206,13 +206,22 @@ def barrier(world):
 
 
 def allreduce_max(x, world):
+    """The maximum of x over the ranks (a CUDA tensor under NCCL, a CPU tensor under gloo)."""
     if world == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_rate(units_per_rank, ms_local, world):
+    """Whole-job rate of `world` replicas that each processed units_per_rank units in ms_local ms:
+    the units of all ranks over the slowest rank's time (weak scaling). Every rank must call it."""
+    ms = allreduce_max(ms_local, world)
+    return world * units_per_rank / (ms / 1e3), ms
 
 
 def cpu_sample(args, seconds, threads):
@@ -458,10 +467,9 @@ def main():
         other = measure_gpu(args, rank, world, S=S, prec=oprec, e2e=False)
         other["prec"] = oprec
     S.close()
-    ms = allreduce_max(res["ms"], world)
-    st0, st1 = res["st0"], res["st1"]
     n_sph = res["n_spheres"]
-    value = world * n_sph * args.steps / (ms / 1e3)
+    value, ms = replica_rate(n_sph * args.steps, res["ms"], world)
+    st0, st1 = res["st0"], res["st1"]
     hbm, src = peaks()
     R = 0.5 * (st0.n_real + st1.n_real)
     P = 0.5 * (st0.n_contacts + st1.n_contacts)
@@ -492,17 +500,17 @@ def main():
     if "bed" in res:
         cfg["bed"] = res["bed"]
     if other is not None:
-        oms = allreduce_max(other["ms"], world)
+        ovalue, oms = replica_rate(n_sph * args.steps, other["ms"], world)
         ost0, ost1 = other["st0"], other["st1"]
         oph = [x / args.steps for x in other["phases"]]
-        line["other_precision"] = {"precision": other["prec"], "value": world * n_sph * args.steps / (oms / 1e3),
+        line["other_precision"] = {"precision": other["prec"], "value": ovalue,
                                    "ms_per_step": oms / args.steps,
                                    "phase_ms": {"leapfrog": oph[0], "contact": oph[1], "collider": oph[3]},
                                    "real": 0.5 * (ost0.n_real + ost1.n_real), "contacts": 0.5 * (ost0.n_contacts + ost1.n_contacts)}
     if "e2e" in res:
         e = res["e2e"]
-        es = allreduce_max(e["seconds"], world)
-        line["e2e"] = {"value": world * n_sph * e["steps"] / es, "unit": UNIT, "h2d_bytes_per_step": e["h2d"],
+        evalue, _ = replica_rate(n_sph * e["steps"], e["seconds"] * 1e3, world)
+        line["e2e"] = {"value": evalue, "unit": UNIT, "h2d_bytes_per_step": e["h2d"],
                        "d2h_bytes_per_step": e["d2h"], "steps": e["steps"],
                        "call": "wg_run_host(1 step) with page-locked host state"}
     if rank == 0 and not args.no_batch:
