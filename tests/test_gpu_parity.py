@@ -153,9 +153,10 @@ def test_errors_are_raised(gpu_lib):
 def test_call_granularity_is_invisible(prec):
     """The step loop queues steps in chunks and resumes after each collider run; running 400 steps
     in one call, in calls of 1 and 37 steps, or one step at a time through wg_run_host (state
-    copied out and back in every step) gives bitwise the same state."""
+    copied out and back in every step, from pageable or page-locked arrays) gives bitwise the
+    same state."""
     out = []
-    for mode in ("one", "steps", "host"):
+    for mode in ("one", "steps", "host", "pinned"):
         S = scenes.box_settle_small(n=1200, seed=5, precision=prec)
         if mode == "one":
             S.run(400)
@@ -170,16 +171,28 @@ def test_call_granularity_is_invisible(prec):
             sim = S._sim
             L, h = sim.H.L, sim.H.h
             na = sim.A.n_nodes
-            parts = [np.zeros(w * na) for w in (3, 4, 3, 3, 3, 3)]
+            pinned = None
+            if mode == "host":  # pageable arrays: staged copies
+                parts = [np.zeros(w * na) for w in (3, 4, 3, 3, 3, 3)]
+            else:  # page-locked arrays (wg_host_alloc)
+                import ctypes
+                pinned = L.wg_host_alloc(19 * 8 * na)
+                assert pinned
+                buf = np.ctypeslib.as_array((ctypes.c_double * (19 * na)).from_address(pinned))
+                cuts = np.cumsum([0, 3, 4, 3, 3, 3, 3]) * na
+                parts = [buf[cuts[q]:cuts[q + 1]] for q in range(6)]
             sim.H.check(L.wg_get_nodes(h, *[_native.ptr(x) for x in parts]), "get_nodes")
             for _ in range(399):
                 sim.H.check(L.wg_run_host(h, 1, *[_native.ptr(x) for x in parts]), "run_host")
+            if pinned:
+                L.wg_host_free(pinned)
         g = _gpu_nodes(S)
         S.close()
         out.append(g)
     for k in ("pos", "vel", "angVel", "force", "torque"):
         assert np.array_equal(out[0][k], out[1][k]), "%s: one call vs many" % k
         assert np.array_equal(out[0][k], out[2][k]), "%s: one call vs host round trips" % k
+        assert np.array_equal(out[0][k], out[3][k]), "%s: one call vs round trips through page-locked arrays" % k
 
 
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])

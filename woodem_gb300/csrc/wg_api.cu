@@ -143,17 +143,25 @@ struct SimEx : Sim {
     std::vector<int32_t> hApiMap;
 };
 
-__global__ void k_put_state(DevNodes N, const int32_t* __restrict__ map, int64_t na, const double* __restrict__ st) {
+// The six per-node arrays of wg_put_state / wg_get_nodes in the device staging buffer (pos 3,
+// ori 4, vel 3, angVel 3, force 3, torque 3 doubles per API node).
+struct StateArrays {
+    double *pos, *ori, *vel, *av, *f, *t;
+};
+__host__ __device__ inline StateArrays stagedArrays(double* st, int64_t na) {
+    return StateArrays{st, st + 3 * na, st + 7 * na, st + 10 * na, st + 13 * na, st + 16 * na};
+}
+__global__ void k_put_state(DevNodes N, const int32_t* __restrict__ map, int64_t na, StateArrays A) {
     const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= na) return;
     const int s = map[a];
     if (s < 0) return;
-    const double* pos = st;
-    const double* ori = st + 3 * na;
-    const double* vel = st + 7 * na;
-    const double* av = st + 10 * na;
-    const double* f = st + 13 * na;
-    const double* t = st + 16 * na;
+    const double* pos = A.pos;
+    const double* ori = A.ori;
+    const double* vel = A.vel;
+    const double* av = A.av;
+    const double* f = A.f;
+    const double* t = A.t;
     const double r = N.posr[s].w;
     N.posr[s] = make_double4_32a(pos[3 * a], pos[3 * a + 1], pos[3 * a + 2], r);
     N.ori[s] = make_double4_32a(ori[4 * a], ori[4 * a + 1], ori[4 * a + 2], ori[4 * a + 3]);
@@ -189,17 +197,17 @@ __global__ void k_put_state(DevNodes N, const int32_t* __restrict__ map, int64_t
     N.force[s] = make_double4_32a(f[3 * a], f[3 * a + 1], f[3 * a + 2], 0.);
     N.torque[s] = make_double4_32a(t[3 * a], t[3 * a + 1], t[3 * a + 2], 0.);
 }
-__global__ void k_get_state(DevNodes N, const int32_t* __restrict__ map, int64_t na, double* __restrict__ st) {
+__global__ void k_get_state(DevNodes N, const int32_t* __restrict__ map, int64_t na, StateArrays A) {
     const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= na) return;
     const int s = map[a];
     if (s < 0) return;
-    double* pos = st;
-    double* ori = st + 3 * na;
-    double* vel = st + 7 * na;
-    double* av = st + 10 * na;
-    double* f = st + 13 * na;
-    double* t = st + 16 * na;
+    double* pos = A.pos;
+    double* ori = A.ori;
+    double* vel = A.vel;
+    double* av = A.av;
+    double* f = A.f;
+    double* t = A.t;
     const double4_32a p = N.posr[s], v = N.vel[s], w = N.angv[s], ff = N.force[s], tt = N.torque[s];
     double4_32a o;
     if (N.orif) {
@@ -1317,13 +1325,16 @@ int wg_put_state(wg_scene* s, const double* pos, const double* ori, const double
     const int64_t na = S.nApiNodes;
     const double* src[6] = {pos, ori, vel, ang_vel, force, torque};
     const int64_t off[6] = {0, 3, 7, 10, 13, 16}, w[6] = {3, 4, 3, 3, 3, 3};
-    // fill missing components from the current device state
+    // staged: one copy per array (the copy engines move page-locked arrays faster than kernels
+    // reading host memory directly), then the conversion into the node slots
     if (!(pos && ori && vel && ang_vel && force && torque)) {
-        k_get_state<<<(unsigned)((na + 255) / 256), 256, 0, S.stream>>>(S.N, X.dApiMap, na, X.dStage);
+        // fill missing components from the current device state
+        k_get_state<<<(unsigned)((na + 255) / 256), 256, 0, S.stream>>>(S.N, X.dApiMap, na, stagedArrays(X.dStage, na));
     }
     for (int q = 0; q < 6; q++)
-        if (src[q]) WG_CUDA_TRY(cudaMemcpyAsync(X.dStage + off[q] * na, src[q], sizeof(double) * w[q] * na, cudaMemcpyHostToDevice, S.stream));
-    k_put_state<<<(unsigned)((na + 255) / 256), 256, 0, S.stream>>>(S.N, X.dApiMap, na, X.dStage);
+        if (src[q])
+            WG_CUDA_TRY(cudaMemcpyAsync(X.dStage + off[q] * na, src[q], sizeof(double) * w[q] * na, cudaMemcpyHostToDevice, S.stream));
+    k_put_state<<<(unsigned)((na + 255) / 256), 256, 0, S.stream>>>(S.N, X.dApiMap, na, stagedArrays(X.dStage, na));
     S.fromEnds = false;  // the next step starts from the forces written here
     if (vel) S.facetsStatic = false;  // facet vertices may have been given a velocity
     launch_facet_prep(S.stream, S.N, S.P, nullptr);
@@ -1344,7 +1355,7 @@ int wg_get_nodes(wg_scene* s, double* pos, double* ori, double* vel, double* ang
             if (dst[q]) std::memcpy(dst[q], S.hApi.data() + off[q] * na, sizeof(double) * w[q] * na);
         return WG_OK;
     }
-    k_get_state<<<(unsigned)((na + 255) / 256), 256, 0, S.stream>>>(S.N, X.dApiMap, na, X.dStage);
+    k_get_state<<<(unsigned)((na + 255) / 256), 256, 0, S.stream>>>(S.N, X.dApiMap, na, stagedArrays(X.dStage, na));
     for (int q = 0; q < 6; q++)
         if (dst[q]) WG_CUDA_TRY(cudaMemcpyAsync(dst[q], X.dStage + off[q] * na, sizeof(double) * w[q] * na, cudaMemcpyDeviceToHost, S.stream));
     WG_CUDA_TRY(cudaGetLastError());
