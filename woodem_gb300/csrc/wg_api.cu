@@ -708,7 +708,22 @@ int Sim::run(int64_t n) {
     int64_t launches = 0;
     bool anyZeroVd = hPar.verletDist == 0;
     for (const ScenePar& q : hPars) anyZeroVd = anyZeroVd || q.verletDist == 0;
-    const int64_t maxChunk = (cfg.periodic || anyZeroVd) ? 1 : std::max<int64_t>(1, std::min<int64_t>(chunkSteps, 1024));
+    const int64_t maxChunk = anyZeroVd ? 1 : std::max<int64_t>(1, std::min<int64_t>(chunkSteps, 1024));
+    // periodic cells: the cell of each queued step is integrated on the host ahead of the chunk (it
+    // depends on the velocity gradient only) and its parameters uploaded as one record per step
+    std::vector<HostCell> cellInt, cellEnd;
+    std::vector<ScenePar> parSeq;
+    if (cfg.periodic) {
+        if (parSeqCap < maxChunk) {
+            if (dParSeq) dfree(dParSeq);
+            dParSeq = (ScenePar*)dalloc(sizeof(ScenePar) * maxChunk);
+            if (!dParSeq) return fail(WG_ERR_CUDA, "out of device memory (cell parameters)");
+            parSeqCap = maxChunk;
+        }
+        cellInt.resize(maxChunk);
+        cellEnd.resize(maxChunk);
+        parSeq.resize(maxChunk);
+    }
     if ((int64_t)evPool.size() < 3 * maxChunk + 2) {
         for (int64_t q = (int64_t)evPool.size(); q < 3 * maxChunk + 2; q++) {
             cudaEvent_t e;
@@ -721,22 +736,22 @@ int Sim::run(int64_t n) {
     const bool fp32 = prec == WG_PREC_FP32;
     bool anyLaw0 = cfg.law == 0;
     for (const wg_config& c : cfgs) anyLaw0 = anyLaw0 || c.law == 0;
-    auto stepLeapfrog = [&](int fromEndsArg) {
+    auto stepLeapfrog = [&](int fromEndsArg, ScenePar* sp) {
         if (fromEndsArg) {
-            if (fp32) launch_forces32(stream, N, P, I, dNodeC, dPar, dFlags, true);
-            else launch_forces(stream, N, P, I, dPar, dFlags, true);
+            if (fp32) launch_forces32(stream, N, P, I, dNodeC, sp, dFlags, true);
+            else launch_forces(stream, N, P, I, sp, dFlags, true);
             launches += I.nHeavyFree > 0;
         }
-        if (fp32) launch_leapfrog32(stream, N, P, I, dNodeC, dPar, dFlags, fromEndsArg, dStep, cfg.periodic != 0);
-        else launch_leapfrog(stream, N, P, I, dPar, dFlags, fromEndsArg, dStep, cfg.periodic != 0);
+        if (fp32) launch_leapfrog32(stream, N, P, I, dNodeC, sp, dFlags, fromEndsArg, dStep, cfg.periodic != 0);
+        else launch_leapfrog(stream, N, P, I, sp, dFlags, fromEndsArg, dStep, cfg.periodic != 0);
         launches++;
     };
-    auto stepContact = [&]() {
+    auto stepContact = [&](ScenePar* sp) {
         bool advanced = false;  // the last contact kernel advanced the step counter itself
         if (fp32)
-            advanced = launch_contact_fp32(stream, concurrentContacts ? side : SideStream{}, N, P, C, I, K, dMats, dPar, dStep, dFlags,
+            advanced = launch_contact_fp32(stream, concurrentContacts ? side : SideStream{}, N, P, C, I, K, dMats, sp, dStep, dFlags,
                                            nMixed, cfg.periodic != 0, anyLaw0, !facetsStatic, contactBlock != 0 ? contactBlock : -256);
-        else launch_contact_fp64(stream, N, P, C, I, dMats, dPar, dStep, dFlags, cfg.periodic != 0,
+        else launch_contact_fp64(stream, N, P, C, I, dMats, sp, dStep, dFlags, cfg.periodic != 0,
                                  (contactBlock > 0 && contactBlock <= 128) ? contactBlock : 128);  // launch bounds 128
         if (!advanced) launch_advance(stream, dStep, dFlags);
         launches += advanced ? 1 : 2;
@@ -751,10 +766,18 @@ int Sim::run(int64_t n) {
         const bool needFull = !initialized || anyZeroVd || forceFull;
         k_set_flags<<<1, 1, 0, stream>>>(dFlags, needFull ? 1 : 0);
         if (cfg.periodic) {
-            X.cell.integrateAndUpdate(cfg.dt);
-            fillCellPar(X);
-            WG_CUDA_TRY(cudaMemcpyAsync(dPar, &hPar, sizeof(ScenePar), cudaMemcpyHostToDevice, stream));
+            // Cell::integrateAndUpdate then setNextGradV for every queued step (Scene::doOneStep)
+            for (int64_t j = 0; j < k; j++) {
+                X.cell.integrateAndUpdate(cfg.dt);
+                fillCellPar(X);
+                parSeq[j] = hPar;
+                cellInt[j] = X.cell;
+                X.cell.setNextGradV();
+                cellEnd[j] = X.cell;
+            }
+            WG_CUDA_TRY(cudaMemcpyAsync(dParSeq, parSeq.data(), sizeof(ScenePar) * k, cudaMemcpyHostToDevice, stream));
         }
+        auto spOf = [&](int64_t j) { return cfg.periodic ? dParSeq + j : dPar; };
         const int64_t s0 = step;
         // a chunk that starts from the end slots and is not due for a full run is replayed as a
         // CUDA graph (re-captured after every full run, whose contact arrays it refers to)
@@ -767,8 +790,8 @@ int Sim::run(int64_t n) {
                 WG_CUDA_TRY(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
                 const int64_t l0 = launches;
                 for (int64_t j = 0; j < k; j++) {
-                    stepLeapfrog(1);
-                    stepContact();
+                    stepLeapfrog(1, dPar);
+                    stepContact(dPar);
                 }
                 graphLaunches = launches - l0;
                 launches = l0;
@@ -785,9 +808,9 @@ int Sim::run(int64_t n) {
         } else {
             for (int64_t j = 0; j < k; j++) {
                 WG_CUDA_TRY(cudaEventRecord(E[3 * j], stream));
-                stepLeapfrog(j == 0 ? (fromEnds ? 1 : 0) : 1);
+                stepLeapfrog(j == 0 ? (fromEnds ? 1 : 0) : 1, spOf(j));
                 WG_CUDA_TRY(cudaEventRecord(E[3 * j + 1], stream));
-                stepContact();
+                stepContact(spOf(j));
                 WG_CUDA_TRY(cudaEventRecord(E[3 * j + 2], stream));
             }
         }
@@ -814,6 +837,12 @@ int Sim::run(int64_t n) {
                 cudaEventElapsedTime(&a, E[3 * ds], E[3 * ds + 1]);
                 ph[0] += a;
             }
+            if (cfg.periodic) {
+                // the cell of step s0+ds, for the collider and that step's contact loop
+                X.cell = cellInt[ds];
+                hPar = parSeq[ds];
+                WG_CUDA_TRY(cudaMemcpyAsync(dPar, &hPar, sizeof(ScenePar), cudaMemcpyHostToDevice, stream));
+            }
             WG_CUDA_TRY(cudaEventRecord(E[3 * maxChunk], stream));
             int r = collide_full_run(*this);
             if (r) return r;
@@ -824,7 +853,7 @@ int Sim::run(int64_t n) {
             k_set_flags<<<1, 1, 0, stream>>>(dFlags, 0);
             if (K.n > 0) packDirty = true;
             WG_CUDA_TRY(cudaEventRecord(E[0], stream));
-            stepContact();
+            stepContact(dPar);
             WG_CUDA_TRY(cudaEventRecord(E[1], stream));
             WG_CUDA_TRY(cudaMemcpyAsync(hFlags, dFlags, sizeof(int) * 4, cudaMemcpyDeviceToHost, stream));
             WG_CUDA_TRY(cudaStreamSynchronize(stream));
@@ -838,7 +867,12 @@ int Sim::run(int64_t n) {
             ds += 1;
         }
         fromEnds = true;
-        if (cfg.periodic) X.cell.setNextGradV();
+        if (cfg.periodic && ds > 0) {
+            // the cell after the last step done; dPar holds that step's parameters (stress, listing)
+            X.cell = cellEnd[ds - 1];
+            hPar = parSeq[ds - 1];
+            WG_CUDA_TRY(cudaMemcpyAsync(dPar, &hPar, sizeof(ScenePar), cudaMemcpyHostToDevice, stream));
+        }
         step += ds;
         time += ds * cfg.dt;
         done += ds;

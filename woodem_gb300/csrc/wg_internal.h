@@ -300,6 +300,8 @@ struct Sim {
     int prec = 0;                  // WG_PREC_*
     ScenePar hPar{};
     ScenePar* dPar = nullptr;  // one per scene
+    ScenePar* dParSeq = nullptr;  // periodic cell: the parameters of each step of a queued chunk
+    int64_t parSeqCap = 0;
     // batch of independent scenes: scene k owns particles [sceneStart[k], sceneStart[k+1])
     int nScenes = 1;
     std::vector<wg_config> cfgs;
