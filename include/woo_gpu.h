@@ -170,6 +170,21 @@ int wg_get_cell(wg_scene* s, double* hsize, double* trsf, double* gradv);
    cell_dist: Contact.cellDist for the (lo,hi) orientation; fglob: force on pA in
    global coordinates; local: phys.force; cpt: geom.node.pos; trsf: L6Geom.trsf. */
 int64_t wg_num_contacts(wg_scene* s);
+/* Contact container snapshot for checkpoint/resume (the reference serializes the
+   ContactContainer with the Scene, lib/object/ObjectIO.hpp:28-90): every contact the collider
+   keeps, in key order, with its key (lo << 32 | hi), flags, creation step, packed cell distance
+   and the persistent state as `wg_contact_state_cols` doubles per contact (row-major; the
+   columns depend on the precision mode). wg_get_contact_state with cap < the count returns
+   WG_ERR_CAPACITY and the count in *n_out. wg_set_contact_state replaces the container of an
+   uploaded (or not yet run) scene; its next step starts with a collider full run, which keeps
+   the state of the real contacts, so a run resumed from wg_put_state + wg_set_contact_state
+   continues as the saved one would have (FP64 mode: bitwise). No counterpart in the reference's
+   C++ interface. */
+int32_t wg_contact_state_cols(wg_scene* s);
+int wg_get_contact_state(wg_scene* s, int64_t cap, int64_t* n_out, uint64_t* key, uint32_t* flags, int32_t* step0, int32_t* cell_dist,
+                         double* cols);
+int wg_set_contact_state(wg_scene* s, int64_t n, const uint64_t* key, const uint32_t* flags, const int32_t* step0,
+                         const int32_t* cell_dist, const double* cols, int32_t ncols);
 int wg_get_contacts(wg_scene* s, int32_t* id_lo, int32_t* id_hi, int32_t* id_a, int32_t* real,
                     int32_t* cell_dist, double* fglob, double* local, double* cpt, double* trsf);
 /* Aabb.min/max per particle from the last full run (verletDist included), 3 doubles each. */

@@ -12,6 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libwoogpu.so")
 
 WG_OK = 0
+WG_ERR_CAPACITY = -5
 ERRORS = {-1: ValueError, -2: RuntimeError, -3: RuntimeError, -4: NotImplementedError, -5: MemoryError, -6: RuntimeError,
           -7: RuntimeError, -8: TimeoutError}
 
@@ -94,6 +95,11 @@ def lib():
         "wg_get_aabbs": (C.c_int, [C.c_void_p, P_D, P_D]),
         "wg_get_timing": (C.c_int, [C.c_void_p, P_D, P_D, P_I64]),
         "wg_profiler": (C.c_int, [C.c_int]),
+        "wg_contact_state_cols": (C.c_int32, [C.c_void_p]),
+        "wg_get_contact_state": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_int64), C.c_void_p, C.c_void_p, C.c_void_p,
+                                          C.c_void_p, C.c_void_p]),
+        "wg_set_contact_state": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                          C.c_int32]),
         "wg_host_alloc": (C.c_void_p, [C.c_int64]),
         "wg_host_free": (None, [C.c_void_p]),
         "wg_broadphase_noalloc": (C.c_int, [C.c_int32, P_D, P_D, P_U32, C.c_uint32, C.c_int64, P_I32, P_I32, P_I64]),

@@ -188,6 +188,7 @@ class Simulation:
 
     def __init__(self, S):
         self.S = S
+        self.t0 = float(S.time)  # Scene.time at upload; the device counts the time run since
         self.A = compile_scene(S)
         self.dirty_structure = False
         self.host_written = False
@@ -241,7 +242,7 @@ class Simulation:
         self._contacts = None
         st = self.stats()
         self.S.step = int(st.step)
-        self.S.time = float(st.time)
+        self.S.time = self.t0 + float(st.time)
         for e in self.S.engines:
             from .dem import InsertionSortCollider
             if isinstance(e, InsertionSortCollider):

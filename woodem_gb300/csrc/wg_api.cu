@@ -1538,6 +1538,126 @@ static int collectContacts(Sim& S, std::vector<int64_t>& keep, std::vector<uint6
     return 0;
 }
 
+// the FP64 columns of the contact state in a snapshot: all in FP64 mode; in FP32-force mode
+// those the mode keeps in FP64 (contact point, IdealElPl shear force), then the FP32 columns
+static std::vector<int> snapshotCols64(const Sim& S) {
+    std::vector<int> q;
+    for (int c = 0; c < CC_NCOL; c++)
+        if (S.C.col[c]) q.push_back(c);
+    return q;
+}
+int32_t wg_contact_state_cols(wg_scene* s) {
+    if (!s) return WG_ERR_ARG;
+    Sim& S = *SIM(s);
+    if (!S.haveCfg) return S.fail(WG_ERR_STATE, "wg_set_config must be called first");
+    if (S.cfg.precision == WG_PREC_FP64) return CC_NCOL;
+    return 5 + CF_NCOL;  // CC_FT1, CC_FT2, CC_CPX, CC_CPY, CC_CPZ and the FP32 columns
+}
+
+int wg_get_contact_state(wg_scene* s, int64_t cap, int64_t* n_out, uint64_t* key, uint32_t* flags, int32_t* step0, int32_t* cell_dist,
+                         double* cols) {
+    if (!s || !n_out) return WG_ERR_ARG;
+    Sim& S = *SIM(s);
+    *n_out = 0;
+    if (!S.uploaded) return WG_OK;
+    int r = S.syncContacts();
+    if (r) return r;
+    WG_CUDA_TRY(cudaSetDevice(S.device));
+    const int64_t n = S.C.n;
+    std::vector<uint64_t> k(n);
+    std::vector<uint32_t> f(n);
+    std::vector<int32_t> s0(n), cd(n);
+    if (n > 0) {
+        WG_CUDA_TRY(cudaMemcpy(k.data(), S.C.key, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost));
+        WG_CUDA_TRY(cudaMemcpy(f.data(), S.C.flags, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
+        WG_CUDA_TRY(cudaMemcpy(s0.data(), S.C.step0, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+        WG_CUDA_TRY(cudaMemcpy(cd.data(), S.C.cdist, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+    }
+    std::vector<int64_t> keep;
+    for (int64_t c = 0; c < n; c++)
+        if (!(f[c] & C_REMOVED)) keep.push_back(c);
+    *n_out = (int64_t)keep.size();
+    if (cap < (int64_t)keep.size()) return keep.empty() ? WG_OK : WG_ERR_CAPACITY;
+    if (keep.empty()) return WG_OK;
+    if (!key || !flags || !step0 || !cell_dist || !cols) return WG_ERR_ARG;
+    const std::vector<int> q64 = snapshotCols64(S);
+    const int ncols = wg_contact_state_cols(s);
+    std::vector<double> v(n);
+    std::vector<float> vf(n);
+    int col = 0;
+    for (int q : q64) {
+        WG_CUDA_TRY(cudaMemcpy(v.data(), S.C.col[q], sizeof(double) * n, cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < keep.size(); i++) cols[(int64_t)i * ncols + col] = v[keep[i]];
+        col++;
+    }
+    if (S.prec == WG_PREC_FP32)
+        for (int q = 0; q < CF_NCOL; q++) {
+            WG_CUDA_TRY(cudaMemcpy(vf.data(), S.C.fcol[q], sizeof(float) * n, cudaMemcpyDeviceToHost));
+            for (size_t i = 0; i < keep.size(); i++) cols[(int64_t)i * ncols + col] = (double)vf[keep[i]];
+            col++;
+        }
+    for (size_t i = 0; i < keep.size(); i++) {
+        key[i] = k[keep[i]];
+        flags[i] = f[keep[i]] & ~(uint32_t)C_DORMANT;
+        step0[i] = s0[keep[i]];
+        cell_dist[i] = cd[keep[i]];
+    }
+    return WG_OK;
+}
+
+int wg_set_contact_state(wg_scene* s, int64_t n, const uint64_t* key, const uint32_t* flags, const int32_t* step0,
+                         const int32_t* cell_dist, const double* cols, int32_t ncols) {
+    if (!s || n < 0 || (n > 0 && (!key || !flags || !step0 || !cell_dist || !cols))) return WG_ERR_ARG;
+    Sim& S = *SIM(s);
+    if (ncols != wg_contact_state_cols(s)) return S.fail(WG_ERR_ARG, "contact state has a different column count (precision mode)");
+    if (S.nScenes > 1) return S.fail(WG_ERR_UNSUPPORTED, "contact snapshots are per scene, not per batch");
+    WG_CUDA_TRY(cudaSetDevice(S.device));
+    if (!S.uploaded) {
+        int r = S.upload();
+        if (r) return r;
+    }
+    // the keys name existing particles, ascending; the type bits agree with the shapes
+    for (int64_t i = 0; i < n; i++) {
+        const int64_t lo = (int64_t)(key[i] >> 32), hi = (int64_t)(key[i] & 0xffffffffu);
+        if (lo >= hi || hi >= S.nPar || (i > 0 && key[i] <= key[i - 1])) return S.fail(WG_ERR_ARG, "contact keys out of order or range");
+        const bool sl = S.hShape[lo] == WG_SHAPE_SPHERE, sh = S.hShape[hi] == WG_SHAPE_SPHERE;
+        const int32_t other = sl ? S.hShape[hi] : S.hShape[lo];
+        const uint32_t ty = (sl && sh) ? CT_SS : ((sl || sh) ? (other == WG_SHAPE_FACET ? CT_FS : CT_WS) : CT_NONE);
+        if (ctype(flags[i]) != ty || (flags[i] & C_REMOVED)) return S.fail(WG_ERR_ARG, "contact flags do not match the particles");
+    }
+    int r = S.ensureContactCapacity(std::max<int64_t>(n, 1));
+    if (r) return r;
+    if (n > 0) {
+        std::vector<uint32_t> f(n);
+        for (int64_t i = 0; i < n; i++) f[i] = flags[i] & ~(uint32_t)C_DORMANT;
+        WG_CUDA_TRY(cudaMemcpy(S.C.key, key, sizeof(uint64_t) * n, cudaMemcpyHostToDevice));
+        WG_CUDA_TRY(cudaMemcpy(S.C.flags, f.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice));
+        WG_CUDA_TRY(cudaMemcpy(S.C.step0, step0, sizeof(int32_t) * n, cudaMemcpyHostToDevice));
+        WG_CUDA_TRY(cudaMemcpy(S.C.cdist, cell_dist, sizeof(int32_t) * n, cudaMemcpyHostToDevice));
+        const std::vector<int> q64 = snapshotCols64(S);
+        std::vector<double> v(n);
+        std::vector<float> vf(n);
+        int col = 0;
+        for (int q : q64) {
+            for (int64_t i = 0; i < n; i++) v[i] = cols[i * ncols + col];
+            WG_CUDA_TRY(cudaMemcpy(S.C.col[q], v.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+            col++;
+        }
+        if (S.prec == WG_PREC_FP32)
+            for (int q = 0; q < CF_NCOL; q++) {
+                for (int64_t i = 0; i < n; i++) vf[i] = (float)cols[i * ncols + col];
+                WG_CUDA_TRY(cudaMemcpy(S.C.fcol[q], vf.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
+                col++;
+            }
+    }
+    S.C.n = n;
+    S.K.n = 0;
+    S.packDirty = false;
+    S.fromEnds = false;    // the first step takes the node forces as written by the host
+    S.forceFull = true;    // and starts with a full run that merges these contacts
+    return WG_OK;
+}
+
 int64_t wg_num_contacts(wg_scene* s) {
     if (!s) return WG_ERR_ARG;
     Sim& S = *SIM(s);
