@@ -60,7 +60,8 @@ def test_resume_fp64_bitwise(kind, tmp_path, gpu_lib):
     other[walls] = False
     for k in ("pos", "ori", "vel", "angVel", "force", "torque"):
         assert np.array_equal(ref[k][other], got[k][other]), "%s differs after resume (max %g)" % (k, np.max(np.abs(ref[k] - got[k])))
-        np.testing.assert_allclose(got[k][walls], ref[k][walls], rtol=1e-12, atol=1e-12 * max(1e-30, np.abs(ref[k][walls]).max()))
+        if len(walls):
+            np.testing.assert_allclose(got[k][walls], ref[k][walls], rtol=1e-12, atol=1e-12 * max(1e-30, np.abs(ref[k][walls]).max()))
     S2.close()
 
 
