@@ -128,3 +128,13 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+# parameter tables of woo-batch (py/batch.py), feeding Batch
+from ._table import (TableParamReader, cartProdParamTable, dbFormatVersion, dbReadResults, inBatch, options,  # noqa: E402,F401
+                     readParamsFromTable, runPreprocessor, runTable, planTable, writeResults)
+
+if __name__ == "__main__":
+    import sys
+    from ._table import main
+    sys.exit(main())

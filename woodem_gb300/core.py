@@ -6,6 +6,11 @@ first ``run``); engines are descriptors compiled into one device plan, so the
 per-step loop of core/Scene.cpp:319-389 runs entirely on the GPU.
 """
 import math
+import os
+import socket
+import time
+import types
+
 import numpy as np
 
 from . import _plan
@@ -107,7 +112,7 @@ class Scene(Object):
 
     _attrs = {
         "dt": NaN, "nextDt": NaN, "dtSafety": 0.9, "step": 0, "time": 0.0, "stopAtStep": 0,
-        "trackEnergy": False, "deterministic": False, "isPeriodic": False, "tags": dict,
+        "trackEnergy": False, "deterministic": False, "isPeriodic": False, "tags": lambda: {},
         "subStepping": False,
     }
 
@@ -117,9 +122,27 @@ class Scene(Object):
         self.cell = Cell()
         self.gpu = _plan.GpuConfig()
         self._sim = None
+        self._clock0 = time.time()
+        self._labModules = {}
         super().__init__(**kw)
+        self._fillDefaultTags()
         for f in self.fields:
             f.scene = self
+
+    def _fillDefaultTags(self):
+        """Tags every new scene carries (core/Scene.cpp:140-163): user@host, isoTime and id (the local
+        time as YYYYMMDDTHHMMSS, id followed by 'p' and the process id), an empty title, and
+        idt/tid equal to the id. Tags given to the constructor are kept."""
+        iso = time.strftime("%Y%m%dT%H%M%S", time.localtime(self._clock0))
+        sid = "%sp%d" % (iso, os.getpid())
+        for k, v in (("user", "%s@%s" % (os.environ.get("USER", ""), socket.gethostname())), ("isoTime", iso), ("id", sid),
+                     ("title", ""), ("idt", sid), ("tid", sid)):
+            self.tags.setdefault(k, v)
+
+    @property
+    def duration(self):
+        """Wall-clock seconds this scene has existed (Scene.duration, core/Scene.hpp:200)."""
+        return int(time.time() - self._clock0)
 
     # reference name for isPeriodic in python is "periodic"
     @property
@@ -153,9 +176,19 @@ class Scene(Object):
 
     @property
     def lab(self):
+        """Labeled engines and functors as attributes, plus the pseudo-modules created with
+        ``S.lab._newModule(name)`` (which persist on the scene, e.g. ``S.lab.table`` of
+        ``woo.batch.readParamsFromTable``)."""
+        mods = self._labModules
+
         class _Lab:
-            pass
+            def _newModule(self, name):
+                mods.setdefault(name, types.SimpleNamespace())
+                setattr(self, name, mods[name])
+                return mods[name]
         lab = _Lab()
+        for name, m in mods.items():
+            setattr(lab, name, m)
         for e in self._engines:
             if getattr(e, "label", ""):
                 setattr(lab, e.label, e)

@@ -280,3 +280,31 @@ def batch_study(n_scenes=256, seed=0, nmin=1000, nmax=50000, rmin=3e-3, rmax=6e-
                                 damping=float(d[k]), precision=precision) for k in range(n_scenes)]
     table = {"n": n, "radius": r, "tanPhi": tp, "young": E, "damping": d}
     return scenes, table
+
+
+class BoxSettle:
+    """Preprocessor of a box settle (``box_settle_scaled``): set the attributes, call it, get the
+    Scene. ``stopAtStep`` is copied to the scene, so that a table runner knows how many steps each
+    line wants. Used as the simulation of parameter tables (``woo.batch.runPreprocessor``)."""
+
+    def __init__(self, n=2000, radius=4e-3, seed=0, density=3000.0, young=1e7, tanPhi=0.5, ktDivKn=0.2, damping=0.2,
+                 verletRel=0.1, precision="fp64", stopAtStep=0):
+        self.n, self.radius, self.seed, self.density, self.young = n, radius, seed, density, young
+        self.tanPhi, self.ktDivKn, self.damping, self.verletRel = tanPhi, ktDivKn, damping, verletRel
+        self.precision, self.stopAtStep = precision, stopAtStep
+
+    def checkAttrTypes(self):
+        for k in ("n", "seed", "stopAtStep"):
+            v = getattr(self, k)
+            if int(v) != v:
+                raise TypeError("%s must be an integer (%r)" % (k, v))
+            setattr(self, k, int(v))
+        if self.precision not in ("fp64", "fp32"):
+            raise ValueError("precision must be 'fp64' or 'fp32' (%r)" % self.precision)
+
+    def __call__(self):
+        S = box_settle_scaled(int(self.n), float(self.radius), seed=int(self.seed), density=float(self.density),
+                              young=float(self.young), tanPhi=float(self.tanPhi), ktDivKn=float(self.ktDivKn),
+                              damping=float(self.damping), verletRel=float(self.verletRel), precision=self.precision)
+        S.stopAtStep = int(self.stopAtStep)
+        return S
