@@ -79,7 +79,35 @@ typedef struct wg_config {
     double cell_next_gradv[9];  /* Cell.nextGradV */
     int32_t precision;          /* WG_PREC_FP64 (plain) or WG_PREC_FP32 (FP32 contact math, FP64 accumulation) */
     int32_t _pad1;
+    /* DynDt (pkg/dem/DynDt.hpp:19-23) as the engine after ContactLoop, with the activation of a
+       PeriodicEngine (core/Engine.cpp:169-194) by step count and/or simulation time. dyndt = 0: no
+       DynDt. The *_last/*_prev/n_done fields are the engine's counters at upload (stepLast < 0:
+       never evaluated); wg_get_dyndt returns their current values. */
+    int32_t dyndt;              /* 1: DynDt in the engine list */
+    int32_t dyndt_dry_run;      /* DynDt.dryRun */
+    int32_t dyndt_step_modulo;  /* PeriodicEngine.stepModulo */
+    int32_t dyndt_init_run;     /* PeriodicEngine.initRun */
+    int64_t dyndt_step_period;  /* PeriodicEngine.stepPeriod (<= 0: off) */
+    int64_t dyndt_n_do;         /* PeriodicEngine.nDo (< 0: unlimited) */
+    int64_t dyndt_n_done;       /* PeriodicEngine.nDone */
+    int64_t dyndt_step_last;    /* PeriodicEngine.stepLast */
+    int64_t dyndt_step_prev;    /* PeriodicEngine.stepPrev */
+    double dyndt_virt_period;   /* PeriodicEngine.virtPeriod (<= 0: off) */
+    double dyndt_virt_last;     /* PeriodicEngine.virtLast */
+    double dyndt_virt_prev;     /* PeriodicEngine.virtPrev */
+    double dyndt_max_rel_inc;   /* DynDt.maxRelInc */
+    double dt_safety;           /* Scene.dtSafety */
+    double next_dt;             /* Scene.nextDt (0 or NaN: none), taken as dt after the next step */
+    double time;                /* Scene.time at upload */
 } wg_config;
+
+/* DynDt state after a run: Scene.dt and nextDt, the engine's counters and DynDt.dt (the dry-run
+   value), and the last critical timestep computed (Inf: no stiff contact). */
+typedef struct wg_dyndt_state {
+    double dt, next_dt, dyndt_dt, crit_dt;
+    int64_t n_done, step_last, step_prev, n_evals;
+    double virt_last, virt_prev;
+} wg_dyndt_state;
 
 typedef struct wg_stats {
     int64_t step;               /* Scene.step */
@@ -162,6 +190,11 @@ int wg_put_state(wg_scene* s, const double* pos, const double* ori, const double
 int wg_get_nodes(wg_scene* s, double* pos, double* ori, double* vel, double* ang_vel,
                  double* force, double* torque);
 int wg_get_stats(wg_scene* s, wg_stats* out);
+/* Scene.dt/nextDt and the DynDt counters after the last run (DynDt::run, pkg/dem/DynDt.cpp:93-113;
+   PeriodicEngine::isActivated, core/Engine.cpp:169-194). */
+int wg_get_dyndt(wg_scene* s, wg_dyndt_state* out);
+/* Scene.dt and Scene.nextDt set between runs (0 or NaN next_dt: none); one scene only. */
+int wg_set_dt(wg_scene* s, double dt, double next_dt);
 /* Set Cell.nextGradV (row-major) between runs (periodic scenes). */
 int wg_set_next_gradv(wg_scene* s, const double* next_gradv);
 int wg_get_cell(wg_scene* s, double* hsize, double* trsf, double* gradv);

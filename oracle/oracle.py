@@ -38,6 +38,7 @@ def lib():
         "wo_collide_only": (C.c_int, [C.c_void_p]),
         "wo_get_nodes": (C.c_int, [C.c_void_p, P_D, P_D, P_D, P_D, P_D, P_D]),
         "wo_get_stats": (C.c_int, [C.c_void_p, C.POINTER(_native.wg_stats)]),
+        "wo_get_dyndt": (C.c_int, [C.c_void_p, C.POINTER(_native.wg_dyndt_state)]),
         "wo_num_contacts": (C.c_int64, [C.c_void_p]),
         "wo_get_contacts": (C.c_int, [C.c_void_p, P_I32, P_I32, P_I32, P_I32, P_I32, P_D, P_D, P_D, P_D]),
         "wo_kinetic_energy": (C.c_int, [C.c_void_p, P_D]),
@@ -94,6 +95,11 @@ class Oracle:
         self._check(self.L.wo_get_nodes(self.h, p(out["pos"]), p(out["ori"]), p(out["vel"]), p(out["angVel"]),
                                         p(out["force"]), p(out["torque"])), "get_nodes")
         return out
+
+    def dyndt(self):
+        st = _native.wg_dyndt_state()
+        self._check(self.L.wo_get_dyndt(self.h, C.byref(st)), "get_dyndt")
+        return st
 
     def stats(self):
         st = _native.wg_stats()

@@ -1109,15 +1109,101 @@ struct Scene {
         if (!ex.empty()) throw std::runtime_error(ex);
     }
 
-    // Scene::doOneStep, core/Scene.cpp:319-389 with the engine list Leapfrog, InsertionSortCollider, ContactLoop
+    // ------------------------------------------------------------ DynDt
+    // PeriodicEngine counters (core/Engine.hpp:136-151), Scene.nextDt and the simulation time
+    // since the scene's time 0 (PeriodicEngine's virtual clock)
+    long ddNDone = 0, ddStepLast = -1, ddStepPrev = -1, ddNEvals = 0;
+    double ddVirtLast = 0, ddVirtPrev = 0;
+    double ddDt = std::numeric_limits<double>::quiet_NaN(), ddCritDt = Inf;
+    double nextDt = std::numeric_limits<double>::quiet_NaN(), timeAbs = 0;
+    // PeriodicEngine::isActivated, core/Engine.cpp:169-194 (realPeriod, the wall clock, is not restated)
+    bool dynDtActivated() {
+        const double virtNow = timeAbs;
+        const long stepNow = step;
+        const bool initNow = ddStepLast < 0;
+        if (initNow) { ddVirtLast = virtNow; ddStepLast = stepNow; }
+        const bool due = (cfg.dyndt_virt_period > 0 && virtNow - ddVirtLast >= cfg.dyndt_virt_period) ||
+                         (cfg.dyndt_step_period > 0 && ((stepNow - ddStepLast >= cfg.dyndt_step_period) ||
+                                                        (cfg.dyndt_step_modulo && stepNow % cfg.dyndt_step_period == 0)));
+        if ((cfg.dyndt_n_do < 0 || ddNDone < cfg.dyndt_n_do) && due) {
+            ddVirtPrev = ddVirtLast; ddVirtLast = virtNow;
+            ddStepPrev = ddStepLast; ddStepLast = stepNow;
+            if (initNow && !cfg.dyndt_init_run) return false;
+            ddNDone++;
+            return true;
+        }
+        return false;
+    }
+    // DynDt::critDt_stiffness with nodalCritDtSq and nodalStiffAdd, pkg/dem/DynDt.cpp:17-76: for
+    // every node, the stiffness of the real contacts of each particle of the node (Particle.contacts,
+    // ordered by the id of the other particle), then 2*min(m/|ktrans_i|, I_i/|krot_i|) over the free
+    // axes; the square root of the minimum over nodes. pow(x,2) of the reference is restated as x*x.
+    double dynDtCritStiffness() {
+        std::vector<std::vector<std::pair<int, Contact*>>> byPar(par.size());
+        for (Contact* C : linView) {
+            if (!C->isReal()) continue;
+            byPar[C->pA].push_back({C->pB, C});
+            byPar[C->pB].push_back({C->pA, C});
+        }
+        for (auto& v : byPar)
+            std::sort(v.begin(), v.end(), [](const std::pair<int, Contact*>& a, const std::pair<int, Contact*>& b) { return a.first < b.first; });
+        std::vector<std::vector<int>> parRef(nodes.size());
+        for (size_t p = 0; p < par.size(); p++)
+            for (int k = 0; k < par[p].nNodes(); k++) parRef[par[p].nodes[k]].push_back((int)p);
+        double ret = Inf;
+        for (size_t i = 0; i < nodes.size(); i++) {
+            const Node& nd = nodes[i];
+            double r = Inf;
+            if ((nd.flags & DOF_ALL) != DOF_ALL) {
+                V3 kt, kr;
+                for (int p : parRef[i]) {
+                    for (const auto& e : byPar[p]) {
+                        const Contact* C = e.second;
+                        const int ix = (C->pA == p) ? 0 : 1;
+                        const V3 n = qrot(C->cori, V3(1, 0, 0));
+                        const V3 n2(n.x * n.x, n.y * n.y, n.z * n.z);
+                        kt = kt + V3(n2.x * (C->kn - C->kt) + C->kt, n2.y * (C->kn - C->kt) + C->kt, n2.z * (C->kn - C->kt) + C->kt);
+                        const double sc = (C->lens[ix] * C->lens[ix]) * C->kt;
+                        kr = kr + V3(sc * (n2.y + n2.z), sc * (n2.z + n2.x), sc * (n2.x + n2.y));
+                    }
+                }
+                for (int a = 0; a < 3; a++)
+                    if (kt[a] != 0 && nd.mass > 0. && !(nd.flags & (1u << a))) r = std::min(r, nd.mass / std::abs(kt[a]));
+                for (int a = 0; a < 3; a++)
+                    if (kr[a] != 0 && nd.inertia[a] > 0. && !(nd.flags & (8u << a))) r = std::min(r, nd.inertia[a] / std::abs(kr[a]));
+                r = 2 * r;
+            }
+            ret = std::min(ret, r);
+        }
+        return std::sqrt(ret);
+    }
+    // DynDt::run, pkg/dem/DynDt.cpp:93-113
+    void dynDtRun() {
+        const double crDt = dynDtCritStiffness();
+        ddCritDt = crDt;
+        ddNEvals++;
+        if (std::isinf(crDt)) return;
+        const int nSteps = (int)(step - ddStepPrev);
+        const double maxNewDt = cfg.dt * std::pow(1. + cfg.dyndt_max_rel_inc, nSteps);
+        const double ndt = std::min(crDt * cfg.dt_safety, maxNewDt);
+        if (!cfg.dyndt_dry_run) {
+            if (ndt != cfg.dt) { ddDt = std::numeric_limits<double>::quiet_NaN(); nextDt = ndt; }
+        } else ddDt = ndt;
+    }
+
+    // Scene::doOneStep, core/Scene.cpp:319-389 with the engine list Leapfrog, InsertionSortCollider,
+    // ContactLoop and, if configured, DynDt
     void doOneStep() {
         if (cfg.periodic) cell.integrateAndUpdate(cfg.dt);
         leapfrogRun();
         colliderRun();
         contactLoopRun();
+        if (cfg.dyndt && dynDtActivated()) dynDtRun();
         if (cfg.periodic) cell.setNextGradV();
         step++;
         time += cfg.dt;
+        timeAbs += cfg.dt;
+        if (!std::isnan(nextDt)) { cfg.dt = nextDt; nextDt = std::numeric_limits<double>::quiet_NaN(); }
     }
     void prepare() {
         size_t T = (size_t)nThreads;
@@ -1150,6 +1236,10 @@ int wo_set_config(void* sp, const wo_config* c) {
     Scene* s = (Scene*)sp;
     s->cfg = *c;
     s->step = c->step;
+    s->ddNDone = c->dyndt_n_done; s->ddStepLast = c->dyndt_step_last; s->ddStepPrev = c->dyndt_step_prev;
+    s->ddVirtLast = c->dyndt_virt_last; s->ddVirtPrev = c->dyndt_virt_prev;
+    s->nextDt = (c->next_dt > 0 && std::isfinite(c->next_dt)) ? c->next_dt : std::numeric_limits<double>::quiet_NaN();
+    s->timeAbs = c->time;
     if (c->law == 1 && c->hz_alpha != 0) { s->err = "Law2_L6Geom_HertzPhys_DMT: the Schwarz branch (alpha!=0) is not part of the restated path"; return -4; }
     if (c->periodic) {
         Cell& cl = s->cell;
@@ -1235,6 +1325,13 @@ int wo_get_stats(void* sp, wo_stats* o) {
     int64_t r = 0; for (auto* c : s->linView) r += c->isReal();
     o->n_real = r; o->time = s->time; o->verlet_dist = s->verletDist;
     for (int i = 0; i < 9; i++) o->stress[i] = s->stress.m[i / 3][i % 3];
+    return 0;
+}
+int wo_get_dyndt(void* sp, wo_dyndt_state* o) {
+    Scene* s = (Scene*)sp;
+    o->dt = s->cfg.dt; o->next_dt = s->nextDt; o->dyndt_dt = s->ddDt; o->crit_dt = s->ddCritDt;
+    o->n_done = s->ddNDone; o->step_last = s->ddStepLast; o->step_prev = s->ddStepPrev; o->n_evals = s->ddNEvals;
+    o->virt_last = s->ddVirtLast; o->virt_prev = s->ddVirtPrev;
     return 0;
 }
 int wo_get_cell(void* sp, double* hsize, double* trsf, double* gradv) {

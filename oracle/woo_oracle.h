@@ -70,7 +70,30 @@ typedef struct wo_config {
     double cell_next_gradv[9];
     int32_t precision;          /* ignored by the oracle (always FP64) */
     int32_t _pad1;
+    /* DynDt engine after ContactLoop (pkg/dem/DynDt.hpp:19-23) and its PeriodicEngine counters */
+    int32_t dyndt;
+    int32_t dyndt_dry_run;
+    int32_t dyndt_step_modulo;
+    int32_t dyndt_init_run;
+    int64_t dyndt_step_period;
+    int64_t dyndt_n_do;
+    int64_t dyndt_n_done;
+    int64_t dyndt_step_last;
+    int64_t dyndt_step_prev;
+    double dyndt_virt_period;
+    double dyndt_virt_last;
+    double dyndt_virt_prev;
+    double dyndt_max_rel_inc;
+    double dt_safety;           /* Scene.dtSafety */
+    double next_dt;             /* Scene.nextDt (NaN: none) */
+    double time;                /* Scene.time at the start */
 } wo_config;
+
+typedef struct wo_dyndt_state {
+    double dt, next_dt, dyndt_dt, crit_dt;
+    int64_t n_done, step_last, step_prev, n_evals;
+    double virt_last, virt_prev;
+} wo_dyndt_state;
 
 typedef struct wo_stats {
     int64_t step;
@@ -100,6 +123,7 @@ int wo_run(void* s, int64_t n_steps);
 int wo_get_nodes(void* s, double* pos, double* ori, double* vel, double* ang_vel,
                  double* force, double* torque);
 int wo_get_stats(void* s, wo_stats* out);
+int wo_get_dyndt(void* s, wo_dyndt_state* out);
 int64_t wo_num_contacts(void* s);
 /* Contacts as (lo id, hi id) pairs plus state. Arrays sized n = wo_num_contacts.
    real: 1 if geom&&phys. fglob: global force on particle A (3/contact, zeros if

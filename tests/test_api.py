@@ -70,10 +70,13 @@ def test_particle_views_and_containers():
 
 
 def test_plan_rejects_unsupported():
-    S = scenes.box_settle_small(n=20)
-    S.engines = utils.defaultEngines(damping=.2)  # DynDt
+    S = scenes.box_settle_small(n=20, precision="fp32")
+    S.engines = utils.defaultEngines(damping=.2)  # DynDt: FP64 mode only
     with pytest.raises(NotImplementedError):
         _plan.compile_scene(S)
+    S = scenes.box_settle_small(n=20)
+    S.engines = utils.defaultEngines(damping=.2)
+    assert _plan.compile_scene(S).config["dyndt"] == 1 and S.engines[-1].stepPeriod == 100
     S.engines = utils.defaultEngines(dynDtPeriod=0, cp2=Cp2_FrictMat_HertzPhys(alpha=.5), law=Law2_L6Geom_HertzPhys_DMT())
     with pytest.raises(NotImplementedError):
         _plan.compile_scene(S)

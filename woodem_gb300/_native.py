@@ -29,7 +29,18 @@ class wg_config(C.Structure):
         ("periodic", C.c_int32), ("homo_deform", C.c_int32), ("eval_stress", C.c_int32),
         ("cell_hsize", C.c_double * 9), ("cell_trsf", C.c_double * 9), ("cell_gradv", C.c_double * 9),
         ("cell_next_gradv", C.c_double * 9), ("precision", C.c_int32), ("_pad1", C.c_int32),
+        ("dyndt", C.c_int32), ("dyndt_dry_run", C.c_int32), ("dyndt_step_modulo", C.c_int32), ("dyndt_init_run", C.c_int32),
+        ("dyndt_step_period", C.c_int64), ("dyndt_n_do", C.c_int64), ("dyndt_n_done", C.c_int64),
+        ("dyndt_step_last", C.c_int64), ("dyndt_step_prev", C.c_int64), ("dyndt_virt_period", C.c_double),
+        ("dyndt_virt_last", C.c_double), ("dyndt_virt_prev", C.c_double), ("dyndt_max_rel_inc", C.c_double),
+        ("dt_safety", C.c_double), ("next_dt", C.c_double), ("time", C.c_double),
     ]
+
+
+class wg_dyndt_state(C.Structure):
+    _fields_ = [("dt", C.c_double), ("next_dt", C.c_double), ("dyndt_dt", C.c_double), ("crit_dt", C.c_double),
+                ("n_done", C.c_int64), ("step_last", C.c_int64), ("step_prev", C.c_int64), ("n_evals", C.c_int64),
+                ("virt_last", C.c_double), ("virt_prev", C.c_double)]
 
 
 class wg_stats(C.Structure):
@@ -79,6 +90,8 @@ def lib():
         "wg_put_state": (C.c_int, [C.c_void_p, P_D, P_D, P_D, P_D, P_D, P_D]),
         "wg_get_nodes": (C.c_int, [C.c_void_p, P_D, P_D, P_D, P_D, P_D, P_D]),
         "wg_get_stats": (C.c_int, [C.c_void_p, C.POINTER(wg_stats)]),
+        "wg_get_dyndt": (C.c_int, [C.c_void_p, C.POINTER(wg_dyndt_state)]),
+        "wg_set_dt": (C.c_int, [C.c_void_p, C.c_double, C.c_double]),
         "wg_set_next_gradv": (C.c_int, [C.c_void_p, P_D]),
         "wg_set_scenes": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.POINTER(C.c_int64)]),
         "wg_get_scene_stats": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),

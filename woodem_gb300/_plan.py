@@ -62,20 +62,42 @@ def compile_scene(S):
         elif isinstance(e, dem.ContactLoop):
             kinds.append("loop")
         elif isinstance(e, dem.DynDt):
-            raise NotImplementedError("DynDt is not part of the GPU path; use utils.defaultEngines(..., dynDtPeriod=0) "
-                                      "and set S.dt (e.g. from utils.pWaveDt)")
+            kinds.append("dyndt")
         else:
             raise NotImplementedError("Engine %s is not part of the GPU path" % type(e).__name__)
-    if kinds != ["leapfrog", "collider", "loop"]:
-        raise NotImplementedError("The GPU path runs the engine sequence [Leapfrog, InsertionSortCollider, ContactLoop] "
-                                  "(got %s)" % kinds)
-    lf, col, loop = eng
+    if kinds not in (["leapfrog", "collider", "loop"], ["leapfrog", "collider", "loop", "dyndt"]):
+        raise NotImplementedError("The GPU path runs the engine sequence [Leapfrog, InsertionSortCollider, ContactLoop"
+                                  "(, DynDt)] (got %s)" % kinds)
+    lf, col, loop = eng[:3]
+    dyn = eng[3] if len(eng) == 4 else None
     if not lf.reset:
         raise NotImplementedError("Leapfrog.reset=False is not part of the GPU path (use reset=True)")
     cfg = {}
     if not (S.dt > 0 and math.isfinite(S.dt)):
-        raise ValueError("Scene.dt must be set to a positive value (automatic critical dt is not part of the GPU path)")
+        # Scene::doOneStep (core/Scene.cpp:332-352): dt = dtSafety times the smallest critical dt of
+        # the engines and fields. Engines give Inf, DynDt too while no contact is real (before the
+        # first step); the DemField gives pWaveDt without clumps (pkg/dem/Particle.cpp:372-377).
+        from .utils import pWaveDt
+        crit = pWaveDt(S, noClumps=True)
+        if not math.isfinite(crit):
+            raise RuntimeError("Failed to obtain meaningful dt from engines and fields automatically.")
+        S.dt = S.dtSafety * crit
     cfg["dt"] = float(S.dt)
+    cfg["dt_safety"] = float(S.dtSafety)
+    cfg["next_dt"] = float(S.nextDt) if (S.nextDt > 0 and math.isfinite(S.nextDt)) else float("nan")
+    cfg["time"] = float(S.time)
+    if dyn is not None:
+        if dyn.realPeriod > 0:
+            raise NotImplementedError("DynDt.realPeriod (wall-clock activation) is not part of the GPU path")
+        if S.gpu.precision != "fp64":
+            raise NotImplementedError("DynDt runs in the FP64 precision mode only")
+        if not (1.0 + dyn.maxRelInc != 1.0 and dyn.maxRelInc > 0):
+            raise ValueError("DynDt: maxRelInc too small (1.0+maxRelInc==1.0)")
+        cfg.update(dyndt=1, dyndt_dry_run=int(bool(dyn.dryRun)), dyndt_step_modulo=int(bool(dyn.stepModulo)),
+                   dyndt_init_run=int(bool(dyn.initRun)), dyndt_step_period=int(dyn.stepPeriod), dyndt_n_do=int(dyn.nDo),
+                   dyndt_n_done=int(dyn.nDone), dyndt_step_last=int(dyn.stepLast), dyndt_step_prev=int(dyn.stepPrev),
+                   dyndt_virt_period=float(dyn.virtPeriod), dyndt_virt_last=float(dyn.virtLast),
+                   dyndt_virt_prev=float(dyn.virtPrev), dyndt_max_rel_inc=float(dyn.maxRelInc))
     cfg["gravity"] = np.asarray(D.gravity, dtype=float)
     cfg["lone_mask"] = int(D.loneMask)
     cfg["deterministic"] = 1
@@ -169,6 +191,11 @@ def compile_scene(S):
     shp = A.particles["shape"]
     if (np.any(shp == 2) and not have_fs) or (np.any(shp == 1) and not have_ws):
         raise NotImplementedError("scene has facets/walls but the ContactLoop lacks their Cg2 functor")
+    if dyn is not None and np.any(shp == 2):
+        fn = A.particles["nodes"][shp == 2].ravel()
+        if np.any((A.nodes["flags"][fn[fn >= 0]] & 63) != 63):
+            raise NotImplementedError("DynDt with facet nodes that are not fully blocked (their stiffness includes the "
+                                      "facets' internal forces) is not part of the GPU path")
     mats = D._mats
     for m in mats:
         from .dem import FrictMat
@@ -237,12 +264,14 @@ class Simulation:
             # Cell.nextGradV set between runs takes effect at the next step (core/Cell.hpp:152)
             g = np.ascontiguousarray(np.asarray(self.S.cell.nextGradV, dtype=float).reshape(9))
             self.H.check(L.wg_set_next_gradv(h, _native.ptr(g)), "set_next_gradv")
+        self._push_dt()
         self.H.check(L.wg_run(h, int(n)), "run")
         self.host_stale = True
         self._contacts = None
         st = self.stats()
         self.S.step = int(st.step)
         self.S.time = self.t0 + float(st.time)
+        self._pull_dt()
         for e in self.S.engines:
             from .dem import InsertionSortCollider
             if isinstance(e, InsertionSortCollider):
@@ -261,6 +290,33 @@ class Simulation:
             for e in self.S.engines:
                 if isinstance(e, ContactLoop):
                     e.stress = np.array(st.stress).reshape(3, 3)
+
+    def dyndt(self):
+        st = _native.wg_dyndt_state()
+        self.H.check(self.H.L.wg_get_dyndt(self.H.h, C_byref(st)), "get_dyndt")
+        return st
+
+    def _push_dt(self):
+        """Scene.dt or Scene.nextDt set on the host since the last run."""
+        S = self.S
+        nxt = float(S.nextDt) if (S.nextDt > 0 and math.isfinite(S.nextDt)) else float("nan")
+        st = self.dyndt()
+        if S.dt != st.dt or not (nxt == st.next_dt or (math.isnan(nxt) and math.isnan(st.next_dt))):
+            if not (S.dt > 0 and math.isfinite(S.dt)):
+                raise ValueError("Scene.dt must be positive and finite")
+            self.H.check(self.H.L.wg_set_dt(self.H.h, float(S.dt), nxt), "set_dt")
+
+    def _pull_dt(self):
+        """Scene.dt/nextDt and the DynDt counters after a run."""
+        from .dem import DynDt
+        st = self.dyndt()
+        self.S.dt = float(st.dt)
+        self.S.nextDt = float(st.next_dt)
+        for e in self.S.engines:
+            if isinstance(e, DynDt) and not e.dead:
+                e.nDone, e.stepLast, e.stepPrev = int(st.n_done), int(st.step_last), int(st.step_prev)
+                e.virtLast, e.virtPrev = float(st.virt_last), float(st.virt_prev)
+                e.dt = float(st.dyndt_dt)
 
     def stats(self):
         st = _native.wg_stats()

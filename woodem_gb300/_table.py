@@ -429,15 +429,23 @@ def buildLine(sim, table, line, results=""):
     return S
 
 
+def _runsAlone(S):
+    """Periodic scenes and scenes whose dt changes (DynDt, Scene.nextDt) are not batched."""
+    from .dem import DynDt
+    return bool(S.isPeriodic or any(isinstance(e, DynDt) and not e.dead for e in S.engines)
+                or (S.nextDt > 0 and math.isfinite(S.nextDt)))
+
+
 def planTable(scenes, steps=None, max_particles=50_000_000):
     """Groups of table lines that run together: aperiodic scenes of one precision and one step
-    count share a Batch, up to ``max_particles`` particles per batch; periodic scenes run alone.
+    count share a Batch, up to ``max_particles`` particles per batch; periodic scenes and scenes
+    with DynDt run alone.
     ``scenes`` maps line -> Scene; returns [(kind, steps, [lines])], kind "batch" or "single"."""
     groups, order = {}, []
     out = []
     for l, S in scenes.items():
         n = _sceneSteps(S, steps)
-        if S.isPeriodic:
+        if _runsAlone(S):
             out.append(("single", n, [l]))
             continue
         key = (S.gpu.precision, n)

@@ -28,6 +28,8 @@ class Batch:
         if not self.scenes:
             raise ValueError("empty batch")
         self.arrays = [_plan.compile_scene(S) for S in self.scenes]
+        if any(A.config.get("dyndt") or A.config["next_dt"] == A.config["next_dt"] for A in self.arrays):
+            raise NotImplementedError("DynDt and Scene.nextDt are not supported in a Batch (each scene keeps its dt)")
         prec = {A.config["precision"] for A in self.arrays}
         if len(prec) != 1:
             raise ValueError("the scenes of a batch share one precision mode")

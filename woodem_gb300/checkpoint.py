@@ -2,7 +2,8 @@
 
 ``save(S, path)`` writes one flat ``.npz`` file: the node state (pos, ori, vel, angVel, force,
 torque), the contact container with the persistent contact state (``wg_get_contact_state``),
-Scene.step/time/dt and the periodic cell (hSize, trsf, gradV, nextGradV). ``load(S, path)``
+Scene.step/time/dt, the counters of a DynDt engine and the periodic cell (hSize, trsf, gradV,
+nextGradV). ``load(S, path)``
 puts that state into a scene built the same way (the same particles, materials and engines:
 a fingerprint of the compiled description is checked) and uploads it; the next step starts with
 a collider full run that keeps the state of the real contacts, as the reference's Scene.load
@@ -19,7 +20,10 @@ from . import _native, _plan
 
 _NODE_COLS = ("pos", "ori", "vel", "angVel", "force", "torque")
 # configuration entries that describe the state, not the scene
-_STATE_CFG = ("step", "cell_hsize", "cell_trsf", "cell_gradv", "cell_next_gradv")
+_STATE_CFG = ("step", "time", "dt", "next_dt", "cell_hsize", "cell_trsf", "cell_gradv", "cell_next_gradv", "dyndt_n_done",
+              "dyndt_step_last", "dyndt_step_prev", "dyndt_virt_last", "dyndt_virt_prev")
+# DynDt counters (PeriodicEngine) saved with the state
+_DYNDT_ATTRS = ("nDone", "stepLast", "stepPrev", "virtLast", "virtPrev")
 
 
 def fingerprint(A):
@@ -67,10 +71,21 @@ def save(S, path):
     arrays.update(con_key=key, con_flags=flags, con_step0=step0, con_cell_dist=cdist, con_state=cols)
     meta = {"step": int(S.step), "time": float(S.time), "dt": float(S.dt), "precision": S.gpu.precision,
             "periodic": bool(S.isPeriodic), "n_nodes": int(len(nd)), "state_cols": ncols, "fingerprint": fingerprint(sim.A)}
+    dyn = _dyndt(S)
+    if dyn is not None:
+        meta["dyndt"] = {k: getattr(dyn, k) for k in _DYNDT_ATTRS}
     if S.isPeriodic:
         for k in ("hSize", "trsf", "gradV", "nextGradV"):
             arrays["cell_" + k] = np.array(getattr(S.cell, k), dtype=float)
     np.savez(path, meta=np.array(json.dumps(meta)), **arrays)
+
+
+def _dyndt(S):
+    from .dem import DynDt
+    for e in S.engines:
+        if isinstance(e, DynDt) and not e.dead:
+            return e
+    return None
 
 
 def load(S, path):
@@ -91,6 +106,12 @@ def load(S, path):
     S.step = meta["step"]
     S.time = meta["time"]
     S.dt = meta["dt"]
+    dyn = _dyndt(S)
+    if (dyn is None) != ("dyndt" not in meta):
+        raise ValueError("the checkpoint and the scene differ in having a DynDt engine")
+    if dyn is not None:
+        for k, v in meta["dyndt"].items():
+            setattr(dyn, k, v)
     if meta["periodic"]:
         S.cell.hSize = arrays["cell_hSize"]
         S.cell.trsf = arrays["cell_trsf"]

@@ -57,7 +57,11 @@ class Engine(Object):
 
 
 class PeriodicEngine(Engine):
-    _attrs = {"stepPeriod": -1, "virtPeriod": 0.0, "realPeriod": 0.0}
+    """Activation by step count, simulation time or wall clock (core/Engine.hpp:136-151); the
+    counters (nDone, stepLast, stepPrev, virtLast, virtPrev) are updated by the runs."""
+    _attrs = {"stepPeriod": 1, "virtPeriod": 0.0, "realPeriod": 0.0, "stepModulo": True, "nDo": -1, "nDone": 0,
+              "initRun": True, "virtLast": NaN, "realLast": NaN, "stepLast": -1, "stepPrev": -1, "virtPrev": -1.0,
+              "realPrev": -1.0}
 
 
 class Field(Object):

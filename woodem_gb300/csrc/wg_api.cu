@@ -696,6 +696,65 @@ int Sim::syncContacts() {
     return 0;
 }
 
+// Scene.dt of the steps from the next one on (core/Scene.cpp:389): the scene parameters the
+// kernels read, and the cell integration of periodic runs (which takes cfg.dt)
+int Sim::applyDt(double ndt) {
+    Sim& S = *this;
+    cfg.dt = ndt;
+    hPar.dt = ndt;
+    hPar.dtF = (float)ndt;
+    if (!hPars.empty()) {
+        hPars[0].dt = ndt;
+        hPars[0].dtF = (float)ndt;
+    }
+    if (!cfg.periodic) WG_CUDA_TRY(cudaMemcpyAsync(dPar, &hPar, sizeof(ScenePar), cudaMemcpyHostToDevice, stream));
+    return 0;
+}
+
+// DynDt::run (pkg/dem/DynDt.cpp:93-113) after the contact loop of step stepNow: the critical
+// timestep from the contact stiffnesses (critDt_stiffness, :66-76, on the device), then
+// nextDt = min(crDt*dtSafety, dt*(1+maxRelInc)^(steps since the previous run)).
+int Sim::runDynDt(int64_t stepNow) {
+    Sim& S = *this;
+    if (I.endCap > kCap || !dCrit) {
+        if (dKA) dfree(dKA);
+        if (dKB) dfree(dKB);
+        kCap = std::max<int64_t>(I.endCap, 1);
+        dKA = (double4_32a*)dalloc(sizeof(double4_32a) * kCap);
+        dKB = (double2*)dalloc(sizeof(double2) * kCap);
+        if (!dCrit) dCrit = (unsigned long long*)dalloc(sizeof(unsigned long long));
+        if (!dKA || !dKB || !dCrit) return fail(WG_ERR_CUDA, "out of device memory (DynDt)");
+    }
+    const double inf = std::numeric_limits<double>::infinity();
+    unsigned long long bits;
+    std::memcpy(&bits, &inf, sizeof bits);
+    WG_CUDA_TRY(cudaMemsetAsync(dKA, 0, sizeof(double4_32a) * kCap, stream));
+    WG_CUDA_TRY(cudaMemsetAsync(dKB, 0, sizeof(double2) * kCap, stream));
+    WG_CUDA_TRY(cudaMemcpyAsync(dCrit, &bits, sizeof bits, cudaMemcpyHostToDevice, stream));
+    launch_dyndt(stream, N, P, C, I, dPar, dKA, dKB, dCrit, dFlags + FL_ERR, cfg.periodic != 0);
+    WG_CUDA_TRY(cudaGetLastError());
+    WG_CUDA_TRY(cudaMemcpyAsync(&bits, dCrit, sizeof bits, cudaMemcpyDeviceToHost, stream));
+    WG_CUDA_TRY(cudaStreamSynchronize(stream));
+    double minSq;
+    std::memcpy(&minSq, &bits, sizeof minSq);
+    const double crDt = std::sqrt(minSq);
+    dd.critDt = crDt;
+    dd.nEvals++;
+    if (std::isinf(crDt)) return 0;  // no timestep computed, the current value stays
+    const int64_t nSteps = stepNow - dd.stepPrev;
+    const double maxNewDt = cfg.dt * std::pow(1. + dd.maxRelInc, (double)nSteps);
+    const double a = crDt * dd.dtSafety;
+    const double ndt = maxNewDt < a ? maxNewDt : a;  // std::min(a, maxNewDt)
+    if (!dd.dryRun) {
+        if (ndt != cfg.dt) {
+            dd.dynDt = std::numeric_limits<double>::quiet_NaN();
+            nextDt = ndt;
+        }
+    } else
+        dd.dynDt = ndt;
+    return 0;
+}
+
 int Sim::run(int64_t n) {
     Sim& S = *this;
     SimEx& X = static_cast<SimEx&>(*this);
@@ -762,7 +821,20 @@ int Sim::run(int64_t n) {
     while (done < n) {
         // the sphere-sphere kernel updates the packed state from here on
         if (K.n > 0) packDirty = true;
-        const int64_t k = std::min<int64_t>(n - done, maxChunk);
+        int64_t k = std::min<int64_t>(n - done, maxChunk);
+        // dt may change after a step (Scene.nextDt, DynDt): such a step ends its chunk
+        if (std::isfinite(nextDt)) k = 1;
+        if (dd.on) {
+            DynDtState t = dd;
+            double tv = timeAbs;
+            for (int64_t j = 0; j < k; j++) {
+                if (t.activated(step + j, tv)) {
+                    k = j + 1;
+                    break;
+                }
+                tv += cfg.dt;
+            }
+        }
         const bool needFull = !initialized || anyZeroVd || forceFull;
         k_set_flags<<<1, 1, 0, stream>>>(dFlags, needFull ? 1 : 0);
         if (cfg.periodic) {
@@ -860,8 +932,12 @@ int Sim::run(int64_t n) {
             cudaEventElapsedTime(&a, E[3 * maxChunk], E[3 * maxChunk + 1]); ph[3] += a;
             cudaEventElapsedTime(&a, E[0], E[1]); ph[1] += a;
             if (hFlags[FL_ERR]) {
+                for (int64_t j = 0; j < ds; j++) {
+                    if (dd.on) dd.activated(step + j, timeAbs);
+                    time += cfg.dt;
+                    timeAbs += cfg.dt;
+                }
                 step += ds;
-                time += ds * cfg.dt;
                 break;
             }
             ds += 1;
@@ -873,9 +949,35 @@ int Sim::run(int64_t n) {
             hPar = parSeq[ds - 1];
             WG_CUDA_TRY(cudaMemcpyAsync(dPar, &hPar, sizeof(ScenePar), cudaMemcpyHostToDevice, stream));
         }
+        // Scene::doOneStep epilogue for each step done (core/Scene.cpp:384-389): the engines' turn
+        // for DynDt (activation counters; it runs after ContactLoop of the chunk's last step, which
+        // the chunk was cut at), then step++, time += dt, dt = nextDt
+        bool dynDtNow = false;
+        for (int64_t j = 0; j < ds; j++) {
+            if (dd.on && dd.activated(step + j, timeAbs)) {
+                if (j != ds - 1) return fail(WG_ERR_STATE, "DynDt activation inside a chunk");
+                dynDtNow = true;
+            }
+            if (j < ds - 1) {
+                time += cfg.dt;
+                timeAbs += cfg.dt;
+            }
+        }
         step += ds;
-        time += ds * cfg.dt;
         done += ds;
+        if (ds > 0) {
+            if (dynDtNow) {
+                int r = runDynDt(step - 1);
+                if (r) return r;
+            }
+            time += cfg.dt;
+            timeAbs += cfg.dt;
+            if (std::isfinite(nextDt)) {
+                int r = applyDt(nextDt);
+                if (r) return r;
+                nextDt = std::numeric_limits<double>::quiet_NaN();
+            }
+        }
     }
     // ContactLoop.stress of the last step (periodic cells with evalStress)
     if (cfg.periodic && cfg.eval_stress && fromEnds && done > 0) {
@@ -966,8 +1068,31 @@ int wg_set_config(wg_scene* s, const wg_config* c) {
     Sim& S = *SIM(s);
     if (S.uploaded) return S.fail(WG_ERR_STATE, "configuration is fixed once the scene runs; create a new scene");
     if (!(c->dt > 0) || !std::isfinite(c->dt)) return S.fail(WG_ERR_ARG, "Scene.dt must be positive and finite");
+    if (c->dyndt && c->precision != WG_PREC_FP64)
+        return S.fail(WG_ERR_UNSUPPORTED, "DynDt runs in the FP64 precision mode only");
+    if (c->dyndt && !(c->dyndt_max_rel_inc > 0 && 1. + c->dyndt_max_rel_inc != 1.))
+        return S.fail(WG_ERR_ARG, "DynDt: maxRelInc too small (1.0+maxRelInc==1.0)");  // DynDt::postLoad, DynDt.cpp:12-14
     S.cfg = *c;
     S.haveCfg = true;
+    DynDtState& d = S.dd;
+    d = DynDtState{};
+    d.on = c->dyndt != 0;
+    d.dryRun = c->dyndt_dry_run != 0;
+    d.stepModulo = c->dyndt_step_modulo != 0;
+    d.initRun = c->dyndt_init_run != 0;
+    d.stepPeriod = c->dyndt_step_period;
+    d.nDo = c->dyndt_n_do;
+    d.nDone = c->dyndt_n_done;
+    d.stepLast = c->dyndt_step_last;
+    d.stepPrev = c->dyndt_step_prev;
+    d.virtPeriod = c->dyndt_virt_period;
+    d.virtLast = c->dyndt_virt_last;
+    d.virtPrev = c->dyndt_virt_prev;
+    d.maxRelInc = c->dyndt_max_rel_inc;
+    d.dtSafety = c->dt_safety;
+    // Scene.nextDt: a positive finite value (0 and NaN: none)
+    S.nextDt = (c->next_dt > 0 && std::isfinite(c->next_dt)) ? c->next_dt : std::numeric_limits<double>::quiet_NaN();
+    S.timeAbs = c->time;
     return WG_OK;
 }
 
@@ -979,6 +1104,8 @@ int wg_set_scenes(wg_scene* s, int32_t n_scenes, const wg_config* cfgs, const in
     for (int k = 0; k < n_scenes; k++) {
         if (particle_start[k + 1] < particle_start[k]) return S.fail(WG_ERR_ARG, "particle_start must be non-decreasing");
         if (!(cfgs[k].dt > 0) || !std::isfinite(cfgs[k].dt)) return S.fail(WG_ERR_ARG, "Scene.dt must be positive and finite");
+        if (cfgs[k].dyndt || (cfgs[k].next_dt > 0 && std::isfinite(cfgs[k].next_dt)))
+            return S.fail(WG_ERR_UNSUPPORTED, "DynDt and Scene.nextDt are not supported in a batch of scenes");
     }
     S.nScenes = n_scenes;
     S.cfgs.assign(cfgs, cfgs + n_scenes);
@@ -1128,6 +1255,8 @@ int wg_slot_load(wg_scene* s, int32_t k, const wg_config* c, int64_t n, const do
     Sim& S = *SIM(s);
     int r = slotCheck(S, k);
     if (r) return r;
+    if (c->dyndt || (c->next_dt > 0 && std::isfinite(c->next_dt)))
+        return S.fail(WG_ERR_UNSUPPORTED, "DynDt and Scene.nextDt are not supported in serving slots");
     const int64_t p0 = S.sceneStart[k], cap = S.sceneStart[k + 1] - p0;
     if (n > cap) return S.fail(WG_ERR_CAPACITY, "job larger than the slot");
     const int32_t matCap = (int32_t)(S.hDensity.size() / S.nScenes);
@@ -1403,6 +1532,40 @@ int wg_run_host(wg_scene* s, int64_t n_steps, double* pos, double* ori, double* 
     r = wg_run(s, n_steps);
     if (r) return r;
     return wg_get_nodes(s, pos, ori, vel, ang_vel, force, torque);
+}
+
+int wg_set_dt(wg_scene* s, double dt, double next_dt) {
+    if (!s) return WG_ERR_ARG;
+    Sim& S = *SIM(s);
+    if (!S.haveCfg) return S.fail(WG_ERR_STATE, "wg_set_config must be called first");
+    if (S.nScenes > 1) return S.fail(WG_ERR_UNSUPPORTED, "the scenes of a batch keep their dt");
+    if (!(dt > 0) || !std::isfinite(dt)) return S.fail(WG_ERR_ARG, "Scene.dt must be positive and finite");
+    if (dt != S.cfg.dt) {
+        if (S.uploaded) {
+            int r = S.applyDt(dt);
+            if (r) return r;
+        } else
+            S.cfg.dt = dt;
+    }
+    S.nextDt = (next_dt > 0 && std::isfinite(next_dt)) ? next_dt : std::numeric_limits<double>::quiet_NaN();
+    return WG_OK;
+}
+
+int wg_get_dyndt(wg_scene* s, wg_dyndt_state* o) {
+    if (!s || !o) return WG_ERR_ARG;
+    Sim& S = *SIM(s);
+    if (!S.haveCfg) return S.fail(WG_ERR_STATE, "wg_set_config must be called first");
+    o->dt = S.cfg.dt;
+    o->next_dt = S.nextDt;
+    o->dyndt_dt = S.dd.dynDt;
+    o->crit_dt = S.dd.critDt;
+    o->n_done = S.dd.nDone;
+    o->step_last = S.dd.stepLast;
+    o->step_prev = S.dd.stepPrev;
+    o->n_evals = S.dd.nEvals;
+    o->virt_last = S.dd.virtLast;
+    o->virt_prev = S.dd.virtPrev;
+    return WG_OK;
 }
 
 int wg_get_stats(wg_scene* s, wg_stats* o) {

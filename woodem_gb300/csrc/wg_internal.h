@@ -3,6 +3,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <limits>
 #include <string>
 #include <vector>
 
@@ -114,6 +115,7 @@ enum {
     CC_CPX, CC_CPY, CC_CPZ,                          // L6Geom node position (contact point)
     CC_P0, CC_P1, CC_P2, CC_P3, CC_P4,               // FrictPhys kn kt tanPhi | HertzPhys kn0 kt0 tanPhi alpha_sqrtMK R
     CC_FN, CC_FT1, CC_FT2,                           // phys.force (local)
+    CC_UN0,                                          // L6Geom.uN of the contact's first step (L6Geom.lens)
     CC_NCOL
 };
 // FP32-force mode columns (the FP64 columns CC_FT1/CC_FT2 keep the IdealElPl shear force and
@@ -219,6 +221,11 @@ void launch_contact_fp64(cudaStream_t st, const DevNodes& N, const DevParticles&
 void launch_forces(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const ScenePar* sp,
                    const int* dFlags, bool perStep);
 void launch_advance(cudaStream_t st, long long* dStep, const int* dFlags);
+// DynDt: per-end stiffness of the real contacts into kA/kB (zeroed by the caller, I.endCap
+// entries), then the minimum over nodes of the squared critical timestep into *out (initialised
+// by the caller to the bits of +Inf). FP64 contact arrays.
+void launch_dyndt(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C, const DevIncidence& I,
+                  const ScenePar* sp, double4_32a* kA, double2* kB, unsigned long long* out, int* dErr, bool periodic);
 // sum over real contacts of F_A (x) branch into out[9] (not divided by the volume); scratch holds
 // 9 doubles per 256 active contacts; returns -1 when it is too small
 int launch_stress(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C, const DevIncidence& I,
@@ -259,6 +266,30 @@ struct Grid {
 struct CollideWork;  // scratch owned by the simulation
 struct Sim;
 int collide_full_run(Sim& S);
+
+// DynDt after ContactLoop (pkg/dem/DynDt.hpp:19-23) with the counters of its PeriodicEngine.
+struct DynDtState {
+    bool on = false, dryRun = false, stepModulo = true, initRun = true;
+    int64_t stepPeriod = 0, nDo = -1, nDone = 0, stepLast = -1, stepPrev = -1, nEvals = 0;
+    double virtPeriod = 0, virtLast = 0, virtPrev = 0, maxRelInc = 1e-4, dtSafety = 0.9;
+    double dynDt = std::numeric_limits<double>::quiet_NaN();   // DynDt.dt (dry run)
+    double critDt = std::numeric_limits<double>::infinity();    // last critical timestep
+    // PeriodicEngine::isActivated (core/Engine.cpp:169-194) by step count and simulation time
+    bool activated(int64_t stepNow, double virtNow) {
+        const bool initNow = stepLast < 0;
+        if (initNow) { virtLast = virtNow; stepLast = stepNow; }
+        if ((nDo < 0 || nDone < nDo) &&
+            ((virtPeriod > 0 && virtNow - virtLast >= virtPeriod) ||
+             (stepPeriod > 0 && ((stepNow - stepLast >= stepPeriod) || (stepModulo && stepNow % stepPeriod == 0))))) {
+            virtPrev = virtLast; virtLast = virtNow;
+            stepPrev = stepLast; stepLast = stepNow;
+            if (initNow && !initRun) return false;
+            nDone++;
+            return true;
+        }
+        return false;
+    }
+};
 
 // ------------------------------------------------------------------ host simulation object
 struct DevBuf {
@@ -336,6 +367,15 @@ struct Sim {
     double* dStress = nullptr;       // 9 doubles + per-block partials
     int64_t stressCap = 0;
     double stress[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // ContactLoop.stress of the last step
+    // DynDt (one scene, FP64 mode): engine state, Scene.nextDt, Scene.time since the scene's
+    // time 0 (for virtPeriod), and the scratch of the stiffness evaluation
+    DynDtState dd;
+    double nextDt = std::numeric_limits<double>::quiet_NaN();
+    double timeAbs = 0;
+    double4_32a* dKA = nullptr;
+    double2* dKB = nullptr;
+    int64_t kCap = 0;
+    unsigned long long* dCrit = nullptr;
     // timing
     std::vector<cudaEvent_t> evPool;  // per queued step: before Leapfrog, before contacts, after
     cudaEvent_t ev[8];
@@ -350,6 +390,8 @@ struct Sim {
     int prepareParams();
     int prepareParamsFor(const wg_config& c, int64_t p0, int64_t p1, ScenePar& out);
     int run(int64_t n);
+    int applyDt(double dt);
+    int runDynDt(int64_t stepNow);
     int checkErr();
     int ensureContactCapacity(int64_t need);
     int syncContacts();  // write the packed sphere-sphere state back to the contact arrays if needed

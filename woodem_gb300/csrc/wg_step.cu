@@ -343,6 +343,7 @@ __global__ void __launch_bounds__(128) k_contact_fp64(DevNodes N, DevParticles P
         C.col[CC_P2][c] = ph2;
         C.col[CC_P3][c] = ph3;
         C.col[CC_P4][c] = ph4;
+        C.col[CC_UN0][c] = g.uN;  // uN of the first step, which fixes L6Geom.lens (DynDt)
         C.step0[c] = (int32_t)step;
     } else {
         // existing geometry: update branch, pkg/dem/L6Geom.cpp:79-216
@@ -612,6 +613,135 @@ int launch_stress(cudaStream_t st, const DevNodes& N, const DevParticles& P, con
     k_stress_partial<<<(unsigned)nb, 256, 0, st>>>(N, P, C, I, sp, scratch);
     k_stress_final<<<1, 32, 0, st>>>(scratch, (int)nb, out);
     return 0;
+}
+
+// ---------------------------------------------------------------------------------- DynDt
+// DynDt::nodalStiffAdd (pkg/dem/DynDt.cpp:17-38), the part of one contact: each real contact
+// writes into the end slot of each of its particles the contact's additions to that node's
+// translational and rotational stiffness,
+//   ktrans += n²(kn - kt) + kt,   krot += lens[ix]²·kt·(n²y + n²z, n²z + n²x, n²x + n²y),
+// n = the L6Geom node orientation (Quaternionr(trsf), L6Geom.cpp:216) applied to the x axis, ix
+// the particle's index in the contact. kn and kt are those the last law call left in the phys:
+// FrictPhys keeps them constant; the Hertz law sets kn = 3/2·kn0·sqrt(-uN) and
+// kt = kt0·sqrt(max(-uN, 0)) (Hertz.cpp:69,157) from the uN of the step, which the geometry
+// functor recomputes here from the unchanged positions. lens are |r| + uN/2 of the contact's first
+// step (L6Geom.cpp:63-66). Facets are left out (their nodes must be fully blocked). The slots
+// are zeroed beforehand, so non-real contacts add nothing.
+template <bool PERI>
+__global__ void __launch_bounds__(128) k_dyndt_ends(DevNodes N, DevParticles P, DevContacts C, DevIncidence I,
+                                                    const ScenePar* __restrict__ spp, double4_32a* __restrict__ kA,
+                                                    double2* __restrict__ kB, int* __restrict__ dErr) {
+    const int64_t rk = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (rk >= I.nAct) return;
+    const int4 wk = I.work[rk];
+    const int64_t c = wk.x;
+    const int A = wk.y, B = wk.z;
+    const uint32_t fl = C.flags[c];
+    if (!(fl & C_REAL)) return;
+    const ScenePar& sp = spp[sceneOfP(P, B)];
+    const uint32_t ty = ctype((uint32_t)wk.w);
+    D3 shift2{0, 0, 0};
+    if (PERI) {
+        int a, b, cc;
+        unpackCellDist(C.cdist[c], a, b, cc);
+        if (fl & C_SWAP) { a = -a; b = -b; cc = -cc; }
+        shift2 = mul(ldm(sp.hSize), D3{(double)a, (double)b, (double)cc});
+    }
+    Geo g;
+    if (ty == CT_SS) geomSS(N, A, B, shift2, true, sp.ssDistFactor, g);
+    else if (ty == CT_WS) geomWS(N, P, C.col[CC_T0X + P.aux[A].x][c], A, B, shift2, true, g);
+    else geomFS(N, P, A, B, shift2, true, g, dErr);
+    const D3 c0{C.col[CC_T0X][c], C.col[CC_T0Y][c], C.col[CC_T0Z][c]};
+    const D3 c1{C.col[CC_T1X][c], C.col[CC_T1Y][c], C.col[CC_T1Z][c]};
+    const D3 n = qrot(quatFromCols(c0, c1, cross(c0, c1)), D3{1., 0., 0.});
+    const D3 n2{n.x * n.x, n.y * n.y, n.z * n.z};
+    double kn, kt;
+    if (sp.law == 0) {
+        kn = C.col[CC_P0][c];
+        kt = C.col[CC_P1][c];
+    } else {
+        kn = (3 / 2.) * C.col[CC_P0][c] * sqrt(-g.uN);
+        kt = C.col[CC_P1][c] * sqrt(g.uN < 0 ? -g.uN : 0);
+    }
+    const double uN0 = C.col[CC_UN0][c];
+    double l0 = fabs(g.r1) + uN0 / 2, l1 = fabs(g.r2) + uN0 / 2;
+    if (l0 < 0) l0 = l1;
+    if (l1 < 0) l1 = l0;
+    const D3 kTr{n2.x * (kn - kt) + kt, n2.y * (kn - kt) + kt, n2.z * (kn - kt) + kt};
+    const D3 rv{n2.y + n2.z, n2.z + n2.x, n2.x + n2.y};
+    const bool aIsLo = !(fl & C_SWAP);
+    if (ty != CT_FS) {
+        const double s0 = (l0 * l0) * kt;
+        const int sA = aIsLo ? I.slotLo[c] : I.slotHi[c];
+        kA[sA] = make_double4_32a(kTr.x, kTr.y, kTr.z, s0 * rv.x);
+        kB[sA] = make_double2(s0 * rv.y, s0 * rv.z);
+    }
+    const double s1 = (l1 * l1) * kt;
+    const int sB = aIsLo ? I.slotHi[c] : I.slotLo[c];
+    kA[sB] = make_double4_32a(kTr.x, kTr.y, kTr.z, s1 * rv.x);
+    kB[sB] = make_double2(s1 * rv.y, s1 * rv.z);
+}
+
+// DynDt::nodalCritDtSq (pkg/dem/DynDt.cpp:42-63) of the node of each sphere and wall: the sums
+// over the particle's end slots in slot order (ascending id of the other particle, the order of
+// Particle.contacts), then 2·min(m/|ktrans_i|, I_i/|krot_i|) over the free, stiff axes; fully
+// blocked nodes are always stable. The minimum over nodes (critDt_stiffness, :66-76) goes to
+// *out as the bits of a non-negative double.
+__global__ void __launch_bounds__(256) k_dyndt_nodes(DevNodes N, DevParticles P, DevIncidence I, const double4_32a* __restrict__ kA,
+                                                     const double2* __restrict__ kB, unsigned long long* __restrict__ out) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const double kInf = __longlong_as_double(0x7ff0000000000000LL);
+    double v = kInf;
+    if (p < P.n && P.shape[p] != WG_SHAPE_FACET) {
+        const uint32_t fl = N.flags[p];
+        if ((fl & F_DOF_ALL) != F_DOF_ALL) {
+            int e0, e1;
+            endRange(I, p, e0, e1);
+            D3 kt{0., 0., 0.}, kr{0., 0., 0.};
+            for (int e = e0; e < e1; e++) {
+                const double4_32a a = kA[e];
+                const double2 b = kB[e];
+                kt = kt + D3{a.x, a.y, a.z};
+                kr = kr + D3{a.w, b.x, b.y};
+            }
+            const double4_32a mi = N.minert[p];
+            const double m = mi.w, in[3] = {mi.x, mi.y, mi.z}, t[3] = {kt.x, kt.y, kt.z}, r[3] = {kr.x, kr.y, kr.z};
+            double ret = kInf;
+            for (int i = 0; i < 3; i++)
+                if (t[i] != 0 && m > 0. && !(fl & (1u << i))) {
+                    const double q = m / fabs(t[i]);
+                    ret = q < ret ? q : ret;
+                }
+            for (int i = 0; i < 3; i++)
+                if (r[i] != 0 && in[i] > 0. && !(fl & (8u << i))) {
+                    const double q = in[i] / fabs(r[i]);
+                    ret = q < ret ? q : ret;
+                }
+            v = 2 * ret;
+        }
+    }
+    // block minimum, then one atomic per block (non-negative doubles order like their bit patterns)
+    __shared__ double sm[256];
+    sm[threadIdx.x] = v;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            const double o = sm[threadIdx.x + w];
+            if (o < sm[threadIdx.x]) sm[threadIdx.x] = o;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) atomicMin(out, (unsigned long long)__double_as_longlong(sm[0]));
+}
+
+void launch_dyndt(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C, const DevIncidence& I,
+                  const ScenePar* sp, double4_32a* kA, double2* kB, unsigned long long* out, int* dErr, bool periodic) {
+    if (I.nAct > 0) {
+        const unsigned g = (unsigned)((I.nAct + 127) / 128);
+        if (periodic) k_dyndt_ends<true><<<g, 128, 0, st>>>(N, P, C, I, sp, kA, kB, dErr);
+        else k_dyndt_ends<false><<<g, 128, 0, st>>>(N, P, C, I, sp, kA, kB, dErr);
+    }
+    if (P.n > 0) k_dyndt_nodes<<<(P.n + 255) / 256, 256, 0, st>>>(N, P, I, kA, kB, out);
 }
 
 // Scene::doOneStep's step counter (core/Scene.cpp:386), advanced only by a step that completed.

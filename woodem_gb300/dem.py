@@ -724,5 +724,8 @@ class ContactLoop(Engine):
 
 
 class DynDt(PeriodicEngine):
-    """Accepted so that utils.defaultEngines scripts load; adaptive dt is not part of the GPU path."""
-    _attrs = {"maxRelInc": 1e-4, "dryRun": False}
+    """Adjusts Scene.dt from the current stiffness of the contacts (pkg/dem/DynDt.hpp:5-25), as the
+    engine after ContactLoop: the critical timestep is evaluated on the device, the new dt
+    (dtSafety times it, growing by at most maxRelInc per step) takes effect after the step. With
+    dryRun, only ``dt`` is set. FP64 precision mode; stepPeriod/virtPeriod activation."""
+    _attrs = {"maxRelInc": 1e-4, "dryRun": False, "dt": NaN}
