@@ -74,7 +74,7 @@ def test_box_idealelpl(gpu_lib):
 
 def test_periodic_virt_period(gpu_lib):
     """Periodic cell compressed and sheared, DynDt by simulation time (virtPeriod)."""
-    S = scenes.periodic_shear(n=600, seed=3, fill_fraction=0.45, shear_rate=0.0)
+    S = scenes.periodic_shear(n=600, seed=3, fill_fraction=0.4, shear_rate=0.0)
     g = -30.0 * np.eye(3)
     g[0, 2] = 40.0
     S.cell.nextGradV = g
