@@ -99,7 +99,16 @@ typedef struct wg_config {
     double dt_safety;           /* Scene.dtSafety */
     double next_dt;             /* Scene.nextDt (0 or NaN: none), taken as dt after the next step */
     double time;                /* Scene.time at upload */
+    int32_t track_energy;       /* Scene.trackEnergy (FP64 mode, one scene) */
+    int32_t kin_split;          /* Leapfrog.kinSplit */
 } wg_config;
+
+/* Scene.energy entries (EnergyTracker, core/EnergyTracker.hpp), in this order: the Leapfrog
+   energies (Leapfrog.cpp:52-97), then those of the contact laws (IdealElPl.cpp:25-90,
+   Hertz.cpp:150-179). kinetic, kinTrans, kinRot and elast hold the last step's value, the others
+   accumulate. */
+#define WG_ENERGY_N 10
+#define WG_ENERGY_NAMES {"kinetic", "kinTrans", "kinRot", "grav", "nonviscDamp", "elast", "plast", "broken", "viscN", "viscT"}
 
 /* DynDt state after a run: Scene.dt and nextDt, the engine's counters and DynDt.dt (the dry-run
    value), and the last critical timestep computed (Inf: no stiff contact). */
@@ -195,6 +204,10 @@ int wg_get_stats(wg_scene* s, wg_stats* out);
 int wg_get_dyndt(wg_scene* s, wg_dyndt_state* out);
 /* Scene.dt and Scene.nextDt set between runs (0 or NaN next_dt: none); one scene only. */
 int wg_set_dt(wg_scene* s, double dt, double next_dt);
+/* Scene.energy: the WG_ENERGY_N values and whether each entry exists (created by an addition);
+   wg_set_energy replaces them (EnergyTracker.clear or a checkpoint). */
+int wg_get_energy(wg_scene* s, double* values, int32_t* created);
+int wg_set_energy(wg_scene* s, const double* values, const int32_t* created);
 /* Set Cell.nextGradV (row-major) between runs (periodic scenes). */
 int wg_set_next_gradv(wg_scene* s, const double* next_gradv);
 int wg_get_cell(wg_scene* s, double* hsize, double* trsf, double* gradv);

@@ -39,6 +39,7 @@ def lib():
         "wo_get_nodes": (C.c_int, [C.c_void_p, P_D, P_D, P_D, P_D, P_D, P_D]),
         "wo_get_stats": (C.c_int, [C.c_void_p, C.POINTER(_native.wg_stats)]),
         "wo_get_dyndt": (C.c_int, [C.c_void_p, C.POINTER(_native.wg_dyndt_state)]),
+        "wo_get_energy": (C.c_int, [C.c_void_p, _native.P_D, _native.P_I32]),
         "wo_num_contacts": (C.c_int64, [C.c_void_p]),
         "wo_get_contacts": (C.c_int, [C.c_void_p, P_I32, P_I32, P_I32, P_I32, P_I32, P_D, P_D, P_D, P_D]),
         "wo_kinetic_energy": (C.c_int, [C.c_void_p, P_D]),
@@ -95,6 +96,13 @@ class Oracle:
         self._check(self.L.wo_get_nodes(self.h, p(out["pos"]), p(out["ori"]), p(out["vel"]), p(out["angVel"]),
                                         p(out["force"]), p(out["torque"])), "get_nodes")
         return out
+
+    def energy(self):
+        """Scene.energy as {name: value} of the entries that exist."""
+        v = np.zeros(len(_native.ENERGY_NAMES))
+        c = np.zeros(len(_native.ENERGY_NAMES), np.int32)
+        self._check(self.L.wo_get_energy(self.h, _native.ptr(v), _native.ptr(c, _native.P_I32)), "get_energy")
+        return {n: float(v[k]) for k, n in enumerate(_native.ENERGY_NAMES) if c[k]}
 
     def dyndt(self):
         st = _native.wg_dyndt_state()

@@ -107,6 +107,10 @@ static inline double mdet(const M3& a) {
            a.m[0][2] * (a.m[1][0] * a.m[2][1] - a.m[1][1] * a.m[2][0]);
 }
 // dual vector of a skew matrix, lib/base/Math.hpp:222-227
+static inline bool isIdentity(const M3& a) {
+    for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) if (a.m[i][j] != (i == j ? 1. : 0.)) return false;
+    return true;
+}
 static inline V3 leviCivita(const M3& m) { return V3(m.m[1][2] - m.m[2][1], m.m[2][0] - m.m[0][2], m.m[0][1] - m.m[1][0]); }
 
 struct Q { double w, x, y, z; };
@@ -163,6 +167,8 @@ enum { SH_SPHERE = 0, SH_WALL = 1, SH_FACET = 2 };
 enum { DOF_X = 1, DOF_Y = 2, DOF_Z = 4, DOF_RX = 8, DOF_RY = 16, DOF_RZ = 32, DOF_ALL = 63, DOF_RXRYRZ = 56,
        CLUMP_CLUMPED = 64, CLUMP_CLUMP = 128, ENERGY_SKIP = 256, GRAVITY_SKIP = 512, DAMPING_SKIP = 2048 };
 enum { HOMO_NONE = 0, HOMO_POS = 1, HOMO_VEL = 2, HOMO_VEL_2ND = 3, HOMO_GRADV2 = 4 };
+// Scene.energy entries (EnergyTracker), in the order of wo_get_energy
+enum { EN_KINETIC, EN_KINTRANS, EN_KINROT, EN_GRAV, EN_DAMP, EN_ELAST, EN_PLAST, EN_BROKEN, EN_VISCN, EN_VISCT, EN_N };
 
 struct Node {
     V3 pos; Q ori;
@@ -182,6 +188,9 @@ struct Contact {
     // FrictPhys / HertzPhys (pkg/dem/FrictMat.hpp:30-41, pkg/dem/Hertz.hpp:5-21)
     double kn, kt, tanPhi; V3 force, torque;
     double K, R, kt0, alpha_sqrtMK, gamma, alpha;
+    // energies added by the law in the current step: elast, plast, broken, viscN, viscT, and the
+    // number of elast and broken additions
+    double en[5]; int enN[2];
     size_t linIx;
     bool isReal() const { return geom && phys; }
     void reset() { geom = false; phys = false; }
@@ -292,6 +301,9 @@ struct Scene {
     std::vector<std::vector<Contact*>> pending;
     M3 stress;
     double sqrt5, viscAlphaConst; bool viscOn;
+    // Scene.energy and whether each entry exists
+    double energy[EN_N] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    int ecreated[EN_N] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
 
     ~Scene() { for (auto* c : linView) delete c; }
 
@@ -854,9 +866,18 @@ struct Scene {
         } else C->alpha_sqrtMK = 0.0;
     }
     // Law2_L6Geom_FrictPhys_IdealElPl::go, pkg/dem/IdealElPl.cpp:12-122 (no energy tracking, no rolling)
+    // (energy tracking: the "broken", "plast" and "elast" additions of :25-37, :58-72, :84-89)
     bool lawIdealElPl(Contact* C) {
         double uN = C->uN;
-        if (uN > 0 && !cfg.no_break) return false;
+        if (uN > 0 && !cfg.no_break) {
+            if (cfg.no_slip && cfg.track_energy) {
+                const double Fn = C->kn * uN;
+                const double fy = C->force.y + (cfg.dt * C->kt) * C->lvel.y, fz = C->force.z + (cfg.dt * C->kt) * C->lvel.z;
+                C->en[2] = .5 * ((Fn * Fn) / C->kn + (fy * fy + fz * fz) / C->kt);
+                C->enN[1] = 1;
+            }
+            return false;
+        }
         C->torque = V3();
         C->force.x = C->kn * uN;
         if (cfg.no_frict || C->tanPhi == 0.) { C->force.y = 0; C->force.z = 0; }
@@ -869,9 +890,17 @@ struct Scene {
                 double FtNorm = std::sqrt(C->force.y * C->force.y + C->force.z * C->force.z);
                 double ratio = maxFt / FtNorm;
                 if (FtNorm == 0.) ratio = 0.;
+                if (cfg.track_energy) C->en[1] = (C->kt != 0. ? (maxFt * (FtNorm - maxFt)) / C->kt : 0.);
                 C->force.y = C->force.y * ratio; C->force.z = C->force.z * ratio;
             }
             if (std::isnan(std::max(std::max(C->force.x, C->force.y), C->force.z))) throw std::runtime_error("NaN force in contact (message above)?!");
+        }
+        if (cfg.track_energy) {
+            double e = 0.5 * ((C->force.x * C->force.x) / C->kn +
+                              (C->kt != 0. ? (C->force.y * C->force.y + C->force.z * C->force.z) / C->kt : 0.));
+            if (std::isnan(e)) e = 0.;
+            C->en[0] = e;
+            C->enN[0] = 1;
         }
         return true;
     }
@@ -892,17 +921,26 @@ struct Scene {
         if (cfg.hz_no_attraction && Fne + Fnv > 0) Fnv = -Fne;
         double Fn = (Fne + Fna) + Fnv;
         C->force.x = Fn;
+        if (cfg.track_energy) C->en[3] = (Fnv * velN) * dt;  // viscN, :154
         C->kt = C->kt0 * std::sqrt(C->uN < 0 ? -C->uN : 0);
         double fy = (dt * C->kt) * vy, fz = (dt * C->kt) * vz;
         double maxFt = std::max(0., Fn) * C->tanPhi;
         if ((fy * fy + fz * fz) > maxFt * maxFt) {
             double FtNorm = std::sqrt(fy * fy + fz * fz);
             double ratio = maxFt / FtNorm;
+            if (cfg.track_energy) C->en[1] = ((.5 * (FtNorm - maxFt) + maxFt) * (FtNorm - maxFt)) / C->kt;  // plast, :166
             fy = fy * ratio; fz = fz * ratio;
         } else {
             fy = fy + eta * vy; fz = fz + eta * vz;
+            if (cfg.track_energy) C->en[4] = (eta * (vy * vy + vz * vz)) * dt;  // viscT, :171
         }
         C->force.y = fy; C->force.z = fz;
+        if (cfg.track_energy && C->uN < 0) {
+            // elast, :174-179: normalElasticEnergy(kn0,-uN) = kn0*(2/5)*pow(sqrt(-uN),5), with the
+            // power written as a product
+            C->en[0] = (kn0 * (2 / 5.)) * ((((su * su) * su) * su) * su) + (0.5 * (fy * fy + fz * fz)) / C->kt;
+            C->enN[0] = 1;
+        }
         return true;
     }
     // Contact::getForceTorqueBranch + ContactLoop::applyForceUninodal,
@@ -952,6 +990,8 @@ struct Scene {
         for (long i = 0; i < size; i++) {
             try {
                 Contact* C = linView[i];
+                for (int q = 0; q < 5; q++) C->en[q] = 0;
+                C->enN[0] = C->enN[1] = 0;
                 const bool fresh = (C->stepCreated == step);
                 if (!C->isReal() && fresh) {
                     // functor order: DEFINE_FUNCTOR_ORDER_2D(Facet,Sphere) / (Wall,Sphere) put the non-sphere first
@@ -997,6 +1037,25 @@ struct Scene {
             }
         }
         if (!ex.empty()) throw std::runtime_error(ex);
+        if (cfg.track_energy) {
+            // EnergyTracker::add of every contact, summed in linView order; elast is reset every step
+            double e[5] = {0, 0, 0, 0, 0};
+            int n[2] = {0, 0};
+            for (Contact* C : linView) {
+                for (int q = 0; q < 5; q++) e[q] = e[q] + C->en[q];
+                n[0] += C->enN[0]; n[1] += C->enN[1];
+            }
+            energy[EN_ELAST] = e[0];
+            if (n[0]) ecreated[EN_ELAST] = 1;
+            energy[EN_PLAST] += e[1];
+            if (e[1] != 0) ecreated[EN_PLAST] = 1;
+            energy[EN_BROKEN] += e[2];
+            if (n[1]) ecreated[EN_BROKEN] = 1;
+            energy[EN_VISCN] += e[3];
+            if (e[3] != 0) ecreated[EN_VISCN] = 1;
+            energy[EN_VISCT] += e[4];
+            if (e[4] != 0) ecreated[EN_VISCT] = 1;
+        }
         if (doStress) stress = mdiv(stress, mdet(cell.hSize));
         if (deterministic && cfg.apply_forces) {
             for (Contact* C : linView) {
@@ -1042,6 +1101,14 @@ struct Scene {
         const bool hasGravity = !isZero(g);
         long n = (long)nodes.size();
         std::string ex;
+        // Leapfrog.cpp:104: energies are tracked, except in the first step of a periodic scene
+        // whose gradV is not the identity
+        const bool track = cfg.track_energy && (!cfg.periodic || step > 0 || isIdentity(cell.gradV));
+        // per node: kinetic (Etrans+Erot, or Etrans and Erot with kinSplit), grav, nonviscDamp, and
+        // whether kinetic/grav were added
+        std::vector<double> eK0, eK1, eGr, eDm;
+        std::vector<char> eNk, eNg;
+        if (track) { eK0.assign(n, 0); eK1.assign(n, 0); eGr.assign(n, 0); eDm.assign(n, 0); eNk.assign(n, 0); eNg.assign(n, 0); }
 #pragma omp parallel for schedule(guided) num_threads(nThreads)
         for (long i = 0; i < n; i++) {
             Node& nd = nodes[i];
@@ -1049,6 +1116,25 @@ struct Scene {
             bool damp = (damping != 0. && !(nd.flags & DAMPING_SKIP));
             V3& f = nd.force; V3& t = nd.torque;
             const bool blockedAll = (nd.flags & DOF_ALL) == DOF_ALL;
+            V3 pvfE = nd.vel, pvaE = nd.angVel;
+            if (track) {
+                // Leapfrog::doDampingDissipation, :52-63 (velocities of the previous half step)
+                if (damp && !(nd.flags & ENERGY_SKIP)) {
+                    const double a = (std::abs(nd.vel.x) * std::abs(f.x) + std::abs(nd.vel.y) * std::abs(f.y)) + std::abs(nd.vel.z) * std::abs(f.z);
+                    const double b = (std::abs(nd.angVel.x) * std::abs(t.x) + std::abs(nd.angVel.y) * std::abs(t.y)) + std::abs(nd.angVel.z) * std::abs(t.z);
+                    eDm[i] = ((a * damping) * dt) + ((b * damping) * dt);
+                }
+                // Leapfrog::doGravityWork, :66-73
+                if (hasGravity && !(nd.flags & GRAVITY_SKIP)) {
+                    double gr = 0;
+                    if ((nd.flags & DOF_ALL) == 0) gr = ((-dot(g, nd.vel)) * nd.mass) * dt;
+                    else for (int k = 0; k < 3; k++) if (!(nd.flags & (1u << k))) gr = gr - ((g[k] * nd.vel[k]) * nd.mass) * dt;
+                    eGr[i] = gr; eNg[i] = 1;
+                }
+                // the fluctuation velocities Leapfrog computes for free nodes; for fully blocked
+                // nodes the reference reads vectors it never set, here the same expressions stand in
+                if (cfg.periodic) { pvfE = cell.pprevFluctVel(nd.pos, nd.vel, dt); pvaE = cell.pprevFluctAngVel(nd.angVel); }
+            }
             const bool aspherical = !(nd.inertia.x == nd.inertia.y && nd.inertia.y == nd.inertia.z);
             const bool useAspherical = aspherical && ((nd.flags & DOF_RXRYRZ) != DOF_RXRYRZ);
             if (useAspherical) {
@@ -1090,6 +1176,16 @@ struct Scene {
                     nd.vel = nd.vel + mul(dGradV, nd.pos);
                 } else if (homoDeform == HOMO_POS) nd.pos = nd.pos + mul(cell.nextGradV, nd.pos) * dt;
             }
+            if (track && !(nd.flags & ENERGY_SKIP)) {
+                // Leapfrog::doKineticEnergy, :75-97 (spherical nodes), on-step velocities
+                const V3 cv = pvfE + (.5 * dt) * linAccel, cw = pvaE + (.5 * dt) * angAccel;
+                const double et = (.5 * nd.mass) * sqn(cv);
+                double er = 0.5 * ((cw.x * (nd.inertia.x * cw.x) + cw.y * (nd.inertia.y * cw.y)) + cw.z * (nd.inertia.z * cw.z));
+                if (std::isnan(er) || std::isinf(std::max(std::max(nd.inertia.x, nd.inertia.y), nd.inertia.z))) er = 0;
+                if (cfg.kin_split) { eK0[i] = et; eK1[i] = er; }
+                else eK0[i] = et + er;
+                eNk[i] = 1;
+            }
             nd.pos = nd.pos + nd.vel * dt;
             V3 axis = nd.angVel;
             if (!isZero(axis)) {
@@ -1107,6 +1203,23 @@ struct Scene {
             }
         }
         if (!ex.empty()) throw std::runtime_error(ex);
+        if (cfg.track_energy) {
+            // EnergyTracker::add of every node, summed in node order; kinetic is reset every step
+            double k0 = 0, k1 = 0, gr = 0, dm = 0; int nk = 0, ng = 0;
+            if (track)
+                for (long i = 0; i < n; i++) { k0 = k0 + eK0[i]; k1 = k1 + eK1[i]; gr = gr + eGr[i]; dm = dm + eDm[i]; nk += eNk[i]; ng += eNg[i]; }
+            if (cfg.kin_split) {
+                energy[EN_KINTRANS] = k0; energy[EN_KINROT] = k1;
+                if (nk) ecreated[EN_KINTRANS] = ecreated[EN_KINROT] = 1;
+            } else {
+                energy[EN_KINETIC] = k0;
+                if (nk) ecreated[EN_KINETIC] = 1;
+            }
+            energy[EN_GRAV] += gr;
+            if (ng) ecreated[EN_GRAV] = 1;
+            energy[EN_DAMP] += dm;
+            if (dm != 0) ecreated[EN_DAMP] = 1;
+        }
     }
 
     // ------------------------------------------------------------ DynDt
@@ -1325,6 +1438,11 @@ int wo_get_stats(void* sp, wo_stats* o) {
     int64_t r = 0; for (auto* c : s->linView) r += c->isReal();
     o->n_real = r; o->time = s->time; o->verlet_dist = s->verletDist;
     for (int i = 0; i < 9; i++) o->stress[i] = s->stress.m[i / 3][i % 3];
+    return 0;
+}
+int wo_get_energy(void* sp, double* values, int32_t* created) {
+    Scene* s = (Scene*)sp;
+    for (int k = 0; k < EN_N; k++) { values[k] = s->energy[k]; created[k] = s->ecreated[k]; }
     return 0;
 }
 int wo_get_dyndt(void* sp, wo_dyndt_state* o) {

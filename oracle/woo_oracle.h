@@ -87,6 +87,8 @@ typedef struct wo_config {
     double dt_safety;           /* Scene.dtSafety */
     double next_dt;             /* Scene.nextDt (NaN: none) */
     double time;                /* Scene.time at the start */
+    int32_t track_energy;       /* Scene.trackEnergy */
+    int32_t kin_split;          /* Leapfrog.kinSplit */
 } wo_config;
 
 typedef struct wo_dyndt_state {
@@ -124,6 +126,9 @@ int wo_get_nodes(void* s, double* pos, double* ori, double* vel, double* ang_vel
                  double* force, double* torque);
 int wo_get_stats(void* s, wo_stats* out);
 int wo_get_dyndt(void* s, wo_dyndt_state* out);
+/* Scene.energy in the order kinetic, kinTrans, kinRot, grav, nonviscDamp, elast, plast, broken,
+   viscN, viscT, and whether each entry exists */
+int wo_get_energy(void* s, double* values, int32_t* created);
 int64_t wo_num_contacts(void* s);
 /* Contacts as (lo id, hi id) pairs plus state. Arrays sized n = wo_num_contacts.
    real: 1 if geom&&phys. fglob: global force on particle A (3/contact, zeros if

@@ -33,8 +33,12 @@ class wg_config(C.Structure):
         ("dyndt_step_period", C.c_int64), ("dyndt_n_do", C.c_int64), ("dyndt_n_done", C.c_int64),
         ("dyndt_step_last", C.c_int64), ("dyndt_step_prev", C.c_int64), ("dyndt_virt_period", C.c_double),
         ("dyndt_virt_last", C.c_double), ("dyndt_virt_prev", C.c_double), ("dyndt_max_rel_inc", C.c_double),
-        ("dt_safety", C.c_double), ("next_dt", C.c_double), ("time", C.c_double),
+        ("dt_safety", C.c_double), ("next_dt", C.c_double), ("time", C.c_double), ("track_energy", C.c_int32),
+        ("kin_split", C.c_int32),
     ]
+
+# Scene.energy entries in the order of WG_ENERGY_NAMES (include/woo_gpu.h)
+ENERGY_NAMES = ("kinetic", "kinTrans", "kinRot", "grav", "nonviscDamp", "elast", "plast", "broken", "viscN", "viscT")
 
 
 class wg_dyndt_state(C.Structure):
@@ -92,6 +96,8 @@ def lib():
         "wg_get_stats": (C.c_int, [C.c_void_p, C.POINTER(wg_stats)]),
         "wg_get_dyndt": (C.c_int, [C.c_void_p, C.POINTER(wg_dyndt_state)]),
         "wg_set_dt": (C.c_int, [C.c_void_p, C.c_double, C.c_double]),
+        "wg_get_energy": (C.c_int, [C.c_void_p, P_D, P_I32]),
+        "wg_set_energy": (C.c_int, [C.c_void_p, P_D, P_I32]),
         "wg_set_next_gradv": (C.c_int, [C.c_void_p, P_D]),
         "wg_set_scenes": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.POINTER(C.c_int64)]),
         "wg_get_scene_stats": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),

@@ -86,6 +86,10 @@ def compile_scene(S):
     cfg["dt_safety"] = float(S.dtSafety)
     cfg["next_dt"] = float(S.nextDt) if (S.nextDt > 0 and math.isfinite(S.nextDt)) else float("nan")
     cfg["time"] = float(S.time)
+    cfg["track_energy"] = int(bool(S.trackEnergy))
+    cfg["kin_split"] = int(bool(lf.kinSplit))
+    if S.trackEnergy and S.gpu.precision != "fp64":
+        raise NotImplementedError("energy tracking (Scene.trackEnergy) runs in the FP64 precision mode only")
     if dyn is not None:
         if dyn.realPeriod > 0:
             raise NotImplementedError("DynDt.realPeriod (wall-clock activation) is not part of the GPU path")
@@ -265,6 +269,7 @@ class Simulation:
             g = np.ascontiguousarray(np.asarray(self.S.cell.nextGradV, dtype=float).reshape(9))
             self.H.check(L.wg_set_next_gradv(h, _native.ptr(g)), "set_next_gradv")
         self._push_dt()
+        self._push_energy()
         self.H.check(L.wg_run(h, int(n)), "run")
         self.host_stale = True
         self._contacts = None
@@ -272,6 +277,7 @@ class Simulation:
         self.S.step = int(st.step)
         self.S.time = self.t0 + float(st.time)
         self._pull_dt()
+        self._pull_energy()
         for e in self.S.engines:
             from .dem import InsertionSortCollider
             if isinstance(e, InsertionSortCollider):
@@ -305,6 +311,30 @@ class Simulation:
             if not (S.dt > 0 and math.isfinite(S.dt)):
                 raise ValueError("Scene.dt must be positive and finite")
             self.H.check(self.H.L.wg_set_dt(self.H.h, float(S.dt), nxt), "set_dt")
+
+    def _push_energy(self):
+        """Scene.energy entries of the device changed on the host (set, added, cleared)."""
+        E = self.S.energy
+        if not (self.S.trackEnergy and E._dirty):
+            return
+        names = _native.ENERGY_NAMES
+        v = np.array([E._vals.get(k, 0.0) for k in names])
+        c = np.array([1 if k in E._vals else 0 for k in names], np.int32)
+        self.H.check(self.H.L.wg_set_energy(self.H.h, _native.ptr(v), _native.ptr(c, _native.P_I32)), "set_energy")
+        E._dirty = False
+
+    def _pull_energy(self):
+        if not self.S.trackEnergy:
+            return
+        names = _native.ENERGY_NAMES
+        v = np.zeros(len(names))
+        c = np.zeros(len(names), np.int32)
+        self.H.check(self.H.L.wg_get_energy(self.H.h, _native.ptr(v), _native.ptr(c, _native.P_I32)), "get_energy")
+        E = self.S.energy
+        for k, name in enumerate(names):
+            if c[k]:
+                E._vals[name] = float(v[k])
+        E._resettable.update(n for n in ("kinetic", "kinTrans", "kinRot", "elast") if n in E._vals)
 
     def _pull_dt(self):
         """Scene.dt/nextDt and the DynDt counters after a run."""

@@ -430,9 +430,10 @@ def buildLine(sim, table, line, results=""):
 
 
 def _runsAlone(S):
-    """Periodic scenes and scenes whose dt changes (DynDt, Scene.nextDt) are not batched."""
+    """Periodic scenes, scenes whose dt changes (DynDt, Scene.nextDt) and scenes that track energy
+    are not batched."""
     from .dem import DynDt
-    return bool(S.isPeriodic or any(isinstance(e, DynDt) and not e.dead for e in S.engines)
+    return bool(S.isPeriodic or S.trackEnergy or any(isinstance(e, DynDt) and not e.dead for e in S.engines)
                 or (S.nextDt > 0 and math.isfinite(S.nextDt)))
 
 

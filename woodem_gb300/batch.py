@@ -30,6 +30,8 @@ class Batch:
         self.arrays = [_plan.compile_scene(S) for S in self.scenes]
         if any(A.config.get("dyndt") or A.config["next_dt"] == A.config["next_dt"] for A in self.arrays):
             raise NotImplementedError("DynDt and Scene.nextDt are not supported in a Batch (each scene keeps its dt)")
+        if any(A.config.get("track_energy") for A in self.arrays):
+            raise NotImplementedError("energy tracking (Scene.trackEnergy) is not supported in a Batch")
         prec = {A.config["precision"] for A in self.arrays}
         if len(prec) != 1:
             raise ValueError("the scenes of a batch share one precision mode")

@@ -2,8 +2,8 @@
 
 ``save(S, path)`` writes one flat ``.npz`` file: the node state (pos, ori, vel, angVel, force,
 torque), the contact container with the persistent contact state (``wg_get_contact_state``),
-Scene.step/time/dt, the counters of a DynDt engine and the periodic cell (hSize, trsf, gradV,
-nextGradV). ``load(S, path)``
+Scene.step/time/dt, the counters of a DynDt engine, Scene.energy and the periodic cell (hSize,
+trsf, gradV, nextGradV). ``load(S, path)``
 puts that state into a scene built the same way (the same particles, materials and engines:
 a fingerprint of the compiled description is checked) and uploads it; the next step starts with
 a collider full run that keeps the state of the real contacts, as the reference's Scene.load
@@ -74,6 +74,8 @@ def save(S, path):
     dyn = _dyndt(S)
     if dyn is not None:
         meta["dyndt"] = {k: getattr(dyn, k) for k in _DYNDT_ATTRS}
+    if S.trackEnergy:
+        meta["energy"] = dict(S.energy._vals)
     if S.isPeriodic:
         for k in ("hSize", "trsf", "gradV", "nextGradV"):
             arrays["cell_" + k] = np.array(getattr(S.cell, k), dtype=float)
@@ -112,6 +114,10 @@ def load(S, path):
     if dyn is not None:
         for k, v in meta["dyndt"].items():
             setattr(dyn, k, v)
+    if "energy" in meta:
+        S.energy.clear()
+        for k, v in meta["energy"].items():
+            S.energy[k] = v
     if meta["periodic"]:
         S.cell.hSize = arrays["cell_hSize"]
         S.cell.trsf = arrays["cell_trsf"]

@@ -111,6 +111,76 @@ class Cell(Object):
         return float(np.linalg.det(np.asarray(self.hSize)))
 
 
+class EnergyTracker:
+    """Scene.energy (core/EnergyTracker.hpp:10-80): named energies. With Scene.trackEnergy the
+    entries of Leapfrog and of the contact laws are computed on the device every step and copied
+    here after each run; ``kinetic``/``kinTrans``/``kinRot``/``elast`` hold the last step's value,
+    the others accumulate. Entries set or added from Python stay on the host, except those of
+    the device, whose new values the next run starts from."""
+
+    def __init__(self):
+        self._vals = {}
+        self._resettable = set()
+        self._dirty = False  # device entries changed on the host since the last run
+
+    def _device_names(self):
+        from ._native import ENERGY_NAMES
+        return ENERGY_NAMES
+
+    def __len__(self):
+        return len(self._vals)
+
+    def __getitem__(self, name):
+        if name not in self._vals:
+            raise KeyError("Unknown energy name '%s'." % name)
+        return self._vals[name]
+
+    def __setitem__(self, name, val):
+        self._vals[name] = float(val)
+        if name in self._device_names():
+            self._dirty = True
+
+    def __contains__(self, name):
+        return name in self._vals
+
+    def __iter__(self):
+        return iter(self.keys())
+
+    def add(self, dE, name, reset=False):
+        """Accumulate dE into ``name`` (a resettable entry with reset=True)."""
+        self._vals[name] = self._vals.get(name, 0.0) + float(dE)
+        if reset:
+            self._resettable.add(name)
+        if name in self._device_names():
+            self._dirty = True
+
+    def clear(self):
+        self._vals.clear()
+        self._resettable.clear()
+        self._dirty = True
+
+    def keys(self):
+        return sorted(self._vals)
+
+    def items(self):
+        return [(k, self._vals[k]) for k in self.keys()]
+
+    def total(self):
+        t = 0.0
+        for k in self.keys():
+            t += self._vals[k]
+        return t
+
+    def relErr(self):
+        """Total energy divided by the sum of absolute values."""
+        sa = sum(abs(v) for v in self._vals.values())
+        return self.total() / sa if sa > 0 else 0.0
+
+    @property
+    def names(self):
+        return {k: i for i, k in enumerate(self.keys())}
+
+
 class Scene(Object):
     """Simulation scene. ``S.run(n)`` advances n steps of the engine list on the GPU."""
 
@@ -128,6 +198,7 @@ class Scene(Object):
         self._sim = None
         self._clock0 = time.time()
         self._labModules = {}
+        self.energy = EnergyTracker()
         super().__init__(**kw)
         self._fillDefaultTags()
         for f in self.fields:

@@ -58,6 +58,12 @@ struct HM {
     double m[3][3];
 };
 static HM hI() { HM r{}; r.m[0][0] = r.m[1][1] = r.m[2][2] = 1; return r; }
+static bool isIdentity(const HM& a) {
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++)
+            if (a.m[i][j] != (i == j ? 1. : 0.)) return false;
+    return true;
+}
 static HM hmul(const HM& A, const HM& B) {
     HM r{};
     for (int i = 0; i < 3; i++)
@@ -293,6 +299,8 @@ int Sim::prepareParamsFor(const wg_config& cfg, int64_t p0, int64_t p1, ScenePar
     p.stepBase = 0;
     p.stepEnd = (long long)1 << 62;
     p.dt = cfg.dt;
+    p.trackEnergy = cfg.track_energy != 0;
+    p.kinSplit = cfg.kin_split != 0;
     for (int i = 0; i < 3; i++) p.g[i] = cfg.gravity[i];
     p.hasGravity = (cfg.gravity[0] != 0 || cfg.gravity[1] != 0 || cfg.gravity[2] != 0);
     p.damping = cfg.damping;
@@ -696,6 +704,37 @@ int Sim::syncContacts() {
     return 0;
 }
 
+// Scratch of the per-step energy contributions, grown to the nodes and active contacts (called
+// outside stream capture: at the start of each chunk and after each full collider run).
+int Sim::ensureEnergyCapacity() {
+    Sim& S = *this;
+    if (!dEnergy) {
+        dEnergy = (double*)dalloc(sizeof(double) * WG_ENERGY_N);
+        dECreated = (int32_t*)dalloc(sizeof(int32_t) * WG_ENERGY_N);
+        dEPartial = (double*)dalloc(sizeof(double) * EN_CON_NCOL * 256);
+        if (!dEnergy || !dECreated || !dEPartial) return fail(WG_ERR_CUDA, "out of device memory (energy)");
+        WG_CUDA_TRY(cudaMemset(dEnergy, 0, sizeof(double) * WG_ENERGY_N));
+        WG_CUDA_TRY(cudaMemset(dECreated, 0, sizeof(int32_t) * WG_ENERGY_N));
+    }
+    if (eNode.cap < N.n) {
+        if (eNode.col) dfree(eNode.col);
+        eNode.cap = std::max<int64_t>(N.n, 1);
+        eNode.col = (double*)dalloc(sizeof(double) * EN_NODE_NCOL * eNode.cap);
+        if (!eNode.col) return fail(WG_ERR_CUDA, "out of device memory (energy)");
+    }
+    if (eCon.cap < I.nAct || !eCon.col) {
+        if (eCon.col) dfree(eCon.col);
+        eCon.cap = std::max<int64_t>(I.nAct + I.nAct / 2, 1024);
+        eCon.col = (double*)dalloc(sizeof(double) * EN_CON_NCOL * eCon.cap);
+        if (!eCon.col) return fail(WG_ERR_CUDA, "out of device memory (energy)");
+        if (graphExec) {  // captured with the old scratch
+            cudaGraphExecDestroy(graphExec);
+            graphExec = nullptr;
+        }
+    }
+    return 0;
+}
+
 // Scene.dt of the steps from the next one on (core/Scene.cpp:389): the scene parameters the
 // kernels read, and the cell integration of periodic runs (which takes cfg.dt)
 int Sim::applyDt(double ndt) {
@@ -802,7 +841,13 @@ int Sim::run(int64_t n) {
             launches += I.nHeavyFree > 0;
         }
         if (fp32) launch_leapfrog32(stream, N, P, I, dNodeC, sp, dFlags, fromEndsArg, dStep, cfg.periodic != 0);
-        else launch_leapfrog(stream, N, P, I, sp, dFlags, fromEndsArg, dStep, cfg.periodic != 0);
+        else if (trackE) {
+            cudaMemsetAsync(eNode.col, 0, sizeof(double) * EN_NODE_NCOL * eNode.cap, stream);
+            launch_leapfrog(stream, N, P, I, sp, dFlags, fromEndsArg, dStep, cfg.periodic != 0, &eNode);
+            launch_energy_sum(stream, eNode, 0, N.n, dEPartial, dEnergy, dECreated, dFlags, cfg.kin_split != 0);
+            launches += 2;
+        } else
+            launch_leapfrog(stream, N, P, I, sp, dFlags, fromEndsArg, dStep, cfg.periodic != 0);
         launches++;
     };
     auto stepContact = [&](ScenePar* sp) {
@@ -810,8 +855,15 @@ int Sim::run(int64_t n) {
         if (fp32)
             advanced = launch_contact_fp32(stream, concurrentContacts ? side : SideStream{}, N, P, C, I, K, dMats, sp, dStep, dFlags,
                                            nMixed, cfg.periodic != 0, anyLaw0, !facetsStatic, contactBlock != 0 ? contactBlock : -256);
-        else launch_contact_fp64(stream, N, P, C, I, dMats, sp, dStep, dFlags, cfg.periodic != 0,
-                                 (contactBlock > 0 && contactBlock <= 128) ? contactBlock : 128);  // launch bounds 128
+        else if (trackE) {
+            cudaMemsetAsync(eCon.col, 0, sizeof(double) * EN_CON_NCOL * eCon.cap, stream);
+            launch_contact_fp64(stream, N, P, C, I, dMats, sp, dStep, dFlags, cfg.periodic != 0,
+                                (contactBlock > 0 && contactBlock <= 128) ? contactBlock : 128, &eCon);
+            launch_energy_sum(stream, eCon, 1, I.nAct, dEPartial, dEnergy, dECreated, dFlags, false);
+            launches += 2;
+        } else
+            launch_contact_fp64(stream, N, P, C, I, dMats, sp, dStep, dFlags, cfg.periodic != 0,
+                                (contactBlock > 0 && contactBlock <= 128) ? contactBlock : 128);  // launch bounds 128
         if (!advanced) launch_advance(stream, dStep, dFlags);
         launches += advanced ? 1 : 2;
     };
@@ -821,6 +873,10 @@ int Sim::run(int64_t n) {
     while (done < n) {
         // the sphere-sphere kernel updates the packed state from here on
         if (K.n > 0) packDirty = true;
+        if (trackE) {
+            int r = ensureEnergyCapacity();
+            if (r) return r;
+        }
         int64_t k = std::min<int64_t>(n - done, maxChunk);
         // dt may change after a step (Scene.nextDt, DynDt): such a step ends its chunk
         if (std::isfinite(nextDt)) k = 1;
@@ -843,6 +899,9 @@ int Sim::run(int64_t n) {
                 X.cell.integrateAndUpdate(cfg.dt);
                 fillCellPar(X);
                 parSeq[j] = hPar;
+                // Leapfrog's reallyTrackEnergy (Leapfrog.cpp:104): not in the first step of a
+                // periodic scene unless gradV is the identity
+                parSeq[j].trackEnergy = cfg.track_energy && (step + j > 0 || isIdentity(X.cell.gradV));
                 cellInt[j] = X.cell;
                 X.cell.setNextGradV();
                 cellEnd[j] = X.cell;
@@ -918,6 +977,10 @@ int Sim::run(int64_t n) {
             WG_CUDA_TRY(cudaEventRecord(E[3 * maxChunk], stream));
             int r = collide_full_run(*this);
             if (r) return r;
+            if (trackE) {
+                r = ensureEnergyCapacity();
+                if (r) return r;
+            }
             initialized = true;
             forceFull = false;
             launches += 12;
@@ -1070,6 +1133,8 @@ int wg_set_config(wg_scene* s, const wg_config* c) {
     if (!(c->dt > 0) || !std::isfinite(c->dt)) return S.fail(WG_ERR_ARG, "Scene.dt must be positive and finite");
     if (c->dyndt && c->precision != WG_PREC_FP64)
         return S.fail(WG_ERR_UNSUPPORTED, "DynDt runs in the FP64 precision mode only");
+    if (c->track_energy && c->precision != WG_PREC_FP64)
+        return S.fail(WG_ERR_UNSUPPORTED, "energy tracking runs in the FP64 precision mode only");
     if (c->dyndt && !(c->dyndt_max_rel_inc > 0 && 1. + c->dyndt_max_rel_inc != 1.))
         return S.fail(WG_ERR_ARG, "DynDt: maxRelInc too small (1.0+maxRelInc==1.0)");  // DynDt::postLoad, DynDt.cpp:12-14
     S.cfg = *c;
@@ -1093,6 +1158,7 @@ int wg_set_config(wg_scene* s, const wg_config* c) {
     // Scene.nextDt: a positive finite value (0 and NaN: none)
     S.nextDt = (c->next_dt > 0 && std::isfinite(c->next_dt)) ? c->next_dt : std::numeric_limits<double>::quiet_NaN();
     S.timeAbs = c->time;
+    S.trackE = c->track_energy != 0;
     return WG_OK;
 }
 
@@ -1104,8 +1170,8 @@ int wg_set_scenes(wg_scene* s, int32_t n_scenes, const wg_config* cfgs, const in
     for (int k = 0; k < n_scenes; k++) {
         if (particle_start[k + 1] < particle_start[k]) return S.fail(WG_ERR_ARG, "particle_start must be non-decreasing");
         if (!(cfgs[k].dt > 0) || !std::isfinite(cfgs[k].dt)) return S.fail(WG_ERR_ARG, "Scene.dt must be positive and finite");
-        if (cfgs[k].dyndt || (cfgs[k].next_dt > 0 && std::isfinite(cfgs[k].next_dt)))
-            return S.fail(WG_ERR_UNSUPPORTED, "DynDt and Scene.nextDt are not supported in a batch of scenes");
+        if (cfgs[k].dyndt || (cfgs[k].next_dt > 0 && std::isfinite(cfgs[k].next_dt)) || cfgs[k].track_energy)
+            return S.fail(WG_ERR_UNSUPPORTED, "DynDt, Scene.nextDt and energy tracking are not supported in a batch of scenes");
     }
     S.nScenes = n_scenes;
     S.cfgs.assign(cfgs, cfgs + n_scenes);
@@ -1255,8 +1321,8 @@ int wg_slot_load(wg_scene* s, int32_t k, const wg_config* c, int64_t n, const do
     Sim& S = *SIM(s);
     int r = slotCheck(S, k);
     if (r) return r;
-    if (c->dyndt || (c->next_dt > 0 && std::isfinite(c->next_dt)))
-        return S.fail(WG_ERR_UNSUPPORTED, "DynDt and Scene.nextDt are not supported in serving slots");
+    if (c->dyndt || (c->next_dt > 0 && std::isfinite(c->next_dt)) || c->track_energy)
+        return S.fail(WG_ERR_UNSUPPORTED, "DynDt, Scene.nextDt and energy tracking are not supported in serving slots");
     const int64_t p0 = S.sceneStart[k], cap = S.sceneStart[k + 1] - p0;
     if (n > cap) return S.fail(WG_ERR_CAPACITY, "job larger than the slot");
     const int32_t matCap = (int32_t)(S.hDensity.size() / S.nScenes);
@@ -1548,6 +1614,37 @@ int wg_set_dt(wg_scene* s, double dt, double next_dt) {
             S.cfg.dt = dt;
     }
     S.nextDt = (next_dt > 0 && std::isfinite(next_dt)) ? next_dt : std::numeric_limits<double>::quiet_NaN();
+    return WG_OK;
+}
+
+int wg_get_energy(wg_scene* s, double* values, int32_t* created) {
+    if (!s || !values || !created) return WG_ERR_ARG;
+    Sim& S = *SIM(s);
+    if (!S.dEnergy) {
+        for (int k = 0; k < WG_ENERGY_N; k++) {
+            values[k] = 0;
+            created[k] = 0;
+        }
+        return WG_OK;
+    }
+    WG_CUDA_TRY(cudaSetDevice(S.device));
+    WG_CUDA_TRY(cudaMemcpy(values, S.dEnergy, sizeof(double) * WG_ENERGY_N, cudaMemcpyDeviceToHost));
+    WG_CUDA_TRY(cudaMemcpy(created, S.dECreated, sizeof(int32_t) * WG_ENERGY_N, cudaMemcpyDeviceToHost));
+    return WG_OK;
+}
+
+int wg_set_energy(wg_scene* s, const double* values, const int32_t* created) {
+    if (!s || !values || !created) return WG_ERR_ARG;
+    Sim& S = *SIM(s);
+    if (!S.haveCfg) return S.fail(WG_ERR_STATE, "wg_set_config must be called first");
+    if (!S.trackE) return S.fail(WG_ERR_STATE, "the scene does not track energy");
+    WG_CUDA_TRY(cudaSetDevice(S.device));
+    if (!S.dEnergy) {
+        int r = S.ensureEnergyCapacity();
+        if (r) return r;
+    }
+    WG_CUDA_TRY(cudaMemcpy(S.dEnergy, values, sizeof(double) * WG_ENERGY_N, cudaMemcpyHostToDevice));
+    WG_CUDA_TRY(cudaMemcpy(S.dECreated, created, sizeof(int32_t) * WG_ENERGY_N, cudaMemcpyHostToDevice));
     return WG_OK;
 }
 

@@ -13,7 +13,19 @@ namespace wg {
 
 // DemData flag bits (pkg/dem/Particle.hpp:179-186)
 enum : uint32_t {
-    F_DOF_ALL = 63u, F_DOF_RXRYRZ = 56u, F_CLUMPED = 64u, F_CLUMP = 128u, F_GRAVITY_SKIP = 512u, F_DAMPING_SKIP = 2048u
+    F_DOF_ALL = 63u, F_DOF_RXRYRZ = 56u, F_CLUMPED = 64u, F_CLUMP = 128u, F_ENERGY_SKIP = 256u, F_GRAVITY_SKIP = 512u,
+    F_DAMPING_SKIP = 2048u
+};
+// Energy tracking (Scene.trackEnergy, core/EnergyTracker.hpp): the slots of Scene.energy, in the
+// order of WG_ENERGY_NAMES (include/woo_gpu.h). kinetic/kinTrans/kinRot/elast are reset every step.
+enum { EN_KINETIC, EN_KINTRANS, EN_KINROT, EN_GRAV, EN_DAMP, EN_ELAST, EN_PLAST, EN_BROKEN, EN_VISCN, EN_VISCT, EN_N };
+// One step's contributions of each node / active contact, SoA columns of `cap` doubles each: the
+// values and, for the entries a zero addition creates, the number of additions.
+enum { EN_NODE_K0, EN_NODE_K1, EN_NODE_GRAV, EN_NODE_DAMP, EN_NODE_NKIN, EN_NODE_NGRAV, EN_NODE_NCOL };
+enum { EN_CON_ELAST, EN_CON_PLAST, EN_CON_BROKEN, EN_CON_VISCN, EN_CON_VISCT, EN_CON_NELAST, EN_CON_NBROKEN, EN_CON_NCOL };
+struct EnergyCols {
+    double* col = nullptr;  // EN_*_NCOL columns of cap entries
+    int64_t cap = 0;
 };
 // contact flag bits
 enum : uint32_t {
@@ -41,6 +53,7 @@ struct ScenePar {
     int32_t law, phys, reset, applyForces;
     int32_t trsfRenorm, approxMask, noRatch, noSlip, noBreak, noFrict, noAttraction, hzViscOn;
     int32_t periodic, homoDeform, hasGravity, evalStress;
+    int32_t trackEnergy, kinSplit;   // Leapfrog energies this step (reallyTrackEnergy), Leapfrog.kinSplit
     uint32_t loneMask;
     float dtF, ssDfAbsF;  // FP32 copies read by the FP32-force kernels
     float gH[3], gL[3];   // gravity as double-float pairs (g = gH + gL)
@@ -212,15 +225,19 @@ __host__ __device__ inline void unpackCellDist(int32_t p, int& a, int& b, int& c
 // several steps without waiting for each verlet test.
 // fromEnds = 0: take DemData.force/torque as stored (first step after the host wrote the state).
 void launch_leapfrog(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const ScenePar* sp,
-                     int* dFlags, int fromEnds, const long long* dStep, bool periodic);
+                     int* dFlags, int fromEnds, const long long* dStep, bool periodic, const EnergyCols* energy = nullptr);
 void launch_contact_fp64(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C,
                          const DevIncidence& I, const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dFlags,
-                         bool periodic, int block = 128);
+                         bool periodic, int block = 128, const EnergyCols* energy = nullptr);
 // perStep: only the heavy particles with a free DOF (guarded by the flags), before Leapfrog;
 // otherwise every particle's DemData.force/torque (reporting at the end of a run).
 void launch_forces(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const ScenePar* sp,
                    const int* dFlags, bool perStep);
 void launch_advance(cudaStream_t st, long long* dStep, const int* dFlags);
+// Adds one step's node (which = 0) or contact (which = 1) contributions in E to the energy slots;
+// partial holds EN_CON_NCOL * 256 doubles.
+void launch_energy_sum(cudaStream_t st, const EnergyCols& E, int which, int64_t n, double* partial, double* energy, int32_t* created,
+                       const int* dFlags, bool kinSplit);
 // DynDt: per-end stiffness of the real contacts into kA/kB (zeroed by the caller, I.endCap
 // entries), then the minimum over nodes of the squared critical timestep into *out (initialised
 // by the caller to the bits of +Inf). FP64 contact arrays.
@@ -376,6 +393,13 @@ struct Sim {
     double2* dKB = nullptr;
     int64_t kCap = 0;
     unsigned long long* dCrit = nullptr;
+    // energy tracking (one scene, FP64 mode): Scene.energy on the device and the per-step scratch
+    bool trackE = false;
+    EnergyCols eNode, eCon;
+    double* dEnergy = nullptr;      // WG_ENERGY_N values
+    int32_t* dECreated = nullptr;   // WG_ENERGY_N flags
+    double* dEPartial = nullptr;    // EN_CON_NCOL * 256 block partials
+    int ensureEnergyCapacity();
     // timing
     std::vector<cudaEvent_t> evPool;  // per queued step: before Leapfrog, before contacts, after
     cudaEvent_t ev[8];

@@ -61,9 +61,36 @@ __device__ __noinline__ void resetForce(DevNodes N, int i, double mass, bool gra
     N.force[i] = st4(G, 0.);
     N.torque[i] = make_double4_32a(0., 0., 0., 0.);
 }
-template <bool PERI>
+// Leapfrog::doDampingDissipation (Leapfrog.cpp:52-63): |v|.|F|*damping*dt + |w|.|T|*damping*dt
+// with the velocities of the previous half step and this step's force and torque.
+__device__ __noinline__ double energyDamp(D3 v, D3 f, D3 w, D3 t, double damping, double dt) {
+    const double a = (fabs(v.x) * fabs(f.x) + fabs(v.y) * fabs(f.y)) + fabs(v.z) * fabs(f.z);
+    const double b = (fabs(w.x) * fabs(t.x) + fabs(w.y) * fabs(t.y)) + fabs(w.z) * fabs(t.z);
+    return ((a * damping) * dt) + ((b * damping) * dt);
+}
+// Leapfrog::doGravityWork (Leapfrog.cpp:66-73): -g.v*m*dt over the free translations.
+__device__ __noinline__ double energyGrav(D3 g, D3 v, double mass, double dt, uint32_t flags) {
+    if ((flags & F_DOF_ALL) == 0) return ((-dot(g, v)) * mass) * dt;
+    double gr = 0;
+    if (!(flags & 1u)) gr = gr - ((g.x * v.x) * mass) * dt;
+    if (!(flags & 2u)) gr = gr - ((g.y * v.y) * mass) * dt;
+    if (!(flags & 4u)) gr = gr - ((g.z * v.z) * mass) * dt;
+    return gr;
+}
+// Leapfrog::doKineticEnergy (Leapfrog.cpp:75-97), spherical nodes: on-step fluctuation
+// velocities v + dt/2 a; returns (Etrans, Erot).
+__device__ __noinline__ double2 energyKin(D3 pvf, D3 pva, D3 la, D3 aa, double mass, D3 inertia, double dt) {
+    const D3 cv = pvf + (.5 * dt) * la, cw = pva + (.5 * dt) * aa;
+    const double et = (.5 * mass) * sqn(cv);
+    double er = 0.5 * ((cw.x * (inertia.x * cw.x) + cw.y * (inertia.y * cw.y)) + cw.z * (inertia.z * cw.z));
+    const double imax = smax(smax(inertia.x, inertia.y), inertia.z);
+    if (isnan(er) || isinf(imax)) er = 0;
+    return make_double2(et, er);
+}
+template <bool PERI, bool ENERGY>
 __global__ void __launch_bounds__(256) k_leapfrog(DevNodes N, DevParticles P, DevIncidence I, const ScenePar* __restrict__ spp,
-                                                  int* __restrict__ dFlags, int fromEnds, const long long* __restrict__ dStepC) {
+                                                  int* __restrict__ dFlags, int fromEnds, const long long* __restrict__ dStepC,
+                                                  EnergyCols E) {
     __shared__ EndStage<double4_32a, double2, 32> stage[8];
     if (halted(dFlags)) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -114,6 +141,23 @@ __global__ void __launch_bounds__(256) k_leapfrog(DevNodes N, DevParticles P, De
     const bool blockedAll = (flags & F_DOF_ALL) == F_DOF_ALL;
     const int homoDeform = PERI ? sp.homoDeform : -1;
     D3 linAccel{0, 0, 0};
+    D3 angAccelE{0, 0, 0}, pvfE = vel, pvaE = angVel;
+    if constexpr (ENERGY) {
+        if (sp.trackEnergy) {
+            if (damp && !(flags & F_ENERGY_SKIP)) E.col[EN_NODE_DAMP * E.cap + i] = energyDamp(vel, f, angVel, t, damping, dt);
+            if (sp.hasGravity && !(flags & F_GRAVITY_SKIP)) {
+                E.col[EN_NODE_GRAV * E.cap + i] = energyGrav(D3{sp.g[0], sp.g[1], sp.g[2]}, vel, mass, dt, flags);
+                E.col[EN_NODE_NGRAV * E.cap + i] = 1.;
+            }
+            // fluctuation velocities of the previous half step; a fully blocked node has none in the
+            // reference (it reads vectors it never set), here its velocities stand in
+            if (PERI) {
+                if (homoDeform == 2 || homoDeform == 3) pvfE = vel - mul(ldm(sp.gradV), pos);
+                else if (homoDeform == 4) pvfE = vel - mul(ldm(sp.gradV), pos - (dt / 2) * vel);
+                if (homoDeform == 4) pvaE = angVel - D3{sp.spinVec[0], sp.spinVec[1], sp.spinVec[2]};
+            }
+        }
+    }
     if (!blockedAll) {
         if ((flags & F_DOF_ALL) == 0) linAccel = f / mass;
         else linAccel = linAccelPartial(f, mass, flags);
@@ -135,6 +179,7 @@ __global__ void __launch_bounds__(256) k_leapfrog(DevNodes N, DevParticles P, De
             else angAccel = angAccelPartial(t, inertia, flags);
             if (damp) angAccel = dampAccel(angAccel, t, pva, damping, dt);
             angVel = angVel + dt * angAccel;
+            if constexpr (ENERGY) angAccelE = angAccel;
             if (PERI && homoDeform == 4) angVel = angVel - D3{sp.deltaSpinVec[0], sp.deltaSpinVec[1], sp.deltaSpinVec[2]};
         }
     } else {
@@ -146,6 +191,17 @@ __global__ void __launch_bounds__(256) k_leapfrog(DevNodes N, DevParticles P, De
             vel = vel + mul(ldm(sp.dGradV), pos);
         } else if (homoDeform == 1) {
             pos = pos + mul(ldm(sp.nextGradV), pos) * dt;
+        }
+    }
+    if constexpr (ENERGY) {
+        if (sp.trackEnergy && !(flags & F_ENERGY_SKIP)) {
+            const double2 ek = energyKin(pvfE, pvaE, linAccel, angAccelE, mass, inertia, dt);
+            if (sp.kinSplit) {
+                E.col[EN_NODE_K0 * E.cap + i] = ek.x;
+                E.col[EN_NODE_K1 * E.cap + i] = ek.y;
+            } else
+                E.col[EN_NODE_K0 * E.cap + i] = ek.x + ek.y;
+            E.col[EN_NODE_NKIN * E.cap + i] = 1.;
         }
     }
     pos = pos + vel * dt;
@@ -173,10 +229,17 @@ __global__ void __launch_bounds__(256) k_leapfrog(DevNodes N, DevParticles P, De
 }
 
 void launch_leapfrog(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const ScenePar* sp,
-                     int* dFlags, int fromEnds, const long long* dStep, bool periodic) {
+                     int* dFlags, int fromEnds, const long long* dStep, bool periodic, const EnergyCols* energy) {
     if (N.n == 0) return;
-    if (periodic) k_leapfrog<true><<<(N.n + 255) / 256, 256, 0, st>>>(N, P, I, sp, dFlags, fromEnds, dStep);
-    else k_leapfrog<false><<<(N.n + 255) / 256, 256, 0, st>>>(N, P, I, sp, dFlags, fromEnds, dStep);
+    const unsigned g = (N.n + 255) / 256;
+    const EnergyCols E = energy ? *energy : EnergyCols{};
+    if (energy) {
+        if (periodic) k_leapfrog<true, true><<<g, 256, 0, st>>>(N, P, I, sp, dFlags, fromEnds, dStep, E);
+        else k_leapfrog<false, true><<<g, 256, 0, st>>>(N, P, I, sp, dFlags, fromEnds, dStep, E);
+    } else {
+        if (periodic) k_leapfrog<true, false><<<g, 256, 0, st>>>(N, P, I, sp, dFlags, fromEnds, dStep, E);
+        else k_leapfrog<false, false><<<g, 256, 0, st>>>(N, P, I, sp, dFlags, fromEnds, dStep, E);
+    }
 }
 
 // ---------------------------------------------------------------------------------- ContactLoop
@@ -275,10 +338,11 @@ __device__ __noinline__ double2 capShear(double ft1, double ft2, double maxFt, b
     return make_double2(ft1 * ratio, ft2 * ratio);
 }
 
-template <bool PERI>
+template <bool PERI, bool ENERGY>
 __global__ void __launch_bounds__(128) k_contact_fp64(DevNodes N, DevParticles P, DevContacts C, DevIncidence I,
                                                      const double4_32a* __restrict__ mats, const ScenePar* __restrict__ spp,
-                                                     const long long* __restrict__ dStep, int* __restrict__ dFlags) {
+                                                     const long long* __restrict__ dStep, int* __restrict__ dFlags,
+                                                     EnergyCols E) {
     if (dFlags[FL_FULL] || halted(dFlags)) {
         // the collider runs before this step's contacts; the steps queued after it wait
         if (blockIdx.x == 0 && threadIdx.x == 0) dFlags[FL_HALT] = 1;
@@ -400,10 +464,20 @@ __global__ void __launch_bounds__(128) k_contact_fp64(DevNodes N, DevParticles P
     }
     const double uN = g.uN;
     bool keep = true;
+    // energies of this contact in this step (EnergyTracker adds, IdealElPl.cpp:25-37,58-90,
+    // Hertz.cpp:154-179)
+    double eElast = 0, ePlast = 0, eBroken = 0, eViscN = 0, eViscT = 0, nElast = 0, nBroken = 0;
     if (sp.law == 0) {
         // Law2_L6Geom_FrictPhys_IdealElPl::go, pkg/dem/IdealElPl.cpp:18-81 (kn kt tanPhi = ph0 ph1 ph2)
-        if (uN > 0 && !sp.noBreak) keep = false;
-        else {
+        if (uN > 0 && !sp.noBreak) {
+            keep = false;
+            if (ENERGY && sp.noSlip) {
+                // the broken contact's current elastic potential is lost
+                const double bf = ph0 * uN, b1 = ft1 + (dt * ph1) * lvel.y, b2 = ft2 + (dt * ph1) * lvel.z;
+                eBroken = .5 * ((bf * bf) / ph0 + (b1 * b1 + b2 * b2) / ph1);
+                nBroken = 1;
+            }
+        } else {
             fn = ph0 * uN;
             if (sp.noFrict || ph2 == 0.) {
                 ft1 = 0;
@@ -413,11 +487,17 @@ __global__ void __launch_bounds__(128) k_contact_fp64(DevNodes N, DevParticles P
                 ft2 = ft2 + (dt * ph1) * lvel.z;
                 const double maxFt = fabs(fn) * ph2;
                 if ((ft1 * ft1 + ft2 * ft2) > maxFt * maxFt && !sp.noSlip) {
+                    if (ENERGY) ePlast = (ph1 != 0. ? (maxFt * (sqrt(ft1 * ft1 + ft2 * ft2) - maxFt)) / ph1 : 0.);
                     const double2 q = capShear(ft1, ft2, maxFt, true);
                     ft1 = q.x;
                     ft2 = q.y;
                 }
                 if (isnan(fn) || isnan(ft1) || isnan(ft2)) atomicCAS(dErr, 0, 101);  // "NaN force in contact"
+            }
+            if (ENERGY) {
+                eElast = 0.5 * ((fn * fn) / ph0 + (ph1 != 0. ? (ft1 * ft1 + ft2 * ft2) / ph1 : 0.));
+                if (isnan(eElast)) eElast = 0.;
+                nElast = 1;
             }
         }
     } else {
@@ -431,19 +511,40 @@ __global__ void __launch_bounds__(128) k_contact_fp64(DevNodes N, DevParticles P
             double Fnv = eta * lvel.x;
             if (sp.noAttraction && Fne + Fnv > 0) Fnv = -Fne;
             fn = (Fne + Fna) + Fnv;
+            if (ENERGY) eViscN = (Fnv * lvel.x) * dt;
             const double kt = ph1 * sqrt(uN < 0 ? -uN : 0);
             ft1 = (dt * kt) * lvel.y;
             ft2 = (dt * kt) * lvel.z;
             const double maxFt = smax(0., fn) * ph2;
             if ((ft1 * ft1 + ft2 * ft2) > maxFt * maxFt) {
+                if (ENERGY) {
+                    const double fN = sqrt(ft1 * ft1 + ft2 * ft2);
+                    ePlast = ((.5 * (fN - maxFt) + maxFt) * (fN - maxFt)) / kt;
+                }
                 const double2 q = capShear(ft1, ft2, maxFt, false);
                 ft1 = q.x;
                 ft2 = q.y;
             } else {
                 ft1 = ft1 + eta * lvel.y;
                 ft2 = ft2 + eta * lvel.z;
+                if (ENERGY) eViscT = (eta * (lvel.y * lvel.y + lvel.z * lvel.z)) * dt;
+            }
+            if (ENERGY && uN < 0) {
+                // normalElasticEnergy(kn0, -uN) = kn0*(2/5)*(-uN)^(5/2) (Hertz.hpp:48), pow(sqrt(x),5) as s^5
+                eElast = (ph0 * (2 / 5.)) * ((((su * su) * su) * su) * su) + (0.5 * (ft1 * ft1 + ft2 * ft2)) / kt;
+                nElast = 1;
             }
         }
+    }
+    if constexpr (ENERGY) {
+        const int64_t cp = E.cap;
+        E.col[EN_CON_ELAST * cp + rk] = eElast;
+        E.col[EN_CON_PLAST * cp + rk] = ePlast;
+        E.col[EN_CON_BROKEN * cp + rk] = eBroken;
+        E.col[EN_CON_VISCN * cp + rk] = eViscN;
+        E.col[EN_CON_VISCT * cp + rk] = eViscT;
+        E.col[EN_CON_NELAST * cp + rk] = nElast;
+        E.col[EN_CON_NBROKEN * cp + rk] = nBroken;
     }
     if (!keep) {
         // ContactContainer::requestRemoval: geom and phys reset, contact pending for the collider
@@ -488,12 +589,92 @@ __global__ void __launch_bounds__(128) k_contact_fp64(DevNodes N, DevParticles P
 }
 
 void launch_contact_fp64(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C, const DevIncidence& I,
-                         const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dFlags, bool periodic, int block) {
+                         const double4_32a* mats, const ScenePar* sp, const long long* dStep, int* dFlags, bool periodic, int block,
+                         const EnergyCols* energy) {
     const int bs = block;
     // launched even without contacts: it raises FL_HALT when a full run is due
     const unsigned g = (unsigned)std::max<int64_t>(1, (I.nAct + bs - 1) / bs);
-    if (periodic) k_contact_fp64<true><<<g, bs, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags);
-    else k_contact_fp64<false><<<g, bs, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags);
+    const EnergyCols E = energy ? *energy : EnergyCols{};
+    if (energy) {
+        if (periodic) k_contact_fp64<true, true><<<g, bs, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags, E);
+        else k_contact_fp64<false, true><<<g, bs, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags, E);
+    } else {
+        if (periodic) k_contact_fp64<true, false><<<g, bs, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags, E);
+        else k_contact_fp64<false, false><<<g, bs, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags, E);
+    }
+}
+
+// ---------------------------------------------------------------------------------- energy sums
+// The step's contributions of every node or active contact (columns of E), summed per column in
+// a fixed order (grid-stride per thread, a shared-memory tree per block, then the blocks in order)
+// and added to Scene.energy: the resettable entries take the step's sum, the others accumulate.
+// An entry exists once a contribution was added (a zero one for the entries that a zero creates).
+// Nothing is added for a step whose kernels did not run (halted; for contacts also a step waiting
+// for the collider, whose contact loop runs after it).
+constexpr int kEnergyBlocks = 256;
+__global__ void __launch_bounds__(256) k_energy_partial(EnergyCols E, int ncol, int64_t n, double* __restrict__ partial,
+                                                        const int* __restrict__ dFlags) {
+    __shared__ double sm[256];
+    if (halted(dFlags)) return;
+    for (int c = 0; c < ncol; c++) {
+        double a = 0;
+        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+            a = a + E.col[c * E.cap + i];
+        sm[threadIdx.x] = a;
+        __syncthreads();
+        for (int w = 128; w > 0; w >>= 1) {
+            if (threadIdx.x < w) sm[threadIdx.x] = sm[threadIdx.x] + sm[threadIdx.x + w];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) partial[c * gridDim.x + blockIdx.x] = sm[0];
+        __syncthreads();
+    }
+}
+// which = 0: node columns, 1: contact columns
+__global__ void k_energy_final(const double* __restrict__ partial, int nb, int which, double* __restrict__ energy,
+                               int32_t* __restrict__ created, const int* __restrict__ dFlags, int kinSplit) {
+    if (threadIdx.x != 0 || halted(dFlags) || (which == 1 && dFlags[FL_FULL])) return;
+    auto sum = [&](int c) {
+        double a = 0;
+        for (int b = 0; b < nb; b++) a = a + partial[c * nb + b];
+        return a;
+    };
+    if (which == 0) {
+        const double k0 = sum(EN_NODE_K0), k1 = sum(EN_NODE_K1), gr = sum(EN_NODE_GRAV), dm = sum(EN_NODE_DAMP);
+        const bool kin = sum(EN_NODE_NKIN) > 0, grav = sum(EN_NODE_NGRAV) > 0;
+        if (kinSplit) {
+            energy[EN_KINTRANS] = k0;
+            energy[EN_KINROT] = k1;
+            if (kin) created[EN_KINTRANS] = created[EN_KINROT] = 1;
+        } else {
+            energy[EN_KINETIC] = k0;
+            if (kin) created[EN_KINETIC] = 1;
+        }
+        energy[EN_GRAV] += gr;
+        if (grav) created[EN_GRAV] = 1;
+        energy[EN_DAMP] += dm;
+        if (dm != 0) created[EN_DAMP] = 1;
+    } else {
+        const double el = sum(EN_CON_ELAST), pl = sum(EN_CON_PLAST), br = sum(EN_CON_BROKEN), vn = sum(EN_CON_VISCN),
+                     vt = sum(EN_CON_VISCT);
+        energy[EN_ELAST] = el;
+        if (sum(EN_CON_NELAST) > 0) created[EN_ELAST] = 1;
+        energy[EN_PLAST] += pl;
+        if (pl != 0) created[EN_PLAST] = 1;
+        energy[EN_BROKEN] += br;
+        if (sum(EN_CON_NBROKEN) > 0) created[EN_BROKEN] = 1;
+        energy[EN_VISCN] += vn;
+        if (vn != 0) created[EN_VISCN] = 1;
+        energy[EN_VISCT] += vt;
+        if (vt != 0) created[EN_VISCT] = 1;
+    }
+}
+void launch_energy_sum(cudaStream_t st, const EnergyCols& E, int which, int64_t n, double* partial, double* energy, int32_t* created,
+                       const int* dFlags, bool kinSplit) {
+    const int ncol = which == 0 ? (int)EN_NODE_NCOL : (int)EN_CON_NCOL;
+    const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(kEnergyBlocks, (n + 255) / 256));
+    k_energy_partial<<<nb, 256, 0, st>>>(E, ncol, n, partial, dFlags);
+    k_energy_final<<<1, 32, 0, st>>>(partial, nb, which, energy, created, dFlags, kinSplit ? 1 : 0);
 }
 
 // ---------------------------------------------------------------------------------- force sum

@@ -73,8 +73,8 @@ class SlotPool:
         nd, pa, mt = A.nodes, A.particles, A.materials
         if np.any(pa["nodes"][:, 0] != np.arange(A.n_particles)) or A.n_nodes != A.n_particles:
             raise ValueError("slot jobs have one node per particle, in particle order")
-        if A.config.get("dyndt"):
-            raise NotImplementedError("DynDt is not supported in serving slots (each slot keeps its dt)")
+        if A.config.get("dyndt") or A.config.get("track_energy"):
+            raise NotImplementedError("DynDt and energy tracking are not supported in serving slots")
         p = _native.ptr
         cfg = _native.make_config(_native.wg_config, A.config)
         self.H.check(L.wg_slot_load(h, k, C.cast(C.byref(cfg), C.c_void_p), A.n_particles, p(nd["pos"]), p(nd["ori"]), p(nd["vel"]),
