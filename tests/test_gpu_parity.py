@@ -5,11 +5,10 @@ FP64 plain mode performs the reference's operations in the reference's order on 
 forces per particle in the order of the reference's deterministic pass
 (ContactLoop.cpp:250-257). The tests therefore require BITWISE equality of positions,
 velocities, forces, torques and of the contact set with its per-contact state, step after
-step. Exceptions, with the tolerance written in the test:
+step (particles with more than 64 contacts included: their slots are added one after the other
+in slot order, component by component). Exception, with the tolerance written in the test:
   * node orientations (the quaternion update uses sin/cos, whose last bit may differ between
-    the CUDA and the C library): |dq| <= 1e-14;
-  * the force on walls with more than 64 contacts, which the GPU sums with a fixed tree
-    instead of the serial order: relative 1e-12 (walls are fixed, this never feeds back).
+    the CUDA and the C library): |dq| <= 1e-14.
 """
 import numpy as np
 import pytest
@@ -36,13 +35,8 @@ def _compare_nodes(g, o, shapes, nodes_of, heavy_ok=True):
     for k in ("pos", "vel", "angVel"):
         assert np.array_equal(g[k], o[k]), "%s differs (max abs %g)" % (k, np.max(np.abs(g[k] - o[k])))
     assert np.max(np.abs(g["ori"] - o["ori"])) <= 1e-14
-    walls = nodes_of[shapes == 1]
-    sel = np.ones(len(g["force"]), bool)
-    sel[walls] = False
     for k in ("force", "torque"):
-        assert np.array_equal(g[k][sel], o[k][sel]), "%s differs (max abs %g)" % (k, np.max(np.abs(g[k][sel] - o[k][sel])))
-        if len(walls):
-            np.testing.assert_allclose(g[k][walls], o[k][walls], rtol=1e-12, atol=1e-12 * max(1.0, np.abs(o[k][walls]).max()))
+        assert np.array_equal(g[k], o[k]), "%s differs (max abs %g)" % (k, np.max(np.abs(g[k] - o[k])))
 
 
 def _compare_contacts(cg, co):

@@ -706,39 +706,31 @@ __global__ void __launch_bounds__(256) k_forces(DevNodes N, DevParticles P, DevI
     }
 }
 
-// Particles with many contacts (walls): one block each, fixed-shape tree sum (deterministic,
-// same result on every run; rounding differs from the serial order only for these particles).
-__global__ void k_forces_heavy(DevNodes N, DevIncidence I, const int32_t* __restrict__ list, const ScenePar* __restrict__ spp,
-                               const int* __restrict__ dFlags) {
+// Particles with many end slots (walls, crowded spheres): one warp each, lane q < 6 adds
+// component q of the particle's slots one after the other in slot order, starting from m*g
+// (force) or 0 (torque): the order of the reference's deterministic pass, the same as the
+// Leapfrog kernel's sum for the other particles, so FP64 results stay bitwise. Six dependent
+// chains per particle; only particles with a free DOF take this path every step.
+__global__ void __launch_bounds__(128) k_forces_heavy(DevNodes N, DevIncidence I, const int32_t* __restrict__ list, int n,
+                                                      const ScenePar* __restrict__ spp, const int* __restrict__ dFlags) {
     if (dFlags && halted(dFlags)) return;
-    const int p = list[blockIdx.x];
+    const int w = blockIdx.x * 4 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (w >= n || lane >= 6) return;
+    const int p = list[w];
     const ScenePar& sp = spp[sceneOfN(N, p)];
     int e0, e1;
     endRange(I, p, e0, e1);
-    D3 F{0, 0, 0}, T{0, 0, 0};
-    for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-        const double4_32a a = I.endA[e];
-        const double2 b = I.endB[e];
-        F = F + D3{a.x, a.y, a.z};
-        T = T + D3{a.w, b.x, b.y};
-    }
-    __shared__ double sh[6][256];
-    sh[0][threadIdx.x] = F.x; sh[1][threadIdx.x] = F.y; sh[2][threadIdx.x] = F.z;
-    sh[3][threadIdx.x] = T.x; sh[4][threadIdx.x] = T.y; sh[5][threadIdx.x] = T.z;
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s)
-            for (int q = 0; q < 6; q++) sh[q][threadIdx.x] = sh[q][threadIdx.x] + sh[q][threadIdx.x + s];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        const uint32_t flags = N.flags[p];
-        const double mass = N.minert[p].w;
-        D3 G{0, 0, 0};
-        if (sp.hasGravity && !(flags & F_GRAVITY_SKIP)) G = mass * D3{sp.g[0], sp.g[1], sp.g[2]};
-        N.force[p] = st4(G + D3{sh[0][0], sh[1][0], sh[2][0]}, 0.);
-        N.torque[p] = st4(D3{sh[3][0], sh[4][0], sh[5][0]}, 0.);
-    }
+    double acc = 0;
+    if (lane < 3 && sp.hasGravity && !(N.flags[p] & F_GRAVITY_SKIP)) acc = N.minert[p].w * sp.g[lane];
+    const double* a = reinterpret_cast<const double*>(I.endA);
+    const double* b = reinterpret_cast<const double*>(I.endB);
+    for (int e = e0; e < e1; e++) acc = acc + (lane < 4 ? a[4 * (int64_t)e + lane] : b[2 * (int64_t)e + (lane - 4)]);
+    double* f = reinterpret_cast<double*>(N.force + p);
+    double* t = reinterpret_cast<double*>(N.torque + p);
+    if (lane < 3) f[lane] = acc;
+    else t[lane - 3] = acc;
+    if (lane == 0) f[3] = 0.;
+    if (lane == 3) t[3] = 0.;
 }
 
 // ContactLoop.stress for periodic scenes (ContactLoop.cpp:211-247): sum over real contacts of
@@ -935,11 +927,11 @@ void launch_forces(cudaStream_t st, const DevNodes& N, const DevParticles& P, co
                    const int* dFlags, bool perStep) {
     if (P.n == 0) return;
     if (perStep) {
-        if (I.nHeavyFree > 0) k_forces_heavy<<<I.nHeavyFree, 256, 0, st>>>(N, I, I.heavyFree, sp, dFlags);
+        if (I.nHeavyFree > 0) k_forces_heavy<<<(I.nHeavyFree + 3) / 4, 128, 0, st>>>(N, I, I.heavyFree, I.nHeavyFree, sp, dFlags);
         return;
     }
     k_forces<<<(P.n + 255) / 256, 256, 0, st>>>(N, P, I, sp);
-    if (I.nHeavy > 0) k_forces_heavy<<<I.nHeavy, 256, 0, st>>>(N, I, I.heavy, sp, nullptr);
+    if (I.nHeavy > 0) k_forces_heavy<<<(I.nHeavy + 3) / 4, 128, 0, st>>>(N, I, I.heavy, I.nHeavy, sp, nullptr);
 }
 
 void launch_advance(cudaStream_t st, long long* dStep, const int* dFlags) { k_step_advance<<<1, 1, 0, st>>>(dStep, dFlags); }
