@@ -524,8 +524,8 @@ int Sim::upload() {
         P.scene = (int32_t*)dalloc(sizeof(int32_t) * nPar);
         N.scene = (int32_t*)dalloc(sizeof(int32_t) * nSlots);
         if (!N.scene) return fail(WG_ERR_CUDA, "out of device memory (scene)");
-        WG_CUDA_TRY(cudaMemcpy(P.scene, hSceneOfPar.data(), sizeof(int32_t) * nPar, cudaMemcpyHostToDevice));
-        WG_CUDA_TRY(cudaMemcpy(N.scene, nsc.data(), sizeof(int32_t) * nSlots, cudaMemcpyHostToDevice));
+        WG_CUDA_TRY(cudaMemcpyAsync(P.scene, hSceneOfPar.data(), sizeof(int32_t) * nPar, cudaMemcpyHostToDevice, S.stream));
+        WG_CUDA_TRY(cudaMemcpyAsync(N.scene, nsc.data(), sizeof(int32_t) * nSlots, cudaMemcpyHostToDevice, S.stream));
     }
     dStep = (long long*)dalloc(sizeof(long long));
     dFlags = (int*)dalloc(sizeof(int) * 4);
@@ -535,28 +535,28 @@ int Sim::upload() {
     WG_CUDA_TRY(cudaMallocHost(&hFlags, sizeof(int) * 4 + sizeof(long long)));
     std::vector<double4_32a> mats(hDensity.size());
     for (size_t m = 0; m < hDensity.size(); m++) mats[m] = make_double4_32a(hDensity[m], hYoung[m], hTanPhi[m], hKtDivKn[m]);
-    WG_CUDA_TRY(cudaMemcpy(N.posr, posr.data(), sizeof(double4_32a) * nSlots, cudaMemcpyHostToDevice));
-    WG_CUDA_TRY(cudaMemcpy(N.vel, vel.data(), sizeof(double4_32a) * nSlots, cudaMemcpyHostToDevice));
-    WG_CUDA_TRY(cudaMemcpy(N.angv, angv.data(), sizeof(double4_32a) * nSlots, cudaMemcpyHostToDevice));
-    WG_CUDA_TRY(cudaMemcpy(N.ori, ori.data(), sizeof(double4_32a) * nSlots, cudaMemcpyHostToDevice));
-    WG_CUDA_TRY(cudaMemcpy(N.force, force.data(), sizeof(double4_32a) * nSlots, cudaMemcpyHostToDevice));
-    WG_CUDA_TRY(cudaMemcpy(N.torque, torque.data(), sizeof(double4_32a) * nSlots, cudaMemcpyHostToDevice));
-    WG_CUDA_TRY(cudaMemcpy(N.minert, minert.data(), sizeof(double4_32a) * nSlots, cudaMemcpyHostToDevice));
-    WG_CUDA_TRY(cudaMemcpy(N.lastPos, posr.data(), sizeof(double4_32a) * nSlots, cudaMemcpyHostToDevice));
-    WG_CUDA_TRY(cudaMemcpy(N.flags, flags.data(), sizeof(uint32_t) * nSlots, cudaMemcpyHostToDevice));
-    WG_CUDA_TRY(cudaMemcpy(P.shape, shape.data(), sizeof(int32_t) * nPar, cudaMemcpyHostToDevice));
-    WG_CUDA_TRY(cudaMemcpy(P.aux, aux.data(), sizeof(int4) * nPar, cudaMemcpyHostToDevice));
+    WG_CUDA_TRY(cudaMemcpyAsync(N.posr, posr.data(), sizeof(double4_32a) * nSlots, cudaMemcpyHostToDevice, S.stream));
+    WG_CUDA_TRY(cudaMemcpyAsync(N.vel, vel.data(), sizeof(double4_32a) * nSlots, cudaMemcpyHostToDevice, S.stream));
+    WG_CUDA_TRY(cudaMemcpyAsync(N.angv, angv.data(), sizeof(double4_32a) * nSlots, cudaMemcpyHostToDevice, S.stream));
+    WG_CUDA_TRY(cudaMemcpyAsync(N.ori, ori.data(), sizeof(double4_32a) * nSlots, cudaMemcpyHostToDevice, S.stream));
+    WG_CUDA_TRY(cudaMemcpyAsync(N.force, force.data(), sizeof(double4_32a) * nSlots, cudaMemcpyHostToDevice, S.stream));
+    WG_CUDA_TRY(cudaMemcpyAsync(N.torque, torque.data(), sizeof(double4_32a) * nSlots, cudaMemcpyHostToDevice, S.stream));
+    WG_CUDA_TRY(cudaMemcpyAsync(N.minert, minert.data(), sizeof(double4_32a) * nSlots, cudaMemcpyHostToDevice, S.stream));
+    WG_CUDA_TRY(cudaMemcpyAsync(N.lastPos, posr.data(), sizeof(double4_32a) * nSlots, cudaMemcpyHostToDevice, S.stream));
+    WG_CUDA_TRY(cudaMemcpyAsync(N.flags, flags.data(), sizeof(uint32_t) * nSlots, cudaMemcpyHostToDevice, S.stream));
+    WG_CUDA_TRY(cudaMemcpyAsync(P.shape, shape.data(), sizeof(int32_t) * nPar, cudaMemcpyHostToDevice, S.stream));
+    WG_CUDA_TRY(cudaMemcpyAsync(P.aux, aux.data(), sizeof(int4) * nPar, cudaMemcpyHostToDevice, S.stream));
     P.nFacets = (int32_t)facetIds.size();
     P.facetIds = nullptr;
     P.prep = nullptr;
     if (P.nFacets > 0) {
         P.facetIds = (int32_t*)dalloc(sizeof(int32_t) * P.nFacets);
         if (!P.facetIds) return fail(WG_ERR_CUDA, "out of device memory (facets)");
-        WG_CUDA_TRY(cudaMemcpy(P.facetIds, facetIds.data(), sizeof(int32_t) * P.nFacets, cudaMemcpyHostToDevice));
+        WG_CUDA_TRY(cudaMemcpyAsync(P.facetIds, facetIds.data(), sizeof(int32_t) * P.nFacets, cudaMemcpyHostToDevice, S.stream));
         if (prec == WG_PREC_FP32) {
             P.prep = (FacetPrep*)dalloc(sizeof(FacetPrep) * P.nFacets);
             if (!P.prep) return fail(WG_ERR_CUDA, "out of device memory (facets)");
-            WG_CUDA_TRY(cudaMemset(P.prep, 0xff, sizeof(FacetPrep) * P.nFacets));  // NaN: made at the first step
+            WG_CUDA_TRY(cudaMemsetAsync(P.prep, 0xff, sizeof(FacetPrep) * P.nFacets, S.stream));  // NaN: made at the first step
         }
     }
     // facets whose vertices are all fully blocked and at rest never move: their FacetPrep records
@@ -569,12 +569,12 @@ int Sim::upload() {
             if ((flags[v] & F_DOF_ALL) != F_DOF_ALL || vel[v].x != 0 || vel[v].y != 0 || vel[v].z != 0) facetsStatic = false;
         }
     }
-    WG_CUDA_TRY(cudaMemcpy(P.facet, facet.data(), sizeof(double4_32a) * nPar, cudaMemcpyHostToDevice));
-    WG_CUDA_TRY(cudaMemcpy(P.mat, mat.data(), sizeof(int32_t) * nPar, cudaMemcpyHostToDevice));
-    WG_CUDA_TRY(cudaMemcpy(P.mask, mask.data(), sizeof(uint32_t) * nPar, cudaMemcpyHostToDevice));
-    WG_CUDA_TRY(cudaMemcpy(dMats, mats.data(), sizeof(double4_32a) * mats.size(), cudaMemcpyHostToDevice));
-    WG_CUDA_TRY(cudaMemcpy(X.dApiMap, map.data(), sizeof(int32_t) * na, cudaMemcpyHostToDevice));
-    WG_CUDA_TRY(cudaMemcpy(X.dStage, hApi.data(), sizeof(double) * 19 * na, cudaMemcpyHostToDevice));
+    WG_CUDA_TRY(cudaMemcpyAsync(P.facet, facet.data(), sizeof(double4_32a) * nPar, cudaMemcpyHostToDevice, S.stream));
+    WG_CUDA_TRY(cudaMemcpyAsync(P.mat, mat.data(), sizeof(int32_t) * nPar, cudaMemcpyHostToDevice, S.stream));
+    WG_CUDA_TRY(cudaMemcpyAsync(P.mask, mask.data(), sizeof(uint32_t) * nPar, cudaMemcpyHostToDevice, S.stream));
+    WG_CUDA_TRY(cudaMemcpyAsync(dMats, mats.data(), sizeof(double4_32a) * mats.size(), cudaMemcpyHostToDevice, S.stream));
+    WG_CUDA_TRY(cudaMemcpyAsync(X.dApiMap, map.data(), sizeof(int32_t) * na, cudaMemcpyHostToDevice, S.stream));
+    WG_CUDA_TRY(cudaMemcpyAsync(X.dStage, hApi.data(), sizeof(double) * 19 * na, cudaMemcpyHostToDevice, S.stream));
     X.hApiMap = map;
     if (prec == WG_PREC_FP32) {
         std::vector<NodeConst32> nc(nSlots);
@@ -605,8 +605,8 @@ int Sim::upload() {
         N.ll = (float4*)dalloc(sizeof(float4) * nSlots);
         if (!N.ll) return fail(WG_ERR_CUDA, "out of device memory (scene)");
         if (!dNodeC || !N.mir || !N.wz || !N.orif || !N.rsplit) return fail(WG_ERR_CUDA, "out of device memory (scene)");
-        WG_CUDA_TRY(cudaMemcpy(N.orif, orf.data(), sizeof(float4) * nSlots, cudaMemcpyHostToDevice));
-        WG_CUDA_TRY(cudaMemcpy(N.rsplit, rsp.data(), sizeof(float2) * nSlots, cudaMemcpyHostToDevice));
+        WG_CUDA_TRY(cudaMemcpyAsync(N.orif, orf.data(), sizeof(float4) * nSlots, cudaMemcpyHostToDevice, S.stream));
+        WG_CUDA_TRY(cudaMemcpyAsync(N.rsplit, rsp.data(), sizeof(float2) * nSlots, cudaMemcpyHostToDevice, S.stream));
         // double-float mirrors of the initial state (x = hi + lo)
         std::vector<float4> hph(nSlots), hpl(nSlots), hvh(nSlots), hvl(nSlots);
         std::vector<float> hwz(nSlots);
@@ -628,17 +628,17 @@ int Sim::upload() {
         }
         std::vector<Mirror> hm(nSlots);
         for (int64_t q = 0; q < nSlots; q++) hm[q] = Mirror{hph[q], hpl[q], hvh[q], hvl[q]};
-        WG_CUDA_TRY(cudaMemcpy(N.mir, hm.data(), sizeof(Mirror) * nSlots, cudaMemcpyHostToDevice));
-        WG_CUDA_TRY(cudaMemcpy(N.wz, hwz.data(), sizeof(float) * nSlots, cudaMemcpyHostToDevice));
-        WG_CUDA_TRY(cudaMemcpy(N.lh, hph.data(), sizeof(float4) * nSlots, cudaMemcpyHostToDevice));
-        WG_CUDA_TRY(cudaMemcpy(N.ll, hpl.data(), sizeof(float4) * nSlots, cudaMemcpyHostToDevice));
-        WG_CUDA_TRY(cudaMemcpy(dNodeC, nc.data(), sizeof(NodeConst32) * nSlots, cudaMemcpyHostToDevice));
+        WG_CUDA_TRY(cudaMemcpyAsync(N.mir, hm.data(), sizeof(Mirror) * nSlots, cudaMemcpyHostToDevice, S.stream));
+        WG_CUDA_TRY(cudaMemcpyAsync(N.wz, hwz.data(), sizeof(float) * nSlots, cudaMemcpyHostToDevice, S.stream));
+        WG_CUDA_TRY(cudaMemcpyAsync(N.lh, hph.data(), sizeof(float4) * nSlots, cudaMemcpyHostToDevice, S.stream));
+        WG_CUDA_TRY(cudaMemcpyAsync(N.ll, hpl.data(), sizeof(float4) * nSlots, cudaMemcpyHostToDevice, S.stream));
+        WG_CUDA_TRY(cudaMemcpyAsync(dNodeC, nc.data(), sizeof(NodeConst32) * nSlots, cudaMemcpyHostToDevice, S.stream));
     }
     launch_facet_prep(stream, N, P, nullptr);
     long long st0 = cfg.step;
     step = cfg.step;
-    WG_CUDA_TRY(cudaMemcpy(dStep, &st0, sizeof(long long), cudaMemcpyHostToDevice));
-    WG_CUDA_TRY(cudaMemset(dFlags, 0, sizeof(int) * 4));
+    WG_CUDA_TRY(cudaMemcpyAsync(dStep, &st0, sizeof(long long), cudaMemcpyHostToDevice, S.stream));
+    WG_CUDA_TRY(cudaMemsetAsync(dFlags, 0, sizeof(int) * 4, S.stream));
     int r = ensureContactCapacity(std::max<int64_t>(1024, 4 * nPar));
     if (r) return r;
     C.n = 0;
@@ -661,9 +661,9 @@ int Sim::upload() {
     if (cfg.periodic) fillCellPar(X);
     if (nScenes > 1) {
         for (int k = 0; k < nScenes; k++) hPars[k].stepBase = (long long)cfg.step - (long long)cfgs[k].step;
-        WG_CUDA_TRY(cudaMemcpy(dPar, hPars.data(), sizeof(ScenePar) * nScenes, cudaMemcpyHostToDevice));
+        WG_CUDA_TRY(cudaMemcpyAsync(dPar, hPars.data(), sizeof(ScenePar) * nScenes, cudaMemcpyHostToDevice, S.stream));
     } else
-        WG_CUDA_TRY(cudaMemcpy(dPar, &hPar, sizeof(ScenePar), cudaMemcpyHostToDevice));
+        WG_CUDA_TRY(cudaMemcpyAsync(dPar, &hPar, sizeof(ScenePar), cudaMemcpyHostToDevice, S.stream));
     uploaded = true;
     initialized = false;
     return 0;
@@ -713,8 +713,8 @@ int Sim::ensureEnergyCapacity() {
         dECreated = (int32_t*)dalloc(sizeof(int32_t) * WG_ENERGY_N);
         dEPartial = (double*)dalloc(sizeof(double) * EN_CON_NCOL * 256);
         if (!dEnergy || !dECreated || !dEPartial) return fail(WG_ERR_CUDA, "out of device memory (energy)");
-        WG_CUDA_TRY(cudaMemset(dEnergy, 0, sizeof(double) * WG_ENERGY_N));
-        WG_CUDA_TRY(cudaMemset(dECreated, 0, sizeof(int32_t) * WG_ENERGY_N));
+        WG_CUDA_TRY(cudaMemsetAsync(dEnergy, 0, sizeof(double) * WG_ENERGY_N, S.stream));
+        WG_CUDA_TRY(cudaMemsetAsync(dECreated, 0, sizeof(int32_t) * WG_ENERGY_N, S.stream));
     }
     if (eNode.cap < N.n) {
         if (eNode.col) dfree(eNode.col);
@@ -1304,8 +1304,8 @@ static int slotCheck(Sim& S, int32_t k) {
         S.P.fresh = (uint8_t*)S.dalloc(S.nPar);
         S.N.fresh = (uint8_t*)S.dalloc(S.N.n);
         if (!S.N.fresh) return S.fail(WG_ERR_CUDA, "out of device memory (slots)");
-        WG_CUDA_TRY(cudaMemset(S.P.fresh, 0, S.nPar));
-        WG_CUDA_TRY(cudaMemset(S.N.fresh, 0, S.N.n));
+        WG_CUDA_TRY(cudaMemsetAsync(S.P.fresh, 0, S.nPar, S.stream));
+        WG_CUDA_TRY(cudaMemsetAsync(S.N.fresh, 0, S.N.n, S.stream));
     }
     if (S.hParked.empty()) S.hParked.assign(S.nPar, 0);
     return 0;
@@ -1345,7 +1345,7 @@ int wg_slot_load(wg_scene* s, int32_t k, const wg_config* c, int64_t n, const do
         S.hTanPhi[matBase + m] = tan_phi[m];
         S.hKtDivKn[matBase + m] = kt_div_kn[m];
     }
-    WG_CUDA_TRY(cudaMemcpy(S.dMats + matBase, mats.data(), sizeof(double4_32a) * n_mat, cudaMemcpyHostToDevice));
+    WG_CUDA_TRY(cudaMemcpyAsync(S.dMats + matBase, mats.data(), sizeof(double4_32a) * n_mat, cudaMemcpyHostToDevice, S.stream));
     r = writeSlot(S, p0, cap, n, pos, ori, vel, ang_vel, mass, inertia, flags, shape, radius, wall_axis, wall_sense, mat, matBase, mask);
     if (r) return r;
     S.cfgs[k] = *c;
@@ -1354,7 +1354,7 @@ int wg_slot_load(wg_scene* s, int32_t k, const wg_config* c, int64_t n, const do
     S.hPars[k].stepEnd = (long long)c->step + (long long)n_steps;
     S.sceneTime0[k] = 0.;
     if (k == 0) S.hPar = S.hPars[0];
-    WG_CUDA_TRY(cudaMemcpy(S.dPar + k, &S.hPars[k], sizeof(ScenePar), cudaMemcpyHostToDevice));
+    WG_CUDA_TRY(cudaMemcpyAsync(S.dPar + k, &S.hPars[k], sizeof(ScenePar), cudaMemcpyHostToDevice, S.stream));
     return WG_OK;
 }
 
@@ -1365,10 +1365,10 @@ int wg_slot_clear(wg_scene* s, int32_t k) {
     if (r) return r;
     const int64_t p0 = S.sceneStart[k], cap = S.sceneStart[k + 1] - p0;
     for (int64_t p = p0; p < p0 + cap; p++) S.hParked[p] = 1;
-    WG_CUDA_TRY(cudaMemset(S.P.fresh + p0, 1, cap));
+    WG_CUDA_TRY(cudaMemsetAsync(S.P.fresh + p0, 1, cap, S.stream));
     S.hPars[k].stepEnd = -((long long)1 << 62);  // frozen
     if (k == 0) S.hPar = S.hPars[0];
-    WG_CUDA_TRY(cudaMemcpy(S.dPar + k, &S.hPars[k], sizeof(ScenePar), cudaMemcpyHostToDevice));
+    WG_CUDA_TRY(cudaMemcpyAsync(S.dPar + k, &S.hPars[k], sizeof(ScenePar), cudaMemcpyHostToDevice, S.stream));
     S.listsDirty = true;
     S.forceFull = true;
     return WG_OK;
@@ -1396,7 +1396,7 @@ int wg_get_slot_nodes(wg_scene* s, int32_t k, int64_t n, double* pos, double* or
     std::vector<double4_32a> a(n);
     auto get = [&](const double4_32a* src, double* dst, int w) -> int {
         if (!dst) return 0;
-        if (cudaMemcpy(a.data(), src + p0, sizeof(double4_32a) * n, cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+        if (cudaMemcpyAsync(a.data(), src + p0, sizeof(double4_32a) * n, cudaMemcpyDeviceToHost, S.stream) != cudaSuccess) return -1;
         for (int64_t q = 0; q < n; q++) {
             const double v[4] = {a[q].x, a[q].y, a[q].z, a[q].w};
             for (int j = 0; j < w; j++) dst[w * q + j] = v[j];
@@ -1409,7 +1409,7 @@ int wg_get_slot_nodes(wg_scene* s, int32_t k, int64_t n, double* pos, double* or
     if (ori) {
         if (S.N.orif) {
             std::vector<float4> f(n);
-            WG_CUDA_TRY(cudaMemcpy(f.data(), S.N.orif + p0, sizeof(float4) * n, cudaMemcpyDeviceToHost));
+            WG_CUDA_TRY(cudaMemcpyAsync(f.data(), S.N.orif + p0, sizeof(float4) * n, cudaMemcpyDeviceToHost, S.stream));
             for (int64_t q = 0; q < n; q++) {
                 ori[4 * q] = f[q].x; ori[4 * q + 1] = f[q].y; ori[4 * q + 2] = f[q].z; ori[4 * q + 3] = f[q].w;
             }
@@ -1450,8 +1450,8 @@ int wg_get_scene_stats(wg_scene* s, int32_t k, wg_stats* o) {
         const int64_t n = S.C.n;
         std::vector<uint32_t> fl(n);
         std::vector<uint64_t> key(n);
-        WG_CUDA_TRY(cudaMemcpy(fl.data(), S.C.flags, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
-        WG_CUDA_TRY(cudaMemcpy(key.data(), S.C.key, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost));
+        WG_CUDA_TRY(cudaMemcpyAsync(fl.data(), S.C.flags, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, S.stream));
+        WG_CUDA_TRY(cudaMemcpyAsync(key.data(), S.C.key, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost, S.stream));
         const int64_t p0 = S.nScenes > 1 ? S.sceneStart[k] : 0, p1 = S.nScenes > 1 ? S.sceneStart[k + 1] : S.nPar;
         for (int64_t c2 = 0; c2 < n; c2++) {
             const int64_t lo = (int64_t)(key[c2] >> 32);
@@ -1628,8 +1628,9 @@ int wg_get_energy(wg_scene* s, double* values, int32_t* created) {
         return WG_OK;
     }
     WG_CUDA_TRY(cudaSetDevice(S.device));
-    WG_CUDA_TRY(cudaMemcpy(values, S.dEnergy, sizeof(double) * WG_ENERGY_N, cudaMemcpyDeviceToHost));
-    WG_CUDA_TRY(cudaMemcpy(created, S.dECreated, sizeof(int32_t) * WG_ENERGY_N, cudaMemcpyDeviceToHost));
+    WG_CUDA_TRY(cudaMemcpyAsync(values, S.dEnergy, sizeof(double) * WG_ENERGY_N, cudaMemcpyDeviceToHost, S.stream));
+    WG_CUDA_TRY(cudaMemcpyAsync(created, S.dECreated, sizeof(int32_t) * WG_ENERGY_N, cudaMemcpyDeviceToHost, S.stream));
+    WG_CUDA_TRY(cudaStreamSynchronize(S.stream));  // the destination may be page-locked
     return WG_OK;
 }
 
@@ -1643,8 +1644,8 @@ int wg_set_energy(wg_scene* s, const double* values, const int32_t* created) {
         int r = S.ensureEnergyCapacity();
         if (r) return r;
     }
-    WG_CUDA_TRY(cudaMemcpy(S.dEnergy, values, sizeof(double) * WG_ENERGY_N, cudaMemcpyHostToDevice));
-    WG_CUDA_TRY(cudaMemcpy(S.dECreated, created, sizeof(int32_t) * WG_ENERGY_N, cudaMemcpyHostToDevice));
+    WG_CUDA_TRY(cudaMemcpyAsync(S.dEnergy, values, sizeof(double) * WG_ENERGY_N, cudaMemcpyHostToDevice, S.stream));
+    WG_CUDA_TRY(cudaMemcpyAsync(S.dECreated, created, sizeof(int32_t) * WG_ENERGY_N, cudaMemcpyHostToDevice, S.stream));
     return WG_OK;
 }
 
@@ -1679,7 +1680,7 @@ int wg_get_stats(wg_scene* s, wg_stats* o) {
     for (int q = 0; q < 9; q++) o->stress[q] = S.stress[q];
     if (S.uploaded && S.C.n > 0) {
         std::vector<uint32_t> fl(S.C.n);
-        WG_CUDA_TRY(cudaMemcpy(fl.data(), S.C.flags, sizeof(uint32_t) * S.C.n, cudaMemcpyDeviceToHost));
+        WG_CUDA_TRY(cudaMemcpyAsync(fl.data(), S.C.flags, sizeof(uint32_t) * S.C.n, cudaMemcpyDeviceToHost, S.stream));
         int64_t r = 0;
         for (uint32_t f : fl) r += (f & C_REAL) ? 1 : 0;
         o->n_real = r;
@@ -1722,20 +1723,20 @@ static int collectContacts(Sim& S, std::vector<int64_t>& keep, std::vector<uint6
     if (n > 0) {
         // global force on pA from the end slots (pB's slot negated where pA is a facet)
         std::vector<int32_t> sLo(n), sHi(n);
-        WG_CUDA_TRY(cudaMemcpy(sLo.data(), S.I.slotLo, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
-        WG_CUDA_TRY(cudaMemcpy(sHi.data(), S.I.slotHi, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+        WG_CUDA_TRY(cudaMemcpyAsync(sLo.data(), S.I.slotLo, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, S.stream));
+        WG_CUDA_TRY(cudaMemcpyAsync(sHi.data(), S.I.slotHi, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, S.stream));
         std::vector<uint32_t> flc(n);
         std::vector<uint64_t> kc(n);
-        WG_CUDA_TRY(cudaMemcpy(flc.data(), S.C.flags, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
-        WG_CUDA_TRY(cudaMemcpy(kc.data(), S.C.key, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost));
+        WG_CUDA_TRY(cudaMemcpyAsync(flc.data(), S.C.flags, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, S.stream));
+        WG_CUDA_TRY(cudaMemcpyAsync(kc.data(), S.C.key, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost, S.stream));
         const int64_t ne = 2 * std::max<int64_t>(S.I.nAct, 1);
         std::vector<double> ef(4 * ne);
         if (S.prec == WG_PREC_FP32) {
             std::vector<float> tmp(4 * ne);
-            WG_CUDA_TRY(cudaMemcpy(tmp.data(), S.I.endAf, sizeof(float4) * ne, cudaMemcpyDeviceToHost));
+            WG_CUDA_TRY(cudaMemcpyAsync(tmp.data(), S.I.endAf, sizeof(float4) * ne, cudaMemcpyDeviceToHost, S.stream));
             for (int64_t q = 0; q < 4 * ne; q++) ef[q] = tmp[q];
         } else {
-            WG_CUDA_TRY(cudaMemcpy(ef.data(), S.I.endA, sizeof(double4_32a) * ne, cudaMemcpyDeviceToHost));
+            WG_CUDA_TRY(cudaMemcpyAsync(ef.data(), S.I.endA, sizeof(double4_32a) * ne, cudaMemcpyDeviceToHost, S.stream));
         }
         for (int64_t c = 0; c < n; c++) {
             const bool aIsLo = !(flc[c] & C_SWAP);
@@ -1747,22 +1748,22 @@ static int collectContacts(Sim& S, std::vector<int64_t>& keep, std::vector<uint6
         }
     }
     if (n > 0) {
-        WG_CUDA_TRY(cudaMemcpy(key.data(), S.C.key, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost));
-        WG_CUDA_TRY(cudaMemcpy(fl.data(), S.C.flags, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
-        WG_CUDA_TRY(cudaMemcpy(cd.data(), S.C.cdist, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+        WG_CUDA_TRY(cudaMemcpyAsync(key.data(), S.C.key, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost, S.stream));
+        WG_CUDA_TRY(cudaMemcpyAsync(fl.data(), S.C.flags, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, S.stream));
+        WG_CUDA_TRY(cudaMemcpyAsync(cd.data(), S.C.cdist, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, S.stream));
         if (S.prec == WG_PREC_FP64) {
-            for (int q = 0; q < CC_NCOL; q++) WG_CUDA_TRY(cudaMemcpy(cols[q].data(), S.C.col[q], sizeof(double) * n, cudaMemcpyDeviceToHost));
+            for (int q = 0; q < CC_NCOL; q++) WG_CUDA_TRY(cudaMemcpyAsync(cols[q].data(), S.C.col[q], sizeof(double) * n, cudaMemcpyDeviceToHost, S.stream));
         } else {
             // FP32-force mode: map the FP32 columns onto the FP64 listing layout
             std::vector<std::vector<float>> fc(CF_NCOL, std::vector<float>(n));
-            for (int q = 0; q < CF_NCOL; q++) WG_CUDA_TRY(cudaMemcpy(fc[q].data(), S.C.fcol[q], sizeof(float) * n, cudaMemcpyDeviceToHost));
+            for (int q = 0; q < CF_NCOL; q++) WG_CUDA_TRY(cudaMemcpyAsync(fc[q].data(), S.C.fcol[q], sizeof(float) * n, cudaMemcpyDeviceToHost, S.stream));
             std::vector<double> cp[3];
             for (int k = 0; k < 3; k++) {
                 cp[k].resize(n);
-                WG_CUDA_TRY(cudaMemcpy(cp[k].data(), S.C.col[CC_CPX + k], sizeof(double) * n, cudaMemcpyDeviceToHost));
+                WG_CUDA_TRY(cudaMemcpyAsync(cp[k].data(), S.C.col[CC_CPX + k], sizeof(double) * n, cudaMemcpyDeviceToHost, S.stream));
             }
             std::vector<double4_32a> pos(S.nPar);
-            WG_CUDA_TRY(cudaMemcpy(pos.data(), S.N.posr, sizeof(double4_32a) * S.nPar, cudaMemcpyDeviceToHost));
+            WG_CUDA_TRY(cudaMemcpyAsync(pos.data(), S.N.posr, sizeof(double4_32a) * S.nPar, cudaMemcpyDeviceToHost, S.stream));
             for (int64_t c = 0; c < n; c++) {
                 const int map[] = {CF_T0X, CF_T0Y, CF_T0Z, CF_T1X, CF_T1Y, CF_T1Z};
                 for (int q = 0; q < 6; q++) cols[CC_T0X + q][c] = fc[map[q]][c];
@@ -1828,10 +1829,10 @@ int wg_get_contact_state(wg_scene* s, int64_t cap, int64_t* n_out, uint64_t* key
     std::vector<uint32_t> f(n);
     std::vector<int32_t> s0(n), cd(n);
     if (n > 0) {
-        WG_CUDA_TRY(cudaMemcpy(k.data(), S.C.key, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost));
-        WG_CUDA_TRY(cudaMemcpy(f.data(), S.C.flags, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
-        WG_CUDA_TRY(cudaMemcpy(s0.data(), S.C.step0, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
-        WG_CUDA_TRY(cudaMemcpy(cd.data(), S.C.cdist, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+        WG_CUDA_TRY(cudaMemcpyAsync(k.data(), S.C.key, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost, S.stream));
+        WG_CUDA_TRY(cudaMemcpyAsync(f.data(), S.C.flags, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, S.stream));
+        WG_CUDA_TRY(cudaMemcpyAsync(s0.data(), S.C.step0, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, S.stream));
+        WG_CUDA_TRY(cudaMemcpyAsync(cd.data(), S.C.cdist, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, S.stream));
     }
     std::vector<int64_t> keep;
     for (int64_t c = 0; c < n; c++)
@@ -1846,13 +1847,13 @@ int wg_get_contact_state(wg_scene* s, int64_t cap, int64_t* n_out, uint64_t* key
     std::vector<float> vf(n);
     int col = 0;
     for (int q : q64) {
-        WG_CUDA_TRY(cudaMemcpy(v.data(), S.C.col[q], sizeof(double) * n, cudaMemcpyDeviceToHost));
+        WG_CUDA_TRY(cudaMemcpyAsync(v.data(), S.C.col[q], sizeof(double) * n, cudaMemcpyDeviceToHost, S.stream));
         for (size_t i = 0; i < keep.size(); i++) cols[(int64_t)i * ncols + col] = v[keep[i]];
         col++;
     }
     if (S.prec == WG_PREC_FP32)
         for (int q = 0; q < CF_NCOL; q++) {
-            WG_CUDA_TRY(cudaMemcpy(vf.data(), S.C.fcol[q], sizeof(float) * n, cudaMemcpyDeviceToHost));
+            WG_CUDA_TRY(cudaMemcpyAsync(vf.data(), S.C.fcol[q], sizeof(float) * n, cudaMemcpyDeviceToHost, S.stream));
             for (size_t i = 0; i < keep.size(); i++) cols[(int64_t)i * ncols + col] = (double)vf[keep[i]];
             col++;
         }
@@ -1890,23 +1891,23 @@ int wg_set_contact_state(wg_scene* s, int64_t n, const uint64_t* key, const uint
     if (n > 0) {
         std::vector<uint32_t> f(n);
         for (int64_t i = 0; i < n; i++) f[i] = flags[i] & ~(uint32_t)C_DORMANT;
-        WG_CUDA_TRY(cudaMemcpy(S.C.key, key, sizeof(uint64_t) * n, cudaMemcpyHostToDevice));
-        WG_CUDA_TRY(cudaMemcpy(S.C.flags, f.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice));
-        WG_CUDA_TRY(cudaMemcpy(S.C.step0, step0, sizeof(int32_t) * n, cudaMemcpyHostToDevice));
-        WG_CUDA_TRY(cudaMemcpy(S.C.cdist, cell_dist, sizeof(int32_t) * n, cudaMemcpyHostToDevice));
+        WG_CUDA_TRY(cudaMemcpyAsync(S.C.key, key, sizeof(uint64_t) * n, cudaMemcpyHostToDevice, S.stream));
+        WG_CUDA_TRY(cudaMemcpyAsync(S.C.flags, f.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice, S.stream));
+        WG_CUDA_TRY(cudaMemcpyAsync(S.C.step0, step0, sizeof(int32_t) * n, cudaMemcpyHostToDevice, S.stream));
+        WG_CUDA_TRY(cudaMemcpyAsync(S.C.cdist, cell_dist, sizeof(int32_t) * n, cudaMemcpyHostToDevice, S.stream));
         const std::vector<int> q64 = snapshotCols64(S);
         std::vector<double> v(n);
         std::vector<float> vf(n);
         int col = 0;
         for (int q : q64) {
             for (int64_t i = 0; i < n; i++) v[i] = cols[i * ncols + col];
-            WG_CUDA_TRY(cudaMemcpy(S.C.col[q], v.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+            WG_CUDA_TRY(cudaMemcpyAsync(S.C.col[q], v.data(), sizeof(double) * n, cudaMemcpyHostToDevice, S.stream));
             col++;
         }
         if (S.prec == WG_PREC_FP32)
             for (int q = 0; q < CF_NCOL; q++) {
                 for (int64_t i = 0; i < n; i++) vf[i] = (float)cols[i * ncols + col];
-                WG_CUDA_TRY(cudaMemcpy(S.C.fcol[q], vf.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
+                WG_CUDA_TRY(cudaMemcpyAsync(S.C.fcol[q], vf.data(), sizeof(float) * n, cudaMemcpyHostToDevice, S.stream));
                 col++;
             }
     }
@@ -1976,8 +1977,8 @@ int wg_get_aabbs(wg_scene* s, double* mn, double* mx) {
     Sim& S = *SIM(s);
     if (!S.uploaded) return S.fail(WG_ERR_STATE, "no boxes before the first run");
     std::vector<double4_32a> a(S.nPar), b(S.nPar);
-    WG_CUDA_TRY(cudaMemcpy(a.data(), S.P.mn, sizeof(double4_32a) * S.nPar, cudaMemcpyDeviceToHost));
-    WG_CUDA_TRY(cudaMemcpy(b.data(), S.P.mx, sizeof(double4_32a) * S.nPar, cudaMemcpyDeviceToHost));
+    WG_CUDA_TRY(cudaMemcpyAsync(a.data(), S.P.mn, sizeof(double4_32a) * S.nPar, cudaMemcpyDeviceToHost, S.stream));
+    WG_CUDA_TRY(cudaMemcpyAsync(b.data(), S.P.mx, sizeof(double4_32a) * S.nPar, cudaMemcpyDeviceToHost, S.stream));
     for (int64_t i = 0; i < S.nPar; i++) {
         mn[3 * i] = a[i].x; mn[3 * i + 1] = a[i].y; mn[3 * i + 2] = a[i].z;
         mx[3 * i] = b[i].x; mx[3 * i + 1] = b[i].y; mx[3 * i + 2] = b[i].z;

@@ -967,7 +967,7 @@ static int buildLists(Sim& S) {
         if (!W.sphereIds || !W.largeIds || !W.globalIds || !W.gStart) return S.fail(WG_ERR_CUDA, "out of device memory");
     }
     W.nLarge = W.nGlobal = 0;
-    if (!sph.empty()) WG_CUDA_TRY(cudaMemcpy(W.sphereIds, sph.data(), sizeof(int32_t) * sph.size(), cudaMemcpyHostToDevice));
+    if (!sph.empty()) WG_CUDA_TRY(cudaMemcpyAsync(W.sphereIds, sph.data(), sizeof(int32_t) * sph.size(), cudaMemcpyHostToDevice, S.stream));
     // non-sphere pairs are possible only if some pair of them shares a mask bit outside loneMask
     bool ll = false;
     std::vector<int32_t> nonSph(large);
@@ -1030,7 +1030,7 @@ int collide_full_run(Sim& S) {
             if (!W.dGrids || !W.dChunk) return S.fail(WG_ERR_CUDA, "out of device memory (grid)");
         }
         if (W.chunksDirty) {
-            WG_CUDA_TRY(cudaMemcpy(W.dChunk, W.hChunk.data(), sizeof(int32_t) * (nb + 1), cudaMemcpyHostToDevice));
+            WG_CUDA_TRY(cudaMemcpyAsync(W.dChunk, W.hChunk.data(), sizeof(int32_t) * (nb + 1), cudaMemcpyHostToDevice, S.stream));
             W.chunksDirty = false;
         }
         k_grid_reduce<<<nb, BS, 0, st>>>(S.P, W.sphereIds, W.dChunk, W.red);
@@ -1119,13 +1119,13 @@ int collide_full_run(Sim& S) {
             std::sort(glo.begin(), glo.end());  // grouped by scene (particles of a batch are)
             W.nLarge = (int)loc.size();
             W.nGlobal = (int)glo.size();
-            if (W.nLarge) WG_CUDA_TRY(cudaMemcpy(W.largeIds, loc.data(), sizeof(int32_t) * loc.size(), cudaMemcpyHostToDevice));
-            if (W.nGlobal) WG_CUDA_TRY(cudaMemcpy(W.globalIds, glo.data(), sizeof(int32_t) * glo.size(), cudaMemcpyHostToDevice));
+            if (W.nLarge) WG_CUDA_TRY(cudaMemcpyAsync(W.largeIds, loc.data(), sizeof(int32_t) * loc.size(), cudaMemcpyHostToDevice, S.stream));
+            if (W.nGlobal) WG_CUDA_TRY(cudaMemcpyAsync(W.globalIds, glo.data(), sizeof(int32_t) * glo.size(), cudaMemcpyHostToDevice, S.stream));
             if (K > 1) {
                 std::vector<int32_t> gs(K + 1, 0);
                 for (int32_t p : glo) gs[S.hSceneOfPar[p] + 1]++;
                 for (int k = 0; k < K; k++) gs[k + 1] += gs[k];
-                WG_CUDA_TRY(cudaMemcpy(W.gStart, gs.data(), sizeof(int32_t) * (K + 1), cudaMemcpyHostToDevice));
+                WG_CUDA_TRY(cudaMemcpyAsync(W.gStart, gs.data(), sizeof(int32_t) * (K + 1), cudaMemcpyHostToDevice, S.stream));
             }
         }
     }
