@@ -52,7 +52,8 @@ def compile_scene(S):
     if not S.fields:
         raise ValueError("Scene has no fields")
     D = S.dem
-    eng = [e for e in S.engines if not getattr(e, "dead", False)]
+    # engines that run on the host between device steps (VtkExport) are not part of the device plan
+    eng = [e for e in S.engines if not getattr(e, "dead", False) and not getattr(e, "_host", False)]
     kinds = []
     for e in eng:
         if isinstance(e, dem.Leapfrog):

@@ -433,7 +433,8 @@ def _runsAlone(S):
     """Periodic scenes, scenes whose dt changes (DynDt, Scene.nextDt) and scenes that track energy
     are not batched."""
     from .dem import DynDt
-    return bool(S.isPeriodic or S.trackEnergy or any(isinstance(e, DynDt) and not e.dead for e in S.engines)
+    return bool(S.isPeriodic or S.trackEnergy or any((isinstance(e, DynDt) or getattr(e, "_host", False)) and not e.dead
+                                                     for e in S.engines)
                 or (S.nextDt > 0 and math.isfinite(S.nextDt)))
 
 

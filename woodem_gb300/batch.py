@@ -27,6 +27,8 @@ class Batch:
         self.scenes = list(scenes)
         if not self.scenes:
             raise ValueError("empty batch")
+        if any(getattr(e, "_host", False) and not e.dead for S in self.scenes for e in S.engines):
+            raise NotImplementedError("engines that run on the host (VtkExport) are not run in a Batch")
         self.arrays = [_plan.compile_scene(S) for S in self.scenes]
         if any(A.config.get("dyndt") or A.config["next_dt"] == A.config["next_dt"] for A in self.arrays):
             raise NotImplementedError("DynDt and Scene.nextDt are not supported in a Batch (each scene keeps its dt)")

@@ -62,6 +62,33 @@ class PeriodicEngine(Engine):
     _attrs = {"stepPeriod": 1, "virtPeriod": 0.0, "realPeriod": 0.0, "stepModulo": True, "nDo": -1, "nDone": 0,
               "initRun": True, "virtLast": NaN, "realLast": NaN, "stepLast": -1, "stepPrev": -1, "virtPrev": -1.0,
               "realPrev": -1.0}
+    _COUNTERS = ("nDone", "stepLast", "stepPrev", "virtLast", "virtPrev", "realLast", "realPrev")
+
+    def _isActivated(self, stepNow, virtNow, realNow, c=None):
+        """PeriodicEngine::isActivated (core/Engine.cpp:169-194) on the counters ``c`` (a dict;
+        the engine's own attributes when None), which it updates."""
+        own = c is None
+        if own:
+            c = {k: getattr(self, k) for k in self._COUNTERS}
+        init = c["stepLast"] < 0
+        if init:
+            c["realLast"], c["virtLast"], c["stepLast"] = realNow, virtNow, stepNow
+        act = False
+        if (self.nDo < 0 or c["nDone"] < self.nDo) and (
+                (self.virtPeriod > 0 and virtNow - c["virtLast"] >= self.virtPeriod) or
+                (self.realPeriod > 0 and realNow - c["realLast"] >= self.realPeriod) or
+                (self.stepPeriod > 0 and ((stepNow - c["stepLast"] >= self.stepPeriod) or
+                                          (self.stepModulo and stepNow % self.stepPeriod == 0)))):
+            c["realPrev"], c["realLast"] = c["realLast"], realNow
+            c["virtPrev"], c["virtLast"] = c["virtLast"], virtNow
+            c["stepPrev"], c["stepLast"] = c["stepLast"], stepNow
+            if not (init and not self.initRun):
+                c["nDone"] += 1
+                act = True
+        if own:
+            for k, v in c.items():
+                setattr(self, k, v)
+        return act
 
 
 class Field(Object):
@@ -294,7 +321,32 @@ class Scene(Object):
         if nSteps <= 0:
             return
         sim = self._ensure_sim()
-        sim.run(int(nSteps))
+        host = [e for e in self._engines if getattr(e, "_host", False) and not e.dead]
+        if not host:
+            sim.run(int(nSteps))
+            return
+        # engines that run on the host (VtkExport) after the device engines of a step: the queued
+        # steps are cut at each step where one of them is due, then it runs on the state of that step
+        left = int(nSteps)
+        while left > 0:
+            k = left
+            now = time.time()
+            for e in host:
+                c = {q: getattr(e, q) for q in e._COUNTERS}
+                for j in range(k):
+                    if e._isActivated(self.step + j, self.time + j * self.dt, now, c):
+                        k = j + 1
+                        break
+            step0, t0, dt0 = self.step, self.time, self.dt
+            sim.run(k)
+            left -= k
+            due = []
+            for e in host:
+                for j in range(k):
+                    if e._isActivated(step0 + j, t0 + j * dt0, now) and j == k - 1:
+                        due.append(e)
+            for e in due:
+                e._runHost(self, step0 + k - 1, t0 + (k - 1) * dt0)
 
     def one(self):
         self.run(1)

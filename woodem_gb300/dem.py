@@ -723,6 +723,31 @@ class ContactLoop(Engine):
         return self.geoDisp + self.phyDisp + self.lawDisp
 
 
+class VtkExport(PeriodicEngine):
+    """Writes the scene to VTK XML files when due (pkg/dem/VtkExport.hpp:30-90): spheres, meshes
+    (facets, walls with glAB) and contacts, named ``{out}spheres.{step}.vtu``,
+    ``{out}mesh.{step}.vtu`` and ``{out}con.{step}.vtp``; ``out`` may hold ``{tag}`` fields of
+    Scene.tags. Runs on the host between queued device steps (woodem_gb300.vtk); the files are
+    ASCII XML (``compress``/``ascii`` are accepted, multiblock output is not built)."""
+    spheres, mesh, con, tri, all = 1, 2, 4, 8, 15
+    _attrs = {"out": "", "compress": True, "ascii": False, "multiblock": False, "mask": 0, "what": 15,
+              "sphereSphereOnly": False, "infError": True, "skipInvisible": True, "subdiv": 16, "thickFacetDiv": 1,
+              "nanValue": 0.0, "outFiles": lambda: {}, "outTimes": lambda: [], "outSteps": lambda: []}
+    _host = True
+
+    def _runHost(self, S, step, time):
+        from . import vtk
+        if self.multiblock:
+            raise NotImplementedError("VtkExport.multiblock is not built")
+        S.sync()
+        files = vtk.export(S, S._sim.contacts(), out=self.out, what=self.what, mask=self.mask,
+                           sphereSphereOnly=self.sphereSphereOnly, infError=self.infError, nanValue=self.nanValue, step=step)
+        for k, f in files.items():
+            self.outFiles.setdefault(k, []).append(f)
+        self.outTimes.append(time)
+        self.outSteps.append(step)
+
+
 class DynDt(PeriodicEngine):
     """Adjusts Scene.dt from the current stiffness of the contacts (pkg/dem/DynDt.hpp:5-25), as the
     engine after ContactLoop: the critical timestep is evaluated on the device, the new dt
