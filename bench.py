@@ -16,13 +16,11 @@ a bounded sample of the same workload and prints the same JSON line.
 """
 import argparse
 import json
-import math
 import os
 import statistics
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 
 import numpy as np

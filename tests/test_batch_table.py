@@ -2,8 +2,6 @@
 answers of the reference's own doctests, the parameter assignment of readParamsFromTable and
 runPreprocessor, the results database, line selection and the grouping of lines into batches."""
 import collections
-import json
-import os
 import sqlite3
 
 import numpy as np

@@ -1,6 +1,5 @@
 """Checkpoint fingerprint on the CPU: equal for scenes built the same way, whatever their
 evolving state (positions, step, cell), different for another scene (particles, materials)."""
-import numpy as np
 
 from woodem_gb300 import scenes, checkpoint, _plan
 

@@ -6,7 +6,6 @@ a head-on contact of two equal spheres, against the activation rule restated ste
 against the dt update rule evaluated in Python with the same libm."""
 import math
 
-import numpy as np
 import pytest
 
 from woodem_gb300 import _plan, scenes, utils

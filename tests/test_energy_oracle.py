@@ -5,7 +5,6 @@ Leapfrog energy expressions (Leapfrog.cpp:52-97) evaluated step by step in Pytho
 falling, damped sphere (same operations, same order: equal bit for bit), and by energy balances:
 with all dissipation and work entries counted, the total of Scene.energy stays at the initial
 kinetic energy (two spheres colliding elastically, with friction and with Hertz viscosity)."""
-import math
 
 import numpy as np
 import pytest

@@ -5,8 +5,6 @@ node and contact order, so the entries agree to a relative 1e-9 (accumulated ove
 steps), while the trajectory itself stays bitwise the oracle's: tracking energy changes no
 state. The device sums are deterministic: the energies do not depend on how the steps are
 split into calls."""
-import math
-
 import numpy as np
 import pytest
 

@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 from woodem_gb300 import _plan, scenes, vtk
-from woodem_gb300.dem import VtkExport, DynDt
+from woodem_gb300.dem import VtkExport
 
 
 def _oracle_state(S, steps):

@@ -25,7 +25,6 @@ import re
 import runpy
 import sqlite3
 import sys
-import types
 
 import numpy as np
 

@@ -5,7 +5,6 @@ core/Engine.hpp:27-104. A Scene owns a device-side simulation (created on the
 first ``run``); engines are descriptors compiled into one device plan, so the
 per-step loop of core/Scene.cpp:319-389 runs entirely on the GPU.
 """
-import math
 import os
 import socket
 import time

@@ -12,7 +12,6 @@ A job's result does not depend on what runs beside it: a slot integrates its job
 operations, in the same order, as the job alone (see woodem_gb300.batch).
 """
 import ctypes as C
-import heapq
 import math
 import threading
 import time
