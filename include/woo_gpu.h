@@ -104,11 +104,12 @@ typedef struct wg_config {
 } wg_config;
 
 /* Scene.energy entries (EnergyTracker, core/EnergyTracker.hpp), in this order: the Leapfrog
-   energies (Leapfrog.cpp:52-97), then those of the contact laws (IdealElPl.cpp:25-90,
-   Hertz.cpp:150-179). kinetic, kinTrans, kinRot and elast hold the last step's value, the others
-   accumulate. */
-#define WG_ENERGY_N 10
-#define WG_ENERGY_NAMES {"kinetic", "kinTrans", "kinRot", "grav", "nonviscDamp", "elast", "plast", "broken", "viscN", "viscT"}
+   energies (Leapfrog.cpp:52-97), those of the contact laws (IdealElPl.cpp:25-90,
+   Hertz.cpp:150-179) and the work of the periodic cell's velocity gradient on the contacts
+   (ContactLoop.cpp:236-246, with ContactLoop.evalStress). kinetic, kinTrans, kinRot and elast
+   hold the last step's value, the others accumulate. */
+#define WG_ENERGY_N 11
+#define WG_ENERGY_NAMES {"kinetic", "kinTrans", "kinRot", "grav", "nonviscDamp", "elast", "plast", "broken", "viscN", "viscT", "gradV"}
 
 /* DynDt state after a run: Scene.dt and nextDt, the engine's counters and DynDt.dt (the dry-run
    value), and the last critical timestep computed (Inf: no stiff contact). */

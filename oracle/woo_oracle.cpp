@@ -168,7 +168,7 @@ enum { DOF_X = 1, DOF_Y = 2, DOF_Z = 4, DOF_RX = 8, DOF_RY = 16, DOF_RZ = 32, DO
        CLUMP_CLUMPED = 64, CLUMP_CLUMP = 128, ENERGY_SKIP = 256, GRAVITY_SKIP = 512, DAMPING_SKIP = 2048 };
 enum { HOMO_NONE = 0, HOMO_POS = 1, HOMO_VEL = 2, HOMO_VEL_2ND = 3, HOMO_GRADV2 = 4 };
 // Scene.energy entries (EnergyTracker), in the order of wo_get_energy
-enum { EN_KINETIC, EN_KINTRANS, EN_KINROT, EN_GRAV, EN_DAMP, EN_ELAST, EN_PLAST, EN_BROKEN, EN_VISCN, EN_VISCT, EN_N };
+enum { EN_KINETIC, EN_KINTRANS, EN_KINROT, EN_GRAV, EN_DAMP, EN_ELAST, EN_PLAST, EN_BROKEN, EN_VISCN, EN_VISCT, EN_GRADV, EN_N };
 
 struct Node {
     V3 pos; Q ori;
@@ -302,8 +302,10 @@ struct Scene {
     M3 stress;
     double sqrt5, viscAlphaConst; bool viscOn;
     // Scene.energy and whether each entry exists
-    double energy[EN_N] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-    int ecreated[EN_N] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    double energy[EN_N] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    int ecreated[EN_N] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    // ContactLoop.prevStress and prevVol (ContactLoop.hpp:119-123)
+    M3 prevStress; double prevVol = std::numeric_limits<double>::quiet_NaN();
 
     ~Scene() { for (auto* c : linView) delete c; }
 
@@ -1056,7 +1058,21 @@ struct Scene {
             energy[EN_VISCT] += e[4];
             if (e[4] != 0) ecreated[EN_VISCT] = 1;
         }
-        if (doStress) stress = mdiv(stress, mdet(cell.hSize));
+        if (doStress) {
+            stress = mdiv(stress, mdet(cell.hSize));
+            // the work of the velocity gradient, ContactLoop.cpp:236-246
+            const double vol = mdet(cell.hSize);
+            if (cfg.track_energy) {
+                const M3 midStress = mscale(madd(stress, prevStress), .5);
+                const double midVol = !std::isnan(prevVol) ? .5 * (prevVol + vol) : vol;
+                const M3 gm = mmul(cell.gradV, midStress);
+                const double dW = ((-((gm.m[0][0] + gm.m[1][1]) + gm.m[2][2])) * cfg.dt) * midVol;
+                energy[EN_GRADV] += dW;
+                if (dW != 0) ecreated[EN_GRADV] = 1;
+            }
+            prevVol = vol;
+            prevStress = stress;
+        }
         if (deterministic && cfg.apply_forces) {
             for (Contact* C : linView) {
                 if (!C->isReal()) continue;

@@ -127,7 +127,7 @@ int wo_get_nodes(void* s, double* pos, double* ori, double* vel, double* ang_vel
 int wo_get_stats(void* s, wo_stats* out);
 int wo_get_dyndt(void* s, wo_dyndt_state* out);
 /* Scene.energy in the order kinetic, kinTrans, kinRot, grav, nonviscDamp, elast, plast, broken,
-   viscN, viscT, and whether each entry exists */
+   viscN, viscT, gradV, and whether each entry exists */
 int wo_get_energy(void* s, double* values, int32_t* created);
 int64_t wo_num_contacts(void* s);
 /* Contacts as (lo id, hi id) pairs plus state. Arrays sized n = wo_num_contacts.

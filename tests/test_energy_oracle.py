@@ -117,6 +117,26 @@ def test_friction_and_hertz_dissipation(oracle_lib):
     assert worst < 2e-2 and e["viscN"] > 0 and "kinTrans" in e and "kinRot" in e and "kinetic" not in e
 
 
+def test_periodic_gradv_work_balance(oracle_lib):
+    """A periodic packing compressed and sheared by the cell, without Leapfrog damping: the work of
+    the velocity gradient (ContactLoop.cpp:236-246, negative: energy put in) balances the kinetic,
+    elastic and plastic entries to a few per cent once the packing is loaded."""
+    from woodem_gb300 import scenes
+    S = scenes.periodic_shear(n=600, seed=3, fill_fraction=0.4, shear_rate=0.0)
+    g = -30.0 * np.eye(3)
+    g[0, 2] = 40.0
+    S.cell.nextGradV = g
+    S.trackEnergy = True
+    S.engines[0].damping = 0.0
+    S.engines[2].evalStress = True
+    O = _oracle(S)
+    O.run(450)
+    for _ in range(3):
+        O.run(150)
+        e = O.energy()
+        assert e["gradV"] < 0 and abs(sum(e.values())) < 0.03 * sum(abs(v) for v in e.values())
+
+
 def test_refusals():
     from woodem_gb300 import scenes
     S = scenes.box_settle_small(n=50, seed=0, precision="fp32")

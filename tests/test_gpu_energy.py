@@ -60,15 +60,18 @@ def test_drum_hertz_energies_kin_split(gpu_lib):
     assert {"kinTrans", "kinRot", "grav", "elast", "viscN"} <= set(e) and "kinetic" not in e
 
 
-def test_periodic_energies(gpu_lib):
+@pytest.mark.parametrize("eval_stress", [False, True])
+def test_periodic_energies(eval_stress, gpu_lib):
     """Periodic cell compressed and sheared (no Leapfrog energies in the first step: gradV is not
-    the identity)."""
+    the identity); with ContactLoop.evalStress, the work of the velocity gradient (gradV)."""
     S = scenes.periodic_shear(n=600, seed=3, fill_fraction=0.4, shear_rate=0.0)
     g = -30.0 * np.eye(3)
     g[0, 2] = 40.0
     S.cell.nextGradV = g
     S.trackEnergy = True
-    _run_pair(S, 3, 300)
+    S.engines[2].evalStress = eval_stress
+    e = _run_pair(S, 3, 300)
+    assert ("gradV" in e) == eval_stress
 
 
 def test_broken_contacts_no_slip(gpu_lib):

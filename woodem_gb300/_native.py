@@ -38,7 +38,7 @@ class wg_config(C.Structure):
     ]
 
 # Scene.energy entries in the order of WG_ENERGY_NAMES (include/woo_gpu.h)
-ENERGY_NAMES = ("kinetic", "kinTrans", "kinRot", "grav", "nonviscDamp", "elast", "plast", "broken", "viscN", "viscT")
+ENERGY_NAMES = ("kinetic", "kinTrans", "kinRot", "grav", "nonviscDamp", "elast", "plast", "broken", "viscN", "viscT", "gradV")
 
 
 class wg_dyndt_state(C.Structure):

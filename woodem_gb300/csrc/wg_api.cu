@@ -712,9 +712,27 @@ int Sim::ensureEnergyCapacity() {
         dEnergy = (double*)dalloc(sizeof(double) * WG_ENERGY_N);
         dECreated = (int32_t*)dalloc(sizeof(int32_t) * WG_ENERGY_N);
         dEPartial = (double*)dalloc(sizeof(double) * EN_CON_NCOL * 256);
-        if (!dEnergy || !dECreated || !dEPartial) return fail(WG_ERR_CUDA, "out of device memory (energy)");
+        dEPrev = (double*)dalloc(sizeof(double) * 10);
+        if (!dEnergy || !dECreated || !dEPartial || !dEPrev) return fail(WG_ERR_CUDA, "out of device memory (energy)");
         WG_CUDA_TRY(cudaMemsetAsync(dEnergy, 0, sizeof(double) * WG_ENERGY_N, S.stream));
         WG_CUDA_TRY(cudaMemsetAsync(dECreated, 0, sizeof(int32_t) * WG_ENERGY_N, S.stream));
+        // ContactLoop.prevStress = 0, prevVol = NaN (ContactLoop.hpp:119-123)
+        double prev[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, std::numeric_limits<double>::quiet_NaN()};
+        WG_CUDA_TRY(cudaMemcpyAsync(dEPrev, prev, sizeof(prev), cudaMemcpyHostToDevice, S.stream));
+        WG_CUDA_TRY(cudaStreamSynchronize(S.stream));
+    }
+    if (cfg.periodic && cfg.eval_stress) {
+        const int64_t need = 9 * (std::max<int64_t>(1, (I.nAct + 255) / 256) + 1);
+        if (stressCap < need) {
+            if (dStress) dfree(dStress);
+            stressCap = need + need / 2;
+            dStress = (double*)dalloc(sizeof(double) * stressCap);
+            if (!dStress) return fail(WG_ERR_CUDA, "out of device memory (stress)");
+            if (graphExec) {
+                cudaGraphExecDestroy(graphExec);
+                graphExec = nullptr;
+            }
+        }
     }
     if (eNode.cap < N.n) {
         if (eNode.col) dfree(eNode.col);
@@ -861,6 +879,12 @@ int Sim::run(int64_t n) {
                                 (contactBlock > 0 && contactBlock <= 128) ? contactBlock : 128, &eCon);
             launch_energy_sum(stream, eCon, 1, I.nAct, dEPartial, dEnergy, dECreated, dFlags, false);
             launches += 2;
+            if (cfg.periodic && cfg.eval_stress) {
+                // the stress of every step, for the gradV work (capacity ensured with the energy scratch)
+                launch_stress(stream, N, P, C, I, sp, dStress + 9, stressCap - 9, dStress);
+                launch_energy_gradv(stream, dStress, sp, dEPrev, dEnergy, dECreated, dFlags);
+                launches += 3;
+            }
         } else
             launch_contact_fp64(stream, N, P, C, I, dMats, sp, dStep, dFlags, cfg.periodic != 0,
                                 (contactBlock > 0 && contactBlock <= 128) ? contactBlock : 128);  // launch bounds 128

@@ -18,7 +18,8 @@ enum : uint32_t {
 };
 // Energy tracking (Scene.trackEnergy, core/EnergyTracker.hpp): the slots of Scene.energy, in the
 // order of WG_ENERGY_NAMES (include/woo_gpu.h). kinetic/kinTrans/kinRot/elast are reset every step.
-enum { EN_KINETIC, EN_KINTRANS, EN_KINROT, EN_GRAV, EN_DAMP, EN_ELAST, EN_PLAST, EN_BROKEN, EN_VISCN, EN_VISCT, EN_N };
+enum { EN_KINETIC, EN_KINTRANS, EN_KINROT, EN_GRAV, EN_DAMP, EN_ELAST, EN_PLAST, EN_BROKEN, EN_VISCN, EN_VISCT, EN_GRADV, EN_N };
+static_assert(EN_N == WG_ENERGY_N, "energy slots");
 // One step's contributions of each node / active contact, SoA columns of `cap` doubles each: the
 // values and, for the entries a zero addition creates, the number of additions.
 enum { EN_NODE_K0, EN_NODE_K1, EN_NODE_GRAV, EN_NODE_DAMP, EN_NODE_NKIN, EN_NODE_NGRAV, EN_NODE_NCOL };
@@ -236,6 +237,10 @@ void launch_forces(cudaStream_t st, const DevNodes& N, const DevParticles& P, co
 void launch_advance(cudaStream_t st, long long* dStep, const int* dFlags);
 // Adds one step's node (which = 0) or contact (which = 1) contributions in E to the energy slots;
 // partial holds EN_CON_NCOL * 256 doubles.
+// ContactLoop's gradV work of a periodic step from the step's stress sum (out of launch_stress);
+// prev holds the previous stress (9) and cell volume (NaN at first).
+void launch_energy_gradv(cudaStream_t st, const double* sum9, const ScenePar* sp, double* prev, double* energy, int32_t* created,
+                         const int* dFlags);
 void launch_energy_sum(cudaStream_t st, const EnergyCols& E, int which, int64_t n, double* partial, double* energy, int32_t* created,
                        const int* dFlags, bool kinSplit);
 // DynDt: per-end stiffness of the real contacts into kA/kB (zeroed by the caller, I.endCap
@@ -399,6 +404,7 @@ struct Sim {
     double* dEnergy = nullptr;      // WG_ENERGY_N values
     int32_t* dECreated = nullptr;   // WG_ENERGY_N flags
     double* dEPartial = nullptr;    // EN_CON_NCOL * 256 block partials
+    double* dEPrev = nullptr;       // periodic gradV work: previous stress (9) and volume
     int ensureEnergyCapacity();
     // timing
     std::vector<cudaEvent_t> evPool;  // per queued step: before Leapfrog, before contacts, after

@@ -669,6 +669,35 @@ __global__ void k_energy_final(const double* __restrict__ partial, int nb, int w
         if (vt != 0) created[EN_VISCT] = 1;
     }
 }
+// ContactLoop::run, pkg/dem/ContactLoop.cpp:236-246: stress = sum / volume, then
+// dW = -tr(gradV * (stress + prevStress)/2) * dt * midVol, midVol the mean of this step's and the
+// previous step's cell volume (this step's at first); prev takes this step's stress and volume.
+__global__ void k_energy_gradv(const double* __restrict__ sum9, const ScenePar* __restrict__ sp, double* __restrict__ prev,
+                               double* __restrict__ energy, int32_t* __restrict__ created, const int* __restrict__ dFlags) {
+    if (threadIdx.x != 0 || halted(dFlags) || dFlags[FL_FULL]) return;
+    const double* a = sp->hSize;
+    const double vol = (a[0] * (a[4] * a[8] - a[5] * a[7]) - a[1] * (a[3] * a[8] - a[5] * a[6])) + a[2] * (a[3] * a[7] - a[4] * a[6]);
+    double st[9], mid[9];
+    for (int q = 0; q < 9; q++) {
+        st[q] = sum9[q] / vol;
+        mid[q] = .5 * (st[q] + prev[q]);
+    }
+    const double pv = prev[9];
+    const double midVol = !isnan(pv) ? .5 * (pv + vol) : vol;
+    const double* g = sp->gradV;
+    double tr = 0;
+    for (int i = 0; i < 3; i++) tr = tr + ((g[3 * i] * mid[i] + g[3 * i + 1] * mid[3 + i]) + g[3 * i + 2] * mid[6 + i]);
+    const double dW = ((-tr) * sp->dt) * midVol;
+    energy[EN_GRADV] += dW;
+    if (dW != 0) created[EN_GRADV] = 1;
+    for (int q = 0; q < 9; q++) prev[q] = st[q];
+    prev[9] = vol;
+}
+void launch_energy_gradv(cudaStream_t st, const double* sum9, const ScenePar* sp, double* prev, double* energy, int32_t* created,
+                         const int* dFlags) {
+    k_energy_gradv<<<1, 32, 0, st>>>(sum9, sp, prev, energy, created, dFlags);
+}
+
 void launch_energy_sum(cudaStream_t st, const EnergyCols& E, int which, int64_t n, double* partial, double* energy, int32_t* created,
                        const int* dFlags, bool kinSplit) {
     const int ncol = which == 0 ? (int)EN_NODE_NCOL : (int)EN_CON_NCOL;
