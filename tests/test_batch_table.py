@@ -252,3 +252,25 @@ def test_cli_dry_run(tmp_path, capsys):
     sim = tmp_path / "sim.py"
     sim.write_text("from woodem_gb300.scenes import BoxSettle\npre = BoxSettle(n=100)\n")
     assert isinstance(_table.loadSimulation(str(sim)), scenes.BoxSettle)
+
+
+def test_spread_and_json(tmp_path):
+    """dbToSpread (CSV) and dbToJSON of a results database (py/batch.py:245-370)."""
+    import woodem_gb300 as woo
+    db = str(tmp_path / "r.sqlite")
+    for k in range(3):
+        S = woo.Scene()
+        S.tags["title"] = "t%d" % k
+        batch.writeResults(S, defaultDb=db, quiet=True, Ek=float(k), nest={"a": [k, k + 1]})
+    txt = batch.dbToSpread(db)
+    cols = {line.split(",")[0]: line.split(",")[1:] for line in txt.strip().splitlines()}
+    assert txt.splitlines()[0].startswith("title,") and cols["title"] == ["t0", "t1", "t2"]
+    assert cols["misc.Ek"] == ["0.0", "1.0", "2.0"] and cols["misc.nest.a.1"] == ["1", "2", "3"]
+    assert not any(k.startswith("tags") for k in cols)
+    txt = batch.dbToSpread(db, rows=True, selector=lambda r: r["title"] != "t1")
+    lines = txt.strip().splitlines()
+    assert len(lines) == 3 and lines[0].split(",")[0] == "title"
+    with pytest.raises(NotImplementedError):
+        batch.dbToSpread(db, out=str(tmp_path / "x.xls"))
+    import json
+    assert [r["title"] for r in json.loads(batch.dbToJSON(db))] == ["t0", "t1", "t2"]

@@ -358,6 +358,69 @@ def dbReadResults(db, basicTypes=False):
     return ret
 
 
+def dbToJSON(db, **kw):
+    """The results database as a JSON string (py/batch.py:245-252); ``kw`` go to json.dumps."""
+    return json.dumps(dbReadResults(db, basicTypes=True), cls=_JSON, **kw)
+
+
+def _flatten(obj, path="", sep=".", out=None):
+    """Nested dicts and lists as {path: value}, path components joined by ``sep``."""
+    if out is None:
+        out = {}
+    if isinstance(obj, dict):
+        for k, v in obj.items():
+            _flatten(v, (path + sep if path else "") + str(k), sep, out)
+    elif isinstance(obj, (list, tuple)):
+        for i, v in enumerate(obj):
+            _flatten(v, (path + sep if path else "") + str(i), sep, out)
+    else:
+        out[path] = obj
+    return out
+
+
+def _naturalKey(s):
+    return [int(t) if t.isdigit() else t for t in re.split(r"(\d+)", s)]
+
+
+def dbToSpread(db, out=None, dialect="excel", rows=False, series=True, ignored=("plotData", "tags"),
+               sortFirst=("title", "batchtable", "batchTableLine", "finished", "sceneId", "duration"), selector=None):
+    """Flatten the rows of a results database and write them as CSV (py/batch.py:255-370): one
+    column per simulation (one row with ``rows``), fields named by their path (``misc.Ek``), sorted
+    naturally with ``sortFirst`` first; ``ignored`` fields and attributes left out; ``selector``
+    (a function of the row dict) picks rows. Dialects ``excel`` and ``excel-tab``; spreadsheet
+    files (xls, xlsx) need packages that are not installed. ``series`` are not written (they go to
+    separate sheets in the reference). Writes to ``out`` or returns the text."""
+    import csv
+    import io
+    if dialect in ("xls", "xlsx") or (out and str(out).lower().endswith((".xls", ".xlsx"))):
+        raise NotImplementedError("spreadsheet output needs xlwt/openpyxl, which are not installed; use a CSV dialect")
+    ign = [i.lower() for i in ignored]
+    first = [f.lower() for f in sortFirst]
+    recs = []
+    for r in dbReadResults(db, basicTypes=True):
+        if selector is not None and not selector(r):
+            continue
+        r = {k: v for k, v in r.items() if k.lower() not in ign and k != "series"}
+        flat = _flatten(r)
+        recs.append({k: v for k, v in flat.items() if k.split(".")[-1].lower() not in ign})
+    fields = sorted({k for r in recs for k in r}, key=lambda f: (0, first.index(f.lower())) if f.lower() in first
+                    else (1, _naturalKey(f)))
+    buf = io.StringIO()
+    w = csv.writer(buf, dialect=dialect)
+    if rows:
+        w.writerow(fields)
+        for r in recs:
+            w.writerow([r.get(f, "") for f in fields])
+    else:
+        for f in fields:
+            w.writerow([f] + [r.get(f, "") for r in recs])
+    text = buf.getvalue()
+    if out is None:
+        return text
+    with open(out, "w", newline="") as fo:
+        fo.write(text)
+
+
 def cartProdParamTable(params, out, same=""):
     """Write a text table traversing the cartesian product of ``params`` (a dict, ordered, of
     name -> list of values; a tuple key spans several columns, its values are tuples), as

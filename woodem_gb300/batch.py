@@ -137,8 +137,8 @@ class Batch:
 
 
 # parameter tables of woo-batch (py/batch.py), feeding Batch
-from ._table import (TableParamReader, cartProdParamTable, dbFormatVersion, dbReadResults, inBatch, options,  # noqa: E402,F401
-                     readParamsFromTable, runPreprocessor, runTable, planTable, writeResults)
+from ._table import (TableParamReader, cartProdParamTable, dbFormatVersion, dbReadResults, dbToJSON, dbToSpread,  # noqa: E402,F401
+                     inBatch, options, readParamsFromTable, runPreprocessor, runTable, planTable, writeResults)
 
 if __name__ == "__main__":
     import sys
