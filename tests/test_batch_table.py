@@ -274,3 +274,16 @@ def test_spread_and_json(tmp_path):
         batch.dbToSpread(db, out=str(tmp_path / "x.xls"))
     import json
     assert [r["title"] for r in json.loads(batch.dbToJSON(db))] == ["t0", "t1", "t2"]
+
+
+def test_deprecated_utils_aliases(tmp_path):
+    import warnings
+    from woodem_gb300 import utils
+    import woodem_gb300 as woo
+    with warnings.catch_warnings(record=True) as w:
+        warnings.simplefilter("always")
+        assert utils.runningInBatch() is False and utils.waitIfBatch() is None
+        S = woo.Scene()
+        utils.readParamsFromTable(S, a=1)
+        assert S.lab.table.a == 1
+    assert sum(issubclass(x.category, DeprecationWarning) for x in w) == 3

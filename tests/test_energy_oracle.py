@@ -5,6 +5,7 @@ Leapfrog energy expressions (Leapfrog.cpp:52-97) evaluated step by step in Pytho
 falling, damped sphere (same operations, same order: equal bit for bit), and by energy balances:
 with all dissipation and work entries counted, the total of Scene.energy stays at the initial
 kinetic energy (two spheres colliding elastically, with friction and with Hertz viscosity)."""
+import math
 
 import numpy as np
 import pytest
@@ -161,3 +162,14 @@ def test_energy_tracker_api():
         E["c"]
     E.clear()
     assert len(E) == 0 and E.relErr() == 0.0
+
+
+def test_unbalanced_energy():
+    S = woo.core.Scene(fields=[DemField()])
+    with pytest.raises(RuntimeError):
+        utils.unbalancedEnergy(S)
+    S.trackEnergy = True
+    assert math.isnan(utils.unbalancedEnergy(S))
+    S.energy["kinetic"] = 2.0
+    S.energy["elast"] = 4.0
+    assert utils.unbalancedEnergy(S) == 0.5

@@ -50,6 +50,12 @@ def inBatch():
     return bool(options.batchTable)
 
 
+def wait():
+    """py/batch.py:32-38 starts the batch line's master scene and blocks until it stops; here every
+    S.run() call is synchronous, so there is nothing to wait for."""
+    return None
+
+
 def _evalNamespace(**extra):
     import woodem_gb300
     ns = dict(math.__dict__)

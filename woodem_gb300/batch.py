@@ -138,7 +138,7 @@ class Batch:
 
 # parameter tables of woo-batch (py/batch.py), feeding Batch
 from ._table import (TableParamReader, cartProdParamTable, dbFormatVersion, dbReadResults, dbToJSON, dbToSpread,  # noqa: E402,F401
-                     inBatch, options, readParamsFromTable, runPreprocessor, runTable, planTable, writeResults)
+                     inBatch, options, readParamsFromTable, runPreprocessor, runTable, planTable, wait, writeResults)
 
 if __name__ == "__main__":
     import sys

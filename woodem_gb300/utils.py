@@ -168,3 +168,47 @@ def facet(vertices, fakeVel=None, halfThick=0.0, fixed=True, wire=True, color=No
     p.mask = mask
     p.shape.visible = visible
     return p
+
+
+def unbalancedEnergy(S):
+    """Kinetic over elastic energy (py/utils.py:816-822); NaN when either is missing or elast is 0."""
+    if not S.trackEnergy:
+        raise RuntimeError("Scene.trackEnergy==False")
+    if "elast" not in S.energy or "kinetic" not in S.energy:
+        return float("nan")
+    if S.energy["elast"] == 0:
+        return float("nan")
+    return S.energy["kinetic"] / S.energy["elast"]
+
+
+def _deprecatedUtilsFunction(old, new):
+    import warnings
+    warnings.warn("Function utils.%s is deprecated, use %s instead." % (old, new), stacklevel=3, category=DeprecationWarning)
+
+
+def runningInBatch():
+    """Deprecated alias of woo.batch.inBatch (py/utils.py:845-847)."""
+    from . import batch
+    _deprecatedUtilsFunction("runningInBatch", "woo.batch.inBatch")
+    return batch.inBatch()
+
+
+def waitIfBatch():
+    """Deprecated alias of woo.batch.wait."""
+    from . import batch
+    _deprecatedUtilsFunction("waitIfBatch", "woo.batch.wait")
+    return batch.wait()
+
+
+def readParamsFromTable(*args, **kw):
+    """Deprecated alias of woo.batch.readParamsFromTable."""
+    from . import batch
+    _deprecatedUtilsFunction("readParamsFromTable", "woo.batch.readParamsFromTable")
+    return batch.readParamsFromTable(*args, **kw)
+
+
+def runPreprocessorInBatch(*args, **kw):
+    """Deprecated alias of woo.batch.runPreprocessor."""
+    from . import batch
+    _deprecatedUtilsFunction("runPreprocessorInBatch", "woo.batch.runPreprocessor")
+    return batch.runPreprocessor(*args, **kw)
