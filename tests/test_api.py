@@ -121,3 +121,17 @@ def test_pack_rsa_non_overlapping(gpu_lib):
     for i, j in t.query_pairs(2 * r.max()):
         assert np.linalg.norm(c[i] - c[j]) >= r[i] + r[j] - 1e-15
     assert np.all(c - r[:, None] >= -1e-15) and np.all(c + r[:, None] <= 0.2 + 1e-15)
+
+
+def test_quadrilateral_mesh():
+    """py/triangulated.py:70-83: 2*div0*div1 facets covering the quadrilateral, vertices shared."""
+    ff = triangulated.quadrilateral((0, 0, 0), (2, 0, 0), (0, 3, 0), (2, 3, 0), div=(4, 3))
+    assert len(ff) == 24
+    area = sum(0.5 * np.linalg.norm(np.cross(np.asarray(f.shape.nodes[1].pos) - np.asarray(f.shape.nodes[0].pos),
+                                             np.asarray(f.shape.nodes[2].pos) - np.asarray(f.shape.nodes[0].pos))) for f in ff)
+    assert area == pytest.approx(6.0, rel=1e-12)
+    assert len({id(n) for f in ff for n in f.shape.nodes}) == 5 * 4
+    assert len(triangulated.quadrilateral((0, 0, 0), (1, 0, 0), (0, 1, 0), (1, 1, 0))) == 8
+    assert len(triangulated.quadrilateral((0, 0, 0), (1, 0, 0), (0, 1, 0), (1, 1, 0), size=0.25)) == 32
+    with pytest.raises(ValueError):
+        triangulated.quadrilateral((0, 0, 0), (1, 0, 0), (0, 1, 0), (1, 1, 0), size=0.5, div=(2, 2))

@@ -1,4 +1,5 @@
-"""``woo.triangulated.cylinder`` counterpart (py/triangulated.py:10-69).
+"""``woo.triangulated`` counterparts: ``cylinder`` (py/triangulated.py:10-69) and
+``quadrilateral`` (py/triangulated.py:70-83).
 
 The reference builds the mantle through GTS (un-vendored here): rings of ``div``
 points (the last one coinciding with the first and merged) at ``axDiv+1`` axial
@@ -83,3 +84,33 @@ def cylinder(A, B, radius, div=20, axDiv=1, capA=False, capB=False, masks=None, 
             if capB:
                 caps[-1].mask = masks[2]
     return caps + ff
+
+
+def quadrilateral(A, B, C, D, size=0, div=(0, 0), **kw):
+    """Triangulated quadrilateral ABDC (a skew one when the points are not coplanar),
+    py/triangulated.py:70-83: ``div`` subdivisions along AB (and CD) and along AC (and BD), or
+    subdivisions of at most ``size`` (at least 2 each), 2x2 by default; two facets per cell of
+    the bilinear grid A + ac*(C-A) + ab*((B + ac*(D-B)) - (A + ac*(C-A))), vertices shared. (The
+    reference normalises the AB-CD direction of that grid, which gives the same points only for
+    sides of unit length.) ``kw`` go to utils.facet."""
+    A, B, C, D = (np.asarray(x, dtype=float) for x in (A, B, C, D))
+    div = tuple(int(x) for x in div)
+    if sum(div) > 0:
+        if min(div) < 1:
+            raise ValueError("Both components of div must be positive")
+        if size > 0:
+            raise ValueError("only one of *div* or *size* may be given (not both)")
+    else:
+        l1 = min(np.linalg.norm(A - C), np.linalg.norm(D - B))
+        l2 = min(np.linalg.norm(A - B), np.linalg.norm(C - D))
+        div = (int(max(2, math.ceil(l1 / size))), int(max(2, math.ceil(l2 / size)))) if size != 0 else (2, 2)
+    AC, BD = C - A, D - B
+    aabb, aacc = np.linspace(0, 1, div[0] + 1), np.linspace(0, 1, div[1] + 1)
+    nodes = [[Node(pos=(A + ac * AC) + ab * ((B + ac * BD) - (A + ac * AC))) for ac in aacc] for ab in aabb]
+    out = []
+    for i in range(div[0]):
+        for j in range(div[1]):
+            a, b, c, d = nodes[i][j], nodes[i + 1][j], nodes[i + 1][j + 1], nodes[i][j + 1]
+            out.append(utils.facet([a, b, c], **kw))
+            out.append(utils.facet([a, c, d], **kw))
+    return out
