@@ -93,3 +93,25 @@ def test_checkpoint_of_another_scene_is_refused(tmp_path, gpu_lib):
     S1.close()
     with pytest.raises(ValueError):
         checkpoint.load(scenes.box_settle_scaled(300, 0.007, seed=1), path)
+
+
+@pytest.mark.parametrize("kind", ["box", "periodic"])
+def test_scene_save_load_resume(kind, tmp_path, gpu_lib):
+    """Scene.save / Scene.load (the scene pickled with its contact container) resume like the
+    checkpoint: FP64 bitwise."""
+    import woodem_gb300 as woo
+    build, n1, n2 = BUILDERS[kind]
+    path = str(tmp_path / "scene.bin.gz")
+    S1 = build("fp64")
+    S1.run(n1)
+    S1.save(path)
+    S1.run(n2)
+    ref, step1 = _nodes(S1), S1.step
+    S1.close()
+    S2 = woo.core.Scene.load(path)
+    assert S2.step == n1
+    S2.run(n2)
+    got = _nodes(S2)
+    assert S2.step == step1
+    for k in ("pos", "vel", "angVel", "force", "torque"):
+        assert np.array_equal(ref[k], got[k]), k

@@ -45,15 +45,12 @@ def fingerprint(A):
     return h.hexdigest()
 
 
-def save(S, path):
-    """Write the device state of scene S (which has run at least once) to ``path``."""
+def contact_snapshot(S):
+    """The contact container of S's device simulation with its persistent state
+    (``wg_get_contact_state``): {con_key, con_flags, con_step0, con_cell_dist, con_state,
+    state_cols}."""
     sim = S._sim
-    if sim is None:
-        raise RuntimeError("the scene has no device state to save; run it first")
-    S.sync()
     L, h = sim.H.L, sim.H.h
-    nd = S.dem._nodes.soa
-    arrays = {"node_" + k: np.array(nd.col(k)) for k in _NODE_COLS}
     ncols = int(L.wg_contact_state_cols(h))
     n = C.c_int64()
     r = L.wg_get_contact_state(h, 0, C.byref(n), None, None, None, None, None)
@@ -68,7 +65,37 @@ def save(S, path):
     if m:
         sim.H.check(L.wg_get_contact_state(h, m, C.byref(n), key.ctypes.data, flags.ctypes.data, step0.ctypes.data, cdist.ctypes.data,
                                            cols.ctypes.data), "get_contact_state")
-    arrays.update(con_key=key, con_flags=flags, con_step0=step0, con_cell_dist=cdist, con_state=cols)
+    return {"con_key": key, "con_flags": flags, "con_step0": step0, "con_cell_dist": cdist, "con_state": cols,
+            "state_cols": ncols}
+
+
+def restore_contacts(S, snap):
+    """Upload the contact container ``snap`` (of contact_snapshot) into S's device simulation,
+    creating it from S's host state; the next step starts with a full collider run that keeps the
+    state of the real contacts."""
+    sim = S._ensure_sim()
+    L, h = sim.H.L, sim.H.h
+    key = np.ascontiguousarray(snap["con_key"], np.uint64)
+    m = len(key)
+    ncols = int(snap["state_cols"])
+    cols = np.ascontiguousarray(snap["con_state"], float).reshape(m, ncols)
+    sim.H.check(L.wg_set_contact_state(h, m, key.ctypes.data, np.ascontiguousarray(snap["con_flags"], np.uint32).ctypes.data,
+                                       np.ascontiguousarray(snap["con_step0"], np.int32).ctypes.data,
+                                       np.ascontiguousarray(snap["con_cell_dist"], np.int32).ctypes.data, cols.ctypes.data,
+                                       ncols), "set_contact_state")
+
+
+def save(S, path):
+    """Write the device state of scene S (which has run at least once) to ``path``."""
+    sim = S._sim
+    if sim is None:
+        raise RuntimeError("the scene has no device state to save; run it first")
+    S.sync()
+    nd = S.dem._nodes.soa
+    arrays = {"node_" + k: np.array(nd.col(k)) for k in _NODE_COLS}
+    snap = contact_snapshot(S)
+    ncols = snap.pop("state_cols")
+    arrays.update(snap)
     meta = {"step": int(S.step), "time": float(S.time), "dt": float(S.dt), "precision": S.gpu.precision,
             "periodic": bool(S.isPeriodic), "n_nodes": int(len(nd)), "state_cols": ncols, "fingerprint": fingerprint(sim.A)}
     dyn = _dyndt(S)
@@ -123,13 +150,6 @@ def load(S, path):
         S.cell.trsf = arrays["cell_trsf"]
         S.cell.setCurrGradV(arrays["cell_gradV"])
         S.cell.nextGradV = arrays["cell_nextGradV"]
-    sim = S._ensure_sim()
-    L, h = sim.H.L, sim.H.h
-    key = np.ascontiguousarray(arrays["con_key"], np.uint64)
-    m = len(key)
-    cols = np.ascontiguousarray(arrays["con_state"], float).reshape(m, meta["state_cols"])
-    sim.H.check(L.wg_set_contact_state(h, m, key.ctypes.data, np.ascontiguousarray(arrays["con_flags"], np.uint32).ctypes.data,
-                                       np.ascontiguousarray(arrays["con_step0"], np.int32).ctypes.data,
-                                       np.ascontiguousarray(arrays["con_cell_dist"], np.int32).ctypes.data, cols.ctypes.data,
-                                       meta["state_cols"]), "set_contact_state")
+    restore_contacts(S, dict({k: arrays[k] for k in ("con_key", "con_flags", "con_step0", "con_cell_dist", "con_state")},
+                             state_cols=meta["state_cols"]))
     return S

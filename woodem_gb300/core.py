@@ -137,6 +137,9 @@ class Cell(Object):
         return float(np.linalg.det(np.asarray(self.hSize)))
 
 
+_TMP = {}  # scenes saved in memory (Scene.saveTmp)
+
+
 class EnergyTracker:
     """Scene.energy (core/EnergyTracker.hpp:10-80): named energies. With Scene.trackEnergy the
     entries of Leapfrog and of the contact laws are computed on the device every step and copied
@@ -302,12 +305,90 @@ class Scene(Object):
         if self._sim is not None:
             self._sim.close()
             self._sim = None
+        # a contact container loaded with the scene belongs to its particles as they were
+        self.__dict__.pop("_pendingContacts", None)
+
+    # --- saving and loading (lib/object/ObjectIO.hpp:28-90): the scene description and state are
+    # pickled (gzip-compressed for names ending in .gz), the contact container with its persistent
+    # state rides along and is uploaded with the state at the next run, so that a loaded scene
+    # continues as the saved one would have.
+    def __getstate__(self):
+        d = self.__dict__.copy()
+        d["_sim"] = None
+        return d
+
+    def _saveBytes(self):
+        import pickle
+        snap = self.__dict__.get("_pendingContacts")
+        if self._sim is not None:
+            from . import checkpoint
+            self.sync()
+            snap = checkpoint.contact_snapshot(self)
+        had, old = "_pendingContacts" in self.__dict__, self.__dict__.get("_pendingContacts")
+        self.__dict__["_pendingContacts"] = snap
+        try:
+            return pickle.dumps(self, protocol=pickle.HIGHEST_PROTOCOL)
+        finally:
+            if had:
+                self.__dict__["_pendingContacts"] = old
+            else:
+                self.__dict__.pop("_pendingContacts", None)
+
+    @staticmethod
+    def _fromBytes(b):
+        import pickle
+        S = pickle.loads(b)
+        if S.__dict__.get("_pendingContacts") is None:
+            S.__dict__.pop("_pendingContacts", None)
+        for f in S.fields:
+            f.scene = S
+        return S
+
+    def save(self, fileName):
+        """Save the scene (Scene.save): its description, state, contacts, engines and counters."""
+        b = self._saveBytes()
+        if str(fileName).endswith(".gz"):
+            import gzip
+            with gzip.open(fileName, "wb") as f:
+                f.write(b)
+        else:
+            with open(fileName, "wb") as f:
+                f.write(b)
+
+    @staticmethod
+    def load(fileName):
+        """A scene saved with Scene.save."""
+        if str(fileName).endswith(".gz"):
+            import gzip
+            with gzip.open(fileName, "rb") as f:
+                return Scene._fromBytes(f.read())
+        with open(fileName, "rb") as f:
+            return Scene._fromBytes(f.read())
+
+    def saveTmp(self, name=""):
+        """Save the scene in memory under ``name`` (Scene.saveTmp)."""
+        _TMP[name] = self._saveBytes()
+
+    @staticmethod
+    def loadTmp(name=""):
+        """The scene saved in memory under ``name``."""
+        if name not in _TMP:
+            raise KeyError("No memory-saved scene named '%s'" % name)
+        return Scene._fromBytes(_TMP[name])
+
+    def deepcopy(self):
+        """An independent copy of the scene (state and contacts included)."""
+        return Scene._fromBytes(self._saveBytes())
 
     def _ensure_sim(self):
         if self._sim is None or self._sim.dirty_structure:
             if self._sim is not None:
                 self._sim.close()
             self._sim = _plan.Simulation(self)
+            pend = self.__dict__.pop("_pendingContacts", None)
+            if pend is not None:
+                from . import checkpoint
+                checkpoint.restore_contacts(self, pend)
         return self._sim
 
     def run(self, nSteps=None, wait=True):
