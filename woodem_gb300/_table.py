@@ -23,7 +23,6 @@ import math
 import os
 import re
 import runpy
-import sqlite3
 import sys
 
 import numpy as np
@@ -310,6 +309,7 @@ def writeResults(scene, defaultDb="woo-results.sqlite", syncXls=False, dbFmt=Non
         raise ValueError('*fmt* must be one of "sqlite", "hdf5", None (autodetect based on suffix)')
     if syncXls:
         raise NotImplementedError("spreadsheet export needs xlwt/openpyxl, which are not installed")
+    import sqlite3
     newDb = not os.path.exists(db)
     if not quiet:
         print("Writing results to the database %s (%s)" % (db, "new" if newDb else "existing"))
@@ -343,6 +343,7 @@ def writeResults(scene, defaultDb="woo-results.sqlite", syncXls=False, dbFmt=Non
 def dbReadResults(db, basicTypes=False):
     """Rows of a results database as dicts, oldest first (py/batch.py:172-243, SQLite): ``tags``,
     ``plots`` and ``misc`` decoded from JSON, ``series`` as numpy arrays unless ``basicTypes``."""
+    import sqlite3
     conn = sqlite3.connect(db, timeout=sqliteTimeout)
     conn.row_factory = sqlite3.Row
     ret = []
