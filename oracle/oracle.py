@@ -1,4 +1,4 @@
-"""ctypes driver of the CPU oracle (test infrastructure only).
+"""ctypes wrapper of the CPU oracle (test infrastructure only).
 
 Feeds the same flat scene description as the GPU library (woodem_gb300._plan.SceneArrays)
 to libwoo_oracle.so and reads back node state and contacts in the same formats.

@@ -1,7 +1,7 @@
 /*
  * CPU oracle for the Woo DEM hot path -- TEST INFRASTRUCTURE ONLY.
  *
- * This library is the checker: a plain C++17/OpenMP FP64 restatement of the
+ * This library is the oracle: a plain C++17/OpenMP FP64 restatement of the
  * reference's per-step loop (Leapfrog -> InsertionSortCollider -> ContactLoop
  * with the Cg2/Cp2/Law2 functors). Only the test-suite, the smoke check and the
  * CPU-baseline leg of the benchmark load it. The product library never links,
@@ -29,7 +29,7 @@ extern "C" {
 
 /* Mirror of the fields of the reference's engine/functor attributes that the
    hot path reads. Layout identical to wg_config in include/woo_gpu.h so the
-   test drivers can fill both from one description. */
+   tests can fill both from one description. */
 typedef struct wo_config {
     double dt;
     double gravity[3];
