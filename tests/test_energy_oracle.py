@@ -173,3 +173,34 @@ def test_unbalanced_energy():
     S.energy["kinetic"] = 2.0
     S.energy["elast"] = 4.0
     assert utils.unbalancedEnergy(S) == 0.5
+
+
+def _sphere_on_wall():
+    """py/tests/energy.py:71-76: a sphere resting deep in a wall, gravity, Leapfrog damping 0.4,
+    DemField.minimalEngines (with DynDt), dt from dtSafety."""
+    from woodem_gb300.core import Scene
+    from woodem_gb300.dem import Wall, Sphere
+    m = utils.defaultMaterial()
+    return Scene(dtSafety=.9, trackEnergy=True, engines=DemField.minimalEngines(damping=.4),
+                 fields=[DemField(gravity=(0, 0, -10), par=[Wall.make(0, axis=2, sense=1, mat=m),
+                                                            Sphere.make((0, 0, .1), radius=.8, mat=m)])])
+
+
+def test_reference_gravity_and_damping_skip(oracle_lib):
+    """py/tests/energy.py:77-93 (TestLeapfrog): with DemData.gravitySkip on every node there is no
+    grav entry and some nonviscDamp; with dampingSkip some grav and no nonviscDamp entry."""
+    S = _sphere_on_wall()
+    for n in S.dem.nodes:
+        n.dem.gravitySkip = True
+    S.dem.par[-1].vel = (0, 0, -1)
+    O = _oracle(S)
+    O.run(400)
+    e = O.energy()
+    assert "grav" not in e and e["nonviscDamp"] != 0.
+    S = _sphere_on_wall()
+    for n in S.dem.nodes:
+        n.dem.dampingSkip = True
+    O = _oracle(S)
+    O.run(400)
+    e = O.energy()
+    assert e["grav"] != 0. and "nonviscDamp" not in e

@@ -89,6 +89,8 @@ class DemData:
                            lambda s, v: setattr(s, "flags", (s.flags | GRAVITY_SKIP) if v else (s.flags & ~GRAVITY_SKIP)))
     dampingSkip = property(lambda s: bool(s.flags & DAMPING_SKIP),
                            lambda s, v: setattr(s, "flags", (s.flags | DAMPING_SKIP) if v else (s.flags & ~DAMPING_SKIP)))
+    energySkip = property(lambda s: bool(s.flags & ENERGY_SKIP),
+                          lambda s, v: setattr(s, "flags", (s.flags | ENERGY_SKIP) if v else (s.flags & ~ENERGY_SKIP)))
 
     @property
     def isAspherical(self):
@@ -193,6 +195,11 @@ class Shape(Object):
 class Sphere(Shape):
     _attrs = {"radius": NaN}
     _kind = SHAPE_SPHERE
+
+    @staticmethod
+    def make(center, radius, **kw):
+        from . import utils
+        return utils.sphere(center, radius, **kw)
 
     def volume(self):
         return (4 / 3.0) * math.pi * self.radius ** 3

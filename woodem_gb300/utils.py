@@ -212,3 +212,7 @@ def runPreprocessorInBatch(*args, **kw):
     from . import batch
     _deprecatedUtilsFunction("runPreprocessorInBatch", "woo.batch.runPreprocessor")
     return batch.runPreprocessor(*args, **kw)
+
+
+# DemField.minimalEngines is defaultEngines (py/_monkey/aliases.py:102)
+DemField.minimalEngines = staticmethod(defaultEngines)
