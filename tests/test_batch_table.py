@@ -287,3 +287,25 @@ def test_deprecated_utils_aliases(tmp_path):
         utils.readParamsFromTable(S, a=1)
         assert S.lab.table.a == 1
     assert sum(issubclass(x.category, DeprecationWarning) for x in w) == 3
+
+
+def test_reference_batch_results(tmp_path):
+    """py/tests/batch.py:12-40 (TestBatchResults, SQLite): misc values and a Woo object in misc,
+    grouped series, read back; the CSV spreadsheet written."""
+    import math
+    import woodem_gb300 as woo
+    misc = dict(a="a", pi=math.pi, sphere=woo.dem.Sphere(radius=2.3))
+    series = dict(random=np.random.default_rng(0).random(100), ones=np.ones(10))
+    series["group1/item1"] = np.ones(10)
+    series["group1/item2"] = 2 * np.ones(10)
+    series["group2/item1"] = 3 * np.ones(10)
+    S = woo.core.Scene(fields=[woo.dem.DemField()])
+    db = str(tmp_path / "res.sqlite")
+    batch.writeResults(S, defaultDb=db, syncXls=False, quiet=True, series=series, **misc)
+    r = batch.dbReadResults(db)[0]
+    assert r["misc"]["a"] == "a" and r["misc"]["pi"] == math.pi
+    assert isinstance(r["misc"]["sphere"], woo.dem.Sphere) and r["misc"]["sphere"].radius == 2.3
+    assert r["series"]["ones"][2] == 1 and r["series"]["group1/item2"][0] == 2
+    assert batch.dbReadResults(db, basicTypes=True)[0]["misc"]["sphere"]["__class__"] == "woo.dem.Sphere"
+    batch.dbToSpread(db, str(tmp_path / "res.csv"), series=False)
+    assert "misc.sphere.radius" in open(str(tmp_path / "res.csv")).read()

@@ -268,12 +268,40 @@ def runPreprocessor(pre, preFile=None):
 
 
 class _JSON(json.JSONEncoder):
+    """numpy values as lists and numbers; Woo objects as {"__class__": "woo.<module>.<Class>",
+    attribute: value, ...} (the form of the reference's WooJSONEncoder); anything else as text."""
+
     def default(self, o):
+        from .core import Object
         if isinstance(o, np.ndarray):
             return o.tolist()
         if isinstance(o, np.generic):
             return o.item()
+        if isinstance(o, Object):
+            d = {"__class__": "woo.%s.%s" % (type(o).__module__.split(".")[-1], type(o).__name__)}
+            for cls in reversed(type(o).__mro__):
+                for k in getattr(cls, "_attrs", {}):
+                    v = getattr(o, k, None)
+                    if isinstance(v, (int, float, str, bool, list, tuple, dict, np.ndarray, np.generic, Object)) or v is None:
+                        d[k] = v
+            return d
         return str(o)
+
+
+def _decodeObject(d):
+    """The inverse of _JSON for Woo objects: an instance of the named class (woo.dem or woo.core)
+    with the attributes it knows; other dicts unchanged."""
+    name = d.get("__class__")
+    if not isinstance(name, str) or not name.startswith("woo."):
+        return d
+    from . import core, dem
+    cls = getattr(dem, name.split(".")[-1], None) or getattr(core, name.split(".")[-1], None)
+    if cls is None:
+        return d
+    known = set()
+    for c in cls.__mro__:
+        known |= set(getattr(c, "_attrs", {}))
+    return cls(**{k: v for k, v in d.items() if k in known})
 
 
 _COLUMNS = ("formatVersion", "finished", "batchtable", "batchTableLine", "sceneId", "title", "duration", "pre", "tags",
@@ -342,7 +370,8 @@ def writeResults(scene, defaultDb="woo-results.sqlite", syncXls=False, dbFmt=Non
 
 def dbReadResults(db, basicTypes=False):
     """Rows of a results database as dicts, oldest first (py/batch.py:172-243, SQLite): ``tags``,
-    ``plots`` and ``misc`` decoded from JSON, ``series`` as numpy arrays unless ``basicTypes``."""
+    ``plots`` and ``misc`` decoded from JSON (Woo objects rebuilt), ``series`` as numpy arrays;
+    with ``basicTypes`` plain JSON types throughout."""
     import sqlite3
     conn = sqlite3.connect(db, timeout=sqliteTimeout)
     conn.row_factory = sqlite3.Row
@@ -353,7 +382,7 @@ def dbReadResults(db, basicTypes=False):
             for key in row.keys():
                 v = row[key]
                 if key in ("pre", "tags", "plots", "misc"):
-                    v = json.loads(v) if v is not None else None
+                    v = (json.loads(v) if basicTypes else json.loads(v, object_hook=_decodeObject)) if v is not None else None
                 elif key == "series":
                     v = json.loads(v)
                     if not basicTypes:
