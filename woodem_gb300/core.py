@@ -45,6 +45,25 @@ class Object:
     def __repr__(self):
         return "<%s @ %x>" % (type(self).__name__, id(self))
 
+    # Object.dump/dumps/load/loads (lib/object/ObjectIO.hpp:28-90): woodem_gb300._objio
+    def dump(self, out, format="auto"):
+        from . import _objio
+        _objio.dump(self, out, format)
+
+    def dumps(self, format="expr"):
+        from . import _objio
+        return _objio.dumps(self, format)
+
+    @classmethod
+    def load(cls, inFile, format="auto"):
+        from . import _objio
+        return _objio.load(inFile, format, cls)
+
+    @classmethod
+    def loads(cls, data, format="auto"):
+        from . import _objio
+        return _objio.loads(data, format, cls)
+
 
 class Engine(Object):
     """Base engine; ``run`` is never called on the host, engines are compiled into the device plan."""

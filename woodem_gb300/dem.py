@@ -104,6 +104,11 @@ class DemData:
 class Node:
     """A point with position and orientation (core/Field.hpp:50-108) and its DemData."""
 
+    @classmethod
+    def load(cls, inFile, format="auto"):
+        from . import _objio
+        return _objio.load(inFile, format, cls)
+
     __slots__ = ("_store", "_i", "_rec")
 
     def __init__(self, pos=(0, 0, 0), ori=None, dem=None):
@@ -702,11 +707,13 @@ class InsertionSortCollider(Collider):
     """pkg/dem/InsertionSortCollider.hpp:252-265. ``nFullRuns`` is read back from the device."""
     _attrs = {"forceInitSort": False, "noBoundOk": False, "sortAxis": 0, "sortThenCollide": False, "verletDist": -0.05,
               "maxVel2": 0.0, "nFullRuns": 0, "numReinit": 0, "ompTuneSort": (1, 1000, 0), "sortChunks": -1,
-              "paraPeri": False}
+              "paraPeri": False,
+              "boundDispatcher": lambda: [Bo1_Sphere_Aabb(), Bo1_Facet_Aabb(), Bo1_Wall_Aabb()]}
 
     def __init__(self, boundFunctors=None, **kw):
         super().__init__(**kw)
-        self.boundDispatcher = list(boundFunctors) if boundFunctors else [Bo1_Sphere_Aabb(), Bo1_Facet_Aabb(), Bo1_Wall_Aabb()]
+        if boundFunctors:
+            self.boundDispatcher = list(boundFunctors)
 
     def _functors(self):
         return list(self.boundDispatcher)
@@ -715,16 +722,17 @@ class InsertionSortCollider(Collider):
 class ContactLoop(Engine):
     """pkg/dem/ContactLoop.hpp:108-124; special constructor ContactLoop([Cg2],[Cp2],[Law2])."""
     _attrs = {"evalStress": False, "applyForces": True, "updatePhys": False, "dist00": True, "reorderEvery": 1000,
-              "alreadyWarnedNoCollider": False}
+              "alreadyWarnedNoCollider": False, "geoDisp": lambda: [], "phyDisp": lambda: [], "lawDisp": lambda: [],
+              "stress": lambda: np.zeros((3, 3))}
 
     def __init__(self, geoms=None, physs=None, laws=None, **kw):
         super().__init__(**kw)
         if (geoms is None) != (laws is None):
             raise ValueError("Exactly 3 lists of functors must be given")
-        self.geoDisp = list(geoms or [])
-        self.phyDisp = list(physs or [])
-        self.lawDisp = list(laws or [])
-        self.stress = np.zeros((3, 3))
+        if geoms is not None:
+            self.geoDisp = list(geoms)
+            self.phyDisp = list(physs or [])
+            self.lawDisp = list(laws)
 
     def _functors(self):
         return self.geoDisp + self.phyDisp + self.lawDisp
