@@ -37,6 +37,11 @@ def test_scene_save_load_description(tmp_path):
         assert A2.config.keys() == A.config.keys()
         assert S2.engines[-1].nDone == 3 and S2.energy["grav"] == 1.5 and S2.tags["title"] == "saved"
         assert S2.dem.scene is S2 and S2 is not S and "_pendingContacts" not in S2.__dict__
+        # a particle added with a loaded material takes that material's index
+        nm = len(S2.dem._mats)
+        m2 = S2.dem.par[len(S2.dem.par) - 1].material
+        S2.dem.par.add(woo.utils.sphere((0, 0, 0), radius=0.003, mat=m2))
+        assert len(S2.dem._mats) == nm and S2.dem.par[len(S2.dem.par) - 1].material is m2
     import pytest
     with pytest.raises(KeyError):
         woo.core.Scene.loadTmp("nothing saved under this name")

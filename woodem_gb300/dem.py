@@ -564,6 +564,11 @@ class DemField(Field):
     def collectNodes(self):
         return 0
 
+    def __setstate__(self, d):
+        # materials are indexed by object identity, which unpickling changes
+        self.__dict__.update(d)
+        self._mat_ids = {id(m): i for i, m in enumerate(self._mats)}
+
     def _mat_index(self, m):
         if m is None:
             raise ValueError("Particle without material")
