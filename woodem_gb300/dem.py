@@ -691,7 +691,61 @@ for _n in ("Bo1_InfCylinder_Aabb", "Bo1_Ellipsoid_Aabb", "Bo1_Rod_Aabb", "Bo1_Ca
            "Cg2_Wall_Ellipsoid_L6Geom", "Cg2_Wall_Facet_L6Geom", "Cg2_Rod_Sphere_L6Geom", "Cg2_Wall_Capsule_L6Geom",
            "Cg2_Capsule_Capsule_L6Geom", "Cg2_InfCylinder_Capsule_L6Geom", "Cg2_Facet_Capsule_L6Geom",
            "Cg2_Sphere_Capsule_L6Geom", "Cg2_Facet_Facet_L6Geom", "Cg2_Facet_InfCylinder_L6Geom"):
-    globals()[_n] = type(_n, (_InertFunctor,), {})
+    globals()[_n] = type(_n, (_InertFunctor, BoundFunctor if _n.startswith("Bo1_") else CGeomFunctor), {})
+
+
+# ------------------------------------------------------------------ dispatchers
+class Dispatcher(list):
+    """The functors of one dispatcher (core/Dispatcher.hpp:40-52): a list that is also the
+    reference's dispatcher object, with ``functors`` and ``add``. Functors of another kind raise
+    TypeError; a functor of a class already present is not added again (the first one stays)."""
+    _functorType = Functor
+
+    def __init__(self, functors=()):
+        super().__init__()
+        self.functors = functors
+
+    @property
+    def functors(self):
+        return list(self)
+
+    @functors.setter
+    def functors(self, ff):
+        del self[:]
+        for f in ff:
+            self.add(f)
+
+    def add(self, f):
+        if not isinstance(f, self._functorType):
+            raise TypeError("%s accepts %s functors only, not %s" % (type(self).__name__, self._functorType.__name__,
+                                                                      type(f).__name__))
+        if not any(type(g).__name__ == type(f).__name__ for g in self):
+            list.append(self, f)
+
+    def __repr__(self):
+        return "%s(%s)" % (type(self).__name__, list.__repr__(self))
+
+
+class BoundDispatcher(Dispatcher):
+    _functorType = BoundFunctor
+
+
+class CGeomDispatcher(Dispatcher):
+    _functorType = CGeomFunctor
+
+
+class CPhysDispatcher(Dispatcher):
+    _functorType = CPhysFunctor
+
+
+class LawDispatcher(Dispatcher):
+    _functorType = LawFunctor
+
+
+def _dispatcherAttr(name, cls):
+    key = "_" + name
+    return property(lambda self: self.__dict__[key],
+                    lambda self, v: self.__dict__.__setitem__(key, v if type(v) is cls else cls(v)))
 
 
 # ------------------------------------------------------------------ engines
@@ -714,6 +768,7 @@ class InsertionSortCollider(Collider):
               "maxVel2": 0.0, "nFullRuns": 0, "numReinit": 0, "ompTuneSort": (1, 1000, 0), "sortChunks": -1,
               "paraPeri": False,
               "boundDispatcher": lambda: [Bo1_Sphere_Aabb(), Bo1_Facet_Aabb(), Bo1_Wall_Aabb()]}
+    boundDispatcher = _dispatcherAttr("boundDispatcher", BoundDispatcher)
 
     def __init__(self, boundFunctors=None, **kw):
         super().__init__(**kw)
@@ -729,6 +784,9 @@ class ContactLoop(Engine):
     _attrs = {"evalStress": False, "applyForces": True, "updatePhys": False, "dist00": True, "reorderEvery": 1000,
               "alreadyWarnedNoCollider": False, "geoDisp": lambda: [], "phyDisp": lambda: [], "lawDisp": lambda: [],
               "stress": lambda: np.zeros((3, 3))}
+    geoDisp = _dispatcherAttr("geoDisp", CGeomDispatcher)
+    phyDisp = _dispatcherAttr("phyDisp", CPhysDispatcher)
+    lawDisp = _dispatcherAttr("lawDisp", LawDispatcher)
 
     def __init__(self, geoms=None, physs=None, laws=None, **kw):
         super().__init__(**kw)

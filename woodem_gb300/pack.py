@@ -310,3 +310,228 @@ class SpherePack:
         if "mat" not in kw:
             kw["mat"] = utils.defaultMaterial()
         return scene.dem.par.add([utils.sphere(R @ c, r, **kw) for c, r, _ in self.pack])
+
+
+# --- predicates (py/_packPredicates.cpp:51-295): solids that say whether a sphere (centre,
+# radius as the padding) lies inside them, with an axis-aligned bounding box; combined with
+# | (union), & (intersection), - (difference) and ^ (symmetric difference).
+_INF = float("inf")
+
+
+class Predicate:
+    def __call__(self, pt, pad=0.0):
+        raise NotImplementedError
+
+    def aabb(self):
+        raise NotImplementedError
+
+    def center(self):
+        mn, mx = self.aabb()
+        return 0.5 * (np.asarray(mn) + np.asarray(mx))
+
+    def dim(self):
+        mn, mx = self.aabb()
+        return np.asarray(mx) - np.asarray(mn)
+
+    def __or__(self, B):
+        return PredicateUnion(self, B)
+
+    def __and__(self, B):
+        return PredicateIntersection(self, B)
+
+    def __sub__(self, B):
+        return PredicateDifference(self, B)
+
+    def __xor__(self, B):
+        return PredicateSymmetricDifference(self, B)
+
+
+class _PredicateBoolean(Predicate):
+    def __init__(self, A, B):
+        self.A, self.B = A, B
+
+
+class PredicateUnion(_PredicateBoolean):
+    def __call__(self, pt, pad=0.0):
+        return self.A(pt, pad) or self.B(pt, pad)
+
+    def aabb(self):
+        (a0, a1), (b0, b1) = self.A.aabb(), self.B.aabb()
+        return np.minimum(a0, b0), np.maximum(a1, b1)
+
+
+class PredicateIntersection(_PredicateBoolean):
+    def __call__(self, pt, pad=0.0):
+        return self.A(pt, pad) and self.B(pt, pad)
+
+    def aabb(self):
+        (a0, a1), (b0, b1) = self.A.aabb(), self.B.aabb()
+        return np.maximum(a0, b0), np.minimum(a1, b1)
+
+
+class PredicateDifference(_PredicateBoolean):
+    """Inside A and not inside B, B tested with the opposite padding."""
+
+    def __call__(self, pt, pad=0.0):
+        return self.A(pt, pad) and not self.B(pt, -pad)
+
+    def aabb(self):
+        return self.A.aabb()
+
+
+class PredicateSymmetricDifference(_PredicateBoolean):
+    def __call__(self, pt, pad=0.0):
+        return self.A(pt, pad) != self.B(pt, pad)
+
+    def aabb(self):
+        (a0, a1), (b0, b1) = self.A.aabb(), self.B.aabb()
+        return np.minimum(a0, b0), np.maximum(a1, b1)
+
+
+class inSphere(Predicate):
+    """Centre within the sphere (the reference's test |pt-c|-pad <= radius-pad: the padding cancels)."""
+
+    def __init__(self, center, radius):
+        self.c, self.radius = np.asarray(center, dtype=float), float(radius)
+
+    def __call__(self, pt, pad=0.0):
+        return float(np.linalg.norm(np.asarray(pt, dtype=float) - self.c)) - pad <= self.radius - pad
+
+    def aabb(self):
+        return self.c - self.radius, self.c + self.radius
+
+
+class inAlignedHalfspace(Predicate):
+    def __init__(self, axis, coord, lower=True):
+        if axis not in (0, 1, 2):
+            raise RuntimeError("inAlignedHalfSpace.axis: must be in {0,1,2} (not %s)" % axis)
+        self.axis, self.coord, self.lower = int(axis), float(coord), bool(lower)
+
+    def __call__(self, pt, pad=0.0):
+        return pt[self.axis] + pad < self.coord if self.lower else pt[self.axis] - pad > self.coord
+
+    def aabb(self):
+        mn, mx = np.full(3, -_INF), np.full(3, _INF)
+        (mx if self.lower else mn)[self.axis] = self.coord
+        return mn, mx
+
+
+class inAxisRange(Predicate):
+    def __init__(self, axis, range):
+        if axis not in (0, 1, 2):
+            raise RuntimeError("inAxisRange.axis: must be in {0,1,2} (not %s)" % axis)
+        self.axis, self.range = int(axis), (float(range[0]), float(range[1]))
+
+    def __call__(self, pt, pad=0.0):
+        return pt[self.axis] - pad >= self.range[0] and pt[self.axis] + pad <= self.range[1]
+
+    def aabb(self):
+        mn, mx = np.full(3, -_INF), np.full(3, _INF)
+        mn[self.axis], mx[self.axis] = self.range
+        return mn, mx
+
+
+class inAlignedBox(Predicate):
+    def __init__(self, minAabb, maxAabb=None):
+        if maxAabb is None:  # a (min, max) pair
+            minAabb, maxAabb = minAabb
+        self.mn, self.mx = np.asarray(minAabb, dtype=float), np.asarray(maxAabb, dtype=float)
+
+    def __call__(self, pt, pad=0.0):
+        return all(self.mn[i] + pad <= pt[i] and self.mx[i] - pad >= pt[i] for i in range(3))
+
+    def aabb(self):
+        return self.mn.copy(), self.mx.copy()
+
+
+class inCylinder(Predicate):
+    """Between the caps at centre1 and centre2 and within radius of their axis."""
+
+    def __init__(self, centerBottom, centerTop, radius):
+        self.c1, self.c2 = np.asarray(centerBottom, dtype=float), np.asarray(centerTop, dtype=float)
+        self.radius = float(radius)
+        self.c12 = self.c2 - self.c1
+        self.ht = float(np.linalg.norm(self.c12))
+
+    def __call__(self, pt, pad=0.0):
+        pt = np.asarray(pt, dtype=float)
+        u = (pt.dot(self.c12) - self.c1.dot(self.c12)) / (self.ht * self.ht)
+        if u * self.ht < pad or u * self.ht > self.ht - pad:
+            return False
+        return float(np.linalg.norm(np.cross(pt - self.c1, pt - self.c2))) / self.ht <= self.radius - pad
+
+    def aabb(self):
+        A, B = self.c1, self.c2
+        k = np.array([math.sqrt((A[1] - B[1]) ** 2 + (A[2] - B[2]) ** 2), math.sqrt((A[0] - B[0]) ** 2 + (A[2] - B[2]) ** 2),
+                      math.sqrt((A[0] - B[0]) ** 2 + (A[1] - B[1]) ** 2)]) / self.ht
+        return np.minimum(A, B) - self.radius * k, np.maximum(A, B) + self.radius * k
+
+
+def _filtered(self, predicate, recenter=True):
+    """SpherePack.filtered (py/_packPredicates.cpp:364-395): the spheres inside ``predicate``
+    (a clump goes when any of its spheres is outside); with ``recenter`` and a finite predicate,
+    the packing is first moved so that the centres of the two bounding boxes coincide."""
+    ret = SpherePack()
+    ret.cellSize = self.cellSize.copy()
+    off = np.zeros(3)
+    pmn, pmx = predicate.aabb()
+    if recenter and np.all(np.isfinite(np.asarray(pmx) - np.asarray(pmn))) and self.pack:
+        smn, smx = self.aabb()
+        off = 0.5 * (np.asarray(pmn) + np.asarray(pmx)) - 0.5 * (smn + smx)
+    inside = [bool(predicate(c + off, r)) for c, r, _ in self.pack]
+    gone = {k for (c, r, k), ok in zip(self.pack, inside) if not ok and k >= 0}
+    for (c, r, k), ok in zip(self.pack, inside):
+        if ok and (k < 0 or k not in gone):
+            ret.add(c + off, r, k)
+    return ret
+
+
+SpherePack.filtered = _filtered
+
+
+def filterSpherePack(predicate, spherePack, **kw):
+    """The spheres of ``spherePack`` inside ``predicate``, recentred (py/pack.py:387-391)."""
+    return spherePack.filtered(predicate)
+
+
+def _finiteAabb(predicate):
+    mn, mx = (np.asarray(v, dtype=float) for v in predicate.aabb())
+    if not np.all(np.isfinite(mx - mn)):
+        raise ValueError("Aabb of the predicate must not be infinite (didn't you use union | instead of intersection & for "
+                         "unbounded predicate such as notInNotch?")
+    return mn, mx
+
+
+def regularOrtho(predicate, radius, gap, **kw):
+    """Spheres of ``radius`` on an orthogonal grid of pitch 2·radius+gap inside ``predicate``
+    (py/pack.py:323-332); ``kw`` go to utils.sphere."""
+    from . import utils
+    mn, mx = _finiteAabb(predicate)
+    xx, yy, zz = [np.arange(mn[i] + radius, mx[i] - radius, 2 * radius + gap) for i in range(3)]
+    return [utils.sphere((x, y, z), radius=radius, **kw) for x in xx for y in yy for z in zz if predicate((x, y, z), radius)]
+
+
+def regularHexa(predicate, radius, gap, **kw):
+    """Spheres of ``radius`` on the reference's hexagonal grid inside ``predicate``
+    (py/pack.py:334-351): rows a=2·radius+gap apart within a row, rows a·√3/2 apart and shifted
+    by a/2 alternately, layers a·√6/3 apart with odd layers shifted by a·√3/4 across the rows.
+    That layer shift puts some centres of adjacent layers a·√(3/16+2/3) ≈ 0.924·a apart (closer
+    than a), which is kept: the same call gives the same spheres as the reference."""
+    from . import utils
+    mn, mx = _finiteAabb(predicate)
+    a = 2 * radius + gap
+    hy, hz = a * math.sqrt(3) / 2., a * math.sqrt(6) / 3.
+    dim = mx - mn
+    out = []
+    for i in range(int(dim[0] / a) + 1):
+        for j in range(int(dim[1] / hy) + 1):
+            for k in range(int(dim[2] / hz) + 1):
+                x, y, z = mn[0] + radius + i * a, mn[1] + radius + j * hy, mn[2] + radius + k * hz
+                if j % 2 == 0:
+                    x += a / 2. if k % 2 == 0 else -a / 2.
+                if k % 2 != 0:
+                    x += a / 2.
+                    y += hy / 2.
+                if predicate((x, y, z), radius):
+                    out.append(utils.sphere((x, y, z), radius=radius, **kw))
+    return out
