@@ -190,7 +190,7 @@ def readParamsFromTable(scene, under="table", noTableOk=True, unknownOk=False, *
     set; ``<under>.explicitParams_`` and ``<under>.defaultParams_`` list what came from the table
     and what stayed at its default."""
     S = scene
-    mod = S.lab._newModule(under)
+    mod = getattr(S.lab, under) if S.lab._whereIs(under) == S.labels.inMod else S.lab._newModule(under)
     tagsParams, dictParams = [], {}
     if not inBatch():
         if not noTableOk:

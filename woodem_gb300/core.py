@@ -5,10 +5,11 @@ core/Engine.hpp:27-104. A Scene owns a device-side simulation (created on the
 first ``run``); engines are descriptors compiled into one device plan, so the
 per-step loop of core/Scene.cpp:319-389 runs entirely on the GPU.
 """
+import logging
 import os
+import re
 import socket
 import time
-import types
 
 import numpy as np
 
@@ -229,6 +230,251 @@ class EnergyTracker:
         return {k: i for i, k in enumerate(self.keys())}
 
 
+_LOG = logging.getLogger("woo.core")
+_RE_SEQ = re.compile(r"([a-zA-Z0-9_.]+)\s*\[([0-9]+)\]")
+_RE_PLAIN = re.compile(r"[a-zA-Z_][.a-zA-Z0-9_]*")
+
+
+class LabelMapper:
+    """Scene.labels (core/LabelMapper.hpp, core/LabelMapper.cpp): named objects of a scene,
+    reached as ``S.lab.name``. A label holds a Woo object (inWoo), a sequence of Woo objects
+    (inWooSeq; ``None`` items allowed, ``name[i]`` labels grow it), a plain Python object (inPy)
+    or is a pseudo-module (inMod, ``S.lab._newModule('a.b')``) holding dotted labels. Engines
+    and functors with a ``label`` are found automatically. Overwriting a label logs a warning
+    unless it was made writable (``_setWritable``)."""
+    nowhere, inWoo, inWooSeq, inPy, inMod = 0, 1, 2, 3, 4
+
+    def __init__(self, scene=None):
+        self._scene = scene
+        self._woo, self._wooSeq, self._py = {}, {}, {}
+        self._mods, self._writables = set(), set()
+
+    # -- classification (LabelMapper::labelType, whereIs, ensureUsedModsOk)
+    @staticmethod
+    def _labelType(label):
+        if label.startswith("_"):
+            raise NameError("LabelMapper: labels may not start with underscore (those are reserved to access the underlying "
+                            "LabelMapper object itself).")
+        if label.startswith(".") or ".." in label or ".[" in label:
+            raise NameError("LabelMapper: label '%s' is not a valid python identifier name." % label)
+        m = _RE_SEQ.fullmatch(label)
+        if m:
+            return m.group(1), int(m.group(2))
+        if _RE_PLAIN.fullmatch(label):
+            return label, None
+        raise NameError("LabelMapper: label '%s' is not a valid python identifier name." % label)
+
+    def _autoLabels(self):
+        out = {}
+        for e in getattr(self._scene, "_engines", []):
+            if getattr(e, "label", ""):
+                out[e.label] = e
+            for f in getattr(e, "_functors", lambda: [])():
+                if getattr(f, "label", ""):
+                    out[f.label] = f
+        return out
+
+    def _whereIs(self, label):
+        if label in self._woo:
+            return self.inWoo
+        if label in self._wooSeq:
+            return self.inWooSeq
+        if label in self._py:
+            return self.inPy
+        if label in self._mods:
+            return self.inMod
+        if label in self._autoLabels():
+            return self.inWoo
+        return self.nowhere
+
+    def _ensureUsedModsOk(self, label):
+        parts = self._labelType(label)[0].split(".")[:-1]
+        for i in range(len(parts)):
+            mod = ".".join(parts[:i + 1])
+            where = self._whereIs(mod)
+            if where == self.nowhere:
+                raise NameError("Label '%s' requires non-existent pseudo-module '%s' (use LabelMapper._newModule to create it)."
+                                % (label, mod))
+            if where != self.inMod:
+                raise NameError("Label '%s' requires pseudo-module '%s', but this name is already used by another object."
+                                % (label, mod))
+
+    def _drop(self, label):
+        for d in (self._woo, self._wooSeq, self._py):
+            d.pop(label, None)
+
+    # -- setting (LabelMapper::__setitem__ and its woo / wooSeq / py cases)
+    def __setitem__(self, label, o):
+        self._ensureUsedModsOk(label)
+        if isinstance(o, Object):
+            return self._setWoo(label, o)
+        if isinstance(o, (list, tuple)):
+            kind = None  # None: only None items (a sequence of Woo objects), else True (Woo) / False (python)
+            for x in o:
+                if x is None:
+                    continue
+                w = isinstance(x, Object)
+                if kind is not None and kind != w:
+                    raise ValueError("Sequence given to LabelMapper mixes python objects and woo.Object's.")
+                kind = w
+            if kind is not False:
+                return self._setWooSeq(label, list(o))
+        self._setPy(label, o)
+
+    def _checkNotMod(self, label):
+        if self._whereIs(label) == self.inMod:
+            raise NameError("Label '%s' is a pseudo-module (cannot be overwritten)." % label)
+
+    def _setWoo(self, label, o):
+        lab0, index = self._labelType(label)
+        self._checkNotMod(label)
+        if index is None:
+            where = self._whereIs(label)
+            old = self._woo.get(label, self._py.get(label, self._wooSeq.get(label)))
+            if where != self.nowhere and old is not None and old is not o and label not in self._writables:
+                _LOG.warning("Label '%s' overwrites %r with %r", label, old, o)
+            self._drop(label)
+            self._woo[label] = o
+            return
+        if self._whereIs(lab0) in (self.inWoo, self.inPy):
+            _LOG.warning("Sequence label '%s[%d]' creates a new sequence, deleting '%s'", lab0, index, lab0)
+            self._drop(lab0)
+        vec = self._wooSeq.setdefault(lab0, [])
+        vec.extend([None] * (index + 1 - len(vec)))
+        vec[index] = o
+
+    def _setWooSeq(self, label, oo):
+        lab0, index = self._labelType(label)
+        if index is not None:
+            if not oo:
+                return self._setPy(label, [])
+            raise NameError("Subscripted label '%s' may not be assigned a sequence of %d woo.core.Objects." % (label, len(oo)))
+        self._checkNotMod(label)
+        where = self._whereIs(label)
+        if where != self.nowhere and (label not in self._writables or where != self.inWooSeq):
+            _LOG.warning("Label '%s' overwrites an existing object with a new sequence of %d woo.Object's.", label, len(oo))
+        self._drop(label)
+        self._wooSeq[label] = oo
+
+    def _setPy(self, label, o):
+        lab0, index = self._labelType(label)
+        self._checkNotMod(label)
+        if index is None:
+            where = self._whereIs(label)
+            if where == self.inPy and self._py[label] is not o and label not in self._writables:
+                _LOG.warning("Label '%s' overwrites %r with %r", label, self._py[label], o)
+            elif where in (self.inWoo, self.inWooSeq):
+                _LOG.warning("Label '%s' changes type to a pure-python object", label)
+            self._drop(label)
+            self._py[label] = o
+            return
+        where = self._whereIs(lab0)
+        if where in (self.inWoo, self.inWooSeq) or (where == self.inPy and not isinstance(self._py[lab0], list)):
+            _LOG.warning("Sequence label '%s[%d]' overwrites '%s' with a new python list", lab0, index, lab0)
+            self._drop(lab0)
+        lst = self._py.setdefault(lab0, [])
+        lst.extend([None] * (index + 1 - len(lst)))
+        if lst[index] is not None and label not in self._writables:
+            _LOG.warning("Label '%s' overwrites old item %r with %r", label, lst[index], o)
+        lst[index] = o
+
+    # -- getting and deleting
+    def __getitem__(self, label):
+        m = re.fullmatch(r"(.*)\[([0-9]+)\]", label)
+        if m:
+            return self[m.group(1)][int(m.group(2))]
+        where = self._whereIs(label)
+        if where == self.nowhere:
+            raise AttributeError("No such label: '%s'" % label)
+        if where == self.inMod:
+            raise ValueError("Label '%s' is a pseudo-module and cannot be obtained directly." % label)
+        if label in self._woo:
+            return self._woo[label]
+        if label in self._wooSeq:
+            return self._wooSeq[label]
+        if label in self._py:
+            return self._py[label]
+        return self._autoLabels()[label]
+
+    def __delitem__(self, label):
+        where = self._whereIs(label)
+        if where == self.nowhere:
+            raise NameError("No such label: '%s'" % label)
+        if where == self.inMod:
+            pre = label + "."
+            for d in (self._woo, self._wooSeq, self._py):
+                for k in [k for k in d if k.startswith(pre)]:
+                    del d[k]
+            self._mods = {m for m in self._mods if m != label and not m.startswith(pre)}
+            return
+        self._drop(label)
+
+    def __contains__(self, label):
+        return self._whereIs(label) != self.nowhere
+
+    def keys(self):
+        return sorted(set(self._woo) | set(self._wooSeq) | set(self._py) | set(self._autoLabels()))
+
+    def _setWritable(self, label):
+        where = self._whereIs(label)
+        if where == self.inMod:
+            raise ValueError("Label '%s' cannot be made writable: is a (pseudo) module." % label)
+        if where == self.nowhere:
+            raise NameError("No such label: '%s'" % label)
+        self._writables.add(label)
+
+    def _newModule(self, name):
+        parts = name.split(".")
+        for i in range(len(parts)):
+            mod = ".".join(parts[:i + 1])
+            where = self._whereIs(mod)
+            if where == self.inMod and i < len(parts) - 1:
+                continue
+            if where != self.nowhere:
+                raise ValueError("Label '%s' already exists." % mod)
+            self._mods.add(mod)
+        return _LabelProxy(self, name)
+
+    def _dir(self, prefix):
+        pre = prefix + "." if prefix else ""
+        names = set()
+        for k in self.keys() + sorted(self._mods):
+            if k.startswith(pre):
+                names.add(k[len(pre):].split(".")[0])
+        return sorted(names)
+
+
+class _LabelProxy:
+    """``S.lab`` and its pseudo-modules: attribute access to the labels under a prefix."""
+
+    def __init__(self, mapper, prefix=""):
+        object.__setattr__(self, "_m", mapper)
+        object.__setattr__(self, "_p", prefix)
+
+    def _full(self, name):
+        return self._p + "." + name if self._p else name
+
+    def __getattr__(self, name):
+        m, p = object.__getattribute__(self, "_m"), object.__getattribute__(self, "_p")
+        if name.startswith("_"):
+            if not p and name in ("_newModule", "_whereIs", "_setWritable"):
+                return getattr(m, name)
+            raise AttributeError(name)
+        full = p + "." + name if p else name
+        if m._whereIs(full) == m.inMod:
+            return _LabelProxy(m, full)
+        return m[full]
+
+    def __setattr__(self, name, v):
+        self._m[self._full(name)] = v
+
+    def __delattr__(self, name):
+        del self._m[self._full(name)]
+
+    def __dir__(self):
+        return self._m._dir(self._p)
+
+
 class Scene(Object):
     """Simulation scene. ``S.run(n)`` advances n steps of the engine list on the GPU."""
 
@@ -245,7 +491,7 @@ class Scene(Object):
         self.gpu = _plan.GpuConfig()
         self._sim = None
         self._clock0 = time.time()
-        self._labModules = {}
+        self.labels = LabelMapper(self)
         self.energy = EnergyTracker()
         super().__init__(**kw)
         self._fillDefaultTags()
@@ -299,26 +545,10 @@ class Scene(Object):
 
     @property
     def lab(self):
-        """Labeled engines and functors as attributes, plus the pseudo-modules created with
-        ``S.lab._newModule(name)`` (which persist on the scene, e.g. ``S.lab.table`` of
-        ``woo.batch.readParamsFromTable``)."""
-        mods = self._labModules
-
-        class _Lab:
-            def _newModule(self, name):
-                mods.setdefault(name, types.SimpleNamespace())
-                setattr(self, name, mods[name])
-                return mods[name]
-        lab = _Lab()
-        for name, m in mods.items():
-            setattr(lab, name, m)
-        for e in self._engines:
-            if getattr(e, "label", ""):
-                setattr(lab, e.label, e)
-            for sub in getattr(e, "_functors", lambda: [])():
-                if getattr(sub, "label", ""):
-                    setattr(lab, sub.label, sub)
-        return lab
+        """The labels of Scene.labels as attributes (``S.lab.name``, ``S.lab.module.name``):
+        labeled engines and functors, objects labeled from Python and the pseudo-modules of
+        ``S.lab._newModule(name)`` (e.g. ``S.lab.table`` of ``woo.batch.readParamsFromTable``)."""
+        return _LabelProxy(self.labels)
 
     def _invalidate(self):
         if self._sim is not None:
