@@ -9,6 +9,7 @@ import logging
 import os
 import re
 import socket
+import threading
 import time
 
 import numpy as np
@@ -551,9 +552,13 @@ class Scene(Object):
         return _LabelProxy(self.labels)
 
     def _invalidate(self):
-        if self._sim is not None:
-            self._sim.close()
-            self._sim = None
+        if self.running and threading.current_thread() is not self.__dict__["_thread"]:
+            self.__dict__["_stopFlag"] = True
+            self.__dict__["_thread"].join()
+        with self._lock():
+            if self._sim is not None:
+                self._sim.close()
+                self._sim = None
         # a contact container loaded with the scene belongs to its particles as they were
         self.__dict__.pop("_pendingContacts", None)
 
@@ -564,24 +569,27 @@ class Scene(Object):
     def __getstate__(self):
         d = self.__dict__.copy()
         d["_sim"] = None
+        for k in ("_runLock", "_thread", "_except", "_stopFlag"):
+            d.pop(k, None)
         return d
 
     def _saveBytes(self):
         import pickle
-        snap = self.__dict__.get("_pendingContacts")
-        if self._sim is not None:
-            from . import checkpoint
-            self.sync()
-            snap = checkpoint.contact_snapshot(self)
-        had, old = "_pendingContacts" in self.__dict__, self.__dict__.get("_pendingContacts")
-        self.__dict__["_pendingContacts"] = snap
-        try:
-            return pickle.dumps(self, protocol=pickle.HIGHEST_PROTOCOL)
-        finally:
-            if had:
-                self.__dict__["_pendingContacts"] = old
-            else:
-                self.__dict__.pop("_pendingContacts", None)
+        with self._lock():  # a background run pauses between its chunks
+            snap = self.__dict__.get("_pendingContacts")
+            if self._sim is not None:
+                from . import checkpoint
+                self.sync()
+                snap = checkpoint.contact_snapshot(self)
+            had, old = "_pendingContacts" in self.__dict__, self.__dict__.get("_pendingContacts")
+            self.__dict__["_pendingContacts"] = snap
+            try:
+                return pickle.dumps(self, protocol=pickle.HIGHEST_PROTOCOL)
+            finally:
+                if had:
+                    self.__dict__["_pendingContacts"] = old
+                else:
+                    self.__dict__.pop("_pendingContacts", None)
 
     @staticmethod
     def _fromBytes(b):
@@ -640,15 +648,85 @@ class Scene(Object):
                 checkpoint.restore_contacts(self, pend)
         return self._sim
 
+    # --- running (core/Scene.cpp:33-96): run(n) queues n steps on the device; run(n, wait=False)
+    # issues them from a background thread in chunks, between which stop() takes effect, and
+    # wait() joins it and raises the exception the run ended with. The device simulation is used
+    # by one thread at a time (the scene's lock, taken per chunk, by sync, save and close).
+    _BG_CHUNK = 1000
+
+    def _lock(self):
+        lk = self.__dict__.get("_runLock")
+        if lk is None:
+            lk = self.__dict__["_runLock"] = threading.RLock()
+        return lk
+
+    @property
+    def running(self):
+        """Whether a background run (``run(wait=False)``) is in progress."""
+        t = self.__dict__.get("_thread")
+        return t is not None and t.is_alive()
+
     def run(self, nSteps=None, wait=True):
-        """Run nSteps steps (core/Scene.cpp:33-48). Runs synchronously; ``wait`` is accepted for API parity."""
+        """Run nSteps steps and set stopAtStep to the step they end at (Scene.run). Without
+        nSteps, run up to stopAtStep; a background run (wait=False) without either runs until
+        stop(). Raises RuntimeError while a background run is in progress."""
+        if self.running:
+            raise RuntimeError("Scene.run: already running")
+        self.__dict__["_except"] = None
+        if nSteps is not None and nSteps > 0:
+            self.stopAtStep = self.step + int(nSteps)
         if nSteps is None:
             if self.stopAtStep > self.step:
                 nSteps = self.stopAtStep - self.step
-            else:
+            elif wait:
                 raise ValueError("S.run() without nSteps needs stopAtStep > step")
-        if nSteps <= 0:
+            else:
+                nSteps = -1  # until stop()
+        elif nSteps <= 0:
             return
+        if wait:
+            with self._lock():
+                self._runSteps(int(nSteps))
+            return
+        self.__dict__["_stopFlag"] = False
+        t = threading.Thread(target=self._backgroundLoop, args=(int(nSteps),), name="woo-scene-run", daemon=True)
+        self.__dict__["_thread"] = t
+        t.start()
+
+    def _backgroundLoop(self, n):
+        try:
+            while n != 0 and not self.__dict__.get("_stopFlag"):
+                k = self._BG_CHUNK if n < 0 else min(n, self._BG_CHUNK)
+                with self._lock():
+                    self._runSteps(k)
+                if n > 0:
+                    n -= k
+        except BaseException as e:  # raised again by wait()
+            self.__dict__["_except"] = e
+
+    def stop(self):
+        """Ask a background run to stop after the chunk in progress (Scene.stop); returns at once."""
+        if self.running:
+            self.__dict__["_stopFlag"] = True
+
+    def wait(self):
+        """Wait for a background run to end; raise the exception it ended with (Scene.wait)."""
+        t = self.__dict__.get("_thread")
+        if t is not None:
+            t.join()
+        e = self.__dict__.get("_except")
+        if e is not None:
+            self.__dict__["_except"] = None
+            raise e
+
+    def one(self):
+        """One step (Scene.one); RuntimeError while a background run is in progress."""
+        if self.running:
+            raise RuntimeError("Scene.step: already running.")
+        with self._lock():
+            self._runSteps(1)
+
+    def _runSteps(self, nSteps):
         sim = self._ensure_sim()
         host = [e for e in self._engines if getattr(e, "_host", False) and not e.dead]
         if not host:
@@ -677,19 +755,11 @@ class Scene(Object):
             for e in due:
                 e._runHost(self, step0 + k - 1, t0 + (k - 1) * dt0)
 
-    def one(self):
-        self.run(1)
-
-    def wait(self):
-        return
-
-    def stop(self):
-        return
-
     def sync(self):
         """Bring device state back to the host containers."""
-        if self._sim is not None:
-            self._sim.pull()
+        with self._lock():
+            if self._sim is not None:
+                self._sim.pull()
 
     def close(self):
         """Pull the device state into the host containers and release the device simulation."""
