@@ -96,3 +96,13 @@ def test_sync_and_save_while_running(S, tmp_path, monkeypatch):
     assert 0 <= S2.step <= 2000 and S2.step % 100 == 0 and not S2.running
     S.close()
     assert S._sim is None
+
+
+def test_batch_wait_runs_the_line_scene(S, monkeypatch):
+    from woodem_gb300 import batch
+    S.stopAtStep = 450
+    batch.wait(S)  # outside a batch: nothing
+    assert S.step == 0
+    monkeypatch.setattr(batch.options, "batchTable", "t.txt")
+    batch.wait(S)
+    assert S.step == 450 and not S.running

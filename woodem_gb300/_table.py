@@ -49,10 +49,15 @@ def inBatch():
     return bool(options.batchTable)
 
 
-def wait():
-    """py/batch.py:32-38 starts the batch line's master scene and blocks until it stops; here every
-    S.run() call is synchronous, so there is nothing to wait for."""
-    return None
+def wait(S=None):
+    """In a batch, start the line's scene ``S`` if it is not running and block until it stops
+    (py/batch.py:32-38, where S is the master scene); it runs up to its stopAtStep. Does nothing
+    outside a batch or without a scene."""
+    if S is None or not inBatch():
+        return None
+    if not S.running and S.stopAtStep > S.step:
+        S.run(wait=False)
+    S.wait()
 
 
 def _evalNamespace(**extra):
