@@ -128,3 +128,9 @@ def test_labels_survive_save_load(S, tmp_path):
     S.save(path)
     S2 = Scene.load(path)
     assert S2.lab.table.radius == 2e-3 and S2.lab.lf is S2.engines[0]
+
+
+def test_expand_tags(S):
+    S.tags["title"] = "drum"
+    assert S.expandTags("/tmp/{title}-{id}.{unknown}") == "/tmp/drum-%s.{unknown}" % S.tags["id"]
+    assert S.expandTags("plain") == "plain"

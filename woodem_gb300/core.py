@@ -509,6 +509,15 @@ class Scene(Object):
                      ("title", ""), ("idt", sid), ("tid", sid)):
             self.tags.setdefault(k, v)
 
+    def expandTags(self, s):
+        """``s`` with each ``{tag}`` replaced by the value of that tag; other braces stay
+        (Scene.expandTags, core/Scene.cpp:174-182)."""
+        if "{" not in s:
+            return s
+        for k, v in self.tags.items():
+            s = s.replace("{" + str(k) + "}", str(v))
+        return s
+
     @property
     def duration(self):
         """Wall-clock seconds this scene has existed (Scene.duration, core/Scene.hpp:200)."""

@@ -98,7 +98,7 @@ def export(S, contacts, out="", what=WHAT_ALL, mask=0, sphereSphereOnly=False, i
     if what > WHAT_ALL or what < 0:
         raise ValueError("VtkExport.what=%d, but should be at most %d." % (what, WHAT_ALL))
     step = int(S.step if step is None else step)
-    out = out.format(**S.tags) if "{" in out else out
+    out = S.expandTags(out)
     d = os.path.dirname(out)
     if d:
         os.makedirs(d, exist_ok=True)
