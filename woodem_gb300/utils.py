@@ -193,11 +193,11 @@ def runningInBatch():
     return batch.inBatch()
 
 
-def waitIfBatch():
+def waitIfBatch(S=None):
     """Deprecated alias of woo.batch.wait."""
     from . import batch
     _deprecatedUtilsFunction("waitIfBatch", "woo.batch.wait")
-    return batch.wait()
+    return batch.wait(S)
 
 
 def readParamsFromTable(*args, **kw):
