@@ -106,3 +106,13 @@ def test_batch_wait_runs_the_line_scene(S, monkeypatch):
     monkeypatch.setattr(batch.options, "batchTable", "t.txt")
     batch.wait(S)
     assert S.step == 450 and not S.running
+
+
+def test_paused_holds_the_background_run(S):
+    S.run(3000, wait=False)
+    with S.paused():
+        step = S.step
+        time.sleep(0.05)
+        assert S.step == step and step % 100 == 0
+    S.wait()
+    assert S.step == 3000

@@ -713,6 +713,11 @@ class Scene(Object):
         except BaseException as e:  # raised again by wait()
             self.__dict__["_except"] = e
 
+    def paused(self):
+        """Context manager that holds a background run between two chunks while its block runs
+        (Scene.paused, core/Scene.cpp:98-124): ``with S.paused(): ...``."""
+        return self._lock()
+
     def stop(self):
         """Ask a background run to stop after the chunk in progress (Scene.stop); returns at once."""
         if self.running:
