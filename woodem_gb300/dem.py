@@ -584,9 +584,8 @@ class DemField(Field):
         return None if sc is None else sc._sim
 
     def _pull_state(self):
-        s = self._sim()
-        if s is not None:
-            s.pull()
+        if self.scene is not None:
+            self.scene.sync()  # under the scene's lock: a background run pauses between chunks
 
     def _state_written(self):
         s = self._sim()
@@ -599,6 +598,12 @@ class DemField(Field):
             s.dirty_structure = True
 
     def _contacts_snapshot(self):
+        if self.scene is not None:
+            with self.scene._lock():
+                return self._contacts_snapshot_locked()
+        return self._contacts_snapshot_locked()
+
+    def _contacts_snapshot_locked(self):
         s = self._sim()
         if s is None:
             z = np.zeros(0, dtype=np.int32)
