@@ -103,3 +103,26 @@ def test_regular_packing_runs_as_scene():
     from woodem_gb300 import _plan
     A = _plan.compile_scene(S)
     assert len(A.particles["shape"]) == len(ids)
+
+
+def test_from_simulation_round_trip():
+    """SpherePack.toSimulation then fromSimulation gives the spheres and the periodic cell back;
+    walls are left out and a sheared cell is refused."""
+    from woodem_gb300 import utils
+    from woodem_gb300.core import Scene
+    from woodem_gb300.dem import DemField
+    sp = pack.SpherePack()
+    sp.makeCloud((0, 0, 0), (0.1, 0.1, 0.1), rMean=0.005, periodic=True, seed=3)
+    S = Scene(fields=[DemField()])
+    sp.toSimulation(S)
+    S.dem.par.add(utils.wall(0.0, axis=2))
+    back = pack.SpherePack().fromSimulation(S)
+    assert len(back) == len(sp)
+    c0, r0 = sp.toCcRr()
+    c1, r1 = back.toCcRr()
+    assert np.array_equal(c0, c1) and np.array_equal(r0, r1) and np.array_equal(back.cellSize, sp.cellSize)
+    h = np.array(S.cell.hSize)
+    h[0, 2] = 0.01
+    S.cell.hSize = h
+    with pytest.raises(RuntimeError):
+        pack.SpherePack().fromSimulation(S)

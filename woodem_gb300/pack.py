@@ -284,6 +284,30 @@ class SpherePack:
             self.add(c, r)
         return len(self.pack)
 
+    def fromSimulation(self, scene, dem=None):
+        """Reset and fill from the spheres of ``scene`` (py/pack.py:71-97): centres as of the
+        last run, radii; a periodic scene gives cellSize = diag(hSize) and raises RuntimeError
+        for a cell whose hSize is not symmetric (sheared)."""
+        from .dem import SHAPE_SPHERE
+        self.reset()
+        de = scene.dem if dem is None else dem
+        scene.sync()
+        par = de.par.soa
+        sel = np.nonzero(np.asarray(par.col("shape")) == SHAPE_SPHERE)[0]
+        pos = np.asarray(de._nodes.soa.col("pos"))[np.asarray(par.col("nodes"))[sel, 0]]
+        for c, r in zip(pos, np.asarray(par.col("radius"))[sel]):
+            self.add(c, r)
+        if scene.periodic:
+            h = np.asarray(scene.cell.hSize, dtype=float)
+            if np.any(h - h.T != 0):
+                raise RuntimeError("Only box-shaped (no shear) periodic boundary conditions can be represented with a "
+                                   "pack.SpherePack object")
+            self.cellSize = h.diagonal().copy()
+        return self
+
+    def fromDem(self, scene, dem):
+        return self.fromSimulation(scene, dem)
+
     def toSimulation(self, scene, rot=None, **kw):
         """Add the spheres to ``scene`` (py/pack.py:104-160); a periodic packing makes the scene
         periodic with cell hSize = rot·diag(cellSize) and trsf the identity. ``rot``: a 3×3 matrix
