@@ -203,6 +203,10 @@ int wg_get_stats(wg_scene* s, wg_stats* out);
 /* Scene.dt/nextDt and the DynDt counters after the last run (DynDt::run, pkg/dem/DynDt.cpp:93-113;
    PeriodicEngine::isActivated, core/Engine.cpp:169-194). */
 int wg_get_dyndt(wg_scene* s, wg_dyndt_state* out);
+/* The same for scene k of a batch (wg_set_scenes) or serving slot k: each scene of a batch keeps
+   its own DynDt counters, Scene.dt, Scene.nextDt and Scene.time (no counterpart in the reference:
+   a reference scene is one process, pkg/dem/DynDt.cpp:93-113 per scene). */
+int wg_get_scene_dyndt(wg_scene* s, int32_t k, wg_dyndt_state* out);
 /* Scene.dt and Scene.nextDt set between runs (0 or NaN next_dt: none); one scene only. */
 int wg_set_dt(wg_scene* s, double dt, double next_dt);
 /* Scene.energy: the WG_ENERGY_N values and whether each entry exists (created by an addition);
@@ -253,18 +257,22 @@ void wg_host_free(void* p);
 int wg_get_timing(wg_scene* s, double* total_ms, double* phase_ms4, int64_t* launches);
 
 /* Allocation-free broad phase (no counterpart in the reference): for callers that must not
-   allocate device memory (memory owned by another runtime's pool, code running during CUDA
-   graph capture, loops that cannot take the synchronisation of cudaMalloc/cudaFree).
+   allocate device memory -- a process whose device memory belongs to another runtime's pool
+   (which forbids raw cudaMalloc/cudaFree), or a loop that cannot take the device-wide
+   synchronisation of cudaMalloc/cudaFree.
    Given n sphere boxes in host memory (mn, mx: 3 doubles each; mask: Particle.mask) it
    returns in host memory the overlapping pairs -- closed 3-axis box overlap and the mask test
    of Collider::mayCollide with lone_mask -- sorted by (id_lo, id_hi), *n_pairs of them.
    All device scratch is one static __device__ array (about 13 MB, held by every GPU that
    loads the library until the process exits); n above 32768 or more than 262144 pairs is
-   rejected with WG_ERR_CAPACITY, as is a pair count above cap (*n_pairs is still set).
-   The first call on a device resolves the scratch address (cudaGetSymbolAddress) and should
-   come before any stream capture. Calls share the scratch: calls that overlap on the GPU
-   (concurrent host threads on one device) race. It runs on the current device and the
-   legacy default stream and returns after the result is in host memory. */
+   rejected with WG_ERR_CAPACITY, as is a pair count above cap (*n_pairs is still set to the
+   true count); a NaN or infinite box coordinate is rejected with WG_ERR_ARG.
+   The first call on a device resolves the scratch address (cudaGetSymbolAddress, with that
+   device current) and should come before any stream capture; the address is kept for the
+   life of the process, so the call must not be used after a cudaDeviceReset. Calls share the
+   scratch: calls that overlap on the GPU (concurrent host threads on one device) race. It
+   runs on the current device and the legacy default stream and returns after the result is
+   in host memory. */
 int wg_broadphase_noalloc(int32_t n, const double* mn, const double* mx, const uint32_t* mask, uint32_t lone_mask,
                           int64_t cap, int32_t* id_lo, int32_t* id_hi, int64_t* n_pairs);
 /* Message of the last failed wg_broadphase_noalloc call on this thread. */

@@ -12,15 +12,15 @@ from woodem_gb300 import _native
 from woodem_gb300._plan import read_contacts
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-_L = None
+_L = {}
 
 
-def lib():
-    global _L
-    if _L is not None:
-        return _L
+def lib(fast=False):
+    """The parity build (bitwise comparisons) or, with ``fast``, the timing build of the CPU baseline."""
+    if fast in _L:
+        return _L[fast]
     from . import build as _b  # noqa
-    path = os.path.join(HERE, "_build", "libwoo_oracle.so")
+    path = os.path.join(HERE, "_build", "libwoo_oracle_fast.so" if fast else "libwoo_oracle.so")
     if not os.path.exists(path):
         _b.build()
     L = C.CDLL(path)
@@ -50,15 +50,15 @@ def lib():
         fn = getattr(L, name)
         fn.restype = res
         fn.argtypes = args
-    _L = L
+    _L[fast] = L
     return L
 
 
 class Oracle:
     """One oracle scene built from SceneArrays."""
 
-    def __init__(self, A, threads=1, deterministic=True):
-        self.L = L = lib()
+    def __init__(self, A, threads=1, deterministic=True, fast=False):
+        self.L = L = lib(fast)
         self.h = L.wo_create()
         self.n_nodes = A.n_nodes
         L.wo_set_threads(self.h, int(threads))

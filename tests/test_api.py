@@ -71,7 +71,9 @@ def test_particle_views_and_containers():
 
 def test_plan_rejects_unsupported():
     S = scenes.box_settle_small(n=20, precision="fp32")
-    S.engines = utils.defaultEngines(damping=.2)  # DynDt: FP64 mode only
+    S.engines = utils.defaultEngines(damping=.2)  # the stock engine list (DynDt) in the FP32-force mode
+    assert _plan.compile_scene(S).config["dyndt"] == 1
+    S.trackEnergy = True
     with pytest.raises(NotImplementedError):
         _plan.compile_scene(S)
     S = scenes.box_settle_small(n=20)

@@ -115,8 +115,7 @@ def test_dry_run_and_dt_update(oracle_lib):
 
 def test_compile_refusals_and_automatic_dt():
     S = _with_dyndt(scenes.box_settle_small(n=50, seed=0, precision="fp32"), stepPeriod=10)
-    with pytest.raises(NotImplementedError, match="FP64"):
-        _plan.compile_scene(S)
+    assert _plan.compile_scene(S).config["dyndt"] == 1  # the FP32-force mode runs DynDt too
     S = _with_dyndt(scenes.box_settle_small(n=50, seed=0), stepPeriod=10, realPeriod=1.0)
     with pytest.raises(NotImplementedError, match="realPeriod"):
         _plan.compile_scene(S)
@@ -130,8 +129,10 @@ def test_compile_refusals_and_automatic_dt():
     with pytest.raises(NotImplementedError, match="facet nodes"):
         _plan.compile_scene(S)
     from woodem_gb300.batch import Batch
-    with pytest.raises(NotImplementedError, match="Batch"):
-        Batch([_with_dyndt(scenes.box_settle_small(n=50, seed=0), stepPeriod=10)])
+    S = _with_dyndt(scenes.box_settle_small(n=50, seed=0), stepPeriod=10)
+    S.trackEnergy = True  # DynDt runs in a Batch; energy tracking does not
+    with pytest.raises(NotImplementedError, match="energy"):
+        Batch([S])
     # Scene.dt unset: dtSafety * pWaveDt, as Scene::doOneStep does before the first step
     S = scenes.box_settle_small(n=50, seed=0)
     S.dt = float("nan")

@@ -73,3 +73,43 @@ def test_batch_scene_parameters_differ(gpu_lib):
     for S in mix:
         assert S.time == pytest.approx(100 * S.dt)
     B.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_batch_with_dyndt_equals_alone(precision, gpu_lib):
+    """The stock engine list with DynDt (utils.defaultEngines appends DynDt(stepPeriod=100)) in a
+    batch: every scene keeps its own DynDt counters and Scene.dt, which change at the steps where
+    they change with the scene alone; states, dt, time and counters equal the scene run alone
+    (bitwise in both modes; walls with many contacts as in test_batch_equals_alone)."""
+    from woodem_gb300.dem import DynDt
+
+    def study():
+        ss = _study(precision, seed=11)
+        for q, S in enumerate(ss):
+            S.engines = list(S.engines) + [DynDt(stepPeriod=(50, 100, 70, 100, 30)[q], maxRelInc=2e-2)]
+        return ss
+
+    mix = study()
+    B = Batch(mix)
+    for _ in range(3):
+        B.run(1000)
+    B.close()
+    alone = study()
+    changed = 0
+    for k, S in enumerate(alone):
+        S.run(3000)
+        S.sync()
+        assert S.step == mix[k].step == 3000
+        assert S.dt == mix[k].dt and S.time == mix[k].time, "scene %d dt/time alone vs batch" % k
+        ea, eb = S.engines[-1], mix[k].engines[-1]
+        assert (ea.nDone, ea.stepLast, ea.stepPrev) == (eb.nDone, eb.stepLast, eb.stepPrev)
+        changed += S.dt != study()[k].dt
+        A = _plan.compile_scene(S)
+        walls = A.particles["nodes"][A.particles["shape"] == 1, 0]
+        other = np.ones(A.n_nodes, bool)
+        other[walls] = False
+        for key in ("pos", "vel", "angVel"):
+            a, b = S.dem._nodes.soa.col(key), mix[k].dem._nodes.soa.col(key)
+            assert np.array_equal(a[other], b[other]), "scene %d %s differs alone vs batch" % (k, key)
+        S.close()
+    assert changed >= 3  # DynDt changed dt in most scenes

@@ -122,3 +122,37 @@ def test_dt_set_between_runs(gpu_lib):
     S.dt = 0.25 * dt0
     S.run(4)
     assert S.dt == 0.25 * dt0 and S.time == pytest.approx(t + 4 * 0.25 * dt0, rel=1e-12)
+
+
+@pytest.mark.parametrize("build", ["drum", "box"])
+def test_fp32_mode_against_fp64(build, gpu_lib):
+    """DynDt in the FP32-force mode: the stiffnesses come from the FP32 contact state (kn, kt and
+    the contact normal rounded to FP32; L6Geom.lens from the current overlap), so each critical
+    timestep agrees with the FP64 path's (bitwise equal to the oracle above) within 1e-3 relative,
+    and the activation counters agree exactly. From the same state, both precisions run 300 steps
+    with DynDt every 25 steps; dt after each evaluation is compared."""
+    if build == "drum":
+        mk = lambda prec: _with_dyndt(scenes.hertz_drum(n=3000, seed=2, diameter=0.3, length=0.12, div=31, axDiv=6,
+                                                        fill_fraction=0.3, settle_steps=3000, precision=prec),
+                                      stepPeriod=25, maxRelInc=5e-3)
+    else:
+        def mk(prec):
+            S = scenes.box_settle_small(n=1500, seed=0, precision=prec)
+            S.run(3000)
+            S.close()
+            return _with_dyndt(S, stepPeriod=25, maxRelInc=1e-2)
+    S64, S32 = mk("fp64"), mk("fp32")
+    crit = {}
+    for S in (S64, S32):
+        dts = []
+        for _ in range(12):
+            S.run(25)
+            dts.append((S.dt, S._sim.dyndt().crit_dt))
+        crit[S.gpu.precision] = dts
+        e = [x for x in S.engines if isinstance(x, DynDt)][0]
+        crit[S.gpu.precision + "_counters"] = (e.nDone, e.stepLast, e.stepPrev)
+    a, b = np.array(crit["fp64"]), np.array(crit["fp32"])
+    assert np.all(np.isfinite(a[:, 1])) and len(set(a[:, 0])) > 2
+    np.testing.assert_allclose(b[:, 1], a[:, 1], rtol=1e-3)
+    np.testing.assert_allclose(b[:, 0], a[:, 0], rtol=1e-3)
+    assert crit["fp64_counters"] == crit["fp32_counters"]

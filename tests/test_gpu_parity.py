@@ -134,7 +134,8 @@ def test_errors_are_raised(gpu_lib):
     """Unsupported engine lists and NaN states raise instead of running."""
     from woodem_gb300 import utils
     S = scenes.box_settle_small(n=50, seed=0, precision="fp32")
-    S.engines = utils.defaultEngines(damping=.2)  # includes DynDt, which runs in FP64 mode only
+    S.engines = utils.defaultEngines(damping=.2)
+    S.engines[0].reset = False  # Leapfrog without the force reset is outside the GPU path
     with pytest.raises(NotImplementedError):
         S.run(1)
     S = scenes.box_settle_small(n=50, seed=0)

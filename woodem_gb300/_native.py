@@ -95,6 +95,7 @@ def lib():
         "wg_get_nodes": (C.c_int, [C.c_void_p, P_D, P_D, P_D, P_D, P_D, P_D]),
         "wg_get_stats": (C.c_int, [C.c_void_p, C.POINTER(wg_stats)]),
         "wg_get_dyndt": (C.c_int, [C.c_void_p, C.POINTER(wg_dyndt_state)]),
+        "wg_get_scene_dyndt": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(wg_dyndt_state)]),
         "wg_set_dt": (C.c_int, [C.c_void_p, C.c_double, C.c_double]),
         "wg_get_energy": (C.c_int, [C.c_void_p, P_D, P_I32]),
         "wg_set_energy": (C.c_int, [C.c_void_p, P_D, P_I32]),

@@ -94,8 +94,6 @@ def compile_scene(S):
     if dyn is not None:
         if dyn.realPeriod > 0:
             raise NotImplementedError("DynDt.realPeriod (wall-clock activation) is not part of the GPU path")
-        if S.gpu.precision != "fp64":
-            raise NotImplementedError("DynDt runs in the FP64 precision mode only")
         if not (1.0 + dyn.maxRelInc != 1.0 and dyn.maxRelInc > 0):
             raise ValueError("DynDt: maxRelInc too small (1.0+maxRelInc==1.0)")
         cfg.update(dyndt=1, dyndt_dry_run=int(bool(dyn.dryRun)), dyndt_step_modulo=int(bool(dyn.stepModulo)),

@@ -10,7 +10,9 @@ different scenes never interact: each scene has its own broad-phase grid.
 
 The results of a scene do not depend on the batch it runs in: its particles are updated with
 the same operations in the same order as when it runs alone (the per-particle force sum follows
-the ids of the scene's own particles, which keep their relative order).
+the ids of the scene's own particles, which keep their relative order). Each scene keeps its own
+Scene.dt and DynDt engine (pkg/dem/DynDt.cpp:93-113): its critical timestep is the minimum over
+its own nodes, and its dt changes at the steps where it would change with the scene alone.
 """
 import ctypes as C
 
@@ -30,8 +32,6 @@ class Batch:
         if any(getattr(e, "_host", False) and not e.dead for S in self.scenes for e in S.engines):
             raise NotImplementedError("engines that run on the host (VtkExport) are not run in a Batch")
         self.arrays = [_plan.compile_scene(S) for S in self.scenes]
-        if any(A.config.get("dyndt") or A.config["next_dt"] == A.config["next_dt"] for A in self.arrays):
-            raise NotImplementedError("DynDt and Scene.nextDt are not supported in a Batch (each scene keeps its dt)")
         if any(A.config.get("track_energy") for A in self.arrays):
             raise NotImplementedError("energy tracking (Scene.trackEnergy) is not supported in a Batch")
         prec = {A.config["precision"] for A in self.arrays}
@@ -77,7 +77,10 @@ class Batch:
         self.stale = False
 
     def run(self, n):
-        """Advance every scene of the batch by ``n`` steps (Scene.run(n) for each)."""
+        """Advance every scene of the batch by ``n`` steps (Scene.run(n) for each); each scene
+        keeps its own Scene.dt, Scene.nextDt and DynDt engine (the batch's chunks of queued steps
+        end where any scene's DynDt is due)."""
+        from .dem import DynDt
         L, h = self.H.L, self.H.h
         self.H.check(L.wg_run(h, int(n)), "run")
         self.stale = True
@@ -85,6 +88,15 @@ class Batch:
             st = self.scene_stats(k)
             S.step = int(st.step)
             S.time = float(st.time)
+            d = _native.wg_dyndt_state()
+            self.H.check(L.wg_get_scene_dyndt(h, k, C.byref(d)), "get_scene_dyndt")
+            S.dt = float(d.dt)
+            S.nextDt = float(d.next_dt)
+            for e in S.engines:
+                if isinstance(e, DynDt) and not e.dead:
+                    e.nDone, e.stepLast, e.stepPrev = int(d.n_done), int(d.step_last), int(d.step_prev)
+                    e.virtLast, e.virtPrev = float(d.virt_last), float(d.virt_prev)
+                    e.dt = float(d.dyndt_dt)
 
     def scene_stats(self, k):
         st = _native.wg_stats()

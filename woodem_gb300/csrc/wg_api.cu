@@ -14,6 +14,12 @@
 #include "wg_math.cuh"
 
 namespace wg {
+// Scene.nextDt of a configuration: a positive finite value (0 and NaN: none)
+static double validNextDt(const wg_config& c) {
+    return (c.next_dt > 0 && std::isfinite(c.next_dt)) ? c.next_dt : std::numeric_limits<double>::quiet_NaN();
+}
+}  // namespace wg
+namespace wg {
 
 void collide_free(Sim& S);
 
@@ -528,7 +534,7 @@ int Sim::upload() {
         WG_CUDA_TRY(cudaMemcpyAsync(N.scene, nsc.data(), sizeof(int32_t) * nSlots, cudaMemcpyHostToDevice, S.stream));
     }
     dStep = (long long*)dalloc(sizeof(long long));
-    dFlags = (int*)dalloc(sizeof(int) * 4);
+    dFlags = (int*)dalloc(sizeof(int) * FL_WORDS);
     X.dApiMap = (int32_t*)dalloc(sizeof(int32_t) * std::max<int64_t>(1, na));
     X.dStage = (double*)dalloc(sizeof(double) * 19 * std::max<int64_t>(1, na));
     if (!X.dStage) return fail(WG_ERR_CUDA, "out of device memory (scene)");
@@ -587,7 +593,7 @@ int Sim::upload() {
             nc[q].mh = (float)m.w;
             nc[q].ml = (float)(m.w - (double)nc[q].mh);
             nc[q].flags = flags[q];
-            nc[q]._pad = 0;
+            nc[q].kind = (q < nPar && shape[q] != WG_SHAPE_FACET) ? NK_SUMMED : 0u;
         }
         std::vector<float4> orf(nSlots);
         std::vector<float2> rsp(nSlots);
@@ -638,7 +644,7 @@ int Sim::upload() {
     long long st0 = cfg.step;
     step = cfg.step;
     WG_CUDA_TRY(cudaMemcpyAsync(dStep, &st0, sizeof(long long), cudaMemcpyHostToDevice, S.stream));
-    WG_CUDA_TRY(cudaMemsetAsync(dFlags, 0, sizeof(int) * 4, S.stream));
+    WG_CUDA_TRY(cudaMemsetAsync(dFlags, 0, sizeof(int) * FL_WORDS, S.stream));
     int r = ensureContactCapacity(std::max<int64_t>(1024, 4 * nPar));
     if (r) return r;
     C.n = 0;
@@ -755,6 +761,96 @@ int Sim::ensureEnergyCapacity() {
 
 // Scene.dt of the steps from the next one on (core/Scene.cpp:389): the scene parameters the
 // kernels read, and the cell integration of periodic runs (which takes cfg.dt)
+// DynDt's engine state from the scene configuration (the counters carried over from the host)
+DynDtState dynDtFromConfig(const wg_config& c) {
+    DynDtState d;
+    d.on = c.dyndt != 0;
+    d.dryRun = c.dyndt_dry_run != 0;
+    d.stepModulo = c.dyndt_step_modulo != 0;
+    d.initRun = c.dyndt_init_run != 0;
+    d.stepPeriod = c.dyndt_step_period;
+    d.nDo = c.dyndt_n_do;
+    d.nDone = c.dyndt_n_done;
+    d.stepLast = c.dyndt_step_last;
+    d.stepPrev = c.dyndt_step_prev;
+    d.virtPeriod = c.dyndt_virt_period;
+    d.virtLast = c.dyndt_virt_last;
+    d.virtPrev = c.dyndt_virt_prev;
+    d.maxRelInc = c.dyndt_max_rel_inc;
+    d.dtSafety = c.dt_safety;
+    return d;
+}
+
+// Scene.dt of scene k of a batch (or slot) from the next step on
+int Sim::applyDtScene(int k, double ndt) {
+    Sim& S = *this;
+    cfgs[k].dt = ndt;
+    hPars[k].dt = ndt;
+    hPars[k].dtF = (float)ndt;
+    if (k == 0) {
+        cfg.dt = ndt;
+        hPar = hPars[0];
+    }
+    WG_CUDA_TRY(cudaMemcpyAsync(dPar + k, &hPars[k], sizeof(ScenePar), cudaMemcpyHostToDevice, stream));
+    return 0;
+}
+
+// DynDt::run (pkg/dem/DynDt.cpp:93-113) for the scenes of a batch whose DynDt is due after the
+// contact loop of device step deviceStep: one stiffness pass over all scenes, the critical
+// timestep of each scene (the minimum over its own nodes), then each due scene's rule.
+int Sim::runDynDtScenes(const std::vector<char>& due, long long deviceStep) {
+    Sim& S = *this;
+    if (I.endCap > kCap || !dCritB) {
+        if (I.endCap > kCap) {
+            if (dKA) dfree(dKA);
+            if (dKB) dfree(dKB);
+            kCap = std::max<int64_t>(I.endCap, 1);
+            dKA = (double4_32a*)dalloc(sizeof(double4_32a) * kCap);
+            dKB = (double2*)dalloc(sizeof(double2) * kCap);
+        }
+        if (!dCritB) dCritB = (unsigned long long*)dalloc(sizeof(unsigned long long) * nScenes);
+        if (!dKA || !dKB || !dCritB) return fail(WG_ERR_CUDA, "out of device memory (DynDt)");
+    }
+    const double inf = std::numeric_limits<double>::infinity();
+    unsigned long long bits;
+    std::memcpy(&bits, &inf, sizeof bits);
+    std::vector<unsigned long long> crit(nScenes, bits);
+    WG_CUDA_TRY(cudaMemsetAsync(dKA, 0, sizeof(double4_32a) * kCap, stream));
+    WG_CUDA_TRY(cudaMemsetAsync(dKB, 0, sizeof(double2) * kCap, stream));
+    WG_CUDA_TRY(cudaMemcpyAsync(dCritB, crit.data(), sizeof(unsigned long long) * nScenes, cudaMemcpyHostToDevice, stream));
+    const bool fp32 = prec == WG_PREC_FP32;
+    if (fp32) {
+        int r = syncContacts();
+        if (r) return r;
+    }
+    launch_dyndt(stream, N, P, C, I, dPar, dKA, dKB, dCritB, dFlags + FL_ERR, cfg.periodic != 0, fp32, true);
+    WG_CUDA_TRY(cudaGetLastError());
+    WG_CUDA_TRY(cudaMemcpyAsync(crit.data(), dCritB, sizeof(unsigned long long) * nScenes, cudaMemcpyDeviceToHost, stream));
+    WG_CUDA_TRY(cudaStreamSynchronize(stream));
+    for (int k = 0; k < nScenes; k++) {
+        if (!due[k]) continue;
+        DynDtState& d = bdd[k];
+        double minSq;
+        std::memcpy(&minSq, &crit[k], sizeof minSq);
+        const double crDt = std::sqrt(minSq);
+        d.critDt = crDt;
+        d.nEvals++;
+        if (std::isinf(crDt)) continue;
+        const int64_t nSteps = sceneStep(k, deviceStep) - d.stepPrev;
+        const double maxNewDt = hPars[k].dt * std::pow(1. + d.maxRelInc, (double)nSteps);
+        const double a = crDt * d.dtSafety;
+        const double ndt = maxNewDt < a ? maxNewDt : a;
+        if (!d.dryRun) {
+            if (ndt != hPars[k].dt) {
+                d.dynDt = std::numeric_limits<double>::quiet_NaN();
+                bNextDt[k] = ndt;
+            }
+        } else
+            d.dynDt = ndt;
+    }
+    return 0;
+}
+
 int Sim::applyDt(double ndt) {
     Sim& S = *this;
     cfg.dt = ndt;
@@ -788,7 +884,12 @@ int Sim::runDynDt(int64_t stepNow) {
     WG_CUDA_TRY(cudaMemsetAsync(dKA, 0, sizeof(double4_32a) * kCap, stream));
     WG_CUDA_TRY(cudaMemsetAsync(dKB, 0, sizeof(double2) * kCap, stream));
     WG_CUDA_TRY(cudaMemcpyAsync(dCrit, &bits, sizeof bits, cudaMemcpyHostToDevice, stream));
-    launch_dyndt(stream, N, P, C, I, dPar, dKA, dKB, dCrit, dFlags + FL_ERR, cfg.periodic != 0);
+    const bool fp32 = prec == WG_PREC_FP32;
+    if (fp32) {
+        int r = syncContacts();  // the packed sphere-sphere state back into the contact arrays
+        if (r) return r;
+    }
+    launch_dyndt(stream, N, P, C, I, dPar, dKA, dKB, dCrit, dFlags + FL_ERR, cfg.periodic != 0, fp32);
     WG_CUDA_TRY(cudaGetLastError());
     WG_CUDA_TRY(cudaMemcpyAsync(&bits, dCrit, sizeof bits, cudaMemcpyDeviceToHost, stream));
     WG_CUDA_TRY(cudaStreamSynchronize(stream));
@@ -891,7 +992,7 @@ int Sim::run(int64_t n) {
         if (!advanced) launch_advance(stream, dStep, dFlags);
         launches += advanced ? 1 : 2;
     };
-    WG_CUDA_TRY(cudaMemsetAsync(dFlags, 0, sizeof(int) * 4, stream));
+    WG_CUDA_TRY(cudaMemsetAsync(dFlags, 0, sizeof(int) * FL_WORDS, stream));
     WG_CUDA_TRY(cudaEventRecord(ev[6], stream));
     int64_t done = 0;
     while (done < n) {
@@ -904,6 +1005,23 @@ int Sim::run(int64_t n) {
         int64_t k = std::min<int64_t>(n - done, maxChunk);
         // dt may change after a step (Scene.nextDt, DynDt): such a step ends its chunk
         if (std::isfinite(nextDt)) k = 1;
+        if (batchDyn) {
+            // the same for every scene of a batch, with the scene's own step, time and dt
+            for (int q = 0; q < nScenes; q++) {
+                if (std::isfinite(bNextDt[q])) k = 1;
+                if (!bdd[q].on) continue;
+                DynDtState t = bdd[q];
+                double tv = bTime[q];
+                for (int64_t j = 0; j < k; j++) {
+                    if (sceneFrozen(q, step + j)) break;
+                    if (t.activated(sceneStep(q, step + j), tv)) {
+                        k = j + 1;
+                        break;
+                    }
+                    tv += hPars[q].dt;
+                }
+            }
+        }
         if (dd.on) {
             DynDtState t = dd;
             double tv = timeAbs;
@@ -1052,6 +1170,34 @@ int Sim::run(int64_t n) {
         }
         step += ds;
         done += ds;
+        if (nScenes > 1 && ds > 0) {
+            // each scene of the batch: its DynDt turn (the chunk ends at any scene's activation),
+            // time += its dt for each step it did (not frozen), then its dt = nextDt
+            std::vector<char> due(nScenes, 0);
+            bool anyDue = false;
+            for (int q = 0; q < nScenes; q++) {
+                for (int64_t j = 0; j < ds; j++) {
+                    const long long sd = step - ds + j;
+                    if (sceneFrozen(q, sd)) break;
+                    if (bdd[q].on && bdd[q].activated(sceneStep(q, sd), bTime[q])) {
+                        if (j != ds - 1) return fail(WG_ERR_STATE, "DynDt activation inside a chunk");
+                        due[q] = 1;
+                        anyDue = true;
+                    }
+                    bTime[q] += hPars[q].dt;
+                }
+            }
+            if (anyDue) {
+                int r = runDynDtScenes(due, step - 1);
+                if (r) return r;
+            }
+            for (int q = 0; q < nScenes; q++)
+                if (std::isfinite(bNextDt[q])) {
+                    int r = applyDtScene(q, bNextDt[q]);
+                    if (r) return r;
+                    bNextDt[q] = std::numeric_limits<double>::quiet_NaN();
+                }
+        }
         if (ds > 0) {
             if (dynDtNow) {
                 int r = runDynDt(step - 1);
@@ -1155,32 +1301,14 @@ int wg_set_config(wg_scene* s, const wg_config* c) {
     Sim& S = *SIM(s);
     if (S.uploaded) return S.fail(WG_ERR_STATE, "configuration is fixed once the scene runs; create a new scene");
     if (!(c->dt > 0) || !std::isfinite(c->dt)) return S.fail(WG_ERR_ARG, "Scene.dt must be positive and finite");
-    if (c->dyndt && c->precision != WG_PREC_FP64)
-        return S.fail(WG_ERR_UNSUPPORTED, "DynDt runs in the FP64 precision mode only");
     if (c->track_energy && c->precision != WG_PREC_FP64)
         return S.fail(WG_ERR_UNSUPPORTED, "energy tracking runs in the FP64 precision mode only");
     if (c->dyndt && !(c->dyndt_max_rel_inc > 0 && 1. + c->dyndt_max_rel_inc != 1.))
         return S.fail(WG_ERR_ARG, "DynDt: maxRelInc too small (1.0+maxRelInc==1.0)");  // DynDt::postLoad, DynDt.cpp:12-14
     S.cfg = *c;
     S.haveCfg = true;
-    DynDtState& d = S.dd;
-    d = DynDtState{};
-    d.on = c->dyndt != 0;
-    d.dryRun = c->dyndt_dry_run != 0;
-    d.stepModulo = c->dyndt_step_modulo != 0;
-    d.initRun = c->dyndt_init_run != 0;
-    d.stepPeriod = c->dyndt_step_period;
-    d.nDo = c->dyndt_n_do;
-    d.nDone = c->dyndt_n_done;
-    d.stepLast = c->dyndt_step_last;
-    d.stepPrev = c->dyndt_step_prev;
-    d.virtPeriod = c->dyndt_virt_period;
-    d.virtLast = c->dyndt_virt_last;
-    d.virtPrev = c->dyndt_virt_prev;
-    d.maxRelInc = c->dyndt_max_rel_inc;
-    d.dtSafety = c->dt_safety;
-    // Scene.nextDt: a positive finite value (0 and NaN: none)
-    S.nextDt = (c->next_dt > 0 && std::isfinite(c->next_dt)) ? c->next_dt : std::numeric_limits<double>::quiet_NaN();
+    S.dd = dynDtFromConfig(*c);
+    S.nextDt = validNextDt(*c);
     S.timeAbs = c->time;
     S.trackE = c->track_energy != 0;
     return WG_OK;
@@ -1194,13 +1322,25 @@ int wg_set_scenes(wg_scene* s, int32_t n_scenes, const wg_config* cfgs, const in
     for (int k = 0; k < n_scenes; k++) {
         if (particle_start[k + 1] < particle_start[k]) return S.fail(WG_ERR_ARG, "particle_start must be non-decreasing");
         if (!(cfgs[k].dt > 0) || !std::isfinite(cfgs[k].dt)) return S.fail(WG_ERR_ARG, "Scene.dt must be positive and finite");
-        if (cfgs[k].dyndt || (cfgs[k].next_dt > 0 && std::isfinite(cfgs[k].next_dt)) || cfgs[k].track_energy)
-            return S.fail(WG_ERR_UNSUPPORTED, "DynDt, Scene.nextDt and energy tracking are not supported in a batch of scenes");
+        if (cfgs[k].track_energy)
+            return S.fail(WG_ERR_UNSUPPORTED, "energy tracking is not supported in a batch of scenes");
+        if (cfgs[k].dyndt && !(cfgs[k].dyndt_max_rel_inc > 0 && 1. + cfgs[k].dyndt_max_rel_inc != 1.))
+            return S.fail(WG_ERR_ARG, "DynDt: maxRelInc too small (1.0+maxRelInc==1.0)");
     }
     S.nScenes = n_scenes;
     S.cfgs.assign(cfgs, cfgs + n_scenes);
     S.sceneStart.assign(particle_start, particle_start + n_scenes + 1);
     S.sceneTime0.assign(n_scenes, 0.0);
+    S.bdd.assign(n_scenes, DynDtState{});
+    S.bTime.assign(n_scenes, 0.0);
+    S.bNextDt.assign(n_scenes, std::numeric_limits<double>::quiet_NaN());
+    S.batchDyn = false;
+    for (int k = 0; k < n_scenes; k++) {
+        S.bdd[k] = dynDtFromConfig(cfgs[k]);
+        S.bTime[k] = cfgs[k].time;
+        S.bNextDt[k] = validNextDt(cfgs[k]);
+        S.batchDyn = S.batchDyn || S.bdd[k].on || std::isfinite(S.bNextDt[k]);
+    }
     S.cfg = cfgs[0];
     S.haveCfg = true;
     return WG_OK;
@@ -1283,7 +1423,7 @@ static int writeSlot(Sim& S, int64_t p0, int64_t cap, int64_t n, const double* p
             nc[q].mh = (float)m.w;
             nc[q].ml = (float)(m.w - (double)nc[q].mh);
             nc[q].flags = fl[q];
-            nc[q]._pad = 0;
+            nc[q].kind = sh[q] != WG_SHAPE_FACET ? NK_SUMMED : 0u;
             split(posr[q].x, ph[q].x, pl[q].x);
             split(posr[q].y, ph[q].y, pl[q].y);
             split(posr[q].z, ph[q].z, pl[q].z);
@@ -1345,8 +1485,9 @@ int wg_slot_load(wg_scene* s, int32_t k, const wg_config* c, int64_t n, const do
     Sim& S = *SIM(s);
     int r = slotCheck(S, k);
     if (r) return r;
-    if (c->dyndt || (c->next_dt > 0 && std::isfinite(c->next_dt)) || c->track_energy)
-        return S.fail(WG_ERR_UNSUPPORTED, "DynDt, Scene.nextDt and energy tracking are not supported in serving slots");
+    if (c->track_energy) return S.fail(WG_ERR_UNSUPPORTED, "energy tracking is not supported in serving slots");
+    if (c->dyndt && !(c->dyndt_max_rel_inc > 0 && 1. + c->dyndt_max_rel_inc != 1.))
+        return S.fail(WG_ERR_ARG, "DynDt: maxRelInc too small (1.0+maxRelInc==1.0)");
     const int64_t p0 = S.sceneStart[k], cap = S.sceneStart[k + 1] - p0;
     if (n > cap) return S.fail(WG_ERR_CAPACITY, "job larger than the slot");
     const int32_t matCap = (int32_t)(S.hDensity.size() / S.nScenes);
@@ -1377,6 +1518,10 @@ int wg_slot_load(wg_scene* s, int32_t k, const wg_config* c, int64_t n, const do
     S.hPars[k].stepBase = (long long)S.step - (long long)c->step;
     S.hPars[k].stepEnd = (long long)c->step + (long long)n_steps;
     S.sceneTime0[k] = 0.;
+    S.bdd[k] = dynDtFromConfig(*c);
+    S.bTime[k] = c->time;
+    S.bNextDt[k] = validNextDt(*c);
+    S.batchDyn = S.batchDyn || S.bdd[k].on || std::isfinite(S.bNextDt[k]);
     if (k == 0) S.hPar = S.hPars[0];
     WG_CUDA_TRY(cudaMemcpyAsync(S.dPar + k, &S.hPars[k], sizeof(ScenePar), cudaMemcpyHostToDevice, S.stream));
     return WG_OK;
@@ -1391,6 +1536,8 @@ int wg_slot_clear(wg_scene* s, int32_t k) {
     for (int64_t p = p0; p < p0 + cap; p++) S.hParked[p] = 1;
     WG_CUDA_TRY(cudaMemsetAsync(S.P.fresh + p0, 1, cap, S.stream));
     S.hPars[k].stepEnd = -((long long)1 << 62);  // frozen
+    S.bdd[k].on = false;
+    S.bNextDt[k] = std::numeric_limits<double>::quiet_NaN();
     if (k == 0) S.hPar = S.hPars[0];
     WG_CUDA_TRY(cudaMemcpyAsync(S.dPar + k, &S.hPars[k], sizeof(ScenePar), cudaMemcpyHostToDevice, S.stream));
     S.listsDirty = true;
@@ -1467,7 +1614,7 @@ int wg_get_scene_stats(wg_scene* s, int32_t k, wg_stats* o) {
     const wg_config& c = S.nScenes > 1 ? S.cfgs[k] : S.cfg;
     const int64_t done = S.step - S.cfg.step;
     o->step = c.step + done;
-    o->time = S.nScenes > 1 ? S.sceneTime0[k] + done * c.dt : S.time;
+    o->time = S.nScenes > 1 ? S.bTime[k] : S.time;
     o->n_full_runs = S.nFullRuns;
     o->verlet_dist = S.nScenes > 1 && S.uploaded ? S.hPars[k].verletDist : S.hPar.verletDist;
     if (S.uploaded && S.C.n > 0) {
@@ -1687,6 +1834,25 @@ int wg_get_dyndt(wg_scene* s, wg_dyndt_state* o) {
     o->n_evals = S.dd.nEvals;
     o->virt_last = S.dd.virtLast;
     o->virt_prev = S.dd.virtPrev;
+    return WG_OK;
+}
+
+int wg_get_scene_dyndt(wg_scene* s, int32_t k, wg_dyndt_state* o) {
+    if (!s || !o) return WG_ERR_ARG;
+    Sim& S = *SIM(s);
+    if (S.nScenes <= 1) return k == 0 ? wg_get_dyndt(s, o) : S.fail(WG_ERR_ARG, "scene index out of range");
+    if (k < 0 || k >= S.nScenes || (int64_t)S.bdd.size() != S.nScenes) return S.fail(WG_ERR_ARG, "scene index out of range");
+    const DynDtState& d = S.bdd[k];
+    o->dt = S.cfgs[k].dt;
+    o->next_dt = S.bNextDt[k];
+    o->dyndt_dt = d.dynDt;
+    o->crit_dt = d.critDt;
+    o->n_done = d.nDone;
+    o->step_last = d.stepLast;
+    o->step_prev = d.stepPrev;
+    o->n_evals = d.nEvals;
+    o->virt_last = d.virtLast;
+    o->virt_prev = d.virtPrev;
     return WG_OK;
 }
 

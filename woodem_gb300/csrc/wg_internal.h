@@ -182,8 +182,9 @@ struct NodeConst32 {
     float invI[3];
     float mh, ml;
     uint32_t flags;
-    uint32_t _pad;
+    uint32_t kind;  // NK_SUMMED: the node of a particle whose force is the sum of its end slots (not a facet)
 };
+enum : uint32_t { NK_SUMMED = 1u };
 // Particles with more end slots than this are summed by a block tree instead of one lane.
 constexpr int kHeavyThreshold = 64;
 // End slots a warp of the FP32 Leapfrog stages per chunk (32 particles of ~6 contacts each fit
@@ -204,11 +205,13 @@ struct DevPackedSS {
     bool ftLive = false;       // ft is copied (some scene used IdealElPl at the last full run); it is
                                // read only for contacts of scenes with that law
 };
-// Step-loop flag words (device int[3]).
+// Step-loop flag words (device int[FL_WORDS]).
 enum { FL_FULL = 0,   // set by Leapfrog: a node moved farther than verletDist, a full collider run is due
        FL_ERR = 1,    // error code raised by a kernel
        FL_HALT = 2,   // set by the contact kernel of a step that found FL_FULL: later queued steps do nothing
-       FL_TICKET = 3 }; // blocks of the last contact kernel of a step that have finished (the last advances the step)
+       FL_TICKET = 3, // blocks of the last contact kernel of a step that have finished (the last advances the step)
+       FL_WORK = 4,   // chunks of the sphere-sphere work handed out in this step (zero between launches)
+       FL_WORDS = 8 };
 
 __host__ __device__ inline int32_t packCellDist(int a, int b, int c) {
     return (int32_t)(((uint32_t)(a + 512) & 1023u) | (((uint32_t)(b + 512) & 1023u) << 10) | (((uint32_t)(c + 512) & 1023u) << 20));
@@ -245,9 +248,12 @@ void launch_energy_sum(cudaStream_t st, const EnergyCols& E, int which, int64_t 
                        const int* dFlags, bool kinSplit);
 // DynDt: per-end stiffness of the real contacts into kA/kB (zeroed by the caller, I.endCap
 // entries), then the minimum over nodes of the squared critical timestep into *out (initialised
-// by the caller to the bits of +Inf). FP64 contact arrays.
+// by the caller to the bits of +Inf). FP64 contact arrays, or with fp32 the FP32-force mode's
+// (the packed sphere-sphere state written back first).
+// perScene: out holds one value per scene of a batch (the minimum over that scene's nodes).
 void launch_dyndt(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C, const DevIncidence& I,
-                  const ScenePar* sp, double4_32a* kA, double2* kB, unsigned long long* out, int* dErr, bool periodic);
+                  const ScenePar* sp, double4_32a* kA, double2* kB, unsigned long long* out, int* dErr, bool periodic,
+                  bool fp32 = false, bool perScene = false);
 // sum over real contacts of F_A (x) branch into out[9] (not divided by the volume); scratch holds
 // 9 doubles per 256 active contacts; returns -1 when it is too small
 int launch_stress(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C, const DevIncidence& I,
@@ -290,6 +296,8 @@ struct Sim;
 int collide_full_run(Sim& S);
 
 // DynDt after ContactLoop (pkg/dem/DynDt.hpp:19-23) with the counters of its PeriodicEngine.
+struct DynDtState;
+DynDtState dynDtFromConfig(const wg_config& c);
 struct DynDtState {
     bool on = false, dryRun = false, stepModulo = true, initRun = true;
     int64_t stepPeriod = 0, nDo = -1, nDone = 0, stepLast = -1, stepPrev = -1, nEvals = 0;
@@ -398,6 +406,16 @@ struct Sim {
     double2* dKB = nullptr;
     int64_t kCap = 0;
     unsigned long long* dCrit = nullptr;
+    // batch of scenes or serving slots (nScenes > 1) with DynDt or Scene.nextDt: per scene the
+    // engine state, Scene.time (accumulated with the scene's own dt) and Scene.nextDt
+    bool batchDyn = false;
+    std::vector<DynDtState> bdd;
+    std::vector<double> bTime, bNextDt;
+    unsigned long long* dCritB = nullptr;  // one critical timestep (squared, as bits) per scene
+    long long sceneStep(int k, long long deviceStep) const { return deviceStep - hPars[k].stepBase; }
+    bool sceneFrozen(int k, long long deviceStep) const { return sceneStep(k, deviceStep) >= hPars[k].stepEnd; }
+    int runDynDtScenes(const std::vector<char>& due, long long deviceStep);
+    int applyDtScene(int k, double dt);
     // energy tracking (one scene, FP64 mode): Scene.energy on the device and the per-step scratch
     bool trackE = false;
     EnergyCols eNode, eCon;

@@ -2,16 +2,17 @@
 //
 // Who needs it: a caller that must not allocate device memory -- for example a host process
 // whose device memory is owned and budgeted by another runtime (a pooled allocator that
-// forbids raw cudaMalloc/cudaFree), code running while a stream is being captured into a CUDA
-// graph (where cudaMalloc would break the capture), or a real-time loop that cannot afford
-// the synchronisation that cudaMalloc/cudaFree imply. Such a caller can still hand over the
-// sphere boxes in host memory and get the overlapping pairs back in host memory.
+// forbids raw cudaMalloc/cudaFree), or a real-time loop that cannot afford the device-wide
+// synchronisation that cudaMalloc/cudaFree imply. Such a caller can still hand over the sphere
+// boxes in host memory and get the overlapping pairs back in host memory.
 //
 // How: the scratch that the regular broad phase allocates (boxes in device layout, grid keys,
 // sort buffers, cell offsets, pair buffers, sort temporaries) lives in one file-scope
 // __device__ array of fixed size. Every GPU that loads libwoogpu.so holds this array
 // (WG_NOALLOC_SCRATCH_BYTES, about 13 MB) until the process exits. Sizes above
-// WG_NOALLOC_MAX_SPHERES spheres or WG_NOALLOC_MAX_PAIRS pairs are rejected.
+// WG_NOALLOC_MAX_SPHERES spheres or WG_NOALLOC_MAX_PAIRS pairs are rejected. Every call uses
+// the same array, so two calls that overlap on the GPU (host threads calling it at the same
+// time on one device) race and corrupt each other's result.
 //
 // The pair set is the one the collider computes for spheres: closed 3-axis overlap of the
 // boxes and the mask test of Collider::mayCollide (pkg/dem/Collision.cpp:19-41).
@@ -49,7 +50,7 @@ constexpr size_t O_PAIRS = O_OFF + align256(sizeof(int32_t) * (NC + 1));
 constexpr size_t O_PAIRSS = O_PAIRS + align256(sizeof(uint64_t) * NP);
 constexpr size_t O_CNT = O_PAIRSS + align256(sizeof(uint64_t) * NP);
 constexpr size_t O_RED = O_CNT + 256;
-constexpr size_t O_TMP = O_RED + align256(sizeof(double) * 7 * 256);
+constexpr size_t O_TMP = O_RED + align256(sizeof(double) * 8 * 256);
 constexpr size_t TMP_BYTES = size_t(4) << 20;
 constexpr size_t SCRATCH_BYTES = O_TMP + TMP_BYTES;
 
@@ -63,28 +64,37 @@ namespace wg_noalloc {
 
 static const int BS = 256;
 
+// Per block: the lowest and highest box minimum per axis, the largest box extent, and the number
+// of box components that are not finite (fmin/fmax skip NaN, so those are counted apart).
+constexpr int NRED = 8;
 __global__ void k_reduce_boxes(const double* __restrict__ mn, const double* __restrict__ mx, int n, double* __restrict__ partial) {
-    __shared__ double s[7][BS];
+    __shared__ double s[NRED][BS];
     const double inf = __longlong_as_double(0x7ff0000000000000LL);
-    double v[7] = {inf, inf, inf, -inf, -inf, -inf, 0.};
+    double v[NRED] = {inf, inf, inf, -inf, -inf, -inf, 0., 0.};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         for (int k = 0; k < 3; k++) {
-            v[k] = fmin(v[k], mn[3 * i + k]);
-            v[3 + k] = fmax(v[3 + k], mn[3 * i + k]);
-            v[6] = fmax(v[6], mx[3 * i + k] - mn[3 * i + k]);
+            const double a = mn[3 * i + k], b = mx[3 * i + k];
+            if (!isfinite(a) || !isfinite(b)) {
+                v[7] += 1.;
+                continue;
+            }
+            v[k] = fmin(v[k], a);
+            v[3 + k] = fmax(v[3 + k], a);
+            v[6] = fmax(v[6], b - a);
         }
     }
-    for (int q = 0; q < 7; q++) s[q][threadIdx.x] = v[q];
+    for (int q = 0; q < NRED; q++) s[q][threadIdx.x] = v[q];
     __syncthreads();
     for (int st = blockDim.x / 2; st > 0; st >>= 1) {
         if (threadIdx.x < st) {
             for (int q = 0; q < 3; q++) s[q][threadIdx.x] = fmin(s[q][threadIdx.x], s[q][threadIdx.x + st]);
             for (int q = 3; q < 7; q++) s[q][threadIdx.x] = fmax(s[q][threadIdx.x], s[q][threadIdx.x + st]);
+            s[7][threadIdx.x] += s[7][threadIdx.x + st];
         }
         __syncthreads();
     }
     if (threadIdx.x == 0)
-        for (int q = 0; q < 7; q++) partial[blockIdx.x * 7 + q] = s[q][0];
+        for (int q = 0; q < NRED; q++) partial[blockIdx.x * NRED + q] = s[q][0];
 }
 
 __device__ __forceinline__ int cellCoord(double v, double o, double h, int n) {
@@ -172,7 +182,8 @@ __global__ void k_split(const uint64_t* __restrict__ p, int64_t n, int32_t* __re
     hi[i] = (int32_t)(p[i] & 0xffffffffu);
 }
 
-// one scratch address per device, resolved once with that device current
+// one scratch address per device, resolved at the first call on that device with the device
+// current (a cudaDeviceReset afterwards invalidates it: the library is not used across one)
 static std::mutex g_mu;
 static unsigned char* g_addr[64] = {nullptr};
 static thread_local std::string g_err;
@@ -240,20 +251,32 @@ int wg_broadphase_noalloc(int32_t n, const double* mn, const double* mx, const u
     // grid over the boxes: cell edge just above the largest box extent
     const int nb = std::min(256, (n + BS - 1) / BS);
     k_reduce_boxes<<<nb, BS, 0, st>>>(dmn, dmx, n, red);
-    double hred[7 * 256];
-    NA_TRY(cudaMemcpy(hred, red, sizeof(double) * 7 * nb, cudaMemcpyDeviceToHost));
-    double v[7] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY, 0.};
+    double hred[NRED * 256];
+    NA_TRY(cudaMemcpy(hred, red, sizeof(double) * NRED * nb, cudaMemcpyDeviceToHost));
+    double v[NRED] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY, 0., 0.};
     for (int b = 0; b < nb; b++) {
-        for (int q = 0; q < 3; q++) v[q] = std::min(v[q], hred[7 * b + q]);
-        for (int q = 3; q < 7; q++) v[q] = std::max(v[q], hred[7 * b + q]);
+        for (int q = 0; q < 3; q++) v[q] = std::min(v[q], hred[NRED * b + q]);
+        for (int q = 3; q < 7; q++) v[q] = std::max(v[q], hred[NRED * b + q]);
+        v[7] += hred[NRED * b + 7];
     }
-    if (!(std::isfinite(v[0]) && std::isfinite(v[3]) && std::isfinite(v[6])))
-        return fail(WG_ERR_ARG, "wg_broadphase_noalloc: boxes must be finite");
-    double h = v[6] * (1 + 1e-9) + 1e-300;
+    if (v[7] != 0. || !(std::isfinite(v[0]) && std::isfinite(v[3]) && std::isfinite(v[6])))
+        return fail(WG_ERR_ARG, "wg_broadphase_noalloc: boxes must be finite (NaN or infinite coordinate)");
+    // cell edge: at least the largest box extent (so that the half shell sees every overlap) and
+    // at least the widest spread over the cube root of the cell budget (so that the grid fits);
+    // the dimensions are formed in double and clamped before they are multiplied
+    double range = 0.;
+    for (int q = 0; q < 3; q++) range = std::max(range, v[3 + q] - v[q]);
+    double h = std::max(v[6] * (1 + 1e-9), range / std::cbrt((double)WG_NOALLOC_MAX_CELLS));
+    if (!(h > 0.) || !std::isfinite(h)) h = 1.;  // every box is the same point: one cell
     int64_t dims[3];
     for (;;) {
-        for (int q = 0; q < 3; q++) dims[q] = (int64_t)std::floor((v[3 + q] - v[q]) / h) + 1;
-        if (dims[0] * dims[1] * dims[2] <= (int64_t)WG_NOALLOC_MAX_CELLS) break;
+        double prod = 1.;
+        for (int q = 0; q < 3; q++) {
+            const double d = std::min(std::floor((v[3 + q] - v[q]) / h) + 1., (double)WG_NOALLOC_MAX_CELLS);
+            dims[q] = (int64_t)d;
+            prod *= d;
+        }
+        if (prod <= (double)WG_NOALLOC_MAX_CELLS) break;
         h *= 1.25;
     }
     const int64_t ncell = dims[0] * dims[1] * dims[2];

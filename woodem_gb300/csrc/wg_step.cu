@@ -829,7 +829,11 @@ int launch_stress(cudaStream_t st, const DevNodes& N, const DevParticles& P, con
 // functor recomputes here from the unchanged positions. lens are |r| + uN/2 of the contact's first
 // step (L6Geom.cpp:63-66). Facets are left out (their nodes must be fully blocked). The slots
 // are zeroed beforehand, so non-real contacts add nothing.
-template <bool PERI>
+// F32: the contact state of the FP32-force mode (trsf columns and phys constants in FP32, written
+// back from the packed sphere-sphere state before the call); n is trsf column 0 itself, and the
+// lens are |r| + uN/2 of the current step (that mode keeps no uN of the first step: the
+// difference is uN0/2 - uN/2, below 1e-4 of the radius for the overlaps of a stable contact).
+template <bool PERI, bool F32>
 __global__ void __launch_bounds__(128) k_dyndt_ends(DevNodes N, DevParticles P, DevContacts C, DevIncidence I,
                                                     const ScenePar* __restrict__ spp, double4_32a* __restrict__ kA,
                                                     double2* __restrict__ kB, int* __restrict__ dErr) {
@@ -850,22 +854,34 @@ __global__ void __launch_bounds__(128) k_dyndt_ends(DevNodes N, DevParticles P, 
         shift2 = mul(ldm(sp.hSize), D3{(double)a, (double)b, (double)cc});
     }
     Geo g;
+    const double wallSense = ty == CT_WS ? (F32 ? (double)C.fcol[CF_T0X + P.aux[A].x][c] : C.col[CC_T0X + P.aux[A].x][c]) : 0.;
     if (ty == CT_SS) geomSS(N, A, B, shift2, true, sp.ssDistFactor, g);
-    else if (ty == CT_WS) geomWS(N, P, C.col[CC_T0X + P.aux[A].x][c], A, B, shift2, true, g);
+    else if (ty == CT_WS) geomWS(N, P, wallSense, A, B, shift2, true, g);
     else geomFS(N, P, A, B, shift2, true, g, dErr);
-    const D3 c0{C.col[CC_T0X][c], C.col[CC_T0Y][c], C.col[CC_T0Z][c]};
-    const D3 c1{C.col[CC_T1X][c], C.col[CC_T1Y][c], C.col[CC_T1Z][c]};
-    const D3 n = qrot(quatFromCols(c0, c1, cross(c0, c1)), D3{1., 0., 0.});
+    D3 n;
+    double p0, p1, uN0;
+    if (F32) {
+        n = D3{(double)C.fcol[CF_T0X][c], (double)C.fcol[CF_T0Y][c], (double)C.fcol[CF_T0Z][c]};
+        p0 = C.fcol[CF_P0][c];
+        p1 = C.fcol[CF_P1][c];
+        uN0 = g.uN;
+    } else {
+        const D3 c0{C.col[CC_T0X][c], C.col[CC_T0Y][c], C.col[CC_T0Z][c]};
+        const D3 c1{C.col[CC_T1X][c], C.col[CC_T1Y][c], C.col[CC_T1Z][c]};
+        n = qrot(quatFromCols(c0, c1, cross(c0, c1)), D3{1., 0., 0.});
+        p0 = C.col[CC_P0][c];
+        p1 = C.col[CC_P1][c];
+        uN0 = C.col[CC_UN0][c];
+    }
     const D3 n2{n.x * n.x, n.y * n.y, n.z * n.z};
     double kn, kt;
     if (sp.law == 0) {
-        kn = C.col[CC_P0][c];
-        kt = C.col[CC_P1][c];
+        kn = p0;
+        kt = p1;
     } else {
-        kn = (3 / 2.) * C.col[CC_P0][c] * sqrt(-g.uN);
-        kt = C.col[CC_P1][c] * sqrt(g.uN < 0 ? -g.uN : 0);
+        kn = (3 / 2.) * p0 * sqrt(-g.uN);
+        kt = p1 * sqrt(g.uN < 0 ? -g.uN : 0);
     }
-    const double uN0 = C.col[CC_UN0][c];
     double l0 = fabs(g.r1) + uN0 / 2, l1 = fabs(g.r2) + uN0 / 2;
     if (l0 < 0) l0 = l1;
     if (l1 < 0) l1 = l0;
@@ -889,8 +905,10 @@ __global__ void __launch_bounds__(128) k_dyndt_ends(DevNodes N, DevParticles P, 
 // Particle.contacts), then 2·min(m/|ktrans_i|, I_i/|krot_i|) over the free, stiff axes; fully
 // blocked nodes are always stable. The minimum over nodes (critDt_stiffness, :66-76) goes to
 // *out as the bits of a non-negative double.
+// perScene: out[scene of the node] instead of *out (a batch of scenes, each with its own DynDt).
 __global__ void __launch_bounds__(256) k_dyndt_nodes(DevNodes N, DevParticles P, DevIncidence I, const double4_32a* __restrict__ kA,
-                                                     const double2* __restrict__ kB, unsigned long long* __restrict__ out) {
+                                                     const double2* __restrict__ kB, unsigned long long* __restrict__ out,
+                                                     int perScene) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     const double kInf = __longlong_as_double(0x7ff0000000000000LL);
     double v = kInf;
@@ -922,6 +940,10 @@ __global__ void __launch_bounds__(256) k_dyndt_nodes(DevNodes N, DevParticles P,
             v = 2 * ret;
         }
     }
+    if (perScene) {  // uniform over the grid
+        if (v < kInf) atomicMin(out + sceneOfP(P, p), (unsigned long long)__double_as_longlong(v));
+        return;
+    }
     // block minimum, then one atomic per block (non-negative doubles order like their bit patterns)
     __shared__ double sm[256];
     sm[threadIdx.x] = v;
@@ -937,13 +959,19 @@ __global__ void __launch_bounds__(256) k_dyndt_nodes(DevNodes N, DevParticles P,
 }
 
 void launch_dyndt(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C, const DevIncidence& I,
-                  const ScenePar* sp, double4_32a* kA, double2* kB, unsigned long long* out, int* dErr, bool periodic) {
+                  const ScenePar* sp, double4_32a* kA, double2* kB, unsigned long long* out, int* dErr, bool periodic, bool fp32,
+                  bool perScene) {
     if (I.nAct > 0) {
         const unsigned g = (unsigned)((I.nAct + 127) / 128);
-        if (periodic) k_dyndt_ends<true><<<g, 128, 0, st>>>(N, P, C, I, sp, kA, kB, dErr);
-        else k_dyndt_ends<false><<<g, 128, 0, st>>>(N, P, C, I, sp, kA, kB, dErr);
+        if (fp32) {
+            if (periodic) k_dyndt_ends<true, true><<<g, 128, 0, st>>>(N, P, C, I, sp, kA, kB, dErr);
+            else k_dyndt_ends<false, true><<<g, 128, 0, st>>>(N, P, C, I, sp, kA, kB, dErr);
+        } else {
+            if (periodic) k_dyndt_ends<true, false><<<g, 128, 0, st>>>(N, P, C, I, sp, kA, kB, dErr);
+            else k_dyndt_ends<false, false><<<g, 128, 0, st>>>(N, P, C, I, sp, kA, kB, dErr);
+        }
     }
-    if (P.n > 0) k_dyndt_nodes<<<(P.n + 255) / 256, 256, 0, st>>>(N, P, I, kA, kB, out);
+    if (P.n > 0) k_dyndt_nodes<<<(P.n + 255) / 256, 256, 0, st>>>(N, P, I, kA, kB, out, perScene ? 1 : 0);
 }
 
 // Scene::doOneStep's step counter (core/Scene.cpp:386), advanced only by a step that completed.

@@ -203,6 +203,26 @@ def hertz_drum(n=1_000_000, seed=0, diameter=1.2, length=0.6, div=201, axDiv=50,
     return S
 
 
+def hertz_drum_from_state(centers, radii, vel=None, angVel=None, diameter=1.2, length=0.6, div=201, axDiv=50, density=2500.0,
+                          young=1e8, poisson=0.25, en=0.6, tanPhi=0.5, omega=1.0, verletRel=0.1, precision="fp64"):
+    """The drum of ``hertz_drum`` around given sphere centres and radii (in sphere order), with the
+    given sphere velocities: rebuilds a scene from a stored state (host only, no device work)."""
+    S = _drum_scene(np.asarray(centers, float), np.asarray(radii, float), diameter, length, div, axDiv, density, young, poisson,
+                    en, tanPhi, omega, verletRel, precision)
+    if vel is not None:
+        _sphere_nodes(S, "vel", np.asarray(vel, float))
+    if angVel is not None:
+        _sphere_nodes(S, "angVel", np.asarray(angVel, float))
+    return S
+
+
+def sphere_radii(S):
+    """Radii of the spheres of a scene, in sphere order."""
+    from . import _plan
+    A = _plan.compile_scene(S)
+    return A.particles["radius"][A.particles["shape"] == 0].copy()
+
+
 def _sphere_nodes(S, col, value=None):
     """Read (or write) a node column for the spheres of a scene, in sphere order."""
     from . import _plan
@@ -216,19 +236,21 @@ def _sphere_nodes(S, col, value=None):
 
 def periodic_shear(n=200_000, seed=0, rmin=2e-3, rmax=4e-3, density=2600.0, young=5e7, tanPhi=0.4, ktDivKn=0.2,
                    fill_fraction=0.35, shear_rate=1.0, damping=0.2, verletRel=0.1, precision="fp64", compress_steps=0,
-                   compress_rate=None):
+                   compress_rate=None, centers=None):
     """Periodic simple shear: ``n`` spheres with radii uniform in [rmin, rmax] placed by seeded random
     sequential insertion in a periodic cube sized to solid fraction ``fill_fraction``; IdealElPl
     contacts, Leapfrog damping ``damping``, dt = 0.3*pWaveDt, verletDist = 0.1*rmin,
     Cell.homoDeform = HomoGradV2. With ``compress_steps`` the cell is first compressed isotropically
     (nextGradV = -compress_rate*I, by default the rate that brings the fill to 0.55 in that many
-    steps); then nextGradV is set to the simple shear with xz component ``shear_rate``."""
+    steps); then nextGradV is set to the simple shear with xz component ``shear_rate``. Given
+    ``centers``, those positions are used instead of the random insertion (a state to restore)."""
     from .core import Cell
     rng = np.random.default_rng(seed)
     radii = rng.uniform(rmin, rmax, n)
     vol = float(np.sum((4 / 3.0) * math.pi * radii ** 3))
     side = (vol / fill_fraction) ** (1 / 3.0)
-    centers = pack_rsa(radii, (0, 0, 0), (side, side, side), region=2, seed=seed + 11)
+    if centers is None:
+        centers = pack_rsa(radii, (0, 0, 0), (side, side, side), region=2, seed=seed + 11)
     S = Scene(fields=[DemField(gravity=(0, 0, 0))])
     S.gpu.precision = precision
     S.periodic = True

@@ -72,8 +72,8 @@ class SlotPool:
         nd, pa, mt = A.nodes, A.particles, A.materials
         if np.any(pa["nodes"][:, 0] != np.arange(A.n_particles)) or A.n_nodes != A.n_particles:
             raise ValueError("slot jobs have one node per particle, in particle order")
-        if A.config.get("dyndt") or A.config.get("track_energy"):
-            raise NotImplementedError("DynDt and energy tracking are not supported in serving slots")
+        if A.config.get("track_energy"):
+            raise NotImplementedError("energy tracking is not supported in serving slots")
         p = _native.ptr
         cfg = _native.make_config(_native.wg_config, A.config)
         self.H.check(L.wg_slot_load(h, k, C.cast(C.byref(cfg), C.c_void_p), A.n_particles, p(nd["pos"]), p(nd["ori"]), p(nd["vel"]),
@@ -113,12 +113,27 @@ class SlotPool:
 
 class Job:
     """A scene job: ``build()`` returns the Scene (built when the job is admitted), ``steps`` the
-    number of steps to run; ``n`` its particle count (for admission)."""
+    number of steps to run; ``n`` its particle count (for admission). A periodic job may give
+    ``phases``: a list of (fraction of its steps, Cell.nextGradV) run in turn (e.g. an isotropic
+    compression, then the shear); the steps of the phases add up to ``steps``."""
 
-    def __init__(self, jid, build, n, steps, arrival, periodic=False):
+    def __init__(self, jid, build, n, steps, arrival, periodic=False, phases=None):
         self.id, self.build, self.n, self.steps, self.arrival, self.periodic = jid, build, n, steps, arrival, periodic
+        self.phases = phases
         self.start = self.end = None
         self.result = None
+        self.done_steps = 0
+
+    def phase_steps(self):
+        """(steps, nextGradV or None) of each phase."""
+        if not self.phases:
+            return [(self.steps, None)]
+        out, left = [], self.steps
+        for k, (frac, g) in enumerate(self.phases):
+            n = left if k == len(self.phases) - 1 else min(left, int(round(frac * self.steps)))
+            out.append((n, g))
+            left -= n
+        return out
 
 
 class Server:
@@ -126,16 +141,18 @@ class Server:
     jobs end), periodic jobs as their own simulations in worker threads. ``clock`` is "wall" (job
     arrivals and latencies in seconds of wall time) or "ticks" (arrivals in ticks, deterministic)."""
 
-    def __init__(self, pool, hbm_budget=150e9, tick=500, max_periodic=4, keep_results=False, clock="wall"):
+    def __init__(self, pool, hbm_budget=150e9, tick=500, max_periodic=4, keep_results=False, clock="wall", periodic_chunk=2000):
         self.pool = pool
         self.budget = hbm_budget
         self.tick = tick
         self.max_periodic = max_periodic
         self.keep = keep_results
         self.clock = clock
+        self.periodic_chunk = periodic_chunk
         self.done = []
         self.steps_done = 0
         self.particle_steps = 0.0
+        self.partial_particle_steps = 0.0   # steps done by jobs still unfinished when the run stopped
         self.pool_bytes = float(pool.start[-1]) * BYTES_PER_PARTICLE
 
     def _now(self, t0, ticks):
@@ -143,28 +160,42 @@ class Server:
 
     def run(self, jobs, horizon=None):
         """Serve ``jobs`` (sorted by arrival); returns the finished jobs. Stops when all jobs are
-        done, or at ``horizon`` (seconds or ticks) with the unfinished ones left out."""
+        done, or at ``horizon`` (seconds or ticks) with the unfinished ones left out (the steps
+        they did are counted in ``partial_particle_steps``)."""
         pending = list(jobs)
         queue = []
         periodic_running = []
         lock = threading.Lock()
+        stop = threading.Event()
         t0 = time.perf_counter()
         ticks = 0
         used_periodic_bytes = [0.0]
 
         def run_periodic(job):
-            S = job.build()
             job.start = self._now(t0, ticks)
-            S.run(job.steps)
-            S.sync()
-            if self.keep:
-                job.result = {k: S.dem._nodes.soa.col(k).copy() for k in ("pos", "vel", "angVel", "force", "torque")}
+            S = job.build()
+            for n, g in job.phase_steps():
+                if g is not None:
+                    S.cell.nextGradV = np.asarray(g, dtype=float)
+                while n > 0 and not stop.is_set():
+                    k = min(n, self.periodic_chunk)
+                    S.run(k)
+                    n -= k
+                    job.done_steps += k
+            finished = job.done_steps >= job.steps
+            if finished:
+                S.sync()
+                if self.keep:
+                    job.result = {k: S.dem._nodes.soa.col(k).copy() for k in ("pos", "vel", "angVel", "force", "torque")}
             S.close()
             with lock:
-                job.end = self._now(t0, ticks)
                 used_periodic_bytes[0] -= job.n * BYTES_PER_PARTICLE
-                self.done.append(job)
-                self.particle_steps += job.n * job.steps
+                if finished:
+                    job.end = self._now(t0, ticks)
+                    self.done.append(job)
+                    self.particle_steps += job.n * job.steps
+                else:
+                    self.partial_particle_steps += job.n * job.done_steps
 
         while True:
             now = self._now(t0, ticks)
@@ -200,6 +231,9 @@ class Server:
             if not active and not queue and not pending and not periodic_running:
                 break
             if horizon is not None and now >= horizon:
+                for k in active:
+                    self.partial_particle_steps += self.pool.job[k].n * min(self.pool.status(k)[0], self.pool.job[k].steps)
+                stop.set()
                 break
             if active:
                 # run to the next tick, or to the end of the earliest job if sooner
@@ -228,10 +262,11 @@ class Server:
         return self.done
 
 
-def poisson_jobs(rate, horizon, seed, make_box, make_peri, nmin, nmax, smin, smax, p_periodic=0.5):
+def poisson_jobs(rate, horizon, seed, make_box, make_peri, nmin, nmax, smin, smax, p_periodic=0.5, peri_phases=None):
     """Seeded Poisson stream of jobs over [0, horizon): sizes log-uniform in [nmin, nmax], step counts
     uniform in [smin, smax], periodic with probability p_periodic; ``make_box(n, seed)`` and
-    ``make_peri(n, seed)`` build the scenes."""
+    ``make_peri(n, seed)`` build the scenes; ``peri_phases(n, steps, seed)`` gives the phases of a
+    periodic job (or None)."""
     rng = np.random.default_rng(seed)
     t, jobs, jid = 0.0, [], 0
     while True:
@@ -243,7 +278,8 @@ def poisson_jobs(rate, horizon, seed, make_box, make_peri, nmin, nmax, smin, sma
         peri = bool(rng.random() < p_periodic)
         s = int(rng.integers(0, 2 ** 31))
         build = (lambda n=n, s=s: make_peri(n, s)) if peri else (lambda n=n, s=s: make_box(n, s))
-        jobs.append(Job(jid, build, n + (0 if peri else 6), steps, t, periodic=peri))
+        phases = peri_phases(n, steps, s) if (peri and peri_phases) else None
+        jobs.append(Job(jid, build, n + (0 if peri else 6), steps, t, periodic=peri, phases=phases))
         jid += 1
     return jobs
 

@@ -44,16 +44,21 @@ def _run_ms(sim, steps):
     return tot.value
 
 
-def autotune(sim, trial_steps=64, candidates=DEFAULT_CANDIDATES, rounds=2):
+def autotune(sim, trial_steps=64, candidates=DEFAULT_CANDIDATES, rounds=3, margin=0.02):
     """Time ``trial_steps`` steps of ``sim`` (a Simulation or a Batch) with each candidate launch
     shape, ``rounds`` times in turn (the median counts), set the fastest and return
-    (best, {candidate: ms per step})."""
+    (best, {candidate: ms per step}). The first candidate is the default shape; another one is
+    chosen only if it is faster than the default by more than ``margin`` (a fraction), so that
+    timing noise does not pick a shape that is no better."""
     times = {c: [] for c in candidates}
     for _ in range(rounds):
         for c in candidates:
             set_launch(sim, *c)
             times[c].append(_run_ms(sim, trial_steps) / trial_steps)
     med = {c: float(np.median(v)) for c, v in times.items()}
+    default = candidates[0]
     best = min(med, key=med.get)
+    if med[best] > (1.0 - margin) * med[default]:
+        best = default
     set_launch(sim, *best)
     return best, med
