@@ -349,8 +349,9 @@ def kinetic(S):
 
 def contact_force_error(S64, S32):
     """Per-contact global force of two simulations of the same state after one step: the largest
-    and the median relative difference over the real contacts both have, and the largest
-    difference of a particle's net force relative to its largest contact force."""
+    and the median relative difference over the real contacts both have (those above 1e-6 of the
+    largest force), and the largest difference of a particle's net force relative to its largest
+    contact force."""
     c64, c32 = S64._sim.contacts(), S32._sim.contacts()
     k64 = c64["id_lo"].astype(np.int64) << 32 | c64["id_hi"].astype(np.int64)
     k32 = c32["id_lo"].astype(np.int64) << 32 | c32["id_hi"].astype(np.int64)
@@ -360,7 +361,9 @@ def contact_force_error(S64, S32):
     f64, f32 = c64["fglob"][i64], c32["fglob"][i32]
     mag = np.linalg.norm(f64, axis=1)
     rel = np.linalg.norm(f32 - f64, axis=1) / np.maximum(mag, 1e-300)
-    ok = mag > 0
+    # the contacts carrying a force above 1e-6 of the largest one (the tests' definition: the
+    # relative error of a force ~1e-7 of the others is its FP32 rounding of the overlap, not the force)
+    ok = mag > 1e-6 * (mag.max() if len(mag) else 0.0)
     S64.sync()
     S32.sync()
     F64, F32 = S64.dem._nodes.soa.col("force"), S32.dem._nodes.soa.col("force")
@@ -428,16 +431,17 @@ def measure_c0(args):
 
 def measure_c1(args):
     """Periodic shear: 200 000 spheres (r uniform in [2, 4] mm) placed by seeded random insertion at
-    solid fraction 0.35 in a periodic cube, compressed isotropically to 0.55, then sheared (xz
-    rate 1/s); the same compressed state is run in FP64 plain and FP32-force mode: the one-step
-    contact-force and stress error, then ``c1_steps`` steps of each with the stress tensor and the
-    coordination number at the end."""
+    solid fraction 0.35 in a periodic cube (random insertion jams below the configuration's 0.55),
+    compressed isotropically to 0.55 and on to ``c1_phi`` (a packing with contacts), then sheared
+    (xz rate 1/s); the same compressed state is run in FP64 plain and FP32-force mode: the
+    one-step contact-force and stress error, then ``c1_steps`` steps of each with the stress
+    tensor and the coordination number at the end."""
     from woodem_gb300 import scenes
     from woodem_gb300.dem import ContactLoop
     n, T = args.c1_spheres, args.c1_steps
     t = time.time()
     S = scenes.periodic_shear(n=n, seed=args.seed, fill_fraction=0.35, shear_rate=1.0, precision="fp32",
-                              compress_steps=args.c1_compress)
+                              compress_steps=args.c1_compress, compress_to=args.c1_phi)
     loop = [e for e in S.engines if isinstance(e, ContactLoop)][0]
     loop.evalStress = True
     snap = snapshot(S)
@@ -446,6 +450,7 @@ def measure_c1(args):
     phi = float(np.sum(4 / 3.0 * math.pi * r ** 3)) / side ** 3
     log("c1: %d spheres placed and compressed (%d steps) in %.1fs, solid fraction %.3f" % (n, args.c1_compress, time.time() - t, phi))
     out = {"workload": "periodic-shear-200k", "spheres": n, "steps": T, "compress_steps": args.c1_compress,
+           "compressed_to": args.c1_phi,
            "solid_fraction_start": phi, "cell_side_m": side, "shear": "nextGradV[0,2] = 1/s, HomoGradV2",
            "law": "Law2_L6Geom_FrictPhys_IdealElPl"}
     hbm, _ = peaks()
@@ -525,7 +530,9 @@ def measure_batch(args):
         # autotune on the same state (its trial steps are not part of the timed window)
         reset(prec)
         B = Batch(ss)
-        best, med = tune.autotune(B, trial_steps=args.tune_steps, rounds=args.tune_rounds)
+        # FP64 batch steps are ~6x longer and the shapes differ less: half as many trial steps
+        best, med = tune.autotune(B, trial_steps=args.tune_steps if prec == "fp32" else max(32, args.tune_steps // 2),
+                                  rounds=args.tune_rounds)
         B.H.close()
         B.H = None
         runs = {}
@@ -654,7 +661,7 @@ def measure_serving(args):
     out["capacity_ratio"] = cb["particle_steps_per_s"] / oa["particle_steps_per_s"] if oa["particle_steps_per_s"] else None
     lr, lh = args.serve_low_rate, args.serve_low_seconds
     out["sub_capacity"] = {"arrival_rate_jobs_per_s": lr, "arrivals_seconds": lh}
-    out["sub_capacity"]["continuous_batching"] = continuous(stream(lr, lh, args.seed + 6), lh * 20)
+    out["sub_capacity"]["continuous_batching"] = continuous(stream(lr, lh, args.seed + 6), lh * 4)
     log("serving: sub-capacity, continuous batching: %s" % out["sub_capacity"]["continuous_batching"])
     return out
 
@@ -685,18 +692,20 @@ def main():
     ap.add_argument("--c0-steps", type=int, default=20000)
     ap.add_argument("--c1-spheres", type=int, default=200000)
     ap.add_argument("--c1-steps", type=int, default=5000)
-    ap.add_argument("--c1-compress", type=int, default=20000)
+    ap.add_argument("--c1-compress", type=int, default=30000)
+    ap.add_argument("--c1-phi", type=float, default=0.62, help="solid fraction the periodic cell is compressed to")
     ap.add_argument("--batch-scenes", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=10000)
-    ap.add_argument("--batch-window", type=int, default=2000)
-    ap.add_argument("--tune-steps", type=int, default=64)
-    ap.add_argument("--tune-rounds", type=int, default=3)
+    ap.add_argument("--batch-window", type=int, default=1000)
+    ap.add_argument("--tune-steps", type=int, default=200, help="autotuner: steps per trial (several collider full runs)")
+    ap.add_argument("--tune-rounds", type=int, default=2)
     ap.add_argument("--serve-precision", default="fp32", choices=["fp64", "fp32"])
     ap.add_argument("--serve-rate", type=float, default=20.0, help="serving: job arrivals per second (overload run)")
     ap.add_argument("--serve-seconds", type=float, default=20.0, help="serving: arrivals over this many seconds")
-    ap.add_argument("--serve-wall", type=float, default=45.0, help="serving: seconds each overload run serves")
-    ap.add_argument("--serve-low-rate", type=float, default=0.5, help="serving: sub-capacity arrivals per second")
-    ap.add_argument("--serve-low-seconds", type=float, default=20.0)
+    ap.add_argument("--serve-wall", type=float, default=30.0, help="serving: seconds each overload run serves")
+    ap.add_argument("--serve-low-rate", type=float, default=0.1, help="serving: sub-capacity arrivals per second "
+                    "(the capacity is ~0.2 jobs/s: a mean job is ~1.6e9 particle-steps)")
+    ap.add_argument("--serve-low-seconds", type=float, default=60.0)
     ap.add_argument("--contact-block", type=int, default=0,
                     help="launch shape of the contact kernels (wg_set_launch): 128/256 one contact per thread, "
                          "-256 the resident-grid FP32 sphere-sphere kernel with prefetch")

@@ -634,8 +634,14 @@ struct Scene {
                 BB[i].loIdx = 0;
                 std::sort(BB[i].vec.begin(), BB[i].vec.end(), [](const Bounds& a, const Bounds& b) { return a.lt(b); });
             }
+            // The reference sweeps serially (InsertionSortCollider.cpp:605-632); the sweep only
+            // fills the contact container, and the pairs do not depend on the order in which it
+            // visits the bounds (the deterministic mode re-sorts the container by key after every
+            // collider run), so it is split over the threads here: serially it takes minutes at a
+            // million spheres, where one sort-axis slab holds thousands of boxes.
             VecBounds& V = BB[cfg.sort_axis];
             if (!colliderPeriodic) {
+#pragma omp parallel for schedule(dynamic, 256) num_threads(nThreads)
                 for (long i = 0; i < n2; i++) {
                     if (!(V[i].isMin && V[i].hasBB)) continue;
                     const int iid = V[i].id;
@@ -645,6 +651,8 @@ struct Scene {
                     }
                 }
             } else {
+                bool loop = false;
+#pragma omp parallel for schedule(dynamic, 256) num_threads(nThreads)
                 for (long i = 0; i < n2; i++) {
                     if (!(V[i].isMin && V[i].hasBB)) continue;
                     const int iid = V[i].id;
@@ -652,9 +660,14 @@ struct Scene {
                     for (long j = V.norm(i + 1); V[j].id != iid; j = V.norm(j + 1)) {
                         if (!V[j].isMin) continue;
                         handleBoundInversionPeri(iid, V[j].id, false);
-                        if (cnt++ > 2 * nPar) throw std::logic_error("Uninterrupted loop in the initial sort?");
+                        if (cnt++ > 2 * nPar) {
+#pragma omp atomic write
+                            loop = true;
+                            break;
+                        }
                     }
                 }
+                if (loop) throw std::logic_error("Uninterrupted loop in the initial sort?");
             }
         }
         makeRemoveContactLater_process();

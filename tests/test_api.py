@@ -74,6 +74,8 @@ def test_plan_rejects_unsupported():
     S.engines = utils.defaultEngines(damping=.2)  # the stock engine list (DynDt) in the FP32-force mode
     assert _plan.compile_scene(S).config["dyndt"] == 1
     S.trackEnergy = True
+    assert _plan.compile_scene(S).config["track_energy"] == 1
+    S.engines[0].reset = False
     with pytest.raises(NotImplementedError):
         _plan.compile_scene(S)
     S = scenes.box_settle_small(n=20)

@@ -141,9 +141,8 @@ def test_periodic_gradv_work_balance(oracle_lib):
 def test_refusals():
     from woodem_gb300 import scenes
     S = scenes.box_settle_small(n=50, seed=0, precision="fp32")
-    S.trackEnergy = True
-    with pytest.raises(NotImplementedError, match="energy"):
-        _plan.compile_scene(S)
+    S.trackEnergy = True  # the FP32-force mode tracks energy too
+    assert _plan.compile_scene(S).config["track_energy"] == 1
     from woodem_gb300.batch import Batch
     S = scenes.box_settle_small(n=50, seed=0)
     S.trackEnergy = True

@@ -14,7 +14,7 @@ LIB_PATH = os.path.join(HERE, "libwoogpu.so")
 WG_OK = 0
 WG_ERR_CAPACITY = -5
 ERRORS = {-1: ValueError, -2: RuntimeError, -3: RuntimeError, -4: NotImplementedError, -5: MemoryError, -6: RuntimeError,
-          -7: RuntimeError, -8: TimeoutError}
+          -7: RuntimeError}
 
 
 class wg_config(C.Structure):

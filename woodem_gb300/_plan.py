@@ -89,8 +89,6 @@ def compile_scene(S):
     cfg["time"] = float(S.time)
     cfg["track_energy"] = int(bool(S.trackEnergy))
     cfg["kin_split"] = int(bool(lf.kinSplit))
-    if S.trackEnergy and S.gpu.precision != "fp64":
-        raise NotImplementedError("energy tracking (Scene.trackEnergy) runs in the FP64 precision mode only")
     if dyn is not None:
         if dyn.realPeriod > 0:
             raise NotImplementedError("DynDt.realPeriod (wall-clock activation) is not part of the GPU path")

@@ -42,6 +42,8 @@ void Sim::dfree(void* p) {
 }
 Sim::~Sim() {
     if (stream) cudaStreamSynchronize(stream);
+    // lines this simulation marked persisting would keep their share of L2 after it is gone
+    if (mirBytes && l2Pin) cudaCtxResetPersistingL2Cache();
     collide_free(*this);
     for (void* p : allocs) cudaFree(p);
     allocs.clear();
@@ -603,8 +605,9 @@ int Sim::upload() {
             rsp[q] = make_float2(rh, (float)(posr[q].w - (double)rh));
         }
         dNodeC = (NodeConst32*)dalloc(sizeof(NodeConst32) * nSlots);
-        N.mir = (Mirror*)dalloc(sizeof(Mirror) * nSlots);
-        N.wz = (float*)dalloc(sizeof(float) * nSlots);
+        // the mirror records and wz in one block, so that one L2 access-policy window covers both
+        N.mir = (Mirror*)dalloc(sizeof(Mirror) * nSlots + sizeof(float) * nSlots);
+        N.wz = N.mir ? (float*)(N.mir + nSlots) : nullptr;
         N.orif = (float4*)dalloc(sizeof(float4) * nSlots);
         N.rsplit = (float2*)dalloc(sizeof(float2) * nSlots);
         N.lh = (float4*)dalloc(sizeof(float4) * nSlots);
@@ -639,6 +642,9 @@ int Sim::upload() {
         WG_CUDA_TRY(cudaMemcpyAsync(N.lh, hph.data(), sizeof(float4) * nSlots, cudaMemcpyHostToDevice, S.stream));
         WG_CUDA_TRY(cudaMemcpyAsync(N.ll, hpl.data(), sizeof(float4) * nSlots, cudaMemcpyHostToDevice, S.stream));
         WG_CUDA_TRY(cudaMemcpyAsync(dNodeC, nc.data(), sizeof(NodeConst32) * nSlots, cudaMemcpyHostToDevice, S.stream));
+        mirBytes = (sizeof(Mirror) + sizeof(float)) * (size_t)nSlots;
+        int r = applyL2Window();
+        if (r) return r;
     }
     launch_facet_prep(stream, N, P, nullptr);
     long long st0 = cfg.step;
@@ -851,6 +857,45 @@ int Sim::runDynDtScenes(const std::vector<char>& due, long long deviceStep) {
     return 0;
 }
 
+// FP32-force mode: the double-float mirror records (and wz), which every contact gathers for both
+// of its particles, are kept in L2 with a persisting access-policy window on the simulation's
+// stream (launch flag WG_LAUNCH_NO_L2_PIN turns it off); the window is sized to the device's
+// persisting-L2 limit for this context, which the first simulation that needs it raises.
+int Sim::applyL2Window() {
+    Sim& S = *this;
+    if (!N.mir || !stream) return 0;
+    int maxPersist = 0, maxWin = 0;
+    if (cudaDeviceGetAttribute(&maxPersist, cudaDevAttrMaxPersistingL2CacheSize, device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&maxWin, cudaDevAttrMaxAccessPolicyWindowSize, device) != cudaSuccess || maxPersist <= 0 ||
+        maxWin <= 0) {
+        cudaGetLastError();
+        return 0;  // no persisting L2 on this device: nothing to do
+    }
+    cudaStreamAttrValue a{};
+    if (l2Pin) {
+        size_t lim = 0;
+        WG_CUDA_TRY(cudaDeviceGetLimit(&lim, cudaLimitPersistingL2CacheSize));
+        const size_t want = std::min<size_t>(mirBytes, (size_t)maxPersist);
+        if (lim < want) WG_CUDA_TRY(cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, want));
+        WG_CUDA_TRY(cudaDeviceGetLimit(&lim, cudaLimitPersistingL2CacheSize));
+        const size_t win = std::min<size_t>(mirBytes, (size_t)maxWin);
+        a.accessPolicyWindow.base_ptr = (void*)N.mir;
+        a.accessPolicyWindow.num_bytes = win;
+        a.accessPolicyWindow.hitRatio = win > 0 ? (float)std::min(1.0, (double)lim / (double)win) : 0.f;
+        a.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+        a.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+    } else {
+        a.accessPolicyWindow.base_ptr = nullptr;
+        a.accessPolicyWindow.num_bytes = 0;
+        a.accessPolicyWindow.hitRatio = 0.f;
+        a.accessPolicyWindow.hitProp = cudaAccessPropertyNormal;
+        a.accessPolicyWindow.missProp = cudaAccessPropertyNormal;
+    }
+    WG_CUDA_TRY(cudaStreamSetAttribute(stream, cudaStreamAttributeAccessPolicyWindow, &a));
+    if (side.st) WG_CUDA_TRY(cudaStreamSetAttribute(side.st, cudaStreamAttributeAccessPolicyWindow, &a));
+    return 0;
+}
+
 int Sim::applyDt(double ndt) {
     Sim& S = *this;
     cfg.dt = ndt;
@@ -959,7 +1004,13 @@ int Sim::run(int64_t n) {
             else launch_forces(stream, N, P, I, sp, dFlags, true);
             launches += I.nHeavyFree > 0;
         }
-        if (fp32) launch_leapfrog32(stream, N, P, I, dNodeC, sp, dFlags, fromEndsArg, dStep, cfg.periodic != 0);
+        if (fp32 && trackE) {
+            cudaMemsetAsync(eNode.col, 0, sizeof(double) * EN_NODE_NCOL * eNode.cap, stream);
+            launch_leapfrog32(stream, N, P, I, dNodeC, sp, dFlags, fromEndsArg, dStep, cfg.periodic != 0, &eNode);
+            launch_energy_sum(stream, eNode, 0, N.n, dEPartial, dEnergy, dECreated, dFlags, cfg.kin_split != 0);
+            launches += 2;
+        } else if (fp32)
+            launch_leapfrog32(stream, N, P, I, dNodeC, sp, dFlags, fromEndsArg, dStep, cfg.periodic != 0);
         else if (trackE) {
             cudaMemsetAsync(eNode.col, 0, sizeof(double) * EN_NODE_NCOL * eNode.cap, stream);
             launch_leapfrog(stream, N, P, I, sp, dFlags, fromEndsArg, dStep, cfg.periodic != 0, &eNode);
@@ -971,7 +1022,20 @@ int Sim::run(int64_t n) {
     };
     auto stepContact = [&](ScenePar* sp) {
         bool advanced = false;  // the last contact kernel advanced the step counter itself
-        if (fp32)
+        if (fp32 && trackE) {
+            // the energy sums after the contact kernels read the step counter those advance: they
+            // run with the step advance at the end instead
+            cudaMemsetAsync(eCon.col, 0, sizeof(double) * EN_CON_NCOL * eCon.cap, stream);
+            launch_contact_fp32(stream, SideStream{}, N, P, C, I, K, dMats, sp, dStep, dFlags, nMixed, cfg.periodic != 0, anyLaw0,
+                                !facetsStatic, 128, &eCon);
+            launch_energy_sum(stream, eCon, 1, I.nAct, dEPartial, dEnergy, dECreated, dFlags, false);
+            launches += 2;
+            if (cfg.periodic && cfg.eval_stress) {
+                launch_stress(stream, N, P, C, I, sp, dStress + 9, stressCap - 9, dStress);
+                launch_energy_gradv(stream, dStress, sp, dEPrev, dEnergy, dECreated, dFlags);
+                launches += 3;
+            }
+        } else if (fp32)
             advanced = launch_contact_fp32(stream, concurrentContacts ? side : SideStream{}, N, P, C, I, K, dMats, sp, dStep, dFlags,
                                            nMixed, cfg.periodic != 0, anyLaw0, !facetsStatic, contactBlock != 0 ? contactBlock : -256);
         else if (trackE) {
@@ -1301,8 +1365,6 @@ int wg_set_config(wg_scene* s, const wg_config* c) {
     Sim& S = *SIM(s);
     if (S.uploaded) return S.fail(WG_ERR_STATE, "configuration is fixed once the scene runs; create a new scene");
     if (!(c->dt > 0) || !std::isfinite(c->dt)) return S.fail(WG_ERR_ARG, "Scene.dt must be positive and finite");
-    if (c->track_energy && c->precision != WG_PREC_FP64)
-        return S.fail(WG_ERR_UNSUPPORTED, "energy tracking runs in the FP64 precision mode only");
     if (c->dyndt && !(c->dyndt_max_rel_inc > 0 && 1. + c->dyndt_max_rel_inc != 1.))
         return S.fail(WG_ERR_ARG, "DynDt: maxRelInc too small (1.0+maxRelInc==1.0)");  // DynDt::postLoad, DynDt.cpp:12-14
     S.cfg = *c;
@@ -1598,9 +1660,22 @@ int wg_set_launch(wg_scene* s, int32_t contact_block, int32_t chunk_steps, int32
     if (chunk_steps < 1 || chunk_steps > 1024) return S.fail(WG_ERR_ARG, "chunk_steps must be in [1, 1024]");
     S.contactBlock = contact_block;
     S.chunkSteps = chunk_steps;
-    if (launch_flags & ~(WG_LAUNCH_GRAPH | WG_LAUNCH_SERIAL)) return S.fail(WG_ERR_ARG, "unknown launch flag");
+    if (launch_flags & ~(WG_LAUNCH_GRAPH | WG_LAUNCH_SERIAL | WG_LAUNCH_NO_L2_PIN)) return S.fail(WG_ERR_ARG, "unknown launch flag");
     S.useGraph = (launch_flags & WG_LAUNCH_GRAPH) != 0;
     S.concurrentContacts = (launch_flags & WG_LAUNCH_SERIAL) == 0;
+    const bool pin = (launch_flags & WG_LAUNCH_NO_L2_PIN) == 0;
+    if (pin != S.l2Pin) {
+        S.l2Pin = pin;
+        if (S.uploaded) {
+            WG_CUDA_TRY(cudaSetDevice(S.device));
+            int r = S.applyL2Window();
+            if (r) return r;
+            if (S.graphExec) {  // captured kernels keep the window they were captured with
+                cudaGraphExecDestroy(S.graphExec);
+                S.graphExec = nullptr;
+            }
+        }
+    }
     return WG_OK;
 }
 

@@ -260,7 +260,8 @@ int launch_stress(cudaStream_t st, const DevNodes& N, const DevParticles& P, con
                   const ScenePar* sp, double* scratch, int64_t scratchDoubles, double* out);
 // FP32-force mode (wg_step32.cu)
 void launch_leapfrog32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const NodeConst32* nc,
-                       const ScenePar* sp, int* dFlags, int fromEnds, const long long* dStep, bool periodic);
+                       const ScenePar* sp, int* dFlags, int fromEnds, const long long* dStep, bool periodic,
+                       const EnergyCols* energy = nullptr);
 // The kernels walk the active contacts I.work[0, I.nAct). Items [0, nMixed) are facet and wall
 // contacts; [nMixed, I.nAct) join two spheres and, in an aperiodic scene, go to a
 // sphere-sphere-only kernel.
@@ -273,7 +274,7 @@ struct SideStream {
 bool launch_contact_fp32(cudaStream_t st, const SideStream& side, const DevNodes& N, const DevParticles& P, const DevContacts& C,
                          const DevIncidence& I, const DevPackedSS& K, const double4_32a* mats, const ScenePar* sp,
                          long long* dStep, int* dFlags, int64_t nMixed, bool periodic, bool anyLaw0, bool prepFacets,
-                         int block = 256);
+                         int block = 256, const EnergyCols* energy = nullptr);
 // copy the packed sphere-sphere state from (pack) / back to (unpack) the contact arrays
 void launch_pack_ss(cudaStream_t st, const DevContacts& C, const DevIncidence& I, const DevParticles& P, const DevPackedSS& K,
                     int64_t nMixed);
@@ -390,6 +391,9 @@ struct Sim {
     bool useGraph = false;
     bool concurrentContacts = true;   // facet/wall contacts beside, not before, the sphere-sphere ones
     bool facetsStatic = false;        // every facet vertex is fully blocked and at rest: FacetPrep is made once
+    bool l2Pin = true;                // keep the FP32-force mirror records in L2 (persisting window)
+    size_t mirBytes = 0;
+    int applyL2Window();
     cudaGraphExec_t graphExec = nullptr;
     int64_t graphSteps = 0;  // steps in the captured chunk, 0: none valid
     int64_t graphEpoch = -1; // nFullRuns when it was captured

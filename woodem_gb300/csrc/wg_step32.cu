@@ -13,6 +13,7 @@
 #include <mutex>
 
 #include "wg_ends.cuh"
+#include "wg_energy.cuh"
 #include "wg_geom.cuh"
 
 namespace wg {
@@ -122,10 +123,12 @@ __device__ __noinline__ void resetNodeForce(DevNodes N, int i, float mh, float m
 
 // PERI: the scene is periodic (homothetic corrections of Leapfrog.cpp:103-255 with the cell's
 // velocity gradient); the aperiodic instantiation carries none of that FP64 code.
-template <bool PERI>
+// ENERGY: Scene.trackEnergy; each node writes its step's energy terms (Leapfrog.cpp:52-97, in FP64
+// from this step's force and torque) into E, as the FP64 Leapfrog does.
+template <bool PERI, bool ENERGY>
 __global__ void __launch_bounds__(256, 4) k_leapfrog32(DevNodes N, DevParticles P, DevIncidence I, const NodeConst32* __restrict__ ncs,
                                                     const ScenePar* __restrict__ spp, int* __restrict__ dFlags, int fromEnds,
-                                                    const long long* __restrict__ dStepC) {
+                                                    const long long* __restrict__ dStepC, EnergyCols E) {
     __shared__ EndStage<float4, float2, kLeapfrogChunk32> stage[8];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < N.n;
@@ -186,7 +189,24 @@ __global__ void __launch_bounds__(256, 4) k_leapfrog32(DevNodes N, DevParticles 
     D3 angVel = ld3(w4);
     const bool blockedAll = (flags & F_DOF_ALL) == F_DOF_ALL;
     const int homoDeform = PERI ? sp.homoDeform : -1;
-    F3 la{0.f, 0.f, 0.f};
+    F3 la{0.f, 0.f, 0.f}, aaE{0.f, 0.f, 0.f};
+    D3 pvfE = vel, pvaE = angVel;
+    if constexpr (ENERGY) {
+        if (sp.trackEnergy) {
+            const D3 fd{(double)f.x, (double)f.y, (double)f.z}, td{(double)t.x, (double)t.y, (double)t.z};
+            const double mass = (double)nc.mh + (double)nc.ml;
+            if (damp && !(flags & F_ENERGY_SKIP)) E.col[EN_NODE_DAMP * E.cap + i] = energyDamp(vel, fd, angVel, td, sp.damping, dt);
+            if (sp.hasGravity && !(flags & F_GRAVITY_SKIP)) {
+                E.col[EN_NODE_GRAV * E.cap + i] = energyGrav(D3{sp.g[0], sp.g[1], sp.g[2]}, vel, mass, dt, flags);
+                E.col[EN_NODE_NGRAV * E.cap + i] = 1.;
+            }
+            if (PERI) {
+                if (homoDeform == 2 || homoDeform == 3) pvfE = vel - mul(*(const DM3*)sp.gradV, pos);
+                else if (homoDeform == 4) pvfE = vel - mul(*(const DM3*)sp.gradV, pos - (dt / 2) * vel);
+                if (homoDeform == 4) pvaE = angVel - D3{sp.spinVec[0], sp.spinVec[1], sp.spinVec[2]};
+            }
+        }
+    }
     if (!blockedAll) {
         la = F3{(flags & 1u) ? 0.f : f.x * nc.invMass, (flags & 2u) ? 0.f : f.y * nc.invMass, (flags & 4u) ? 0.f : f.z * nc.invMass};
         F3 pvf{0.f, 0.f, 0.f}, pva{0.f, 0.f, 0.f};
@@ -219,6 +239,7 @@ __global__ void __launch_bounds__(256, 4) k_leapfrog32(DevNodes N, DevParticles 
                 aa.z *= 1.f - d * fsgn(t.z * (pva.z + 0.5f * dtf * aa.z));
             }
             angVel = angVel + D3{f2d(dtf * aa.x), f2d(dtf * aa.y), f2d(dtf * aa.z)};
+            if constexpr (ENERGY) aaE = aa;
             if (PERI && homoDeform == 4) angVel = angVel - D3{sp.deltaSpinVec[0], sp.deltaSpinVec[1], sp.deltaSpinVec[2]};
         }
     } else {
@@ -231,6 +252,20 @@ __global__ void __launch_bounds__(256, 4) k_leapfrog32(DevNodes N, DevParticles 
             vel = vel + mul(*(const DM3*)sp.dGradV, pos);
         } else if (homoDeform == 1) {
             pos = pos + mul(*(const DM3*)sp.nextGradV, pos) * dt;
+        }
+    }
+    if constexpr (ENERGY) {
+        if (sp.trackEnergy && !(flags & F_ENERGY_SKIP)) {
+            const double4_32a mi = N.minert[i];
+            const double2 ek = energyKin(pvfE, pvaE, D3{(double)la.x, (double)la.y, (double)la.z},
+                                         D3{(double)aaE.x, (double)aaE.y, (double)aaE.z}, (double)nc.mh + (double)nc.ml,
+                                         D3{mi.x, mi.y, mi.z}, dt);
+            if (sp.kinSplit) {
+                E.col[EN_NODE_K0 * E.cap + i] = ek.x;
+                E.col[EN_NODE_K1 * E.cap + i] = ek.y;
+            } else
+                E.col[EN_NODE_K0 * E.cap + i] = ek.x + ek.y;
+            E.col[EN_NODE_NKIN * E.cap + i] = 1.;
         }
     }
     pos = pos + vel * dt;
@@ -278,10 +313,17 @@ __global__ void __launch_bounds__(256, 4) k_leapfrog32(DevNodes N, DevParticles 
 }
 
 void launch_leapfrog32(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevIncidence& I, const NodeConst32* nc,
-                       const ScenePar* sp, int* dFlags, int fromEnds, const long long* dStep, bool periodic) {
+                       const ScenePar* sp, int* dFlags, int fromEnds, const long long* dStep, bool periodic, const EnergyCols* energy) {
     if (N.n == 0) return;
-    if (periodic) k_leapfrog32<true><<<(N.n + 255) / 256, 256, 0, st>>>(N, P, I, nc, sp, dFlags, fromEnds, dStep);
-    else k_leapfrog32<false><<<(N.n + 255) / 256, 256, 0, st>>>(N, P, I, nc, sp, dFlags, fromEnds, dStep);
+    const unsigned g = (N.n + 255) / 256;
+    const EnergyCols E = energy ? *energy : EnergyCols{};
+    if (energy) {
+        if (periodic) k_leapfrog32<true, true><<<g, 256, 0, st>>>(N, P, I, nc, sp, dFlags, fromEnds, dStep, E);
+        else k_leapfrog32<false, true><<<g, 256, 0, st>>>(N, P, I, nc, sp, dFlags, fromEnds, dStep, E);
+    } else {
+        if (periodic) k_leapfrog32<true, false><<<g, 256, 0, st>>>(N, P, I, nc, sp, dFlags, fromEnds, dStep, E);
+        else k_leapfrog32<false, false><<<g, 256, 0, st>>>(N, P, I, nc, sp, dFlags, fromEnds, dStep, E);
+    }
 }
 
 // ---------------------------------------------------------------------------------- ContactLoop
@@ -446,6 +488,50 @@ __device__ __forceinline__ void physCreate(const ScenePar* __restrict__ spp, int
     ph3 = q.p3;
 }
 
+// Energies of one contact in one step (Scene.trackEnergy: EnergyTracker adds of IdealElPl.cpp:25-37,
+// 58-90 and Hertz.cpp:154-179), in FP64 from the FP32 quantities of the law, written to the contact's
+// entry of the per-step energy columns (zeroed before the step) as the FP64 contact kernel does.
+struct EnergyTerms {
+    double elast = 0, plast = 0, broken = 0, viscN = 0, viscT = 0, nElast = 0, nBroken = 0;
+    // IdealElPl: the elastic potential of a contact that breaks (noSlip), lost
+    __device__ __noinline__ void brokenElPl(float kn, float kt, float uN, double b1, double b2) {
+        const double bf = (double)kn * (double)uN;
+        broken = .5 * ((bf * bf) / (double)kn + (b1 * b1 + b2 * b2) / (double)kt);
+        nBroken = 1;
+    }
+    // IdealElPl: dissipation of the Coulomb slip, from the trial shear force (squared norm q)
+    __device__ __noinline__ void plastElPl(float kt, double maxFt, double q) {
+        plast = kt != 0.f ? (maxFt * (sqrt(q) - maxFt)) / (double)kt : 0.;
+    }
+    __device__ __noinline__ void elastElPl(float kn, float kt, float fn, float ft1, float ft2) {
+        const double n = fn, a = ft1, b = ft2;
+        elast = 0.5 * ((n * n) / (double)kn + (kt != 0.f ? (a * a + b * b) / (double)kt : 0.));
+        if (isnan(elast)) elast = 0.;
+        nElast = 1;
+    }
+    // Hertz: slip dissipation from the trial shear force (squared norm q), tangent stiffness kt
+    __device__ __noinline__ void plastHertz(float q, float maxFt, float kt) {
+        const double fN = sqrt((double)q), m = maxFt;
+        plast = ((.5 * (fN - m) + m) * (fN - m)) / (double)kt;
+    }
+    // Hertz: kn0 (2/5) (-uN)^(5/2) + |Ft|^2 / (2 kt), su = sqrt(-uN)
+    __device__ __noinline__ void elastHertz(float kn0, float su, float ft1, float ft2, float kt) {
+        const double s = su, a = ft1, b = ft2;
+        elast = ((double)kn0 * (2 / 5.)) * ((((s * s) * s) * s) * s) + (0.5 * (a * a + b * b)) / (double)kt;
+        nElast = 1;
+    }
+    __device__ __forceinline__ void store(const EnergyCols& E, int64_t rk) const {
+        const int64_t cp = E.cap;
+        E.col[EN_CON_ELAST * cp + rk] = elast;
+        E.col[EN_CON_PLAST * cp + rk] = plast;
+        E.col[EN_CON_BROKEN * cp + rk] = broken;
+        E.col[EN_CON_VISCN * cp + rk] = viscN;
+        E.col[EN_CON_VISCT * cp + rk] = viscT;
+        E.col[EN_CON_NELAST * cp + rk] = nElast;
+        E.col[EN_CON_NBROKEN * cp + rk] = nBroken;
+    }
+};
+
 // The values one sphere-sphere contact is evaluated from: its packed item, flags, state and the
 // two particles' mirror records.
 struct SSIn {
@@ -478,9 +564,11 @@ __device__ __forceinline__ void stepTicket(int* dFlags, long long* dStep, int to
 // One sphere-sphere contact of an aperiodic scene (packed position j): Cg2_Sphere_Sphere_L6Geom,
 // Cp2 on creation, Law2, the two end slots and the packed state. FP32 arithmetic throughout
 // except the IdealElPl shear accumulation (FP64) and contact creation.
+template <bool ENERGY>
 __device__ __forceinline__ void ssContact(const SSIn& x, int64_t j, const DevNodes& N, const DevParticles& P, const DevContacts& C,
                                           const DevIncidence& I, const DevPackedSS& K, const double4_32a* __restrict__ mats,
-                                          const ScenePar* __restrict__ spp, long long stepAbs, int* dFlags, int64_t nm) {
+                                          const ScenePar* __restrict__ spp, long long stepAbs, int* dFlags, int64_t nm,
+                                          const EnergyCols& E) {
     const int4 it = x.it;
     const uint32_t pf = x.pf;
     const float* st = x.st;
@@ -544,10 +632,14 @@ __device__ __forceinline__ void ssContact(const SSIn& x, int64_t j, const DevNod
     }
     float fn, ft1 = 0.f, ft2 = 0.f;
     bool keep = true;
+    EnergyTerms en;
     if (sp.law == 0) {
         // Law2_L6Geom_FrictPhys_IdealElPl (IdealElPl.cpp:18-81), shear force accumulated in FP64
-        if (uN > 0 && !sp.noBreak) keep = false;
-        else {
+        if (uN > 0 && !sp.noBreak) {
+            keep = false;
+            if constexpr (ENERGY)
+                if (sp.noSlip) en.brokenElPl(ph0, ph1, uN, ft1o + (double)(dtf * ph1 * lvel.y), ft2o + (double)(dtf * ph1 * lvel.z));
+        } else {
             fn = ph0 * uN;
             if (sp.noFrict || ph2 == 0.f) {
                 K.ft[0][j] = 0.;
@@ -559,6 +651,7 @@ __device__ __forceinline__ void ssContact(const SSIn& x, int64_t j, const DevNod
                 const double maxFt = (double)(fabsf(fn) * ph2);
                 const double q = t1 * t1 + t2 * t2;
                 if (q > maxFt * maxFt && !sp.noSlip) {
+                    if constexpr (ENERGY) en.plastElPl(ph1, maxFt, q);
                     const double ratio = (q > 0) ? maxFt * rsqrt(q) : 0.;
                     t1 *= ratio;
                     t2 *= ratio;
@@ -569,6 +662,7 @@ __device__ __forceinline__ void ssContact(const SSIn& x, int64_t j, const DevNod
                 ft2 = (float)t2;
                 if (isnan(fn) || isnan(t1) || isnan(t2)) atomicCAS(dErr, 0, 101);
             }
+            if constexpr (ENERGY) en.elastElPl(ph0, ph1, fn, ft1, ft2);
         }
     } else {
         // Law2_L6Geom_HertzPhys_DMT, DMT branch (Hertz.cpp:58-87,143-172)
@@ -580,21 +674,27 @@ __device__ __forceinline__ void ssContact(const SSIn& x, int64_t j, const DevNod
             float Fnv = eta * lvel.x;
             if (sp.noAttraction && Fne + Fnv > 0.f) Fnv = -Fne;
             fn = Fne + Fnv;  // the adhesion term 4 pi R gamma is zero (gamma = 0 is required in this mode)
+            if constexpr (ENERGY) en.viscN = ((double)Fnv * (double)lvel.x) * (double)dtf;
             const float kt = ph1 * su;
             ft1 = dtf * kt * lvel.y;
             ft2 = dtf * kt * lvel.z;
             const float maxFt = fmaxf(0.f, fn) * ph2;
             const float q = ft1 * ft1 + ft2 * ft2;
             if (q > maxFt * maxFt) {
+                if constexpr (ENERGY) en.plastHertz(q, maxFt, kt);
                 const float ratio = maxFt * rsqrtf(q);
                 ft1 *= ratio;
                 ft2 *= ratio;
             } else {
                 ft1 += eta * lvel.y;
                 ft2 += eta * lvel.z;
+                if constexpr (ENERGY) en.viscT = ((double)eta * ((double)lvel.y * lvel.y + (double)lvel.z * lvel.z)) * (double)dtf;
             }
+            if constexpr (ENERGY)
+                if (uN < 0.f) en.elastHertz(ph0, su, ft1, ft2, kt);
         }
     }
+    if constexpr (ENERGY) en.store(E, nm + j);
     if (!keep) {
         K.flags[j] = ((fl & ~C_REAL) | C_PENDING) | hiBits;
         if (real) {
@@ -626,11 +726,11 @@ __device__ __forceinline__ void ssContact(const SSIn& x, int64_t j, const DevNod
 // flags and state are read at the contact's position in the work list (coalesced), the two
 // particles' mirror records are gathered; every load is issued before the step guard and the
 // branches, so a contact waits for two memory round trips.
-template <int MINB>
+template <int MINB, bool ENERGY>
 __global__ void __launch_bounds__(256, MINB) k_contact_ss32(DevNodes N, DevParticles P, DevContacts C, DevIncidence I, DevPackedSS K,
                                                             const double4_32a* __restrict__ mats, const ScenePar* __restrict__ spp,
                                                             const long long* __restrict__ dStep, int* __restrict__ dFlags, int64_t nm,
-                                                            int haltBlock, int loadFt) {
+                                                            int haltBlock, int loadFt, EnergyCols E) {
     const int64_t j0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool in = j0 < K.n;
     const int64_t j = in ? j0 : 0;
@@ -655,7 +755,7 @@ __global__ void __launch_bounds__(256, MINB) k_contact_ss32(DevNodes N, DevParti
         return;
     }
     if (!in) return;
-    ssContact(x, j, N, P, C, I, K, mats, spp, stepAbs, dFlags, nm);
+    ssContact<ENERGY>(x, j, N, P, C, I, K, mats, spp, stepAbs, dFlags, nm, E);
 }
 
 // The same contacts through a resident grid whose warps take chunks of kSSChunk consecutive
@@ -666,11 +766,11 @@ __global__ void __launch_bounds__(256, MINB) k_contact_ss32(DevNodes N, DevParti
 // state and mirror records are in flight, so each contact waits for one memory round trip; the
 // persistent state of a contact that is not real (pending, or not touching) is not loaded.
 constexpr int kSSChunk = 256;
-template <int MINB>
+template <int MINB, bool ENERGY>
 __global__ void __launch_bounds__(256, MINB) k_contact_ss32p(DevNodes N, DevParticles P, DevContacts C, DevIncidence I, DevPackedSS K,
                                                              const double4_32a* __restrict__ mats, const ScenePar* __restrict__ spp,
                                                              long long* __restrict__ dStep, int* __restrict__ dFlags, int64_t nm,
-                                                             int haltBlock, int loadFt, int ticketTotal) {
+                                                             int haltBlock, int loadFt, int ticketTotal, EnergyCols E) {
     const long long stepAbs = *dStep;
     if (dFlags[FL_FULL] || halted(dFlags)) {  // the same for every thread of the grid
         if (haltBlock && blockIdx.x == 0 && threadIdx.x == 0) dFlags[FL_HALT] = 1;
@@ -727,7 +827,7 @@ __global__ void __launch_bounds__(256, MINB) k_contact_ss32p(DevNodes N, DevPart
             x.mb = N.mir[x.it.y];
             x.wza = N.wz[x.it.x];
             x.wzb = N.wz[x.it.y];
-            ssContact(x, j, N, P, C, I, K, mats, spp, stepAbs, dFlags, nm);
+            ssContact<ENERGY>(x, j, N, P, C, I, K, mats, spp, stepAbs, dFlags, nm, E);
         }
         if (cn != cur) {
             cur = cn;
@@ -892,10 +992,11 @@ __device__ __forceinline__ bool geomFS32(const DevNodes& N, const DevParticles& 
 
 // Work items [c0, c1): facet and wall contacts, and every contact of a periodic scene (cell shifts,
 // FP64 geometry of the shifted pairs); the state is read and written in the contact arrays.
-template <bool PERI>
+template <bool PERI, bool ENERGY>
 __device__ __forceinline__ void mixedContact(int64_t rk, const DevNodes& N, const DevParticles& P, const DevContacts& C,
                                              const DevIncidence& I, const double4_32a* __restrict__ mats,
-                                             const ScenePar* __restrict__ spp, const long long* __restrict__ dStep, int* dFlags) {
+                                             const ScenePar* __restrict__ spp, const long long* __restrict__ dStep, int* dFlags,
+                                             const EnergyCols& E) {
     int* dErr = dFlags + FL_ERR;
     // work item: contact index, pA, pB and the static flag bits (type, swap) fixed at the full run
     const int4 wk = I.work[rk];
@@ -1033,10 +1134,16 @@ __device__ __forceinline__ void mixedContact(int64_t rk, const DevNodes& N, cons
     }
     float fn, ft1 = 0.f, ft2 = 0.f;
     bool keep = true;
+    EnergyTerms en;
     if (sp.law == 0) {
         // Law2_L6Geom_FrictPhys_IdealElPl (IdealElPl.cpp:18-81), shear force accumulated in FP64
-        if (uN > 0 && !sp.noBreak) keep = false;
-        else {
+        if (uN > 0 && !sp.noBreak) {
+            keep = false;
+            if constexpr (ENERGY)
+                if (sp.noSlip)
+                    en.brokenElPl(ph0, ph1, uN, (real ? C.col[CC_FT1][c] : 0.) + (double)(dtf * ph1 * lvel.y),
+                                  (real ? C.col[CC_FT2][c] : 0.) + (double)(dtf * ph1 * lvel.z));
+        } else {
             fn = ph0 * uN;
             if (sp.noFrict || ph2 == 0.f) {
                 if (real) { C.col[CC_FT1][c] = 0.; C.col[CC_FT2][c] = 0.; }
@@ -1047,6 +1154,7 @@ __device__ __forceinline__ void mixedContact(int64_t rk, const DevNodes& N, cons
                 const double maxFt = (double)(fabsf(fn) * ph2);
                 const double q = t1 * t1 + t2 * t2;
                 if (q > maxFt * maxFt && !sp.noSlip) {
+                    if constexpr (ENERGY) en.plastElPl(ph1, maxFt, q);
                     const double ratio = (q > 0) ? maxFt * rsqrt(q) : 0.;
                     t1 *= ratio;
                     t2 *= ratio;
@@ -1057,6 +1165,7 @@ __device__ __forceinline__ void mixedContact(int64_t rk, const DevNodes& N, cons
                 ft2 = (float)t2;
                 if (isnan(fn) || isnan(t1) || isnan(t2)) atomicCAS(dErr, 0, 101);
             }
+            if constexpr (ENERGY) en.elastElPl(ph0, ph1, fn, ft1, ft2);
         }
     } else {
         // Law2_L6Geom_HertzPhys_DMT, DMT branch (Hertz.cpp:58-87,143-172)
@@ -1068,21 +1177,27 @@ __device__ __forceinline__ void mixedContact(int64_t rk, const DevNodes& N, cons
             float Fnv = eta * lvel.x;
             if (sp.noAttraction && Fne + Fnv > 0.f) Fnv = -Fne;
             fn = Fne + Fnv;  // the adhesion term 4 pi R gamma is zero (gamma = 0 is required in this mode)
+            if constexpr (ENERGY) en.viscN = ((double)Fnv * (double)lvel.x) * (double)dtf;
             const float kt = ph1 * su;
             ft1 = dtf * kt * lvel.y;
             ft2 = dtf * kt * lvel.z;
             const float maxFt = fmaxf(0.f, fn) * ph2;
             const float q = ft1 * ft1 + ft2 * ft2;
             if (q > maxFt * maxFt) {
+                if constexpr (ENERGY) en.plastHertz(q, maxFt, kt);
                 const float ratio = maxFt * rsqrtf(q);
                 ft1 *= ratio;
                 ft2 *= ratio;
             } else {
                 ft1 += eta * lvel.y;
                 ft2 += eta * lvel.z;
+                if constexpr (ENERGY) en.viscT = ((double)eta * ((double)lvel.y * lvel.y + (double)lvel.z * lvel.z)) * (double)dtf;
             }
+            if constexpr (ENERGY)
+                if (uN < 0.f) en.elastHertz(ph0, su, ft1, ft2, kt);
         }
     }
+    if constexpr (ENERGY) en.store(E, rk);
     const bool aIsLo = !(fl & C_SWAP);
     if (!keep) {
         C.flags[c] = (fl & ~C_REAL) | C_PENDING;
@@ -1119,18 +1234,18 @@ __device__ __forceinline__ void mixedContact(int64_t rk, const DevNodes& N, cons
 
 // One thread per work item of [c0, c1), looping over the range with the grid's stride (the
 // launch sizes the grid so that its blocks leave room for the sphere-sphere kernel beside it).
-template <bool PERI>
+template <bool PERI, bool ENERGY>
 __global__ void __launch_bounds__(128, 4) k_contact_fp32(DevNodes N, DevParticles P, DevContacts C, DevIncidence I,
                                                        const double4_32a* __restrict__ mats, const ScenePar* __restrict__ spp,
                                                        long long* __restrict__ dStep, int* __restrict__ dFlags, int64_t c0,
-                                                       int64_t c1, int haltBlock, int ticketTotal) {
+                                                       int64_t c1, int haltBlock, int ticketTotal, EnergyCols E) {
     if (dFlags[FL_FULL] || halted(dFlags)) {  // the same for every thread of the grid
         if (haltBlock && blockIdx.x == 0 && threadIdx.x == 0) dFlags[FL_HALT] = 1;
         return;
     }
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t rk = c0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; rk < c1; rk += stride)
-        mixedContact<PERI>(rk, N, P, C, I, mats, spp, dStep, dFlags);
+        mixedContact<PERI, ENERGY>(rk, N, P, C, I, mats, spp, dStep, dFlags, E);
     stepTicket(dFlags, dStep, ticketTotal);
 }
 
@@ -1155,41 +1270,42 @@ static int smCount() {
 static int ssGrid(const DevPackedSS& K, int block, int blocksPerSM) {
     return block < 0 ? (int)std::min<int64_t>((K.n + 255) / 256, (int64_t)blocksPerSM * smCount()) : 0;
 }
+template <bool ENERGY>
 static void launchSS(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C, const DevIncidence& I,
                      const DevPackedSS& K, const double4_32a* mats, const ScenePar* sp, long long* dStep, int* dFlags, int64_t nm,
-                     int halt, int loadFt, int block, int grid, int ticketTotal) {
+                     int halt, int loadFt, int block, int grid, int ticketTotal, const EnergyCols& E) {
     if (block < 0) {
-        k_contact_ss32p<kSSMinBlocks><<<(unsigned)grid, 256, 0, st>>>(N, P, C, I, K, mats, sp, dStep, dFlags, nm, halt, loadFt,
-                                                                      ticketTotal);
+        k_contact_ss32p<kSSMinBlocks, ENERGY><<<(unsigned)grid, 256, 0, st>>>(N, P, C, I, K, mats, sp, dStep, dFlags, nm, halt, loadFt,
+                                                                              ticketTotal, E);
         // without a ticket nobody resets the chunk counter in the kernel
         if (ticketTotal <= 0) cudaMemsetAsync(dFlags + FL_WORK, 0, sizeof(int), st);
         return;
     }
-    k_contact_ss32<kSSMinBlocks><<<(unsigned)((K.n + block - 1) / block), (unsigned)block, 0, st>>>(N, P, C, I, K, mats, sp, dStep,
-                                                                                                 dFlags, nm, halt, loadFt);
+    k_contact_ss32<kSSMinBlocks, ENERGY><<<(unsigned)((K.n + block - 1) / block), (unsigned)block, 0, st>>>(
+        N, P, C, I, K, mats, sp, dStep, dFlags, nm, halt, loadFt, E);
 }
 
-bool launch_contact_fp32(cudaStream_t st, const SideStream& side, const DevNodes& N, const DevParticles& P, const DevContacts& C,
+template <bool ENERGY>
+static bool contactsFP32(cudaStream_t st, const SideStream& side, const DevNodes& N, const DevParticles& P, const DevContacts& C,
                          const DevIncidence& I, const DevPackedSS& K, const double4_32a* mats, const ScenePar* sp,
                          long long* dStep, int* dFlags, int64_t nMixed, bool periodic, bool anyLaw0, bool prepFacets,
-                         int block) {
+                         int block, const EnergyCols& E) {
     const int64_t nm = periodic ? I.nAct : std::min<int64_t>(nMixed, I.nAct);
     const int64_t ns = periodic ? 0 : K.n;
     if (ns > 0 && nm > 0 && side.st) {
         // the mixed range (facets and walls, FP64 geometry) beside the sphere-sphere range: one block
-        // of 128 threads per SM, and two resident sphere-sphere blocks per SM beside it; the
-        // sphere-sphere launch raises FL_HALT when a full run is due; the last block of either
+        // of 128 threads per SM beside a full resident sphere-sphere grid, whose blocks that do not
+        // fit beside the facet/wall blocks start when those end and take the chunks that are left;
+        // the sphere-sphere launch raises FL_HALT when a full run is due; the last block of either
         // advances the step counter
         const int gM = (int)std::min<int64_t>((nm + 127) / 128, smCount());
-        // a full resident grid: the blocks that do not fit beside the facet/wall blocks start
-        // when those end and take the chunks that are left
         const int gS = ssGrid(K, block, kSSMinBlocks);
         const int total = gS > 0 ? gM + gS : 0;
         cudaEventRecord(side.fork, st);
         cudaStreamWaitEvent(side.st, side.fork, 0);
         if (prepFacets) launch_facet_prep(side.st, N, P, dFlags);
-        k_contact_fp32<false><<<(unsigned)gM, 128, 0, side.st>>>(N, P, C, I, mats, sp, dStep, dFlags, 0, nm, 0, total);
-        launchSS(st, N, P, C, I, K, mats, sp, dStep, dFlags, nm, 1, anyLaw0, block, gS, total);
+        k_contact_fp32<false, ENERGY><<<(unsigned)gM, 128, 0, side.st>>>(N, P, C, I, mats, sp, dStep, dFlags, 0, nm, 0, total, E);
+        launchSS<ENERGY>(st, N, P, C, I, K, mats, sp, dStep, dFlags, nm, 1, anyLaw0, block, gS, total, E);
         cudaEventRecord(side.join, side.st);
         cudaStreamWaitEvent(st, side.join, 0);
         return total > 0;
@@ -1200,10 +1316,21 @@ bool launch_contact_fp32(cudaStream_t st, const SideStream& side, const DevNodes
     const int gS = ns > 0 ? ssGrid(K, block, kSSMinBlocks) : 0;
     const int gM = (int)std::max<int64_t>(1, std::min<int64_t>((nm + 127) / 128, 4 * smCount()));
     const int totalM = ns > 0 ? 0 : gM;
-    if (periodic) k_contact_fp32<true><<<(unsigned)gM, 128, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags, 0, nm, 1, totalM);
-    else k_contact_fp32<false><<<(unsigned)gM, 128, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags, 0, nm, 1, totalM);
-    if (ns > 0) launchSS(st, N, P, C, I, K, mats, sp, dStep, dFlags, nm, 0, anyLaw0, block, gS, gS);
+    if (periodic) k_contact_fp32<true, ENERGY><<<(unsigned)gM, 128, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags, 0, nm, 1, totalM, E);
+    else k_contact_fp32<false, ENERGY><<<(unsigned)gM, 128, 0, st>>>(N, P, C, I, mats, sp, dStep, dFlags, 0, nm, 1, totalM, E);
+    if (ns > 0) launchSS<ENERGY>(st, N, P, C, I, K, mats, sp, dStep, dFlags, nm, 0, anyLaw0, block, gS, gS, E);
     return totalM > 0 || gS > 0;
+}
+
+bool launch_contact_fp32(cudaStream_t st, const SideStream& side, const DevNodes& N, const DevParticles& P, const DevContacts& C,
+                         const DevIncidence& I, const DevPackedSS& K, const double4_32a* mats, const ScenePar* sp,
+                         long long* dStep, int* dFlags, int64_t nMixed, bool periodic, bool anyLaw0, bool prepFacets,
+                         int block, const EnergyCols* energy) {
+    if (energy)
+        return contactsFP32<true>(st, side, N, P, C, I, K, mats, sp, dStep, dFlags, nMixed, periodic, anyLaw0, prepFacets, block,
+                                  *energy);
+    return contactsFP32<false>(st, side, N, P, C, I, K, mats, sp, dStep, dFlags, nMixed, periodic, anyLaw0, prepFacets, block,
+                               EnergyCols{});
 }
 
 // ---------------------------------------------------------------------------------- force sum

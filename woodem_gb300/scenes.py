@@ -236,13 +236,13 @@ def _sphere_nodes(S, col, value=None):
 
 def periodic_shear(n=200_000, seed=0, rmin=2e-3, rmax=4e-3, density=2600.0, young=5e7, tanPhi=0.4, ktDivKn=0.2,
                    fill_fraction=0.35, shear_rate=1.0, damping=0.2, verletRel=0.1, precision="fp64", compress_steps=0,
-                   compress_rate=None, centers=None):
+                   compress_rate=None, centers=None, compress_to=0.55):
     """Periodic simple shear: ``n`` spheres with radii uniform in [rmin, rmax] placed by seeded random
     sequential insertion in a periodic cube sized to solid fraction ``fill_fraction``; IdealElPl
     contacts, Leapfrog damping ``damping``, dt = 0.3*pWaveDt, verletDist = 0.1*rmin,
     Cell.homoDeform = HomoGradV2. With ``compress_steps`` the cell is first compressed isotropically
-    (nextGradV = -compress_rate*I, by default the rate that brings the fill to 0.55 in that many
-    steps); then nextGradV is set to the simple shear with xz component ``shear_rate``. Given
+    (nextGradV = -compress_rate*I, by default the rate that brings the fill to ``compress_to`` in
+    that many steps); then nextGradV is set to the simple shear with xz component ``shear_rate``. Given
     ``centers``, those positions are used instead of the random insertion (a state to restore)."""
     from .core import Cell
     rng = np.random.default_rng(seed)
@@ -263,7 +263,7 @@ def periodic_shear(n=200_000, seed=0, rmin=2e-3, rmax=4e-3, density=2600.0, youn
     if compress_steps:
         rate = compress_rate
         if rate is None:
-            rate = math.log((0.55 / fill_fraction) ** (1 / 3.0)) / (compress_steps * S.dt)
+            rate = math.log((compress_to / fill_fraction) ** (1 / 3.0)) / (compress_steps * S.dt)
         S.cell.nextGradV = -rate * np.eye(3)
         S.run(compress_steps)
     g = np.zeros((3, 3))
