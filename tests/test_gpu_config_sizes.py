@@ -1,7 +1,7 @@
 """Parity at the sizes of the benchmark configurations themselves.
 
 * 1M-sphere rotating Hertz drum (20 000 facets, 2 rotating wall caps), compacted on the GPU:
-  FP64 plain mode against the FP64 oracle, bitwise, over 40 steps that include collider full
+  FP64 plain mode against the FP64 oracle, bitwise, over 80 steps that include collider full
   runs; FP32-force mode against FP64 from the same state after one step.
 * 200 000-sphere periodic cell, compressed to solid fraction 0.55 and sheared (xz rate 1/s):
   FP64 plain mode against the oracle, bitwise (cellDist, the cell and ContactLoop.stress
@@ -105,10 +105,10 @@ def _one_step_errors(S64, S32, A):
 @pytest.fixture(scope="module")
 def drum_1m(gpu_lib):
     """The benchmark drum: 1 000 000 lognormal spheres (median 3 mm), a 1.2 m x 0.6 m drum of
-    20 000 facets and 2 rotating wall caps, Hertz DMT; the random fill compacted on the GPU for
-    2 000 steps at 40 g (and 1 500 easing back to 1 g), so that the bed carries millions of real
-    contacts, facet and cap contacts included. Returns the sphere state."""
-    S = scenes.hertz_drum(n=1_000_000, seed=0, precision="fp64", settle_steps=2000, settle_g=40.0)
+    20 000 facets and 2 rotating wall caps, Hertz DMT; the random fill compacted on the GPU as the
+    benchmark does (16 000 steps at 40 g, 12 000 easing back to 1 g), so that the bed carries
+    millions of real contacts, facet and cap contacts included. Returns the sphere state."""
+    S = scenes.hertz_drum(n=1_000_000, seed=0, precision="fp64", settle_steps=16000, settle_g=40.0)
     st = {k: scenes._sphere_nodes(S, k) for k in ("pos", "vel", "angVel")}
     st["radius"] = scenes.sphere_radii(S)
     S.close()
@@ -122,11 +122,11 @@ def _drum(st, prec):
 def test_drum_1m_fp64_bitwise(drum_1m):
     S = _drum(drum_1m, "fp64")
     O = _oracle(_plan.compile_scene(S))
-    for k in (1, 9, 30):
+    for k in (1, 19, 60):
         S.run(k)
         O.run(k)
         n_real, n_con = _assert_bitwise(S, O)
-    print("1M drum: %d contacts, %d real, %d full runs, bitwise over 40 steps" % (n_con, n_real, O.stats().n_full_runs))
+    print("1M drum: %d contacts, %d real, %d full runs, bitwise over 80 steps" % (n_con, n_real, O.stats().n_full_runs))
     assert n_real > 1_000_000 and O.stats().n_full_runs >= 2
     A = _plan.compile_scene(S)
     facet_or_wall = A.particles["shape"][S._sim.contacts()["id_lo"]] != 0

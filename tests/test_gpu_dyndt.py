@@ -127,10 +127,13 @@ def test_dt_set_between_runs(gpu_lib):
 @pytest.mark.parametrize("build", ["drum", "box"])
 def test_fp32_mode_against_fp64(build, gpu_lib):
     """DynDt in the FP32-force mode: the stiffnesses come from the FP32 contact state (kn, kt and
-    the contact normal rounded to FP32; L6Geom.lens from the current overlap), so each critical
-    timestep agrees with the FP64 path's (bitwise equal to the oracle above) within 1e-3 relative,
-    and the activation counters agree exactly. From the same state, both precisions run 300 steps
-    with DynDt every 25 steps; dt after each evaluation is compared."""
+    the contact normal rounded to FP32; L6Geom.lens from the current overlap). From the same state
+    both precisions run 300 steps with DynDt every 25 steps (the FP64 path is bitwise the
+    oracle's, above). The first evaluation, on states that are still equal up to the FP32
+    rounding of one step, gives the same critical timestep within 1e-5 relative; later
+    evaluations follow trajectories that part slowly (the minimum over the nodes can move to
+    another node), so there the critical timestep and Scene.dt agree within 5 %; the activation
+    counters agree exactly."""
     if build == "drum":
         mk = lambda prec: _with_dyndt(scenes.hertz_drum(n=3000, seed=2, diameter=0.3, length=0.12, div=31, axDiv=6,
                                                         fill_fraction=0.3, settle_steps=3000, precision=prec),
@@ -153,6 +156,7 @@ def test_fp32_mode_against_fp64(build, gpu_lib):
         crit[S.gpu.precision + "_counters"] = (e.nDone, e.stepLast, e.stepPrev)
     a, b = np.array(crit["fp64"]), np.array(crit["fp32"])
     assert np.all(np.isfinite(a[:, 1])) and len(set(a[:, 0])) > 2
-    np.testing.assert_allclose(b[:, 1], a[:, 1], rtol=1e-3)
-    np.testing.assert_allclose(b[:, 0], a[:, 0], rtol=1e-3)
+    assert b[0, 1] == pytest.approx(a[0, 1], rel=1e-5)
+    np.testing.assert_allclose(b[:, 1], a[:, 1], rtol=5e-2)
+    np.testing.assert_allclose(b[:, 0], a[:, 0], rtol=5e-2)
     assert crit["fp64_counters"] == crit["fp32_counters"]

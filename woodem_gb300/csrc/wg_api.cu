@@ -42,8 +42,6 @@ void Sim::dfree(void* p) {
 }
 Sim::~Sim() {
     if (stream) cudaStreamSynchronize(stream);
-    // lines this simulation marked persisting would keep their share of L2 after it is gone
-    if (mirBytes && l2Pin) cudaCtxResetPersistingL2Cache();
     collide_free(*this);
     for (void* p : allocs) cudaFree(p);
     allocs.clear();
@@ -605,9 +603,8 @@ int Sim::upload() {
             rsp[q] = make_float2(rh, (float)(posr[q].w - (double)rh));
         }
         dNodeC = (NodeConst32*)dalloc(sizeof(NodeConst32) * nSlots);
-        // the mirror records and wz in one block, so that one L2 access-policy window covers both
-        N.mir = (Mirror*)dalloc(sizeof(Mirror) * nSlots + sizeof(float) * nSlots);
-        N.wz = N.mir ? (float*)(N.mir + nSlots) : nullptr;
+        N.mir = (Mirror*)dalloc(sizeof(Mirror) * nSlots);
+        N.wz = (float*)dalloc(sizeof(float) * nSlots);
         N.orif = (float4*)dalloc(sizeof(float4) * nSlots);
         N.rsplit = (float2*)dalloc(sizeof(float2) * nSlots);
         N.lh = (float4*)dalloc(sizeof(float4) * nSlots);
@@ -642,9 +639,6 @@ int Sim::upload() {
         WG_CUDA_TRY(cudaMemcpyAsync(N.lh, hph.data(), sizeof(float4) * nSlots, cudaMemcpyHostToDevice, S.stream));
         WG_CUDA_TRY(cudaMemcpyAsync(N.ll, hpl.data(), sizeof(float4) * nSlots, cudaMemcpyHostToDevice, S.stream));
         WG_CUDA_TRY(cudaMemcpyAsync(dNodeC, nc.data(), sizeof(NodeConst32) * nSlots, cudaMemcpyHostToDevice, S.stream));
-        mirBytes = (sizeof(Mirror) + sizeof(float)) * (size_t)nSlots;
-        int r = applyL2Window();
-        if (r) return r;
     }
     launch_facet_prep(stream, N, P, nullptr);
     long long st0 = cfg.step;
@@ -854,45 +848,6 @@ int Sim::runDynDtScenes(const std::vector<char>& due, long long deviceStep) {
         } else
             d.dynDt = ndt;
     }
-    return 0;
-}
-
-// FP32-force mode: the double-float mirror records (and wz), which every contact gathers for both
-// of its particles, are kept in L2 with a persisting access-policy window on the simulation's
-// stream (launch flag WG_LAUNCH_NO_L2_PIN turns it off); the window is sized to the device's
-// persisting-L2 limit for this context, which the first simulation that needs it raises.
-int Sim::applyL2Window() {
-    Sim& S = *this;
-    if (!N.mir || !stream) return 0;
-    int maxPersist = 0, maxWin = 0;
-    if (cudaDeviceGetAttribute(&maxPersist, cudaDevAttrMaxPersistingL2CacheSize, device) != cudaSuccess ||
-        cudaDeviceGetAttribute(&maxWin, cudaDevAttrMaxAccessPolicyWindowSize, device) != cudaSuccess || maxPersist <= 0 ||
-        maxWin <= 0) {
-        cudaGetLastError();
-        return 0;  // no persisting L2 on this device: nothing to do
-    }
-    cudaStreamAttrValue a{};
-    if (l2Pin) {
-        size_t lim = 0;
-        WG_CUDA_TRY(cudaDeviceGetLimit(&lim, cudaLimitPersistingL2CacheSize));
-        const size_t want = std::min<size_t>(mirBytes, (size_t)maxPersist);
-        if (lim < want) WG_CUDA_TRY(cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, want));
-        WG_CUDA_TRY(cudaDeviceGetLimit(&lim, cudaLimitPersistingL2CacheSize));
-        const size_t win = std::min<size_t>(mirBytes, (size_t)maxWin);
-        a.accessPolicyWindow.base_ptr = (void*)N.mir;
-        a.accessPolicyWindow.num_bytes = win;
-        a.accessPolicyWindow.hitRatio = win > 0 ? (float)std::min(1.0, (double)lim / (double)win) : 0.f;
-        a.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
-        a.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
-    } else {
-        a.accessPolicyWindow.base_ptr = nullptr;
-        a.accessPolicyWindow.num_bytes = 0;
-        a.accessPolicyWindow.hitRatio = 0.f;
-        a.accessPolicyWindow.hitProp = cudaAccessPropertyNormal;
-        a.accessPolicyWindow.missProp = cudaAccessPropertyNormal;
-    }
-    WG_CUDA_TRY(cudaStreamSetAttribute(stream, cudaStreamAttributeAccessPolicyWindow, &a));
-    if (side.st) WG_CUDA_TRY(cudaStreamSetAttribute(side.st, cudaStreamAttributeAccessPolicyWindow, &a));
     return 0;
 }
 
@@ -1655,27 +1610,15 @@ int wg_get_slot_nodes(wg_scene* s, int32_t k, int64_t n, double* pos, double* or
 int wg_set_launch(wg_scene* s, int32_t contact_block, int32_t chunk_steps, int32_t launch_flags) {
     if (!s) return WG_ERR_ARG;
     Sim& S = *SIM(s);
-    if (contact_block != 0 && contact_block != 64 && contact_block != 128 && contact_block != 256 && contact_block != -256)
-        return S.fail(WG_ERR_ARG, "contact_block must be 0, 64, 128, 256 or -256");
+    if (contact_block != 0 && contact_block != 64 && contact_block != 128 && contact_block != 256 && contact_block != -256 &&
+        contact_block != -512)
+        return S.fail(WG_ERR_ARG, "contact_block must be 0, 64, 128, 256, -256 or -512");
     if (chunk_steps < 1 || chunk_steps > 1024) return S.fail(WG_ERR_ARG, "chunk_steps must be in [1, 1024]");
     S.contactBlock = contact_block;
     S.chunkSteps = chunk_steps;
-    if (launch_flags & ~(WG_LAUNCH_GRAPH | WG_LAUNCH_SERIAL | WG_LAUNCH_NO_L2_PIN)) return S.fail(WG_ERR_ARG, "unknown launch flag");
+    if (launch_flags & ~(WG_LAUNCH_GRAPH | WG_LAUNCH_SERIAL)) return S.fail(WG_ERR_ARG, "unknown launch flag");
     S.useGraph = (launch_flags & WG_LAUNCH_GRAPH) != 0;
     S.concurrentContacts = (launch_flags & WG_LAUNCH_SERIAL) == 0;
-    const bool pin = (launch_flags & WG_LAUNCH_NO_L2_PIN) == 0;
-    if (pin != S.l2Pin) {
-        S.l2Pin = pin;
-        if (S.uploaded) {
-            WG_CUDA_TRY(cudaSetDevice(S.device));
-            int r = S.applyL2Window();
-            if (r) return r;
-            if (S.graphExec) {  // captured kernels keep the window they were captured with
-                cudaGraphExecDestroy(S.graphExec);
-                S.graphExec = nullptr;
-            }
-        }
-    }
     return WG_OK;
 }
 

@@ -210,8 +210,7 @@ enum { FL_FULL = 0,   // set by Leapfrog: a node moved farther than verletDist, 
        FL_ERR = 1,    // error code raised by a kernel
        FL_HALT = 2,   // set by the contact kernel of a step that found FL_FULL: later queued steps do nothing
        FL_TICKET = 3, // blocks of the last contact kernel of a step that have finished (the last advances the step)
-       FL_WORK = 4,   // chunks of the sphere-sphere work handed out in this step (zero between launches)
-       FL_WORDS = 8 };
+       FL_WORDS = 4 };
 
 __host__ __device__ inline int32_t packCellDist(int a, int b, int c) {
     return (int32_t)(((uint32_t)(a + 512) & 1023u) | (((uint32_t)(b + 512) & 1023u) << 10) | (((uint32_t)(c + 512) & 1023u) << 20));
@@ -391,9 +390,6 @@ struct Sim {
     bool useGraph = false;
     bool concurrentContacts = true;   // facet/wall contacts beside, not before, the sphere-sphere ones
     bool facetsStatic = false;        // every facet vertex is fully blocked and at rest: FacetPrep is made once
-    bool l2Pin = true;                // keep the FP32-force mirror records in L2 (persisting window)
-    size_t mirBytes = 0;
-    int applyL2Window();
     cudaGraphExec_t graphExec = nullptr;
     int64_t graphSteps = 0;  // steps in the captured chunk, 0: none valid
     int64_t graphEpoch = -1; // nFullRuns when it was captured

@@ -126,7 +126,7 @@ __device__ __noinline__ void resetNodeForce(DevNodes N, int i, float mh, float m
 // ENERGY: Scene.trackEnergy; each node writes its step's energy terms (Leapfrog.cpp:52-97, in FP64
 // from this step's force and torque) into E, as the FP64 Leapfrog does.
 template <bool PERI, bool ENERGY>
-__global__ void __launch_bounds__(256, 4) k_leapfrog32(DevNodes N, DevParticles P, DevIncidence I, const NodeConst32* __restrict__ ncs,
+__global__ void __launch_bounds__(256) k_leapfrog32(DevNodes N, DevParticles P, DevIncidence I, const NodeConst32* __restrict__ ncs,
                                                     const ScenePar* __restrict__ spp, int* __restrict__ dFlags, int fromEnds,
                                                     const long long* __restrict__ dStepC, EnergyCols E) {
     __shared__ EndStage<float4, float2, kLeapfrogChunk32> stage[8];
@@ -545,9 +545,7 @@ struct SSIn {
 
 // k_step_advance folded into the last kernel(s) of a step: every block of the `total` blocks of
 // those kernels calls this at its end; the last one to finish advances the step counter (unless
-// the queued steps were halted) and resets the ticket and the sphere-sphere chunk counter (every
-// block of the sphere-sphere kernel has taken its last chunk before it arrives here).
-// total <= 0: nothing.
+// the queued steps were halted) and resets the ticket. total <= 0: nothing.
 __device__ __forceinline__ void stepTicket(int* dFlags, long long* dStep, int total) {
     if (total <= 0) return;
     __syncthreads();
@@ -555,7 +553,6 @@ __device__ __forceinline__ void stepTicket(int* dFlags, long long* dStep, int to
         __threadfence();
         if (atomicAdd(dFlags + FL_TICKET, 1) == total - 1) {
             dFlags[FL_TICKET] = 0;
-            dFlags[FL_WORK] = 0;
             if (!halted(dFlags)) *dStep += 1;
         }
     }
@@ -758,15 +755,12 @@ __global__ void __launch_bounds__(256, MINB) k_contact_ss32(DevNodes N, DevParti
     ssContact<ENERGY>(x, j, N, P, C, I, K, mats, spp, stepAbs, dFlags, nm, E);
 }
 
-// The same contacts through a resident grid whose warps take chunks of kSSChunk consecutive
-// contacts from a counter in the flag words (FL_WORK, reset by the block that finishes last), so
-// that blocks which become resident late -- beside the facet/wall kernel, whose blocks hold part
-// of each SM at first -- take less work instead of finishing late. Each lane walks its chunk with
-// a stride of 32; the next contact's packed item and flags are loaded while the current contact's
-// state and mirror records are in flight, so each contact waits for one memory round trip; the
-// persistent state of a contact that is not real (pending, or not touching) is not loaded.
-constexpr int kSSChunk = 256;
-template <int MINB, bool ENERGY>
+// The same contacts through a resident grid, each thread walking the range with the grid's
+// stride: the next contact's packed item is loaded while the current contact's state and mirror
+// records are in flight, so each contact waits for one memory round trip instead of two.
+// REALONLY: the next contact's flags are prefetched with its item, and the persistent state is
+// loaded only for a contact that is real (the others need none of it).
+template <int MINB, bool ENERGY, bool REALONLY>
 __global__ void __launch_bounds__(256, MINB) k_contact_ss32p(DevNodes N, DevParticles P, DevContacts C, DevIncidence I, DevPackedSS K,
                                                              const double4_32a* __restrict__ mats, const ScenePar* __restrict__ spp,
                                                              long long* __restrict__ dStep, int* __restrict__ dFlags, int64_t nm,
@@ -776,69 +770,34 @@ __global__ void __launch_bounds__(256, MINB) k_contact_ss32p(DevNodes N, DevPart
         if (haltBlock && blockIdx.x == 0 && threadIdx.x == 0) dFlags[FL_HALT] = 1;
         return;
     }
-    const unsigned FULL = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    unsigned* ctr = (unsigned*)(dFlags + FL_WORK);
-    const int64_t nChunks = (K.n + kSSChunk - 1) / kSSChunk;
-    // the warp holds its current chunk and the one after it (taken one chunk ahead, so that the
-    // prefetch of the next item never waits for the counter)
-    unsigned c0 = 0, c1 = 0;
-    if (lane == 0) {
-        c0 = atomicAdd(ctr, 1u);
-        c1 = atomicAdd(ctr, 1u);
-    }
-    int64_t cur = __shfl_sync(FULL, c0, 0), nxt = __shfl_sync(FULL, c1, 0);
-    int u = 0;  // position of the lane's contact in its chunk: cur * kSSChunk + 32 * u + lane
-    int64_t j = cur * kSSChunk + lane;
-    int4 nextIt = make_int4(0, 0, 0, 0);
-    uint32_t nextFl = 0;
-    if (cur < nChunks && j < K.n) {
-        nextIt = K.item[j];
-        nextFl = K.flags[j];
-    }
-    while (cur < nChunks) {
-        // the contact after this one
-        int un = u + 1;
-        int64_t cn = cur;
-        if (un == kSSChunk / 32) {
-            un = 0;
-            cn = nxt;
-        }
-        const int64_t jn = cn * kSSChunk + 32 * un + lane;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int4 next = j < K.n ? K.item[j] : make_int4(0, 0, 0, 0);
+    uint32_t nextFl = (REALONLY && j < K.n) ? K.flags[j] : 0u;
+    for (; j < K.n; j += stride) {
         SSIn x;
-        x.it = nextIt;
-        x.pf = nextFl;
-        const bool in = j < K.n;
-        if (cn < nChunks && jn < K.n) {
-            nextIt = K.item[jn];
-            nextFl = K.flags[jn];
+        x.it = next;
+        if (REALONLY) x.pf = nextFl;
+        if (j + stride < K.n) {
+            next = K.item[j + stride];
+            if (REALONLY) nextFl = K.flags[j + stride];
         }
-        if (in) {
-            const bool real = x.pf & C_REAL;
+        if (!REALONLY) x.pf = K.flags[j];
+        const bool ld = !REALONLY || (x.pf & C_REAL);
 #pragma unroll
-            for (int q = 0; q < CF_NCOL; q++) x.st[q] = real ? K.col[q][j] : 0.f;
-            x.ft1o = 0.;
-            x.ft2o = 0.;
-            if (loadFt && real) {
-                x.ft1o = K.ft[0][j];
-                x.ft2o = K.ft[1][j];
-            }
-            x.ma = N.mir[x.it.x];
-            x.mb = N.mir[x.it.y];
-            x.wza = N.wz[x.it.x];
-            x.wzb = N.wz[x.it.y];
-            ssContact<ENERGY>(x, j, N, P, C, I, K, mats, spp, stepAbs, dFlags, nm, E);
+        for (int q = 0; q < CF_NCOL; q++) x.st[q] = ld ? K.col[q][j] : 0.f;
+        x.ft1o = 0.;
+        x.ft2o = 0.;
+        if (loadFt && ld) {
+            x.ft1o = K.ft[0][j];
+            x.ft2o = K.ft[1][j];
         }
-        if (cn != cur) {
-            cur = cn;
-            unsigned c2 = 0;
-            if (lane == 0) c2 = atomicAdd(ctr, 1u);
-            nxt = __shfl_sync(FULL, c2, 0);
-        }
-        u = un;
-        j = jn;
+        x.ma = N.mir[x.it.x];
+        x.mb = N.mir[x.it.y];
+        x.wza = N.wz[x.it.x];
+        x.wzb = N.wz[x.it.y];
+        ssContact<ENERGY>(x, j, N, P, C, I, K, mats, spp, stepAbs, dFlags, nm, E);
     }
-    // the block that finishes last advances the step and resets the chunk counter
     stepTicket(dFlags, dStep, ticketTotal);
 }
 
@@ -1274,11 +1233,14 @@ template <bool ENERGY>
 static void launchSS(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C, const DevIncidence& I,
                      const DevPackedSS& K, const double4_32a* mats, const ScenePar* sp, long long* dStep, int* dFlags, int64_t nm,
                      int halt, int loadFt, int block, int grid, int ticketTotal, const EnergyCols& E) {
+    if (block == -512) {
+        k_contact_ss32p<kSSMinBlocks, ENERGY, true><<<(unsigned)grid, 256, 0, st>>>(N, P, C, I, K, mats, sp, dStep, dFlags, nm, halt,
+                                                                                    loadFt, ticketTotal, E);
+        return;
+    }
     if (block < 0) {
-        k_contact_ss32p<kSSMinBlocks, ENERGY><<<(unsigned)grid, 256, 0, st>>>(N, P, C, I, K, mats, sp, dStep, dFlags, nm, halt, loadFt,
-                                                                              ticketTotal, E);
-        // without a ticket nobody resets the chunk counter in the kernel
-        if (ticketTotal <= 0) cudaMemsetAsync(dFlags + FL_WORK, 0, sizeof(int), st);
+        k_contact_ss32p<kSSMinBlocks, ENERGY, false><<<(unsigned)grid, 256, 0, st>>>(N, P, C, I, K, mats, sp, dStep, dFlags, nm, halt,
+                                                                                     loadFt, ticketTotal, E);
         return;
     }
     k_contact_ss32<kSSMinBlocks, ENERGY><<<(unsigned)((K.n + block - 1) / block), (unsigned)block, 0, st>>>(
@@ -1294,12 +1256,11 @@ static bool contactsFP32(cudaStream_t st, const SideStream& side, const DevNodes
     const int64_t ns = periodic ? 0 : K.n;
     if (ns > 0 && nm > 0 && side.st) {
         // the mixed range (facets and walls, FP64 geometry) beside the sphere-sphere range: one block
-        // of 128 threads per SM beside a full resident sphere-sphere grid, whose blocks that do not
-        // fit beside the facet/wall blocks start when those end and take the chunks that are left;
-        // the sphere-sphere launch raises FL_HALT when a full run is due; the last block of either
+        // of 128 threads per SM, and two resident sphere-sphere blocks per SM beside it; the
+        // sphere-sphere launch raises FL_HALT when a full run is due; the last block of either
         // advances the step counter
         const int gM = (int)std::min<int64_t>((nm + 127) / 128, smCount());
-        const int gS = ssGrid(K, block, kSSMinBlocks);
+        const int gS = ssGrid(K, block, kSSMinBlocks - 1);
         const int total = gS > 0 ? gM + gS : 0;
         cudaEventRecord(side.fork, st);
         cudaStreamWaitEvent(side.st, side.fork, 0);

@@ -12,8 +12,8 @@ import numpy as np
 
 DEFAULT_CANDIDATES = (
     # (contact threads per block, steps per chunk, CUDA graph, facet/wall contacts on a second
-    # stream beside the sphere-sphere ones[, FP32 mirror records pinned in L2]); block -256 selects
-    # the resident-grid FP32 sphere-sphere kernel whose warps take chunks of contacts
+    # stream beside the sphere-sphere ones); block -256 selects the resident-grid FP32
+    # sphere-sphere kernel whose threads prefetch their next contact
     (-256, 32, False, True),
     (-256, 32, False, False),
     (256, 32, False, True),
@@ -29,9 +29,9 @@ def _handle(sim):
     return sim.H.L, sim.H.h
 
 
-def set_launch(sim, block=0, chunk=32, graph=False, concurrent=True, l2pin=True):
+def set_launch(sim, block=0, chunk=32, graph=False, concurrent=True):
     L, h = _handle(sim)
-    flags = (1 if graph else 0) | (0 if concurrent else 2) | (0 if l2pin else 4)
+    flags = (1 if graph else 0) | (0 if concurrent else 2)
     sim.H.check(L.wg_set_launch(h, int(block), int(chunk), flags), "set_launch")
 
 
