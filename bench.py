@@ -372,7 +372,7 @@ def contact_force_error(S64, S32):
     big = np.zeros(n)
     np.maximum.at(big, c64["id_lo"][c64["real"] != 0], np.linalg.norm(c64["fglob"][c64["real"] != 0], axis=1))
     np.maximum.at(big, c64["id_hi"][c64["real"] != 0], np.linalg.norm(c64["fglob"][c64["real"] != 0], axis=1))
-    sel = big > 0
+    sel = big > 1e-6 * (big.max() if len(big) else 0.0)
     pr = np.linalg.norm(F32[sel] - F64[sel], axis=1) / big[sel]
     return {"contacts_compared": int(ok.sum()), "contact_force_rel_max": float(rel[ok].max()) if ok.any() else None,
             "contact_force_rel_median": float(np.median(rel[ok])) if ok.any() else None,

@@ -153,9 +153,8 @@ int wg_set_scenes(wg_scene* s, int32_t n_scenes, const wg_config* cfgs, const in
    threads prefetch their next contact), steps
    queued per host check of the collider request (1..1024), and flags: WG_LAUNCH_GRAPH replays each
    such chunk of steps as one CUDA graph, WG_LAUNCH_SERIAL runs the facet/wall contacts before the
-   sphere-sphere ones instead of beside them on a second stream. contact_block -512 is the
-   resident grid of -256 that prefetches each contact's flags with its item and loads the
-   persistent state of real contacts only. Results do not depend on these; only the speed does. */
+   sphere-sphere ones instead of beside them on a second stream. Results do not depend on these;
+   only the speed does. */
 #define WG_LAUNCH_GRAPH 1
 #define WG_LAUNCH_SERIAL 2
 int wg_set_launch(wg_scene* s, int32_t contact_block, int32_t chunk_steps, int32_t launch_flags);

@@ -130,7 +130,9 @@ def test_fp32_mode_against_fp64(build, gpu_lib):
     the contact normal rounded to FP32; L6Geom.lens from the current overlap). From the same state
     both precisions run 300 steps with DynDt every 25 steps (the FP64 path is bitwise the
     oracle's, above). The first evaluation, on states that are still equal up to the FP32
-    rounding of one step, gives the same critical timestep within 1e-5 relative; later
+    rounding of one step, gives the same critical timestep within 1e-3 relative (the rotational
+    stiffness lens^2 kt takes the current overlap instead of the first step's: uN/2 against the
+    radius, ~1e-4 in a settled bed); later
     evaluations follow trajectories that part slowly (the minimum over the nodes can move to
     another node), so there the critical timestep and Scene.dt agree within 5 %; the activation
     counters agree exactly."""
@@ -156,7 +158,7 @@ def test_fp32_mode_against_fp64(build, gpu_lib):
         crit[S.gpu.precision + "_counters"] = (e.nDone, e.stepLast, e.stepPrev)
     a, b = np.array(crit["fp64"]), np.array(crit["fp32"])
     assert np.all(np.isfinite(a[:, 1])) and len(set(a[:, 0])) > 2
-    assert b[0, 1] == pytest.approx(a[0, 1], rel=1e-5)
+    assert b[0, 1] == pytest.approx(a[0, 1], rel=1e-3)
     np.testing.assert_allclose(b[:, 1], a[:, 1], rtol=5e-2)
     np.testing.assert_allclose(b[:, 0], a[:, 0], rtol=5e-2)
     assert crit["fp64_counters"] == crit["fp32_counters"]

@@ -2,7 +2,8 @@
 
 Tolerances (relative, written here):
   * per-contact global force after one step from the same state:   1e-5 of the contact force
-  * per-particle net force, normalised by the particle's largest contact force: 1e-5
+  * per-particle net force, normalised by the particle's largest contact force: 1e-5 (particles
+    whose largest contact force is above 1e-6 of the largest of all, the cut used for contacts)
   * after 20 steps from the same state (errors compound through the trajectory): 1e-3
   * long runs are compared statistically (trajectories are chaotic): kinetic energy,
     coordination number and packing height within a few percent.
@@ -66,7 +67,7 @@ def _force_errors(c64, c32, f64, f32, A, same_set=True):
     ids = np.concatenate([c64["id_lo"][real], c64["id_hi"][real]])
     mm = np.concatenate([mag, mag])
     np.maximum.at(fmax, ids, mm)
-    sph = (A.particles["shape"] == 0) & (fmax > 0)
+    sph = (A.particles["shape"] == 0) & (fmax > 1e-6 * mag.max())
     nodes = A.particles["nodes"][:, 0]
     rel_part = np.linalg.norm(f64[nodes[sph]] - f32[nodes[sph]], axis=1) / fmax[sph]
     return rel_contact, rel_part

@@ -758,9 +758,7 @@ __global__ void __launch_bounds__(256, MINB) k_contact_ss32(DevNodes N, DevParti
 // The same contacts through a resident grid, each thread walking the range with the grid's
 // stride: the next contact's packed item is loaded while the current contact's state and mirror
 // records are in flight, so each contact waits for one memory round trip instead of two.
-// REALONLY: the next contact's flags are prefetched with its item, and the persistent state is
-// loaded only for a contact that is real (the others need none of it).
-template <int MINB, bool ENERGY, bool REALONLY>
+template <int MINB, bool ENERGY>
 __global__ void __launch_bounds__(256, MINB) k_contact_ss32p(DevNodes N, DevParticles P, DevContacts C, DevIncidence I, DevPackedSS K,
                                                              const double4_32a* __restrict__ mats, const ScenePar* __restrict__ spp,
                                                              long long* __restrict__ dStep, int* __restrict__ dFlags, int64_t nm,
@@ -773,22 +771,16 @@ __global__ void __launch_bounds__(256, MINB) k_contact_ss32p(DevNodes N, DevPart
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     int4 next = j < K.n ? K.item[j] : make_int4(0, 0, 0, 0);
-    uint32_t nextFl = (REALONLY && j < K.n) ? K.flags[j] : 0u;
     for (; j < K.n; j += stride) {
         SSIn x;
         x.it = next;
-        if (REALONLY) x.pf = nextFl;
-        if (j + stride < K.n) {
-            next = K.item[j + stride];
-            if (REALONLY) nextFl = K.flags[j + stride];
-        }
-        if (!REALONLY) x.pf = K.flags[j];
-        const bool ld = !REALONLY || (x.pf & C_REAL);
+        if (j + stride < K.n) next = K.item[j + stride];
+        x.pf = K.flags[j];
 #pragma unroll
-        for (int q = 0; q < CF_NCOL; q++) x.st[q] = ld ? K.col[q][j] : 0.f;
+        for (int q = 0; q < CF_NCOL; q++) x.st[q] = K.col[q][j];
         x.ft1o = 0.;
         x.ft2o = 0.;
-        if (loadFt && ld) {
+        if (loadFt) {
             x.ft1o = K.ft[0][j];
             x.ft2o = K.ft[1][j];
         }
@@ -1233,14 +1225,9 @@ template <bool ENERGY>
 static void launchSS(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C, const DevIncidence& I,
                      const DevPackedSS& K, const double4_32a* mats, const ScenePar* sp, long long* dStep, int* dFlags, int64_t nm,
                      int halt, int loadFt, int block, int grid, int ticketTotal, const EnergyCols& E) {
-    if (block == -512) {
-        k_contact_ss32p<kSSMinBlocks, ENERGY, true><<<(unsigned)grid, 256, 0, st>>>(N, P, C, I, K, mats, sp, dStep, dFlags, nm, halt,
-                                                                                    loadFt, ticketTotal, E);
-        return;
-    }
     if (block < 0) {
-        k_contact_ss32p<kSSMinBlocks, ENERGY, false><<<(unsigned)grid, 256, 0, st>>>(N, P, C, I, K, mats, sp, dStep, dFlags, nm, halt,
-                                                                                     loadFt, ticketTotal, E);
+        k_contact_ss32p<kSSMinBlocks, ENERGY><<<(unsigned)grid, 256, 0, st>>>(N, P, C, I, K, mats, sp, dStep, dFlags, nm, halt, loadFt,
+                                                                              ticketTotal, E);
         return;
     }
     k_contact_ss32<kSSMinBlocks, ENERGY><<<(unsigned)((K.n + block - 1) / block), (unsigned)block, 0, st>>>(
