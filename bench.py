@@ -349,9 +349,9 @@ def kinetic(S):
 
 def contact_force_error(S64, S32):
     """Per-contact global force of two simulations of the same state after one step: the largest
-    and the median relative difference over the real contacts both have (those above 1e-6 of the
-    largest force), and the largest difference of a particle's net force relative to its largest
-    contact force."""
+    and the median difference over the real contacts both have, relative to the contact's force
+    (or to 1e-4 of the largest force for weaker contacts), and the largest difference of a
+    particle's net force relative to its largest contact force."""
     c64, c32 = S64._sim.contacts(), S32._sim.contacts()
     k64 = c64["id_lo"].astype(np.int64) << 32 | c64["id_hi"].astype(np.int64)
     k32 = c32["id_lo"].astype(np.int64) << 32 | c32["id_hi"].astype(np.int64)
@@ -360,10 +360,11 @@ def contact_force_error(S64, S32):
     i32 = np.searchsorted(k32, both)
     f64, f32 = c64["fglob"][i64], c32["fglob"][i32]
     mag = np.linalg.norm(f64, axis=1)
-    rel = np.linalg.norm(f32 - f64, axis=1) / np.maximum(mag, 1e-300)
-    # the contacts carrying a force above 1e-6 of the largest one (the tests' definition: the
-    # relative error of a force ~1e-7 of the others is its FP32 rounding of the overlap, not the force)
-    ok = mag > 1e-6 * (mag.max() if len(mag) else 0.0)
+    # relative to the contact's force, or to 1e-4 of the largest force for the weaker contacts (the
+    # tests' definition: the FP32-force overlap is exact to ~2^-46 of the centre distance, a growing
+    # fraction of an ever smaller overlap)
+    rel = np.linalg.norm(f32 - f64, axis=1) / np.maximum(mag, 1e-4 * (mag.max() if len(mag) else 0.0) + 1e-300)
+    ok = mag > 0
     S64.sync()
     S32.sync()
     F64, F32 = S64.dem._nodes.soa.col("force"), S32.dem._nodes.soa.col("force")

@@ -13,7 +13,9 @@ Tolerances (written here; the same definitions as in test_gpu_fp32 and test_gpu_
     node orientation within 1e-14 (sin/cos last bit); ContactLoop.stress within 1e-12 relative
     (the oracle adds the contact terms in another order).
   * FP32-force against FP64, one step from the same state: per-contact global force within 1e-5
-    of the contact force (contacts above 1e-6 of the largest force), per-particle net force within
+    of the contact force for contacts above 1e-4 of the largest force, and within 1e-9 of the
+    largest force below that (the FP32-force overlap is exact to ~2^-46 of the centre distance,
+    which is a growing fraction of an ever smaller overlap), per-particle net force within
     1e-5 of the particle's largest contact force (particles whose largest contact force is above
     1e-6 of the largest one: the same cut as for contacts), stress tensor within 1e-5 (Frobenius, relative),
     identical coordination number (same contact set and real flags).
@@ -91,8 +93,7 @@ def _one_step_errors(S64, S32, A):
     real = c64["real"] != 0
     F64, F32 = c64["fglob"][real], c32["fglob"][real]
     mag = np.linalg.norm(F64, axis=1)
-    big = mag > 1e-6 * mag.max()
-    rel_contact = np.linalg.norm(F64 - F32, axis=1)[big] / mag[big]
+    rel_contact = np.linalg.norm(F64 - F32, axis=1) / np.maximum(mag, 1e-4 * mag.max())
     f64, f32 = _nodes(S64)["force"], _nodes(S32)["force"]
     fmax = np.zeros(A.n_particles)
     np.maximum.at(fmax, np.concatenate([c64["id_lo"][real], c64["id_hi"][real]]), np.concatenate([mag, mag]))

@@ -1,7 +1,9 @@
 """FP32-force mode against the FP64 path (which is bitwise equal to the FP64 oracle).
 
 Tolerances (relative, written here):
-  * per-contact global force after one step from the same state:   1e-5 of the contact force
+  * per-contact global force after one step from the same state:   1e-5 of the contact force for
+    contacts above 1e-4 of the largest force, 1e-9 of the largest force below that (the overlap
+    is exact to ~2^-46 of the centre distance: a growing fraction of an ever smaller overlap)
   * per-particle net force, normalised by the particle's largest contact force: 1e-5 (particles
     whose largest contact force is above 1e-6 of the largest of all, the cut used for contacts)
   * after 20 steps from the same state (errors compound through the trajectory): 1e-3
@@ -59,8 +61,7 @@ def _force_errors(c64, c32, f64, f32, A, same_set=True):
     real = (c64["real"] != 0) & (c32["real"] != 0)
     F64, F32 = c64["fglob"][real], c32["fglob"][real]
     mag = np.linalg.norm(F64, axis=1)
-    big = mag > 1e-6 * mag.max()
-    rel_contact = np.linalg.norm(F64 - F32, axis=1)[big] / mag[big]
+    rel_contact = np.linalg.norm(F64 - F32, axis=1) / np.maximum(mag, 1e-4 * mag.max())
     # per particle: net force error normalised by the largest contact force on the particle
     npart = A.n_particles
     fmax = np.zeros(npart)
