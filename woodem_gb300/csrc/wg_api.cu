@@ -54,23 +54,7 @@ Sim::~Sim() {
     if (side.fork) cudaEventDestroy(side.fork);
     if (side.join) cudaEventDestroy(side.join);
     if (side.st) cudaStreamDestroy(side.st);
-    for (int k = 0; k < kCopyStreams; k++) {
-        if (copySt[k]) {
-            cudaStreamSynchronize(copySt[k]);
-            cudaStreamDestroy(copySt[k]);
-        }
-    }
-    for (int k = 0; k <= kCopyStreams; k++)
-        if (copyEv[k]) cudaEventDestroy(copyEv[k]);
     if (stream) cudaStreamDestroy(stream);
-}
-
-int Sim::copyStreams() {
-    Sim& S = *this;
-    if (copySt[0]) return 0;
-    for (int k = 0; k < kCopyStreams; k++) WG_CUDA_TRY(cudaStreamCreateWithFlags(&copySt[k], cudaStreamNonBlocking));
-    for (int k = 0; k <= kCopyStreams; k++) WG_CUDA_TRY(cudaEventCreateWithFlags(&copyEv[k], cudaEventDisableTiming));
-    return 0;
 }
 
 // ------------------------------------------------------------------ periodic cell (host)
@@ -1739,39 +1723,6 @@ int wg_collide_only(wg_scene* s) {
     return WG_OK;
 }
 
-namespace wg {
-// The six state arrays (pos 3, ori 4, vel 3, angVel 3, force 3, torque 3 doubles per API node)
-// between the caller's arrays and the staging buffer: each array is cut into kCopyStreams parts,
-// part k of every array goes on copy stream k, so that several copy engines move the state at
-// once; the copies start after the work queued on the simulation stream and the simulation
-// stream waits for all of them. Null arrays are skipped.
-static int copyState(Sim& S, double* stage, int64_t na, const double* const host[6], bool toDevice) {
-    const int64_t off[6] = {0, 3, 7, 10, 13, 16}, w[6] = {3, 4, 3, 3, 3, 3};
-    const int K = Sim::kCopyStreams;
-    int r = S.copyStreams();
-    if (r) return r;
-    WG_CUDA_TRY(cudaEventRecord(S.copyEv[K], S.stream));
-    for (int k = 0; k < K; k++) WG_CUDA_TRY(cudaStreamWaitEvent(S.copySt[k], S.copyEv[K], 0));
-    for (int q = 0; q < 6; q++) {
-        if (!host[q]) continue;
-        const int64_t total = w[q] * na, per = (total + K - 1) / K;
-        for (int k = 0; k < K; k++) {
-            const int64_t beg = k * per, len = std::min<int64_t>(per, total - beg);
-            if (len <= 0) continue;
-            double* dev = stage + off[q] * na + beg;
-            double* hst = const_cast<double*>(host[q]) + beg;
-            if (toDevice) WG_CUDA_TRY(cudaMemcpyAsync(dev, hst, sizeof(double) * len, cudaMemcpyHostToDevice, S.copySt[k]));
-            else WG_CUDA_TRY(cudaMemcpyAsync(hst, dev, sizeof(double) * len, cudaMemcpyDeviceToHost, S.copySt[k]));
-        }
-    }
-    for (int k = 0; k < K; k++) {
-        WG_CUDA_TRY(cudaEventRecord(S.copyEv[k], S.copySt[k]));
-        WG_CUDA_TRY(cudaStreamWaitEvent(S.stream, S.copyEv[k], 0));
-    }
-    return 0;
-}
-}  // namespace wg
-
 int wg_put_state(wg_scene* s, const double* pos, const double* ori, const double* vel, const double* ang_vel, const double* force,
                  const double* torque) {
     if (!s) return WG_ERR_ARG;
@@ -1790,16 +1741,17 @@ int wg_put_state(wg_scene* s, const double* pos, const double* ori, const double
     }
     const int64_t na = S.nApiNodes;
     const double* src[6] = {pos, ori, vel, ang_vel, force, torque};
-    // staged: copies by the copy engines (they move page-locked arrays faster than kernels
-    // reading host memory directly), then the conversion into the node slots
+    const int64_t off[6] = {0, 3, 7, 10, 13, 16}, w[6] = {3, 4, 3, 3, 3, 3};
+    // staged: one copy per array (the copy engines move page-locked arrays faster than kernels
+    // reading host memory directly; one stream already fills the host link), then the
+    // conversion into the node slots
     if (!(pos && ori && vel && ang_vel && force && torque)) {
         // fill missing components from the current device state
         k_get_state<<<(unsigned)((na + 255) / 256), 256, 0, S.stream>>>(S.N, X.dApiMap, na, stagedArrays(X.dStage, na));
     }
-    {
-        int r = copyState(S, X.dStage, na, src, true);
-        if (r) return r;
-    }
+    for (int q = 0; q < 6; q++)
+        if (src[q])
+            WG_CUDA_TRY(cudaMemcpyAsync(X.dStage + off[q] * na, src[q], sizeof(double) * w[q] * na, cudaMemcpyHostToDevice, S.stream));
     k_put_state<<<(unsigned)((na + 255) / 256), 256, 0, S.stream>>>(S.N, X.dApiMap, na, stagedArrays(X.dStage, na));
     S.fromEnds = false;  // the next step starts from the forces written here
     if (vel) S.facetsStatic = false;  // facet vertices may have been given a velocity
@@ -1822,11 +1774,8 @@ int wg_get_nodes(wg_scene* s, double* pos, double* ori, double* vel, double* ang
         return WG_OK;
     }
     k_get_state<<<(unsigned)((na + 255) / 256), 256, 0, S.stream>>>(S.N, X.dApiMap, na, stagedArrays(X.dStage, na));
-    {
-        const double* const d[6] = {dst[0], dst[1], dst[2], dst[3], dst[4], dst[5]};
-        int r = copyState(S, X.dStage, na, d, false);
-        if (r) return r;
-    }
+    for (int q = 0; q < 6; q++)
+        if (dst[q]) WG_CUDA_TRY(cudaMemcpyAsync(dst[q], X.dStage + off[q] * na, sizeof(double) * w[q] * na, cudaMemcpyDeviceToHost, S.stream));
     WG_CUDA_TRY(cudaGetLastError());
     WG_CUDA_TRY(cudaStreamSynchronize(S.stream));
     return WG_OK;

@@ -424,12 +424,6 @@ struct Sim {
     double* dEPartial = nullptr;    // EN_CON_NCOL * 256 block partials
     double* dEPrev = nullptr;       // periodic gradV work: previous stress (9) and volume
     int ensureEnergyCapacity();
-    // host <-> device copies of the state (wg_put_state / wg_get_nodes), each array split over
-    // several streams so that several copy engines move it at once (created at the first use)
-    static constexpr int kCopyStreams = 4;
-    cudaStream_t copySt[kCopyStreams] = {};
-    cudaEvent_t copyEv[kCopyStreams + 1] = {};
-    int copyStreams();
     // timing
     std::vector<cudaEvent_t> evPool;  // per queued step: before Leapfrog, before contacts, after
     cudaEvent_t ev[8];
