@@ -589,7 +589,8 @@ def measure_serving(args):
     def make_peri(n, seed):
         m = materials(seed)
         return scenes.periodic_shear(n=n, seed=seed % 100000, rmin=m["radius"] / 2, rmax=m["radius"], young=m["young"],
-                                     tanPhi=m["tanPhi"], damping=m["damping"], fill_fraction=0.3, shear_rate=1.0, precision=prec)
+                                     tanPhi=m["tanPhi"], damping=m["damping"], fill_fraction=0.3, shear_rate=1.0, precision=prec,
+                                     pack_device=True)
 
     def peri_phases(n, steps, seed):
         # the first 30 % of the steps compress the cell isotropically from 0.30 to 0.55 solid

@@ -283,6 +283,15 @@ const char* wg_broadphase_noalloc_error(void);
    params[2], clipped at z <= params[3]; 2: periodic box lo..hi. Returns the number placed. */
 int64_t wg_pack_rsa(int64_t n, const double* radii, const double* lo, const double* hi, int32_t region_kind,
                     const double* params, uint64_t seed, int64_t max_attempts, double* centers);
+/* The same insertion on the current device, in rounds over a window of the lowest-indexed
+   unplaced spheres: every sphere of the window draws a candidate (a hash of seed, index and
+   attempt), a candidate clear of the placed spheres is accepted unless it overlaps the clear
+   candidate of a lower-indexed sphere of its round, the others draw again. Arguments and result
+   as wg_pack_rsa (the prefix of spheres before the first that found no place in max_attempts);
+   the packing is a sequential insertion of its own, not wg_pack_rsa's sphere for sphere.
+   -1: CUDA error, -2: invalid argument. */
+int64_t wg_pack_rsa_device(int64_t n, const double* radii, const double* lo, const double* hi, int32_t region_kind,
+                           const double* params, uint64_t seed, int64_t max_attempts, double* centers);
 
 #ifdef __cplusplus
 }

@@ -127,6 +127,24 @@ def test_pack_rsa_non_overlapping(gpu_lib):
     assert np.all(c - r[:, None] >= -1e-15) and np.all(c + r[:, None] <= 0.2 + 1e-15)
 
 
+def test_pack_rsa_device_rejects_arguments(gpu_lib):
+    """wg_pack_rsa_device validates its arguments before any device call: -2 for a bad region
+    kind, a non-positive radius, an empty box or a missing cylinder description."""
+    from woodem_gb300 import _native
+    r = np.full(10, 1e-3)
+    out = np.zeros((10, 3))
+    lo, hi = np.zeros(3), np.full(3, 0.1)
+    P = _native.ptr
+
+    def call(radii, lo_, hi_, kind, params):
+        return gpu_lib.wg_pack_rsa_device(len(radii), P(radii), P(lo_), P(hi_), kind, params, 1, 100, P(out))
+    assert call(r, lo, hi, 3, P(np.zeros(4))) == -2
+    assert call(np.r_[r[:9], -1.0], lo, hi, 0, P(np.zeros(4))) == -2
+    assert call(r, lo, lo, 0, P(np.zeros(4))) == -2
+    assert call(r, lo, hi, 1, None) == -2
+    assert gpu_lib.wg_pack_rsa_device(0, P(r), P(lo), P(hi), 0, P(np.zeros(4)), 1, 100, P(out)) == 0
+
+
 def test_quadrilateral_mesh():
     """py/triangulated.py:70-83: 2*div0*div1 facets covering the quadrilateral, vertices shared."""
     ff = triangulated.quadrilateral((0, 0, 0), (2, 0, 0), (0, 3, 0), (2, 3, 0), div=(4, 3))

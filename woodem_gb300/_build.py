@@ -25,6 +25,7 @@ UNITS = {
     "wg_step32.cu": ["--fmad=true", "-Xcompiler", "-ffp-contract=fast"],
     "wg_noalloc.cu": ["--fmad=false"],
     "wg_pack.cpp": [],
+    "wg_pack_gpu.cu": ["--fmad=false"],
 }
 
 

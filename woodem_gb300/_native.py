@@ -125,6 +125,7 @@ def lib():
         "wg_broadphase_noalloc": (C.c_int, [C.c_int32, P_D, P_D, P_U32, C.c_uint32, C.c_int64, P_I32, P_I32, P_I64]),
         "wg_broadphase_noalloc_error": (C.c_char_p, []),
         "wg_pack_rsa": (C.c_int64, [C.c_int64, P_D, P_D, P_D, C.c_int32, P_D, C.c_uint64, C.c_int64, P_D]),
+        "wg_pack_rsa_device": (C.c_int64, [C.c_int64, P_D, P_D, P_D, C.c_int32, P_D, C.c_uint64, C.c_int64, P_D]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

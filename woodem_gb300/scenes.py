@@ -15,8 +15,11 @@ from .core import Scene
 from .dem import DemField, FrictMat, Cp2_FrictMat_HertzPhys, Law2_L6Geom_HertzPhys_DMT
 
 
-def pack_rsa(radii, lo, hi, region=0, params=(0, 0, 0, 0), seed=0, max_attempts=2000):
-    """Seeded random sequential insertion (largest spheres first). Returns centers in input order."""
+def pack_rsa(radii, lo, hi, region=0, params=(0, 0, 0, 0), seed=0, max_attempts=2000, device=False):
+    """Seeded random sequential insertion (largest spheres first). Returns centers in input order.
+    ``device``: insert on the current GPU (wg_pack_rsa_device, rounds over a window of spheres)
+    instead of the host (wg_pack_rsa); both give valid packings of the same statistics, not the
+    same one."""
     radii = np.ascontiguousarray(radii, dtype=float)
     order = np.argsort(-radii, kind="stable")
     r_sorted = np.ascontiguousarray(radii[order])
@@ -24,8 +27,11 @@ def pack_rsa(radii, lo, hi, region=0, params=(0, 0, 0, 0), seed=0, max_attempts=
     lo = np.ascontiguousarray(lo, dtype=float)
     hi = np.ascontiguousarray(hi, dtype=float)
     pr = np.ascontiguousarray(params, dtype=float)
-    n = _native.lib().wg_pack_rsa(len(radii), _native.ptr(r_sorted), _native.ptr(lo), _native.ptr(hi), int(region),
-                                  _native.ptr(pr), int(seed), int(max_attempts), _native.ptr(out))
+    fn = _native.lib().wg_pack_rsa_device if device else _native.lib().wg_pack_rsa
+    n = fn(len(radii), _native.ptr(r_sorted), _native.ptr(lo), _native.ptr(hi), int(region), _native.ptr(pr), int(seed),
+           int(max_attempts), _native.ptr(out))
+    if n < 0:
+        raise RuntimeError("device random insertion failed (%s)" % ("CUDA error" if n == -1 else "invalid argument"))
     if n != len(radii):
         raise RuntimeError("random insertion placed only %d of %d spheres; enlarge the region" % (n, len(radii)))
     res = np.empty_like(out)
@@ -236,21 +242,22 @@ def _sphere_nodes(S, col, value=None):
 
 def periodic_shear(n=200_000, seed=0, rmin=2e-3, rmax=4e-3, density=2600.0, young=5e7, tanPhi=0.4, ktDivKn=0.2,
                    fill_fraction=0.35, shear_rate=1.0, damping=0.2, verletRel=0.1, precision="fp64", compress_steps=0,
-                   compress_rate=None, centers=None, compress_to=0.55):
+                   compress_rate=None, centers=None, compress_to=0.55, pack_device=False):
     """Periodic simple shear: ``n`` spheres with radii uniform in [rmin, rmax] placed by seeded random
     sequential insertion in a periodic cube sized to solid fraction ``fill_fraction``; IdealElPl
     contacts, Leapfrog damping ``damping``, dt = 0.3*pWaveDt, verletDist = 0.1*rmin,
     Cell.homoDeform = HomoGradV2. With ``compress_steps`` the cell is first compressed isotropically
     (nextGradV = -compress_rate*I, by default the rate that brings the fill to ``compress_to`` in
     that many steps); then nextGradV is set to the simple shear with xz component ``shear_rate``. Given
-    ``centers``, those positions are used instead of the random insertion (a state to restore)."""
+    ``centers``, those positions are used instead of the random insertion (a state to restore);
+    ``pack_device`` makes the insertion on the GPU (``pack_rsa(device=True)``)."""
     from .core import Cell
     rng = np.random.default_rng(seed)
     radii = rng.uniform(rmin, rmax, n)
     vol = float(np.sum((4 / 3.0) * math.pi * radii ** 3))
     side = (vol / fill_fraction) ** (1 / 3.0)
     if centers is None:
-        centers = pack_rsa(radii, (0, 0, 0), (side, side, side), region=2, seed=seed + 11)
+        centers = pack_rsa(radii, (0, 0, 0), (side, side, side), region=2, seed=seed + 11, device=pack_device)
     S = Scene(fields=[DemField(gravity=(0, 0, 0))])
     S.gpu.precision = precision
     S.periodic = True
