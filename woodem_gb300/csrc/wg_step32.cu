@@ -793,63 +793,6 @@ __global__ void __launch_bounds__(256, MINB) k_contact_ss32p(DevNodes N, DevPart
     stepTicket(dFlags, dStep, ticketTotal);
 }
 
-// every load of packed contact j whose item is `it` (state, flags, the two mirror records)
-__device__ __forceinline__ void ssLoad(SSIn& x, const int4 it, int64_t j, const DevNodes& N, const DevPackedSS& K, int loadFt) {
-    x.it = it;
-    x.pf = K.flags[j];
-#pragma unroll
-    for (int q = 0; q < CF_NCOL; q++) x.st[q] = K.col[q][j];
-    x.ft1o = 0.;
-    x.ft2o = 0.;
-    if (loadFt) {
-        x.ft1o = K.ft[0][j];
-        x.ft2o = K.ft[1][j];
-    }
-    x.ma = N.mir[it.x];
-    x.mb = N.mir[it.y];
-    x.wza = N.wz[it.x];
-    x.wzb = N.wz[it.y];
-}
-
-// The resident grid software-pipelined two deep: while a thread evaluates contact j, the state
-// and mirror records of its next contact (j + stride) are in flight, and the item of the one
-// after that (j + 2 stride), on which those gathers depend.
-template <bool ENERGY>
-__global__ void __launch_bounds__(128, 3) k_contact_ss32q(DevNodes N, DevParticles P, DevContacts C, DevIncidence I, DevPackedSS K,
-                                                          const double4_32a* __restrict__ mats, const ScenePar* __restrict__ spp,
-                                                          long long* __restrict__ dStep, int* __restrict__ dFlags, int64_t nm,
-                                                          int haltBlock, int loadFt, int ticketTotal, EnergyCols E) {
-    const long long stepAbs = *dStep;
-    if (dFlags[FL_FULL] || halted(dFlags)) {  // the same for every thread of the grid
-        if (haltBlock && blockIdx.x == 0 && threadIdx.x == 0) dFlags[FL_HALT] = 1;
-        return;
-    }
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (j < K.n) {
-        const int4 zero = make_int4(0, 0, 0, 0);
-        int4 it1 = j + stride < K.n ? K.item[j + stride] : zero;
-        SSIn x;
-        ssLoad(x, K.item[j], j, N, K, loadFt);
-        for (;;) {
-            const int64_t jn = j + stride;
-            const bool more = jn < K.n;
-            SSIn y;
-            int4 it2 = zero;
-            if (more) {
-                if (jn + stride < K.n) it2 = K.item[jn + stride];
-                ssLoad(y, it1, jn, N, K, loadFt);
-            }
-            ssContact<ENERGY>(x, j, N, P, C, I, K, mats, spp, stepAbs, dFlags, nm, E);
-            if (!more) break;
-            x = y;
-            it1 = it2;
-            j = jn;
-        }
-    }
-    stepTicket(dFlags, dStep, ticketTotal);
-}
-
 __global__ void k_pack_ss(DevContacts C, DevIncidence I, DevParticles P, DevPackedSS K, int64_t nm, int copyFt) {
     const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= K.n) return;
@@ -1272,22 +1215,16 @@ static int smCount() {
 }
 
 // sphere-sphere range: block > 0 one contact per thread with that many threads per block;
-// block -256 the resident-grid kernel with prefetch (256 threads per block); block -128 the
-// resident grid pipelined two deep (128 threads per block)
+// block < 0 the resident-grid kernel with prefetch (256 threads per block)
 // Returns true when the launch also advances the step counter (advance requested and possible).
 // grid of the resident sphere-sphere kernel (block < 0), or 0 for the one-contact-per-thread kernel
 static int ssGrid(const DevPackedSS& K, int block, int blocksPerSM) {
-    if (block == -128) return (int)std::min<int64_t>((K.n + 127) / 128, (int64_t)blocksPerSM * smCount());
     return block < 0 ? (int)std::min<int64_t>((K.n + 255) / 256, (int64_t)blocksPerSM * smCount()) : 0;
 }
 template <bool ENERGY>
 static void launchSS(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C, const DevIncidence& I,
                      const DevPackedSS& K, const double4_32a* mats, const ScenePar* sp, long long* dStep, int* dFlags, int64_t nm,
                      int halt, int loadFt, int block, int grid, int ticketTotal, const EnergyCols& E) {
-    if (block == -128) {
-        k_contact_ss32q<ENERGY><<<(unsigned)grid, 128, 0, st>>>(N, P, C, I, K, mats, sp, dStep, dFlags, nm, halt, loadFt, ticketTotal, E);
-        return;
-    }
     if (block < 0) {
         k_contact_ss32p<kSSMinBlocks, ENERGY><<<(unsigned)grid, 256, 0, st>>>(N, P, C, I, K, mats, sp, dStep, dFlags, nm, halt, loadFt,
                                                                               ticketTotal, E);
