@@ -147,11 +147,12 @@ def test_errors_are_raised(gpu_lib):
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])
 def test_call_granularity_is_invisible(prec):
     """The step loop queues steps in chunks and resumes after each collider run; running 400 steps
-    in one call, in calls of 1 and 37 steps, or one step at a time through wg_run_host (state
-    copied out and back in every step, from pageable or page-locked arrays) gives bitwise the
-    same state."""
+    in one call, in calls of 1 and 37 steps, or through wg_run_host (state copied out and back in
+    every call, from pageable or page-locked arrays; with page-locked arrays the kinematic state
+    is copied out while the last contact loop of the call runs), one step or five steps per call,
+    gives bitwise the same state, and the arrays hold the state wg_get_nodes reads after the call."""
     out = []
-    for mode in ("one", "steps", "host", "pinned"):
+    for mode in ("one", "steps", "host", "pinned", "pinned5"):
         S = scenes.box_settle_small(n=1200, seed=5, precision=prec)
         if mode == "one":
             S.run(400)
@@ -177,17 +178,24 @@ def test_call_granularity_is_invisible(prec):
                 cuts = np.cumsum([0, 3, 4, 3, 3, 3, 3]) * na
                 parts = [buf[cuts[q]:cuts[q + 1]] for q in range(6)]
             sim.H.check(L.wg_get_nodes(h, *[_native.ptr(x) for x in parts]), "get_nodes")
-            for _ in range(399):
-                sim.H.check(L.wg_run_host(h, 1, *[_native.ptr(x) for x in parts]), "run_host")
+            calls = [1] * 399 if mode != "pinned5" else [5] * 79 + [1] * 4
+            for c in calls:
+                sim.H.check(L.wg_run_host(h, c, *[_native.ptr(x) for x in parts]), "run_host")
+            held = [x.copy() for x in parts]
             if pinned:
                 L.wg_host_free(pinned)
         g = _gpu_nodes(S)
+        if mode in ("host", "pinned", "pinned5"):
+            for x, k in zip(held, ("pos", "ori", "vel", "angVel", "force", "torque")):
+                if k != "ori":
+                    assert np.array_equal(x.reshape(g[k].shape), g[k]), "%s: the arrays after wg_run_host (%s)" % (k, mode)
         S.close()
         out.append(g)
     for k in ("pos", "vel", "angVel", "force", "torque"):
         assert np.array_equal(out[0][k], out[1][k]), "%s: one call vs many" % k
         assert np.array_equal(out[0][k], out[2][k]), "%s: one call vs host round trips" % k
         assert np.array_equal(out[0][k], out[3][k]), "%s: one call vs round trips through page-locked arrays" % k
+        assert np.array_equal(out[0][k], out[4][k]), "%s: one call vs five-step calls through page-locked arrays" % k
 
 
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])

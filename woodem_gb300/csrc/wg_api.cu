@@ -54,6 +54,11 @@ Sim::~Sim() {
     if (side.fork) cudaEventDestroy(side.fork);
     if (side.join) cudaEventDestroy(side.join);
     if (side.st) cudaStreamDestroy(side.st);
+    if (earlySt) {
+        cudaStreamSynchronize(earlySt);
+        cudaStreamDestroy(earlySt);
+    }
+    if (earlyFork) cudaEventDestroy(earlyFork);
     if (stream) cudaStreamDestroy(stream);
 }
 
@@ -209,29 +214,58 @@ __global__ void k_put_state(DevNodes N, const int32_t* __restrict__ map, int64_t
     N.force[s] = make_double4_32a(f[3 * a], f[3 * a + 1], f[3 * a + 2], 0.);
     N.torque[s] = make_double4_32a(t[3 * a], t[3 * a + 1], t[3 * a + 2], 0.);
 }
-__global__ void k_get_state(DevNodes N, const int32_t* __restrict__ map, int64_t na, StateArrays A) {
+// part 0: the whole state; 1: position, orientation, velocity, angular velocity; 2: force, torque
+__global__ void k_get_state(DevNodes N, const int32_t* __restrict__ map, int64_t na, StateArrays A, int part = 0) {
     const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= na) return;
     const int s = map[a];
     if (s < 0) return;
-    double* pos = A.pos;
-    double* ori = A.ori;
-    double* vel = A.vel;
-    double* av = A.av;
-    double* f = A.f;
-    double* t = A.t;
-    const double4_32a p = N.posr[s], v = N.vel[s], w = N.angv[s], ff = N.force[s], tt = N.torque[s];
-    double4_32a o;
-    if (N.orif) {
-        const float4 q = N.orif[s];
-        o = make_double4_32a(q.x, q.y, q.z, q.w);
-    } else o = N.ori[s];
-    pos[3 * a] = p.x; pos[3 * a + 1] = p.y; pos[3 * a + 2] = p.z;
-    ori[4 * a] = o.x; ori[4 * a + 1] = o.y; ori[4 * a + 2] = o.z; ori[4 * a + 3] = o.w;
-    vel[3 * a] = v.x; vel[3 * a + 1] = v.y; vel[3 * a + 2] = v.z;
-    av[3 * a] = w.x; av[3 * a + 1] = w.y; av[3 * a + 2] = w.z;
-    f[3 * a] = ff.x; f[3 * a + 1] = ff.y; f[3 * a + 2] = ff.z;
-    t[3 * a] = tt.x; t[3 * a + 1] = tt.y; t[3 * a + 2] = tt.z;
+    if (part != 2) {
+        double* pos = A.pos;
+        double* ori = A.ori;
+        double* vel = A.vel;
+        double* av = A.av;
+        const double4_32a p = N.posr[s], v = N.vel[s], w = N.angv[s];
+        double4_32a o;
+        if (N.orif) {
+            const float4 q = N.orif[s];
+            o = make_double4_32a(q.x, q.y, q.z, q.w);
+        } else o = N.ori[s];
+        pos[3 * a] = p.x; pos[3 * a + 1] = p.y; pos[3 * a + 2] = p.z;
+        ori[4 * a] = o.x; ori[4 * a + 1] = o.y; ori[4 * a + 2] = o.z; ori[4 * a + 3] = o.w;
+        vel[3 * a] = v.x; vel[3 * a + 1] = v.y; vel[3 * a + 2] = v.z;
+        av[3 * a] = w.x; av[3 * a + 1] = w.y; av[3 * a + 2] = w.z;
+    }
+    if (part != 1) {
+        double* f = A.f;
+        double* t = A.t;
+        const double4_32a ff = N.force[s], tt = N.torque[s];
+        f[3 * a] = ff.x; f[3 * a + 1] = ff.y; f[3 * a + 2] = ff.z;
+        t[3 * a] = tt.x; t[3 * a + 1] = tt.y; t[3 * a + 2] = tt.z;
+    }
+}
+
+// The early part of wg_run_host's copy-out (see Sim::earlyOut), issued right after the run's
+// last Leapfrog is queued: the early stream waits for it, converts the kinematic state into the
+// staging buffer and copies it to the caller's arrays. The contact loop that follows reads that
+// state and writes none of it.
+int Sim::issueEarlyGet() {
+    Sim& S = *this;
+    SimEx& X = static_cast<SimEx&>(*this);
+    if (!earlySt) {
+        WG_CUDA_TRY(cudaStreamCreateWithFlags(&earlySt, cudaStreamNonBlocking));
+        WG_CUDA_TRY(cudaEventCreateWithFlags(&earlyFork, cudaEventDisableTiming));
+    }
+    const int64_t na = nApiNodes;
+    const int64_t off[4] = {0, 3, 7, 10}, w[4] = {3, 4, 3, 3};
+    WG_CUDA_TRY(cudaEventRecord(earlyFork, stream));
+    WG_CUDA_TRY(cudaStreamWaitEvent(earlySt, earlyFork, 0));
+    k_get_state<<<(unsigned)((na + 255) / 256), 256, 0, earlySt>>>(N, X.dApiMap, na, stagedArrays(X.dStage, na), 1);
+    for (int q = 0; q < 4; q++)
+        if (earlyOut[q])
+            WG_CUDA_TRY(cudaMemcpyAsync(earlyOut[q], X.dStage + off[q] * na, sizeof(double) * w[q] * na, cudaMemcpyDeviceToHost, earlySt));
+    earlyIssued = true;
+    return 0;
 }
 
 int Sim::ensureContactCapacity(int64_t need) {
@@ -1024,6 +1058,9 @@ int Sim::run(int64_t n) {
         int64_t k = std::min<int64_t>(n - done, maxChunk);
         // dt may change after a step (Scene.nextDt, DynDt): such a step ends its chunk
         if (std::isfinite(nextDt)) k = 1;
+        // wg_run_host's early copy-out: the run's last step gets a chunk of its own, whose first
+        // Leapfrog always runs (a halt only stops the steps after a full-run request)
+        if (earlyWanted && !earlyIssued && done < n - 1) k = std::min<int64_t>(k, n - 1 - done);
         if (batchDyn) {
             // the same for every scene of a batch, with the scene's own step, time and dt
             for (int q = 0; q < nScenes; q++) {
@@ -1073,7 +1110,8 @@ int Sim::run(int64_t n) {
         const int64_t s0 = step;
         // a chunk that starts from the end slots and is not due for a full run is replayed as a
         // CUDA graph (re-captured after every full run, whose contact arrays it refers to)
-        const bool graphChunk = useGraph && fromEnds && !needFull && k == maxChunk && !cfg.periodic;
+        const bool lastEarly = earlyWanted && !earlyIssued && done + k == n && k == 1;
+        const bool graphChunk = useGraph && fromEnds && !needFull && k == maxChunk && !cfg.periodic && !lastEarly;
         if (graphChunk) {
             if (!graphExec || graphSteps != k || graphEpoch != nFullRuns) {
                 if (graphExec) cudaGraphExecDestroy(graphExec);
@@ -1102,6 +1140,10 @@ int Sim::run(int64_t n) {
                 WG_CUDA_TRY(cudaEventRecord(E[3 * j], stream));
                 stepLeapfrog(j == 0 ? (fromEnds ? 1 : 0) : 1, spOf(j));
                 WG_CUDA_TRY(cudaEventRecord(E[3 * j + 1], stream));
+                if (lastEarly) {
+                    int r = issueEarlyGet();
+                    if (r) return r;
+                }
                 stepContact(spOf(j));
                 WG_CUDA_TRY(cudaEventRecord(E[3 * j + 2], stream));
             }
@@ -1773,7 +1815,8 @@ int wg_get_nodes(wg_scene* s, double* pos, double* ori, double* vel, double* ang
             if (dst[q]) std::memcpy(dst[q], S.hApi.data() + off[q] * na, sizeof(double) * w[q] * na);
         return WG_OK;
     }
-    k_get_state<<<(unsigned)((na + 255) / 256), 256, 0, S.stream>>>(S.N, X.dApiMap, na, stagedArrays(X.dStage, na));
+    const int part = (pos || ori || vel || ang_vel) ? ((force || torque) ? 0 : 1) : 2;
+    k_get_state<<<(unsigned)((na + 255) / 256), 256, 0, S.stream>>>(S.N, X.dApiMap, na, stagedArrays(X.dStage, na), part);
     for (int q = 0; q < 6; q++)
         if (dst[q]) WG_CUDA_TRY(cudaMemcpyAsync(dst[q], X.dStage + off[q] * na, sizeof(double) * w[q] * na, cudaMemcpyDeviceToHost, S.stream));
     WG_CUDA_TRY(cudaGetLastError());
@@ -1781,12 +1824,44 @@ int wg_get_nodes(wg_scene* s, double* pos, double* ori, double* vel, double* ang
     return WG_OK;
 }
 
+namespace {
+bool pageLocked(const void* p) {
+    cudaPointerAttributes a;
+    if (!p) return true;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+}  // namespace
+
 int wg_run_host(wg_scene* s, int64_t n_steps, double* pos, double* ori, double* vel, double* ang_vel, double* force, double* torque) {
     int r = wg_put_state(s, pos, ori, vel, ang_vel, force, torque);
     if (r) return r;
+    Sim& S = *SIM(s);
+    // with page-locked arrays the kinematic state leaves during the last contact loop (an async
+    // copy into pageable memory would hold the host until it is done)
+    if (n_steps < 1 || !(pageLocked(pos) && pageLocked(ori) && pageLocked(vel) && pageLocked(ang_vel))) {
+        r = wg_run(s, n_steps);
+        if (r) return r;
+        return wg_get_nodes(s, pos, ori, vel, ang_vel, force, torque);
+    }
+    double* early[4] = {pos, ori, vel, ang_vel};
+    for (int q = 0; q < 4; q++) S.earlyOut[q] = early[q];
+    S.earlyWanted = true;
+    S.earlyIssued = false;
     r = wg_run(s, n_steps);
+    const bool issued = S.earlyIssued;
+    S.earlyWanted = false;
+    S.earlyIssued = false;
+    for (int q = 0; q < 4; q++) S.earlyOut[q] = nullptr;
+    // the caller's arrays are not touched after return: the early copies end here, failed run or not
+    const cudaError_t e = issued ? cudaStreamSynchronize(S.earlySt) : cudaSuccess;
     if (r) return r;
-    return wg_get_nodes(s, pos, ori, vel, ang_vel, force, torque);
+    if (e != cudaSuccess) return S.fail(WG_ERR_CUDA, cudaGetErrorString(e));
+    if (!issued) return wg_get_nodes(s, pos, ori, vel, ang_vel, force, torque);
+    return wg_get_nodes(s, nullptr, nullptr, nullptr, nullptr, force, torque);
 }
 
 int wg_set_dt(wg_scene* s, double dt, double next_dt) {

@@ -429,6 +429,14 @@ struct Sim {
     cudaEvent_t ev[8];
     double lastTotalMs = 0, phaseMs[4] = {0, 0, 0, 0};
     int64_t lastLaunches = 0;
+    // wg_run_host: the node state the last Leapfrog of a run leaves (position, orientation,
+    // velocity, angular velocity) is copied to the caller's page-locked arrays on a stream of its
+    // own while that step's contact loop runs; earlyOut are those arrays (null: not wanted)
+    cudaStream_t earlySt = nullptr;
+    cudaEvent_t earlyFork = nullptr;
+    double* earlyOut[4] = {nullptr, nullptr, nullptr, nullptr};
+    bool earlyWanted = false, earlyIssued = false;
+    int issueEarlyGet();
 
     ~Sim();
     void* dalloc(size_t bytes);
