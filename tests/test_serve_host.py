@@ -99,3 +99,15 @@ def test_latency_stats_and_poisson_stream():
     assert [(j.n, j.steps, j.arrival, j.periodic) for j in a] == [(j.n, j.steps, j.arrival, j.periodic) for j in b]
     assert all(0 <= j.arrival < 10.0 for j in a) and all(2000 <= j.steps <= 5000 for j in a)
     assert all(2000 <= j.n <= 30000 + 6 for j in a)
+
+
+def test_failed_periodic_job_stops_the_server():
+    """A periodic job whose scene cannot be built (its build raises in the worker thread) stops
+    the serving loop with an error instead of leaving the job unfinished and its HBM reserved."""
+    def bad_build():
+        raise RuntimeError("no room for the spheres")
+    jobs = [serve.Job(0, (lambda: Desc(100)), 100, 10, 0.0),
+            serve.Job(1, bad_build, 1000, 10, 0.0, periodic=True)]
+    srv = serve.Server(FakePool([200, 200]), tick=5, clock="ticks")
+    with pytest.raises(RuntimeError, match="periodic job failed"):
+        srv.run(jobs)

@@ -4,7 +4,8 @@
 // SpherePack::makeCloud (lib/sphere-pack/SpherePack.hpp:75) for the regions of the benchmark
 // scenes. The host version places sphere i (in the given order) at the first of up to
 // max_attempts uniform candidate centres that overlaps no sphere placed before it. Here the
-// spheres are inserted in rounds over a window of the lowest-indexed unplaced spheres:
+// spheres are inserted in rounds over a window of the lowest-indexed unplaced spheres (1/64 of
+// the spheres, at least 256 and at most 32768):
 //   1. every sphere of the window draws its next candidate centre (a counter-based hash of the
 //      seed, the sphere index and the attempt number, so the result does not depend on the
 //      launch shape) and tests it against the spheres placed in earlier rounds;
@@ -150,14 +151,16 @@ __global__ void k_rsa_resolve(PackGrid G, int64_t w0, int64_t w1, const double* 
 // round step 3: accepted spheres join the placed set (their round-list links are dead after
 // the round; the placed set keeps its own links)
 __global__ void k_rsa_commit(PackGrid G, int64_t w0, int64_t w1, int32_t* __restrict__ state, const double* __restrict__ cand,
-                             const int32_t* __restrict__ accepted, double* __restrict__ pos, int32_t* __restrict__ headP,
-                             int32_t* __restrict__ nextP) {
+                             const int32_t* __restrict__ clear, const int32_t* __restrict__ accepted, double* __restrict__ pos,
+                             int32_t* __restrict__ headP, int32_t* __restrict__ nextP, int32_t* __restrict__ headR) {
     const int64_t i = w0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= w1 || !accepted[i]) return;
+    if (i >= w1 || !clear[i]) return;
     const double c[3] = {cand[3 * i], cand[3 * i + 1], cand[3 * i + 2]};
-    for (int k = 0; k < 3; k++) pos[3 * i + k] = c[k];
     int ci[3];
     const int cell = cellOf(G, c, ci);
+    headR[cell] = -1;  // the round lists end with the round (every clear candidate clears its cell)
+    if (!accepted[i]) return;
+    for (int k = 0; k < 3; k++) pos[3 * i + k] = c[k];
     nextP[i] = atomicExch(headP + cell, (int32_t)i);
     state[i] = 1;
 }
@@ -239,21 +242,26 @@ int64_t wg_pack_rsa_device(int64_t n, const double* radii, const double* lo, con
     bool ok = cudaMemcpyAsync(dRad, radii, sizeof(double) * n, cudaMemcpyHostToDevice, st) == cudaSuccess &&
               cudaMemsetAsync(dState, 0, sizeof(int32_t) * n, st) == cudaSuccess &&
               cudaMemsetAsync(dAtt, 0, sizeof(int64_t) * n, st) == cudaSuccess &&
-              cudaMemsetAsync(dHeadP, 0xff, sizeof(int32_t) * ncell, st) == cudaSuccess;
+              cudaMemsetAsync(dHeadP, 0xff, sizeof(int32_t) * ncell, st) == cudaSuccess &&
+              cudaMemsetAsync(dHeadR, 0xff, sizeof(int32_t) * ncell, st) == cudaSuccess;
     if (!ok) return -1;
-    // the window: the unplaced spheres of [w0, w1), w1 - w0 at most kWindow; after each round the
-    // state of the window comes back to the host, which moves w0 past the placed prefix and
-    // stops at the first sphere that found no place
-    const int64_t kWindow = 32768;
-    std::vector<int32_t> hState((size_t)std::min<int64_t>(n, kWindow));
+    // the window: the unplaced spheres of [w0, w1), w1 - w0 at most W, a small fraction of the
+    // spheres so that the window holds spheres of similar rank (the insertion order puts the
+    // largest first: a window of all spheres would let small ones fill the gaps the large ones
+    // need); after every few rounds the state of the window comes back to the host, which moves w0
+    // past the placed prefix and stops at the first sphere that found no place
+    const int64_t W = std::min<int64_t>(32768, std::max<int64_t>(256, n / 64));
+    const int kRoundsPerCheck = 4;
+    std::vector<int32_t> hState((size_t)std::min<int64_t>(n, W));
     int64_t w0 = 0, prefix = n;
     while (w0 < n) {
-        const int64_t w1 = std::min<int64_t>(n, w0 + kWindow);
+        const int64_t w1 = std::min<int64_t>(n, w0 + W);
         const unsigned g = (unsigned)((w1 - w0 + 255) / 256);
-        if (cudaMemsetAsync(dHeadR, 0xff, sizeof(int32_t) * ncell, st) != cudaSuccess) return -1;
-        k_rsa_draw<<<g, 256, 0, st>>>(G, w0, w1, dRad, seed, dState, dAtt, dCand, dClear, dHeadP, dNextP, dPos, dHeadR, dNextR);
-        k_rsa_resolve<<<g, 256, 0, st>>>(G, w0, w1, dRad, max_attempts, dState, dAtt, dCand, dClear, dHeadR, dNextR, dAcc);
-        k_rsa_commit<<<g, 256, 0, st>>>(G, w0, w1, dState, dCand, dAcc, dPos, dHeadP, dNextP);
+        for (int round = 0; round < kRoundsPerCheck; round++) {
+            k_rsa_draw<<<g, 256, 0, st>>>(G, w0, w1, dRad, seed, dState, dAtt, dCand, dClear, dHeadP, dNextP, dPos, dHeadR, dNextR);
+            k_rsa_resolve<<<g, 256, 0, st>>>(G, w0, w1, dRad, max_attempts, dState, dAtt, dCand, dClear, dHeadR, dNextR, dAcc);
+            k_rsa_commit<<<g, 256, 0, st>>>(G, w0, w1, dState, dCand, dClear, dAcc, dPos, dHeadP, dNextP, dHeadR);
+        }
         if (cudaMemcpyAsync(hState.data(), dState + w0, sizeof(int32_t) * (w1 - w0), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
             cudaStreamSynchronize(st) != cudaSuccess)
             return -1;

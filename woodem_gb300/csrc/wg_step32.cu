@@ -561,7 +561,14 @@ __device__ __forceinline__ void stepTicket(int* dFlags, long long* dStep, int to
 // One sphere-sphere contact of an aperiodic scene (packed position j): Cg2_Sphere_Sphere_L6Geom,
 // Cp2 on creation, Law2, the two end slots and the packed state. FP32 arithmetic throughout
 // except the IdealElPl shear accumulation (FP64) and contact creation.
-template <bool ENERGY>
+// store of a packed-state word: CS marks it evict-first in L2 (the state streams through once
+// per step; the mirror records gathered by every contact should stay)
+template <bool CS, class T>
+__device__ __forceinline__ void stState(T* p, T v) {
+    if constexpr (CS) __stcs(p, v);
+    else *p = v;
+}
+template <bool ENERGY, bool CS = false>
 __device__ __forceinline__ void ssContact(const SSIn& x, int64_t j, const DevNodes& N, const DevParticles& P, const DevContacts& C,
                                           const DevIncidence& I, const DevPackedSS& K, const double4_32a* __restrict__ mats,
                                           const ScenePar* __restrict__ spp, long long stepAbs, int* dFlags, int64_t nm,
@@ -579,14 +586,14 @@ __device__ __forceinline__ void ssContact(const SSIn& x, int64_t j, const DevNod
     uint32_t fl = fl0;
     if (fl & C_REMOVED) return;
     if ((fl & C_PENDING) && !pendingStays(P, A, B, false, nullptr, dErr)) {
-        K.flags[j] = ((fl & ~C_PENDING) | C_REMOVED) | hiBits;
+        stState<CS>(&K.flags[j], (uint32_t)(((fl & ~C_PENDING) | C_REMOVED) | hiBits));
         return;
     }
     fl &= ~C_PENDING;
     const bool real = fl & C_REAL;
     SSGeo g;
     if (!geomSS32(x.ma, x.mb, x.wza, x.wzb, sp.ssDfAbsF, real, g)) {
-        if (fl != fl0) K.flags[j] = fl | hiBits;
+        if (fl != fl0) stState<CS>(&K.flags[j], (uint32_t)(fl | hiBits));
         return;
     }
     const float dtf = sp.dtF;
@@ -601,16 +608,16 @@ __device__ __forceinline__ void ssContact(const SSIn& x, int64_t j, const DevNod
     if (!real) {
         frameInit(n, f);
         physCreate(spp, (int)(pf >> 8), r1, r2, uN, mats[P.mat[A]], mats[P.mat[B]], N.minert[A].w, N.minert[B].w, ph0, ph1, ph2, ph3);
-        K.col[CF_P0][j] = ph0;
-        K.col[CF_P1][j] = ph1;
-        K.col[CF_P2][j] = ph2;
-        K.col[CF_P3][j] = ph3;
+        stState<CS>(&K.col[CF_P0][j], ph0);
+        stState<CS>(&K.col[CF_P1][j], ph1);
+        stState<CS>(&K.col[CF_P2][j], ph2);
+        stState<CS>(&K.col[CF_P3][j], ph3);
         C.step0[I.work[nm + j].x] = (int32_t)step;
         ft1o = 0.;
         ft2o = 0.;
         if (sp.law == 0) {
-            K.ft[0][j] = 0.;
-            K.ft[1][j] = 0.;
+            stState<CS>(&K.ft[0][j], (double)(0.));
+            stState<CS>(&K.ft[1][j], (double)(0.));
         }
     } else {
         const F3 pn{st[CF_T0X], st[CF_T0Y], st[CF_T0Z]};
@@ -639,8 +646,8 @@ __device__ __forceinline__ void ssContact(const SSIn& x, int64_t j, const DevNod
         } else {
             fn = ph0 * uN;
             if (sp.noFrict || ph2 == 0.f) {
-                K.ft[0][j] = 0.;
-                K.ft[1][j] = 0.;
+                stState<CS>(&K.ft[0][j], (double)(0.));
+                stState<CS>(&K.ft[1][j], (double)(0.));
             } else {
                 double t1 = ft1o, t2 = ft2o;
                 t1 += (double)(dtf * ph1 * lvel.y);
@@ -653,8 +660,8 @@ __device__ __forceinline__ void ssContact(const SSIn& x, int64_t j, const DevNod
                     t1 *= ratio;
                     t2 *= ratio;
                 }
-                K.ft[0][j] = t1;
-                K.ft[1][j] = t2;
+                stState<CS>(&K.ft[0][j], (double)(t1));
+                stState<CS>(&K.ft[1][j], (double)(t2));
                 ft1 = (float)t1;
                 ft2 = (float)t2;
                 if (isnan(fn) || isnan(t1) || isnan(t2)) atomicCAS(dErr, 0, 101);
@@ -693,7 +700,7 @@ __device__ __forceinline__ void ssContact(const SSIn& x, int64_t j, const DevNod
     }
     if constexpr (ENERGY) en.store(E, nm + j);
     if (!keep) {
-        K.flags[j] = ((fl & ~C_REAL) | C_PENDING) | hiBits;
+        stState<CS>(&K.flags[j], (uint32_t)(((fl & ~C_REAL) | C_PENDING) | hiBits));
         if (real) {
             I.endAf[it.z] = make_float4(0.f, 0.f, 0.f, 0.f);
             I.endBf[it.z] = make_float2(0.f, 0.f);
@@ -709,14 +716,14 @@ __device__ __forceinline__ void ssContact(const SSIn& x, int64_t j, const DevNod
     I.endBf[it.z] = make_float2(TA.y, TA.z);
     I.endAf[it.w] = make_float4(-F.x, -F.y, -F.z, TB.x);
     I.endBf[it.w] = make_float2(TB.y, TB.z);
-    K.col[CF_T0X][j] = f.c0.x;
-    K.col[CF_T0Y][j] = f.c0.y;
-    K.col[CF_T0Z][j] = f.c0.z;
-    K.col[CF_T1X][j] = f.c1.x;
-    K.col[CF_T1Y][j] = f.c1.y;
-    K.col[CF_T1Z][j] = f.c1.z;
-    K.col[CF_UN][j] = uN;
-    if ((fl | C_REAL) != fl0) K.flags[j] = (fl | C_REAL) | hiBits;
+    stState<CS>(&K.col[CF_T0X][j], f.c0.x);
+    stState<CS>(&K.col[CF_T0Y][j], f.c0.y);
+    stState<CS>(&K.col[CF_T0Z][j], f.c0.z);
+    stState<CS>(&K.col[CF_T1X][j], f.c1.x);
+    stState<CS>(&K.col[CF_T1Y][j], f.c1.y);
+    stState<CS>(&K.col[CF_T1Z][j], f.c1.z);
+    stState<CS>(&K.col[CF_UN][j], uN);
+    if ((fl | C_REAL) != fl0) stState<CS>(&K.flags[j], (uint32_t)((fl | C_REAL) | hiBits));
 }
 
 // Sphere-sphere contacts of aperiodic scenes (work items [nMixed, nAct)), one per thread: item,
@@ -758,7 +765,7 @@ __global__ void __launch_bounds__(256, MINB) k_contact_ss32(DevNodes N, DevParti
 // The same contacts through a resident grid, each thread walking the range with the grid's
 // stride: the next contact's packed item is loaded while the current contact's state and mirror
 // records are in flight, so each contact waits for one memory round trip instead of two.
-template <int MINB, bool ENERGY>
+template <int MINB, bool ENERGY, bool CS = false>
 __global__ void __launch_bounds__(256, MINB) k_contact_ss32p(DevNodes N, DevParticles P, DevContacts C, DevIncidence I, DevPackedSS K,
                                                              const double4_32a* __restrict__ mats, const ScenePar* __restrict__ spp,
                                                              long long* __restrict__ dStep, int* __restrict__ dFlags, int64_t nm,
@@ -770,25 +777,25 @@ __global__ void __launch_bounds__(256, MINB) k_contact_ss32p(DevNodes N, DevPart
     }
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    int4 next = j < K.n ? K.item[j] : make_int4(0, 0, 0, 0);
+    int4 next = j < K.n ? (CS ? __ldcs(K.item + j) : K.item[j]) : make_int4(0, 0, 0, 0);
     for (; j < K.n; j += stride) {
         SSIn x;
         x.it = next;
-        if (j + stride < K.n) next = K.item[j + stride];
-        x.pf = K.flags[j];
+        if (j + stride < K.n) next = CS ? __ldcs(K.item + j + stride) : K.item[j + stride];
+        x.pf = CS ? __ldcs(K.flags + j) : K.flags[j];
 #pragma unroll
-        for (int q = 0; q < CF_NCOL; q++) x.st[q] = K.col[q][j];
+        for (int q = 0; q < CF_NCOL; q++) x.st[q] = CS ? __ldcs(K.col[q] + j) : K.col[q][j];
         x.ft1o = 0.;
         x.ft2o = 0.;
         if (loadFt) {
-            x.ft1o = K.ft[0][j];
-            x.ft2o = K.ft[1][j];
+            x.ft1o = CS ? __ldcs(K.ft[0] + j) : K.ft[0][j];
+            x.ft2o = CS ? __ldcs(K.ft[1] + j) : K.ft[1][j];
         }
         x.ma = N.mir[x.it.x];
         x.mb = N.mir[x.it.y];
         x.wza = N.wz[x.it.x];
         x.wzb = N.wz[x.it.y];
-        ssContact<ENERGY>(x, j, N, P, C, I, K, mats, spp, stepAbs, dFlags, nm, E);
+        ssContact<ENERGY, CS>(x, j, N, P, C, I, K, mats, spp, stepAbs, dFlags, nm, E);
     }
     stepTicket(dFlags, dStep, ticketTotal);
 }
@@ -1225,6 +1232,11 @@ template <bool ENERGY>
 static void launchSS(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C, const DevIncidence& I,
                      const DevPackedSS& K, const double4_32a* mats, const ScenePar* sp, long long* dStep, int* dFlags, int64_t nm,
                      int halt, int loadFt, int block, int grid, int ticketTotal, const EnergyCols& E) {
+    if (block == -512) {  // the same grid with evict-first packed-state traffic
+        k_contact_ss32p<kSSMinBlocks, ENERGY, true><<<(unsigned)grid, 256, 0, st>>>(N, P, C, I, K, mats, sp, dStep, dFlags, nm, halt,
+                                                                                    loadFt, ticketTotal, E);
+        return;
+    }
     if (block < 0) {
         k_contact_ss32p<kSSMinBlocks, ENERGY><<<(unsigned)grid, 256, 0, st>>>(N, P, C, I, K, mats, sp, dStep, dFlags, nm, halt, loadFt,
                                                                               ticketTotal, E);

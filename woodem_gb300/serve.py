@@ -171,7 +171,18 @@ class Server:
         ticks = 0
         used_periodic_bytes = [0.0]
 
+        errors = []
+
         def run_periodic(job):
+            try:
+                run_periodic_job(job)
+            except BaseException as e:  # re-raised by the serving loop
+                with lock:
+                    errors.append(e)
+                    used_periodic_bytes[0] -= job.n * BYTES_PER_PARTICLE
+                stop.set()
+
+        def run_periodic_job(job):
             job.start = self._now(t0, ticks)
             S = job.build()
             for n, g in job.phase_steps():
@@ -198,6 +209,8 @@ class Server:
                     self.partial_particle_steps += job.n * job.done_steps
 
         while True:
+            if errors:
+                break
             now = self._now(t0, ticks)
             while pending and pending[0].arrival <= now:
                 queue.append(pending.pop(0))
@@ -258,6 +271,8 @@ class Server:
                 ticks += 1
         for th in periodic_running:
             th.join()
+        if errors:
+            raise RuntimeError("a periodic job failed: %r" % (errors[0],)) from errors[0]
         self.elapsed = time.perf_counter() - t0
         return self.done
 
