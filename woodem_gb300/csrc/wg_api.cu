@@ -245,6 +245,27 @@ __global__ void k_get_state(DevNodes N, const int32_t* __restrict__ map, int64_t
     }
 }
 
+// Copies between the staging buffer (pos 3, ori 4, vel 3, angVel 3, force 3, torque 3 doubles
+// per API node, array after array) and the caller's arrays q0..q1-1: arrays that follow each
+// other in host memory as they do in the staging buffer go as one copy. Null arrays are skipped.
+static cudaError_t copyState(double* stage, int64_t na, double* const host[6], int q0, int q1, bool toDevice, cudaStream_t st) {
+    const int64_t off[6] = {0, 3, 7, 10, 13, 16}, w[6] = {3, 4, 3, 3, 3, 3};
+    for (int q = q0; q < q1;) {
+        if (!host[q]) {
+            q++;
+            continue;
+        }
+        int e = q + 1;
+        while (e < q1 && host[e] && host[e] == host[e - 1] + w[e - 1] * na) e++;
+        const size_t bytes = sizeof(double) * (size_t)(off[e - 1] + w[e - 1] - off[q]) * (size_t)na;
+        const cudaError_t r = toDevice ? cudaMemcpyAsync(stage + off[q] * na, host[q], bytes, cudaMemcpyHostToDevice, st)
+                                       : cudaMemcpyAsync(host[q], stage + off[q] * na, bytes, cudaMemcpyDeviceToHost, st);
+        if (r != cudaSuccess) return r;
+        q = e;
+    }
+    return cudaSuccess;
+}
+
 // The early part of wg_run_host's copy-out (see Sim::earlyOut), issued right after the run's
 // last Leapfrog is queued: the early stream waits for it, converts the kinematic state into the
 // staging buffer and copies it to the caller's arrays. The contact loop that follows reads that
@@ -257,13 +278,11 @@ int Sim::issueEarlyGet() {
         WG_CUDA_TRY(cudaEventCreateWithFlags(&earlyFork, cudaEventDisableTiming));
     }
     const int64_t na = nApiNodes;
-    const int64_t off[4] = {0, 3, 7, 10}, w[4] = {3, 4, 3, 3};
     WG_CUDA_TRY(cudaEventRecord(earlyFork, stream));
     WG_CUDA_TRY(cudaStreamWaitEvent(earlySt, earlyFork, 0));
     k_get_state<<<(unsigned)((na + 255) / 256), 256, 0, earlySt>>>(N, X.dApiMap, na, stagedArrays(X.dStage, na), 1);
-    for (int q = 0; q < 4; q++)
-        if (earlyOut[q])
-            WG_CUDA_TRY(cudaMemcpyAsync(earlyOut[q], X.dStage + off[q] * na, sizeof(double) * w[q] * na, cudaMemcpyDeviceToHost, earlySt));
+    double* const host[6] = {earlyOut[0], earlyOut[1], earlyOut[2], earlyOut[3], nullptr, nullptr};
+    WG_CUDA_TRY(copyState(X.dStage, na, host, 0, 4, false, earlySt));
     earlyIssued = true;
     return 0;
 }
@@ -1783,18 +1802,18 @@ int wg_put_state(wg_scene* s, const double* pos, const double* ori, const double
         return WG_OK;
     }
     const int64_t na = S.nApiNodes;
-    const double* src[6] = {pos, ori, vel, ang_vel, force, torque};
-    const int64_t off[6] = {0, 3, 7, 10, 13, 16}, w[6] = {3, 4, 3, 3, 3, 3};
-    // staged: one copy per array (the copy engines move page-locked arrays faster than kernels
-    // reading host memory directly; one stream already fills the host link), then the
-    // conversion into the node slots
+    // staged: copies by the copy engines (they move page-locked arrays faster than kernels
+    // reading host memory directly; one stream already fills the host link), one per run of
+    // arrays adjacent in host memory, then the conversion into the node slots
     if (!(pos && ori && vel && ang_vel && force && torque)) {
         // fill missing components from the current device state
         k_get_state<<<(unsigned)((na + 255) / 256), 256, 0, S.stream>>>(S.N, X.dApiMap, na, stagedArrays(X.dStage, na));
     }
-    for (int q = 0; q < 6; q++)
-        if (src[q])
-            WG_CUDA_TRY(cudaMemcpyAsync(X.dStage + off[q] * na, src[q], sizeof(double) * w[q] * na, cudaMemcpyHostToDevice, S.stream));
+    {
+        double* const host[6] = {const_cast<double*>(pos), const_cast<double*>(ori), const_cast<double*>(vel),
+                                 const_cast<double*>(ang_vel), const_cast<double*>(force), const_cast<double*>(torque)};
+        WG_CUDA_TRY(copyState(X.dStage, na, host, 0, 6, true, S.stream));
+    }
     k_put_state<<<(unsigned)((na + 255) / 256), 256, 0, S.stream>>>(S.N, X.dApiMap, na, stagedArrays(X.dStage, na));
     S.fromEnds = false;  // the next step starts from the forces written here
     if (vel) S.facetsStatic = false;  // facet vertices may have been given a velocity
@@ -1818,8 +1837,7 @@ int wg_get_nodes(wg_scene* s, double* pos, double* ori, double* vel, double* ang
     }
     const int part = (pos || ori || vel || ang_vel) ? ((force || torque) ? 0 : 1) : 2;
     k_get_state<<<(unsigned)((na + 255) / 256), 256, 0, S.stream>>>(S.N, X.dApiMap, na, stagedArrays(X.dStage, na), part);
-    for (int q = 0; q < 6; q++)
-        if (dst[q]) WG_CUDA_TRY(cudaMemcpyAsync(dst[q], X.dStage + off[q] * na, sizeof(double) * w[q] * na, cudaMemcpyDeviceToHost, S.stream));
+    WG_CUDA_TRY(copyState(X.dStage, na, dst, 0, 6, false, S.stream));
     WG_CUDA_TRY(cudaGetLastError());
     WG_CUDA_TRY(cudaStreamSynchronize(S.stream));
     return WG_OK;
