@@ -251,7 +251,7 @@ int64_t wg_pack_rsa_device(int64_t n, const double* radii, const double* lo, con
     // need); after every few rounds the state of the window comes back to the host, which moves w0
     // past the placed prefix and stops at the first sphere that found no place
     const int64_t W = std::min<int64_t>(32768, std::max<int64_t>(256, n / 64));
-    const int kRoundsPerCheck = 4;
+    const int kRoundsPerCheck = 16;
     std::vector<int32_t> hState((size_t)std::min<int64_t>(n, W));
     int64_t w0 = 0, prefix = n;
     while (w0 < n) {

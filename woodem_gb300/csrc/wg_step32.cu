@@ -561,14 +561,7 @@ __device__ __forceinline__ void stepTicket(int* dFlags, long long* dStep, int to
 // One sphere-sphere contact of an aperiodic scene (packed position j): Cg2_Sphere_Sphere_L6Geom,
 // Cp2 on creation, Law2, the two end slots and the packed state. FP32 arithmetic throughout
 // except the IdealElPl shear accumulation (FP64) and contact creation.
-// store of a packed-state word: CS marks it evict-first in L2 (the state streams through once
-// per step; the mirror records gathered by every contact should stay)
-template <bool CS, class T>
-__device__ __forceinline__ void stState(T* p, T v) {
-    if constexpr (CS) __stcs(p, v);
-    else *p = v;
-}
-template <bool ENERGY, bool CS = false>
+template <bool ENERGY>
 __device__ __forceinline__ void ssContact(const SSIn& x, int64_t j, const DevNodes& N, const DevParticles& P, const DevContacts& C,
                                           const DevIncidence& I, const DevPackedSS& K, const double4_32a* __restrict__ mats,
                                           const ScenePar* __restrict__ spp, long long stepAbs, int* dFlags, int64_t nm,
@@ -586,14 +579,14 @@ __device__ __forceinline__ void ssContact(const SSIn& x, int64_t j, const DevNod
     uint32_t fl = fl0;
     if (fl & C_REMOVED) return;
     if ((fl & C_PENDING) && !pendingStays(P, A, B, false, nullptr, dErr)) {
-        stState<CS>(&K.flags[j], (uint32_t)(((fl & ~C_PENDING) | C_REMOVED) | hiBits));
+        K.flags[j] = ((fl & ~C_PENDING) | C_REMOVED) | hiBits;
         return;
     }
     fl &= ~C_PENDING;
     const bool real = fl & C_REAL;
     SSGeo g;
     if (!geomSS32(x.ma, x.mb, x.wza, x.wzb, sp.ssDfAbsF, real, g)) {
-        if (fl != fl0) stState<CS>(&K.flags[j], (uint32_t)(fl | hiBits));
+        if (fl != fl0) K.flags[j] = fl | hiBits;
         return;
     }
     const float dtf = sp.dtF;
@@ -608,16 +601,16 @@ __device__ __forceinline__ void ssContact(const SSIn& x, int64_t j, const DevNod
     if (!real) {
         frameInit(n, f);
         physCreate(spp, (int)(pf >> 8), r1, r2, uN, mats[P.mat[A]], mats[P.mat[B]], N.minert[A].w, N.minert[B].w, ph0, ph1, ph2, ph3);
-        stState<CS>(&K.col[CF_P0][j], ph0);
-        stState<CS>(&K.col[CF_P1][j], ph1);
-        stState<CS>(&K.col[CF_P2][j], ph2);
-        stState<CS>(&K.col[CF_P3][j], ph3);
+        K.col[CF_P0][j] = ph0;
+        K.col[CF_P1][j] = ph1;
+        K.col[CF_P2][j] = ph2;
+        K.col[CF_P3][j] = ph3;
         C.step0[I.work[nm + j].x] = (int32_t)step;
         ft1o = 0.;
         ft2o = 0.;
         if (sp.law == 0) {
-            stState<CS>(&K.ft[0][j], (double)(0.));
-            stState<CS>(&K.ft[1][j], (double)(0.));
+            K.ft[0][j] = 0.;
+            K.ft[1][j] = 0.;
         }
     } else {
         const F3 pn{st[CF_T0X], st[CF_T0Y], st[CF_T0Z]};
@@ -646,8 +639,8 @@ __device__ __forceinline__ void ssContact(const SSIn& x, int64_t j, const DevNod
         } else {
             fn = ph0 * uN;
             if (sp.noFrict || ph2 == 0.f) {
-                stState<CS>(&K.ft[0][j], (double)(0.));
-                stState<CS>(&K.ft[1][j], (double)(0.));
+                K.ft[0][j] = 0.;
+                K.ft[1][j] = 0.;
             } else {
                 double t1 = ft1o, t2 = ft2o;
                 t1 += (double)(dtf * ph1 * lvel.y);
@@ -660,8 +653,8 @@ __device__ __forceinline__ void ssContact(const SSIn& x, int64_t j, const DevNod
                     t1 *= ratio;
                     t2 *= ratio;
                 }
-                stState<CS>(&K.ft[0][j], (double)(t1));
-                stState<CS>(&K.ft[1][j], (double)(t2));
+                K.ft[0][j] = t1;
+                K.ft[1][j] = t2;
                 ft1 = (float)t1;
                 ft2 = (float)t2;
                 if (isnan(fn) || isnan(t1) || isnan(t2)) atomicCAS(dErr, 0, 101);
@@ -700,7 +693,7 @@ __device__ __forceinline__ void ssContact(const SSIn& x, int64_t j, const DevNod
     }
     if constexpr (ENERGY) en.store(E, nm + j);
     if (!keep) {
-        stState<CS>(&K.flags[j], (uint32_t)(((fl & ~C_REAL) | C_PENDING) | hiBits));
+        K.flags[j] = ((fl & ~C_REAL) | C_PENDING) | hiBits;
         if (real) {
             I.endAf[it.z] = make_float4(0.f, 0.f, 0.f, 0.f);
             I.endBf[it.z] = make_float2(0.f, 0.f);
@@ -716,14 +709,14 @@ __device__ __forceinline__ void ssContact(const SSIn& x, int64_t j, const DevNod
     I.endBf[it.z] = make_float2(TA.y, TA.z);
     I.endAf[it.w] = make_float4(-F.x, -F.y, -F.z, TB.x);
     I.endBf[it.w] = make_float2(TB.y, TB.z);
-    stState<CS>(&K.col[CF_T0X][j], f.c0.x);
-    stState<CS>(&K.col[CF_T0Y][j], f.c0.y);
-    stState<CS>(&K.col[CF_T0Z][j], f.c0.z);
-    stState<CS>(&K.col[CF_T1X][j], f.c1.x);
-    stState<CS>(&K.col[CF_T1Y][j], f.c1.y);
-    stState<CS>(&K.col[CF_T1Z][j], f.c1.z);
-    stState<CS>(&K.col[CF_UN][j], uN);
-    if ((fl | C_REAL) != fl0) stState<CS>(&K.flags[j], (uint32_t)((fl | C_REAL) | hiBits));
+    K.col[CF_T0X][j] = f.c0.x;
+    K.col[CF_T0Y][j] = f.c0.y;
+    K.col[CF_T0Z][j] = f.c0.z;
+    K.col[CF_T1X][j] = f.c1.x;
+    K.col[CF_T1Y][j] = f.c1.y;
+    K.col[CF_T1Z][j] = f.c1.z;
+    K.col[CF_UN][j] = uN;
+    if ((fl | C_REAL) != fl0) K.flags[j] = (fl | C_REAL) | hiBits;
 }
 
 // Sphere-sphere contacts of aperiodic scenes (work items [nMixed, nAct)), one per thread: item,
@@ -765,7 +758,7 @@ __global__ void __launch_bounds__(256, MINB) k_contact_ss32(DevNodes N, DevParti
 // The same contacts through a resident grid, each thread walking the range with the grid's
 // stride: the next contact's packed item is loaded while the current contact's state and mirror
 // records are in flight, so each contact waits for one memory round trip instead of two.
-template <int MINB, bool ENERGY, bool CS = false>
+template <int MINB, bool ENERGY>
 __global__ void __launch_bounds__(256, MINB) k_contact_ss32p(DevNodes N, DevParticles P, DevContacts C, DevIncidence I, DevPackedSS K,
                                                              const double4_32a* __restrict__ mats, const ScenePar* __restrict__ spp,
                                                              long long* __restrict__ dStep, int* __restrict__ dFlags, int64_t nm,
@@ -777,25 +770,25 @@ __global__ void __launch_bounds__(256, MINB) k_contact_ss32p(DevNodes N, DevPart
     }
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    int4 next = j < K.n ? (CS ? __ldcs(K.item + j) : K.item[j]) : make_int4(0, 0, 0, 0);
+    int4 next = j < K.n ? K.item[j] : make_int4(0, 0, 0, 0);
     for (; j < K.n; j += stride) {
         SSIn x;
         x.it = next;
-        if (j + stride < K.n) next = CS ? __ldcs(K.item + j + stride) : K.item[j + stride];
-        x.pf = CS ? __ldcs(K.flags + j) : K.flags[j];
+        if (j + stride < K.n) next = K.item[j + stride];
+        x.pf = K.flags[j];
 #pragma unroll
-        for (int q = 0; q < CF_NCOL; q++) x.st[q] = CS ? __ldcs(K.col[q] + j) : K.col[q][j];
+        for (int q = 0; q < CF_NCOL; q++) x.st[q] = K.col[q][j];
         x.ft1o = 0.;
         x.ft2o = 0.;
         if (loadFt) {
-            x.ft1o = CS ? __ldcs(K.ft[0] + j) : K.ft[0][j];
-            x.ft2o = CS ? __ldcs(K.ft[1] + j) : K.ft[1][j];
+            x.ft1o = K.ft[0][j];
+            x.ft2o = K.ft[1][j];
         }
         x.ma = N.mir[x.it.x];
         x.mb = N.mir[x.it.y];
         x.wza = N.wz[x.it.x];
         x.wzb = N.wz[x.it.y];
-        ssContact<ENERGY, CS>(x, j, N, P, C, I, K, mats, spp, stepAbs, dFlags, nm, E);
+        ssContact<ENERGY>(x, j, N, P, C, I, K, mats, spp, stepAbs, dFlags, nm, E);
     }
     stepTicket(dFlags, dStep, ticketTotal);
 }
@@ -876,14 +869,24 @@ void launch_facet_prep(cudaStream_t st, const DevNodes& N, const DevParticles& P
 
 // rare paths of the facet geometry, out of line (see physCreateFP64)
 __device__ __noinline__ D3 closestSegmentPtOut(D3 P, D3 A, D3 B) { return closestSegmentPt(P, A, B); }
-__device__ __noinline__ D3 facetAngVelOut(D3 p0, D3 p1, D3 p2, D3 c, D3 v0, D3 v1, D3 v2) {
-    return (cross(p0 - c, v0) + cross(p1 - c, v1)) + cross(p2 - c, v2);
-}
 __device__ __noinline__ D3 normalPartOut(D3 v, D3 n) { return dot(v, n) * n; }
+// Facet::interpolatePtLinAngVel (Facet.cpp:158-174): the barycentric interpolation of the vertex
+// velocities at contPt and the angular velocity they imply, for facets whose vertices move (a
+// drum's facets are static and move the spheres by fakeVel only: there both are zero)
+__device__ __noinline__ void facetVelOut(D3 contPt, D3 p0, D3 p1, D3 p2, double4_32a q0, double4_32a q1, double4_32a q2,
+                                         double4_32a qn, D3 v0, D3 v1, D3 v2, D3& linVel, D3& angVel) {
+    const D3 vX = contPt - p0;
+    const double b0 = dot(vX, p1 - p0), b1 = dot(vX, p2 - p0);
+    const double u = q0.w * b0 + q1.w * b1, v = q2.w * b0 + qn.w * b1;
+    const double a0 = (1 - u) - v;
+    linVel = (a0 * v0 + u * v1) + v * v2;
+    angVel = (cross(p0 - contPt, v0) + cross(p1 - contPt, v1)) + cross(p2 - contPt, v2);
+}
 
 // Cg2_Facet_Sphere_L6Geom::go (Facet.cpp:235-288, Facet::interpolatePtLinAngVel :158-174) in FP64
 // from the facet's FacetPrep of this step: the per-contact part of the functor (plane distance,
 // region tests, closest point, barycentric velocity).
+template <bool PERI>
 __device__ __forceinline__ bool geomFS32(const DevNodes& N, const DevParticles& P, int A, int B, D3 shift2, bool real, Geo& g, int* dErr) {
     const int4 fn = P.aux[A];
     const FacetPrep& F = P.prep[fn.w];
@@ -893,7 +896,7 @@ __device__ __forceinline__ bool geomFS32(const DevNodes& N, const DevParticles& 
     const double4_32a ps = N.posr[B];
     const double4_32a q0 = F.p0, q1 = F.p1, q2 = F.p2, qn = F.n;
     const double radius = ps.w;
-    const D3 sC = ld3(ps) + shift2;
+    const D3 sC = PERI ? ld3(ps) + shift2 : ld3(ps);
     const D3 p0 = ld3(q0), p1 = ld3(q1), p2 = ld3(q2);
     const D3 fNormal = ld3(qn);
     const double planeDist = dot(sC - p0, fNormal);
@@ -922,15 +925,10 @@ __device__ __forceinline__ bool geomFS32(const DevNodes& N, const DevParticles& 
     normal = normal * (1. / dist);
     if (halfThick > 0) contPt = contPt + normal * halfThick;
     g.uN = (dist - radius) - halfThick;
-    // barycentric interpolation of the facet node velocities at contPt
-    const D3 vX = contPt - p0;
-    const double b0 = dot(vX, p1 - p0), b1 = dot(vX, p2 - p0);
-    const double u = q0.w * b0 + q1.w * b1, v = q2.w * b0 + qn.w * b1;
-    const double a0 = (1 - u) - v;
+    // the facet node velocities interpolated at contPt (zero for static vertices)
     const D3 v0 = ld3(N.vel[fn.x]), v1 = ld3(N.vel[fn.y]), v2 = ld3(N.vel[fn.z]);
-    D3 linVel = (a0 * v0 + u * v1) + v * v2;
-    D3 angVel{0, 0, 0};
-    if (!isZero(v0) || !isZero(v1) || !isZero(v2)) angVel = facetAngVelOut(p0, p1, p2, contPt, v0, v1, v2);
+    D3 linVel{0, 0, 0}, angVel{0, 0, 0};
+    if (!isZero(v0) || !isZero(v1) || !isZero(v2)) facetVelOut(contPt, p0, p1, p2, q0, q1, q2, qn, v0, v1, v2, linVel, angVel);
     if (!isZero(fakeVel)) {
         if (!isnan(fakeVel.x)) linVel = linVel + fakeVel;
         else linVel = normalPartOut(linVel, fNormal);
@@ -972,7 +970,6 @@ __device__ __forceinline__ void mixedContact(int64_t rk, const DevNodes& N, cons
     const uint32_t ty = ctype((uint32_t)wk.w);
     const bool real = fl & C_REAL;
     const long long step = *dStep - sp.stepBase;
-    const double dt = sp.dt;
     const float dtf = sp.dtF;
     bool shifted = false;
     D3 shift2{0, 0, 0}, shiftVel2{0, 0, 0};
@@ -1038,7 +1035,7 @@ __device__ __forceinline__ void mixedContact(int64_t rk, const DevNodes& N, cons
         Geo g;
         bool touch;
         if (ty == CT_WS) touch = geomWS(N, P, real ? (double)C.fcol[CF_T0X + P.aux[A].x][c] : 0., A, B, shift2, real, g);
-        else touch = geomFS32(N, P, A, B, shift2, real, g, dErr);
+        else touch = geomFS32<PERI>(N, P, A, B, shift2, real, g, dErr);
         if (!touch) {
             C.flags[c] = fl;
             return;
@@ -1050,13 +1047,16 @@ __device__ __forceinline__ void mixedContact(int64_t rk, const DevNodes& N, cons
         // walls are uninodal (their node is pos1); facets take no force here
         armA = (ty == CT_WS) ? toFt(g.contPt - g.pos1) : F3{0.f, 0.f, 0.f};
         armB = toFt(g.contPt - g.pos2);
+        const D3 vel2 = PERI ? g.vel2 + shiftVel2 : g.vel2;
         if (real) {
+            // mid-step branch vectors (L6Geom.cpp:156-160): (prevCp + contPt)/2 - (pos - dt/2 vel),
+            // from the FP64 differences of nearby points (a few mm) rounded to FP32
             const D3 prevCp{C.col[CC_CPX][c], C.col[CC_CPY][c], C.col[CC_CPZ][c]};
-            const D3 mc = .5 * (prevCp + g.contPt);
-            c1x = toFt(mc - (g.pos1 - (dt / 2.) * g.vel1));
-            c2x = toFt(mc - (g.pos2 - (dt / 2.) * (g.vel2 + shiftVel2)));
+            const float hdt = 0.5f * dtf;
+            c1x = 0.5f * (toFt(prevCp - g.pos1) + toFt(g.contPt - g.pos1)) + hdt * toFt(g.vel1);
+            c2x = 0.5f * (toFt(prevCp - g.pos2) + armB) + hdt * toFt(vel2);
         }
-        dv = toFt((g.vel2 + shiftVel2) - g.vel1);
+        dv = toFt(vel2 - g.vel1);
         w1 = toFt(g.angVel1);
         w2 = toFt(g.angVel2);
         C.col[CC_CPX][c] = g.contPt.x;
@@ -1232,11 +1232,6 @@ template <bool ENERGY>
 static void launchSS(cudaStream_t st, const DevNodes& N, const DevParticles& P, const DevContacts& C, const DevIncidence& I,
                      const DevPackedSS& K, const double4_32a* mats, const ScenePar* sp, long long* dStep, int* dFlags, int64_t nm,
                      int halt, int loadFt, int block, int grid, int ticketTotal, const EnergyCols& E) {
-    if (block == -512) {  // the same grid with evict-first packed-state traffic
-        k_contact_ss32p<kSSMinBlocks, ENERGY, true><<<(unsigned)grid, 256, 0, st>>>(N, P, C, I, K, mats, sp, dStep, dFlags, nm, halt,
-                                                                                    loadFt, ticketTotal, E);
-        return;
-    }
     if (block < 0) {
         k_contact_ss32p<kSSMinBlocks, ENERGY><<<(unsigned)grid, 256, 0, st>>>(N, P, C, I, K, mats, sp, dStep, dFlags, nm, halt, loadFt,
                                                                               ticketTotal, E);
@@ -1259,7 +1254,7 @@ static bool contactsFP32(cudaStream_t st, const SideStream& side, const DevNodes
         // sphere-sphere launch raises FL_HALT when a full run is due; the last block of either
         // advances the step counter
         const int gM = (int)std::min<int64_t>((nm + 127) / 128, smCount());
-        const int gS = ssGrid(K, block, kSSMinBlocks - 1);
+        const int gS = ssGrid(K, block, block == -257 ? kSSMinBlocks : kSSMinBlocks - 1);
         const int total = gS > 0 ? gM + gS : 0;
         cudaEventRecord(side.fork, st);
         cudaStreamWaitEvent(side.st, side.fork, 0);
