@@ -1671,9 +1671,8 @@ int wg_get_slot_nodes(wg_scene* s, int32_t k, int64_t n, double* pos, double* or
 int wg_set_launch(wg_scene* s, int32_t contact_block, int32_t chunk_steps, int32_t launch_flags) {
     if (!s) return WG_ERR_ARG;
     Sim& S = *SIM(s);
-    if (contact_block != 0 && contact_block != 64 && contact_block != 128 && contact_block != 256 && contact_block != -256 &&
-        contact_block != -257)
-        return S.fail(WG_ERR_ARG, "contact_block must be 0, 64, 128, 256, -256 or -257");
+    if (contact_block != 0 && contact_block != 64 && contact_block != 128 && contact_block != 256 && contact_block != -256)
+        return S.fail(WG_ERR_ARG, "contact_block must be 0, 64, 128, 256 or -256");
     if (chunk_steps < 1 || chunk_steps > 1024) return S.fail(WG_ERR_ARG, "chunk_steps must be in [1, 1024]");
     S.contactBlock = contact_block;
     S.chunkSteps = chunk_steps;

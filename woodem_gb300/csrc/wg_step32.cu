@@ -1254,7 +1254,7 @@ static bool contactsFP32(cudaStream_t st, const SideStream& side, const DevNodes
         // sphere-sphere launch raises FL_HALT when a full run is due; the last block of either
         // advances the step counter
         const int gM = (int)std::min<int64_t>((nm + 127) / 128, smCount());
-        const int gS = ssGrid(K, block, block == -257 ? kSSMinBlocks : kSSMinBlocks - 1);
+        const int gS = ssGrid(K, block, kSSMinBlocks - 1);
         const int total = gS > 0 ? gM + gS : 0;
         cudaEventRecord(side.fork, st);
         cudaStreamWaitEvent(side.st, side.fork, 0);
