@@ -47,6 +47,7 @@ def build(verbose=False, force=False):
     os.makedirs(OUT, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers.append(os.path.join(HERE, "..", "include", "woo_gpu.h"))
+    headers.append(os.path.abspath(__file__))  # the flags below
     procs = []
     objs = []
     for unit, extra in UNITS.items():
