@@ -751,13 +751,13 @@ __global__ void k_set_flags(int* f, int full) {
 // device flag words, and once Leapfrog of step s finds a node past verletDist, the contact
 // kernel of step s raises FL_HALT and everything queued after it does nothing. The host then
 // reads the step counter, runs the collider for step s, finishes its contact loop and goes on.
-int Sim::syncContacts() {
+int Sim::syncContacts(bool hostWait) {
     Sim& S = *this;
     if (packDirty && K.n > 0) {
         WG_CUDA_TRY(cudaSetDevice(device));
         launch_unpack_ss(stream, C, I, K, nMixed);
         WG_CUDA_TRY(cudaGetLastError());
-        WG_CUDA_TRY(cudaStreamSynchronize(stream));
+        if (hostWait) WG_CUDA_TRY(cudaStreamSynchronize(stream));
     }
     packDirty = false;
     return 0;

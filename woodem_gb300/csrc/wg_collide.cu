@@ -992,7 +992,7 @@ int collide_full_run(Sim& S) {
     cudaStream_t st = S.stream;
     // the contact arrays take back the packed sphere-sphere state before they are merged
     {
-        int r = S.syncContacts();
+        int r = S.syncContacts(false);  // the merge below is queued on the same stream
         if (r) return r;
         S.K.n = 0;
     }

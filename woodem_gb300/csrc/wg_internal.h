@@ -450,7 +450,9 @@ struct Sim {
     int runDynDt(int64_t stepNow);
     int checkErr();
     int ensureContactCapacity(int64_t need);
-    int syncContacts();  // write the packed sphere-sphere state back to the contact arrays if needed
+    // write the packed sphere-sphere state back to the contact arrays if needed; hostWait: also wait
+    // for it (the host reads the arrays next), else it is only queued on the simulation stream
+    int syncContacts(bool hostWait = true);
 };
 
 #define WG_CUDA_TRY(expr)                                                                  \
