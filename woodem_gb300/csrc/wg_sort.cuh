@@ -4,9 +4,9 @@
 // Sort: 8-bit digits, one pass per digit of the key's [beginBit, endBit) range. A pass is three
 // launches: per-tile digit counts (tiles of 4096 keys, counts stored digit-major), their exclusive
 // prefix sum (which is the output start of every (digit, tile) group), and the scatter, in which
-// each tile ranks its keys in order -- 16 rounds of 256 keys, a round's keys ranked within their
-// warp by __match_any_sync and across the 8 warps by per-digit counters in shared memory -- so
-// that keys of equal digit keep their input order (the pass is stable, and so the sort).
+// each warp ranks its 512 keys of the tile in order (32 at a time, grouped by __match_any_sync)
+// against per-warp digit counters in shared memory, so that keys of equal digit keep their input
+// order (the pass is stable, and so the sort).
 // Scan: tiles of 4096 values scanned by a block each, the tile totals scanned by one block, the
 // totals added back.
 #pragma once
@@ -49,50 +49,60 @@ __global__ void __launch_bounds__(kThreads) k_rs_hist(const K* __restrict__ keys
     for (int d = threadIdx.x; d < kRadix; d += kThreads) hist[(int64_t)d * nTiles + blockIdx.x] = cnt[d];
 }
 
-// stable scatter of one tile to the start offsets off[d * nTiles + tile]
+// stable scatter of one tile to the start offsets off[d * nTiles + tile]. Warp w of the block owns
+// the w-th run of kItems * 32 keys of the tile: it counts its digits (a round of 32 keys at a
+// time, equal digits grouped by __match_any_sync, the group's first lane adding the group size to
+// the warp's counter), the block turns the counters into output starts (warps in order within
+// every digit), and the warp writes its keys in order, each at its counter plus its rank in its
+// round's group. Keys keep their order: tile, warp, round and lane order is input order.
 template <class K, class V>
 __global__ void __launch_bounds__(kThreads) k_rs_scatter(const K* __restrict__ kin, const V* __restrict__ vin, K* __restrict__ kout,
                                                          V* __restrict__ vout, int64_t n, int shift, unsigned mask,
                                                          const int32_t* __restrict__ off, int nTiles) {
-    __shared__ int32_t base[kRadix];
-    __shared__ int32_t wpos[kWarps][kRadix];
+    __shared__ int32_t cnt[kWarps][kRadix];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int d = threadIdx.x; d < kRadix; d += kThreads) {
-        base[d] = off[(int64_t)d * nTiles + blockIdx.x];
-        for (int w = 0; w < kWarps; w++) wpos[w][d] = 0;
+    for (int d = threadIdx.x; d < kRadix; d += kThreads)
+        for (int w = 0; w < kWarps; w++) cnt[w][d] = 0;
+    __syncthreads();
+    const int64_t s0 = (int64_t)blockIdx.x * kTile + (int64_t)warp * (kItems * 32);
+    const unsigned below = (1u << lane) - 1u;
+    K k[kItems];
+    V v[kItems];
+    unsigned dg[kItems];
+#pragma unroll
+    for (int r = 0; r < kItems; r++) {
+        const int64_t i = s0 + r * 32 + lane;
+        const bool valid = i < n;
+        k[r] = valid ? kin[i] : K(0);
+        v[r] = (valid && vin) ? vin[i] : V(0);
+        dg[r] = valid ? digitOf(k[r], shift, mask) : 0xffffffffu;  // past the end: a group of their own
+        const unsigned peers = __match_any_sync(0xffffffffu, dg[r]);
+        if (valid && (peers & below) == 0) cnt[warp][dg[r]] += __popc(peers);
+        __syncwarp();
     }
     __syncthreads();
-    const int64_t t0 = (int64_t)blockIdx.x * kTile;
-    const unsigned below = (1u << lane) - 1u;
+    for (int d = threadIdx.x; d < kRadix; d += kThreads) {
+        int run = off[(int64_t)d * nTiles + blockIdx.x];
+        for (int w = 0; w < kWarps; w++) {
+            const int c = cnt[w][d];
+            cnt[w][d] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+#pragma unroll
     for (int r = 0; r < kItems; r++) {
-        const int64_t i = t0 + (int64_t)r * kThreads + threadIdx.x;
-        const bool valid = i < n;
-        const K k = valid ? kin[i] : K(0);
-        const unsigned d = valid ? digitOf(k, shift, mask) : 0xffffffffu;  // past the end: a group of their own
-        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const bool valid = s0 + r * 32 + lane < n;
+        const unsigned peers = __match_any_sync(0xffffffffu, dg[r]);
         const int rank = __popc(peers & below);
-        if (valid && rank == 0) wpos[warp][d] = __popc(peers);  // the warp's count of digit d
-        __syncthreads();
-        // counts -> start of each warp's group of digit dd in this round; the base moves past them
-        for (int dd = threadIdx.x; dd < kRadix; dd += kThreads) {
-            int run = base[dd];
-            for (int w = 0; w < kWarps; w++) {
-                const int c = wpos[w][dd];
-                wpos[w][dd] = run;
-                run += c;
-            }
-            base[dd] = run;
-        }
-        __syncthreads();
         if (valid) {
-            const int32_t pos = wpos[warp][d] + rank;
-            kout[pos] = k;
-            if (vout) vout[pos] = vin[i];
+            const int32_t pos = cnt[warp][dg[r]] + rank;
+            kout[pos] = k[r];
+            if (vout) vout[pos] = v[r];
         }
-        __syncthreads();
-        for (int dd = threadIdx.x; dd < kRadix; dd += kThreads)
-            for (int w = 0; w < kWarps; w++) wpos[w][dd] = 0;
-        __syncthreads();
+        __syncwarp();
+        if (valid && rank == 0) cnt[warp][dg[r]] += __popc(peers);
+        __syncwarp();
     }
 }
 
