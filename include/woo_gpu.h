@@ -277,14 +277,6 @@ int wg_broadphase_noalloc(int32_t n, const double* mn, const double* mx, const u
 /* Message of the last failed wg_broadphase_noalloc call on this thread. */
 const char* wg_broadphase_noalloc_error(void);
 
-/* Self-tests of the broad phase's stable radix sort and exclusive prefix sum (the sorts of the
-   cell keys, pair keys and hi-id keys of a full collider run), on the current device, host arrays
-   in and out; no counterpart in the reference. wg_test_sort sorts n keys of key_bytes (4 or 8)
-   bytes by bits [begin_bit, end_bit), carrying vals (may be null) along. */
-int wg_test_sort(int64_t n, int32_t key_bytes, int32_t begin_bit, int32_t end_bit, const void* keys, const int32_t* vals,
-                 void* keys_out, int32_t* vals_out);
-int wg_test_scan(int64_t n, const int32_t* in, int32_t* out);
-
 /* Scene generation (host only): seeded random sequential insertion of n non-overlapping
    spheres, the role of SpherePack::makeCloud (lib/sphere-pack/SpherePack.hpp:75).
    region_kind 0: box lo..hi; 1: x-axis cylinder through (params[0],params[1]) of radius

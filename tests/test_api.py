@@ -145,16 +145,6 @@ def test_pack_rsa_device_rejects_arguments(gpu_lib):
     assert gpu_lib.wg_pack_rsa_device(0, P(r), P(lo), P(hi), 0, P(np.zeros(4)), 1, 100, P(out)) == 0
 
 
-def test_sort_selftest_rejects_arguments(gpu_lib):
-    """The sort and scan self-tests check their arguments before any device call."""
-    k = np.zeros(4, dtype=np.uint32)
-    assert gpu_lib.wg_test_sort(4, 3, 0, 8, k.ctypes.data, None, k.ctypes.data, None) == -1
-    assert gpu_lib.wg_test_sort(-1, 4, 0, 8, k.ctypes.data, None, k.ctypes.data, None) == -1
-    assert gpu_lib.wg_test_sort(0, 4, 0, 8, None, None, None, None) == 0
-    assert gpu_lib.wg_test_scan(-1, None, None) == -1
-    assert gpu_lib.wg_test_scan(0, None, None) == 0
-
-
 def test_quadrilateral_mesh():
     """py/triangulated.py:70-83: 2*div0*div1 facets covering the quadrilateral, vertices shared."""
     ff = triangulated.quadrilateral((0, 0, 0), (2, 0, 0), (0, 3, 0), (2, 3, 0), div=(4, 3))

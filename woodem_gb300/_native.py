@@ -126,8 +126,6 @@ def lib():
         "wg_broadphase_noalloc_error": (C.c_char_p, []),
         "wg_pack_rsa": (C.c_int64, [C.c_int64, P_D, P_D, P_D, C.c_int32, P_D, C.c_uint64, C.c_int64, P_D]),
         "wg_pack_rsa_device": (C.c_int64, [C.c_int64, P_D, P_D, P_D, C.c_int32, P_D, C.c_uint64, C.c_int64, P_D]),
-        "wg_test_sort": (C.c_int, [C.c_int64, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
-        "wg_test_scan": (C.c_int, [C.c_int64, C.c_void_p, C.c_void_p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

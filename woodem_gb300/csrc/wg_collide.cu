@@ -10,13 +10,14 @@
 // that set on the GPU:
 //   1. Bo1 functors + verlet enlargement per particle            (k_aabb)
 //   2. spheres bucketed into a uniform grid whose cell is at least the largest sphere box,
-//      keyed by the cell of the box minimum and radix-sorted      (k_cellkey + radix sort, wg_sort.cuh)
+//      keyed by the cell of the box minimum and radix-sorted      (k_cellkey + cub radix sort)
 //   3. half-shell sweep over the sorted cells: every candidate pair is tested once with the
 //      reference's closed-interval comparisons                   (k_pairs_ss)
 //   4. facets query the cells their box covers; walls (infinite boxes) test every sphere
 //   5. the new pair keys are radix-sorted and merged with the real contacts of the previous
 //      set, carrying their persistent state                      (k_mark_orphans .. k_gather)
 //   6. CSR incidence for the deterministic force sum              (k_lo_start, hi sort, k_hi_start)
+#include <cub/cub.cuh>
 
 
 #include <algorithm>
@@ -26,7 +27,6 @@
 #include "wg_math.cuh"
 #include "wg_ends.cuh"
 #include "wg_geom.cuh"
-#include "wg_sort.cuh"
 
 namespace wg {
 
@@ -91,8 +91,8 @@ struct CollideWork {
     int64_t hiCap = 0;
     int32_t* heavyCount = nullptr;
     int32_t* hHeavy = nullptr;
-    void* sortTmp = nullptr;  // scratch of the radix sorts and scans
-    size_t sortTmpBytes = 0;
+    void* cubTmp = nullptr;
+    size_t cubBytes = 0;
 };
 
 static const int BS = 256;
@@ -916,15 +916,13 @@ __global__ void k_heavy(DevIncidence I, DevParticles P, const uint32_t* __restri
 }
 
 // ---------------------------------------------------------------- host orchestration
-// scratch of the sorts and scans (int32 words) of n items
-static size_t sortBytes(int64_t n) { return sizeof(int32_t) * (size_t)std::max(rsort::sortScratch(n), rsort::scanScratch(n)); }
-static int ensureSortScratch(Sim& S, size_t bytes) {
+static int ensureCub(Sim& S, size_t bytes) {
     CollideWork& W = *S.cw;
-    if (bytes <= W.sortTmpBytes) return 0;
-    if (W.sortTmp) S.dfree(W.sortTmp);
-    W.sortTmpBytes = bytes * 3 / 2 + 1024;
-    W.sortTmp = S.dalloc(W.sortTmpBytes);
-    return W.sortTmp ? 0 : S.fail(WG_ERR_CUDA, "out of device memory (collider scratch)");
+    if (bytes <= W.cubBytes) return 0;
+    if (W.cubTmp) S.dfree(W.cubTmp);
+    W.cubBytes = bytes * 3 / 2 + 1024;
+    W.cubTmp = S.dalloc(W.cubBytes);
+    return W.cubTmp ? 0 : S.fail(WG_ERR_CUDA, "out of device memory (collider scratch)");
 }
 
 template <class T>
@@ -1094,9 +1092,11 @@ int collide_full_run(Sim& S) {
         else k_cellkey<<<(ns + BS - 1) / BS, BS, 0, st>>>(S.P, W.sphereIds, ns, W.dGrids, W.cellKey, W.cellVal);
         int endBit = 1;
         while ((int64_t(1) << endBit) < ncellAll) endBit++;
-        if (ensureSortScratch(S, sortBytes(ns))) return WG_ERR_CUDA;
-        if (!rsort::sortPairs(W.cellKey, W.cellKeySorted, W.cellVal, W.sid, ns, 0, endBit, (int32_t*)W.sortTmp, st))
-            return S.fail(WG_ERR_CAPACITY, "broad phase: too many spheres for the cell sort");
+        size_t tb = 0;
+        cub::DeviceRadixSort::SortPairs(nullptr, tb, W.cellKey, W.cellKeySorted, W.cellVal, W.sid, ns, 0, endBit, st);
+        if (ensureCub(S, tb)) return WG_ERR_CUDA;
+        tb = W.cubBytes;
+        WG_CUDA_TRY(cub::DeviceRadixSort::SortPairs(W.cubTmp, tb, W.cellKey, W.cellKeySorted, W.cellVal, W.sid, ns, 0, endBit, st));
         k_cell_off<<<(unsigned)((ncellAll + 1 + BS - 1) / BS), BS, 0, st>>>(W.cellKeySorted, ns, ncellAll, W.cellOff);
         k_gather_sorted<<<(ns + BS - 1) / BS, BS, 0, st>>>(S.P, W.sid, ns, W.smn, W.smx, W.smask, W.smnf, W.smxf, W.smnfi, W.smxfi);
     }
@@ -1195,16 +1195,21 @@ int collide_full_run(Sim& S) {
     int idBits = 1;
     while ((int64_t(1) << idBits) < S.nPar) idBits++;
     if (nNew > 0 && peri) {
-        if (ensureSortScratch(S, sortBytes(nNew))) return WG_ERR_CUDA;
-        if (!rsort::sortPairs(W.pairs, W.pairsSorted, W.pairCd, W.pairCdSorted, nNew, 0, 32 + idBits, (int32_t*)W.sortTmp, st))
-            return S.fail(WG_ERR_CAPACITY, "broad phase: too many pairs for the pair sort");
+        size_t tb = 0;
+        cub::DeviceRadixSort::SortPairs(nullptr, tb, W.pairs, W.pairsSorted, W.pairCd, W.pairCdSorted, nNew, 0, 32 + idBits, st);
+        if (ensureCub(S, tb)) return WG_ERR_CUDA;
+        tb = W.cubBytes;
+        WG_CUDA_TRY(cub::DeviceRadixSort::SortPairs(W.cubTmp, tb, W.pairs, W.pairsSorted, W.pairCd, W.pairCdSorted, nNew, 0,
+                                                    32 + idBits, st));
     } else if (nNew > 0) {
         // ids take idBits each: sort (lo << idBits | hi), the same order in fewer radix passes
         const unsigned pb = (unsigned)((nNew + BS - 1) / BS);
         k_pack_keys<<<pb, BS, 0, st>>>(W.pairs, nNew, idBits);
-        if (ensureSortScratch(S, sortBytes(nNew))) return WG_ERR_CUDA;
-        if (!rsort::sortPairs<uint64_t, int32_t>(W.pairs, W.pairsSorted, nullptr, nullptr, nNew, 0, 2 * idBits, (int32_t*)W.sortTmp, st))
-            return S.fail(WG_ERR_CAPACITY, "broad phase: too many pairs for the pair sort");
+        size_t tb = 0;
+        cub::DeviceRadixSort::SortKeys(nullptr, tb, W.pairs, W.pairsSorted, nNew, 0, 2 * idBits, st);
+        if (ensureCub(S, tb)) return WG_ERR_CUDA;
+        tb = W.cubBytes;
+        WG_CUDA_TRY(cub::DeviceRadixSort::SortKeys(W.cubTmp, tb, W.pairs, W.pairsSorted, nNew, 0, 2 * idBits, st));
         k_unpack_keys<<<pb, BS, 0, st>>>(W.pairsSorted, nNew, idBits);
     }
     // 5. merge with the previous contact set
@@ -1227,9 +1232,11 @@ int collide_full_run(Sim& S) {
         int32_t* flagsArr = W.orph;
         int32_t* scanArr = W.orph + (std::max<int64_t>(nOld, 1) + 1);
         k_mark_orphans<<<(unsigned)((nOld + BS - 1) / BS), BS, 0, st>>>(S.C, W.pairsSorted, W.newLo, flagsArr, S.P.fresh);
-        if (ensureSortScratch(S, sortBytes(nOld))) return WG_ERR_CUDA;
-        if (!rsort::exclusiveScan(flagsArr, scanArr, nOld, (int32_t*)W.sortTmp, st))
-            return S.fail(WG_ERR_CAPACITY, "broad phase: too many contacts for the merge");
+        size_t tb = 0;
+        cub::DeviceScan::ExclusiveSum(nullptr, tb, flagsArr, scanArr, (int)nOld, st);
+        if (ensureCub(S, tb)) return WG_ERR_CUDA;
+        tb = W.cubBytes;
+        WG_CUDA_TRY(cub::DeviceScan::ExclusiveSum(W.cubTmp, tb, flagsArr, scanArr, (int)nOld, st));
         int32_t last[2];
         WG_CUDA_TRY(cudaMemcpyAsync(&last[0], flagsArr + nOld - 1, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
         WG_CUDA_TRY(cudaMemcpyAsync(&last[1], scanArr + nOld - 1, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
@@ -1293,10 +1300,13 @@ int collide_full_run(Sim& S) {
         WG_CUDA_TRY(cudaMemsetAsync(W.actSS, 0, sizeof(int32_t) * (n + 1), st));
         if (n > 0) {
             k_active<<<(unsigned)((n + BS - 1) / BS), BS, 0, st>>>(S.C.flags, n, W.act, W.actSS);
-            if (ensureSortScratch(S, sortBytes(n + 1))) return WG_ERR_CUDA;
-            if (!rsort::exclusiveScan(W.act, W.act, n + 1, (int32_t*)W.sortTmp, st) ||
-                !rsort::exclusiveScan(W.actSS, W.actSS, n + 1, (int32_t*)W.sortTmp, st))
-                return S.fail(WG_ERR_CAPACITY, "broad phase: too many contacts for the incidence lists");
+            size_t tb = 0;
+            cub::DeviceScan::ExclusiveSum(nullptr, tb, W.act, W.act, (int)(n + 1), st);
+            if (ensureCub(S, tb)) return WG_ERR_CUDA;
+            tb = W.cubBytes;
+            WG_CUDA_TRY(cub::DeviceScan::ExclusiveSum(W.cubTmp, tb, W.act, W.act, (int)(n + 1), st));
+            tb = W.cubBytes;
+            WG_CUDA_TRY(cub::DeviceScan::ExclusiveSum(W.cubTmp, tb, W.actSS, W.actSS, (int)(n + 1), st));
         }
         int32_t h[2] = {0, 0};
         WG_CUDA_TRY(cudaMemcpyAsync(&h[0], W.act + n, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
@@ -1325,9 +1335,11 @@ int collide_full_run(Sim& S) {
     while ((int64_t(1) << hiBits) <= S.nPar) hiBits++;
     if (n > 0) {
         k_hi_keys<<<(unsigned)((n + BS - 1) / BS), BS, 0, st>>>(S.C.key, S.C.flags, n, (uint32_t)S.nPar, W.hiKeys, W.hiVals);
-        if (ensureSortScratch(S, sortBytes(n))) return WG_ERR_CUDA;
-        if (!rsort::sortPairs(W.hiKeys, W.hiKeysSorted, W.hiVals, S.I.hiList, n, 0, hiBits, (int32_t*)W.sortTmp, st))
-            return S.fail(WG_ERR_CAPACITY, "broad phase: too many contacts for the incidence lists");
+        size_t tb = 0;
+        cub::DeviceRadixSort::SortPairs(nullptr, tb, W.hiKeys, W.hiKeysSorted, W.hiVals, S.I.hiList, n, 0, hiBits, st);
+        if (ensureCub(S, tb)) return WG_ERR_CUDA;
+        tb = W.cubBytes;
+        WG_CUDA_TRY(cub::DeviceRadixSort::SortPairs(W.cubTmp, tb, W.hiKeys, W.hiKeysSorted, W.hiVals, S.I.hiList, n, 0, hiBits, st));
     }
     k_hi_start<<<(unsigned)((S.nPar + 1 + BS - 1) / BS), BS, 0, st>>>(W.hiKeysSorted, n, (int)S.nPar, S.I.hiStart);
     if (n > 0) k_slots<<<(unsigned)((n + BS - 1) / BS), BS, 0, st>>>(S.C.key, S.C.flags, n, nAct, W.act, W.actSS, nAct - nSS, S.I);
@@ -1401,63 +1413,3 @@ void collide_free(Sim& S) {
 }
 
 }  // namespace wg
-
-// ------------------------------------------------------------------ self-tests of the sort and scan
-namespace {
-// device copies of host arrays for the self-tests, freed at scope end
-struct TestBufs {
-    std::vector<void*> p;
-    ~TestBufs() {
-        for (void* q : p) cudaFree(q);
-    }
-    void* get(size_t bytes) {
-        void* q = nullptr;
-        if (cudaMalloc(&q, bytes < 16 ? 16 : bytes) != cudaSuccess) return nullptr;
-        p.push_back(q);
-        return q;
-    }
-};
-template <class K>
-int testSort(int64_t n, int32_t beginBit, int32_t endBit, const void* keys, const int32_t* vals, void* keysOut, int32_t* valsOut) {
-    TestBufs B;
-    K* kin = (K*)B.get(sizeof(K) * n);
-    K* kout = (K*)B.get(sizeof(K) * n);
-    int32_t* vin = vals ? (int32_t*)B.get(sizeof(int32_t) * n) : nullptr;
-    int32_t* vout = vals ? (int32_t*)B.get(sizeof(int32_t) * n) : nullptr;
-    int32_t* scratch = (int32_t*)B.get(sizeof(int32_t) * (size_t)wg::rsort::sortScratch(n));
-    if (!kin || !kout || !scratch || (vals && (!vin || !vout))) return WG_ERR_CUDA;
-    if (cudaMemcpy(kin, keys, sizeof(K) * n, cudaMemcpyHostToDevice) != cudaSuccess) return WG_ERR_CUDA;
-    if (vals && cudaMemcpy(vin, vals, sizeof(int32_t) * n, cudaMemcpyHostToDevice) != cudaSuccess) return WG_ERR_CUDA;
-    if (!wg::rsort::sortPairs<K, int32_t>(kin, kout, vin, vout, n, beginBit, endBit, scratch, 0)) return WG_ERR_ARG;
-    if (cudaDeviceSynchronize() != cudaSuccess || cudaGetLastError() != cudaSuccess) return WG_ERR_CUDA;
-    if (cudaMemcpy(keysOut, kout, sizeof(K) * n, cudaMemcpyDeviceToHost) != cudaSuccess) return WG_ERR_CUDA;
-    if (vals && cudaMemcpy(valsOut, vout, sizeof(int32_t) * n, cudaMemcpyDeviceToHost) != cudaSuccess) return WG_ERR_CUDA;
-    return WG_OK;
-}
-}  // namespace
-
-extern "C" {
-
-int wg_test_sort(int64_t n, int32_t key_bytes, int32_t begin_bit, int32_t end_bit, const void* keys, const int32_t* vals,
-                 void* keys_out, int32_t* vals_out) {
-    if (n < 0 || (key_bytes != 4 && key_bytes != 8) || (n > 0 && (!keys || !keys_out)) || (vals && !vals_out)) return WG_ERR_ARG;
-    if (n == 0) return WG_OK;
-    return key_bytes == 4 ? testSort<uint32_t>(n, begin_bit, end_bit, keys, vals, keys_out, vals_out)
-                          : testSort<uint64_t>(n, begin_bit, end_bit, keys, vals, keys_out, vals_out);
-}
-
-int wg_test_scan(int64_t n, const int32_t* in, int32_t* out) {
-    if (n < 0 || (n > 0 && (!in || !out))) return WG_ERR_ARG;
-    if (n == 0) return WG_OK;
-    TestBufs B;
-    int32_t* d = (int32_t*)B.get(sizeof(int32_t) * n);
-    int32_t* scratch = (int32_t*)B.get(sizeof(int32_t) * (size_t)wg::rsort::scanScratch(n));
-    if (!d || !scratch) return WG_ERR_CUDA;
-    if (cudaMemcpy(d, in, sizeof(int32_t) * n, cudaMemcpyHostToDevice) != cudaSuccess) return WG_ERR_CUDA;
-    if (!wg::rsort::exclusiveScan(d, d, n, scratch, 0)) return WG_ERR_ARG;
-    if (cudaDeviceSynchronize() != cudaSuccess || cudaGetLastError() != cudaSuccess) return WG_ERR_CUDA;
-    if (cudaMemcpy(out, d, sizeof(int32_t) * n, cudaMemcpyDeviceToHost) != cudaSuccess) return WG_ERR_CUDA;
-    return WG_OK;
-}
-
-}  // extern "C"
