@@ -91,3 +91,61 @@ def test_cross_cell_contact_exists(oracle_lib):
     c = O.contacts()
     assert len(c["id_lo"]) == 1
     assert tuple(c["cell_dist"][0]) == (0, 0, -10)
+
+
+def _overlap_peri(mn, mx, a, b, size):
+    """InsertionSortCollider::spatialOverlapPeri (pkg/dem/InsertionSortCollider.cpp:903-957)."""
+    per = [0, 0, 0]
+    for ax in range(3):
+        dim = size[ax]
+        m1, m2 = mn[a, ax], mn[b, ax]
+        rel = lambda x, x0: ((x - x0) / dim - np.floor((x - x0) / dim)) * dim
+        w = m2 if rel(m1, m2) < rel(m2, m1) else m1
+
+        def wrap(x):
+            xn = (x - w) / dim
+            p = np.floor(xn)
+            return w + (xn - p) * dim, int(p)
+        (mn1, p1), (mx1, _) = wrap(mn[a, ax]), wrap(mx[a, ax])
+        (mn2, p2), (mx2, _) = wrap(mn[b, ax]), wrap(mx[b, ax])
+        per[ax] = p1 - p2
+        if not (mn1 <= mx2 and mx1 >= mn2):
+            return False, per
+    return True, per
+
+
+def test_periodic_insertion_sort_can_miss_an_overlap(oracle_lib):
+    """The reference's periodic insertion sort (InsertionSortCollider.cpp:718-791, serial form)
+    makes one pass over each circular bound list; a pass can leave an inversion next to the wrap
+    point, and the overlap it hides is reported only at a later inversion of that pair. The oracle
+    restates the pass; in this 40-sphere periodic cell (seeded fast random motion, a full run every
+    step) the boxes of spheres 1 and 28 overlap across the z boundary after step 26 while the
+    contact container does not hold the pair. The GPU broad phase computes the exact overlap set
+    and holds it (its parity tests accept exactly such pairs)."""
+    from oracle.oracle import Oracle
+    rng = np.random.default_rng(44)
+    S = woo.core.Scene(fields=[DemField(gravity=(0, 0, 0))])
+    S.periodic = True
+    L, r = 0.1, 0.006
+    S.cell.setBox(L, L, L)
+    mat = FrictMat(density=1e3, young=1e5, ktDivKn=.2, tanPhi=.5)
+    ps = [utils.sphere(tuple(p), r, mat=mat) for p in rng.uniform(0, L, (40, 3))]
+    S.dem.par.add(ps)
+    for p in ps:
+        p.vel = tuple(rng.uniform(-3.0, 3.0, 3))
+    S.engines = utils.defaultEngines(damping=0, dynDtPeriod=0, verletDist=-0.05)
+    S.dt = 1e-4
+    A = _plan.compile_scene(S)
+    O = Oracle(A, threads=1, deterministic=True)
+    O.run(26)
+    mn, mx = O.aabbs(A.n_particles)
+    size = np.linalg.norm(O.cell()[0], axis=0)
+    c = O.contacts()
+    held = set(zip(c["id_lo"].tolist(), c["id_hi"].tolist()))
+    assert O.stats().n_full_runs == 26
+    ov, per = _overlap_peri(mn, mx, 1, 28, size)
+    assert ov and per == [0, 0, 1] and (1, 28) not in held
+    # every other overlap is held
+    missing = [(a, b) for a in range(40) for b in range(a + 1, 40) if _overlap_peri(mn, mx, a, b, size)[0] and (a, b) not in held]
+    assert missing == [(1, 28)]
+    O.close()
