@@ -15,7 +15,7 @@ from woodem_gb300.core import Cell
 
 from test_gpu_parity import _gpu_nodes, _compare_nodes, _compare_contacts
 from test_gpu_fp32 import _clone_state, _run_mode, _force_errors
-from test_oracle_pbc import pbc_scene
+from test_oracle_pbc import pbc_scene, fast_periodic_scene, _overlap_peri
 
 pytestmark = pytest.mark.gpu
 
@@ -100,3 +100,35 @@ def test_particle_larger_than_half_cell(gpu_lib):
     S.cell.setBox(0.8, 2.5, 3)  # sphere diameter 1 > 0.4
     with pytest.raises(RuntimeError, match="larger than half of the cell"):
         S.run(1)
+
+
+def test_gpu_holds_the_overlap_the_periodic_sort_misses(gpu_lib):
+    """The scene of test_oracle_pbc.test_periodic_insertion_sort_can_miss_an_overlap on the GPU
+    (FP64): after 26 steps its pair set is the exact overlap set of its boxes -- the pair (1, 28)
+    that the oracle's one-pass periodic sort leaves out included, with periods (0, 0, 1) as
+    cellDist -- and otherwise the oracle's; that pair is not real, and the states are bitwise
+    equal."""
+    S = fast_periodic_scene()
+    O = _oracle(S)
+    S.run(26)
+    O.run(26)
+    A = _plan.compile_scene(S)
+    n = A.n_particles
+    mn, mx = np.empty((n, 3)), np.empty((n, 3))
+    from woodem_gb300 import _native
+    S._sim.H.check(S._sim.H.L.wg_get_aabbs(S._sim.H.h, _native.ptr(mn), _native.ptr(mx)), "get_aabbs")
+    size = np.linalg.norm(np.asarray(S.cell.hSize, float), axis=0)
+    cg, co = S._sim.contacts(), O.contacts()
+    kg = list(zip(cg["id_lo"].tolist(), cg["id_hi"].tolist()))
+    ko = set(zip(co["id_lo"].tolist(), co["id_hi"].tolist()))
+    exact = {(a, b) for a in range(n) for b in range(a + 1, n) if _overlap_peri(mn, mx, a, b, size)[0]}
+    real = {k for k, rl in zip(kg, cg["real"].tolist()) if rl}
+    assert set(kg) == exact | real
+    assert set(kg) - ko == {(1, 28)}
+    i = kg.index((1, 28))
+    assert cg["real"][i] == 0 and list(cg["cell_dist"][i]) == [0, 0, 1]
+    g, o = _gpu_nodes(S), O.nodes()
+    for k in ("pos", "vel", "angVel", "force", "torque"):
+        assert np.array_equal(g[k], o[k]), k
+    O.close()
+    S.close()

@@ -114,6 +114,23 @@ def _overlap_peri(mn, mx, a, b, size):
     return True, per
 
 
+def fast_periodic_scene(seed=44, n=40, L=0.1, r=0.006, vmax=3.0):
+    """n spheres of radius r at seeded random places in an L-cube periodic cell, moving with
+    seeded random velocities of up to vmax per axis (a full collider run at every step)."""
+    rng = np.random.default_rng(seed)
+    S = woo.core.Scene(fields=[DemField(gravity=(0, 0, 0))])
+    S.periodic = True
+    S.cell.setBox(L, L, L)
+    mat = FrictMat(density=1e3, young=1e5, ktDivKn=.2, tanPhi=.5)
+    ps = [utils.sphere(tuple(p), r, mat=mat) for p in rng.uniform(0, L, (n, 3))]
+    S.dem.par.add(ps)
+    for p in ps:
+        p.vel = tuple(rng.uniform(-vmax, vmax, 3))
+    S.engines = utils.defaultEngines(damping=0, dynDtPeriod=0, verletDist=-0.05)
+    S.dt = 1e-4
+    return S
+
+
 def test_periodic_insertion_sort_can_miss_an_overlap(oracle_lib):
     """The reference's periodic insertion sort (InsertionSortCollider.cpp:718-791, serial form)
     makes one pass over each circular bound list; a pass can leave an inversion next to the wrap
@@ -123,18 +140,7 @@ def test_periodic_insertion_sort_can_miss_an_overlap(oracle_lib):
     contact container does not hold the pair. The GPU broad phase computes the exact overlap set
     and holds it (its parity tests accept exactly such pairs)."""
     from oracle.oracle import Oracle
-    rng = np.random.default_rng(44)
-    S = woo.core.Scene(fields=[DemField(gravity=(0, 0, 0))])
-    S.periodic = True
-    L, r = 0.1, 0.006
-    S.cell.setBox(L, L, L)
-    mat = FrictMat(density=1e3, young=1e5, ktDivKn=.2, tanPhi=.5)
-    ps = [utils.sphere(tuple(p), r, mat=mat) for p in rng.uniform(0, L, (40, 3))]
-    S.dem.par.add(ps)
-    for p in ps:
-        p.vel = tuple(rng.uniform(-3.0, 3.0, 3))
-    S.engines = utils.defaultEngines(damping=0, dynDtPeriod=0, verletDist=-0.05)
-    S.dt = 1e-4
+    S = fast_periodic_scene()
     A = _plan.compile_scene(S)
     O = Oracle(A, threads=1, deterministic=True)
     O.run(26)
