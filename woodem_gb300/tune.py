@@ -4,7 +4,8 @@ The results of a simulation do not depend on the launch shape (threads per block
 kernels, steps queued per host check of the collider request, CUDA-graph replay of such a chunk of
 steps): every contact and every particle is updated by the same operations in the same order.
 The tuner therefore measures candidate shapes on real steps of the simulation it tunes (the steps
-count as part of the run) and keeps the fastest.
+count as part of the run) and keeps the fastest by the median over rounds, the default shape
+unless another is faster by more than a margin.
 """
 import ctypes as C
 
